@@ -1,0 +1,379 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 wavefront path-tracing pass.
+
+Workload (the plain pass at scale): the procedural terrain scene of 1,482,242
+triangles (512 x 512-vertex fBm heightfield + 2000 UV spheres, gradient sky
+baked to a 1024 x 512 RGBA16F equirect map with an importance-sampling CDF, one
+sun), rendered at 1920 x 1080, 64 spp, 8 extend segments (primary + 7
+bounces), fp32 accumulation.  A step is one full frame.  Inputs are synthetic
+and seeded (no dataset exists for this pass).
+
+Metric: Mrays/s = rays entering the closest-hit (extend) kernel per second of
+device time; frames/s reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU implementation of the pass (the
+multithreaded C++ oracle: the reference's own pass runs only through a
+graphics API's ray-tracing pipeline, which this machine does not have) on the
+host cores, on the same workload, as a bounded sample per step.
+Prints ONE JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s (extend rays entering closest-hit) at 1 GB300, plain wavefront PT"
+DEV_VIEW_BYTES = 112  # bytes of the per-view record the render call uploads (DevView)
+EXTEND_BYTES_PER_RAY = 48  # 32 B ray read + 16 B hit written (compulsory HBM)
+NODE_BYTES, TRI_BYTES = 80, 48
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--spp", type=int, default=64)
+    p.add_argument("--segments", type=int, default=8)
+    p.add_argument("--grid", type=int, default=512)
+    p.add_argument("--spheres", type=int, default=2000)
+    p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload_config(a, tris=None):
+    return {"workload": f"terrain fBm {a.grid}x{a.grid} + {a.spheres} UV spheres, {a.width}x{a.height}, "
+                        f"{a.spp} spp, {a.segments} segments",
+            "scene_triangles": tris, "width": a.width, "height": a.height, "spp": a.spp,
+            "max_segments": a.segments, "sky": "1024x512 RGBA16F equirect + 2-D CDF", "seed": a.seed,
+            "parallelism": "replicas" if a.gpus > 1 else "single GPU",
+            "l2": "inputs larger than L2 (wavefront queues ~2 GB per chunk) and a 512 MB device copy "
+                  "between timed steps flushes L2"}
+
+
+# ----------------------------------------------------------- distributed ----
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------- clocks ----
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            c = [x.strip() for x in line.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                mx.append(float(c[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, c[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-ray DRAM traffic of the extend kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "k_extend_traffic.json")
+    try:
+        with open(path) as f:
+            j = json.load(f)
+        return float(j["dram_bytes_per_ray"]), j.get("source", path)
+    except (OSError, KeyError, ValueError):
+        return None, None
+
+
+# -------------------------------------------------------------- CPU legs ----
+def cpu_sample(scene, cam_arr, a, budget_s: float, threads: int = 0):
+    """Times the oracle on whole rows of the frame at 1 spp, sized to about budget_s seconds."""
+    import oracle
+    osc = oracle.OracleScene(scene)
+    h = a.height
+    mid = h // 2
+    probe = (mid - 4, mid + 4)
+    _, st, sec = osc.render(cam_arr, spp=1, max_segments=a.segments, seed=a.seed, rows=probe, threads=threads)
+    per_row = max(sec / 8.0, 1e-4)
+    rows = int(min(h, max(8, budget_s / per_row)))
+    r0 = max(0, mid - rows // 2)
+    r1 = min(h, r0 + rows)
+    _, st, sec = osc.render(cam_arr, spp=1, max_segments=a.segments, seed=a.seed, rows=(r0, r1), threads=threads)
+    rays = int(st[:16].sum())
+    return {"rays": rays, "seconds": sec, "rows": (r0, r1), "shadow_rays": int(st[16:].sum())}
+
+
+def nthreads():
+    return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------ reference ----
+def run_reference(a, dist: Dist):
+    if dist.rank != 0:
+        return 0
+    bsm = importlib.import_module("bisemutum-engine_gb300")
+    scene = bsm.generate_scene(bsm.BSM_SCENE_TERRAIN, seed=a.seed, grid=a.grid, spheres=a.spheres, width=a.width,
+                               height=a.height)
+    cam = scene.camera.as_array()
+    budget = max(1.0, min(a.cpu_seconds, 20.0))
+    for _ in range(a.warmup):
+        cpu_sample(scene, cam, a, budget / 4)
+    rays, secs, rows = 0, 0.0, None
+    for _ in range(a.steps):
+        r = cpu_sample(scene, cam, a, budget)
+        rays += r["rays"]
+        secs += r["seconds"]
+        rows = r["rows"]
+    value = rays / secs / 1e6
+    cores = nthreads()
+    sample = f"rows {rows[0]}-{rows[1]} of the {a.width}x{a.height} frame at 1 spp per step, {a.segments} segments"
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(secs / a.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(a, scene.num_triangles),
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "CPU implementation of the pass (multithreaded C++ oracle, -O2, no fast-math); the reference's "
+                    "own pass needs a graphics ray-tracing pipeline, unavailable on this box"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ ours ----
+def run_ours(a, dist: Dist):
+    bsm = importlib.import_module("bisemutum-engine_gb300")
+    scene = bsm.generate_scene(bsm.BSM_SCENE_TERRAIN, seed=a.seed, grid=a.grid, spheres=a.spheres, width=a.width,
+                               height=a.height)
+    ctx = bsm.Context(dist.local)
+    t0 = time.perf_counter()
+    sid = ctx.upload(scene)
+    bvh = ctx.build_bvh(sid)
+    setup_s = time.perf_counter() - t0
+    cam = scene.camera
+    seed = a.seed + 1000 * dist.rank
+    flags_timed = bsm.BSM_PT_STAGE_TIMING
+    s_timed = bsm.settings(spp=a.spp, max_segments=a.segments, seed=seed, flags=flags_timed)
+
+    # traversal working set of this workload (counting variant, untimed)
+    _, cst = ctx.render(sid, [cam], bsm.settings(spp=max(1, a.spp // 16), max_segments=a.segments, seed=seed,
+                                                 flags=bsm.BSM_PT_COUNT_TRAVERSAL), outputs=False)
+    nodes_per_ray = cst.traversal_nodes / max(1, cst.extend_rays)
+    tris_per_ray = cst.traversal_tris / max(1, cst.extend_rays)
+
+    # L2 flush buffer (512 MB device copy between timed steps)
+    L = bsm.lib()
+    import ctypes as C
+    flush = C.c_void_p()
+    ctx.check(L.bsm_device_alloc(ctx.h, 2 << 28, C.byref(flush)))
+
+    def flush_l2():
+        ctx.check(L.bsm_memcpy(ctx.h, C.c_void_p(flush.value + (1 << 28)), flush, 1 << 28, 2))
+
+    for _ in range(a.warmup):
+        ctx.render(sid, [cam], s_timed, outputs=False)
+    ctx.sync()
+
+    clocks = Clocks(dist.local) if dist.rank == 0 else None
+    dist.barrier()
+    ctx.sync()
+    wall0 = time.perf_counter()
+    ms_dev, ms_ext, ms_shade, ms_shadow, ms_cam, rays, shadow_rays, launches = [], 0.0, 0.0, 0.0, 0.0, 0, 0, 0
+    for _ in range(a.steps):
+        flush_l2()
+        _, st = ctx.render(sid, [cam], s_timed, outputs=False)
+        ms_dev.append(st.ms_total)
+        ms_ext += st.ms_extend
+        ms_shade += st.ms_shade
+        ms_shadow += st.ms_shadow
+        ms_cam += st.ms_camera
+        rays += st.extend_rays
+        shadow_rays += st.shadow_rays
+        launches += st.chunks * (1 + 3 * a.segments)
+        ext_launches = st.extend_launches
+    ctx.sync()
+    dist.barrier()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop() if clocks else None
+
+    dev_s = sum(ms_dev) / 1e3
+    dev_s_max = dist.max(dev_s)
+    rays_all = dist.sum(float(rays))
+    value = rays_all / dev_s_max / 1e6
+    ms_per_step = dev_s_max / a.steps * 1e3
+
+    # e2e: public API with host buffers (pinned output, camera uploaded each step)
+    out_px = a.width * a.height
+    host = C.c_void_p()
+    ctx.check(L.bsm_host_alloc(ctx.h, out_px * 16, C.byref(host)))
+    outs = (bsm.ViewOutput * 1)()
+    outs[0].rgba = host.value
+    outs[0].row_pitch_px = 0
+    outs[0].location = bsm.BSM_HOST
+    cams = (bsm.Camera * 1)(cam)
+    s_e2e = bsm.settings(spp=a.spp, max_segments=a.segments, seed=seed)
+    ctx.check(L.bsm_render(ctx.h, sid, cams, 1, C.byref(s_e2e), outs, None))
+    dist.barrier()
+    e0 = time.perf_counter()
+    e2e_steps = max(1, min(a.steps, 3))
+    for _ in range(e2e_steps):
+        ctx.check(L.bsm_render(ctx.h, sid, cams, 1, C.byref(s_e2e), outs, None))  # returns after the D2H copy
+    e2e_s = dist.max(time.perf_counter() - e0)
+    e2e_val = rays_all / a.steps * e2e_steps / e2e_s / 1e6
+    L.bsm_host_free(ctx.h, host)
+    L.bsm_device_free(ctx.h, flush)
+
+    line = None
+    if dist.rank == 0:
+        peak, peak_kind = peaks()
+        per_launch_rays = rays / max(1, a.steps * ext_launches)
+        per_launch_ms = ms_ext / max(1, a.steps * ext_launches)
+        achieved = EXTEND_BYTES_PER_RAY * rays / (ms_ext / 1e3) / 1e9 if ms_ext > 0 else None
+        traffic_per_ray, traffic_src = profile_traffic()
+        roofline = {"bound": "hbm", "kernel": "k_extend", "achieved": round(achieved, 2) if achieved else None,
+                    "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
+                    "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                    "traffic": round(traffic_per_ray * per_launch_rays) if traffic_per_ray else None,
+                    "traffic_source": traffic_src,
+                    "algorithmic_bytes_per_launch": round(EXTEND_BYTES_PER_RAY * per_launch_rays),
+                    "avg_launch_ms": round(per_launch_ms, 4),
+                    "l2_traversal_gbs": round((NODE_BYTES * nodes_per_ray + TRI_BYTES * tris_per_ray) * rays /
+                                              (ms_ext / 1e3) / 1e9, 1) if ms_ext > 0 else None,
+                    "nodes_per_ray": round(nodes_per_ray, 2), "tris_per_ray": round(tris_per_ray, 2),
+                    "extend_mrays_per_s_kernel_only": round(rays / (ms_ext / 1e3) / 1e6, 1) if ms_ext > 0 else None}
+        cpu = None
+        if not a.no_cpu_baseline:
+            r = cpu_sample(scene, cam.as_array(), a, a.cpu_seconds)
+            cpu = {"value": round(r["rays"] / r["seconds"] / 1e6, 3), "unit": "Mrays/s", "cores": nthreads(),
+                   "kind": "port",
+                   "sample": f"rows {r['rows'][0]}-{r['rows'][1]} of the frame at 1 spp ({r['rays']} extend rays, "
+                             f"{r['seconds']:.1f} s)"}
+        line = {"metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": a.gpus, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+                "config": workload_config(a, scene.num_triangles),
+                "frames_per_s": round(1e3 / ms_per_step * a.gpus, 4),
+                "e2e": {"value": round(e2e_val, 2), "unit": "Mrays/s",
+                        "h2d_bytes_per_step": DEV_VIEW_BYTES, "d2h_bytes_per_step": out_px * 16,
+                        "api": "bsm_render with a host camera and a pinned host RGBA32F output"},
+                "gpu_launches": launches,
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "stages_ms_per_step": {"camera": round(ms_cam / a.steps, 3), "extend": round(ms_ext / a.steps, 3),
+                                       "shade": round(ms_shade / a.steps, 3),
+                                       "shadow": round(ms_shadow / a.steps, 3)},
+                "rays_per_step": {"extend": rays // a.steps, "shadow": shadow_rays // a.steps},
+                "shadow_mrays_per_s": round(shadow_rays / (ms_shadow / 1e3) / 1e6, 1) if ms_shadow > 0 else None,
+                "bvh": {"build_s_host": round(bvh.build_ms / 1e3, 3), "nodes": bvh.num_nodes,
+                        "depth": bvh.max_depth, "bytes": bvh.node_bytes + bvh.tri_bytes,
+                        "upload_and_build_s": round(setup_s, 3)},
+                "wall_s_timed": round(wall, 3)}
+    ctx.close()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    a = parse()
+    dist = Dist()
+    if dist.world > 1:
+        a.gpus = dist.world
+    try:
+        if a.impl == "reference":
+            return run_reference(a, dist)
+        return run_ours(a, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

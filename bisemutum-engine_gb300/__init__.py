@@ -1,0 +1,446 @@
+"""Host-side Python mirror of the GB300 path-tracing pass (ctypes over libbsm_pt.so).
+
+The product is the C ABI in ``include/bsm_pt.h``; this module binds it for
+tests, the benchmark and Python callers.  ``PathTracingPass`` mirrors the
+reference pass's interface (bisemutum/src/renderer/pass/path_tracing.hpp:27-35:
+``update_params(lights, skybox, settings)`` then ``render(camera, ..., settings)``
+returning the colour output), ``PathTracingSettings`` mirrors
+``BasicRenderer::PathTracingSettings`` (bisemutum/include/bisemutum/renderer/basic.hpp:76-81).
+
+There is no CPU fallback: if the native library is missing or no CUDA device
+is present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbsm_pt.so")
+
+# ---------------------------------------------------------------- status ----
+BSM_OK = 0
+STATUS_NAMES = {
+    0: "BSM_OK", -1: "BSM_ERR_INVALID_ARG", -2: "BSM_ERR_OUT_OF_MEMORY", -3: "BSM_ERR_CUDA", -4: "BSM_ERR_TIMEOUT",
+    -5: "BSM_ERR_NOT_FOUND", -6: "BSM_ERR_BAD_STATE", -7: "BSM_ERR_NO_DEVICE", -8: "BSM_ERR_UNSUPPORTED",
+    -9: "BSM_ERR_DEVICE_CHECK", -10: "BSM_ERR_ADMISSION",
+}
+BSM_HOST, BSM_DEVICE = 0, 1
+BSM_SKY_CONSTANT, BSM_SKY_EQUIRECT = 0, 1
+BSM_SCENE_ROOM, BSM_SCENE_TERRAIN = 0, 1
+BSM_PT_JITTER, BSM_PT_NO_SUN_NEE, BSM_PT_NO_SKY_NEE, BSM_PT_STAGE_TIMING, BSM_PT_NO_GRAPH = 1, 2, 4, 8, 16
+BSM_PT_COUNT_TRAVERSAL = 32
+MISS = 0xFFFFFFFF
+
+
+class BsmError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+# ---------------------------------------------------------- C structures ----
+class Material(C.Structure):
+    _fields_ = [("base_color", C.c_float * 3), ("roughness", C.c_float), ("metallic", C.c_float),
+                ("emission", C.c_float * 3)]
+
+
+class DirLight(C.Structure):
+    _fields_ = [("direction", C.c_float * 3), ("emission", C.c_float * 3)]
+
+
+class Sky(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("color", C.c_float * 3), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("rgba16f", C.POINTER(C.c_uint16))]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("positions", C.POINTER(C.c_float)),
+                ("num_triangles", C.c_uint32), ("indices", C.POINTER(C.c_uint32)),
+                ("material_ids", C.POINTER(C.c_uint32)), ("num_materials", C.c_uint32),
+                ("materials", C.POINTER(Material)), ("num_dir_lights", C.c_uint32),
+                ("dir_lights", C.POINTER(DirLight)), ("sky", Sky)]
+
+
+class BvhOpts(C.Structure):
+    _fields_ = [("sah_bins", C.c_uint32), ("max_leaf_tris", C.c_uint32), ("num_threads", C.c_uint32)]
+
+
+class BvhStats(C.Structure):
+    _fields_ = [("num_nodes", C.c_uint32), ("num_tris", C.c_uint32), ("max_depth", C.c_uint32),
+                ("reserved", C.c_uint32), ("build_ms", C.c_double), ("sah_cost", C.c_double),
+                ("node_bytes", C.c_uint64), ("tri_bytes", C.c_uint64)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("front", C.c_float * 3), ("up", C.c_float * 3),
+                ("yfov_deg", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+    def as_array(self) -> np.ndarray:
+        """pos3 front3 up3 fov w h — the oracle's camera layout."""
+        return np.array([*self.position, *self.front, *self.up, self.yfov_deg, self.width, self.height], np.float32)
+
+
+class PtSettings(C.Structure):
+    _fields_ = [("ray_length", C.c_float), ("max_bounces", C.c_uint32), ("accumulate", C.c_uint32),
+                ("denoise", C.c_uint32), ("spp", C.c_uint32), ("max_segments", C.c_uint32), ("seed", C.c_uint64),
+                ("sample_offset", C.c_uint32), ("flags", C.c_uint32), ("t_min", C.c_float),
+                ("ray_offset", C.c_float), ("wavefront_capacity", C.c_uint32), ("block_size", C.c_uint32)]
+
+
+class ViewOutput(C.Structure):
+    _fields_ = [("rgba", C.c_void_p), ("row_pitch_px", C.c_uint32), ("location", C.c_uint32)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("rays_per_segment", C.c_uint64 * 16), ("chunks", C.c_uint32), ("extend_launches", C.c_uint32),
+                ("ms_total", C.c_float), ("ms_camera", C.c_float), ("ms_extend", C.c_float),
+                ("ms_shade", C.c_float), ("ms_shadow", C.c_float), ("ms_resolve", C.c_float),
+                ("traversal_nodes", C.c_uint64), ("traversal_tris", C.c_uint64)]
+
+
+class SceneGenParams(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("seed", C.c_uint64), ("grid", C.c_uint32), ("spheres", C.c_uint32),
+                ("sky_width", C.c_uint32), ("sky_height", C.c_uint32)]
+
+
+# -------------------------------------------------------------- library ----
+_lib = None
+
+_SIGS = {
+    "bsm_create": (C.c_int32, [C.POINTER(C.c_void_p), C.c_int, C.c_uint64]),
+    "bsm_destroy": (None, [C.c_void_p]),
+    "bsm_last_error": (C.c_char_p, [C.c_void_p]),
+    "bsm_api_version": (C.c_int, []),
+    "bsm_sync": (C.c_int32, [C.c_void_p, C.c_uint32]),
+    "bsm_device_alloc": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "bsm_device_free": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "bsm_memcpy": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int]),
+    "bsm_host_alloc": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "bsm_host_free": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "bsm_scene_upload": (C.c_int32, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(C.c_uint32)]),
+    "bsm_scene_build_bvh": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(BvhOpts), C.POINTER(BvhStats)]),
+    "bsm_scene_release": (C.c_int32, [C.c_void_p, C.c_uint32]),
+    "bsm_bvh_build_host": (C.c_int32, [C.POINTER(SceneDesc), C.POINTER(BvhOpts), C.c_void_p, C.c_uint64,
+                                       C.c_void_p, C.c_uint64, C.POINTER(BvhStats)]),
+    "bsm_scene_device_bytes": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64)]),
+    "bsm_scene_download_bvh": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "bsm_pt_settings_default": (None, [C.POINTER(PtSettings)]),
+    "bsm_render": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.c_uint32, C.POINTER(PtSettings),
+                               C.POINTER(ViewOutput), C.POINTER(RenderStats)]),
+    "bsm_read_view": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(ViewOutput)]),
+    "bsm_export_history": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32), C.c_uint32]),
+    "bsm_import_history": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.c_void_p, C.c_uint32,
+                                       C.c_uint32]),
+    "bsm_trace_closest": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
+    "bsm_trace_any": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
+    "bsm_trace_counts": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "bsm_scene_generate": (C.c_int32, [C.POINTER(SceneGenParams), C.POINTER(SceneDesc), C.POINTER(Camera)]),
+    "bsm_scene_gen_free": (None, [C.POINTER(SceneDesc)]),
+}
+
+
+def lib() -> C.CDLL:
+    """Loads libbsm_pt.so (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from importlib import util
+        spec = util.spec_from_file_location("_bsm_build", os.path.join(HERE, "build.py"))
+        mod = util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    L = C.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def declared_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def _ptr(a: np.ndarray, ctype=C.c_float):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+# ----------------------------------------------------------- scene data ----
+@dataclass
+class SceneData:
+    """A scene in host memory (numpy arrays) — what bsm_scene_desc points at."""
+    positions: np.ndarray             # (V, 3) float32
+    indices: np.ndarray | None        # (T, 3) uint32
+    material_ids: np.ndarray          # (T,) uint32
+    materials: np.ndarray             # (M, 5) float32: base rgb, roughness, metallic
+    lights: np.ndarray                # (L, 6) float32: direction to light, emission
+    sky_kind: int = BSM_SKY_CONSTANT
+    sky_color: tuple = (0.5, 0.5, 0.5)
+    sky_texels: np.ndarray | None = None  # (H, W, 4) uint16 IEEE half
+    camera: Camera | None = None
+    _keep: list = field(default_factory=list, repr=False)
+
+    @property
+    def num_triangles(self) -> int:
+        return int(self.material_ids.shape[0])
+
+    def desc(self) -> SceneDesc:
+        pos = np.ascontiguousarray(self.positions, np.float32)
+        idx = None if self.indices is None else np.ascontiguousarray(self.indices, np.uint32)
+        mids = np.ascontiguousarray(self.material_ids, np.uint32)
+        mats = (Material * len(self.materials))()
+        for i, m in enumerate(self.materials):
+            mats[i].base_color[:] = [float(m[0]), float(m[1]), float(m[2])]
+            mats[i].roughness = float(m[3])
+            mats[i].metallic = float(m[4])
+        lights = (DirLight * max(1, len(self.lights)))()
+        for i, l in enumerate(self.lights):
+            lights[i].direction[:] = [float(x) for x in l[:3]]
+            lights[i].emission[:] = [float(x) for x in l[3:6]]
+        d = SceneDesc()
+        d.num_vertices = pos.shape[0]
+        d.positions = _ptr(pos)
+        d.num_triangles = mids.shape[0]
+        d.indices = _ptr(idx, C.c_uint32) if idx is not None else None
+        d.material_ids = _ptr(mids, C.c_uint32)
+        d.num_materials = len(self.materials)
+        d.materials = mats
+        d.num_dir_lights = len(self.lights)
+        d.dir_lights = lights
+        d.sky.kind = self.sky_kind
+        d.sky.color[:] = list(self.sky_color)
+        if self.sky_texels is not None:
+            tex = np.ascontiguousarray(self.sky_texels, np.uint16)
+            d.sky.width = tex.shape[1]
+            d.sky.height = tex.shape[0]
+            d.sky.rgba16f = _ptr(tex, C.c_uint16)
+            self._keep = [pos, idx, mids, mats, lights, tex]
+        else:
+            self._keep = [pos, idx, mids, mats, lights]
+        return d
+
+
+def generate_scene(kind: int, seed: int = 1, grid: int = 0, spheres: int = 0, sky_width: int = 0,
+                   sky_height: int = 0, width: int = 256, height: int = 256) -> SceneData:
+    """Seeded procedural scene (bsm_scene_generate), copied into numpy arrays."""
+    L = lib()
+    p = SceneGenParams(kind, seed, grid, spheres, sky_width, sky_height)
+    d = SceneDesc()
+    cam = Camera()
+    st = L.bsm_scene_generate(C.byref(p), C.byref(d), C.byref(cam))
+    if st != BSM_OK:
+        raise BsmError(st, "bsm_scene_generate failed")
+    try:
+        nv, nt, nm, nl = d.num_vertices, d.num_triangles, d.num_materials, d.num_dir_lights
+        pos = np.ctypeslib.as_array(d.positions, (nv, 3)).copy()
+        idx = np.ctypeslib.as_array(d.indices, (nt, 3)).copy() if d.indices else None
+        mids = np.ctypeslib.as_array(d.material_ids, (nt,)).copy()
+        mats = np.array([[*d.materials[i].base_color, d.materials[i].roughness, d.materials[i].metallic]
+                         for i in range(nm)], np.float32)
+        lights = np.array([[*d.dir_lights[i].direction, *d.dir_lights[i].emission] for i in range(nl)], np.float32)
+        tex = None
+        if d.sky.kind == BSM_SKY_EQUIRECT:
+            tex = np.ctypeslib.as_array(d.sky.rgba16f, (d.sky.height, d.sky.width, 4)).copy()
+        sky_color = tuple(d.sky.color)
+        sky_kind = d.sky.kind
+    finally:
+        L.bsm_scene_gen_free(C.byref(d))
+    cam.width, cam.height = width, height
+    return SceneData(pos, idx, mids, mats, lights, sky_kind, sky_color, tex, cam)
+
+
+def bvh_build_host(scene: SceneData, sah_bins=0, max_leaf=0, threads=0):
+    """Host build of the compressed 8-wide BVH: returns (nodes bytes, tris bytes, BvhStats)."""
+    L = lib()
+    d = scene.desc()
+    o = BvhOpts(sah_bins, max_leaf, threads)
+    s = BvhStats()
+    st = L.bsm_bvh_build_host(C.byref(d), C.byref(o), None, 0, None, 0, C.byref(s))
+    if st != BSM_OK:
+        raise BsmError(st, "bsm_bvh_build_host failed")
+    nodes = np.zeros(s.node_bytes, np.uint8)
+    tris = np.zeros(s.tri_bytes, np.uint8)
+    st = L.bsm_bvh_build_host(C.byref(d), C.byref(o), nodes.ctypes.data, nodes.size, tris.ctypes.data, tris.size,
+                              C.byref(s))
+    if st != BSM_OK:
+        raise BsmError(st, "bsm_bvh_build_host failed")
+    return nodes, tris, s
+
+
+def make_camera(position, front, up=(0.0, 1.0, 0.0), yfov_deg=60.0, width=256, height=256) -> Camera:
+    c = Camera()
+    c.position[:] = [float(x) for x in position]
+    c.front[:] = [float(x) for x in front]
+    c.up[:] = [float(x) for x in up]
+    c.yfov_deg = yfov_deg
+    c.width, c.height = width, height
+    return c
+
+
+def settings(spp=1, max_segments=0, max_bounces=3, seed=1, flags=0, ray_length=100.0, accumulate=0,
+             sample_offset=0, wavefront_capacity=0, block_size=0, t_min=0.0) -> PtSettings:
+    s = PtSettings()
+    lib().bsm_pt_settings_default(C.byref(s))
+    s.spp, s.max_segments, s.max_bounces, s.seed, s.flags = spp, max_segments, max_bounces, seed, flags
+    s.ray_length, s.accumulate, s.sample_offset = ray_length, accumulate, sample_offset
+    s.wavefront_capacity, s.block_size, s.t_min = wavefront_capacity, block_size, t_min
+    return s
+
+
+# -------------------------------------------------------------- context ----
+class Context:
+    """One CUDA device context (bsm_context)."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0):
+        self._L = lib()
+        h = C.c_void_p()
+        st = self._L.bsm_create(C.byref(h), device, budget_bytes)
+        if st != BSM_OK:
+            raise BsmError(st, "bsm_create failed (no CUDA device?)")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self._L.bsm_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def check(self, st: int):
+        if st != BSM_OK:
+            raise BsmError(st, self._L.bsm_last_error(self.h).decode())
+
+    # scenes
+    def upload(self, scene: SceneData) -> int:
+        sid = C.c_uint32()
+        self.check(self._L.bsm_scene_upload(self.h, C.byref(scene.desc()), C.byref(sid)))
+        return sid.value
+
+    def build_bvh(self, scene_id: int, sah_bins=0, max_leaf=0, threads=0) -> BvhStats:
+        o = BvhOpts(sah_bins, max_leaf, threads)
+        s = BvhStats()
+        self.check(self._L.bsm_scene_build_bvh(self.h, scene_id, C.byref(o), C.byref(s)))
+        return s
+
+    def load_scene(self, scene: SceneData) -> int:
+        sid = self.upload(scene)
+        self.build_bvh(sid)
+        return sid
+
+    def release(self, scene_id: int):
+        self.check(self._L.bsm_scene_release(self.h, scene_id))
+
+    def scene_bytes(self, scene_id: int) -> int:
+        b = C.c_uint64()
+        self.check(self._L.bsm_scene_device_bytes(self.h, scene_id, C.byref(b)))
+        return b.value
+
+    def download_bvh(self, scene_id: int, stats: BvhStats):
+        nodes = np.zeros(stats.node_bytes, np.uint8)
+        tris = np.zeros(stats.tri_bytes, np.uint8)
+        self.check(self._L.bsm_scene_download_bvh(self.h, scene_id, nodes.ctypes.data, tris.ctypes.data))
+        return nodes, tris
+
+    # stages
+    def trace_closest(self, scene_id: int, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        hits = np.zeros((rays.shape[0], 4), np.uint32)
+        self.check(self._L.bsm_trace_closest(self.h, scene_id, rays.ctypes.data, rays.shape[0], hits.ctypes.data,
+                                             BSM_HOST))
+        return hits
+
+    def trace_any(self, scene_id: int, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        occ = np.zeros(rays.shape[0], np.uint8)
+        self.check(self._L.bsm_trace_any(self.h, scene_id, rays.ctypes.data, rays.shape[0], occ.ctypes.data,
+                                         BSM_HOST))
+        return occ
+
+    def trace_counts(self, scene_id: int, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        cnt = np.zeros((rays.shape[0], 2), np.uint32)
+        self.check(self._L.bsm_trace_counts(self.h, scene_id, rays.ctypes.data, rays.shape[0], cnt.ctypes.data))
+        return cnt
+
+    # render
+    def render(self, scene_id: int, cameras, s: PtSettings, outputs: bool = True, stats: bool = True):
+        """Renders views; returns (list of (H, W, 4) float32 images or None, RenderStats or None)."""
+        if isinstance(cameras, Camera):
+            cameras = [cameras]
+        n = len(cameras)
+        cams = (Camera * n)(*cameras)
+        outs = None
+        imgs = None
+        if outputs:
+            imgs = [np.zeros((c.height, c.width, 4), np.float32) for c in cameras]
+            outs = (ViewOutput * n)()
+            for i, im in enumerate(imgs):
+                outs[i].rgba = im.ctypes.data
+                outs[i].row_pitch_px = 0
+                outs[i].location = BSM_HOST
+        rs = RenderStats() if stats else None
+        self.check(self._L.bsm_render(self.h, scene_id, cams, n, C.byref(s), outs,
+                                      C.byref(rs) if rs is not None else None))
+        return imgs, rs
+
+    def sync(self, timeout_ms: int = 0):
+        self.check(self._L.bsm_sync(self.h, timeout_ms))
+
+
+# -------------------------------------------------- reference-shaped API ----
+@dataclass
+class PathTracingSettings:
+    """BasicRenderer::PathTracingSettings (basic.hpp:76-81) plus the explicit spp and seed."""
+    ray_length: float = 100.0
+    max_bounces: int = 3
+    denoise: bool = True
+    accumulate: bool = True
+    spp: int = 1
+    seed: int = 1
+
+
+class PathTracingPass:
+    """Mirror of PathTracingPass (path_tracing.hpp:13-35) on the GB300 pass.
+
+    update_params() takes the lights and skybox the reference reads from its
+    LightsContext / SkyboxContext; render() traces one camera and returns the
+    pass output's colour (the running mean over accumulated frames)."""
+
+    @dataclass
+    class OutputData:
+        color: np.ndarray
+
+    def __init__(self, ctx: Context, scene: SceneData):
+        self.ctx = ctx
+        self.scene = scene
+        self.scene_id = None
+        self.frame = 0
+
+    def update_params(self, lights=None, skybox=None, settings_: PathTracingSettings | None = None):
+        if lights is not None:
+            self.scene.lights = np.asarray(lights, np.float32).reshape(-1, 6)
+        if skybox is not None:
+            self.scene.sky_kind, self.scene.sky_color, self.scene.sky_texels = skybox
+        if self.scene_id is not None:
+            self.ctx.release(self.scene_id)
+        self.scene_id = self.ctx.load_scene(self.scene)
+
+    def render(self, camera: Camera, settings_: PathTracingSettings) -> "PathTracingPass.OutputData":
+        if self.scene_id is None:
+            self.update_params()
+        s = settings(spp=settings_.spp, max_bounces=settings_.max_bounces, seed=settings_.seed,
+                     ray_length=settings_.ray_length, accumulate=1 if settings_.accumulate else 0)
+        imgs, _ = self.ctx.render(self.scene_id, [camera], s, outputs=True, stats=False)
+        self.frame += 1
+        return PathTracingPass.OutputData(color=imgs[0])

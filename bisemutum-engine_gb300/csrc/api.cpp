@@ -1,0 +1,904 @@
+// api.cpp — host side of the C ABI (include/bsm_pt.h): context, scene upload,
+// BVH build, the wavefront render loop and the stage entry points.
+//
+// Replaces the reference's host orchestration of the pass:
+//   PathTracingPass::update_params  (bisemutum/src/renderer/pass/path_tracing.cpp:183-222)
+//   PathTracingPass::render         (path_tracing.cpp:224-490): per camera, the
+//       history check (:231-245), the bounce loop of camera ray / sample ray /
+//       trace / lighting passes (:290-462) and the running-mean accumulation (:464-478).
+// The render graph's passes become launches on one CUDA stream; their queue
+// sizes stay on the device, and a render's launch sequence is captured once
+// into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "bsm_pt.h"
+#include "bvh_build.h"
+#include "pt_device.h"
+#include "pt_math.cuh"
+
+using namespace bsm;
+
+namespace {
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct Scene {
+    // host copies (kept for rebuilds)
+    std::vector<float> positions;
+    std::vector<uint32_t> indices;
+    std::vector<uint32_t> material_ids;
+    uint32_t num_triangles = 0;
+    float extent = 1.0f;
+    bool has_bvh = false;
+    bsm_bvh_stats bvh_stats{};
+    DevBuf nodes, tris, materials, texels, cdf_marg, cdf_cond, pdf_tab;
+    DevScene dev{};
+};
+
+struct ViewHist {
+    bsm_camera cam{};
+    uint32_t spp = 0;
+    uint32_t accum_base = 0;
+    bool valid = false;
+};
+
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uint8_t> key;
+};
+
+}  // namespace
+
+struct bsm_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t budget = 0;
+    uint64_t used = 0;
+    std::string err;
+    std::map<uint32_t, std::unique_ptr<Scene>> scenes;
+    uint32_t next_scene = 1;
+    LaunchCfg lc{};
+    int lc_block = 0;
+    // wavefront buffers
+    Wavefront wf{};
+    DevBuf wf_buf;
+    uint32_t wf_lights = 0;
+    // views and history
+    DevBuf views_dev;
+    std::vector<DevView> views_host;
+    DevBuf accum;                 // float4 per pixel, all views
+    std::vector<ViewHist> hist;   // per view index
+    std::vector<std::pair<uint32_t, uint32_t>> layout;  // (width, height) per view
+    DevBuf out_stage;             // device staging for host outputs
+    DevBuf tmp;                   // stage entry points (host buffers)
+    std::vector<GraphEntry> graphs;
+    cudaEvent_t ev[16] = {};
+    std::vector<cudaEvent_t> stage_ev;
+    std::mutex mu;
+};
+
+namespace {
+
+void clear_graphs(bsm_context* ctx);
+
+bsm_status fail(bsm_context* ctx, bsm_status st, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return st;
+}
+bsm_status cuda_fail(bsm_context* ctx, cudaError_t e, const char* what) {
+    return fail(ctx, BSM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                            \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+bsm_status dev_alloc(bsm_context* ctx, DevBuf& b, size_t bytes) {
+    if (b.bytes >= bytes && b.ptr) return BSM_OK;
+    if (b.ptr) { cudaFree(b.ptr); ctx->used -= b.bytes; b.ptr = nullptr; b.bytes = 0; }
+    if (bytes == 0) return BSM_OK;
+    if (ctx->budget && ctx->used + bytes > ctx->budget)
+        return fail(ctx, BSM_ERR_OUT_OF_MEMORY, "device memory budget exceeded (" + std::to_string(ctx->used + bytes) +
+                                                    " > " + std::to_string(ctx->budget) + " bytes)");
+    cudaError_t e = cudaMalloc(&b.ptr, bytes);
+    if (e != cudaSuccess) {
+        b.ptr = nullptr;
+        cudaGetLastError();
+        return fail(ctx, BSM_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    b.bytes = bytes;
+    ctx->used += bytes;
+    return BSM_OK;
+}
+void dev_free(bsm_context* ctx, DevBuf& b) {
+    if (b.ptr) { cudaFree(b.ptr); ctx->used -= b.bytes; }
+    b.ptr = nullptr;
+    b.bytes = 0;
+}
+
+V3 vnorm(V3 a) { return normalize(a); }
+
+// Camera basis of glm::lookAt(position, position + front, up) (right-handed):
+// s = normalize(cross(f, up)), u = cross(s, f).  camera.cpp:96-98.
+void make_view(const bsm_camera& c, DevView& v) {
+    V3 f = vnorm(v3(c.front[0], c.front[1], c.front[2]));
+    V3 s = vnorm(cross(f, v3(c.up[0], c.up[1], c.up[2])));
+    V3 u = cross(s, f);
+    v.pos[0] = c.position[0]; v.pos[1] = c.position[1]; v.pos[2] = c.position[2];
+    v.s[0] = s.x; v.s[1] = s.y; v.s[2] = s.z;
+    v.u[0] = u.x; v.u[1] = u.y; v.u[2] = u.z;
+    v.f[0] = f.x; v.f[1] = f.y; v.f[2] = f.z;
+    v.tan_half = (float)std::tan((double)c.yfov_deg * 3.14159265358979323846 / 360.0);
+    v.aspect = (float)c.width / (float)c.height;
+    v.width = c.width;
+    v.height = c.height;
+}
+
+bool same_camera(const bsm_camera& a, const bsm_camera& b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
+
+// Sky sampling tables: weights (r + g + b) * sin(theta at the row centre),
+// prefix sums in double, stored as float.
+void build_sky_tables(const bsm_sky& sky, std::vector<float>& marg, std::vector<float>& cond, std::vector<float>& pdf) {
+    const uint32_t W = sky.width, H = sky.height;
+    marg.assign(H + 1, 0.0f);
+    cond.assign((size_t)H * (W + 1), 0.0f);
+    pdf.assign((size_t)H * W, 0.0f);
+    std::vector<double> w((size_t)H * W), rows(H);
+    double total = 0.0;
+    for (uint32_t i = 0; i < H; ++i) {
+        float st, ct;
+        sincos_turns(((float)i + 0.5f) / (2.0f * (float)H), &st, &ct);
+        double rs = 0.0;
+        for (uint32_t j = 0; j < W; ++j) {
+            const uint16_t* t = sky.rgba16f + ((size_t)i * W + j) * 4;
+            float lum = half_to_float(t[0]) + half_to_float(t[1]) + half_to_float(t[2]);
+            double wij = lum > 0.0f ? (double)lum * (double)st : 0.0;
+            w[(size_t)i * W + j] = wij;
+            rs += wij;
+        }
+        rows[i] = rs;
+        total += rs;
+    }
+    for (uint32_t i = 0; i < H; ++i) {
+        float* c = &cond[(size_t)i * (W + 1)];
+        double acc = 0.0;
+        for (uint32_t j = 0; j < W; ++j) {
+            c[j] = rows[i] > 0.0 ? (float)(acc / rows[i]) : (float)j / (float)W;
+            acc += w[(size_t)i * W + j];
+        }
+        c[W] = 1.0f;
+    }
+    double acc = 0.0;
+    for (uint32_t i = 0; i < H; ++i) {
+        marg[i] = total > 0.0 ? (float)(acc / total) : (float)i / (float)H;
+        acc += rows[i];
+    }
+    marg[H] = 1.0f;
+    for (size_t k = 0; k < (size_t)H * W; ++k)
+        pdf[k] = total > 0.0 ? (float)(w[k] * (double)W * (double)H / total) : 0.0f;
+}
+
+bsm_status ensure_launch_cfg(bsm_context* ctx, uint32_t block) {
+    int b = block ? (int)block : 128;
+    if (b != 64 && b != 128 && b != 256) return fail(ctx, BSM_ERR_INVALID_ARG, "block_size must be 64, 128 or 256");
+    if (ctx->lc_block == b) return BSM_OK;
+    query_launch_cfg(ctx->device, b, &ctx->lc);
+    ctx->lc_block = b;
+    return BSM_OK;
+}
+
+bsm_status ensure_wavefront(bsm_context* ctx, uint32_t capacity, uint32_t lights) {
+    if (ctx->wf.capacity >= capacity && ctx->wf_lights >= lights && ctx->wf_buf.ptr) return BSM_OK;
+    size_t C = capacity;
+    size_t sh = C * (lights + 1);
+    size_t bytes = 0;
+    auto sz = [&](size_t n) { size_t off = bytes; bytes += (n + 255) & ~(size_t)255; return off; };
+    size_t o_ro0 = sz(C * 16), o_ro1 = sz(C * 16), o_rd0 = sz(C * 16), o_rd1 = sz(C * 16);
+    size_t o_p0 = sz(C * 16), o_p1 = sz(C * 16), o_t0 = sz(C * 16), o_t1 = sz(C * 16);
+    size_t o_hit = sz(C * 16), o_sho = sz(sh * 16), o_shd = sz(sh * 16), o_shc = sz(sh * 16);
+    size_t o_cnt = sz(kCntWords * 4), o_st = sz(kStatWords * 8);
+    clear_graphs(ctx);  // graphs hold the old pointers
+    dev_free(ctx, ctx->wf_buf);
+    bsm_status s = dev_alloc(ctx, ctx->wf_buf, bytes);
+    if (s) { ctx->wf = Wavefront{}; return s; }
+    char* b = (char*)ctx->wf_buf.ptr;
+    Wavefront& w = ctx->wf;
+    w.capacity = capacity;
+    w.ray_o[0] = (float4*)(b + o_ro0); w.ray_o[1] = (float4*)(b + o_ro1);
+    w.ray_d[0] = (float4*)(b + o_rd0); w.ray_d[1] = (float4*)(b + o_rd1);
+    w.path[0] = (uint4*)(b + o_p0); w.path[1] = (uint4*)(b + o_p1);
+    w.thr[0] = (float4*)(b + o_t0); w.thr[1] = (float4*)(b + o_t1);
+    w.hit = (float4*)(b + o_hit);
+    w.sh_o = (float4*)(b + o_sho); w.sh_d = (float4*)(b + o_shd); w.sh_c = (float4*)(b + o_shc);
+    w.counters = (uint32_t*)(b + o_cnt);
+    w.stats = (unsigned long long*)(b + o_st);
+    ctx->wf_lights = lights;
+    return BSM_OK;
+}
+
+void clear_graphs(bsm_context* ctx) {
+    for (auto& g : ctx->graphs) if (g.exec) cudaGraphExecDestroy(g.exec);
+    ctx->graphs.clear();
+}
+
+Scene* find_scene(bsm_context* ctx, uint32_t id) {
+    auto it = ctx->scenes.find(id);
+    return it == ctx->scenes.end() ? nullptr : it->second.get();
+}
+
+}  // namespace
+
+// ============================================================== context ====
+extern "C" int bsm_api_version(void) { return BSM_API_VERSION; }
+
+extern "C" bsm_status bsm_create(bsm_context** out, int device, uint64_t budget) {
+    if (!out) return BSM_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) { cudaGetLastError(); return BSM_ERR_NO_DEVICE; }
+    if (device < 0 || device >= n) return BSM_ERR_INVALID_ARG;
+    auto* ctx = new bsm_context();
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return BSM_ERR_CUDA; }
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return BSM_ERR_CUDA; }
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    ctx->budget = budget ? budget : (uint64_t)((double)fr * 0.9);
+    for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+    *out = ctx;
+    return BSM_OK;
+}
+
+extern "C" void bsm_destroy(bsm_context* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& g : ctx->graphs) if (g.exec) cudaGraphExecDestroy(g.exec);
+    for (auto& kv : ctx->scenes) {
+        Scene* s = kv.second.get();
+        for (DevBuf* b : {&s->nodes, &s->tris, &s->materials, &s->texels, &s->cdf_marg, &s->cdf_cond, &s->pdf_tab})
+            dev_free(ctx, *b);
+    }
+    dev_free(ctx, ctx->wf_buf);
+    dev_free(ctx, ctx->views_dev);
+    dev_free(ctx, ctx->accum);
+    dev_free(ctx, ctx->out_stage);
+    dev_free(ctx, ctx->tmp);
+    for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
+    for (auto& ev : ctx->stage_ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" const char* bsm_last_error(const bsm_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+extern "C" bsm_status bsm_sync(bsm_context* ctx, uint32_t timeout_ms) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        cudaError_t e = cudaStreamQuery(ctx->stream);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) return cuda_fail(ctx, e, "cudaStreamQuery");
+        auto ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_ms && ms > timeout_ms) return fail(ctx, BSM_ERR_TIMEOUT, "bsm_sync timed out");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    if (ctx->wf.counters) {
+        uint32_t flag = 0;
+        CK(cudaMemcpy(&flag, ctx->wf.counters + kCntError, 4, cudaMemcpyDeviceToHost));
+        if (flag) return fail(ctx, BSM_ERR_DEVICE_CHECK, "a kernel queue overflowed (error flag set)");
+    }
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_device_alloc(bsm_context* ctx, uint64_t bytes, void** ptr) {
+    if (!ctx || !ptr) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->budget && ctx->used + bytes > ctx->budget) return fail(ctx, BSM_ERR_OUT_OF_MEMORY, "budget exceeded");
+    CK(cudaMalloc(ptr, bytes ? bytes : 1));
+    ctx->used += bytes;
+    return BSM_OK;
+}
+extern "C" bsm_status bsm_device_free(bsm_context* ctx, void* ptr) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaFree(ptr));
+    return BSM_OK;
+}
+extern "C" bsm_status bsm_memcpy(bsm_context* ctx, void* dst, const void* src, uint64_t bytes, int kind) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : kind == 1 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    CK(cudaMemcpyAsync(dst, src, bytes, k, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_host_alloc(bsm_context* ctx, uint64_t bytes, void** ptr) {
+    if (!ctx || !ptr) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocDefault));
+    return BSM_OK;
+}
+extern "C" bsm_status bsm_host_free(bsm_context* ctx, void* ptr) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    CK(cudaFreeHost(ptr));
+    return BSM_OK;
+}
+
+// ================================================================ scenes ====
+extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d, uint32_t* scene_id) {
+    if (!ctx || !d || !scene_id) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (d->num_triangles == 0 || !d->positions || d->num_vertices == 0)
+        return fail(ctx, BSM_ERR_INVALID_ARG, "scene needs vertices and triangles");
+    if (d->num_materials == 0 || !d->materials) return fail(ctx, BSM_ERR_INVALID_ARG, "scene needs at least one material");
+    if (d->num_dir_lights > (uint32_t)kMaxLights)
+        return fail(ctx, BSM_ERR_INVALID_ARG, "at most " + std::to_string(kMaxLights) + " directional lights");
+    if (d->sky.kind == BSM_SKY_EQUIRECT && (!d->sky.rgba16f || d->sky.width == 0 || d->sky.height == 0))
+        return fail(ctx, BSM_ERR_INVALID_ARG, "equirect sky needs texels");
+    if (d->sky.kind > BSM_SKY_EQUIRECT) return fail(ctx, BSM_ERR_INVALID_ARG, "unknown sky kind");
+    auto sc = std::make_unique<Scene>();
+    sc->positions.assign(d->positions, d->positions + 3 * (size_t)d->num_vertices);
+    if (d->indices) {
+        sc->indices.assign(d->indices, d->indices + 3 * (size_t)d->num_triangles);
+        for (uint32_t x : sc->indices)
+            if (x >= d->num_vertices) return fail(ctx, BSM_ERR_INVALID_ARG, "vertex index out of range");
+    } else if ((size_t)d->num_vertices < 3 * (size_t)d->num_triangles) {
+        return fail(ctx, BSM_ERR_INVALID_ARG, "triangle soup needs 3 vertices per triangle");
+    }
+    if (d->material_ids) {
+        sc->material_ids.assign(d->material_ids, d->material_ids + d->num_triangles);
+        for (uint32_t m : sc->material_ids)
+            if (m >= d->num_materials) return fail(ctx, BSM_ERR_INVALID_ARG, "material id out of range");
+    }
+    sc->num_triangles = d->num_triangles;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t i = 0; i < (size_t)d->num_vertices; ++i)
+        for (int k = 0; k < 3; ++k) {
+            float p = d->positions[3 * i + k];
+            if (!std::isfinite(p)) return fail(ctx, BSM_ERR_INVALID_ARG, "non-finite vertex position");
+            lo[k] = std::min(lo[k], p); hi[k] = std::max(hi[k], p);
+        }
+    sc->extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
+    // materials: (base.rgb, roughness), (f0.rgb, metallic); f0 = lerp(0.04, base, metallic)
+    std::vector<float4> mats(2 * (size_t)d->num_materials);
+    for (uint32_t m = 0; m < d->num_materials; ++m) {
+        const bsm_material& M = d->materials[m];
+        float f0[3];
+        for (int k = 0; k < 3; ++k) f0[k] = 0.04f + (M.base_color[k] - 0.04f) * M.metallic;
+        mats[2 * m] = make_float4(M.base_color[0], M.base_color[1], M.base_color[2], M.roughness);
+        mats[2 * m + 1] = make_float4(f0[0], f0[1], f0[2], M.metallic);
+    }
+    bsm_status st;
+    if ((st = dev_alloc(ctx, sc->materials, mats.size() * sizeof(float4)))) return st;
+    CK(cudaMemcpy(sc->materials.ptr, mats.data(), mats.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    DevScene& ds = sc->dev;
+    ds.materials = (const float4*)sc->materials.ptr;
+    ds.num_materials = d->num_materials;
+    ds.num_lights = d->num_dir_lights;
+    for (uint32_t l = 0; l < d->num_dir_lights; ++l) {
+        const bsm_dir_light& L = d->dir_lights[l];
+        V3 dir = normalize(v3(L.direction[0], L.direction[1], L.direction[2]));
+        ds.light_dir[l] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+        ds.light_e[l] = make_float4(L.emission[0], L.emission[1], L.emission[2], 0.0f);
+    }
+    ds.sky.kind = d->sky.kind;
+    ds.sky.cr = d->sky.color[0]; ds.sky.cg = d->sky.color[1]; ds.sky.cb = d->sky.color[2];
+    if (d->sky.kind == BSM_SKY_EQUIRECT) {
+        const uint32_t W = d->sky.width, H = d->sky.height;
+        std::vector<float> marg, cond, pdf;
+        build_sky_tables(d->sky, marg, cond, pdf);
+        size_t tb = (size_t)W * H * 8;
+        if ((st = dev_alloc(ctx, sc->texels, tb))) return st;
+        if ((st = dev_alloc(ctx, sc->cdf_marg, marg.size() * 4))) return st;
+        if ((st = dev_alloc(ctx, sc->cdf_cond, cond.size() * 4))) return st;
+        if ((st = dev_alloc(ctx, sc->pdf_tab, pdf.size() * 4))) return st;
+        CK(cudaMemcpy(sc->texels.ptr, d->sky.rgba16f, tb, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->cdf_marg.ptr, marg.data(), marg.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->cdf_cond.ptr, cond.data(), cond.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->pdf_tab.ptr, pdf.data(), pdf.size() * 4, cudaMemcpyHostToDevice));
+        ds.sky.width = W; ds.sky.height = H;
+        ds.sky.texels = (const ushort4*)sc->texels.ptr;
+        ds.sky.cdf_marg = (const float*)sc->cdf_marg.ptr;
+        ds.sky.cdf_cond = (const float*)sc->cdf_cond.ptr;
+        ds.sky.pdf_tab = (const float*)sc->pdf_tab.ptr;
+    }
+    ds.ray_offset = 2e-5f * sc->extent;
+    uint32_t id = ctx->next_scene++;
+    ctx->scenes[id] = std::move(sc);
+    *scene_id = id;
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_scene_build_bvh(bsm_context* ctx, uint32_t scene_id, const bsm_bvh_opts* opts,
+                                          bsm_bvh_stats* stats) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
+    BvhBuildResult r;
+    std::string err;
+    if (!build_cwbvh(sc->positions.data(), sc->indices.empty() ? nullptr : sc->indices.data(), sc->num_triangles,
+                     sc->material_ids.empty() ? nullptr : sc->material_ids.data(), opts, r, err))
+        return fail(ctx, BSM_ERR_INVALID_ARG, "BVH build failed: " + err);
+    if (r.max_depth > (uint32_t)kMaxTraversalDepth)
+        return fail(ctx, BSM_ERR_UNSUPPORTED, "BVH deeper than the traversal stack (" + std::to_string(r.max_depth) + ")");
+    bsm_status st;
+    dev_free(ctx, sc->nodes);
+    dev_free(ctx, sc->tris);
+    if ((st = dev_alloc(ctx, sc->nodes, r.nodes.size() * sizeof(CwNode)))) return st;
+    if ((st = dev_alloc(ctx, sc->tris, r.tris.size() * sizeof(CwTri)))) return st;
+    CK(cudaMemcpy(sc->nodes.ptr, r.nodes.data(), r.nodes.size() * sizeof(CwNode), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sc->tris.ptr, r.tris.data(), r.tris.size() * sizeof(CwTri), cudaMemcpyHostToDevice));
+    sc->dev.nodes = (const CwNode*)sc->nodes.ptr;
+    sc->dev.tris = (const CwTri*)sc->tris.ptr;
+    sc->has_bvh = true;
+    bsm_bvh_stats s{};
+    s.num_nodes = (uint32_t)r.nodes.size();
+    s.num_tris = (uint32_t)r.tris.size();
+    s.max_depth = r.max_depth;
+    s.build_ms = r.build_ms;
+    s.sah_cost = r.sah_cost;
+    s.node_bytes = r.nodes.size() * sizeof(CwNode);
+    s.tri_bytes = r.tris.size() * sizeof(CwTri);
+    sc->bvh_stats = s;
+    clear_graphs(ctx);
+    if (stats) *stats = s;
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_bvh_build_host(const bsm_scene_desc* d, const bsm_bvh_opts* opts, void* nodes,
+                                         uint64_t nodes_bytes, void* tris, uint64_t tris_bytes,
+                                         bsm_bvh_stats* stats) {
+    if (!d || !stats || !d->positions || d->num_triangles == 0) return BSM_ERR_INVALID_ARG;
+    if (d->indices)
+        for (size_t i = 0; i < 3 * (size_t)d->num_triangles; ++i)
+            if (d->indices[i] >= d->num_vertices) return BSM_ERR_INVALID_ARG;
+    BvhBuildResult r;
+    std::string err;
+    if (!build_cwbvh(d->positions, d->indices, d->num_triangles, d->material_ids, opts, r, err))
+        return BSM_ERR_INVALID_ARG;
+    bsm_bvh_stats s{};
+    s.num_nodes = (uint32_t)r.nodes.size();
+    s.num_tris = (uint32_t)r.tris.size();
+    s.max_depth = r.max_depth;
+    s.build_ms = r.build_ms;
+    s.sah_cost = r.sah_cost;
+    s.node_bytes = r.nodes.size() * sizeof(CwNode);
+    s.tri_bytes = r.tris.size() * sizeof(CwTri);
+    *stats = s;
+    if (nodes) {
+        if (nodes_bytes < s.node_bytes) return BSM_ERR_INVALID_ARG;
+        std::memcpy(nodes, r.nodes.data(), s.node_bytes);
+    }
+    if (tris) {
+        if (tris_bytes < s.tri_bytes) return BSM_ERR_INVALID_ARG;
+        std::memcpy(tris, r.tris.data(), s.tri_bytes);
+    }
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_scene_release(bsm_context* ctx, uint32_t scene_id) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
+    cudaStreamSynchronize(ctx->stream);
+    for (DevBuf* b : {&sc->nodes, &sc->tris, &sc->materials, &sc->texels, &sc->cdf_marg, &sc->cdf_cond, &sc->pdf_tab})
+        dev_free(ctx, *b);
+    ctx->scenes.erase(scene_id);
+    clear_graphs(ctx);
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_scene_device_bytes(bsm_context* ctx, uint32_t scene_id, uint64_t* bytes) {
+    if (!ctx || !bytes) return BSM_ERR_INVALID_ARG;
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
+    uint64_t b = 0;
+    for (DevBuf* x : {&sc->nodes, &sc->tris, &sc->materials, &sc->texels, &sc->cdf_marg, &sc->cdf_cond, &sc->pdf_tab})
+        b += x->bytes;
+    *bytes = b;
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_scene_download_bvh(bsm_context* ctx, uint32_t scene_id, void* nodes, void* tris) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc || !sc->has_bvh) return fail(ctx, BSM_ERR_NOT_FOUND, "scene has no BVH");
+    if (nodes) CK(cudaMemcpy(nodes, sc->nodes.ptr, sc->bvh_stats.node_bytes, cudaMemcpyDeviceToHost));
+    if (tris) CK(cudaMemcpy(tris, sc->tris.ptr, sc->bvh_stats.tri_bytes, cudaMemcpyDeviceToHost));
+    return BSM_OK;
+}
+
+// =============================================================== render ====
+extern "C" void bsm_pt_settings_default(bsm_pt_settings* s) {
+    if (!s) return;
+    std::memset(s, 0, sizeof(*s));
+    s->ray_length = 100.0f;
+    s->max_bounces = 3;
+    s->accumulate = 1;
+    s->denoise = 1;
+    s->spp = 1;
+    s->seed = 1;
+}
+
+namespace {
+
+// Records the launch sequence of one render (all chunks) on ctx->stream.
+// With `ev` non-null an event is recorded after every launch (no host waits):
+// ev[0] before the first launch, then one per stage; `tags` gets the stage of
+// each interval (0 camera, 1 extend, 2 shade, 3 shadow).
+void record_render(bsm_context* ctx, const Scene* sc, uint32_t n_views, uint64_t total_paths, uint32_t capacity,
+                   uint32_t max_seg, bool count_traversal, std::vector<cudaEvent_t>* ev, std::vector<int>* tags) {
+    const LaunchCfg& lc = ctx->lc;
+    cudaStream_t st = ctx->stream;
+    const DevView* views = (const DevView*)ctx->views_dev.ptr;
+    float4* accum = (float4*)ctx->accum.ptr;
+    size_t k = 0;
+    auto mark = [&](int tag) {
+        if (!ev) return;
+        if (k >= ev->size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ev->push_back(e);
+        }
+        cudaEventRecord((*ev)[k++], st);
+        if (tag >= 0) tags->push_back(tag);
+    };
+    mark(-1);
+    for (uint64_t begin = 0; begin < total_paths; begin += capacity) {
+        uint32_t count = (uint32_t)std::min<uint64_t>(capacity, total_paths - begin);
+        cudaMemsetAsync(ctx->wf.counters, 0, kCntError * 4, st);
+        launch_camera(lc, st, views, n_views, begin, count, ctx->wf, max_seg);
+        mark(0);
+        int q = 0;
+        for (uint32_t seg = 0; seg < max_seg; ++seg) {
+            launch_extend(lc, st, sc->dev, ctx->wf, q, seg, count_traversal);
+            mark(1);
+            launch_shade(lc, st, sc->dev, views, ctx->wf, q, seg, accum);
+            mark(2);
+            launch_shadow(lc, st, sc->dev, ctx->wf, seg, accum);
+            mark(3);
+            q ^= 1;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_camera* views, uint32_t n_views,
+                                 const bsm_pt_settings* settings, const bsm_view_output* outputs,
+                                 bsm_render_stats* stats) {
+    if (!ctx || !views || n_views == 0 || !settings) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
+    if (!sc->has_bvh) return fail(ctx, BSM_ERR_BAD_STATE, "scene BVH not built (bsm_scene_build_bvh)");
+    const bsm_pt_settings& s = *settings;
+    if (s.spp == 0) return fail(ctx, BSM_ERR_INVALID_ARG, "spp must be >= 1");
+    uint32_t max_seg = s.max_segments ? s.max_segments : (std::min(std::max(s.max_bounces, 2u), 16u) - 1u);
+    if (max_seg == 0 || max_seg > (uint32_t)kMaxSeg) return fail(ctx, BSM_ERR_INVALID_ARG, "max_segments must be 1..16");
+    if (!(s.ray_length > 0.0f)) return fail(ctx, BSM_ERR_INVALID_ARG, "ray_length must be > 0");
+    if (s.t_min < 0.0f) return fail(ctx, BSM_ERR_INVALID_ARG, "t_min must be >= 0");
+    bsm_status st;
+    if ((st = ensure_launch_cfg(ctx, s.block_size))) return st;
+
+    // view layout and history (path_tracing.cpp:231-245: history kept per camera,
+    // reset when it moves or the target changes size)
+    bool relayout = ctx->layout.size() != n_views;
+    for (uint32_t v = 0; v < n_views && !relayout; ++v)
+        relayout = ctx->layout[v].first != views[v].width || ctx->layout[v].second != views[v].height;
+    uint64_t total_px = 0;
+    for (uint32_t v = 0; v < n_views; ++v) {
+        if (views[v].width == 0 || views[v].height == 0) return fail(ctx, BSM_ERR_INVALID_ARG, "view size must be > 0");
+        if (!(views[v].yfov_deg > 0.0f && views[v].yfov_deg < 180.0f))
+            return fail(ctx, BSM_ERR_INVALID_ARG, "yfov_deg must be in (0, 180)");
+        total_px += (uint64_t)views[v].width * views[v].height;
+    }
+    if (total_px >= (1ull << 32)) return fail(ctx, BSM_ERR_INVALID_ARG, "too many pixels in one call");
+    if (n_views > 65535) return fail(ctx, BSM_ERR_INVALID_ARG, "at most 65535 views per call");
+    if (relayout) {
+        cudaStreamSynchronize(ctx->stream);
+        clear_graphs(ctx);
+        if ((st = dev_alloc(ctx, ctx->accum, total_px * sizeof(float4)))) return st;
+        CK(cudaMemsetAsync(ctx->accum.ptr, 0, total_px * sizeof(float4), ctx->stream));
+        ctx->layout.assign(n_views, {0, 0});
+        ctx->hist.assign(n_views, ViewHist{});
+        uint32_t base = 0;
+        for (uint32_t v = 0; v < n_views; ++v) {
+            ctx->layout[v] = {views[v].width, views[v].height};
+            ctx->hist[v].accum_base = base;
+            base += views[v].width * views[v].height;
+        }
+    }
+    ctx->views_host.resize(n_views);
+    uint64_t total_paths = 0;
+    for (uint32_t v = 0; v < n_views; ++v) {
+        ViewHist& h = ctx->hist[v];
+        bool reset = !s.accumulate || !h.valid || !same_camera(h.cam, views[v]);
+        if (reset) {
+            CK(cudaMemsetAsync((float4*)ctx->accum.ptr + h.accum_base, 0,
+                               (size_t)views[v].width * views[v].height * sizeof(float4), ctx->stream));
+            h.spp = 0;
+            h.cam = views[v];
+            h.valid = true;
+        }
+        DevView& dv = ctx->views_host[v];
+        std::memset(&dv, 0, sizeof(dv));
+        make_view(views[v], dv);
+        dv.ray_length = s.ray_length;
+        dv.t_min = s.t_min;
+        dv.spp = s.spp;
+        dv.sample_offset = s.sample_offset + h.spp;
+        dv.seed = s.seed;
+        dv.path_base = total_paths;
+        dv.accum_base = h.accum_base;
+        dv.max_segments = max_seg;
+        dv.flags = s.flags;
+        total_paths += (uint64_t)views[v].width * views[v].height * s.spp;
+    }
+    uint32_t capacity = s.wavefront_capacity ? s.wavefront_capacity : (uint32_t)std::min<uint64_t>(total_paths, 1u << 23);
+    capacity = std::max(capacity, 1024u);
+    if ((st = ensure_wavefront(ctx, capacity, std::max(sc->dev.num_lights, 1u)))) return st;
+    capacity = std::min(capacity, ctx->wf.capacity);
+    if ((st = dev_alloc(ctx, ctx->views_dev, n_views * sizeof(DevView)))) return st;
+    CK(cudaMemcpyAsync(ctx->views_dev.ptr, ctx->views_host.data(), n_views * sizeof(DevView), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemsetAsync(ctx->wf.stats, 0, kStatWords * 8, ctx->stream));
+    CK(cudaMemsetAsync(ctx->wf.counters + kCntError, 0, 4, ctx->stream));
+
+    bool timing = (s.flags & BSM_PT_STAGE_TIMING) != 0;
+    bool counting = (s.flags & BSM_PT_COUNT_TRAVERSAL) != 0;
+    bool use_graph = !timing && !counting && !(s.flags & BSM_PT_NO_GRAPH);
+    float stage_ms[4] = {0, 0, 0, 0};
+    std::vector<int> tags;
+    CK(cudaEventRecord(ctx->ev[8], ctx->stream));
+    if (use_graph) {
+        // key: everything the recorded launches depend on
+        std::vector<uint8_t> key(64);
+        uint64_t kv[8] = {(uint64_t)scene_id, (uint64_t)n_views, total_paths, capacity, max_seg,
+                          (uint64_t)(uintptr_t)ctx->wf_buf.ptr, (uint64_t)(uintptr_t)ctx->accum.ptr,
+                          (uint64_t)(uintptr_t)ctx->views_dev.ptr ^ ((uint64_t)ctx->lc_block << 56)};
+        std::memcpy(key.data(), kv, 64);
+        cudaGraphExec_t exec = nullptr;
+        for (auto& g : ctx->graphs) if (g.key == key) exec = g.exec;
+        if (!exec) {
+            cudaGraph_t graph;
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            record_render(ctx, sc, n_views, total_paths, capacity, max_seg, false, nullptr, nullptr);
+            CK(cudaStreamEndCapture(ctx->stream, &graph));
+            CK(cudaGraphInstantiate(&exec, graph, 0));
+            cudaGraphDestroy(graph);
+            if (ctx->graphs.size() >= 16) {
+                cudaGraphExecDestroy(ctx->graphs.front().exec);
+                ctx->graphs.erase(ctx->graphs.begin());
+            }
+            ctx->graphs.push_back({exec, key});
+        }
+        CK(cudaGraphLaunch(exec, ctx->stream));
+    } else {
+        record_render(ctx, sc, n_views, total_paths, capacity, max_seg, counting, timing ? &ctx->stage_ev : nullptr,
+                      &tags);
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[9], ctx->stream));
+    for (uint32_t v = 0; v < n_views; ++v) ctx->hist[v].spp += s.spp;
+
+    // outputs: running mean
+    bool host_out = false;
+    if (outputs) {
+        for (uint32_t v = 0; v < n_views; ++v) {
+            const bsm_view_output& o = outputs[v];
+            if (!o.rgba) continue;
+            uint32_t W = views[v].width, H = views[v].height;
+            uint32_t pitch = o.row_pitch_px ? o.row_pitch_px : W;
+            if (pitch < W) return fail(ctx, BSM_ERR_INVALID_ARG, "row_pitch_px < width");
+            float inv = 1.0f / (float)ctx->hist[v].spp;
+            const float4* acc = (const float4*)ctx->accum.ptr + ctx->hist[v].accum_base;
+            if (o.location == BSM_DEVICE) {
+                launch_resolve(ctx->stream, acc, W, H, inv, (float4*)o.rgba, pitch);
+            } else {
+                if ((st = dev_alloc(ctx, ctx->out_stage, (size_t)W * H * sizeof(float4)))) return st;
+                launch_resolve(ctx->stream, acc, W, H, inv, (float4*)ctx->out_stage.ptr, W);
+                CK(cudaMemcpy2DAsync(o.rgba, (size_t)pitch * 16, ctx->out_stage.ptr, (size_t)W * 16, (size_t)W * 16, H,
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+                host_out = true;
+            }
+        }
+        CK(cudaGetLastError());
+    }
+    if (timing) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (size_t i = 0; i < tags.size(); ++i) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ctx->stage_ev[i], ctx->stage_ev[i + 1]);
+            stage_ms[tags[i]] += ms;
+        }
+    }
+    if (host_out || stats) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        uint32_t flag = 0;
+        CK(cudaMemcpy(&flag, ctx->wf.counters + kCntError, 4, cudaMemcpyDeviceToHost));
+        if (flag) return fail(ctx, BSM_ERR_DEVICE_CHECK, "a kernel queue overflowed (error flag set)");
+    }
+    if (stats) {
+        unsigned long long h[kStatWords];
+        CK(cudaMemcpy(h, ctx->wf.stats, sizeof(h), cudaMemcpyDeviceToHost));
+        std::memset(stats, 0, sizeof(*stats));
+        stats->paths = total_paths;
+        for (uint32_t k = 0; k < (uint32_t)kMaxSeg; ++k) {
+            stats->rays_per_segment[k] = h[kStatExtend + k];
+            stats->extend_rays += h[kStatExtend + k];
+            stats->shadow_rays += h[kStatShadow + k];
+        }
+        stats->chunks = (uint32_t)((total_paths + capacity - 1) / capacity);
+        stats->extend_launches = stats->chunks * max_seg;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ctx->ev[8], ctx->ev[9]);
+        stats->ms_total = ms;
+        stats->ms_camera = stage_ms[0];
+        stats->ms_extend = stage_ms[1];
+        stats->ms_shade = stage_ms[2];
+        stats->ms_shadow = stage_ms[3];
+        stats->traversal_nodes = h[kStatNodes];
+        stats->traversal_tris = h[kStatTris];
+    }
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_read_view(bsm_context* ctx, uint32_t view_index, const bsm_view_output* o) {
+    if (!ctx || !o || !o->rgba) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (view_index >= ctx->hist.size() || !ctx->hist[view_index].valid || ctx->hist[view_index].spp == 0)
+        return fail(ctx, BSM_ERR_NOT_FOUND, "view has no history");
+    const ViewHist& h = ctx->hist[view_index];
+    uint32_t W = ctx->layout[view_index].first, H = ctx->layout[view_index].second;
+    uint32_t pitch = o->row_pitch_px ? o->row_pitch_px : W;
+    const float4* acc = (const float4*)ctx->accum.ptr + h.accum_base;
+    float inv = 1.0f / (float)h.spp;
+    if (o->location == BSM_DEVICE) {
+        launch_resolve(ctx->stream, acc, W, H, inv, (float4*)o->rgba, pitch);
+        CK(cudaGetLastError());
+        return BSM_OK;
+    }
+    bsm_status st;
+    if ((st = dev_alloc(ctx, ctx->out_stage, (size_t)W * H * sizeof(float4)))) return st;
+    launch_resolve(ctx->stream, acc, W, H, inv, (float4*)ctx->out_stage.ptr, W);
+    CK(cudaMemcpy2DAsync(o->rgba, (size_t)pitch * 16, ctx->out_stage.ptr, (size_t)W * 16, (size_t)W * 16, H,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_export_history(bsm_context* ctx, uint32_t view_index, float* sums, uint32_t* spp,
+                                         uint32_t location) {
+    if (!ctx || !sums || !spp) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (view_index >= ctx->hist.size() || !ctx->hist[view_index].valid)
+        return fail(ctx, BSM_ERR_NOT_FOUND, "view has no history");
+    const ViewHist& h = ctx->hist[view_index];
+    size_t bytes = (size_t)ctx->layout[view_index].first * ctx->layout[view_index].second * sizeof(float4);
+    CK(cudaMemcpyAsync(sums, (float4*)ctx->accum.ptr + h.accum_base, bytes,
+                       location == BSM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *spp = h.spp;
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_import_history(bsm_context* ctx, uint32_t view_index, const bsm_camera* cam,
+                                         const float* sums, uint32_t spp, uint32_t location) {
+    if (!ctx || !sums || !cam) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (view_index >= ctx->hist.size()) return fail(ctx, BSM_ERR_NOT_FOUND, "view slot does not exist (render once first)");
+    if (ctx->layout[view_index].first != cam->width || ctx->layout[view_index].second != cam->height)
+        return fail(ctx, BSM_ERR_INVALID_ARG, "camera size differs from the view slot");
+    ViewHist& h = ctx->hist[view_index];
+    size_t bytes = (size_t)cam->width * cam->height * sizeof(float4);
+    CK(cudaMemcpyAsync((float4*)ctx->accum.ptr + h.accum_base, sums, bytes,
+                       location == BSM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    h.cam = *cam;
+    h.spp = spp;
+    h.valid = true;
+    return BSM_OK;
+}
+
+// ===================================================== stage entry points ====
+namespace {
+bsm_status stage_prep(bsm_context* ctx, uint32_t scene_id, Scene** out) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
+    if (!sc->has_bvh) return fail(ctx, BSM_ERR_BAD_STATE, "scene BVH not built");
+    *out = sc;
+    return BSM_OK;
+}
+}  // namespace
+
+extern "C" bsm_status bsm_trace_closest(bsm_context* ctx, uint32_t scene_id, const float* rays, uint32_t n, void* hits,
+                                        uint32_t location) {
+    Scene* sc;
+    bsm_status st = stage_prep(ctx, scene_id, &sc);
+    if (st) return st;
+    if (n == 0) return BSM_OK;
+    if (!rays || !hits) return BSM_ERR_INVALID_ARG;
+    if (location == BSM_DEVICE) {
+        launch_trace_closest(ctx->stream, sc->dev, (const float4*)rays, n, (uint4*)hits, 128);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(ctx->stream));
+        return BSM_OK;
+    }
+    size_t rb = (size_t)n * 32, hb = (size_t)n * 16;
+    if ((st = dev_alloc(ctx, ctx->tmp, rb + hb))) return st;
+    char* b = (char*)ctx->tmp.ptr;
+    CK(cudaMemcpyAsync(b, rays, rb, cudaMemcpyHostToDevice, ctx->stream));
+    launch_trace_closest(ctx->stream, sc->dev, (const float4*)b, n, (uint4*)(b + rb), 128);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(hits, b + rb, hb, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_trace_any(bsm_context* ctx, uint32_t scene_id, const float* rays, uint32_t n,
+                                    uint8_t* occluded, uint32_t location) {
+    Scene* sc;
+    bsm_status st = stage_prep(ctx, scene_id, &sc);
+    if (st) return st;
+    if (n == 0) return BSM_OK;
+    if (!rays || !occluded) return BSM_ERR_INVALID_ARG;
+    if (location == BSM_DEVICE) {
+        launch_trace_any(ctx->stream, sc->dev, (const float4*)rays, n, occluded, 128);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(ctx->stream));
+        return BSM_OK;
+    }
+    size_t rb = (size_t)n * 32;
+    if ((st = dev_alloc(ctx, ctx->tmp, rb + n + 16))) return st;
+    char* b = (char*)ctx->tmp.ptr;
+    CK(cudaMemcpyAsync(b, rays, rb, cudaMemcpyHostToDevice, ctx->stream));
+    launch_trace_any(ctx->stream, sc->dev, (const float4*)b, n, (uint8_t*)(b + rb), 128);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(occluded, b + rb, n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BSM_OK;
+}
+
+// Per-ray traversal counters (nodes visited, triangles tested) for the
+// traversal-bytes figure; not part of the reference interface.
+extern "C" bsm_status bsm_trace_counts(bsm_context* ctx, uint32_t scene_id, const float* rays, uint32_t n,
+                                               uint32_t* counts) {
+    Scene* sc;
+    bsm_status st = stage_prep(ctx, scene_id, &sc);
+    if (st) return st;
+    if (n == 0) return BSM_OK;
+    size_t rb = (size_t)n * 32, cb = (size_t)n * 8;
+    if ((st = dev_alloc(ctx, ctx->tmp, rb + cb))) return st;
+    char* b = (char*)ctx->tmp.ptr;
+    CK(cudaMemcpyAsync(b, rays, rb, cudaMemcpyHostToDevice, ctx->stream));
+    launch_trace_count(ctx->stream, sc->dev, (const float4*)b, n, (uint2*)(b + rb));
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(counts, b + rb, cb, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BSM_OK;
+}

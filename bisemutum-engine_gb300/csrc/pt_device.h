@@ -1,0 +1,119 @@
+// pt_device.h — device-side structures of the wavefront pass and the launch
+// wrappers the host orchestration (api.cpp) calls.
+//
+// HBM layout of one wavefront chunk (capacity C paths, L directional lights):
+//   ray_o[2][C]  float4  origin.xyz, tmin            (ping-pong queues)
+//   ray_d[2][C]  float4  direction.xyz, tmax
+//   path[2][C]   uint4   accum index, flags (segment | max segments | view),
+//                        PCG32 state low/high word
+//   thr[2][C]    float4  throughput.rgb, pdf of the sampled direction
+//   hit[C]       float4  t, leaf triangle index, u, v
+//   sh_o/sh_d/sh_c[(L+1) C] float4  shadow rays and their contributions
+//   counters     uint32  queue sizes per segment, work counters, error flags
+//   stats        uint64  rays per segment (summed over chunks)
+// All queues are structures of arrays read with 128-bit loads.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bvh_layout.h"
+
+namespace bsm {
+
+constexpr int kMaxLights = 4;
+constexpr int kMaxSeg = 16;
+
+struct DevSky {
+    uint32_t kind;             // BSM_SKY_CONSTANT / BSM_SKY_EQUIRECT
+    uint32_t width, height;
+    float cr, cg, cb;          // colour / multiplier
+    const ushort4* texels;     // width*height RGBA16F
+    const float* cdf_marg;     // height + 1
+    const float* cdf_cond;     // height * (width + 1)
+    const float* pdf_tab;      // height * width: pdf in (u,v) space
+};
+
+struct DevScene {
+    const CwNode* nodes;
+    const CwTri* tris;
+    const float4* materials;   // 2 per material: (base.rgb, roughness), (f0.rgb, metallic)
+    uint32_t num_materials;
+    uint32_t num_lights;
+    float4 light_dir[kMaxLights];
+    float4 light_e[kMaxLights];
+    DevSky sky;
+    float ray_offset;          // origin offset along the geometric normal
+};
+
+struct DevView {
+    float pos[3]; float tan_half;
+    float s[3]; float aspect;
+    float u[3]; float ray_length;
+    float f[3]; float t_min;
+    uint32_t width, height, spp, sample_offset;
+    uint64_t seed;
+    uint64_t path_base;        // first path index of this view in the render's path space
+    uint32_t accum_base;       // first accumulator pixel of this view
+    uint32_t max_segments;
+    uint32_t flags;            // BSM_PT_* bits that reach the device
+    uint32_t pad;
+};
+
+// counters[] word offsets
+enum : uint32_t {
+    kCntQueue = 0,                 // [kMaxSeg + 1] extend queue size entering segment s
+    kCntShadow = kCntQueue + 17,   // [kMaxSeg] shadow queue size of segment s
+    kCntWork = kCntShadow + 16,    // [2 * kMaxSeg] persistent-kernel work counters
+    kCntError = kCntWork + 32,     // error flags (bit 0: queue overflow)
+    kCntWords = kCntError + 1
+};
+// stats[] (uint64) offsets
+enum : uint32_t {
+    kStatExtend = 0,               // [kMaxSeg]
+    kStatShadow = kMaxSeg,         // [kMaxSeg]
+    kStatNodes = 2 * kMaxSeg,      // traversal counters (counting extend variant)
+    kStatTris = 2 * kMaxSeg + 1,
+    kStatWords = 2 * kMaxSeg + 2
+};
+
+struct Wavefront {
+    uint32_t capacity;
+    float4* ray_o[2];
+    float4* ray_d[2];
+    uint4* path[2];
+    float4* thr[2];
+    float4* hit;
+    float4* sh_o;
+    float4* sh_d;
+    float4* sh_c;
+    uint32_t* counters;
+    unsigned long long* stats;
+};
+
+struct LaunchCfg {
+    int grid_persistent;    // blocks for the persistent traversal kernels
+    int block_trace;        // threads per block, traversal
+    int block_shade;        // threads per block, shading / camera
+    int grid_shade;
+};
+
+// ---- launch wrappers (pt_kernels.cu) ----
+void launch_camera(const LaunchCfg& lc, cudaStream_t st, const DevView* views, uint32_t n_views,
+                   uint64_t path_begin, uint32_t path_count, const Wavefront& wf, uint32_t max_segments);
+void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, int q,
+                   uint32_t seg, bool count_traversal);
+void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const DevView* views,
+                  const Wavefront& wf, int q, uint32_t seg, float4* accum);
+void launch_shadow(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, uint32_t seg,
+                   float4* accum);
+void launch_resolve(cudaStream_t st, const float4* accum, uint32_t width, uint32_t height, float inv_spp,
+                    float4* out, uint32_t pitch_px);
+void launch_trace_closest(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint4* hits,
+                          int block);
+void launch_trace_any(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint8_t* occluded,
+                      int block);
+void launch_trace_count(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint2* counts);
+// Fills the persistent-kernel grids from the device's SM count and occupancy.
+void query_launch_cfg(int device, int block_trace, LaunchCfg* lc);
+
+}  // namespace bsm

@@ -1,0 +1,411 @@
+// pt_kernels.cu — the sm_103a kernels of the wavefront path-tracing pass.
+//
+// One render is a sequence of chunks; each chunk runs
+//   k_camera  -> [k_extend -> k_shade -> k_shadow] x segments
+// over device-resident queues whose sizes live in device counters, so no
+// stage waits for the host and a whole render can be captured as one CUDA
+// graph.  Stage <-> reference shader:
+//   k_camera   generate_camera_ray_cs   (direction_sample/generate_camera_ray.hlsl:4-16)
+//   k_extend   rt_gbuffer_rgen/rchit/rmiss (rt_gbuffer.hlsl:7-36, hits/rt_gbuffer_hit.hlsl:6-18)
+//   k_shade    deferred_lighting_secondary_cs + sample_secondary_ray_cs
+//              (deferred_lighting_secondary.hlsl:11-111, sample_secondary_ray.hlsl:11-69)
+//   k_shadow   the visibility term of the direct light (there: shadow maps,
+//              lights.hlsl:27-104; here: any-hit rays)
+//   k_resolve  additive blit + pt_accumulate_cs (path_tracing.cpp:436-478, pt_accumulate.hlsl:3-11)
+// Compiled with --fmad=false: every float operation outside the explicit
+// __fmaf_rn of the box test rounds once, as on the CPU oracle.
+#include <cuda_runtime.h>
+
+#include "bsm_pt.h"
+#include "pt_device.h"
+#include "pt_sky.cuh"
+#include "pt_trace.cuh"
+
+namespace bsm {
+
+// Warp-aggregated queue allocation: one atomic per warp, slots in lane order.
+// Must be reached by all 32 lanes (pred may be false).
+__device__ __forceinline__ uint32_t warp_alloc(bool pred, uint32_t* counter) {
+    uint32_t b = __ballot_sync(0xffffffffu, pred);
+    uint32_t base = 0;
+    int lane = threadIdx.x & 31;
+    if (b != 0u && lane == __ffs(b) - 1) base = atomicAdd(counter, (uint32_t)__popc(b));
+    base = __shfl_sync(0xffffffffu, base, b != 0u ? __ffs(b) - 1 : 0);
+    return base + (uint32_t)__popc(b & lanemask_lt());
+}
+
+__device__ __forceinline__ void accum_add(float4* accum, uint32_t idx, V3 c) {
+    atomicAdd(accum + idx, make_float4(c.x, c.y, c.z, 0.0f));
+}
+
+// ---------------------------------------------------------------- camera ----
+__global__ void k_camera(const DevView* __restrict__ views, uint32_t n_views, uint64_t path_begin,
+                         uint32_t path_count, Wavefront wf, uint32_t max_segments_cap) {
+    uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid == 0) wf.counters[kCntQueue + 0] = path_count;
+    if (gid >= path_count) return;
+    uint64_t p = path_begin + gid;
+    // view lookup (views sorted by path_base)
+    uint32_t lo = 0, hi = n_views - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if (views[mid].path_base <= p) lo = mid; else hi = mid - 1;
+    }
+    const DevView& v = views[lo];
+    uint64_t local = p - v.path_base;
+    uint32_t npix = v.width * v.height;
+    uint32_t sample = (uint32_t)(local / npix);
+    uint32_t pixel = (uint32_t)(local - (uint64_t)sample * npix);
+    uint32_t px = pixel % v.width, py = pixel / v.width;
+    Pcg g = pcg_seed(sample_initstate(v.seed, v.sample_offset + sample), (uint64_t)pixel);
+    float jx = 0.5f, jy = 0.5f;
+    if (v.flags & BSM_PT_JITTER) { jx = pcg_uniform(g); jy = pcg_uniform(g); }
+    // generate_camera_ray.hlsl:9-11 restated without the matrices: the inverse
+    // reverse-Z projection of (ndc, 1, 1) is (ndc.x * aspect * tan, ndc.y * tan, -1).
+    float uvx = ((float)px + jx) / (float)v.width;
+    float uvy = ((float)py + jy) / (float)v.height;
+    float ndx = uvx * 2.0f - 1.0f;
+    float ndy = 1.0f - uvy * 2.0f;
+    V3 dl = normalize(v3(ndx * v.aspect * v.tan_half, ndy * v.tan_half, -1.0f));
+    V3 s = v3(v.s[0], v.s[1], v.s[2]), u = v3(v.u[0], v.u[1], v.u[2]), f = v3(v.f[0], v.f[1], v.f[2]);
+    V3 dw = normalize(s * dl.x + u * dl.y + (-f) * dl.z);
+    uint32_t maxseg = v.max_segments < max_segments_cap ? v.max_segments : max_segments_cap;
+    wf.ray_o[0][gid] = make_float4(v.pos[0], v.pos[1], v.pos[2], v.t_min);
+    wf.ray_d[0][gid] = make_float4(dw.x, dw.y, dw.z, v.ray_length);
+    wf.path[0][gid] = make_uint4(v.accum_base + pixel, (maxseg << 8) | (lo << 16), (uint32_t)g.state,
+                                 (uint32_t)(g.state >> 32));
+    wf.thr[0][gid] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+}
+
+// ---------------------------------------------------------------- extend ----
+template <bool kCount>
+__global__ void __launch_bounds__(256) k_extend(DevScene sc, const float4* __restrict__ ray_o,
+                                                const float4* __restrict__ ray_d, float4* __restrict__ hit,
+                                                uint32_t* counters, unsigned long long* stats, uint32_t seg) {
+    uint32_t n = counters[kCntQueue + seg];
+    if (blockIdx.x == 0 && threadIdx.x == 0) stats[kStatExtend + seg] += n;
+    TraceCounters c{0, 0};
+    trace_queue<false, kCount>(
+        sc.nodes, sc.tris, n, counters + kCntWork + 2 * seg,
+        [&](uint32_t i, float4& o, float4& d) { o = ray_o[i]; d = ray_d[i]; },
+        [&](uint32_t i, uint32_t leaf, float t, float u, float v) {
+            hit[i] = make_float4(t, __uint_as_float(leaf), u, v);
+        },
+        &c);
+    if (kCount) {
+        uint32_t cn = c.nodes, ct = c.tris;
+        for (int off = 16; off > 0; off >>= 1) {
+            cn += __shfl_xor_sync(0xffffffffu, cn, off);
+            ct += __shfl_xor_sync(0xffffffffu, ct, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(stats + kStatNodes, (unsigned long long)cn);
+            atomicAdd(stats + kStatTris, (unsigned long long)ct);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- shadow ----
+__global__ void __launch_bounds__(256) k_shadow(DevScene sc, Wavefront wf, uint32_t seg, float4* accum) {
+    uint32_t n = wf.counters[kCntShadow + seg];
+    if (blockIdx.x == 0 && threadIdx.x == 0) wf.stats[kStatShadow + seg] += n;
+    const float4* __restrict__ so = wf.sh_o;
+    const float4* __restrict__ sd = wf.sh_d;
+    const float4* __restrict__ scn = wf.sh_c;
+    trace_queue<true, false>(
+        sc.nodes, sc.tris, n, wf.counters + kCntWork + 2 * seg + 1,
+        [&](uint32_t i, float4& o, float4& d) { o = so[i]; d = sd[i]; },
+        [&](uint32_t i, uint32_t leaf, float, float, float) {
+            if (leaf == kMissPrim) {
+                float4 c = scn[i];
+                accum_add(accum, __float_as_uint(c.w), v3(c.x, c.y, c.z));
+            }
+        },
+        nullptr);
+}
+
+// ----------------------------------------------------------------- shade ----
+__global__ void __launch_bounds__(256) k_shade(DevScene sc, const DevView* __restrict__ views, Wavefront wf,
+                                               int q, uint32_t seg, float4* accum) {
+    const uint32_t n = wf.counters[kCntQueue + seg];
+    const uint32_t cap = wf.capacity;
+    const uint32_t sh_cap = cap * (sc.num_lights + 1u);
+    const float4* __restrict__ in_o = wf.ray_o[q];
+    const float4* __restrict__ in_d = wf.ray_d[q];
+    const uint4* __restrict__ in_p = wf.path[q];
+    const float4* __restrict__ in_t = wf.thr[q];
+    float4* out_o = wf.ray_o[q ^ 1];
+    float4* out_d = wf.ray_d[q ^ 1];
+    uint4* out_p = wf.path[q ^ 1];
+    float4* out_t = wf.thr[q ^ 1];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        uint32_t i = base + threadIdx.x;
+        bool active = i < n;
+        float4 o4 = make_float4(0, 0, 0, 0), d4 = make_float4(0, 0, 1, 0), h4 = make_float4(0, 0, 0, 0);
+        float4 t4 = make_float4(0, 0, 0, 0);
+        uint4 m4 = make_uint4(0, 0, 0, 0);
+        if (active) { o4 = in_o[i]; d4 = in_d[i]; h4 = wf.hit[i]; t4 = in_t[i]; m4 = in_p[i]; }
+        uint32_t leaf = active ? __float_as_uint(h4.y) : kMissPrim;
+        bool is_hit = active && leaf != kMissPrim;
+        uint32_t segi = m4.y & 0xffu, maxseg = (m4.y >> 8) & 0xffu, view_id = m4.y >> 16;
+        V3 thr = v3(t4.x, t4.y, t4.z);
+        V3 d = v3(d4.x, d4.y, d4.z);
+        bool sky_nee = sc.num_lights + 1u > 0u;  // placeholder, refined below per view
+        uint32_t vflags = 0;
+        uint32_t stream = 0;
+        if (active) {
+            const DevView& v = views[view_id];
+            vflags = v.flags;
+            stream = m4.x - v.accum_base;
+        }
+        sky_nee = (vflags & BSM_PT_NO_SKY_NEE) == 0u;
+        if (active && !is_hit) {
+            // deferred_lighting_secondary.hlsl:23-29: skybox x weight on a miss,
+            // here with the MIS weight against sky next-event estimation.
+            V3 le = sky_eval(sc.sky, d);
+            float w = 1.0f;
+            if (segi > 0u && sky_nee) {
+                float pb = t4.w;
+                float pl = sky_pdf(sc.sky, d);
+                float pb2 = pb * pb, pl2 = pl * pl;
+                w = pb2 + pl2 > 0.0f ? pb2 / (pb2 + pl2) : 1.0f;
+            }
+            V3 c = thr * le * w;
+            if (max_comp(c) > 0.0f) accum_add(accum, m4.x, c);
+        }
+        // surface at the hit
+        V3 N = v3(0.0f, 0.0f, 1.0f), P = v3(0.0f, 0.0f, 0.0f);
+        Surface surf;
+        surf.base_color = v3s(0.5f); surf.f0 = v3s(0.04f); surf.f90 = v3s(1.0f); surf.roughness = 0.5f; surf.ior = 1.5f;
+        if (is_hit) {
+            const float4* tp = reinterpret_cast<const float4*>(sc.tris + leaf);
+            float4 a = tp[0], b = tp[1], c = tp[2];
+            V3 va = v3(a.x, a.y, a.z), vb = v3(b.x, b.y, b.z), vc = v3(c.x, c.y, c.z);
+            V3 ng = normalize(cross(vb - va, vc - va));
+            if (dot(ng, d) > 0.0f) ng = -ng;
+            N = ng;
+            P = v3(o4.x, o4.y, o4.z) + d * h4.x;
+            uint32_t mi = __float_as_uint(b.w);
+            if (mi >= sc.num_materials) mi = 0;
+            float4 m0 = sc.materials[2 * mi], m1 = sc.materials[2 * mi + 1];
+            surf.base_color = v3(m0.x, m0.y, m0.z);
+            surf.roughness = m0.w;
+            surf.f0 = v3(m1.x, m1.y, m1.z);
+        }
+        Frame fr = create_frame(N);
+        V3 V = -d;
+        Pcg g;
+        g.state = ((uint64_t)m4.w << 32) | m4.z;
+        g.inc = ((uint64_t)stream << 1) | 1u;
+        float u_sky0 = 0.0f, u_sky1 = 0.0f, u_lobe = 0.0f, u_b0 = 0.0f, u_b1 = 0.0f;
+        if (is_hit) {
+            u_sky0 = pcg_uniform(g); u_sky1 = pcg_uniform(g); u_lobe = pcg_uniform(g);
+            u_b0 = pcg_uniform(g); u_b1 = pcg_uniform(g);
+        }
+        V3 org = P + N * sc.ray_offset;
+        const DevView* vp = views + view_id;
+        float ray_len = is_hit ? vp->ray_length : 0.0f;
+        float tmin = is_hit ? vp->t_min : 0.0f;
+        float rx = 0.001f, ry = 0.001f;
+        aniso_roughness(surf.roughness, &rx, &ry);
+        V3 lv = to_local(fr, V);
+        float p_spec = spec_probability(surf, lv.z);
+        // next-event estimation: directional lights (lights.hlsl:10-13, dir_light_eval)
+        for (uint32_t l = 0; l < sc.num_lights; ++l) {
+            V3 c = v3s(0.0f);
+            V3 L = v3(sc.light_dir[l].x, sc.light_dir[l].y, sc.light_dir[l].z);
+            bool emit = false;
+            if (is_hit && (vflags & BSM_PT_NO_SUN_NEE) == 0u) {
+                V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
+                V3 e = v3(sc.light_e[l].x, sc.light_e[l].y, sc.light_e[l].z);
+                c = thr * e * f;
+                emit = max_comp(c) > 0.0f;
+            }
+            uint32_t slot = warp_alloc(emit, wf.counters + kCntShadow + seg);
+            if (emit) {
+                if (slot < sh_cap) {
+                    wf.sh_o[slot] = make_float4(org.x, org.y, org.z, tmin);
+                    wf.sh_d[slot] = make_float4(L.x, L.y, L.z, ray_len);
+                    wf.sh_c[slot] = make_float4(c.x, c.y, c.z, __uint_as_float(m4.x));
+                } else {
+                    atomicOr(wf.counters + kCntError, 1u);
+                }
+            }
+        }
+        // next-event estimation: sky, MIS (power heuristic) against BSDF sampling
+        {
+            V3 c = v3s(0.0f), L = v3s(0.0f);
+            bool emit = false;
+            if (is_hit && sky_nee) {
+                float pl;
+                V3 le;
+                L = sky_sample(sc.sky, u_sky0, u_sky1, pl, le);
+                if (pl > 0.0f) {
+                    V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
+                    if (max_comp(f) > 0.0f) {
+                        V3 ll = to_local(fr, L);
+                        float pb = mixture_pdf(lv, ll, rx, ry, p_spec);
+                        float pl2 = pl * pl, pb2 = pb * pb;
+                        float w = pl2 / (pl2 + pb2);
+                        c = thr * le * f * (w / pl);
+                        emit = max_comp(c) > 0.0f;
+                    }
+                }
+            }
+            uint32_t slot = warp_alloc(emit, wf.counters + kCntShadow + seg);
+            if (emit) {
+                if (slot < sh_cap) {
+                    wf.sh_o[slot] = make_float4(org.x, org.y, org.z, tmin);
+                    wf.sh_d[slot] = make_float4(L.x, L.y, L.z, ray_len);
+                    wf.sh_c[slot] = make_float4(c.x, c.y, c.z, __uint_as_float(m4.x));
+                } else {
+                    atomicOr(wf.counters + kCntError, 1u);
+                }
+            }
+        }
+        // next direction: lobe mixture (sample_secondary_ray.hlsl:16-28 termination, :51-64 weight)
+        bool cont = false;
+        V3 nthr = v3s(0.0f), L = v3s(0.0f);
+        float pdf = 0.0f;
+        if (is_hit && segi + 1u < maxseg && max_comp(thr) >= 0.001f) {
+            V3 ll;
+            if (u_lobe < p_spec) {
+                V3 h = ggx_vndf_sample(lv, rx, ry, u_b0, u_b1);
+                ll = reflect(-lv, h);
+            } else {
+                ll = cos_hemisphere_sample(u_b0, u_b1);
+            }
+            if (ll.z > 0.0f) {
+                L = to_world(fr, ll);
+                pdf = mixture_pdf(lv, ll, rx, ry, p_spec);
+                V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
+                V3 w = pdf > 0.0f ? f / pdf : v3s(0.0f);
+                if (!isfinite(w.x) || !isfinite(w.y) || !isfinite(w.z)) w = v3s(0.0f);
+                nthr = thr * w;
+                cont = max_comp(nthr) > 0.0f;
+            }
+        }
+        uint32_t slot = warp_alloc(cont, wf.counters + kCntQueue + seg + 1);
+        if (cont) {
+            if (slot < cap) {
+                out_o[slot] = make_float4(org.x, org.y, org.z, tmin);
+                out_d[slot] = make_float4(L.x, L.y, L.z, ray_len);
+                out_p[slot] = make_uint4(m4.x, (m4.y & 0xffffff00u) | (segi + 1u), (uint32_t)g.state,
+                                         (uint32_t)(g.state >> 32));
+                out_t[slot] = make_float4(nthr.x, nthr.y, nthr.z, pdf);
+            } else {
+                atomicOr(wf.counters + kCntError, 1u);
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------------- resolve ----
+__global__ void k_resolve(const float4* __restrict__ accum, uint32_t width, uint32_t height, float inv_spp,
+                          float4* __restrict__ out, uint32_t pitch) {
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t y = blockIdx.y;
+    if (x >= width || y >= height) return;
+    float4 a = accum[(size_t)y * width + x];
+    out[(size_t)y * pitch + x] = make_float4(a.x * inv_spp, a.y * inv_spp, a.z * inv_spp, 1.0f);
+}
+
+// ------------------------------------------------------ stage entry points ----
+__global__ void __launch_bounds__(256) k_trace_closest(DevScene sc, const float4* __restrict__ rays, uint32_t n,
+                                                       uint4* __restrict__ hits) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 o = rays[2 * (size_t)i], d = rays[2 * (size_t)i + 1];
+    RayPre r = make_ray(o, d);
+    float t, u, v;
+    uint32_t leaf = trace_ray<false, false>(r, d.w, sc.nodes, sc.tris, t, u, v, nullptr);
+    uint32_t prim = leaf == kMissPrim ? kMissPrim : sc.tris[leaf].prim;
+    hits[i] = make_uint4(__float_as_uint(t), prim, __float_as_uint(u), __float_as_uint(v));
+}
+
+__global__ void __launch_bounds__(256) k_trace_any(DevScene sc, const float4* __restrict__ rays, uint32_t n,
+                                                   uint8_t* __restrict__ occluded) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 o = rays[2 * (size_t)i], d = rays[2 * (size_t)i + 1];
+    RayPre r = make_ray(o, d);
+    float t, u, v;
+    uint32_t leaf = trace_ray<true, false>(r, d.w, sc.nodes, sc.tris, t, u, v, nullptr);
+    occluded[i] = leaf == kMissPrim ? 0 : 1;
+}
+
+__global__ void __launch_bounds__(256) k_trace_count(DevScene sc, const float4* __restrict__ rays, uint32_t n,
+                                                     uint2* __restrict__ counts) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 o = rays[2 * (size_t)i], d = rays[2 * (size_t)i + 1];
+    RayPre r = make_ray(o, d);
+    float t, u, v;
+    TraceCounters c{0, 0};
+    trace_ray<false, true>(r, d.w, sc.nodes, sc.tris, t, u, v, &c);
+    counts[i] = make_uint2(c.nodes, c.tris);
+}
+
+// ------------------------------------------------------------ launchers ----
+void launch_camera(const LaunchCfg& lc, cudaStream_t st, const DevView* views, uint32_t n_views,
+                   uint64_t path_begin, uint32_t path_count, const Wavefront& wf, uint32_t max_segments) {
+    uint32_t blocks = (path_count + lc.block_shade - 1) / lc.block_shade;
+    if (blocks == 0) blocks = 1;
+    k_camera<<<blocks, lc.block_shade, 0, st>>>(views, n_views, path_begin, path_count, wf, max_segments);
+}
+void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, int q,
+                   uint32_t seg, bool count_traversal) {
+    if (count_traversal)
+        k_extend<true><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
+                                                                        wf.counters, wf.stats, seg);
+    else
+        k_extend<false><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
+                                                                         wf.counters, wf.stats, seg);
+}
+void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const DevView* views,
+                  const Wavefront& wf, int q, uint32_t seg, float4* accum) {
+    k_shade<<<lc.grid_shade, lc.block_shade, 0, st>>>(sc, views, wf, q, seg, accum);
+}
+void launch_shadow(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, uint32_t seg,
+                   float4* accum) {
+    k_shadow<<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum);
+}
+void launch_resolve(cudaStream_t st, const float4* accum, uint32_t width, uint32_t height, float inv_spp,
+                    float4* out, uint32_t pitch_px) {
+    dim3 grid((width + 255) / 256, height);
+    k_resolve<<<grid, 256, 0, st>>>(accum, width, height, inv_spp, out, pitch_px);
+}
+void launch_trace_closest(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint4* hits,
+                          int block) {
+    if (n == 0) return;
+    k_trace_closest<<<(n + block - 1) / block, block, 0, st>>>(sc, rays, n, hits);
+}
+void launch_trace_any(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint8_t* occluded,
+                      int block) {
+    if (n == 0) return;
+    k_trace_any<<<(n + block - 1) / block, block, 0, st>>>(sc, rays, n, occluded);
+}
+void launch_trace_count(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint2* counts) {
+    if (n == 0) return;
+    k_trace_count<<<(n + 127) / 128, 128, 0, st>>>(sc, rays, n, counts);
+}
+
+// Occupancy-derived grid of the persistent kernels: every SM filled.
+void query_launch_cfg(int device, int block_trace, LaunchCfg* lc) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    int per_sm_ext = 0, per_sm_sh = 0, per_sm_shade = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false>, block_trace, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow, block_trace, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_shade, k_shade, 256, 0);
+    int per_sm = per_sm_ext < per_sm_sh ? per_sm_ext : per_sm_sh;
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm_shade < 1) per_sm_shade = 1;
+    lc->block_trace = block_trace;
+    lc->grid_persistent = sms * per_sm;
+    lc->block_shade = 256;
+    lc->grid_shade = sms * per_sm_shade * 4;
+}
+
+}  // namespace bsm

@@ -1,0 +1,351 @@
+// pt_trace.cuh — device-side ray traversal of the compressed 8-wide BVH.
+//
+// Replaces TraceRay on the RT cores (bisemutum/shaders/renderer/raytracing/
+// rt_gbuffer.hlsl:17-25) with a software traversal:
+//   * node test: eight quantised child boxes per 80-byte node; a plane is
+//     rebuilt from its byte with one PRMT and one exact FADD, then one fused
+//     multiply-add gives its slab distance; three-input min/max close the
+//     slabs; the child hit bits of four children are decoded at once from the
+//     packed meta bytes, octant-ordered so the highest bit is the nearest
+//     child (Ylitie, Karras, Laine, HPG 2017);
+//   * node groups (base index + hit bits) on a per-thread stack; triangle
+//     groups are postponed onto the stack while few lanes of the warp have
+//     triangles, so node and triangle work stay converged;
+//   * persistent warps refill lanes whose rays finished from a global queue
+//     counter (one atomic per refill per warp);
+//   * triangle test: the watertight ray/triangle intersection of Woop,
+//     Benthin and Wald (JCGT 2013) with its double-precision fallback on zero
+//     edge functions, in plain IEEE single precision in a fixed order, so t
+//     and the hit primitive are reproducible bit for bit on a CPU.
+// Ties at equal t resolve to the lower primitive id, which makes the closest
+// hit independent of the BVH's shape.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bvh_layout.h"
+
+namespace bsm {
+
+// Far-plane pad: a box is kept when max(near) <= min(far) * (1 + 2^-20).  The
+// builder also pads every child box outward by one quantisation step, so the
+// rounding of the slab arithmetic never culls a box that holds a hit.
+#define BSM_BOX_PAD 1.00000095f
+constexpr int kStackSize = 40;        // node groups (<= tree depth) + postponed triangle groups
+constexpr int kPostponeMaxSp = 16;    // postpone triangle groups only below this stack depth
+
+struct RayPre {
+    float ox, oy, oz, tmin;
+    float dx, dy, dz;
+    float idx, idy, idz;     // 1 / direction (+-inf for a zero component)
+    uint32_t oct_key;        // 7 ^ (sign bits): child visiting key = slot ^ oct_key
+    int kx, ky, kz;          // watertight axis permutation
+    float Sx, Sy, Sz;        // watertight shear
+};
+
+__device__ __forceinline__ float sel3(int k, float x, float y, float z) {
+    return k == 0 ? x : (k == 1 ? y : z);
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+__device__ __forceinline__ RayPre make_ray(float4 o, float4 d) {
+    RayPre r;
+    r.ox = o.x; r.oy = o.y; r.oz = o.z; r.tmin = o.w;
+    r.dx = d.x; r.dy = d.y; r.dz = d.z;
+    // a zero component gives an infinite reciprocal: its slab is then either
+    // (-inf, inf), or empty, or NaN when the origin lies on the plane, and the
+    // NaN is dropped by min/max — the test stays conservative.
+    r.idx = __fdiv_rn(1.0f, d.x);
+    r.idy = __fdiv_rn(1.0f, d.y);
+    r.idz = __fdiv_rn(1.0f, d.z);
+    uint32_t oct = (r.idx < 0.0f ? 1u : 0u) | (r.idy < 0.0f ? 2u : 0u) | (r.idz < 0.0f ? 4u : 0u);
+    r.oct_key = 7u ^ oct;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = 0;
+    float m = ax;
+    if (ay > m) { kz = 1; m = ay; }
+    if (az > m) { kz = 2; }
+    int kx = kz + 1; if (kx == 3) kx = 0;
+    int ky = kx + 1; if (ky == 3) ky = 0;
+    float dkz = sel3(kz, d.x, d.y, d.z);
+    if (dkz < 0.0f) { int t = kx; kx = ky; ky = t; }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.Sx = __fdiv_rn(sel3(kx, d.x, d.y, d.z), dkz);
+    r.Sy = __fdiv_rn(sel3(ky, d.x, d.y, d.z), dkz);
+    r.Sz = __fdiv_rn(1.0f, dkz);
+    return r;
+}
+
+// Watertight test.  Returns true and writes t/u/v when the triangle is hit at
+// t in (tmin, tbest], preferring the lower primitive id on a tie at tbest.
+__device__ __forceinline__ bool tri_test(const RayPre& r, float4 a, float4 b, float4 c, float tbest,
+                                         uint32_t prim, uint32_t best_prim, float& t_out, float& u_out,
+                                         float& v_out) {
+    float Ax0 = a.x - r.ox, Ay0 = a.y - r.oy, Az0 = a.z - r.oz;
+    float Bx0 = b.x - r.ox, By0 = b.y - r.oy, Bz0 = b.z - r.oz;
+    float Cx0 = c.x - r.ox, Cy0 = c.y - r.oy, Cz0 = c.z - r.oz;
+    float Akx = sel3(r.kx, Ax0, Ay0, Az0), Aky = sel3(r.ky, Ax0, Ay0, Az0), Akz = sel3(r.kz, Ax0, Ay0, Az0);
+    float Bkx = sel3(r.kx, Bx0, By0, Bz0), Bky = sel3(r.ky, Bx0, By0, Bz0), Bkz = sel3(r.kz, Bx0, By0, Bz0);
+    float Ckx = sel3(r.kx, Cx0, Cy0, Cz0), Cky = sel3(r.ky, Cx0, Cy0, Cz0), Ckz = sel3(r.kz, Cx0, Cy0, Cz0);
+    float Ax = __fsub_rn(Akx, __fmul_rn(r.Sx, Akz));
+    float Ay = __fsub_rn(Aky, __fmul_rn(r.Sy, Akz));
+    float Bx = __fsub_rn(Bkx, __fmul_rn(r.Sx, Bkz));
+    float By = __fsub_rn(Bky, __fmul_rn(r.Sy, Bkz));
+    float Cx = __fsub_rn(Ckx, __fmul_rn(r.Sx, Ckz));
+    float Cy = __fsub_rn(Cky, __fmul_rn(r.Sy, Ckz));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        double CxBy = (double)Cx * (double)By, CyBx = (double)Cy * (double)Bx;
+        U = (float)(CxBy - CyBx);
+        double AxCy = (double)Ax * (double)Cy, AyCx = (double)Ay * (double)Cx;
+        V = (float)(AxCy - AyCx);
+        double BxAy = (double)Bx * (double)Ay, ByAx = (double)By * (double)Ax;
+        W = (float)(BxAy - ByAx);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    float Az = __fmul_rn(r.Sz, Akz), Bz = __fmul_rn(r.Sz, Bkz), Cz = __fmul_rn(r.Sz, Ckz);
+    float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    // conservative rejections before the division (exact sign logic, padded bound)
+    float Ts = det < 0.0f ? -T : T;
+    float adet = fabsf(det);
+    if (Ts <= 0.0f && r.tmin >= 0.0f) return false;
+    if (Ts > adet * tbest * BSM_BOX_PAD) return false;
+    float rcp = __fdiv_rn(1.0f, det);
+    float t = __fmul_rn(T, rcp);
+    if (!(t > r.tmin)) return false;
+    if (!(t < tbest || (t == tbest && prim < best_prim))) return false;
+    t_out = t;
+    u_out = __fmul_rn(U, rcp);
+    v_out = __fmul_rn(V, rcp);
+    return true;
+}
+
+// Byte k of w as a float: PRMT builds 2^23 + byte, the FADD removes 2^23 exactly.
+__device__ __forceinline__ float qbyte(uint32_t w, uint32_t k) {
+    return __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7440u | k)) - 8388608.0f;
+}
+
+// Intersects the eight children of node `ni`; returns the group of internal
+// children hit (base index, hit bits 24..31 in octant order | imask) and the
+// group of triangles hit (base index, bits 0..23).
+__device__ __forceinline__ void node_test(const RayPre& r, const CwNode* __restrict__ nodes, uint32_t ni, float tbest,
+                                          uint2& G, uint2& T) {
+    const uint4* p = reinterpret_cast<const uint4*>(nodes + ni);
+    uint4 n0 = __ldg(p + 0), n1 = __ldg(p + 1), n2 = __ldg(p + 2), n3 = __ldg(p + 3), n4 = __ldg(p + 4);
+    uint32_t ew = n0.w;
+    // slab distance of plane q: q * s + a (near planes) and (q * s + a) * pad (far planes)
+    float sx = __uint_as_float((ew & 0xffu) << 23) * r.idx;
+    float sy = __uint_as_float(((ew >> 8) & 0xffu) << 23) * r.idy;
+    float sz = __uint_as_float(((ew >> 16) & 0xffu) << 23) * r.idz;
+    float ax = (__uint_as_float(n0.x) - r.ox) * r.idx;
+    float ay = (__uint_as_float(n0.y) - r.oy) * r.idy;
+    float az = (__uint_as_float(n0.z) - r.oz) * r.idz;
+    float sxf = sx * BSM_BOX_PAD, syf = sy * BSM_BOX_PAD, szf = sz * BSM_BOX_PAD;
+    float axf = ax * BSM_BOX_PAD, ayf = ay * BSM_BOX_PAD, azf = az * BSM_BOX_PAD;
+    uint32_t imask = ew >> 24;
+    bool nx = r.idx < 0.0f, ny = r.idy < 0.0f, nz = r.idz < 0.0f;
+    uint32_t nlx0 = nx ? n3.z : n2.x, nlx1 = nx ? n3.w : n2.y;
+    uint32_t nfx0 = nx ? n2.x : n3.z, nfx1 = nx ? n2.y : n3.w;
+    uint32_t nly0 = ny ? n4.x : n2.z, nly1 = ny ? n4.y : n2.w;
+    uint32_t nfy0 = ny ? n2.z : n4.x, nfy1 = ny ? n2.w : n4.y;
+    uint32_t nlz0 = nz ? n4.z : n3.x, nlz1 = nz ? n4.w : n3.y;
+    uint32_t nfz0 = nz ? n3.x : n4.z, nfz1 = nz ? n3.y : n4.w;
+    // meta decode, four children per word: inner children have bits 4 and 3 set
+    uint32_t oct4 = r.oct_key * 0x01010101u;
+    uint32_t m0 = n1.z, m1 = n1.w;
+    uint32_t in0 = ((m0 & (m0 << 1)) & 0x10101010u) >> 4, in1 = ((m1 & (m1 << 1)) & 0x10101010u) >> 4;
+    uint32_t bi0 = (m0 ^ (oct4 & (in0 * 0xffu))) & 0x1f1f1f1fu;
+    uint32_t bi1 = (m1 ^ (oct4 & (in1 * 0xffu))) & 0x1f1f1f1fu;
+    uint32_t cb0 = (m0 >> 5) & 0x07070707u, cb1 = (m1 >> 5) & 0x07070707u;
+    uint32_t hits = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const uint32_t k = (uint32_t)(c & 3);
+        const bool lo = c < 4;
+        float tnx = __fmaf_rn(qbyte(lo ? nlx0 : nlx1, k), sx, ax);
+        float tny = __fmaf_rn(qbyte(lo ? nly0 : nly1, k), sy, ay);
+        float tnz = __fmaf_rn(qbyte(lo ? nlz0 : nlz1, k), sz, az);
+        float tfx = __fmaf_rn(qbyte(lo ? nfx0 : nfx1, k), sxf, axf);
+        float tfy = __fmaf_rn(qbyte(lo ? nfy0 : nfy1, k), syf, ayf);
+        float tfz = __fmaf_rn(qbyte(lo ? nfz0 : nfz1, k), szf, azf);
+        float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
+        float tf = min3f(tfx, tfy, fminf(tfz, tbest));
+        if (tn <= tf) {
+            uint32_t bits = ((lo ? cb0 : cb1) >> (8 * k)) & 0xffu;
+            uint32_t pos = ((lo ? bi0 : bi1) >> (8 * k)) & 0xffu;
+            hits |= bits << pos;
+        }
+    }
+    G = make_uint2(n1.x, (hits & 0xff000000u) | imask);
+    T = make_uint2(n1.y, hits & 0x00ffffffu);
+}
+
+struct TraceCounters { uint32_t nodes, tris; };
+
+// Single-ray closest / any hit (used by the stage entry points).  Returns the
+// leaf-ordered triangle index (kMissPrim on a miss); t = tmax on a miss.
+template <bool kAnyHit, bool kCount>
+__device__ __forceinline__ uint32_t trace_ray(const RayPre& r, float tmax, const CwNode* __restrict__ nodes,
+                                              const CwTri* __restrict__ tris, float& t_out, float& u_out,
+                                              float& v_out, TraceCounters* cnt) {
+    float tbest = tmax;
+    uint32_t best_leaf = kMissPrim, best_prim = kMissPrim;
+    float bu = 0.0f, bv = 0.0f;
+    uint2 stack[kStackSize];
+    int sp = 0;
+    uint32_t root_slot = 7u ^ r.oct_key;
+    bool zero = r.dx == 0.0f && r.dy == 0.0f && r.dz == 0.0f;  // skipped as a miss (rt_gbuffer.hlsl:13-15)
+    uint2 G = make_uint2(0u, zero ? 0u : (0x80000000u | (1u << root_slot)));
+    uint2 T = make_uint2(0u, 0u);
+    while (true) {
+        while (T.y != 0u) {
+            int bit = __ffs(T.y) - 1;
+            T.y &= T.y - 1u;
+            uint32_t ti = T.x + (uint32_t)bit;
+            const float4* tp = reinterpret_cast<const float4*>(tris + ti);
+            float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            uint32_t prim = __float_as_uint(a.w);
+            if (kCount) cnt->tris++;
+            float t, u, v;
+            if (tri_test(r, a, b, c, tbest, prim, best_prim, t, u, v)) {
+                if (kAnyHit) { t_out = t; u_out = u; v_out = v; return ti; }
+                tbest = t; best_leaf = ti; best_prim = prim; bu = u; bv = v;
+            }
+        }
+        if ((G.y & 0xff000000u) == 0u) {
+            if (sp == 0) break;
+            G = stack[--sp];
+        }
+        uint32_t bit = 31u - (uint32_t)__clz(G.y & 0xff000000u);
+        G.y &= ~(1u << bit);
+        uint32_t slot = (bit - 24u) ^ r.oct_key;
+        uint32_t ni = G.x + (uint32_t)__popc(G.y & 0xffu & ((1u << slot) - 1u));
+        if ((G.y & 0xff000000u) != 0u) stack[sp++] = G;
+        if (kCount) cnt->nodes++;
+        node_test(r, nodes, ni, tbest, G, T);
+    }
+    t_out = tbest;
+    u_out = bu;
+    v_out = bv;
+    return best_leaf;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Persistent, warp-synchronous traversal of a queue of n rays.  Every lane of
+// the warp runs this loop together (all ballots use the full mask).  `load`
+// (index -> (origin/tmin, direction/tmax)) supplies rays; `finish(index, leaf,
+// t, u, v)` receives each result (leaf = kMissPrim on a miss; for any-hit the
+// first hit found).
+template <bool kAnyHit, bool kCount, class Load, class Finish>
+__device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, const CwTri* __restrict__ tris,
+                                            uint32_t n, uint32_t* work, Load load, Finish finish,
+                                            TraceCounters* cnt) {
+    const uint32_t lane = threadIdx.x & 31u;
+    bool has = false;
+    bool exhausted = false;  // warp-uniform
+    RayPre r;
+    float tbest = 0.0f, bu = 0.0f, bv = 0.0f;
+    uint32_t best_leaf = kMissPrim, best_prim = kMissPrim, idx = 0;
+    uint2 G = make_uint2(0, 0), T = make_uint2(0, 0);
+    uint2 stack[kStackSize];
+    int sp = 0;
+    while (true) {
+        // refill lanes whose ray finished (one atomic per warp)
+        uint32_t idle = __ballot_sync(0xffffffffu, !has);
+        if (!exhausted && (__popc(idle) >= 8 || idle == 0xffffffffu)) {
+            uint32_t cntn = (uint32_t)__popc(idle);
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(work, cntn);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (!has) {
+                uint32_t i = base + (uint32_t)__popc(idle & lanemask_lt());
+                if (i < n) {
+                    float4 o, d;
+                    load(i, o, d);
+                    r = make_ray(o, d);
+                    tbest = d.w;
+                    best_leaf = kMissPrim; best_prim = kMissPrim; bu = 0.0f; bv = 0.0f;
+                    // a zero direction is skipped as a miss (rt_gbuffer.hlsl:13-15)
+                    bool zero = d.x == 0.0f && d.y == 0.0f && d.z == 0.0f;
+                    G = make_uint2(0u, zero ? 0u : (0x80000000u | (1u << (7u ^ r.oct_key))));
+                    T = make_uint2(0u, 0u);
+                    sp = 0;
+                    idx = i;
+                    has = true;
+                }
+            }
+            if (base + cntn >= n) exhausted = true;
+        }
+        if (__ballot_sync(0xffffffffu, has) == 0u) break;
+        // node step
+        if (has) {
+            if ((G.y & 0xff000000u) != 0u) {
+                uint32_t bit = 31u - (uint32_t)__clz(G.y & 0xff000000u);
+                G.y &= ~(1u << bit);
+                uint32_t slot = (bit - 24u) ^ r.oct_key;
+                uint32_t ni = G.x + (uint32_t)__popc(G.y & 0xffu & ((1u << slot) - 1u));
+                if ((G.y & 0xff000000u) != 0u) stack[sp++] = G;
+                if (kCount) cnt->nodes++;
+                node_test(r, nodes, ni, tbest, G, T);
+            } else {
+                T = G;  // a postponed triangle group popped from the stack
+                G = make_uint2(0u, 0u);
+            }
+        }
+        // triangle steps, postponed while fewer than 1/4 of the active lanes have triangles
+        while (true) {
+            bool want = has && T.y != 0u;
+            uint32_t m = __ballot_sync(0xffffffffu, want);
+            if (m == 0u) break;
+            uint32_t act = __ballot_sync(0xffffffffu, has);
+            if (__popc(m) * 4 < __popc(act)) {
+                if (want && sp < kPostponeMaxSp) { stack[sp++] = T; T.y = 0u; }
+                if (__ballot_sync(0xffffffffu, has && T.y != 0u) == 0u) break;
+                want = has && T.y != 0u;
+            }
+            if (want) {
+                int bit = __ffs(T.y) - 1;
+                T.y &= T.y - 1u;
+                uint32_t ti = T.x + (uint32_t)bit;
+                const float4* tp = reinterpret_cast<const float4*>(tris + ti);
+                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                uint32_t prim = __float_as_uint(a.w);
+                if (kCount) cnt->tris++;
+                float t, u, v;
+                if (tri_test(r, a, b, c, tbest, prim, best_prim, t, u, v)) {
+                    tbest = t; best_leaf = ti; best_prim = prim; bu = u; bv = v;
+                    if (kAnyHit) { T.y = 0u; G.y = 0u; sp = 0; }
+                }
+            }
+        }
+        // next group, or done
+        if (has && (G.y & 0xff000000u) == 0u && T.y == 0u) {
+            if (sp > 0 && !(kAnyHit && best_leaf != kMissPrim)) {
+                G = stack[--sp];
+            } else {
+                finish(idx, best_leaf, tbest, bu, bv);
+                has = false;
+            }
+        }
+    }
+}
+
+}  // namespace bsm

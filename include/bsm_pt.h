@@ -1,0 +1,286 @@
+/*
+ * bsm_pt.h — C ABI of the GB300 wavefront path-tracing pass.
+ *
+ * This library is a drop-in for the path-tracing pass of the bisemutum builtin
+ * renderer.  The pass keeps the reference's contract: camera, scene (meshes,
+ * materials, directional lights, skybox), spp and bounce settings in, an HDR
+ * accumulation buffer out.  Everything behind these entry points runs as
+ * hand-written sm_103a CUDA kernels on one GPU.
+ *
+ * Reference interfaces replaced (paths relative to the bisemutum-engine repo):
+ *   - PathTracingPass::update_params / ::render
+ *       bisemutum/src/renderer/pass/path_tracing.hpp:27-35
+ *       bisemutum/src/renderer/pass/path_tracing.cpp:183-222, 224-490
+ *   - BasicRenderer::PathTracingSettings
+ *       bisemutum/include/bisemutum/renderer/basic.hpp:76-81
+ *   - acceleration structure build (driver BLAS/TLAS)
+ *       bisemutum/src/graphics/accel.cpp:11-159
+ *   - TraceRay closest hit / any hit
+ *       bisemutum/shaders/renderer/raytracing/rt_gbuffer.hlsl:7-36
+ *       bisemutum/shaders/renderer/raytracing/hits/rt_gbuffer_hit.hlsl:6-35
+ *   - scene inputs: DirLightData (bisemutum/src/renderer/context/lights.hpp:12-22),
+ *     skybox colour/texture (bisemutum/src/renderer/context/skybox.cpp),
+ *     camera matrices (bisemutum/src/graphics/camera.cpp:73-118).
+ *
+ * Conventions
+ *   - Every call returns a bsm_status; 0 is success, negative values are errors.
+ *     bsm_last_error(ctx) returns a message for the last failing call on ctx.
+ *   - Plain pointers and sizes only.  A `location` argument says whether a
+ *     buffer lives in host memory (BSM_HOST) or device memory (BSM_DEVICE).
+ *   - One context per host thread.  Calls on one context are serialised by the
+ *     caller; the serving entry points (bsm_server_*) take an internal lock.
+ *   - Scene data passed to bsm_scene_upload is copied; the caller may free its
+ *     buffers when the call returns.
+ */
+#ifndef BSM_PT_H
+#define BSM_PT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BSM_API_VERSION 1
+
+#if defined(_WIN32)
+#define BSM_API __declspec(dllexport)
+#else
+#define BSM_API __attribute__((visibility("default")))
+#endif
+
+typedef int32_t bsm_status;
+enum {
+    BSM_OK = 0,
+    BSM_ERR_INVALID_ARG = -1,
+    BSM_ERR_OUT_OF_MEMORY = -2,
+    BSM_ERR_CUDA = -3,
+    BSM_ERR_TIMEOUT = -4,
+    BSM_ERR_NOT_FOUND = -5,
+    BSM_ERR_BAD_STATE = -6,
+    BSM_ERR_NO_DEVICE = -7,
+    BSM_ERR_UNSUPPORTED = -8,
+    BSM_ERR_DEVICE_CHECK = -9,   /* a kernel's own bounds/overflow check fired */
+    BSM_ERR_ADMISSION = -10      /* serving: request does not fit the memory budget */
+};
+
+enum { BSM_HOST = 0, BSM_DEVICE = 1 };
+
+typedef struct bsm_context bsm_context;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Creates a context on CUDA device `device_ordinal`.  `mem_budget_bytes`
+ * bounds the device memory the context may hold (0 = 90% of free memory).
+ * Replaces the graphics-device setup the reference does in
+ * GraphicsManager::initialize (bisemutum/src/graphics/graphics_manager.cpp). */
+BSM_API bsm_status bsm_create(bsm_context** ctx, int device_ordinal, uint64_t mem_budget_bytes);
+BSM_API void bsm_destroy(bsm_context* ctx);
+BSM_API const char* bsm_last_error(const bsm_context* ctx);
+BSM_API int bsm_api_version(void);
+/* Waits for all work on the context's streams; BSM_ERR_TIMEOUT after timeout_ms. */
+BSM_API bsm_status bsm_sync(bsm_context* ctx, uint32_t timeout_ms);
+
+/* Device memory helpers for callers without their own allocator. */
+BSM_API bsm_status bsm_device_alloc(bsm_context* ctx, uint64_t bytes, void** ptr);
+BSM_API bsm_status bsm_device_free(bsm_context* ctx, void* ptr);
+/* kind: 0 host->device, 1 device->host, 2 device->device (synchronous). */
+BSM_API bsm_status bsm_memcpy(bsm_context* ctx, void* dst, const void* src, uint64_t bytes, int kind);
+
+/* ---- scene description (DirLightData, skybox, GPU scene buffers) ------ */
+
+typedef struct bsm_material {
+    float base_color[3];   /* SurfaceData::base_color (utils.hlsl:5-16) */
+    float roughness;       /* perceptual roughness, alpha = max(r^2, 1e-3) */
+    float metallic;        /* f0 = lerp(0.04, base_color, metallic) (import_model.cpp:217-219) */
+    float emission[3];     /* kept for the descriptor; the reference PT drops it (gbuffer.hlsl) */
+} bsm_material;
+
+typedef struct bsm_dir_light {
+    float direction[3];    /* unit vector pointing TO the light (lights.cpp:59-65) */
+    float emission[3];     /* colour * strength; the radiance term of dir_light_eval (lights.hlsl:10-13) */
+} bsm_dir_light;
+
+enum { BSM_SKY_CONSTANT = 0, BSM_SKY_EQUIRECT = 1 };
+typedef struct bsm_sky {
+    uint32_t kind;          /* BSM_SKY_CONSTANT or BSM_SKY_EQUIRECT */
+    float color[3];         /* constant radiance, or a multiplier of the map (skybox_color) */
+    uint32_t width, height; /* equirect size; row 0 looks at +y, column 0 at azimuth -pi */
+    const uint16_t* rgba16f;/* width*height RGBA IEEE half texels (host) */
+} bsm_sky;
+
+typedef struct bsm_scene_desc {
+    uint32_t num_vertices;
+    const float* positions;       /* 3 * num_vertices */
+    uint32_t num_triangles;
+    const uint32_t* indices;      /* 3 * num_triangles, or NULL for a triangle soup */
+    const uint32_t* material_ids; /* num_triangles, or NULL (all material 0) */
+    uint32_t num_materials;
+    const bsm_material* materials;
+    uint32_t num_dir_lights;
+    const bsm_dir_light* dir_lights;
+    bsm_sky sky;
+} bsm_scene_desc;
+
+typedef struct bsm_bvh_opts {
+    uint32_t sah_bins;        /* 0 = 32 */
+    uint32_t max_leaf_tris;   /* 1..3, 0 = 3 */
+    uint32_t num_threads;     /* 0 = hardware concurrency */
+} bsm_bvh_opts;
+
+typedef struct bsm_bvh_stats {
+    uint32_t num_nodes;       /* 8-wide compressed nodes (80 B each) */
+    uint32_t num_tris;
+    uint32_t max_depth;
+    uint32_t reserved;
+    double build_ms;          /* host build time */
+    double sah_cost;          /* SAH cost of the binary BVH before collapsing */
+    uint64_t node_bytes;
+    uint64_t tri_bytes;
+} bsm_bvh_stats;
+
+/* Copies a scene to the device.  Replaces the GPU-scene upload the reference
+ * does in GpuSceneSystem (bisemutum/src/graphics/gpu_scene_system.cpp). */
+BSM_API bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* desc, uint32_t* scene_id);
+/* SAH-binned build of the compressed 8-wide BVH; replaces the driver BLAS/TLAS
+ * build of AccelerationStructure (bisemutum/src/graphics/accel.cpp:11-159). */
+BSM_API bsm_status bsm_scene_build_bvh(bsm_context* ctx, uint32_t scene_id, const bsm_bvh_opts* opts,
+                                       bsm_bvh_stats* stats);
+BSM_API bsm_status bsm_scene_release(bsm_context* ctx, uint32_t scene_id);
+/* Host-only build of the same BVH into caller buffers (no device needed).
+ * Call with nodes == tris == NULL to get the sizes in `stats`, then again
+ * with buffers of stats->node_bytes and stats->tri_bytes. */
+BSM_API bsm_status bsm_bvh_build_host(const bsm_scene_desc* desc, const bsm_bvh_opts* opts, void* nodes,
+                                      uint64_t nodes_bytes, void* tris, uint64_t tris_bytes,
+                                      bsm_bvh_stats* stats);
+/* Device bytes held by one scene (BVH + triangles + materials + sky). */
+BSM_API bsm_status bsm_scene_device_bytes(bsm_context* ctx, uint32_t scene_id, uint64_t* bytes);
+/* Copies the built BVH back to the host (node_bytes / tri_bytes as in the stats).
+ * Either pointer may be NULL.  Used by tests that check the BVH invariants. */
+BSM_API bsm_status bsm_scene_download_bvh(bsm_context* ctx, uint32_t scene_id, void* nodes, void* tris);
+
+/* ---- camera and settings (Camera, PathTracingSettings) ----------------- */
+
+typedef struct bsm_camera {
+    float position[3];
+    float front[3];          /* view direction (lookAt(position, position + front, up)) */
+    float up[3];
+    float yfov_deg;          /* vertical field of view (camera.cpp:96-98) */
+    uint32_t width, height;
+} bsm_camera;
+
+enum {
+    BSM_PT_JITTER = 1u << 0,        /* jitter primary rays inside the pixel (reference: centre) */
+    BSM_PT_NO_SUN_NEE = 1u << 1,
+    BSM_PT_NO_SKY_NEE = 1u << 2,    /* sky only through BSDF-sampled escapes */
+    BSM_PT_STAGE_TIMING = 1u << 3,  /* record per-stage CUDA events into bsm_render_stats */
+    BSM_PT_NO_GRAPH = 1u << 4,      /* launch stages directly instead of replaying a CUDA graph */
+    BSM_PT_COUNT_TRAVERSAL = 1u << 5 /* count BVH nodes visited / triangles tested by the extend stage */
+};
+
+typedef struct bsm_pt_settings {
+    float ray_length;          /* PathTracingSettings::ray_length, default 100 (basic.hpp:77) */
+    uint32_t max_bounces;      /* PathTracingSettings::max_bounces (>=2); segments = max_bounces - 1 */
+    uint32_t accumulate;       /* PathTracingSettings::accumulate: add to the view's history */
+    uint32_t denoise;          /* PathTracingSettings::denoise: accepted and ignored, as in the reference PT */
+    uint32_t spp;              /* samples per pixel in this call */
+    uint32_t max_segments;     /* extend stages including the primary ray; 0 = max_bounces - 1 */
+    uint64_t seed;             /* scene seed for the PCG32 per-pixel streams */
+    uint32_t sample_offset;    /* index of the first sample (progressive rendering) */
+    uint32_t flags;            /* BSM_PT_* */
+    float t_min;               /* ray TMin; 0 = default 0 (origins are offset instead) */
+    float ray_offset;          /* origin offset along the geometric normal; 0 = 2e-5 * scene extent */
+    uint32_t wavefront_capacity; /* paths in flight per chunk; 0 = automatic */
+    uint32_t block_size;       /* threads per block of the traversal kernels; 0 = tuned default */
+} bsm_pt_settings;
+
+/* Fills `s` with the reference defaults plus spp = 1, seed = 1. */
+BSM_API void bsm_pt_settings_default(bsm_pt_settings* s);
+
+typedef struct bsm_view_output {
+    float* rgba;             /* width*height RGBA fp32 (mean radiance), row pitch below */
+    uint32_t row_pitch_px;   /* 0 = width */
+    uint32_t location;       /* BSM_HOST or BSM_DEVICE */
+} bsm_view_output;
+
+#define BSM_MAX_SEGMENTS 16
+typedef struct bsm_render_stats {
+    uint64_t paths;
+    uint64_t extend_rays;                 /* rays that entered the closest-hit kernel */
+    uint64_t shadow_rays;                 /* rays that entered the any-hit kernel */
+    uint64_t rays_per_segment[BSM_MAX_SEGMENTS];
+    uint32_t chunks;
+    uint32_t extend_launches;
+    float ms_total;                       /* device time of the whole render (events) */
+    float ms_camera, ms_extend, ms_shade, ms_shadow, ms_resolve; /* BSM_PT_STAGE_TIMING only */
+    uint64_t traversal_nodes;             /* BSM_PT_COUNT_TRAVERSAL only: nodes visited by extend rays */
+    uint64_t traversal_tris;              /* BSM_PT_COUNT_TRAVERSAL only: triangles tested by extend rays */
+} bsm_render_stats;
+
+/* Renders `n_views` views of one scene (PathTracingPass::render for each
+ * camera).  With settings->accumulate the samples are added to the view's
+ * history (kept per view index, reset when the camera or size changes, as
+ * path_tracing.cpp:224-245 does); outputs receive the running mean.
+ * `outputs` may be NULL to keep the result on the device (bsm_read_view).
+ * `stats` may be NULL. */
+BSM_API bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_camera* views, uint32_t n_views,
+                              const bsm_pt_settings* settings, const bsm_view_output* outputs,
+                              bsm_render_stats* stats);
+/* Reads the current mean of a view's history into `out`. */
+BSM_API bsm_status bsm_read_view(bsm_context* ctx, uint32_t view_index, const bsm_view_output* out);
+/* Exports / imports a view's raw history (sum RGB + sample count) so a render
+ * can resume to more samples.  `sums` holds width*height*4 floats. */
+BSM_API bsm_status bsm_export_history(bsm_context* ctx, uint32_t view_index, float* sums, uint32_t* spp,
+                                      uint32_t location);
+BSM_API bsm_status bsm_import_history(bsm_context* ctx, uint32_t view_index, const bsm_camera* camera,
+                                      const float* sums, uint32_t spp, uint32_t location);
+
+/* ---- stage entry points (TraceRay closest hit / any hit) --------------- */
+
+/* rays: n * 8 floats (ox, oy, oz, tmin, dx, dy, dz, tmax).
+ * hits: n * 4 words (t as f32, primitive id as u32, u, v as f32); a miss has
+ * primitive id 0xffffffff and t = tmax.  Replaces TraceRay in rt_gbuffer_rgen
+ * with the closest-hit shader (rt_gbuffer.hlsl:7-36, rt_gbuffer_hit.hlsl:6-18). */
+BSM_API bsm_status bsm_trace_closest(bsm_context* ctx, uint32_t scene_id, const float* rays, uint32_t n,
+                                     void* hits, uint32_t location);
+/* occluded: n bytes, 1 if any triangle lies in (tmin, tmax].  Replaces the
+ * any-hit path (rt_gbuffer_hit.hlsl:20-35) for opaque geometry. */
+BSM_API bsm_status bsm_trace_any(bsm_context* ctx, uint32_t scene_id, const float* rays, uint32_t n,
+                                 uint8_t* occluded, uint32_t location);
+
+/* Per-ray traversal counters: counts[2*i] = BVH nodes visited, counts[2*i+1] =
+ * triangles tested, for the closest-hit traversal of ray i (host buffers).
+ * No reference counterpart: it measures the traversal working set. */
+BSM_API bsm_status bsm_trace_counts(bsm_context* ctx, uint32_t scene_id, const float* rays, uint32_t n,
+                                    uint32_t* counts);
+
+/* Page-locked host memory for fast host<->device copies (cudaHostAlloc). */
+BSM_API bsm_status bsm_host_alloc(bsm_context* ctx, uint64_t bytes, void** ptr);
+BSM_API bsm_status bsm_host_free(bsm_context* ctx, void* ptr);
+
+/* ---- synthetic scenes --------------------------------------------------- */
+
+enum {
+    BSM_SCENE_ROOM = 0,     /* 12 quads + 64 icospheres, constant sky (20,504 triangles) */
+    BSM_SCENE_TERRAIN = 1   /* fBm heightfield + UV spheres, baked gradient sky */
+};
+typedef struct bsm_scene_gen_params {
+    uint32_t kind;           /* BSM_SCENE_* */
+    uint64_t seed;
+    uint32_t grid;           /* terrain vertices per side (512 for 1,482,242 triangles) */
+    uint32_t spheres;        /* terrain: UV spheres (2000); room: icospheres (64) */
+    uint32_t sky_width, sky_height; /* terrain sky map (1024 x 512) */
+} bsm_scene_gen_params;
+
+/* Generates a procedural scene.  The arrays in `desc` belong to the library
+ * until bsm_scene_gen_free(desc).  `camera` receives the scene's fixed camera
+ * (width/height left as passed in). */
+BSM_API bsm_status bsm_scene_generate(const bsm_scene_gen_params* params, bsm_scene_desc* desc,
+                                      bsm_camera* camera);
+BSM_API void bsm_scene_gen_free(bsm_scene_desc* desc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BSM_PT_H */

@@ -1,0 +1,165 @@
+"""CPU ORACLE of the wavefront path-tracing pass — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg load
+this package.  It wraps ``oracle/_build/liboracle.so`` (pt_oracle.cpp, a
+multithreaded C++ restatement of the pass; each function there cites the
+reference shader it follows) and, where the reference tree was present at
+build time, ``oracle/_ref/libref_bsdf.so`` (the reference's own HLSL material
+math compiled through a C++ shim; used only to generate golden vectors).
+
+Parity pins: BSDF / frame / sampler formulas against golden vectors produced
+from the reference's shader sources (tests/golden/bsdf_golden.npz); PCG32
+against the published pcg32 demo output.  Traversal and BVH: the reference's
+are inside the graphics driver, so closest-hit parity is pinned to this
+restatement of the published watertight test only.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+_ref = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        from . import build as _b
+        path = _b.build_oracle()
+        L = C.CDLL(path)
+        vp, u32, u64, f32, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_int
+        L.orc_scene_create.argtypes = [vp, u32, vp, u32, vp, vp, u32, vp, u32, u32, vp, u32, u32, vp,
+                                       C.POINTER(vp)]
+        L.orc_scene_create.restype = i32
+        L.orc_scene_destroy.argtypes = [vp]
+        L.orc_trace.argtypes = [vp, vp, u32, vp, i32, i32, vp]
+        L.orc_trace.restype = i32
+        L.orc_render.argtypes = [vp, vp, u32, u32, u32, u32, u64, f32, f32, u32, u32, vp, vp, i32,
+                                 C.POINTER(C.c_double)]
+        L.orc_render.restype = i32
+        L.orc_pcg32.argtypes = [u64, u64, u32, vp]
+        L.orc_sincos_turns.argtypes = [vp, u32, vp, vp]
+        L.orc_atan2.argtypes = [vp, vp, u32, vp]
+        L.orc_eval_lit.argtypes = [vp, u32, vp]
+        L.orc_vndf.argtypes = [vp, u32, vp]
+        L.orc_frame.argtypes = [vp, u32, vp]
+        L.orc_scene_bvh_nodes.argtypes = [vp]
+        L.orc_scene_bvh_nodes.restype = u32
+        _lib = L
+    return _lib
+
+
+def ref_lib() -> C.CDLL | None:
+    """The reference's shader math compiled from its sources, or None where the reference tree is absent."""
+    global _ref
+    if _ref is None:
+        from . import build as _b
+        path = _b.build_reference()
+        if path is None:
+            return None
+        R = C.CDLL(path)
+        for fn in ("ref_eval_lit", "ref_vndf", "ref_frame", "ref_aniso", "ref_samplers"):
+            getattr(R, fn).argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+        R.ref_inv_pi.restype = C.c_float
+        _ref = R
+    return _ref
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+class OracleScene:
+    """A scene inside the oracle (own binary SAH BVH)."""
+
+    def __init__(self, scene):
+        L = lib()
+        self._L = L
+        pos = _f32(scene.positions)
+        idx = None if scene.indices is None else np.ascontiguousarray(scene.indices, np.uint32)
+        mids = np.ascontiguousarray(scene.material_ids, np.uint32)
+        mats = _f32(scene.materials)
+        lights = _f32(scene.lights).reshape(-1, 6)
+        color = _f32(scene.sky_color)
+        tex = None if scene.sky_texels is None else np.ascontiguousarray(scene.sky_texels, np.uint16)
+        h = C.c_void_p()
+        st = L.orc_scene_create(pos.ctypes.data, pos.shape[0], None if idx is None else idx.ctypes.data,
+                                mids.shape[0], mids.ctypes.data, mats.ctypes.data, mats.shape[0],
+                                lights.ctypes.data, lights.shape[0], scene.sky_kind, color.ctypes.data,
+                                0 if tex is None else tex.shape[1], 0 if tex is None else tex.shape[0],
+                                None if tex is None else tex.ctypes.data, C.byref(h))
+        if st != 0:
+            raise RuntimeError("orc_scene_create failed")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.orc_scene_destroy(self.h)
+            self.h = None
+
+    def trace(self, rays: np.ndarray, any_hit: bool = False, threads: int = 0, counts: bool = False):
+        rays = _f32(rays).reshape(-1, 8)
+        hits = np.zeros((rays.shape[0], 4), np.uint32)
+        cnt = np.zeros((rays.shape[0], 2), np.uint32) if counts else None
+        self._L.orc_trace(self.h, rays.ctypes.data, rays.shape[0], hits.ctypes.data, 1 if any_hit else 0, threads,
+                          None if cnt is None else cnt.ctypes.data)
+        return (hits, cnt) if counts else hits
+
+    def render(self, camera: np.ndarray, spp: int, max_segments: int, seed: int = 1, flags: int = 0,
+               ray_length: float = 100.0, t_min: float = 0.0, sample_offset: int = 0, rows=None, threads: int = 0):
+        """Returns (mean RGBA image of the rows, stats[32], seconds)."""
+        cam = _f32(camera)
+        w, h = int(cam[10]), int(cam[11])
+        r0, r1 = rows if rows is not None else (0, h)
+        out = np.zeros((r1 - r0, w, 4), np.float32)
+        stats = np.zeros(32, np.uint64)
+        sec = C.c_double()
+        st = self._L.orc_render(self.h, cam.ctypes.data, spp, max_segments, sample_offset, flags, seed, ray_length,
+                                t_min, r0, r1, out.ctypes.data, stats.ctypes.data, threads, C.byref(sec))
+        if st != 0:
+            raise RuntimeError("orc_render failed")
+        return out, stats, sec.value
+
+
+def pcg32(initstate: int, initseq: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.uint32)
+    lib().orc_pcg32(initstate, initseq, n, out.ctypes.data)
+    return out
+
+
+def sincos_turns(t):
+    t = _f32(t)
+    s = np.zeros_like(t)
+    c = np.zeros_like(t)
+    lib().orc_sincos_turns(t.ctypes.data, t.size, s.ctypes.data, c.ctypes.data)
+    return s, c
+
+
+def atan2(y, x):
+    y, x = _f32(y), _f32(x)
+    o = np.zeros_like(y)
+    lib().orc_atan2(y.ctypes.data, x.ctypes.data, y.size, o.ctypes.data)
+    return o
+
+
+def _batch(fn, a, cols_in, cols_out):
+    a = _f32(a).reshape(-1, cols_in)
+    o = np.zeros((a.shape[0], cols_out), np.float32)
+    fn(a.ctypes.data, a.shape[0], o.ctypes.data)
+    return o
+
+
+def eval_lit(a):
+    return _batch(lib().orc_eval_lit, a, 16, 3)
+
+
+def vndf(a):
+    return _batch(lib().orc_vndf, a, 7, 4)
+
+
+def frame(a):
+    return _batch(lib().orc_frame, a, 3, 6)

@@ -1,0 +1,905 @@
+// pt_oracle.cpp — CPU ORACLE of the wavefront path-tracing pass.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA pass and
+// the timed CPU baseline; the product library never links or calls it.
+//
+// It restates, in plain multithreaded C++, the stages of the bisemutum
+// builtin renderer's path-tracing pass (paths relative to the reference repo):
+//   camera rays      bisemutum/shaders/renderer/raytracing/direction_sample/generate_camera_ray.hlsl:9-15
+//                    with the reverse-Z projection of bisemutum/src/math/math.cpp:5-11 and
+//                    lookAt/perspective of bisemutum/src/graphics/camera.cpp:96-98
+//   closest / any hit rt_gbuffer.hlsl:17-35 (TraceRay, TMin, TMax = ray_length)
+//   lighting         deferred_lighting_secondary.hlsl:23-29 (sky on a miss), :51-60
+//                    (directional light x visibility x surface_eval), lights.hlsl:10-13
+//   BSDF             bisemutum/shaders/core/material/utils.hlsl:40-121, lit.hlsl:5-35
+//   frame            bisemutum/shaders/core/utils/frame.hlsl:9-18
+//   samplers         bisemutum/shaders/core/utils/sampling.hlsl:13-31
+//   next direction   sample_secondary_ray.hlsl:16-28 (termination), :51-64 (weight, NaN guard)
+//   accumulation     pt_accumulate.hlsl:3-11 (running mean = sum / samples)
+// and the decisions the CUDA pass takes where the reference has none (PCG32
+// streams keyed to pixel and sample, next-event estimation towards the sun
+// and the importance-sampled sky with MIS, lobe-mixture sampling).  It keeps
+// its own binary SAH BVH: the closest hit does not depend on the tree, and
+// agreement with the GPU's compressed 8-wide BVH is itself part of the check.
+// Arithmetic is IEEE single precision in the same order as the CUDA kernels
+// (built with -ffp-contract=off), so primitive ids, t values and path
+// decisions agree bit for bit.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#define ORC_API extern "C" __attribute__((visibility("default")))
+
+namespace orc {
+
+// ------------------------------------------------------------- vectors ----
+struct F3 { float x, y, z; };
+static inline F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+static inline F3 add(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline F3 sub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline F3 neg(F3 a) { return f3(-a.x, -a.y, -a.z); }
+static inline F3 mul(F3 a, F3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline F3 muls(F3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+static inline F3 smul(float s, F3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+static inline F3 divs(F3 a, float s) { return f3(a.x / s, a.y / s, a.z / s); }
+static inline float dot3(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline F3 cross3(F3 a, F3 b) { return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static inline F3 norm3(F3 a) { float inv = 1.0f / std::sqrt(dot3(a, a)); return muls(a, inv); }
+static inline float maxc(F3 a) { return std::fmax(a.x, std::fmax(a.y, a.z)); }
+static inline F3 lerp3(F3 a, F3 b, float t) { return add(a, muls(sub(b, a), t)); }
+static inline float sq(float x) { return x * x; }
+
+// sin/cos of 2*pi*t and atan2, from their Taylor series with range reduction
+// (the CUDA pass uses the same polynomials so both sides round identically).
+static void sincos_turns(float t, float* s, float* c) {
+    float q = std::floor(t * 4.0f + 0.5f);
+    float r = t - q * 0.25f;
+    int iq = ((int)q) & 3;
+    float x = r * 6.28318548f;
+    float x2 = x * x;
+    float ps = x + x * x2 * (-0.166666672f + x2 * (0.00833333377f + x2 * (-0.000198412701f + x2 * 2.75573188e-06f)));
+    float pc = 1.0f + x2 * (-0.5f + x2 * (0.0416666679f + x2 * (-0.00138888892f + x2 * (2.48015876e-05f + x2 * -2.75573188e-07f))));
+    if (iq == 0) { *s = ps; *c = pc; }
+    else if (iq == 1) { *s = pc; *c = -ps; }
+    else if (iq == 2) { *s = -ps; *c = -pc; }
+    else { *s = -pc; *c = ps; }
+}
+static float atan_unit(float z) {
+    float off = 0.0f;
+    if (z > 0.414213568f) { z = (z - 1.0f) / (z + 1.0f); off = 0.785398185f; }
+    float z2 = z * z;
+    float p = 1.0f + z2 * (-0.333333343f + z2 * (0.200000003f + z2 * (-0.142857149f + z2 * (0.111111112f +
+              z2 * (-0.0909090936f + z2 * (0.0769230798f + z2 * (-0.0666666701f + z2 * 0.0588235296f)))))));
+    return off + z * p;
+}
+static float atan2_det(float y, float x) {
+    float ax = std::fabs(x), ay = std::fabs(y);
+    float mx = std::fmax(ax, ay), mn = std::fmin(ax, ay);
+    if (mx == 0.0f) return 0.0f;
+    float a = atan_unit(mn / mx);
+    if (ay > ax) a = 1.57079637f - a;
+    if (x < 0.0f) a = 3.14159274f - a;
+    if (y < 0.0f) a = -a;
+    return a;
+}
+static float half_to_float(uint16_t h) {
+    uint32_t sign = (uint32_t)(h & 0x8000u) << 16, exp = (h >> 10) & 0x1fu, man = h & 0x3ffu;
+    if (exp == 0) { float f = (float)man * 5.96046448e-08f; return sign ? -f : f; }
+    uint32_t bits = exp == 31 ? (sign | 0x7f800000u | (man << 13)) : (sign | ((exp + 112u) << 23) | (man << 13));
+    float f;
+    std::memcpy(&f, &bits, 4);
+    return f;
+}
+
+// ------------------------------------------------------------- PCG32 ----
+// O'Neill 2014, pcg32 XSH-RR with a 64-bit LCG (pcg_basic).
+struct Pcg { uint64_t state, inc; };
+static uint32_t pcg_next(Pcg& g) {
+    uint64_t old = g.state;
+    g.state = old * 6364136223846793005ULL + g.inc;
+    uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    uint32_t rot = (uint32_t)(old >> 59u);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+}
+static Pcg pcg_seed(uint64_t initstate, uint64_t initseq) {
+    Pcg g{0u, (initseq << 1u) | 1u};
+    pcg_next(g);
+    g.state += initstate;
+    pcg_next(g);
+    return g;
+}
+static float pcg_uniform(Pcg& g) { return (float)(pcg_next(g) >> 8) * 5.96046448e-08f; }
+static uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+static uint64_t sample_initstate(uint64_t seed, uint32_t sample) {
+    return mix64(seed + 0x9e3779b97f4a7c15ULL * ((uint64_t)sample + 1u));
+}
+
+// -------------------------------------------------- reference BSDF ----
+static const float kInvPi = 0.318309873f;
+struct Surf { F3 base, f0, f90; float rough, ior; };
+
+static F3 schlick_mix(F3 f0, F3 f90, float c) {            // utils.hlsl:40-42
+    float x = 1.0f - c;
+    float x2 = x * x;
+    return lerp3(f0, f90, (x2 * x2) * x);
+}
+static F3 schlick_fresnel(F3 f0, F3 f90, float c, float ior) {  // utils.hlsl:44-51
+    if (c < 0.0f) {
+        float eta = 1.0f / ior;
+        float s2 = eta * eta * (1.0f - c * c);
+        c = std::sqrt(std::fmax(1.0f - s2, 0.0f));
+    }
+    return schlick_mix(f0, f90, c);
+}
+static void aniso_rough(float r, float* rx, float* ry) {  // utils.hlsl:54-59, anisotropy 0
+    float aniso = std::sqrt(1.0f - 0.0f * 0.9f);
+    float r2 = r * r;
+    *rx = std::fmax(r2 / aniso, 0.001f);
+    *ry = std::fmax(r2 * aniso, 0.001f);
+}
+static float ggx_ndf(F3 h, float rx, float ry) {  // utils.hlsl:62-65
+    float a = sq(h.x / rx) + sq(h.y / ry) + sq(h.z);
+    return kInvPi / (rx * ry * a * a);
+}
+static float ggx_g1(F3 v, float rx, float ry) {  // utils.hlsl:67-70
+    float a = (sq(rx * v.x) + sq(ry * v.y)) / std::fmax(v.z * v.z, 0.0001f);
+    return 2.0f / (1.0f + std::sqrt(1.0f + a));
+}
+static float ggx_vis_hc(F3 v, F3 l, float rx, float ry) {  // utils.hlsl:92-96
+    float a = l.z * std::sqrt(sq(rx * v.x) + sq(ry * v.y) + sq(v.z));
+    float b = v.z * std::sqrt(sq(rx * l.x) + sq(ry * l.y) + sq(l.z));
+    return 0.5f / std::fmax(a + b, 0.0001f);
+}
+static F3 ggx_vndf_sample(F3 v, float rx, float ry, float u0, float u1) {  // utils.hlsl:98-116
+    if (v.z < 0.0f) v = neg(v);
+    F3 vh = norm3(f3(rx * v.x, ry * v.y, v.z));
+    float ls = vh.x * vh.x + vh.y * vh.y;
+    F3 t1v = ls > 0.0f ? divs(f3(-vh.y, vh.x, 0.0f), std::sqrt(ls)) : f3(1.0f, 0.0f, 0.0f);
+    F3 t2v = cross3(vh, t1v);
+    float r = std::sqrt(u0);
+    float sp, cp;
+    sincos_turns(u1, &sp, &cp);
+    float t1 = r * cp, t2 = r * sp;
+    float s = 0.5f * (1.0f + vh.z);
+    t2 = (1.0f - s) * std::sqrt(1.0f - t1 * t1) + s * t2;
+    F3 nh = add(add(smul(t1, t1v), smul(t2, t2v)), smul(std::sqrt(std::fmax(1.0f - t1 * t1 - t2 * t2, 0.0f)), vh));
+    return norm3(f3(rx * nh.x, ry * nh.y, std::fmax(nh.z, 0.0f)));
+}
+static float ggx_vndf_pdf(F3 h, F3 v, float rx, float ry) {  // utils.hlsl:118-121
+    return ggx_g1(v, rx, ry) * ggx_ndf(h, rx, ry) * std::fmax(dot3(h, v), 0.0f) / std::fmax(v.z, 0.0001f);
+}
+struct Frm { F3 x, y, z; };
+static Frm make_frame(F3 n) {  // frame.hlsl:9-18
+    Frm f;
+    f.z = n;
+    float sign = n.z > 0.0f ? 1.0f : -1.0f;
+    float a = -1.0f / (sign + n.z);
+    float b = n.x * n.y * a;
+    f.x = f3(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    f.y = f3(b, sign + n.y * n.y * a, -n.y);
+    return f;
+}
+static F3 local_of(const Frm& f, F3 v) { return f3(dot3(v, f.x), dot3(v, f.y), dot3(v, f.z)); }
+static F3 world_of(const Frm& f, F3 v) { return add(add(smul(v.x, f.x), smul(v.y, f.y)), smul(v.z, f.z)); }
+static F3 eval_lit(F3 N, F3 T, F3 B, F3 V, F3 L, const Surf& s) {  // lit.hlsl:5-35
+    F3 H = norm3(add(V, L));
+    F3 lh = f3(dot3(H, T), dot3(H, B), dot3(H, N));
+    F3 lv = f3(dot3(V, T), dot3(V, B), dot3(V, N));
+    F3 ll = f3(dot3(L, T), dot3(L, B), dot3(L, N));
+    if (lv.z <= 0.0f || ll.z <= 0.0f) return f3(0, 0, 0);
+    F3 fr = schlick_fresnel(s.f0, s.f90, std::fmax(dot3(V, H), 0.0f), s.ior);
+    F3 diffuse = muls(muls(mul(sub(f3(1, 1, 1), fr), s.base), kInvPi), std::fmax(ll.z, 0.0f));
+    float rx, ry;
+    aniso_rough(s.rough, &rx, &ry);
+    float ndf = ggx_ndf(lh, rx, ry);
+    float vis = ggx_vis_hc(lv, ll, rx, ry);
+    F3 spec = muls(muls(muls(fr, ndf), vis), std::fmax(ll.z, 0.0f));
+    return add(diffuse, spec);
+}
+static F3 sphere_sample(float u0, float u1) {  // sampling.hlsl:13-19
+    float z = u1 * 2.0f - 1.0f;
+    float r = std::sqrt(std::fmax(1.0f - z * z, 0.0f));
+    float sp, cp;
+    sincos_turns(u0, &sp, &cp);
+    return f3(cp * r, sp * r, z);
+}
+static F3 cos_hemi_sample(float u0, float u1) {  // sampling.hlsl:24-28
+    float r = std::sqrt(u1);
+    float sp, cp;
+    sincos_turns(u0, &sp, &cp);
+    return f3(cp * r, sp * r, std::sqrt(std::fmax(1.0f - u1, 0.0f)));
+}
+static float spec_prob(const Surf& s, float ndotv) {
+    F3 fn = schlick_mix(s.f0, s.f90, ndotv);
+    float ws = fn.x + fn.y + fn.z;
+    float wd = (1.0f - fn.x) * s.base.x + (1.0f - fn.y) * s.base.y + (1.0f - fn.z) * s.base.z;
+    float p = ws / (ws + wd);
+    return std::fmin(std::fmax(p, 0.1f), 0.9f);
+}
+static float mix_pdf(F3 lv, F3 ll, float rx, float ry, float ps) {
+    if (ll.z <= 0.0f) return 0.0f;
+    F3 h = norm3(add(lv, ll));
+    float hv = std::fabs(dot3(h, lv));
+    float pspec = hv > 0.0f ? ggx_vndf_pdf(h, lv, rx, ry) / (4.0f * hv) : 0.0f;
+    return ps * pspec + (1.0f - ps) * (ll.z * kInvPi);
+}
+
+// ------------------------------------------------------------- scene ----
+struct Tri { F3 a, b, c; uint32_t prim, mat; };
+struct BNode { float lo[3], hi[3]; uint32_t left_or_first, count; uint32_t axis; };  // count > 0: leaf
+
+struct Scene {
+    std::vector<Tri> tris;         // in BVH leaf order
+    std::vector<BNode> nodes;
+    std::vector<float> mats;       // 8 per material: base rgb, rough, f0 rgb, metallic
+    uint32_t nmat = 0;
+    uint32_t nlights = 0;
+    F3 ldir[4], le[4];
+    uint32_t sky_kind = 0;
+    F3 sky_color{0, 0, 0};
+    uint32_t sw = 0, sh = 0;
+    std::vector<uint16_t> texels;
+    std::vector<float> cmarg, ccond, ptab;
+    float extent = 1.0f, offset = 0.0f;
+};
+
+// binned SAH binary BVH (16 bins, leaves of up to 4 triangles)
+struct BuildRef { float lo[3], hi[3], c[3]; uint32_t t; };
+static double area(const float lo[3], const float hi[3]) {
+    double d0 = std::max(0.0, (double)hi[0] - lo[0]), d1 = std::max(0.0, (double)hi[1] - lo[1]),
+           d2 = std::max(0.0, (double)hi[2] - lo[2]);
+    return 2.0 * (d0 * d1 + d1 * d2 + d2 * d0);
+}
+static uint32_t build_rec(Scene& S, std::vector<BuildRef>& refs, uint32_t b, uint32_t e) {
+    uint32_t ni = (uint32_t)S.nodes.size();
+    S.nodes.push_back(BNode{});
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = b; i < e; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], refs[i].lo[k]); hi[k] = std::max(hi[k], refs[i].hi[k]);
+            clo[k] = std::min(clo[k], refs[i].c[k]); chi[k] = std::max(chi[k], refs[i].c[k]);
+        }
+    uint32_t n = e - b;
+    auto make_leaf = [&]() {
+        BNode& nd = S.nodes[ni];
+        for (int k = 0; k < 3; ++k) { nd.lo[k] = lo[k]; nd.hi[k] = hi[k]; }
+        nd.left_or_first = b;
+        nd.count = n;
+        return ni;
+    };
+    if (n <= 2) return make_leaf();
+    const int NB = 16;
+    double best = INFINITY;
+    int ba = -1, bs = 0;
+    for (int a = 0; a < 3; ++a) {
+        float ext = chi[a] - clo[a];
+        if (!(ext > 0.0f)) continue;
+        uint32_t cnt[NB] = {0};
+        float blo[NB][3], bhi[NB][3];
+        for (int j = 0; j < NB; ++j)
+            for (int k = 0; k < 3; ++k) { blo[j][k] = INFINITY; bhi[j][k] = -INFINITY; }
+        for (uint32_t i = b; i < e; ++i) {
+            int j = std::min(NB - 1, (int)((refs[i].c[a] - clo[a]) / ext * NB));
+            cnt[j]++;
+            for (int k = 0; k < 3; ++k) { blo[j][k] = std::min(blo[j][k], refs[i].lo[k]); bhi[j][k] = std::max(bhi[j][k], refs[i].hi[k]); }
+        }
+        for (int s = 1; s < NB; ++s) {
+            float l0[3] = {INFINITY, INFINITY, INFINITY}, l1[3] = {-INFINITY, -INFINITY, -INFINITY};
+            float r0[3] = {INFINITY, INFINITY, INFINITY}, r1[3] = {-INFINITY, -INFINITY, -INFINITY};
+            uint32_t nl = 0, nr = 0;
+            for (int j = 0; j < NB; ++j) {
+                float* x0 = j < s ? l0 : r0;
+                float* x1 = j < s ? l1 : r1;
+                if (j < s) nl += cnt[j]; else nr += cnt[j];
+                for (int k = 0; k < 3; ++k) { x0[k] = std::min(x0[k], blo[j][k]); x1[k] = std::max(x1[k], bhi[j][k]); }
+            }
+            if (!nl || !nr) continue;
+            double c = area(l0, l1) * nl + area(r0, r1) * nr;
+            if (c < best) { best = c; ba = a; bs = s; }
+        }
+    }
+    uint32_t mid;
+    if (ba < 0) {
+        if (n <= 4) return make_leaf();
+        mid = b + n / 2;
+    } else {
+        double leaf_cost = (double)n, split_cost = 0.5 + best / std::max(area(lo, hi), 1e-30);
+        if (n <= 4 && leaf_cost <= split_cost) return make_leaf();
+        float ext = chi[ba] - clo[ba];
+        auto it = std::partition(refs.begin() + b, refs.begin() + e, [&](const BuildRef& r) {
+            return std::min(NB - 1, (int)((r.c[ba] - clo[ba]) / ext * NB)) < bs;
+        });
+        mid = (uint32_t)(it - refs.begin());
+        if (mid == b || mid == e) mid = b + n / 2;
+    }
+    int axis = 0;
+    float ext0 = hi[0] - lo[0];
+    if (hi[1] - lo[1] > ext0) { axis = 1; ext0 = hi[1] - lo[1]; }
+    if (hi[2] - lo[2] > ext0) axis = 2;
+    if (ba >= 0) axis = ba;
+    build_rec(S, refs, b, mid);
+    uint32_t right = build_rec(S, refs, mid, e);
+    BNode& nd = S.nodes[ni];
+    for (int k = 0; k < 3; ++k) { nd.lo[k] = lo[k]; nd.hi[k] = hi[k]; }
+    nd.left_or_first = right;  // left child is ni + 1
+    nd.count = 0;
+    nd.axis = (uint32_t)axis;
+    return ni;
+}
+
+// ------------------------------------------------------------ traversal ----
+struct Ray {
+    F3 o, d;
+    float tmin, tmax;
+    float id[3];
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+static float comp(F3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+static Ray make_ray(F3 o, float tmin, F3 d, float tmax) {
+    Ray r;
+    r.o = o; r.d = d; r.tmin = tmin; r.tmax = tmax;
+    for (int k = 0; k < 3; ++k) {
+        float dk = comp(d, k);
+        r.id[k] = 1.0f / dk;
+    }
+    float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+    int kz = 0;
+    float m = ax;
+    if (ay > m) { kz = 1; m = ay; }
+    if (az > m) kz = 2;
+    int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+    float dkz = comp(d, kz);
+    if (dkz < 0.0f) std::swap(kx, ky);
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.Sx = comp(d, kx) / dkz;
+    r.Sy = comp(d, ky) / dkz;
+    r.Sz = 1.0f / dkz;
+    return r;
+}
+// Woop, Benthin, Wald 2013 watertight test (fp32, double fallback on zero edges)
+static bool tri_hit(const Ray& r, const Tri& t, float tbest, uint32_t best_prim, float& to, float& uo, float& vo) {
+    F3 A = sub(t.a, r.o), B = sub(t.b, r.o), C = sub(t.c, r.o);
+    float Akx = comp(A, r.kx), Aky = comp(A, r.ky), Akz = comp(A, r.kz);
+    float Bkx = comp(B, r.kx), Bky = comp(B, r.ky), Bkz = comp(B, r.kz);
+    float Ckx = comp(C, r.kx), Cky = comp(C, r.ky), Ckz = comp(C, r.kz);
+    float Ax = Akx - r.Sx * Akz, Ay = Aky - r.Sy * Akz;
+    float Bx = Bkx - r.Sx * Bkz, By = Bky - r.Sy * Bkz;
+    float Cx = Ckx - r.Sx * Ckz, Cy = Cky - r.Sy * Ckz;
+    float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    float det = U + V + W;
+    if (det == 0.0f) return false;
+    float Az = r.Sz * Akz, Bz = r.Sz * Bkz, Cz = r.Sz * Ckz;
+    float T = U * Az + V * Bz + W * Cz;
+    float rcp = 1.0f / det;
+    float tt = T * rcp;
+    if (!(tt > r.tmin)) return false;
+    if (!(tt < tbest || (tt == tbest && t.prim < best_prim))) return false;
+    to = tt; uo = U * rcp; vo = V * rcp;
+    return true;
+}
+static bool box_hit(const Ray& r, const BNode& n, float tbest) {
+    float tn = r.tmin, tf = INFINITY;
+    const float o[3] = {r.o.x, r.o.y, r.o.z};
+    const float d[3] = {r.d.x, r.d.y, r.d.z};
+    for (int k = 0; k < 3; ++k) {
+        if (d[k] == 0.0f) {  // parallel to the slab: inside it (boundary included) or never
+            if (o[k] < n.lo[k] || o[k] > n.hi[k]) return false;
+            continue;
+        }
+        float t0 = (n.lo[k] - o[k]) * r.id[k], t1 = (n.hi[k] - o[k]) * r.id[k];
+        if (t0 > t1) std::swap(t0, t1);
+        tn = std::fmax(tn, t0);
+        tf = std::fmin(tf, t1);
+    }
+    // relative pad on both ends: rounding of the slab products never culls a
+    // box that holds a hit at t <= tbest (ties at tbest included)
+    float hi = std::fmin(tf, tbest);
+    return tn - std::fabs(tn) * 9.5e-7f <= hi + std::fabs(hi) * 9.5e-7f;
+}
+struct Counts { uint64_t nodes = 0, tris = 0; };
+// returns index into S.tris (leaf order) or UINT32_MAX
+static uint32_t trace(const Scene& S, const Ray& r, bool any, float& to, float& uo, float& vo, Counts* cnt) {
+    float tbest = r.tmax;
+    uint32_t best = UINT32_MAX, best_prim = UINT32_MAX;
+    float bu = 0, bv = 0;
+    uint32_t stack[128];
+    int sp = 0;
+    // a zero direction is skipped as a miss (rt_gbuffer.hlsl:13-15)
+    if (!(r.d.x == 0.0f && r.d.y == 0.0f && r.d.z == 0.0f)) stack[sp++] = 0;
+    while (sp) {
+        uint32_t ni = stack[--sp];
+        const BNode& n = S.nodes[ni];
+        if (cnt) cnt->nodes++;
+        if (!box_hit(r, n, tbest)) continue;
+        if (n.count) {
+            for (uint32_t i = 0; i < n.count; ++i) {
+                const Tri& t = S.tris[n.left_or_first + i];
+                if (cnt) cnt->tris++;
+                float tt, u, v;
+                if (tri_hit(r, t, tbest, best_prim, tt, u, v)) {
+                    tbest = tt; best = n.left_or_first + i; best_prim = t.prim; bu = u; bv = v;
+                    if (any) { to = tt; uo = u; vo = v; return best; }
+                }
+            }
+        } else {
+            uint32_t l = ni + 1, rr = n.left_or_first;
+            bool neg = comp(r.d, (int)n.axis) < 0.0f;
+            // push the far child first
+            if (neg) { stack[sp++] = l; stack[sp++] = rr; } else { stack[sp++] = rr; stack[sp++] = l; }
+        }
+    }
+    to = tbest; uo = bu; vo = bv;
+    return best;
+}
+
+// ------------------------------------------------------------------ sky ----
+static uint32_t cdf_search(const float* cdf, uint32_t n, float u) {
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if (cdf[mid] <= u) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+static float cdf_rem(const float* cdf, uint32_t i, float u) {
+    float w = cdf[i + 1] - cdf[i];
+    float f = w > 0.0f ? (u - cdf[i]) / w : 0.5f;
+    return std::fmin(std::fmax(f, 0.0f), 0.99999994f);
+}
+static F3 texel(const Scene& S, uint32_t i, uint32_t j) {
+    const uint16_t* t = &S.texels[((size_t)i * S.sw + j) * 4];
+    return f3(half_to_float(t[0]) * S.sky_color.x, half_to_float(t[1]) * S.sky_color.y, half_to_float(t[2]) * S.sky_color.z);
+}
+static void dir_texel(const Scene& S, F3 d, uint32_t& i, uint32_t& j, float& st) {
+    float rxz = std::sqrt(d.x * d.x + d.z * d.z);
+    float theta = atan2_det(rxz, d.y);
+    float phi = atan2_det(d.z, d.x);
+    float v = theta * kInvPi;
+    float u = phi * (0.5f * kInvPi) + 0.5f;
+    int ii = (int)std::floor(v * (float)S.sh), jj = (int)std::floor(u * (float)S.sw);
+    ii = std::min(std::max(ii, 0), (int)S.sh - 1);
+    jj = std::min(std::max(jj, 0), (int)S.sw - 1);
+    i = (uint32_t)ii; j = (uint32_t)jj; st = rxz;
+}
+static const float kTwoPiSq = 19.7392082f;
+static F3 sky_eval(const Scene& S, F3 d) {
+    if (S.sky_kind == 0) return S.sky_color;
+    uint32_t i, j; float st;
+    dir_texel(S, d, i, j, st);
+    return texel(S, i, j);
+}
+static float sky_pdf(const Scene& S, F3 d) {
+    if (S.sky_kind == 0) return 0.0795774683f;
+    uint32_t i, j; float st;
+    dir_texel(S, d, i, j, st);
+    if (!(st > 0.0f)) return 0.0f;
+    return S.ptab[(size_t)i * S.sw + j] / (kTwoPiSq * st);
+}
+static F3 sky_sample(const Scene& S, float u0, float u1, float& pdf, F3& le) {
+    if (S.sky_kind == 0) { pdf = 0.0795774683f; le = S.sky_color; return sphere_sample(u0, u1); }
+    uint32_t i = cdf_search(S.cmarg.data(), S.sh, u0);
+    float fy = cdf_rem(S.cmarg.data(), i, u0);
+    const float* row = S.ccond.data() + (size_t)i * (S.sw + 1);
+    uint32_t j = cdf_search(row, S.sw, u1);
+    float fx = cdf_rem(row, j, u1);
+    float st, ct, sp, cp;
+    sincos_turns(((float)i + fy) / (2.0f * (float)S.sh), &st, &ct);
+    sincos_turns(((float)j + fx) / (float)S.sw - 0.5f, &sp, &cp);
+    F3 d = f3(st * cp, ct, st * sp);
+    float p = S.ptab[(size_t)i * S.sw + j];
+    pdf = (st > 0.0f && p > 0.0f) ? p / (kTwoPiSq * st) : 0.0f;
+    le = texel(S, i, j);
+    return d;
+}
+static void build_sky(Scene& S) {
+    const uint32_t W = S.sw, H = S.sh;
+    S.cmarg.assign(H + 1, 0.0f);
+    S.ccond.assign((size_t)H * (W + 1), 0.0f);
+    S.ptab.assign((size_t)H * W, 0.0f);
+    std::vector<double> w((size_t)H * W), rows(H);
+    double total = 0.0;
+    for (uint32_t i = 0; i < H; ++i) {
+        float st, ct;
+        sincos_turns(((float)i + 0.5f) / (2.0f * (float)H), &st, &ct);
+        double rs = 0.0;
+        for (uint32_t j = 0; j < W; ++j) {
+            const uint16_t* t = &S.texels[((size_t)i * W + j) * 4];
+            float lum = half_to_float(t[0]) + half_to_float(t[1]) + half_to_float(t[2]);
+            double x = lum > 0.0f ? (double)lum * (double)st : 0.0;
+            w[(size_t)i * W + j] = x;
+            rs += x;
+        }
+        rows[i] = rs;
+        total += rs;
+    }
+    for (uint32_t i = 0; i < H; ++i) {
+        float* c = &S.ccond[(size_t)i * (W + 1)];
+        double acc = 0.0;
+        for (uint32_t j = 0; j < W; ++j) {
+            c[j] = rows[i] > 0.0 ? (float)(acc / rows[i]) : (float)j / (float)W;
+            acc += w[(size_t)i * W + j];
+        }
+        c[W] = 1.0f;
+    }
+    double acc = 0.0;
+    for (uint32_t i = 0; i < H; ++i) {
+        S.cmarg[i] = total > 0.0 ? (float)(acc / total) : (float)i / (float)H;
+        acc += rows[i];
+    }
+    S.cmarg[H] = 1.0f;
+    for (size_t k = 0; k < (size_t)H * W; ++k)
+        S.ptab[k] = total > 0.0 ? (float)(w[k] * (double)W * (double)H / total) : 0.0f;
+}
+
+// --------------------------------------------------------- wavefront ----
+struct Cam { F3 pos, s, u, f; float tan_half, aspect; uint32_t w, h; };
+static Cam make_cam(const float* c) {  // pos3 front3 up3 fov w h
+    Cam k;
+    k.pos = f3(c[0], c[1], c[2]);
+    k.f = norm3(f3(c[3], c[4], c[5]));
+    k.s = norm3(cross3(k.f, f3(c[6], c[7], c[8])));
+    k.u = cross3(k.s, k.f);
+    k.w = (uint32_t)c[10];
+    k.h = (uint32_t)c[11];
+    k.tan_half = (float)std::tan((double)c[9] * 3.14159265358979323846 / 360.0);
+    k.aspect = (float)k.w / (float)k.h;
+    return k;
+}
+
+struct Settings {
+    uint32_t spp, max_seg, sample_offset, flags;
+    uint64_t seed;
+    float ray_length, t_min;
+};
+enum { F_JITTER = 1, F_NO_SUN = 2, F_NO_SKY = 4 };
+
+struct PathQ {  // one wavefront queue in the oracle (structure of arrays)
+    std::vector<F3> o, d, thr;
+    std::vector<float> tmin, tmax, lpdf;
+    std::vector<uint32_t> pix, seg;
+    std::vector<Pcg> rng;
+    void clear() { o.clear(); d.clear(); thr.clear(); tmin.clear(); tmax.clear(); lpdf.clear(); pix.clear(); seg.clear(); rng.clear(); }
+    size_t size() const { return o.size(); }
+    void push(F3 oo, float tn, F3 dd, float tx, F3 t, float lp, uint32_t p, uint32_t s, Pcg g) {
+        o.push_back(oo); tmin.push_back(tn); d.push_back(dd); tmax.push_back(tx); thr.push_back(t); lpdf.push_back(lp);
+        pix.push_back(p); seg.push_back(s); rng.push_back(g);
+    }
+};
+struct ShadowQ {
+    std::vector<F3> o, d, c;
+    std::vector<float> tmin, tmax;
+    std::vector<uint32_t> pix;
+    void clear() { o.clear(); d.clear(); c.clear(); tmin.clear(); tmax.clear(); pix.clear(); }
+};
+
+// Renders pixels [pix_begin, pix_end) of one camera; `acc` receives RGB sums
+// (3 floats per pixel, indexed from pix_begin).
+static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32_t pix_begin, uint32_t pix_end,
+                        float* acc, uint64_t* ext_cnt, uint64_t* sh_cnt) {
+    PathQ q, nq;
+    ShadowQ sq;
+    for (uint32_t s = 0; s < st.spp; ++s) {
+        q.clear();
+        // camera (generate_camera_ray.hlsl:9-15)
+        for (uint32_t p = pix_begin; p < pix_end; ++p) {
+            uint32_t px = p % K.w, py = p / K.w;
+            Pcg g = pcg_seed(sample_initstate(st.seed, st.sample_offset + s), (uint64_t)p);
+            float jx = 0.5f, jy = 0.5f;
+            if (st.flags & F_JITTER) { jx = pcg_uniform(g); jy = pcg_uniform(g); }
+            float uvx = ((float)px + jx) / (float)K.w;
+            float uvy = ((float)py + jy) / (float)K.h;
+            float ndx = uvx * 2.0f - 1.0f, ndy = 1.0f - uvy * 2.0f;
+            F3 dl = norm3(f3(ndx * K.aspect * K.tan_half, ndy * K.tan_half, -1.0f));
+            F3 dw = norm3(add(add(muls(K.s, dl.x), muls(K.u, dl.y)), muls(neg(K.f), dl.z)));
+            q.push(K.pos, st.t_min, dw, st.ray_length, f3(1, 1, 1), 0.0f, p, 0, g);
+        }
+        for (uint32_t seg = 0; seg < st.max_seg && q.size(); ++seg) {
+            ext_cnt[seg] += q.size();
+            nq.clear();
+            sq.clear();
+            for (size_t i = 0; i < q.size(); ++i) {
+                // extend
+                Ray r = make_ray(q.o[i], q.tmin[i], q.d[i], q.tmax[i]);
+                float t, u, v;
+                uint32_t hit = trace(S, r, false, t, u, v, nullptr);
+                F3 d = q.d[i], thr = q.thr[i];
+                float* a = acc + 3 * (size_t)(q.pix[i] - pix_begin);
+                if (hit == UINT32_MAX) {  // deferred_lighting_secondary.hlsl:23-29
+                    F3 le = sky_eval(S, d);
+                    float w = 1.0f;
+                    if (seg > 0 && !(st.flags & F_NO_SKY)) {
+                        float pb = q.lpdf[i], pl = sky_pdf(S, d);
+                        float pb2 = pb * pb, pl2 = pl * pl;
+                        w = pb2 + pl2 > 0.0f ? pb2 / (pb2 + pl2) : 1.0f;
+                    }
+                    F3 c = muls(mul(thr, le), w);
+                    if (maxc(c) > 0.0f) { a[0] += c.x; a[1] += c.y; a[2] += c.z; }
+                    continue;
+                }
+                // shade
+                const Tri& T = S.tris[hit];
+                F3 ng = norm3(cross3(sub(T.b, T.a), sub(T.c, T.a)));
+                if (dot3(ng, d) > 0.0f) ng = neg(ng);
+                F3 N = ng;
+                F3 P = add(q.o[i], muls(d, t));
+                const float* m = &S.mats[8 * (size_t)T.mat];
+                Surf surf{f3(m[0], m[1], m[2]), f3(m[4], m[5], m[6]), f3(1, 1, 1), m[3], 1.5f};
+                Frm fr = make_frame(N);
+                F3 V = neg(d);
+                Pcg g = q.rng[i];
+                float us0 = pcg_uniform(g), us1 = pcg_uniform(g), ul = pcg_uniform(g), ub0 = pcg_uniform(g),
+                      ub1 = pcg_uniform(g);
+                F3 org = add(P, muls(N, S.offset));
+                float rx, ry;
+                aniso_rough(surf.rough, &rx, &ry);
+                F3 lv = local_of(fr, V);
+                float ps = spec_prob(surf, lv.z);
+                for (uint32_t l = 0; l < S.nlights; ++l) {  // deferred_lighting_secondary.hlsl:51-60
+                    if (st.flags & F_NO_SUN) break;
+                    F3 f = eval_lit(N, fr.x, fr.y, V, S.ldir[l], surf);
+                    F3 c = mul(mul(thr, S.le[l]), f);
+                    if (maxc(c) > 0.0f) {
+                        sq.o.push_back(org); sq.tmin.push_back(st.t_min); sq.d.push_back(S.ldir[l]);
+                        sq.tmax.push_back(st.ray_length); sq.c.push_back(c); sq.pix.push_back(q.pix[i]);
+                    }
+                }
+                if (!(st.flags & F_NO_SKY)) {
+                    float pl;
+                    F3 le;
+                    F3 L = sky_sample(S, us0, us1, pl, le);
+                    if (pl > 0.0f) {
+                        F3 f = eval_lit(N, fr.x, fr.y, V, L, surf);
+                        if (maxc(f) > 0.0f) {
+                            F3 ll = local_of(fr, L);
+                            float pb = mix_pdf(lv, ll, rx, ry, ps);
+                            float pl2 = pl * pl, pb2 = pb * pb;
+                            float w = pl2 / (pl2 + pb2);
+                            F3 c = muls(mul(mul(thr, le), f), w / pl);
+                            if (maxc(c) > 0.0f) {
+                                sq.o.push_back(org); sq.tmin.push_back(st.t_min); sq.d.push_back(L);
+                                sq.tmax.push_back(st.ray_length); sq.c.push_back(c); sq.pix.push_back(q.pix[i]);
+                            }
+                        }
+                    }
+                }
+                // sample_secondary_ray.hlsl:16-28 (termination) and :51-64 (weight)
+                if (seg + 1 < st.max_seg && maxc(thr) >= 0.001f) {
+                    F3 ll;
+                    if (ul < ps) ll = [&] { F3 h = ggx_vndf_sample(lv, rx, ry, ub0, ub1); return sub(neg(lv), muls(h, 2.0f * dot3(neg(lv), h))); }();
+                    else ll = cos_hemi_sample(ub0, ub1);
+                    if (ll.z > 0.0f) {
+                        F3 L = world_of(fr, ll);
+                        float pdf = mix_pdf(lv, ll, rx, ry, ps);
+                        F3 f = eval_lit(N, fr.x, fr.y, V, L, surf);
+                        F3 w = pdf > 0.0f ? divs(f, pdf) : f3(0, 0, 0);
+                        if (!std::isfinite(w.x) || !std::isfinite(w.y) || !std::isfinite(w.z)) w = f3(0, 0, 0);
+                        F3 nt = mul(thr, w);
+                        if (maxc(nt) > 0.0f) nq.push(org, st.t_min, L, st.ray_length, nt, pdf, q.pix[i], seg + 1, g);
+                    }
+                }
+            }
+            // shadow (any hit)
+            sh_cnt[seg] += sq.o.size();
+            for (size_t k = 0; k < sq.o.size(); ++k) {
+                Ray r = make_ray(sq.o[k], sq.tmin[k], sq.d[k], sq.tmax[k]);
+                float t, u, v;
+                if (trace(S, r, true, t, u, v, nullptr) == UINT32_MAX) {
+                    float* a = acc + 3 * (size_t)(sq.pix[k] - pix_begin);
+                    a[0] += sq.c[k].x; a[1] += sq.c[k].y; a[2] += sq.c[k].z;
+                }
+            }
+            std::swap(q, nq);
+        }
+    }
+}
+
+static int nthreads(int req) {
+    int hc = (int)std::thread::hardware_concurrency();
+    return req > 0 ? req : (hc > 0 ? hc : 1);
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+ORC_API int orc_scene_create(const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt, const uint32_t* mat_ids,
+                             const float* materials, uint32_t nm, const float* lights, uint32_t nl, uint32_t sky_kind,
+                             const float* sky_color, uint32_t sky_w, uint32_t sky_h, const uint16_t* sky_texels,
+                             void** out) {
+    if (!pos || !nt || !materials || !nm || !out || nl > 4) return -1;
+    Scene* S = new Scene();
+    std::vector<BuildRef> refs(nt);
+    std::vector<Tri> soup(nt);
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = 0; i < nv; ++i)
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], pos[3 * i + k]); hi[k] = std::max(hi[k], pos[3 * i + k]); }
+    S->extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
+    S->offset = 2e-5f * S->extent;
+    for (uint32_t t = 0; t < nt; ++t) {
+        uint32_t v[3];
+        for (int c = 0; c < 3; ++c) v[c] = idx ? idx[3 * t + c] : 3 * t + c;
+        Tri& T = soup[t];
+        T.a = f3(pos[3 * v[0]], pos[3 * v[0] + 1], pos[3 * v[0] + 2]);
+        T.b = f3(pos[3 * v[1]], pos[3 * v[1] + 1], pos[3 * v[1] + 2]);
+        T.c = f3(pos[3 * v[2]], pos[3 * v[2] + 1], pos[3 * v[2] + 2]);
+        T.prim = t;
+        T.mat = mat_ids ? mat_ids[t] : 0;
+        BuildRef& R = refs[t];
+        const F3 vs[3] = {T.a, T.b, T.c};
+        for (int k = 0; k < 3; ++k) {
+            R.lo[k] = std::min({comp(vs[0], k), comp(vs[1], k), comp(vs[2], k)});
+            R.hi[k] = std::max({comp(vs[0], k), comp(vs[1], k), comp(vs[2], k)});
+            R.c[k] = 0.5f * (R.lo[k] + R.hi[k]);
+        }
+        R.t = t;
+    }
+    S->nodes.reserve(2 * (size_t)nt);
+    build_rec(*S, refs, 0, nt);
+    S->tris.resize(nt);
+    for (uint32_t i = 0; i < nt; ++i) S->tris[i] = soup[refs[i].t];
+    S->nmat = nm;
+    S->mats.resize(8 * (size_t)nm);
+    for (uint32_t m = 0; m < nm; ++m) {
+        const float* M = materials + 5 * (size_t)m;  // base rgb, roughness, metallic
+        float* o = &S->mats[8 * (size_t)m];
+        o[0] = M[0]; o[1] = M[1]; o[2] = M[2]; o[3] = M[3];
+        for (int k = 0; k < 3; ++k) o[4 + k] = 0.04f + (M[k] - 0.04f) * M[4];  // lerp(0.04, base, metallic)
+        o[7] = M[4];
+    }
+    S->nlights = nl;
+    for (uint32_t l = 0; l < nl; ++l) {
+        S->ldir[l] = norm3(f3(lights[6 * l], lights[6 * l + 1], lights[6 * l + 2]));
+        S->le[l] = f3(lights[6 * l + 3], lights[6 * l + 4], lights[6 * l + 5]);
+    }
+    S->sky_kind = sky_kind;
+    S->sky_color = f3(sky_color[0], sky_color[1], sky_color[2]);
+    if (sky_kind == 1) {
+        if (!sky_texels || !sky_w || !sky_h) { delete S; return -1; }
+        S->sw = sky_w; S->sh = sky_h;
+        S->texels.assign(sky_texels, sky_texels + (size_t)sky_w * sky_h * 4);
+        build_sky(*S);
+    }
+    *out = S;
+    return 0;
+}
+
+ORC_API void orc_scene_destroy(void* s) { delete (Scene*)s; }
+
+// rays: n x 8 floats; hits: n x 4 u32 (t bits, prim, u bits, v bits)
+ORC_API int orc_trace(void* sp, const float* rays, uint32_t n, uint32_t* hits, int any, int threads,
+                      uint32_t* counts) {
+    const Scene& S = *(Scene*)sp;
+    int nt = nthreads(threads);
+    std::atomic<uint32_t> next{0};
+    auto work = [&]() {
+        while (true) {
+            uint32_t b = next.fetch_add(4096);
+            if (b >= n) break;
+            uint32_t e = std::min(n, b + 4096);
+            for (uint32_t i = b; i < e; ++i) {
+                const float* R = rays + 8 * (size_t)i;
+                Ray r = make_ray(f3(R[0], R[1], R[2]), R[3], f3(R[4], R[5], R[6]), R[7]);
+                float t, u, v;
+                Counts c;
+                uint32_t h = trace(S, r, any != 0, t, u, v, counts ? &c : nullptr);
+                uint32_t* H = hits + 4 * (size_t)i;
+                std::memcpy(&H[0], &t, 4);
+                H[1] = h == UINT32_MAX ? UINT32_MAX : S.tris[h].prim;
+                std::memcpy(&H[2], &u, 4);
+                std::memcpy(&H[3], &v, 4);
+                if (counts) { counts[2 * (size_t)i] = (uint32_t)c.nodes; counts[2 * (size_t)i + 1] = (uint32_t)c.tris; }
+            }
+        }
+    };
+    std::vector<std::thread> ts;
+    for (int k = 1; k < nt; ++k) ts.emplace_back(work);
+    work();
+    for (auto& t : ts) t.join();
+    return 0;
+}
+
+// camera: pos3 front3 up3 fov w h (12 floats); settings: spp, max_seg, sample_offset, flags (u32),
+// seed (u64), ray_length, t_min.  Renders rows [row_begin, row_end); out = w x (rows) x 4 mean RGBA.
+// stats: [16] extend rays per segment, [16] shadow rays per segment.
+ORC_API int orc_render(void* sp, const float* camera, uint32_t spp, uint32_t max_seg, uint32_t sample_offset,
+                       uint32_t flags, uint64_t seed, float ray_length, float t_min, uint32_t row_begin,
+                       uint32_t row_end, float* out, uint64_t* stats, int threads, double* seconds) {
+    const Scene& S = *(Scene*)sp;
+    Cam K = make_cam(camera);
+    if (row_end > K.h || row_begin >= row_end || max_seg == 0 || max_seg > 16 || spp == 0) return -1;
+    Settings st{spp, max_seg, sample_offset, flags, seed, ray_length, t_min};
+    uint32_t p0 = row_begin * K.w, p1 = row_end * K.w;
+    std::vector<float> acc(3 * (size_t)(p1 - p0), 0.0f);
+    const uint32_t tile = 256;  // 16 x 16 pixels worth of paths per task
+    uint32_t ntiles = (p1 - p0 + tile - 1) / tile;
+    std::atomic<uint32_t> next{0};
+    int nt = nthreads(threads);
+    std::vector<std::vector<uint64_t>> ext(nt, std::vector<uint64_t>(16, 0)), sh(nt, std::vector<uint64_t>(16, 0));
+    auto t0 = std::chrono::steady_clock::now();
+    auto work = [&](int id) {
+        while (true) {
+            uint32_t k = next.fetch_add(1);
+            if (k >= ntiles) break;
+            uint32_t b = p0 + k * tile, e = std::min(p1, b + tile);
+            render_tile(S, K, st, b, e, acc.data() + 3 * (size_t)(b - p0), ext[id].data(), sh[id].data());
+        }
+    };
+    std::vector<std::thread> ts;
+    for (int k = 1; k < nt; ++k) ts.emplace_back(work, k);
+    work(0);
+    for (auto& t : ts) t.join();
+    double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (seconds) *seconds = sec;
+    float inv = 1.0f / (float)spp;
+    for (size_t p = 0; p < (size_t)(p1 - p0); ++p) {
+        out[4 * p] = acc[3 * p] * inv;
+        out[4 * p + 1] = acc[3 * p + 1] * inv;
+        out[4 * p + 2] = acc[3 * p + 2] * inv;
+        out[4 * p + 3] = 1.0f;
+    }
+    if (stats) {
+        for (int s = 0; s < 32; ++s) stats[s] = 0;
+        for (int k = 0; k < nt; ++k)
+            for (int s = 0; s < 16; ++s) { stats[s] += ext[k][s]; stats[16 + s] += sh[k][s]; }
+    }
+    return 0;
+}
+
+// Building blocks exposed for the unit tests (known-answer checks).
+ORC_API void orc_pcg32(uint64_t initstate, uint64_t initseq, uint32_t n, uint32_t* out) {
+    Pcg g = pcg_seed(initstate, initseq);
+    for (uint32_t i = 0; i < n; ++i) out[i] = pcg_next(g);
+}
+ORC_API void orc_sincos_turns(const float* t, uint32_t n, float* s, float* c) {
+    for (uint32_t i = 0; i < n; ++i) sincos_turns(t[i], &s[i], &c[i]);
+}
+ORC_API void orc_atan2(const float* y, const float* x, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) out[i] = atan2_det(y[i], x[i]);
+}
+// in: N3 V3 L3 base3 f0_3 roughness (16 floats); out: diffuse+specular (3)
+ORC_API void orc_eval_lit(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + 16 * (size_t)i;
+        F3 N = f3(a[0], a[1], a[2]), V = f3(a[3], a[4], a[5]), L = f3(a[6], a[7], a[8]);
+        Surf s{f3(a[9], a[10], a[11]), f3(a[12], a[13], a[14]), f3(1, 1, 1), a[15], 1.5f};
+        Frm fr = make_frame(N);
+        F3 r = eval_lit(N, fr.x, fr.y, V, L, s);
+        out[3 * i] = r.x; out[3 * i + 1] = r.y; out[3 * i + 2] = r.z;
+    }
+}
+// in: V3 (local) rx ry u0 u1 (7 floats); out: h (3) and pdf of h (1)
+ORC_API void orc_vndf(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + 7 * (size_t)i;
+        F3 v = f3(a[0], a[1], a[2]);
+        F3 h = ggx_vndf_sample(v, a[3], a[4], a[5], a[6]);
+        out[4 * i] = h.x; out[4 * i + 1] = h.y; out[4 * i + 2] = h.z;
+        out[4 * i + 3] = ggx_vndf_pdf(h, v, a[3], a[4]);
+    }
+}
+// in: N3; out: frame x3 y3
+ORC_API void orc_frame(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        Frm f = make_frame(f3(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+        float* o = out + 6 * (size_t)i;
+        o[0] = f.x.x; o[1] = f.x.y; o[2] = f.x.z; o[3] = f.y.x; o[4] = f.y.y; o[5] = f.y.z;
+    }
+}
+ORC_API uint32_t orc_scene_bvh_nodes(void* sp) { return (uint32_t)((Scene*)sp)->nodes.size(); }

@@ -1,0 +1,63 @@
+// ref_bsdf.cpp — TEST INFRASTRUCTURE: compiles the reference's shader math
+// (bisemutum/shaders/core/utils/math.hlsl, core/material/utils.hlsl,
+// core/material/lit.hlsl, core/utils/frame.hlsl, core/utils/sampling.hlsl)
+// through hlsl_shim.h and exposes it to the golden-vector generator.  The
+// sources are read where they lie in the reference tree by oracle/build.py,
+// which only rewrites `out T x` / `inout T x` parameters to `T& x`; the result
+// is built into oracle/_ref/ and never shipped.
+#include "hlsl_shim.h"
+
+#include "ref_sources.inc"  // generated: the five reference files, concatenated
+
+#define REF_API extern "C" __attribute__((visibility("default")))
+
+// in: N3 V3 L3 base3 f0_3 roughness; out: diffuse + specular of surface_eval_lit
+// with the frame of create_frame(N) (frame.hlsl:9-18) as T, B.
+REF_API void ref_eval_lit(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + 16 * (size_t)i;
+        float3 N(a[0], a[1], a[2]), V(a[3], a[4], a[5]), L(a[6], a[7], a[8]);
+        SurfaceData s = surface_data_default();
+        s.base_color = float3(a[9], a[10], a[11]);
+        s.f0_color = float3(a[12], a[13], a[14]);
+        s.roughness = a[15];
+        Frame fr = create_frame(N);
+        float3 d, sp;
+        surface_eval_lit(N, fr.x, fr.y, V, L, s, d, sp);
+        float3 r = d + sp;
+        out[3 * i] = r.x; out[3 * i + 1] = r.y; out[3 * i + 2] = r.z;
+    }
+}
+// in: V3 rx ry u0 u1; out: h3, ggx_vndf_sample_pdf(h, v)
+REF_API void ref_vndf(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + 7 * (size_t)i;
+        float3 v(a[0], a[1], a[2]);
+        float3 h = ggx_vndf_sample(v, a[3], a[4], float2(a[5], a[6]));
+        out[4 * i] = h.x; out[4 * i + 1] = h.y; out[4 * i + 2] = h.z;
+        out[4 * i + 3] = ggx_vndf_sample_pdf(h, v, a[3], a[4]);
+    }
+}
+// in: N3; out: frame.x, frame.y
+REF_API void ref_frame(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        Frame f = create_frame(float3(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+        float* o = out + 6 * (size_t)i;
+        o[0] = f.x.x; o[1] = f.x.y; o[2] = f.x.z; o[3] = f.y.x; o[4] = f.y.y; o[5] = f.y.z;
+    }
+}
+// in: roughness; out: (roughness_x, roughness_y) of get_anisotropic_roughness(r, 0)
+REF_API void ref_aniso(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) get_anisotropic_roughness(in[i], 0.0f, out[2 * i], out[2 * i + 1]);
+}
+// in: u0 u1; out: cos_hemisphere_sample (3), uniform_sphere_sample (3)
+REF_API void ref_samplers(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        float2 u(in[2 * i], in[2 * i + 1]);
+        float3 c = cos_hemisphere_sample(u);
+        float3 s = uniform_sphere_sample(u);
+        float* o = out + 6 * (size_t)i;
+        o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = s.x; o[4] = s.y; o[5] = s.z;
+    }
+}
+REF_API float ref_inv_pi(void) { return INV_PI; }

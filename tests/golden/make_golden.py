@@ -1,0 +1,77 @@
+"""Generates tests/golden/bsdf_golden.npz from the reference's own shader math.
+
+The reference's material / frame / sampling HLSL files (bisemutum/shaders/core/
+material/utils.hlsl, lit.hlsl, core/utils/frame.hlsl, sampling.hlsl, math.hlsl)
+are compiled from their sources by oracle/build.py (through a C++ HLSL shim)
+and evaluated here on a seeded grid of inputs.  Needs the reference tree;
+the committed .npz is what the tests read.
+
+    python tests/golden/make_golden.py
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import oracle  # noqa: E402
+
+
+def unit(v):
+    return v / np.linalg.norm(v, axis=-1, keepdims=True)
+
+
+def main():
+    R = oracle.ref_lib()
+    if R is None:
+        raise SystemExit("reference tree not present: cannot regenerate the golden vectors")
+    rng = np.random.default_rng(20240601)
+    n = 4096
+    # surface_eval_lit inputs: N, V, L on the upper side of N, base, f0, roughness
+    N = unit(rng.normal(size=(n, 3)))
+    V = unit(rng.normal(size=(n, 3)))
+    L = unit(rng.normal(size=(n, 3)))
+    V = np.where((np.sum(V * N, 1) < 0)[:, None], -V, V)
+    L = np.where((np.sum(L * N, 1) < 0)[:, None], -L, L)
+    base = rng.uniform(0.1, 0.9, (n, 3))
+    metal = (rng.uniform(size=(n, 1)) < 0.3).astype(np.float64)
+    f0 = 0.04 + (base - 0.04) * metal
+    rough = rng.uniform(0.05, 1.0, (n, 1))
+    lit_in = np.concatenate([N, V, L, base, f0, rough], 1).astype(np.float32)
+    lit_out = np.zeros((n, 3), np.float32)
+    R.ref_eval_lit(lit_in.ctypes.data, n, lit_out.ctypes.data)
+    # VNDF sample + pdf: local view on the upper hemisphere
+    v = unit(rng.normal(size=(n, 3)))
+    v[:, 2] = np.abs(v[:, 2]) + 1e-3
+    v = unit(v)
+    r = rng.uniform(0.05, 1.0, n) ** 2
+    r = np.maximum(r, 0.001)
+    u = rng.uniform(0.0, 1.0, (n, 2))
+    vndf_in = np.concatenate([v, r[:, None], r[:, None], u], 1).astype(np.float32)
+    vndf_out = np.zeros((n, 4), np.float32)
+    R.ref_vndf(vndf_in.ctypes.data, n, vndf_out.ctypes.data)
+    # frames
+    fr_in = unit(rng.normal(size=(n, 3))).astype(np.float32)
+    fr_out = np.zeros((n, 6), np.float32)
+    R.ref_frame(fr_in.ctypes.data, n, fr_out.ctypes.data)
+    # anisotropic roughness (anisotropy 0) and samplers
+    an_in = rng.uniform(0.0, 1.0, n).astype(np.float32)
+    an_out = np.zeros((n, 2), np.float32)
+    R.ref_aniso(an_in.ctypes.data, n, an_out.ctypes.data)
+    sm_in = rng.uniform(0.0, 1.0, (n, 2)).astype(np.float32)
+    sm_out = np.zeros((n, 6), np.float32)
+    R.ref_samplers(sm_in.ctypes.data, n, sm_out.ctypes.data)
+    inv_pi = np.float32(R.ref_inv_pi())
+    out = os.path.join(HERE, "bsdf_golden.npz")
+    np.savez_compressed(out, lit_in=lit_in, lit_out=lit_out, vndf_in=vndf_in, vndf_out=vndf_out, frame_in=fr_in,
+                        frame_out=fr_out, aniso_in=an_in, aniso_out=an_out, samplers_in=sm_in,
+                        samplers_out=sm_out, inv_pi=inv_pi)
+    print("wrote", out, os.path.getsize(out), "bytes")
+
+
+if __name__ == "__main__":
+    R_ = C  # keep ctypes imported for the loaded library's argtypes
+    main()
