@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--grid", type=int, default=512)
     p.add_argument("--spheres", type=int, default=2000)
     p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--block", type=int, default=0, help="threads per block of the traversal kernels (0 = tuned)")
+    p.add_argument("--capacity", type=int, default=0, help="wavefront paths per chunk (0 = automatic)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
@@ -242,7 +244,8 @@ def run_ours(a, dist: Dist):
     cam = scene.camera
     seed = a.seed + 1000 * dist.rank
     flags_timed = bsm.BSM_PT_STAGE_TIMING
-    s_timed = bsm.settings(spp=a.spp, max_segments=a.segments, seed=seed, flags=flags_timed)
+    s_timed = bsm.settings(spp=a.spp, max_segments=a.segments, seed=seed, flags=flags_timed, block_size=a.block,
+                           wavefront_capacity=a.capacity)
 
     # traversal working set of this workload (counting variant, untimed)
     _, cst = ctx.render(sid, [cam], bsm.settings(spp=max(1, a.spp // 16), max_segments=a.segments, seed=seed,
@@ -300,7 +303,8 @@ def run_ours(a, dist: Dist):
     outs[0].row_pitch_px = 0
     outs[0].location = bsm.BSM_HOST
     cams = (bsm.Camera * 1)(cam)
-    s_e2e = bsm.settings(spp=a.spp, max_segments=a.segments, seed=seed)
+    s_e2e = bsm.settings(spp=a.spp, max_segments=a.segments, seed=seed, block_size=a.block,
+                         wavefront_capacity=a.capacity)
     ctx.check(L.bsm_render(ctx.h, sid, cams, 1, C.byref(s_e2e), outs, None))
     dist.barrier()
     e0 = time.perf_counter()
