@@ -139,6 +139,8 @@ _SIGS = {
     "bsm_trace_closest": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
     "bsm_trace_any": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
     "bsm_trace_counts": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "bsm_render_noalloc": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.POINTER(PtSettings),
+                                       C.c_void_p]),
     "bsm_scene_generate": (C.c_int32, [C.POINTER(SceneGenParams), C.POINTER(SceneDesc), C.POINTER(Camera)]),
     "bsm_scene_gen_free": (None, [C.POINTER(SceneDesc)]),
 }

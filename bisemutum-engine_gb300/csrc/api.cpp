@@ -902,3 +902,17 @@ extern "C" bsm_status bsm_trace_counts(bsm_context* ctx, uint32_t scene_id, cons
     CK(cudaStreamSynchronize(ctx->stream));
     return BSM_OK;
 }
+
+// ============================================ internals for other entry points ====
+namespace bsm {
+bool ctx_scene(bsm_context* ctx, uint32_t scene_id, DevScene* out) {
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc || !sc->has_bvh) return false;
+    *out = sc->dev;
+    return true;
+}
+cudaStream_t ctx_stream(bsm_context* ctx) { return ctx->stream; }
+int ctx_device(bsm_context* ctx) { return ctx->device; }
+void ctx_set_error(bsm_context* ctx, const char* msg) { ctx->err = msg; }
+void ctx_make_view(const bsm_camera* c, DevView* v) { make_view(*c, *v); }
+}  // namespace bsm

@@ -117,3 +117,16 @@ void launch_trace_count(cudaStream_t st, const DevScene& sc, const float4* rays,
 void query_launch_cfg(int device, int block_trace, LaunchCfg* lc);
 
 }  // namespace bsm
+
+struct bsm_context;
+struct bsm_camera;
+
+namespace bsm {
+// Context internals for entry points defined outside api.cpp.
+bool ctx_scene(bsm_context* ctx, uint32_t scene_id, DevScene* out);
+cudaStream_t ctx_stream(bsm_context* ctx);
+int ctx_device(bsm_context* ctx);
+void ctx_set_error(bsm_context* ctx, const char* msg);
+void ctx_make_view(const bsm_camera* c, DevView* v);
+
+}  // namespace bsm

@@ -259,6 +259,26 @@ BSM_API bsm_status bsm_trace_counts(bsm_context* ctx, uint32_t scene_id, const f
 BSM_API bsm_status bsm_host_alloc(bsm_context* ctx, uint64_t bytes, void** ptr);
 BSM_API bsm_status bsm_host_free(bsm_context* ctx, void* ptr);
 
+/* Renders one view without allocating any device memory.  No counterpart in
+ * the reference: it exists for callers that cannot call cudaMalloc while they
+ * render — an engine that owns all device memory through its own allocator and
+ * budget, a frame loop that must not take the synchronisation an allocation can
+ * cost, a host with a fixed memory arena.  The scene must already be resident
+ * (bsm_scene_upload + bsm_scene_build_bvh, done at set-up).  The working memory
+ * (queue counters, the view record, the wavefront queues) is one fixed 64 MiB
+ * device array inside the library, held by every GPU that loads it until the
+ * process exits; it bounds a chunk to wavefront_capacity paths (0 = the
+ * maximum, 279,552 paths for one light); a larger wavefront_capacity is
+ * rejected with BSM_ERR_INVALID_ARG.  Any image size works: paths run in chunks.
+ * `out_rgba` is a caller-owned device buffer of width*height RGBA floats,
+ * tightly packed; it receives the per-pixel sums and then the mean.  The first
+ * call on a device looks up the array's device address (set-up); make that
+ * first call before any stream capture.  All calls share the array and it
+ * keeps the last call's contents, so calls that overlap on the GPU race.  The
+ * call is asynchronous on the context's stream (bsm_sync waits for it). */
+BSM_API bsm_status bsm_render_noalloc(bsm_context* ctx, uint32_t scene_id, const bsm_camera* camera,
+                                      const bsm_pt_settings* settings, float* out_rgba);
+
 /* ---- synthetic scenes --------------------------------------------------- */
 
 enum {
