@@ -37,7 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Mrays/s (extend rays entering closest-hit) at 1 GB300, plain wavefront PT"
-DEV_VIEW_BYTES = 112  # bytes of the per-view record the render call uploads (DevView)
+DEV_VIEW_BYTES = 120  # bytes of the per-view record the render call uploads (DevView)
 EXTEND_BYTES_PER_RAY = 48  # 32 B ray read + 16 B hit written (compulsory HBM)
 NODE_BYTES, TRI_BYTES = 80, 48
 
@@ -57,6 +57,14 @@ def parse():
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--block", type=int, default=0, help="threads per block of the traversal kernels (0 = tuned)")
     p.add_argument("--capacity", type=int, default=0, help="wavefront paths per chunk (0 = automatic)")
+    p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve"],
+                   help="plain: the single-frame pass (the bench line); batch: 256 uneven views in one wavefront "
+                        "against a loop of plain renders")
+    p.add_argument("--views", type=int, default=256)
+    p.add_argument("--rates", default="10,50,100,200,500,1000,2000", help="serve: Poisson arrival rates (req/s)")
+    p.add_argument("--serve-seconds", type=float, default=6.0, help="serve: arrival window per rate")
+    p.add_argument("--max-requests", type=int, default=600, help="serve: cap on requests per rate")
+    p.add_argument("--tune-cache", default=None, help="autotuner cache file (batch workload)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
@@ -366,6 +374,148 @@ def run_ours(a, dist: Dist):
     return 0
 
 
+# ----------------------------------------------------------------- batch ----
+def batch_views(bsm, a):
+    """Uneven views of the terrain: side log-uniform in [64, 1024], spp in {4, 8, 16, 32, 64}."""
+    rng = np.random.default_rng(a.seed + 77)
+    views = []
+    for i in range(a.views):
+        side = int(round(float(np.exp(rng.uniform(np.log(64), np.log(1024))))))
+        spp = int(rng.choice([4, 8, 16, 32, 64]))
+        pos = (rng.uniform(0.15, 0.85), rng.uniform(0.35, 0.6), rng.uniform(-0.15, 0.35))
+        tgt = (rng.uniform(0.25, 0.75), 0.0, rng.uniform(0.45, 0.85))
+        cam = bsm.make_camera(pos, tuple(np.subtract(tgt, pos)), yfov_deg=60.0, width=side, height=side)
+        views.append((cam, spp, a.segments, a.seed + i))
+    return views
+
+
+def run_batch(a, dist):
+    bsm = importlib.import_module("bisemutum-engine_gb300")
+    scene = bsm.generate_scene(bsm.BSM_SCENE_TERRAIN, seed=a.seed, grid=a.grid, spheres=a.spheres)
+    ctx = bsm.Context(dist.local)
+    sid = ctx.load_scene(scene)
+    views = batch_views(bsm, a)
+    s = bsm.settings(max_segments=a.segments, spp=1)
+    t0 = time.perf_counter()
+    tune = ctx.autotune(sid, views, s, a.tune_cache)
+    tune_s = time.perf_counter() - t0
+    # batched: one wavefront over all views
+    ctx.render_batch(sid, views, s, outputs=False)
+    b_ms, b_rays = [], 0
+    for _ in range(a.steps):
+        _, st = ctx.render_batch(sid, views, s, outputs=False)
+        b_ms.append(st.ms_total)
+        b_rays += st.extend_rays
+    # plain: one render call per view (each replays its own captured graph)
+    for cam, spp, segs, seed in views[:4]:
+        ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=segs, seed=seed), outputs=False)
+    p_ms, p_wall, p_rays = 0.0, 0.0, 0
+    for _ in range(max(1, a.steps // 2)):
+        ctx.sync()
+        w0 = time.perf_counter()
+        for cam, spp, segs, seed in views:
+            _, st = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=segs, seed=seed), outputs=False)
+            p_ms += st.ms_total
+            p_rays += st.extend_rays
+        ctx.sync()
+        p_wall += time.perf_counter() - w0
+    p_steps = max(1, a.steps // 2)
+    # equal relMSE: both forms trace the same paths; compare the images of a sample of views
+    sample = views[:16]
+    imgs, _ = ctx.render_batch(sid, sample, s)
+    worst = 0.0
+    for (cam, spp, segs, seed), img in zip(sample, imgs):
+        alone, _ = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=segs, seed=seed))
+        g, c = img[..., :3].astype(np.float64), alone[0][..., :3].astype(np.float64)
+        worst = max(worst, float((np.abs(g - c) / np.maximum(np.abs(c), 1e-3)).max()))
+    ctx.close()
+    b_s = min(b_ms) / 1e3
+    p_s = p_ms / p_steps / 1e3
+    px = sum(v[0].width * v[0].height for v in views)
+    paths = sum(v[0].width * v[0].height * v[1] for v in views)
+    line = {"workload": "batch", "metric": "views/s at equal relMSE, batched vs one render per view",
+            "views": len(views), "pixels": px, "paths": paths,
+            "batched_views_per_s": round(len(views) / b_s, 2), "plain_views_per_s": round(len(views) / p_s, 2),
+            "plain_views_per_s_wall": round(len(views) * p_steps / p_wall, 2),
+            "speedup": round(p_s / b_s, 3),
+            "batched_mrays_per_s": round(b_rays / a.steps / b_s / 1e6, 1),
+            "plain_mrays_per_s": round(p_rays / p_steps / p_s / 1e6, 1),
+            "batch_ms": round(b_s * 1e3, 2), "plain_ms_device": round(p_s * 1e3, 2),
+            "equal_relmse_check": {"views_compared": len(sample), "max_rel_diff": worst},
+            "tune": {"block_size": tune.best.block_size, "wavefront_capacity": tune.best.wavefront_capacity,
+                     "postpone_depth": tune.best.postpone_depth, "refill_lanes": tune.best.refill_lanes,
+                     "best_ms": round(tune.best_ms, 3), "default_ms": round(tune.default_ms, 3),
+                     "tried": tune.tried, "from_cache": tune.from_cache, "seconds": round(tune_s, 2)},
+            "config": workload_config(a, scene.num_triangles)}
+    line["config"]["workload"] = (f"{len(views)} views of the terrain, side log-uniform 64..1024, "
+                                  f"spp in {{4,8,16,32,64}}, {a.segments} segments")
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------- serve ----
+def run_serve(a, dist):
+    """Poisson request stream over four resident scenes (20,504 / 250,050 / 1,482,242 / 4,973,058 triangles);
+    per request: scene uniform, resolution log-uniform 128x128..1920x1080, spp in {1,4,16,32}, bounces in
+    {2,4,8}.  Reports p50/p99 latency (submit -> result in host memory) and rays/s per arrival rate."""
+    bsm = importlib.import_module("bisemutum-engine_gb300")
+    ctx = bsm.Context(dist.local)
+    specs = [(bsm.BSM_SCENE_ROOM, 0, 64), (bsm.BSM_SCENE_TERRAIN, 256, 250), (bsm.BSM_SCENE_TERRAIN, 512, 2000),
+             (bsm.BSM_SCENE_TERRAIN, 1024, 6000)]
+    scenes, ids, tris = [], [], []
+    t0 = time.perf_counter()
+    for kind, grid, sph in specs:
+        sc = bsm.generate_scene(kind, seed=a.seed, grid=grid, spheres=sph)
+        scenes.append(sc)
+        ids.append(ctx.load_scene(sc))
+        tris.append(sc.num_triangles)
+    setup_s = time.perf_counter() - t0
+    rng = np.random.default_rng(a.seed + 5)
+    results = []
+    for lam in [float(x) for x in a.rates.split(",")]:
+        n = int(min(a.max_requests, max(20, lam * a.serve_seconds)))
+        ctx.server_start(pool_bytes=16 << 30, chunk_paths=1 << 21, lanes=4)
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, n))
+        reqs = []
+        for i in range(n):
+            k = int(rng.integers(0, 4))
+            u = float(rng.uniform())
+            w = int(round(128 * (1920 / 128) ** u))
+            h = int(round(128 * (1080 / 128) ** u))
+            base = scenes[k].camera
+            cam = bsm.make_camera(tuple(base.position), tuple(base.front), width=w, height=h)
+            reqs.append((ids[k], cam, int(rng.choice([1, 4, 16, 32])), int(rng.choice([2, 4, 8])), int(i + 1)))
+        start = time.perf_counter()
+        rids = []
+        for (sid, cam, spp, segs, seed), t_arr in zip(reqs, arrivals):
+            delay = start + t_arr - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            rids.append(ctx.submit(sid, cam, spp, segs, seed)[0])
+        lat = []
+        for rid in rids:
+            st = ctx.wait(rid, timeout_ms=600000)
+            lat.append(st.done_ms - st.submit_ms)
+        wall = time.perf_counter() - start
+        ss = ctx.server_stats()
+        ctx.server_stop()
+        lat = np.array(lat)
+        results.append({"rate_req_s": lam, "requests": n, "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                        "p99_ms": round(float(np.percentile(lat, 99)), 2),
+                        "mean_ms": round(float(lat.mean()), 2), "completed_req_s": round(n / wall, 2),
+                        "mrays_per_s": round(ss.extend_rays / wall / 1e6, 1), "wall_s": round(wall, 2)})
+    ctx.close()
+    line = {"workload": "serve", "metric": "p50/p99 request latency and rays/s per Poisson arrival rate",
+            "scenes_triangles": tris, "setup_s": round(setup_s, 1), "results": results,
+            "request_mix": "scene uniform, resolution log-uniform 128x128..1920x1080, spp {1,4,16,32}, "
+                           "bounces {2,4,8}", "server": {"pool_bytes": 16 << 30, "chunk_paths": 1 << 21,
+                                                          "lanes": 4}}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     a = parse()
     dist = Dist()
@@ -374,6 +524,10 @@ def main():
     try:
         if a.impl == "reference":
             return run_reference(a, dist)
+        if a.workload == "batch":
+            return run_batch(a, dist)
+        if a.workload == "serve":
+            return run_serve(a, dist)
         return run_ours(a, dist)
     finally:
         dist.close()

@@ -103,6 +103,45 @@ class RenderStats(C.Structure):
                 ("traversal_nodes", C.c_uint64), ("traversal_tris", C.c_uint64)]
 
 
+class ViewDesc(C.Structure):
+    _fields_ = [("camera", Camera), ("spp", C.c_uint32), ("max_segments", C.c_uint32), ("seed", C.c_uint64)]
+
+
+class TuneParams(C.Structure):
+    _fields_ = [("block_size", C.c_uint32), ("wavefront_capacity", C.c_uint32), ("postpone_depth", C.c_uint32),
+                ("refill_lanes", C.c_uint32)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("best", TuneParams), ("best_ms", C.c_float), ("default_ms", C.c_float), ("tried", C.c_uint32),
+                ("from_cache", C.c_uint32)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("pool_bytes", C.c_uint64), ("chunk_paths", C.c_uint32), ("lanes", C.c_uint32),
+                ("max_views_per_chunk", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("scene_id", C.c_uint32), ("camera", Camera), ("spp", C.c_uint32), ("max_segments", C.c_uint32),
+                ("seed", C.c_uint64), ("out_rgba", C.c_void_p)]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("reserved", C.c_uint32), ("submit_ms", C.c_double),
+                ("admit_ms", C.c_double), ("done_ms", C.c_double), ("paths", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
+                ("rejected", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("pool_bytes", C.c_uint64), ("pool_used_bytes", C.c_uint64), ("active", C.c_uint32),
+                ("queued", C.c_uint32), ("elapsed_ms", C.c_double)]
+
+
+BSM_REQ_QUEUED, BSM_REQ_RUNNING, BSM_REQ_DONE, BSM_REQ_FAILED = 0, 1, 2, 3
+
+
 class SceneGenParams(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("seed", C.c_uint64), ("grid", C.c_uint32), ("spheres", C.c_uint32),
                 ("sky_width", C.c_uint32), ("sky_height", C.c_uint32)]
@@ -132,6 +171,11 @@ _SIGS = {
     "bsm_pt_settings_default": (None, [C.POINTER(PtSettings)]),
     "bsm_render": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.c_uint32, C.POINTER(PtSettings),
                                C.POINTER(ViewOutput), C.POINTER(RenderStats)]),
+    "bsm_render_batch": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(ViewDesc), C.c_uint32,
+                                     C.POINTER(PtSettings), C.POINTER(ViewOutput), C.POINTER(RenderStats)]),
+    "bsm_autotune": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(ViewDesc), C.c_uint32, C.POINTER(PtSettings),
+                                 C.c_char_p, C.POINTER(TuneResult)]),
+    "bsm_set_tuning": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(TuneParams)]),
     "bsm_read_view": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(ViewOutput)]),
     "bsm_export_history": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32), C.c_uint32]),
     "bsm_import_history": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.c_void_p, C.c_uint32,
@@ -141,6 +185,12 @@ _SIGS = {
     "bsm_trace_counts": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]),
     "bsm_render_noalloc": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.POINTER(PtSettings),
                                        C.c_void_p]),
+    "bsm_server_start": (C.c_int32, [C.c_void_p, C.POINTER(ServerOpts)]),
+    "bsm_server_submit": (C.c_int32, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    "bsm_server_poll": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(RequestStatus)]),
+    "bsm_server_wait": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(RequestStatus)]),
+    "bsm_server_get_stats": (C.c_int32, [C.c_void_p, C.POINTER(ServerStats)]),
+    "bsm_server_stop": (C.c_int32, [C.c_void_p]),
     "bsm_scene_generate": (C.c_int32, [C.POINTER(SceneGenParams), C.POINTER(SceneDesc), C.POINTER(Camera)]),
     "bsm_scene_gen_free": (None, [C.POINTER(SceneDesc)]),
 }
@@ -395,6 +445,73 @@ class Context:
         self.check(self._L.bsm_render(self.h, scene_id, cams, n, C.byref(s), outs,
                                       C.byref(rs) if rs is not None else None))
         return imgs, rs
+
+    def render_batch(self, scene_id: int, views, s: PtSettings, outputs: bool = True, stats: bool = True):
+        """views: list of (Camera, spp, max_segments, seed); returns (images, RenderStats)."""
+        n = len(views)
+        descs = (ViewDesc * n)()
+        for i, (cam, spp, segs, seed) in enumerate(views):
+            descs[i].camera = cam
+            descs[i].spp, descs[i].max_segments, descs[i].seed = spp, segs, seed
+        outs, imgs = None, None
+        if outputs:
+            imgs = [np.zeros((v[0].height, v[0].width, 4), np.float32) for v in views]
+            outs = (ViewOutput * n)()
+            for i, im in enumerate(imgs):
+                outs[i].rgba = im.ctypes.data
+                outs[i].location = BSM_HOST
+        rs = RenderStats() if stats else None
+        self.check(self._L.bsm_render_batch(self.h, scene_id, descs, n, C.byref(s), outs,
+                                            C.byref(rs) if rs is not None else None))
+        return imgs, rs
+
+    def autotune(self, scene_id: int, views, s: PtSettings, cache_path: str | None = None) -> TuneResult:
+        n = len(views)
+        descs = (ViewDesc * n)()
+        for i, (cam, spp, segs, seed) in enumerate(views):
+            descs[i].camera = cam
+            descs[i].spp, descs[i].max_segments, descs[i].seed = spp, segs, seed
+        r = TuneResult()
+        self.check(self._L.bsm_autotune(self.h, scene_id, descs, n, C.byref(s),
+                                        cache_path.encode() if cache_path else None, C.byref(r)))
+        return r
+
+    def set_tuning(self, scene_id: int, params: TuneParams | None):
+        self.check(self._L.bsm_set_tuning(self.h, scene_id, C.byref(params) if params is not None else None))
+
+    # serving loop
+    def server_start(self, pool_bytes=0, chunk_paths=0, lanes=0, max_views_per_chunk=0):
+        self._reqs = {}
+        self.check(self._L.bsm_server_start(self.h, C.byref(ServerOpts(pool_bytes, chunk_paths, lanes,
+                                                                       max_views_per_chunk, 0))))
+
+    def submit(self, scene_id: int, cam: Camera, spp: int, max_segments: int = 8, seed: int = 1):
+        """Queues a request; returns (id, output array filled when the request is done)."""
+        out = np.zeros((cam.height, cam.width, 4), np.float32)
+        r = Request(scene_id, cam, spp, max_segments, seed, out.ctypes.data)
+        rid = C.c_uint64()
+        self.check(self._L.bsm_server_submit(self.h, C.byref(r), C.byref(rid)))
+        self._reqs[rid.value] = out
+        return rid.value, out
+
+    def wait(self, rid: int, timeout_ms: int = 0) -> RequestStatus:
+        st = RequestStatus()
+        self.check(self._L.bsm_server_wait(self.h, rid, timeout_ms, C.byref(st)))
+        return st
+
+    def poll(self, rid: int) -> RequestStatus:
+        st = RequestStatus()
+        self.check(self._L.bsm_server_poll(self.h, rid, C.byref(st)))
+        return st
+
+    def server_stats(self) -> ServerStats:
+        st = ServerStats()
+        self.check(self._L.bsm_server_get_stats(self.h, C.byref(st)))
+        return st
+
+    def server_stop(self):
+        self.check(self._L.bsm_server_stop(self.h))
+        self._reqs = {}
 
     def sync(self, timeout_ms: int = 0):
         self.check(self._L.bsm_sync(self.h, timeout_ms))

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -45,6 +46,8 @@ struct Scene {
     float extent = 1.0f;
     bool has_bvh = false;
     bsm_bvh_stats bvh_stats{};
+    bool tuned = false;
+    bsm_tune_params tune{};
     DevBuf nodes, tris, materials, texels, cdf_marg, cdf_cond, pdf_tab;
     DevScene dev{};
 };
@@ -89,6 +92,7 @@ struct bsm_context {
     cudaEvent_t ev[16] = {};
     std::vector<cudaEvent_t> stage_ev;
     std::mutex mu;
+    void* server = nullptr;       // serving loop (serve.cpp), null when not started
 };
 
 namespace {
@@ -268,6 +272,7 @@ extern "C" bsm_status bsm_create(bsm_context** out, int device, uint64_t budget)
 extern "C" void bsm_destroy(bsm_context* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
+    if (ctx->server) bsm_server_stop(ctx);
     cudaStreamSynchronize(ctx->stream);
     for (auto& g : ctx->graphs) if (g.exec) cudaGraphExecDestroy(g.exec);
     for (auto& kv : ctx->scenes) {
@@ -422,6 +427,8 @@ extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d
         ds.sky.pdf_tab = (const float*)sc->pdf_tab.ptr;
     }
     ds.ray_offset = 2e-5f * sc->extent;
+    if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
+    std::lock_guard<std::mutex> lk(ctx->mu);
     uint32_t id = ctx->next_scene++;
     ctx->scenes[id] = std::move(sc);
     *scene_id = id;
@@ -434,6 +441,7 @@ extern "C" bsm_status bsm_scene_build_bvh(bsm_context* ctx, uint32_t scene_id, c
     cudaSetDevice(ctx->device);
     Scene* sc = find_scene(ctx, scene_id);
     if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
+    if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
     BvhBuildResult r;
     std::string err;
     if (!build_cwbvh(sc->positions.data(), sc->indices.empty() ? nullptr : sc->indices.data(), sc->num_triangles,
@@ -501,6 +509,7 @@ extern "C" bsm_status bsm_scene_release(bsm_context* ctx, uint32_t scene_id) {
     cudaSetDevice(ctx->device);
     Scene* sc = find_scene(ctx, scene_id);
     if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
+    if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&sc->nodes, &sc->tris, &sc->materials, &sc->texels, &sc->cdf_marg, &sc->cdf_cond, &sc->pdf_tab})
         dev_free(ctx, *b);
@@ -586,22 +595,43 @@ void record_render(bsm_context* ctx, const Scene* sc, uint32_t n_views, uint64_t
 
 }  // namespace
 
-extern "C" bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_camera* views, uint32_t n_views,
-                                 const bsm_pt_settings* settings, const bsm_view_output* outputs,
-                                 bsm_render_stats* stats) {
-    if (!ctx || !views || n_views == 0 || !settings) return BSM_ERR_INVALID_ARG;
+namespace {
+
+// One view of a render call: camera plus the per-view sample count, segment
+// limit and seed (uniform for bsm_render, per view for bsm_render_batch).
+struct ViewReq {
+    bsm_camera cam;
+    uint32_t spp;
+    uint32_t max_seg;
+    uint64_t seed;
+};
+
+bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<ViewReq>& req,
+                       const bsm_pt_settings& s, const bsm_view_output* outputs, bsm_render_stats* stats) {
+    const uint32_t n_views = (uint32_t)req.size();
     cudaSetDevice(ctx->device);
     Scene* sc = find_scene(ctx, scene_id);
     if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
     if (!sc->has_bvh) return fail(ctx, BSM_ERR_BAD_STATE, "scene BVH not built (bsm_scene_build_bvh)");
-    const bsm_pt_settings& s = *settings;
-    if (s.spp == 0) return fail(ctx, BSM_ERR_INVALID_ARG, "spp must be >= 1");
-    uint32_t max_seg = s.max_segments ? s.max_segments : (std::min(std::max(s.max_bounces, 2u), 16u) - 1u);
-    if (max_seg == 0 || max_seg > (uint32_t)kMaxSeg) return fail(ctx, BSM_ERR_INVALID_ARG, "max_segments must be 1..16");
+    uint32_t max_seg = 0;
+    for (const ViewReq& r : req) {
+        if (r.spp == 0) return fail(ctx, BSM_ERR_INVALID_ARG, "spp must be >= 1");
+        if (r.max_seg == 0 || r.max_seg > (uint32_t)kMaxSeg)
+            return fail(ctx, BSM_ERR_INVALID_ARG, "max_segments must be 1..16");
+        max_seg = std::max(max_seg, r.max_seg);
+    }
     if (!(s.ray_length > 0.0f)) return fail(ctx, BSM_ERR_INVALID_ARG, "ray_length must be > 0");
     if (s.t_min < 0.0f) return fail(ctx, BSM_ERR_INVALID_ARG, "t_min must be >= 0");
     bsm_status st;
-    if ((st = ensure_launch_cfg(ctx, s.block_size))) return st;
+    // tuned parameters of this scene fill in what the settings leave at 0
+    uint32_t block = s.block_size ? s.block_size : (sc->tuned ? sc->tune.block_size : 0u);
+    if ((st = ensure_launch_cfg(ctx, block))) return st;
+    ctx->lc.postpone_sp = sc->tuned ? (int)sc->tune.postpone_depth : 16;
+    ctx->lc.refill_min = sc->tuned ? (int)sc->tune.refill_lanes : 8;
+    const bsm_camera* views = nullptr;
+    std::vector<bsm_camera> cams(n_views);
+    for (uint32_t v = 0; v < n_views; ++v) cams[v] = req[v].cam;
+    views = cams.data();
 
     // view layout and history (path_tracing.cpp:231-245: history kept per camera,
     // reset when it moves or the target changes size)
@@ -648,16 +678,17 @@ extern "C" bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_
         make_view(views[v], dv);
         dv.ray_length = s.ray_length;
         dv.t_min = s.t_min;
-        dv.spp = s.spp;
+        dv.spp = req[v].spp;
         dv.sample_offset = s.sample_offset + h.spp;
-        dv.seed = s.seed;
+        dv.seed = req[v].seed;
         dv.path_base = total_paths;
         dv.accum_base = h.accum_base;
-        dv.max_segments = max_seg;
+        dv.max_segments = req[v].max_seg;
         dv.flags = s.flags;
-        total_paths += (uint64_t)views[v].width * views[v].height * s.spp;
+        total_paths += (uint64_t)views[v].width * views[v].height * req[v].spp;
     }
-    uint32_t capacity = s.wavefront_capacity ? s.wavefront_capacity : (uint32_t)std::min<uint64_t>(total_paths, 1u << 23);
+    uint32_t cap_req = s.wavefront_capacity ? s.wavefront_capacity : (sc->tuned ? sc->tune.wavefront_capacity : 0u);
+    uint32_t capacity = cap_req ? cap_req : (uint32_t)std::min<uint64_t>(total_paths, 1u << 23);
     capacity = std::max(capacity, 1024u);
     if ((st = ensure_wavefront(ctx, capacity, std::max(sc->dev.num_lights, 1u)))) return st;
     capacity = std::min(capacity, ctx->wf.capacity);
@@ -676,8 +707,9 @@ extern "C" bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_
     if (use_graph) {
         // key: everything the recorded launches depend on
         std::vector<uint8_t> key(64);
-        uint64_t kv[8] = {(uint64_t)scene_id, (uint64_t)n_views, total_paths, capacity, max_seg,
-                          (uint64_t)(uintptr_t)ctx->wf_buf.ptr, (uint64_t)(uintptr_t)ctx->accum.ptr,
+        uint64_t kv[8] = {(uint64_t)scene_id, (uint64_t)n_views, total_paths,
+                          capacity | ((uint64_t)ctx->lc.postpone_sp << 32) | ((uint64_t)ctx->lc.refill_min << 40),
+                          max_seg, (uint64_t)(uintptr_t)ctx->wf_buf.ptr, (uint64_t)(uintptr_t)ctx->accum.ptr,
                           (uint64_t)(uintptr_t)ctx->views_dev.ptr ^ ((uint64_t)ctx->lc_block << 56)};
         std::memcpy(key.data(), kv, 64);
         cudaGraphExec_t exec = nullptr;
@@ -702,7 +734,7 @@ extern "C" bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[9], ctx->stream));
-    for (uint32_t v = 0; v < n_views; ++v) ctx->hist[v].spp += s.spp;
+    for (uint32_t v = 0; v < n_views; ++v) ctx->hist[v].spp += req[v].spp;
 
     // outputs: running mean
     bool host_out = false;
@@ -762,6 +794,177 @@ extern "C" bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_
         stats->ms_shadow = stage_ms[3];
         stats->traversal_nodes = h[kStatNodes];
         stats->traversal_tris = h[kStatTris];
+    }
+    return BSM_OK;
+}
+
+}  // namespace
+
+extern "C" bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_camera* views, uint32_t n_views,
+                                 const bsm_pt_settings* settings, const bsm_view_output* outputs,
+                                 bsm_render_stats* stats) {
+    if (!ctx || !views || n_views == 0 || !settings) return BSM_ERR_INVALID_ARG;
+    if (n_views > 65535) return fail(ctx, BSM_ERR_INVALID_ARG, "at most 65535 views per call");
+    const bsm_pt_settings& s = *settings;
+    uint32_t max_seg = s.max_segments ? s.max_segments : (std::min(std::max(s.max_bounces, 2u), 16u) - 1u);
+    std::vector<ViewReq> req(n_views);
+    for (uint32_t v = 0; v < n_views; ++v) req[v] = ViewReq{views[v], s.spp, max_seg, s.seed};
+    return render_impl(ctx, scene_id, req, s, outputs, stats);
+}
+
+extern "C" bsm_status bsm_render_batch(bsm_context* ctx, uint32_t scene_id, const bsm_view_desc* views,
+                                       uint32_t n_views, const bsm_pt_settings* settings,
+                                       const bsm_view_output* outputs, bsm_render_stats* stats) {
+    if (!ctx || !views || n_views == 0 || !settings) return BSM_ERR_INVALID_ARG;
+    if (n_views > 65535) return fail(ctx, BSM_ERR_INVALID_ARG, "at most 65535 views per call");
+    const bsm_pt_settings& s = *settings;
+    uint32_t def_seg = s.max_segments ? s.max_segments : (std::min(std::max(s.max_bounces, 2u), 16u) - 1u);
+    std::vector<ViewReq> req(n_views);
+    for (uint32_t v = 0; v < n_views; ++v)
+        req[v] = ViewReq{views[v].camera, views[v].spp ? views[v].spp : s.spp,
+                         views[v].max_segments ? views[v].max_segments : def_seg, views[v].seed ? views[v].seed : s.seed};
+    return render_impl(ctx, scene_id, req, s, outputs, stats);
+}
+
+// ============================================================ autotune ====
+namespace {
+
+bool valid_tune(const bsm_tune_params& p) {
+    return (p.block_size == 64 || p.block_size == 128 || p.block_size == 256) &&
+           (p.wavefront_capacity == 0 || p.wavefront_capacity >= 1024) && p.postpone_depth <= 16 &&
+           p.refill_lanes >= 1 && p.refill_lanes <= 32;
+}
+
+std::string tune_key(bsm_context* ctx, const Scene* sc, uint64_t paths) {
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, ctx->device);
+    int tri_bucket = 0, path_bucket = 0;
+    for (uint64_t x = sc->num_triangles; x > 1; x >>= 1) ++tri_bucket;
+    for (uint64_t x = paths; x > 1; x >>= 1) ++path_bucket;
+    std::string name = prop.name;
+    for (char& c : name) if (c == ' ' || c == '|') c = '_';
+    return name + "|sm" + std::to_string(prop.multiProcessorCount) + "|tri2^" + std::to_string(tri_bucket) +
+           "|paths2^" + std::to_string(path_bucket);
+}
+
+}  // namespace
+
+extern "C" bsm_status bsm_set_tuning(bsm_context* ctx, uint32_t scene_id, const bsm_tune_params* p) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
+    if (!p) { sc->tuned = false; return BSM_OK; }
+    if (!valid_tune(*p)) return fail(ctx, BSM_ERR_INVALID_ARG, "invalid tuning parameters");
+    sc->tune = *p;
+    sc->tuned = true;
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_autotune(bsm_context* ctx, uint32_t scene_id, const bsm_view_desc* views, uint32_t n_views,
+                                   const bsm_pt_settings* settings, const char* cache_path, bsm_tune_result* result) {
+    if (!ctx || !views || n_views == 0 || !settings || !result) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc || !sc->has_bvh) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene or BVH not built");
+    const bsm_pt_settings& s0 = *settings;
+    uint32_t def_seg = s0.max_segments ? s0.max_segments : (std::min(std::max(s0.max_bounces, 2u), 16u) - 1u);
+    std::vector<ViewReq> req(n_views);
+    uint64_t paths = 0;
+    for (uint32_t v = 0; v < n_views; ++v) {
+        uint32_t spp = views[v].spp ? views[v].spp : s0.spp;
+        req[v] = ViewReq{views[v].camera, std::max(1u, spp / 16), views[v].max_segments ? views[v].max_segments : def_seg,
+                         views[v].seed ? views[v].seed : s0.seed};
+        paths += (uint64_t)views[v].camera.width * views[v].camera.height * req[v].spp;
+    }
+    std::memset(result, 0, sizeof(*result));
+    std::string key = tune_key(ctx, sc, paths);
+    if (cache_path) {
+        FILE* f = std::fopen(cache_path, "r");
+        if (f) {
+            char line[512];
+            while (std::fgets(line, sizeof(line), f)) {
+                char k[400];
+                bsm_tune_params p{};
+                float ms = 0.0f;
+                if (std::sscanf(line, "%399s %u %u %u %u %f", k, &p.block_size, &p.wavefront_capacity,
+                                &p.postpone_depth, &p.refill_lanes, &ms) == 6 && key == k && valid_tune(p)) {
+                    result->best = p;
+                    result->best_ms = ms;
+                    result->from_cache = 1;
+                }
+            }
+            std::fclose(f);
+            if (result->from_cache) {
+                sc->tune = result->best;
+                sc->tuned = true;
+                return BSM_OK;
+            }
+        }
+    }
+    bsm_pt_settings s = s0;
+    s.flags &= ~(uint32_t)(BSM_PT_STAGE_TIMING | BSM_PT_COUNT_TRAVERSAL | BSM_PT_NO_GRAPH);
+    s.accumulate = 0;
+    s.block_size = 0;
+    s.wavefront_capacity = 0;
+    bool had = sc->tuned;
+    bsm_tune_params saved = sc->tune;
+    auto measure = [&](const bsm_tune_params& p, float* ms_out) -> bsm_status {
+        sc->tune = p;
+        sc->tuned = true;
+        bsm_render_stats st{};
+        bsm_status e = render_impl(ctx, scene_id, req, s, nullptr, &st);  // captures the graph
+        if (e) return e;
+        float best = 1e30f;
+        for (int r = 0; r < 2; ++r) {
+            e = render_impl(ctx, scene_id, req, s, nullptr, &st);
+            if (e) return e;
+            best = std::min(best, st.ms_total);
+        }
+        *ms_out = best;
+        result->tried++;
+        return BSM_OK;
+    };
+    bsm_tune_params cur{128, 0, 16, 8};
+    float cur_ms = 0.0f;
+    bsm_status e = measure(cur, &cur_ms);
+    if (e) { sc->tune = saved; sc->tuned = had; return e; }
+    result->default_ms = cur_ms;
+    const uint32_t blocks[] = {64, 128, 256};
+    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
+    const uint32_t postpones[] = {0, 4, 8, 16};
+    const uint32_t refills[] = {4, 8, 16, 24};
+    for (int pass = 0; pass < 2; ++pass) {
+        bool improved = false;
+        auto try_one = [&](bsm_tune_params p) -> bsm_status {
+            float ms;
+            bsm_status e2 = measure(p, &ms);
+            if (e2) return e2;
+            if (ms < cur_ms * 0.995f) { cur = p; cur_ms = ms; improved = true; }
+            return BSM_OK;
+        };
+        for (uint32_t b : blocks) if (b != cur.block_size) { bsm_tune_params p = cur; p.block_size = b; if ((e = try_one(p))) break; }
+        for (uint32_t c : caps) {
+            if (e) break;
+            if ((uint64_t)c > paths * 2 || c == cur.wavefront_capacity) continue;
+            bsm_tune_params p = cur; p.wavefront_capacity = c;
+            e = try_one(p);
+        }
+        for (uint32_t v : postpones) { if (e) break; if (v != cur.postpone_depth) { bsm_tune_params p = cur; p.postpone_depth = v; e = try_one(p); } }
+        for (uint32_t v : refills) { if (e) break; if (v != cur.refill_lanes) { bsm_tune_params p = cur; p.refill_lanes = v; e = try_one(p); } }
+        if (e) { sc->tune = saved; sc->tuned = had; return e; }
+        if (!improved) break;
+    }
+    sc->tune = cur;
+    sc->tuned = true;
+    result->best = cur;
+    result->best_ms = cur_ms;
+    if (cache_path) {
+        FILE* f = std::fopen(cache_path, "a");
+        if (f) {
+            std::fprintf(f, "%s %u %u %u %u %.4f\n", key.c_str(), cur.block_size, cur.wavefront_capacity,
+                         cur.postpone_depth, cur.refill_lanes, cur_ms);
+            std::fclose(f);
+        }
     }
     return BSM_OK;
 }
@@ -906,6 +1109,7 @@ extern "C" bsm_status bsm_trace_counts(bsm_context* ctx, uint32_t scene_id, cons
 // ============================================ internals for other entry points ====
 namespace bsm {
 bool ctx_scene(bsm_context* ctx, uint32_t scene_id, DevScene* out) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
     Scene* sc = find_scene(ctx, scene_id);
     if (!sc || !sc->has_bvh) return false;
     *out = sc->dev;
@@ -915,4 +1119,10 @@ cudaStream_t ctx_stream(bsm_context* ctx) { return ctx->stream; }
 int ctx_device(bsm_context* ctx) { return ctx->device; }
 void ctx_set_error(bsm_context* ctx, const char* msg) { ctx->err = msg; }
 void ctx_make_view(const bsm_camera* c, DevView* v) { make_view(*c, *v); }
+void*& ctx_server_slot(bsm_context* ctx) { return ctx->server; }
+uint32_t ctx_max_lights(bsm_context* ctx) {
+    uint32_t m = 1;
+    for (auto& kv : ctx->scenes) m = std::max(m, kv.second->dev.num_lights);
+    return m;
+}
 }  // namespace bsm

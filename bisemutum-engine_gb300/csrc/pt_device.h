@@ -57,6 +57,7 @@ struct DevView {
     uint32_t max_segments;
     uint32_t flags;            // BSM_PT_* bits that reach the device
     uint32_t pad;
+    uint64_t first_path;       // index (within the view) of the path at path_base; >0 when a view is split
 };
 
 // counters[] word offsets
@@ -95,6 +96,8 @@ struct LaunchCfg {
     int block_trace;        // threads per block, traversal
     int block_shade;        // threads per block, shading / camera
     int grid_shade;
+    int postpone_sp = 16;   // traversal stack budget for postponed triangle groups
+    int refill_min = 8;     // idle lanes that trigger a warp refill
 };
 
 // ---- launch wrappers (pt_kernels.cu) ----
@@ -128,5 +131,7 @@ cudaStream_t ctx_stream(bsm_context* ctx);
 int ctx_device(bsm_context* ctx);
 void ctx_set_error(bsm_context* ctx, const char* msg);
 void ctx_make_view(const bsm_camera* c, DevView* v);
+void*& ctx_server_slot(bsm_context* ctx);
+uint32_t ctx_max_lights(bsm_context* ctx);
 
 }  // namespace bsm

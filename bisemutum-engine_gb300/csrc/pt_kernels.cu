@@ -52,7 +52,7 @@ __global__ void k_camera(const DevView* __restrict__ views, uint32_t n_views, ui
         if (views[mid].path_base <= p) lo = mid; else hi = mid - 1;
     }
     const DevView& v = views[lo];
-    uint64_t local = p - v.path_base;
+    uint64_t local = p - v.path_base + v.first_path;
     uint32_t npix = v.width * v.height;
     uint32_t sample = (uint32_t)(local / npix);
     uint32_t pixel = (uint32_t)(local - (uint64_t)sample * npix);
@@ -81,7 +81,8 @@ __global__ void k_camera(const DevView* __restrict__ views, uint32_t n_views, ui
 template <bool kCount>
 __global__ void __launch_bounds__(256) k_extend(DevScene sc, const float4* __restrict__ ray_o,
                                                 const float4* __restrict__ ray_d, float4* __restrict__ hit,
-                                                uint32_t* counters, unsigned long long* stats, uint32_t seg) {
+                                                uint32_t* counters, unsigned long long* stats, uint32_t seg,
+                                                int postpone_sp, int refill_min) {
     uint32_t n = counters[kCntQueue + seg];
     if (blockIdx.x == 0 && threadIdx.x == 0) stats[kStatExtend + seg] += n;
     TraceCounters c{0, 0};
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(256) k_extend(DevScene sc, const float4* __res
         [&](uint32_t i, uint32_t leaf, float t, float u, float v) {
             hit[i] = make_float4(t, __uint_as_float(leaf), u, v);
         },
-        &c);
+        &c, postpone_sp, refill_min);
     if (kCount) {
         uint32_t cn = c.nodes, ct = c.tris;
         for (int off = 16; off > 0; off >>= 1) {
@@ -106,7 +107,8 @@ __global__ void __launch_bounds__(256) k_extend(DevScene sc, const float4* __res
 }
 
 // ---------------------------------------------------------------- shadow ----
-__global__ void __launch_bounds__(256) k_shadow(DevScene sc, Wavefront wf, uint32_t seg, float4* accum) {
+__global__ void __launch_bounds__(256) k_shadow(DevScene sc, Wavefront wf, uint32_t seg, float4* accum,
+                                                int postpone_sp, int refill_min) {
     uint32_t n = wf.counters[kCntShadow + seg];
     if (blockIdx.x == 0 && threadIdx.x == 0) wf.stats[kStatShadow + seg] += n;
     const float4* __restrict__ so = wf.sh_o;
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(256) k_shadow(DevScene sc, Wavefront wf, uint3
                 accum_add(accum, __float_as_uint(c.w), v3(c.x, c.y, c.z));
             }
         },
-        nullptr);
+        nullptr, postpone_sp, refill_min);
 }
 
 // ----------------------------------------------------------------- shade ----
@@ -358,10 +360,12 @@ void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, con
                    uint32_t seg, bool count_traversal) {
     if (count_traversal)
         k_extend<true><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
-                                                                        wf.counters, wf.stats, seg);
+                                                                        wf.counters, wf.stats, seg, lc.postpone_sp,
+                                                                        lc.refill_min);
     else
         k_extend<false><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
-                                                                         wf.counters, wf.stats, seg);
+                                                                         wf.counters, wf.stats, seg, lc.postpone_sp,
+                                                                         lc.refill_min);
 }
 void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const DevView* views,
                   const Wavefront& wf, int q, uint32_t seg, float4* accum) {
@@ -369,7 +373,7 @@ void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, cons
 }
 void launch_shadow(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, uint32_t seg,
                    float4* accum) {
-    k_shadow<<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum);
+    k_shadow<<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp, lc.refill_min);
 }
 void launch_resolve(cudaStream_t st, const float4* accum, uint32_t width, uint32_t height, float inv_spp,
                     float4* out, uint32_t pitch_px) {

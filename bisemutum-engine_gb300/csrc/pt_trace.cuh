@@ -32,7 +32,7 @@ namespace bsm {
 // rounding of the slab arithmetic never culls a box that holds a hit.
 #define BSM_BOX_PAD 1.00000095f
 constexpr int kStackSize = 40;        // node groups (<= tree depth) + postponed triangle groups
-constexpr int kPostponeMaxSp = 16;    // postpone triangle groups only below this stack depth
+constexpr int kPostponeMaxSp = 16;    // largest stack budget for postponed triangle groups
 
 struct RayPre {
     float ox, oy, oz, tmin;
@@ -254,10 +254,14 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // (index -> (origin/tmin, direction/tmax)) supplies rays; `finish(index, leaf,
 // t, u, v)` receives each result (leaf = kMissPrim on a miss; for any-hit the
 // first hit found).
+// `postpone_sp` (<= kPostponeMaxSp) is the stack depth below which triangle
+// groups may be postponed (0 disables postponing); `refill_min` is the number
+// of idle lanes that makes the warp fetch new rays.  Both are tuning knobs.
 template <bool kAnyHit, bool kCount, class Load, class Finish>
 __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, const CwTri* __restrict__ tris,
                                             uint32_t n, uint32_t* work, Load load, Finish finish,
-                                            TraceCounters* cnt) {
+                                            TraceCounters* cnt, int postpone_sp, int refill_min) {
+    postpone_sp = postpone_sp < kPostponeMaxSp ? postpone_sp : kPostponeMaxSp;
     const uint32_t lane = threadIdx.x & 31u;
     bool has = false;
     bool exhausted = false;  // warp-uniform
@@ -270,7 +274,7 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
     while (true) {
         // refill lanes whose ray finished (one atomic per warp)
         uint32_t idle = __ballot_sync(0xffffffffu, !has);
-        if (!exhausted && (__popc(idle) >= 8 || idle == 0xffffffffu)) {
+        if (!exhausted && (__popc(idle) >= refill_min || idle == 0xffffffffu)) {
             uint32_t cntn = (uint32_t)__popc(idle);
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(work, cntn);
@@ -317,7 +321,7 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
             if (m == 0u) break;
             uint32_t act = __ballot_sync(0xffffffffu, has);
             if (__popc(m) * 4 < __popc(act)) {
-                if (want && sp < kPostponeMaxSp) { stack[sp++] = T; T.y = 0u; }
+                if (want && sp < postpone_sp) { stack[sp++] = T; T.y = 0u; }
                 if (__ballot_sync(0xffffffffu, has && T.y != 0u) == 0u) break;
                 want = has && T.y != 0u;
             }

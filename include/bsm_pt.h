@@ -227,6 +227,54 @@ typedef struct bsm_render_stats {
 BSM_API bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_camera* views, uint32_t n_views,
                               const bsm_pt_settings* settings, const bsm_view_output* outputs,
                               bsm_render_stats* stats);
+/* One view of a batched render: its camera, samples per pixel, segment limit
+ * and seed (0 = the value in the settings). */
+typedef struct bsm_view_desc {
+    bsm_camera camera;
+    uint32_t spp;
+    uint32_t max_segments;
+    uint64_t seed;
+} bsm_view_desc;
+
+/* Renders many views of different sizes and sample counts in one wavefront:
+ * all views' paths share the queues and one CUDA graph replays the whole
+ * bounce loop.  Each view's result equals a bsm_render of that view alone with
+ * the same spp, segments and seed (same paths; per-pixel sums in another
+ * order).  Replaces a loop of PathTracingPass::render over cameras
+ * (graphics_manager.cpp:407-427 runs one per enabled camera). */
+BSM_API bsm_status bsm_render_batch(bsm_context* ctx, uint32_t scene_id, const bsm_view_desc* views,
+                                    uint32_t n_views, const bsm_pt_settings* settings,
+                                    const bsm_view_output* outputs, bsm_render_stats* stats);
+
+/* Launch parameters the autotuner chooses. */
+typedef struct bsm_tune_params {
+    uint32_t block_size;          /* threads per block of the traversal kernels: 64, 128 or 256 */
+    uint32_t wavefront_capacity;  /* paths per chunk (queue capacity) */
+    uint32_t postpone_depth;      /* traversal stack entries open to postponed triangle groups (0..16) */
+    uint32_t refill_lanes;        /* idle lanes that make a warp fetch new rays (1..32) */
+} bsm_tune_params;
+
+typedef struct bsm_tune_result {
+    bsm_tune_params best;
+    float best_ms;                /* device time of the tuning workload with `best` */
+    float default_ms;             /* ... with the built-in defaults */
+    uint32_t tried;               /* configurations timed (0 when read from the cache file) */
+    uint32_t from_cache;
+} bsm_tune_result;
+
+/* Picks block size, queue capacity and traversal stack budget for a scene and
+ * a workload (views + settings) by timing short renders (each view at
+ * max(1, spp / 16) samples), coordinate descent over the four parameters.  The
+ * result is kept for the scene (used whenever the settings leave these fields
+ * at 0) and, when `cache_path` is not NULL, appended to that text file keyed
+ * by GPU name, SM count, scene size and path count, and read back from it on
+ * later calls.  No reference counterpart (the driver picks these for its RT
+ * pipeline). */
+BSM_API bsm_status bsm_autotune(bsm_context* ctx, uint32_t scene_id, const bsm_view_desc* views, uint32_t n_views,
+                                const bsm_pt_settings* settings, const char* cache_path, bsm_tune_result* result);
+/* Sets a scene's launch parameters by hand (NULL clears them). */
+BSM_API bsm_status bsm_set_tuning(bsm_context* ctx, uint32_t scene_id, const bsm_tune_params* params);
+
 /* Reads the current mean of a view's history into `out`. */
 BSM_API bsm_status bsm_read_view(bsm_context* ctx, uint32_t view_index, const bsm_view_output* out);
 /* Exports / imports a view's raw history (sum RGB + sample count) so a render
@@ -278,6 +326,61 @@ BSM_API bsm_status bsm_host_free(bsm_context* ctx, void* ptr);
  * call is asynchronous on the context's stream (bsm_sync waits for it). */
 BSM_API bsm_status bsm_render_noalloc(bsm_context* ctx, uint32_t scene_id, const bsm_camera* camera,
                                       const bsm_pt_settings* settings, float* out_rgba);
+
+/* ---- serving: resident scenes, requests admitted by memory, continuous batching ---- */
+
+typedef struct bsm_server_opts {
+    uint64_t pool_bytes;          /* accumulator pool: admission budget (16 B per pixel); 0 = 1 GiB */
+    uint32_t chunk_paths;         /* paths per in-flight chunk (queue capacity of a lane); 0 = 2^21 */
+    uint32_t lanes;               /* chunks in flight at once, one CUDA stream each; 0 = 4 */
+    uint32_t max_views_per_chunk; /* request ranges one chunk can hold; 0 = 256 */
+    uint32_t reserved;
+} bsm_server_opts;
+
+typedef struct bsm_request {
+    uint32_t scene_id;
+    bsm_camera camera;            /* at most 1920 x 1080 pixels */
+    uint32_t spp;
+    uint32_t max_segments;        /* 0 = 8 */
+    uint64_t seed;
+    float* out_rgba;              /* host buffer of width*height RGBA floats, written when done;
+                                     must stay valid until the request is done */
+} bsm_request;
+
+enum { BSM_REQ_QUEUED = 0, BSM_REQ_RUNNING = 1, BSM_REQ_DONE = 2, BSM_REQ_FAILED = 3 };
+
+typedef struct bsm_request_status {
+    uint32_t state;               /* BSM_REQ_* */
+    uint32_t reserved;
+    double submit_ms, admit_ms, done_ms;  /* since bsm_server_start */
+    uint64_t paths;
+} bsm_request_status;
+
+typedef struct bsm_server_stats {
+    uint64_t submitted, admitted, completed, rejected;
+    uint64_t extend_rays, shadow_rays;
+    uint64_t pool_bytes, pool_used_bytes;
+    uint32_t active, queued;
+    double elapsed_ms;
+} bsm_server_stats;
+
+/* Starts the serving loop on a context: a worker thread that admits requests
+ * in arrival order as accumulator memory frees up and packs the paths of all
+ * admitted requests of a scene into shared wavefront chunks, several chunks in
+ * flight on separate streams.  A request's image equals bsm_render of the same
+ * camera, spp, segments and seed.  Scenes must not be uploaded or released
+ * while the server runs.  No reference counterpart (the engine renders its
+ * cameras once per window frame, graphics_manager.cpp:407-427). */
+BSM_API bsm_status bsm_server_start(bsm_context* ctx, const bsm_server_opts* opts);
+/* Queues a request; BSM_ERR_ADMISSION if it can never fit the pool. */
+BSM_API bsm_status bsm_server_submit(bsm_context* ctx, const bsm_request* request, uint64_t* request_id);
+BSM_API bsm_status bsm_server_poll(bsm_context* ctx, uint64_t request_id, bsm_request_status* status);
+/* Waits for a request (timeout_ms = 0: no limit); BSM_ERR_TIMEOUT when it runs out. */
+BSM_API bsm_status bsm_server_wait(bsm_context* ctx, uint64_t request_id, uint32_t timeout_ms,
+                                   bsm_request_status* status);
+BSM_API bsm_status bsm_server_get_stats(bsm_context* ctx, bsm_server_stats* stats);
+/* Stops the worker after the chunks in flight; queued requests are dropped. */
+BSM_API bsm_status bsm_server_stop(bsm_context* ctx);
 
 /* ---- synthetic scenes --------------------------------------------------- */
 
