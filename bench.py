@@ -57,13 +57,15 @@ def parse():
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--block", type=int, default=0, help="threads per block of the traversal kernels (0 = tuned)")
     p.add_argument("--capacity", type=int, default=0, help="wavefront paths per chunk (0 = automatic)")
-    p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve"],
+    p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "cache"],
                    help="plain: the single-frame pass (the bench line); batch: 256 uneven views in one wavefront "
                         "against a loop of plain renders")
     p.add_argument("--views", type=int, default=256)
     p.add_argument("--rates", default="10,50,100,200,500,1000,2000", help="serve: Poisson arrival rates (req/s)")
     p.add_argument("--serve-seconds", type=float, default=6.0, help="serve: arrival window per rate")
     p.add_argument("--max-requests", type=int, default=600, help="serve: cap on requests per rate")
+    p.add_argument("--ref-spp", type=int, default=4096, help="cache: spp of the plain reference render")
+    p.add_argument("--train-frames", type=int, default=120, help="cache: online training frames before timing")
     p.add_argument("--tune-cache", default=None, help="autotuner cache file (batch workload)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -516,6 +518,83 @@ def run_serve(a, dist):
     return 0
 
 
+# ----------------------------------------------------------------- cache ----
+def run_cache(a, dist):
+    """Radiance cache on the terrain scene: relMSE against a high-spp plain render and device time per frame,
+    for the plain pass (8 segments) and the cached pass (paths end in the cache at their third vertex; the cache
+    keeps training online, 65,536 training paths and 4 Adam steps of 16,384 vertices per frame, counted in its
+    frame time), then frames/s of each at equal relMSE."""
+    bsm = importlib.import_module("bisemutum-engine_gb300")
+    scene = bsm.generate_scene(bsm.BSM_SCENE_TERRAIN, seed=a.seed, grid=a.grid, spheres=a.spheres, width=a.width,
+                               height=a.height)
+    ctx = bsm.Context(dist.local)
+    sid = ctx.load_scene(scene)
+    cam = scene.camera
+    # reference: ref_spp in progressive calls of 256
+    per = min(256, a.ref_spp)
+    ctx.render(sid, [cam], bsm.settings(spp=per, max_segments=a.segments, seed=90000, accumulate=0), outputs=False)
+    for k in range(1, a.ref_spp // per):
+        last = k == a.ref_spp // per - 1
+        imgs, _ = ctx.render(sid, [cam], bsm.settings(spp=per, max_segments=a.segments, seed=90000, accumulate=1),
+                             outputs=last)
+    ref = imgs[0] if a.ref_spp > per else ctx.render(sid, [cam], bsm.settings(spp=per, max_segments=a.segments,
+                                                                              seed=90000))[0][0]
+    spps = [1, 2, 4, 8, 16, 32]
+    plain = []
+    for spp in spps:
+        ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=a.segments, seed=5 + spp), outputs=False)
+        img, st = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=a.segments, seed=7 + spp))
+        plain.append({"spp": spp, "relmse": bsm.rel_mse(img[0], ref), "ms": st.ms_total})
+    cache = bsm.RadianceCache(ctx, seed=a.seed)
+    cs = bsm.cache_settings()
+    t0 = time.perf_counter()
+    losses = []
+    for f in range(a.train_frames):
+        _, _, loss = cache.render(sid, cam, bsm.settings(spp=1, seed=1000 + f), cs, outputs=False)
+        losses.append(loss)
+    train_s = time.perf_counter() - t0
+    cached = []
+    for spp in spps:
+        ctx.sync()
+        w0 = time.perf_counter()
+        img, st, _ = cache.render(sid, cam, bsm.settings(spp=spp, seed=3000 + spp), cs)   # trains, then renders
+        wall = (time.perf_counter() - w0) * 1e3
+        cached.append({"spp": spp, "relmse": bsm.rel_mse(img, ref), "ms": wall, "ms_render": st.ms_total})
+    cache.close()
+    ctx.close()
+
+    def time_at(curve, target):
+        """Frame time needed to reach `target` relMSE (log-log interpolation; None if never reached)."""
+        pts = sorted((c["relmse"], c["ms"]) for c in curve)
+        for (e0, t0_), (e1, t1) in zip(pts[1:], pts[:-1]):
+            pass
+        xs = [c["relmse"] for c in curve]
+        ts = [c["ms"] for c in curve]
+        for i in range(len(curve) - 1):
+            e0, e1 = xs[i], xs[i + 1]
+            if (e0 - target) * (e1 - target) <= 0 and e0 != e1:
+                u = (np.log(target) - np.log(e0)) / (np.log(e1) - np.log(e0))
+                return float(np.exp(np.log(ts[i]) + u * (np.log(ts[i + 1]) - np.log(ts[i]))))
+        return None
+    equal = []
+    for c in cached:
+        tp = time_at(plain, c["relmse"])
+        equal.append({"relmse": round(c["relmse"], 6), "cached_fps": round(1e3 / c["ms"], 2),
+                      "plain_fps": round(1e3 / tp, 2) if tp else None,
+                      "speedup": round(tp / c["ms"], 3) if tp else None})
+    line = {"workload": "cache", "metric": "frames/s at equal relMSE, cached vs plain pass",
+            "reference_spp": a.ref_spp, "plain": plain, "cached": cached, "equal_relmse": equal,
+            "train": {"frames": a.train_frames, "seconds": round(train_s, 2),
+                      "loss_first10": round(float(np.mean(losses[:10])), 4),
+                      "loss_last10": round(float(np.mean(losses[-10:])), 4),
+                      "per_frame": "65536 training paths, 4 Adam steps of 16384 vertices, lr 1e-2"},
+            "config": workload_config(a, scene.num_triangles)}
+    line["config"]["workload"] = f"radiance cache on the terrain scene, {a.width}x{a.height}, cache after 2 bounces"
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     a = parse()
     dist = Dist()
@@ -528,6 +607,8 @@ def main():
             return run_batch(a, dist)
         if a.workload == "serve":
             return run_serve(a, dist)
+        if a.workload == "cache":
+            return run_cache(a, dist)
         return run_ours(a, dist)
     finally:
         dist.close()

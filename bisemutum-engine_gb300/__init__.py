@@ -142,6 +142,11 @@ class ServerStats(C.Structure):
 BSM_REQ_QUEUED, BSM_REQ_RUNNING, BSM_REQ_DONE, BSM_REQ_FAILED = 0, 1, 2, 3
 
 
+class CacheSettings(C.Structure):
+    _fields_ = [("cache_segment", C.c_uint32), ("train_paths", C.c_uint32), ("train_segments", C.c_uint32),
+                ("train_batch", C.c_uint32), ("train_steps", C.c_uint32), ("lr", C.c_float)]
+
+
 class SceneGenParams(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("seed", C.c_uint64), ("grid", C.c_uint32), ("spheres", C.c_uint32),
                 ("sky_width", C.c_uint32), ("sky_height", C.c_uint32)]
@@ -191,6 +196,20 @@ _SIGS = {
     "bsm_server_wait": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(RequestStatus)]),
     "bsm_server_get_stats": (C.c_int32, [C.c_void_p, C.POINTER(ServerStats)]),
     "bsm_server_stop": (C.c_int32, [C.c_void_p]),
+    "bsm_cache_settings_default": (None, [C.POINTER(CacheSettings)]),
+    "bsm_cache_param_count": (C.c_uint32, []),
+    "bsm_cache_create": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "bsm_cache_destroy": (None, [C.c_void_p]),
+    "bsm_cache_weights": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "bsm_cache_predict": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "bsm_cache_gradient": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)]),
+    "bsm_cache_train": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,
+                                    C.POINTER(C.c_float)]),
+    "bsm_cache_save": (C.c_int32, [C.c_void_p, C.c_char_p]),
+    "bsm_cache_load": (C.c_int32, [C.c_void_p, C.c_char_p]),
+    "bsm_render_cached": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.POINTER(PtSettings), C.c_void_p,
+                                      C.POINTER(CacheSettings), C.POINTER(ViewOutput), C.POINTER(RenderStats),
+                                      C.POINTER(C.c_float)]),
     "bsm_scene_generate": (C.c_int32, [C.POINTER(SceneGenParams), C.POINTER(SceneDesc), C.POINTER(Camera)]),
     "bsm_scene_gen_free": (None, [C.POINTER(SceneDesc)]),
 }
@@ -515,6 +534,90 @@ class Context:
 
     def sync(self, timeout_ms: int = 0):
         self.check(self._L.bsm_sync(self.h, timeout_ms))
+
+
+# ------------------------------------------------------- radiance cache ----
+def cache_settings(**kw) -> CacheSettings:
+    cs = CacheSettings()
+    lib().bsm_cache_settings_default(C.byref(cs))
+    for k, v in kw.items():
+        setattr(cs, k, v)
+    return cs
+
+
+class RadianceCache:
+    """The learned radiance cache (bsm_cache) of one context."""
+
+    def __init__(self, ctx: Context, seed: int = 1):
+        self.ctx = ctx
+        self._L = ctx._L
+        h = C.c_void_p()
+        ctx.check(self._L.bsm_cache_create(ctx.h, seed, C.byref(h)))
+        self.h = h
+        self.nparams = self._L.bsm_cache_param_count()
+
+    def close(self):
+        if self.h:
+            self._L.bsm_cache_destroy(self.h)
+            self.h = None
+
+    def _st(self, st):
+        if st != BSM_OK:
+            raise BsmError(st, "radiance cache call failed")
+
+    def weights(self, set_to: np.ndarray | None = None) -> np.ndarray:
+        w = np.zeros(self.nparams, np.float32)
+        src = None if set_to is None else np.ascontiguousarray(set_to, np.float32)
+        self._st(self._L.bsm_cache_weights(self.h, w.ctypes.data, None if src is None else src.ctypes.data))
+        return w if set_to is None else src
+
+    def predict(self, samples: np.ndarray) -> np.ndarray:
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 16)
+        out = np.zeros((s.shape[0], 3), np.float32)
+        self._st(self._L.bsm_cache_predict(self.h, s.ctypes.data, s.shape[0], out.ctypes.data))
+        return out
+
+    def gradient(self, samples: np.ndarray):
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 16)
+        dW = np.zeros(self.nparams, np.float32)
+        loss = C.c_float()
+        self._st(self._L.bsm_cache_gradient(self.h, s.ctypes.data, s.shape[0], dW.ctypes.data, C.byref(loss)))
+        return dW, loss.value
+
+    def train(self, samples: np.ndarray, batch: int = 16384, lr: float = 1e-2) -> float:
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 16)
+        loss = C.c_float()
+        self._st(self._L.bsm_cache_train(self.h, s.ctypes.data, s.shape[0], batch, lr, C.byref(loss)))
+        return loss.value
+
+    def save(self, path: str):
+        self._st(self._L.bsm_cache_save(self.h, path.encode()))
+
+    def load(self, path: str):
+        self._st(self._L.bsm_cache_load(self.h, path.encode()))
+
+    def render(self, scene_id: int, cam: Camera, s: PtSettings, cs: CacheSettings | None = None, outputs=True):
+        """One frame with the cache (training first when cs.train_steps > 0); returns (image, stats, loss)."""
+        cs = cs or cache_settings()
+        img = np.zeros((cam.height, cam.width, 4), np.float32) if outputs else None
+        out = None
+        if outputs:
+            out = ViewOutput()
+            out.rgba = img.ctypes.data
+            out.location = BSM_HOST
+        st = RenderStats()
+        loss = C.c_float()
+        self.ctx.check(self._L.bsm_render_cached(self.ctx.h, scene_id, C.byref(cam), C.byref(s), self.h, C.byref(cs),
+                                                 C.byref(out) if out is not None else None, C.byref(st),
+                                                 C.byref(loss)))
+        return img, st, loss.value
+
+
+def rel_mse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
+    """Relative MSE over pixels and RGB: mean((I - R)^2 / (R^2 + eps))."""
+    a = img[..., :3].astype(np.float64)
+    b = ref[..., :3].astype(np.float64)
+    return float(np.mean((a - b) ** 2 / (b * b + eps)))
 
 
 # -------------------------------------------------- reference-shaped API ----

@@ -25,6 +25,7 @@
 
 #include "bsm_pt.h"
 #include "bvh_build.h"
+#include "cache_impl.h"
 #include "pt_device.h"
 #include "pt_math.cuh"
 
@@ -214,7 +215,7 @@ bsm_status ensure_wavefront(bsm_context* ctx, uint32_t capacity, uint32_t lights
     auto sz = [&](size_t n) { size_t off = bytes; bytes += (n + 255) & ~(size_t)255; return off; };
     size_t o_ro0 = sz(C * 16), o_ro1 = sz(C * 16), o_rd0 = sz(C * 16), o_rd1 = sz(C * 16);
     size_t o_p0 = sz(C * 16), o_p1 = sz(C * 16), o_t0 = sz(C * 16), o_t1 = sz(C * 16);
-    size_t o_hit = sz(C * 16), o_sho = sz(sh * 16), o_shd = sz(sh * 16), o_shc = sz(sh * 16);
+    size_t o_hit = sz(C * 16), o_sho = sz(sh * 16), o_shd = sz(sh * 16), o_shc = sz(sh * 16), o_cq = sz(C * 64);
     size_t o_cnt = sz(kCntWords * 4), o_st = sz(kStatWords * 8);
     clear_graphs(ctx);  // graphs hold the old pointers
     dev_free(ctx, ctx->wf_buf);
@@ -229,9 +230,11 @@ bsm_status ensure_wavefront(bsm_context* ctx, uint32_t capacity, uint32_t lights
     w.thr[0] = (float4*)(b + o_t0); w.thr[1] = (float4*)(b + o_t1);
     w.hit = (float4*)(b + o_hit);
     w.sh_o = (float4*)(b + o_sho); w.sh_d = (float4*)(b + o_shd); w.sh_c = (float4*)(b + o_shc);
+    w.cache_q = (float4*)(b + o_cq);
     w.counters = (uint32_t*)(b + o_cnt);
     w.stats = (unsigned long long*)(b + o_st);
     ctx->wf_lights = lights;
+    if (cudaMemset(w.counters, 0, kCntWords * 4) != cudaSuccess) return fail(ctx, BSM_ERR_CUDA, "counter clear failed");
     return BSM_OK;
 }
 
@@ -427,6 +430,10 @@ extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d
         ds.sky.pdf_tab = (const float*)sc->pdf_tab.ptr;
     }
     ds.ray_offset = 2e-5f * sc->extent;
+    for (int k = 0; k < 3; ++k) {
+        ds.box_lo[k] = lo[k];
+        ds.box_inv[k] = 1.0f / std::max(hi[k] - lo[k], 1e-6f);
+    }
     if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
     std::lock_guard<std::mutex> lk(ctx->mu);
     uint32_t id = ctx->next_scene++;
@@ -558,7 +565,8 @@ namespace {
 // ev[0] before the first launch, then one per stage; `tags` gets the stage of
 // each interval (0 camera, 1 extend, 2 shade, 3 shadow).
 void record_render(bsm_context* ctx, const Scene* sc, uint32_t n_views, uint64_t total_paths, uint32_t capacity,
-                   uint32_t max_seg, bool count_traversal, std::vector<cudaEvent_t>* ev, std::vector<int>* tags) {
+                   uint32_t max_seg, bool count_traversal, std::vector<cudaEvent_t>* ev, std::vector<int>* tags,
+                   const void* cache_wb = nullptr) {
     const LaunchCfg& lc = ctx->lc;
     cudaStream_t st = ctx->stream;
     const DevView* views = (const DevView*)ctx->views_dev.ptr;
@@ -590,6 +598,8 @@ void record_render(bsm_context* ctx, const Scene* sc, uint32_t n_views, uint64_t
             mark(3);
             q ^= 1;
         }
+        if (cache_wb)
+            launch_mlp_infer(ctx->device, st, cache_wb, ctx->wf.cache_q, ctx->wf.counters + kCntCache, capacity, accum);
     }
 }
 
@@ -607,7 +617,8 @@ struct ViewReq {
 };
 
 bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<ViewReq>& req,
-                       const bsm_pt_settings& s, const bsm_view_output* outputs, bsm_render_stats* stats) {
+                       const bsm_pt_settings& s, const bsm_view_output* outputs, bsm_render_stats* stats,
+                       const void* cache_wb = nullptr, uint32_t cache_seg = 0) {
     const uint32_t n_views = (uint32_t)req.size();
     cudaSetDevice(ctx->device);
     Scene* sc = find_scene(ctx, scene_id);
@@ -685,6 +696,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         dv.accum_base = h.accum_base;
         dv.max_segments = req[v].max_seg;
         dv.flags = s.flags;
+        dv.cache_segment = cache_wb ? cache_seg : 0u;
         total_paths += (uint64_t)views[v].width * views[v].height * req[v].spp;
     }
     uint32_t cap_req = s.wavefront_capacity ? s.wavefront_capacity : (sc->tuned ? sc->tune.wavefront_capacity : 0u);
@@ -709,7 +721,8 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         std::vector<uint8_t> key(64);
         uint64_t kv[8] = {(uint64_t)scene_id, (uint64_t)n_views, total_paths,
                           capacity | ((uint64_t)ctx->lc.postpone_sp << 32) | ((uint64_t)ctx->lc.refill_min << 40),
-                          max_seg, (uint64_t)(uintptr_t)ctx->wf_buf.ptr, (uint64_t)(uintptr_t)ctx->accum.ptr,
+                          max_seg | ((uint64_t)(uintptr_t)cache_wb << 8), (uint64_t)(uintptr_t)ctx->wf_buf.ptr,
+                          (uint64_t)(uintptr_t)ctx->accum.ptr,
                           (uint64_t)(uintptr_t)ctx->views_dev.ptr ^ ((uint64_t)ctx->lc_block << 56)};
         std::memcpy(key.data(), kv, 64);
         cudaGraphExec_t exec = nullptr;
@@ -717,7 +730,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         if (!exec) {
             cudaGraph_t graph;
             CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-            record_render(ctx, sc, n_views, total_paths, capacity, max_seg, false, nullptr, nullptr);
+            record_render(ctx, sc, n_views, total_paths, capacity, max_seg, false, nullptr, nullptr, cache_wb);
             CK(cudaStreamEndCapture(ctx->stream, &graph));
             CK(cudaGraphInstantiate(&exec, graph, 0));
             cudaGraphDestroy(graph);
@@ -730,7 +743,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         CK(cudaGraphLaunch(exec, ctx->stream));
     } else {
         record_render(ctx, sc, n_views, total_paths, capacity, max_seg, counting, timing ? &ctx->stage_ev : nullptr,
-                      &tags);
+                      &tags, cache_wb);
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[9], ctx->stream));
@@ -810,6 +823,35 @@ extern "C" bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_
     std::vector<ViewReq> req(n_views);
     for (uint32_t v = 0; v < n_views; ++v) req[v] = ViewReq{views[v], s.spp, max_seg, s.seed};
     return render_impl(ctx, scene_id, req, s, outputs, stats);
+}
+
+extern "C" bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, const bsm_camera* cam,
+                                        const bsm_pt_settings* settings, bsm_cache* cache,
+                                        const bsm_cache_settings* cs_in, const bsm_view_output* output,
+                                        bsm_render_stats* stats, float* train_loss) {
+    if (!ctx || !cam || !settings || !cache) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc || !sc->has_bvh) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene or BVH not built");
+    if (cache->ctx != ctx) return fail(ctx, BSM_ERR_INVALID_ARG, "cache belongs to another context");
+    bsm_cache_settings cs;
+    if (cs_in) cs = *cs_in; else bsm_cache_settings_default(&cs);
+    if (cs.cache_segment == 0 || cs.cache_segment >= (uint32_t)kMaxSeg)
+        return fail(ctx, BSM_ERR_INVALID_ARG, "cache_segment must be 1..15");
+    if (train_loss) *train_loss = 0.0f;
+    if (cs.train_steps > 0 && cs.train_paths > 0) {
+        DevView dv{};
+        make_view(*cam, dv);
+        dv.ray_length = settings->ray_length;
+        dv.t_min = settings->t_min;
+        dv.seed = settings->seed;
+        dv.max_segments = std::min(std::max(cs.train_segments, 1u), 16u);
+        bsm_status e = cache_train_frame(cache, sc->dev, dv, cs, ctx->stream, train_loss, nullptr);
+        if (e) return fail(ctx, e, "radiance-cache training failed");
+    }
+    std::vector<ViewReq> req(1);
+    req[0] = ViewReq{*cam, settings->spp, cs.cache_segment + 1, settings->seed};
+    return render_impl(ctx, scene_id, req, *settings, output, stats, cache->w_bf16, cs.cache_segment);
 }
 
 extern "C" bsm_status bsm_render_batch(bsm_context* ctx, uint32_t scene_id, const bsm_view_desc* views,

@@ -1,0 +1,233 @@
+// cache.cpp — host side of the radiance cache: weights, Adam state, training
+// on tracer-generated samples, save/load.  The kernels are in mlp.cu and
+// train_paths.cu; bsm_render_cached (api.cpp) renders with the cache.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "bsm_pt.h"
+#include "cache_impl.h"
+#include "mlp.cuh"
+
+using namespace bsm;
+
+namespace {
+
+bsm_status cache_io(bsm_cache* c, size_t bytes) {
+    if (c->io_bytes >= bytes) return BSM_OK;
+    if (c->io) cudaFree(c->io);
+    c->io = nullptr;
+    c->io_bytes = 0;
+    if (cudaMalloc(&c->io, bytes) != cudaSuccess) return BSM_ERR_OUT_OF_MEMORY;
+    c->io_bytes = bytes;
+    return BSM_OK;
+}
+
+void upload_weights(bsm_cache* c, const float* w) {
+    std::vector<__nv_bfloat16> b(kMlpParams);
+    for (int i = 0; i < kMlpParams; ++i) b[i] = __float2bfloat16_rn(w[i]);
+    cudaMemcpy(c->w_master, w, kMlpParams * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->w_bf16, b.data(), kMlpParams * 2, cudaMemcpyHostToDevice);
+    cudaMemset(c->adam_m, 0, kMlpParams * 4);
+    cudaMemset(c->adam_v, 0, kMlpParams * 4);
+    c->step = 0;
+}
+
+}  // namespace
+
+extern "C" void bsm_cache_settings_default(bsm_cache_settings* cs) {
+    if (!cs) return;
+    cs->cache_segment = 2;
+    cs->train_paths = 65536;
+    cs->train_segments = 8;
+    cs->train_batch = 16384;
+    cs->train_steps = 4;
+    cs->lr = 1e-2f;
+}
+
+extern "C" uint32_t bsm_cache_param_count(void) { return (uint32_t)kMlpParams; }
+
+extern "C" bsm_status bsm_cache_create(bsm_context* ctx, uint64_t seed, bsm_cache** out) {
+    if (!ctx || !out) return BSM_ERR_INVALID_ARG;
+    *out = nullptr;
+    auto* c = new bsm_cache();
+    c->ctx = ctx;
+    c->device = ctx_device(ctx);
+    cudaSetDevice(c->device);
+    bool ok = cudaMalloc((void**)&c->w_master, kMlpParams * 4) == cudaSuccess &&
+              cudaMalloc(&c->w_bf16, kMlpParams * 2) == cudaSuccess &&
+              cudaMalloc((void**)&c->adam_m, kMlpParams * 4) == cudaSuccess &&
+              cudaMalloc((void**)&c->adam_v, kMlpParams * 4) == cudaSuccess &&
+              cudaMalloc((void**)&c->dW, kMlpParams * 4) == cudaSuccess &&
+              cudaMalloc((void**)&c->loss, 4) == cudaSuccess &&
+              cudaMalloc((void**)&c->sample_count, 4) == cudaSuccess &&
+              cudaMalloc((void**)&c->view_dev, sizeof(DevView)) == cudaSuccess;
+    if (!ok) {
+        bsm_cache_destroy(c);
+        return BSM_ERR_OUT_OF_MEMORY;
+    }
+    // He-uniform initialisation, U(-sqrt(6/fan_in), sqrt(6/fan_in)), from a SplitMix64 stream
+    std::vector<float> w(kMlpParams, 0.0f);
+    uint64_t st = seed * 0x9e3779b97f4a7c15ULL + 0x632be59bd9b4e019ULL;
+    const float lim = std::sqrt(6.0f / 64.0f);
+    for (int i = 0; i < kMlpParams; ++i) {
+        st += 0x9e3779b97f4a7c15ULL;
+        float u = (float)(mix64(st) >> 40) * (1.0f / 16777216.0f);
+        w[i] = (2.0f * u - 1.0f) * lim;
+        if (i >= kMlpHidden * kMlpLayerParams + kMlpOut * kMlpHid) w[i] = 0.0f;
+        else if (i >= kMlpHidden * kMlpLayerParams) w[i] *= 0.1f;  // small initial output
+    }
+    upload_weights(c, w.data());
+    *out = c;
+    return BSM_OK;
+}
+
+extern "C" void bsm_cache_destroy(bsm_cache* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    for (void* p : {(void*)c->w_master, c->w_bf16, (void*)c->adam_m, (void*)c->adam_v, (void*)c->dW, (void*)c->loss,
+                    (void*)c->samples, (void*)c->sample_count, (void*)c->view_dev, (void*)c->io})
+        if (p) cudaFree(p);
+    delete c;
+}
+
+extern "C" bsm_status bsm_cache_weights(bsm_cache* c, float* get, const float* set) {
+    if (!c) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    if (get && cudaMemcpy(get, c->w_master, kMlpParams * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BSM_ERR_CUDA;
+    if (set) upload_weights(c, set);
+    return cudaGetLastError() == cudaSuccess ? BSM_OK : BSM_ERR_CUDA;
+}
+
+extern "C" bsm_status bsm_cache_predict(bsm_cache* c, const float* samples, uint32_t n, float* out) {
+    if (!c || (!samples && n) || (!out && n)) return BSM_ERR_INVALID_ARG;
+    if (n == 0) return BSM_OK;
+    cudaSetDevice(c->device);
+    size_t in_b = (size_t)n * 64, out_b = (size_t)n * 12;
+    if (cache_io(c, in_b + out_b)) return BSM_ERR_OUT_OF_MEMORY;
+    char* b = (char*)c->io;
+    cudaMemcpy(b, samples, in_b, cudaMemcpyHostToDevice);
+    if (launch_mlp_predict(c->device, 0, c->w_bf16, (const float4*)b, n, (float*)(b + in_b)) != cudaSuccess)
+        return BSM_ERR_CUDA;
+    if (cudaMemcpy(out, b + in_b, out_b, cudaMemcpyDeviceToHost) != cudaSuccess) return BSM_ERR_CUDA;
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_cache_gradient(bsm_cache* c, const float* samples, uint32_t n, float* dW, float* loss) {
+    if (!c || !samples || !dW || n == 0) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    size_t in_b = (size_t)n * 64;
+    if (cache_io(c, in_b)) return BSM_ERR_OUT_OF_MEMORY;
+    cudaMemcpy(c->io, samples, in_b, cudaMemcpyHostToDevice);
+    cudaMemset(c->dW, 0, kMlpParams * 4);
+    cudaMemset(c->loss, 0, 4);
+    if (launch_mlp_train(c->device, 0, c->w_bf16, (const float4*)c->io, n, c->dW, c->loss) != cudaSuccess)
+        return BSM_ERR_CUDA;
+    if (cudaMemcpy(dW, c->dW, kMlpParams * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BSM_ERR_CUDA;
+    if (loss) cudaMemcpy(loss, c->loss, 4, cudaMemcpyDeviceToHost);
+    return BSM_OK;
+}
+
+namespace {
+bsm_status train_device(bsm_cache* c, const float4* samples, uint32_t n, uint32_t batch, float lr, cudaStream_t st,
+                        float* mean_loss) {
+    if (batch == 0) batch = 16384;
+    double loss_sum = 0.0;
+    uint32_t steps = 0;
+    for (uint32_t off = 0; off < n; off += batch) {
+        uint32_t nb = std::min(batch, n - off);
+        cudaMemsetAsync(c->dW, 0, kMlpParams * 4, st);
+        cudaMemsetAsync(c->loss, 0, 4, st);
+        if (launch_mlp_train(c->device, st, c->w_bf16, samples + 4 * (size_t)off, nb, c->dW, c->loss) != cudaSuccess)
+            return BSM_ERR_CUDA;
+        c->step++;
+        if (launch_mlp_adam(st, c->w_master, c->w_bf16, c->dW, c->adam_m, c->adam_v, lr, c->step) != cudaSuccess)
+            return BSM_ERR_CUDA;
+        float l = 0.0f;
+        cudaMemcpyAsync(&l, c->loss, 4, cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        loss_sum += l;
+        ++steps;
+    }
+    if (mean_loss) *mean_loss = steps ? (float)(loss_sum / steps) : 0.0f;
+    return BSM_OK;
+}
+}  // namespace
+
+extern "C" bsm_status bsm_cache_train(bsm_cache* c, const float* samples, uint32_t n, uint32_t batch, float lr,
+                                      float* loss) {
+    if (!c || !samples || n == 0 || !(lr > 0.0f)) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    size_t in_b = (size_t)n * 64;
+    if (cache_io(c, in_b)) return BSM_ERR_OUT_OF_MEMORY;
+    cudaMemcpy(c->io, samples, in_b, cudaMemcpyHostToDevice);
+    return train_device(c, (const float4*)c->io, n, batch, lr, 0, loss);
+}
+
+extern "C" bsm_status bsm_cache_save(bsm_cache* c, const char* path) {
+    if (!c || !path) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    std::vector<float> w(kMlpParams), m(kMlpParams), v(kMlpParams);
+    cudaMemcpy(w.data(), c->w_master, kMlpParams * 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(m.data(), c->adam_m, kMlpParams * 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(v.data(), c->adam_v, kMlpParams * 4, cudaMemcpyDeviceToHost);
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return BSM_ERR_INVALID_ARG;
+    const uint32_t hdr[4] = {0x43534d42u /* "BMSC" */, 1u, (uint32_t)kMlpParams, (uint32_t)c->step};
+    bool ok = std::fwrite(hdr, 4, 4, f) == 4 && std::fwrite(w.data(), 4, kMlpParams, f) == (size_t)kMlpParams &&
+              std::fwrite(m.data(), 4, kMlpParams, f) == (size_t)kMlpParams &&
+              std::fwrite(v.data(), 4, kMlpParams, f) == (size_t)kMlpParams;
+    std::fclose(f);
+    return ok ? BSM_OK : BSM_ERR_INVALID_ARG;
+}
+
+extern "C" bsm_status bsm_cache_load(bsm_cache* c, const char* path) {
+    if (!c || !path) return BSM_ERR_INVALID_ARG;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return BSM_ERR_NOT_FOUND;
+    uint32_t hdr[4];
+    std::vector<float> w(kMlpParams), m(kMlpParams), v(kMlpParams);
+    bool ok = std::fread(hdr, 4, 4, f) == 4 && hdr[0] == 0x43534d42u && hdr[1] == 1u && hdr[2] == (uint32_t)kMlpParams &&
+              std::fread(w.data(), 4, kMlpParams, f) == (size_t)kMlpParams &&
+              std::fread(m.data(), 4, kMlpParams, f) == (size_t)kMlpParams &&
+              std::fread(v.data(), 4, kMlpParams, f) == (size_t)kMlpParams;
+    std::fclose(f);
+    if (!ok) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    upload_weights(c, w.data());
+    cudaMemcpy(c->adam_m, m.data(), kMlpParams * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->adam_v, v.data(), kMlpParams * 4, cudaMemcpyHostToDevice);
+    c->step = (int)hdr[3];
+    return BSM_OK;
+}
+
+namespace bsm {
+bsm_status cache_train_frame(bsm_cache* c, const DevScene& sc, const DevView& view, const bsm_cache_settings& cs,
+                             cudaStream_t st, float* loss_out, uint32_t* samples_out) {
+    uint32_t cap = cs.train_paths * std::max(1u, std::min(cs.train_segments, 16u));
+    if (c->sample_cap < cap) {
+        if (c->samples) cudaFree(c->samples);
+        c->samples = nullptr;
+        c->sample_cap = 0;
+        if (cudaMalloc((void**)&c->samples, (size_t)cap * 64) != cudaSuccess) return BSM_ERR_OUT_OF_MEMORY;
+        c->sample_cap = cap;
+    }
+    cudaMemcpyAsync(c->view_dev, &view, sizeof(DevView), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(c->sample_count, 0, 4, st);
+    launch_train_paths(st, sc, c->view_dev, cs.train_paths, c->frame++, cs.train_segments, c->samples,
+                       c->sample_count, c->sample_cap);
+    uint32_t n = 0;
+    cudaMemcpyAsync(&n, c->sample_count, 4, cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return BSM_ERR_CUDA;
+    n = std::min(n, c->sample_cap);
+    uint32_t use = std::min(n, cs.train_batch * cs.train_steps);
+    if (samples_out) *samples_out = n;
+    return train_device(c, c->samples, use, cs.train_batch, cs.lr, st, loss_out);
+}
+}  // namespace bsm

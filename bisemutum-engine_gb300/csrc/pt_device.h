@@ -43,6 +43,8 @@ struct DevScene {
     float4 light_e[kMaxLights];
     DevSky sky;
     float ray_offset;          // origin offset along the geometric normal
+    float box_lo[3];           // scene bounds: radiance-cache inputs are normalised to them
+    float box_inv[3];
 };
 
 struct DevView {
@@ -56,7 +58,7 @@ struct DevView {
     uint32_t accum_base;       // first accumulator pixel of this view
     uint32_t max_segments;
     uint32_t flags;            // BSM_PT_* bits that reach the device
-    uint32_t pad;
+    uint32_t cache_segment;    // >0: hits of this segment query the radiance cache instead of shading
     uint64_t first_path;       // index (within the view) of the path at path_base; >0 when a view is split
 };
 
@@ -65,7 +67,8 @@ enum : uint32_t {
     kCntQueue = 0,                 // [kMaxSeg + 1] extend queue size entering segment s
     kCntShadow = kCntQueue + 17,   // [kMaxSeg] shadow queue size of segment s
     kCntWork = kCntShadow + 16,    // [2 * kMaxSeg] persistent-kernel work counters
-    kCntError = kCntWork + 32,     // error flags (bit 0: queue overflow)
+    kCntCache = kCntWork + 32,     // radiance-cache queries of the chunk
+    kCntError = kCntCache + 1,     // error flags (bit 0: queue overflow); words below it are cleared per chunk
     kCntWords = kCntError + 1
 };
 // stats[] (uint64) offsets
@@ -87,6 +90,7 @@ struct Wavefront {
     float4* sh_o;
     float4* sh_d;
     float4* sh_c;
+    float4* cache_q;           // radiance-cache queries (4 float4 each), capacity C; may be null
     uint32_t* counters;
     unsigned long long* stats;
 };
@@ -116,6 +120,19 @@ void launch_trace_closest(cudaStream_t st, const DevScene& sc, const float4* ray
 void launch_trace_any(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint8_t* occluded,
                       int block);
 void launch_trace_count(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint2* counts);
+// radiance cache (mlp.cu)
+cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const float4* queries, const uint32_t* count,
+                             uint32_t capacity, float4* accum);
+cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
+                               float* out);
+cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
+                             float* dW, float* loss);
+cudaError_t launch_mlp_adam(cudaStream_t st, float* wm, void* wb, const float* dW, float* m, float* v, float lr,
+                            int step);
+// training paths (train_paths.cu): full-length paths that record per-vertex cache samples
+void launch_train_paths(cudaStream_t st, const DevScene& sc, const DevView* view, uint32_t n_paths, uint32_t frame,
+                        uint32_t max_segments, float4* samples, uint32_t* count, uint32_t max_samples);
+
 // Fills the persistent-kernel grids from the device's SM count and occupancy.
 void query_launch_cfg(int device, int block_trace, LaunchCfg* lc);
 

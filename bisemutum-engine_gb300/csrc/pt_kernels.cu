@@ -20,6 +20,7 @@
 #include "pt_device.h"
 #include "pt_sky.cuh"
 #include "pt_trace.cuh"
+#include "mlp.cuh"
 
 namespace bsm {
 
@@ -156,10 +157,12 @@ __global__ void __launch_bounds__(256) k_shade(DevScene sc, const DevView* __res
         bool sky_nee = sc.num_lights + 1u > 0u;  // placeholder, refined below per view
         uint32_t vflags = 0;
         uint32_t stream = 0;
+        uint32_t cache_seg = 0;
         if (active) {
             const DevView& v = views[view_id];
             vflags = v.flags;
             stream = m4.x - v.accum_base;
+            cache_seg = v.cache_segment;
         }
         sky_nee = (vflags & BSM_PT_NO_SKY_NEE) == 0u;
         if (active && !is_hit) {
@@ -205,6 +208,28 @@ __global__ void __launch_bounds__(256) k_shade(DevScene sc, const DevView* __res
             u_sky0 = pcg_uniform(g); u_sky1 = pcg_uniform(g); u_lobe = pcg_uniform(g);
             u_b0 = pcg_uniform(g); u_b1 = pcg_uniform(g);
         }
+        // radiance cache: a hit of the cache segment becomes a query (NRC-style
+        // termination) — the cache's prediction includes the direct light there
+        bool cache_q = is_hit && cache_seg != 0u && segi == cache_seg;
+        {
+            uint32_t slot = warp_alloc(cache_q, wf.counters + kCntCache);
+            if (cache_q) {
+                if (slot < cap && wf.cache_q) {
+                    float raw[kMlpRaw];
+                    mlp_raw_inputs(P, v3(sc.box_lo[0], sc.box_lo[1], sc.box_lo[2]),
+                                   v3(sc.box_inv[0], sc.box_inv[1], sc.box_inv[2]), -d, N, surf.roughness,
+                                   surf.base_color, (float)segi * 0.125f, raw);
+                    float4* qd = wf.cache_q + 4 * (size_t)slot;
+                    qd[0] = make_float4(raw[0], raw[1], raw[2], raw[3]);
+                    qd[1] = make_float4(raw[4], raw[5], raw[6], raw[7]);
+                    qd[2] = make_float4(raw[8], raw[9], raw[10], raw[11]);
+                    qd[3] = make_float4(thr.x, thr.y, thr.z, __uint_as_float(m4.x));
+                } else {
+                    atomicOr(wf.counters + kCntError, 1u);
+                }
+            }
+        }
+        if (cache_q) is_hit = false;  // no NEE, no continuation at a cache vertex
         V3 org = P + N * sc.ray_offset;
         const DevView* vp = views + view_id;
         float ray_len = is_hit ? vp->ray_length : 0.0f;

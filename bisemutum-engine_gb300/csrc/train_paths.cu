@@ -1,0 +1,154 @@
+// train_paths.cu — training data for the radiance cache, generated by the tracer.
+//
+// One thread traces one full-length path (the plain pass's stages in one loop:
+// closest hit, sun and sky next-event estimation with any-hit visibility, lobe
+// sampling, sky on escape with MIS) and records every vertex k it reaches: the
+// cache's raw inputs there and the radiance the rest of the path carried back
+// to it, T_k = (sum of contributions at vertices j >= k) / throughput_k.  Those
+// (input, T_k) pairs are what the network learns, so that a path cut short at
+// a vertex can be finished with throughput x cache(vertex).
+// Pixels are drawn per frame by a hash of (frame, path index); random numbers
+// are PCG32 streams keyed to the pixel and a per-frame sample index.
+#include <cuda_runtime.h>
+
+#include "bsm_pt.h"
+#include "mlp.cuh"
+#include "pt_device.h"
+#include "pt_sky.cuh"
+#include "pt_trace.cuh"
+
+namespace bsm {
+
+constexpr int kTrainMaxVerts = 16;
+
+__global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView* __restrict__ view, uint32_t n_paths,
+                                                     uint32_t frame, uint32_t max_seg, float4* samples,
+                                                     uint32_t* count, uint32_t max_samples) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_paths) return;
+    const DevView& v = *view;
+    uint32_t npix = v.width * v.height;
+    uint32_t pixel = (uint32_t)(mix64(((uint64_t)frame << 32) ^ (uint64_t)i ^ 0x5851f42d4c957f2dULL) % npix);
+    uint32_t px = pixel % v.width, py = pixel / v.width;
+    Pcg g = pcg_seed(sample_initstate(v.seed ^ 0x7f4a7c159e3779b9ULL, frame * n_paths + i), (uint64_t)pixel);
+    float uvx = ((float)px + pcg_uniform(g)) / (float)v.width;
+    float uvy = ((float)py + pcg_uniform(g)) / (float)v.height;
+    V3 dl = normalize(v3((uvx * 2.0f - 1.0f) * v.aspect * v.tan_half, (1.0f - uvy * 2.0f) * v.tan_half, -1.0f));
+    V3 sx = v3(v.s[0], v.s[1], v.s[2]), ux = v3(v.u[0], v.u[1], v.u[2]), fx = v3(v.f[0], v.f[1], v.f[2]);
+    V3 d = normalize(sx * dl.x + ux * dl.y + (-fx) * dl.z);
+    V3 o = v3(v.pos[0], v.pos[1], v.pos[2]);
+    V3 thr = v3s(1.0f);
+    float last_pdf = 0.0f;
+    float raw[kTrainMaxVerts][kMlpRaw];
+    V3 thr_k[kTrainMaxVerts], contrib[kTrainMaxVerts];
+    int nv = 0;
+    const V3 box_lo = v3(sc.box_lo[0], sc.box_lo[1], sc.box_lo[2]);
+    const V3 box_inv = v3(sc.box_inv[0], sc.box_inv[1], sc.box_inv[2]);
+    uint32_t segs = max_seg < (uint32_t)kTrainMaxVerts ? max_seg : (uint32_t)kTrainMaxVerts;
+    for (uint32_t seg = 0; seg < segs; ++seg) {
+        RayPre r = make_ray(make_float4(o.x, o.y, o.z, v.t_min), make_float4(d.x, d.y, d.z, v.ray_length));
+        float t, hu, hv;
+        uint32_t leaf = trace_ray<false, false>(r, v.ray_length, sc.nodes, sc.tris, t, hu, hv, nullptr);
+        if (leaf == kMissPrim) {
+            if (nv > 0) {
+                V3 le = sky_eval(sc.sky, d);
+                float pl = sky_pdf(sc.sky, d), pb = last_pdf;
+                float w = (pb * pb + pl * pl) > 0.0f ? pb * pb / (pb * pb + pl * pl) : 1.0f;
+                contrib[nv - 1] = contrib[nv - 1] + thr * le * w;
+            }
+            break;
+        }
+        const CwTri& tri = sc.tris[leaf];
+        V3 va = v3(tri.v0x, tri.v0y, tri.v0z), vb = v3(tri.v1x, tri.v1y, tri.v1z), vc = v3(tri.v2x, tri.v2y, tri.v2z);
+        V3 N = normalize(cross(vb - va, vc - va));
+        if (dot(N, d) > 0.0f) N = -N;
+        V3 P = o + d * t;
+        uint32_t mi = tri.material < sc.num_materials ? tri.material : 0u;
+        float4 m0 = sc.materials[2 * mi], m1 = sc.materials[2 * mi + 1];
+        Surface surf;
+        surf.base_color = v3(m0.x, m0.y, m0.z);
+        surf.roughness = m0.w;
+        surf.f0 = v3(m1.x, m1.y, m1.z);
+        surf.f90 = v3s(1.0f);
+        surf.ior = 1.5f;
+        V3 V = -d;
+        mlp_raw_inputs(P, box_lo, box_inv, V, N, surf.roughness, surf.base_color, (float)seg * 0.125f, raw[nv]);
+        thr_k[nv] = thr;
+        contrib[nv] = v3s(0.0f);
+        int k = nv++;
+        Frame fr = create_frame(N);
+        V3 org = P + N * sc.ray_offset;
+        float u_sky0 = pcg_uniform(g), u_sky1 = pcg_uniform(g), u_lobe = pcg_uniform(g), u_b0 = pcg_uniform(g),
+              u_b1 = pcg_uniform(g);
+        float rx, ry;
+        aniso_roughness(surf.roughness, &rx, &ry);
+        V3 lv = to_local(fr, V);
+        float p_spec = spec_probability(surf, lv.z);
+        for (uint32_t l = 0; l < sc.num_lights; ++l) {
+            V3 L = v3(sc.light_dir[l].x, sc.light_dir[l].y, sc.light_dir[l].z);
+            V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
+            V3 c = thr * v3(sc.light_e[l].x, sc.light_e[l].y, sc.light_e[l].z) * f;
+            if (max_comp(c) > 0.0f) {
+                RayPre sr = make_ray(make_float4(org.x, org.y, org.z, v.t_min), make_float4(L.x, L.y, L.z, v.ray_length));
+                float a, b2, c2;
+                if (trace_ray<true, false>(sr, v.ray_length, sc.nodes, sc.tris, a, b2, c2, nullptr) == kMissPrim)
+                    contrib[k] = contrib[k] + c;
+            }
+        }
+        {
+            float pl;
+            V3 le;
+            V3 L = sky_sample(sc.sky, u_sky0, u_sky1, pl, le);
+            if (pl > 0.0f) {
+                V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
+                if (max_comp(f) > 0.0f) {
+                    float pb = mixture_pdf(lv, to_local(fr, L), rx, ry, p_spec);
+                    V3 c = thr * le * f * ((pl * pl) / (pl * pl + pb * pb) / pl);
+                    RayPre sr = make_ray(make_float4(org.x, org.y, org.z, v.t_min), make_float4(L.x, L.y, L.z, v.ray_length));
+                    float a, b2, c2;
+                    if (max_comp(c) > 0.0f &&
+                        trace_ray<true, false>(sr, v.ray_length, sc.nodes, sc.tris, a, b2, c2, nullptr) == kMissPrim)
+                        contrib[k] = contrib[k] + c;
+                }
+            }
+        }
+        if (seg + 1 >= segs || max_comp(thr) < 0.001f) break;
+        V3 ll = u_lobe < p_spec ? reflect(-lv, ggx_vndf_sample(lv, rx, ry, u_b0, u_b1)) : cos_hemisphere_sample(u_b0, u_b1);
+        if (!(ll.z > 0.0f)) break;
+        V3 L = to_world(fr, ll);
+        float pdf = mixture_pdf(lv, ll, rx, ry, p_spec);
+        V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
+        V3 w = pdf > 0.0f ? f / pdf : v3s(0.0f);
+        if (!isfinite(w.x) || !isfinite(w.y) || !isfinite(w.z)) break;
+        thr = thr * w;
+        if (!(max_comp(thr) > 0.0f)) break;
+        o = org;
+        d = L;
+        last_pdf = pdf;
+    }
+    // targets: radiance carried back to each vertex
+    V3 acc = v3s(0.0f);
+    for (int k = nv - 1; k >= 0; --k) {
+        acc = acc + contrib[k];
+        V3 tk = thr_k[k];
+        if (!(tk.x > 0.0f && tk.y > 0.0f && tk.z > 0.0f)) continue;
+        V3 target = v3(acc.x / tk.x, acc.y / tk.y, acc.z / tk.z);
+        if (!isfinite(target.x) || !isfinite(target.y) || !isfinite(target.z)) continue;
+        uint32_t slot = atomicAdd(count, 1u);
+        if (slot >= max_samples) continue;
+        float4* sd = samples + 4 * (size_t)slot;
+        sd[0] = make_float4(raw[k][0], raw[k][1], raw[k][2], raw[k][3]);
+        sd[1] = make_float4(raw[k][4], raw[k][5], raw[k][6], raw[k][7]);
+        sd[2] = make_float4(raw[k][8], raw[k][9], raw[k][10], raw[k][11]);
+        sd[3] = make_float4(target.x, target.y, target.z, 0.0f);
+    }
+}
+
+void launch_train_paths(cudaStream_t st, const DevScene& sc, const DevView* view, uint32_t n_paths, uint32_t frame,
+                        uint32_t max_segments, float4* samples, uint32_t* count, uint32_t max_samples) {
+    if (n_paths == 0) return;
+    k_train_paths<<<(n_paths + 127) / 128, 128, 0, st>>>(sc, view, n_paths, frame, max_segments, samples, count,
+                                                        max_samples);
+}
+
+}  // namespace bsm

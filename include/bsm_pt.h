@@ -382,6 +382,50 @@ BSM_API bsm_status bsm_server_get_stats(bsm_context* ctx, bsm_server_stats* stat
 /* Stops the worker after the chunks in flight; queued requests are dropped. */
 BSM_API bsm_status bsm_server_stop(bsm_context* ctx);
 
+/* ---- radiance cache (learned) ------------------------------------------ */
+
+/* A small BF16 MLP (64 encoded inputs, 4 hidden ReLU layers of 64, RGB out,
+ * FP32 accumulation on the tensor cores) trained online on the path vertices
+ * the tracer generates.  Paths terminate into it after a short prefix.  No
+ * reference counterpart: the engine's DDGI probes (ddgi_update.cpp) are its
+ * closest relative, and the plain pass stays the fallback and the judge. */
+typedef struct bsm_cache bsm_cache;
+
+typedef struct bsm_cache_settings {
+    uint32_t cache_segment;   /* hits of this segment query the cache (2 = after two bounces) */
+    uint32_t train_paths;     /* full-length training paths per frame (65536) */
+    uint32_t train_segments;  /* their maximum segments (8) */
+    uint32_t train_batch;     /* samples per Adam step (16384) */
+    uint32_t train_steps;     /* Adam steps per frame (4); 0 = render only */
+    float lr;                 /* Adam learning rate (1e-2) */
+} bsm_cache_settings;
+
+BSM_API void bsm_cache_settings_default(bsm_cache_settings* cs);
+/* Number of network parameters (fp32 master weights, row-major W0..W3 [64][64], W4 [8][64]). */
+BSM_API uint32_t bsm_cache_param_count(void);
+/* Creates a cache on ctx's device with He-uniform random weights from `seed`. */
+BSM_API bsm_status bsm_cache_create(bsm_context* ctx, uint64_t seed, bsm_cache** cache);
+BSM_API void bsm_cache_destroy(bsm_cache* cache);
+/* Reads (get != NULL) and/or writes (set != NULL) the fp32 master weights; a write resets Adam. */
+BSM_API bsm_status bsm_cache_weights(bsm_cache* cache, float* get, const float* set);
+/* samples: n x 16 floats (12 raw inputs, 3 target radiance, 1 unused), host memory.
+ * Prediction (n x 3) / gradient of the mean relative L2 loss (bsm_cache_param_count floats). */
+BSM_API bsm_status bsm_cache_predict(bsm_cache* cache, const float* samples, uint32_t n, float* out);
+BSM_API bsm_status bsm_cache_gradient(bsm_cache* cache, const float* samples, uint32_t n, float* dW, float* loss);
+/* Adam steps over `samples` in batches; returns the mean loss. */
+BSM_API bsm_status bsm_cache_train(bsm_cache* cache, const float* samples, uint32_t n, uint32_t batch, float lr,
+                                   float* loss);
+BSM_API bsm_status bsm_cache_save(bsm_cache* cache, const char* path);
+BSM_API bsm_status bsm_cache_load(bsm_cache* cache, const char* path);
+
+/* One frame with the cache: optionally trains on `train_paths` fresh full-length
+ * paths of this camera, then renders with paths terminated into the cache at
+ * `cache_segment` (settings->max_segments is ignored).  `train_loss` may be NULL. */
+BSM_API bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, const bsm_camera* camera,
+                                     const bsm_pt_settings* settings, bsm_cache* cache,
+                                     const bsm_cache_settings* cache_settings, const bsm_view_output* output,
+                                     bsm_render_stats* stats, float* train_loss);
+
 /* ---- synthetic scenes --------------------------------------------------- */
 
 enum {

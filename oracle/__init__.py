@@ -47,6 +47,10 @@ def lib() -> C.CDLL:
         L.orc_eval_lit.argtypes = [vp, u32, vp]
         L.orc_vndf.argtypes = [vp, u32, vp]
         L.orc_frame.argtypes = [vp, u32, vp]
+        L.orc_mlp_forward.argtypes = [vp, vp, u32, vp, i32]
+        L.orc_mlp_gradient.argtypes = [vp, vp, u32, vp, i32]
+        L.orc_mlp_gradient.restype = f32
+        L.orc_mlp_adam.argtypes = [vp, vp, vp, vp, f32, i32]
         L.orc_scene_bvh_nodes.argtypes = [vp]
         L.orc_scene_bvh_nodes.restype = u32
         _lib = L
@@ -163,3 +167,30 @@ def vndf(a):
 
 def frame(a):
     return _batch(lib().orc_frame, a, 3, 6)
+
+
+# ---- radiance-cache network (see pt_oracle.cpp) ----
+MLP_PARAMS = 4 * 4096 + 8 * 64
+
+
+def mlp_forward(W, samples, bf16=True):
+    W = _f32(W)
+    S = _f32(samples).reshape(-1, 16)
+    out = np.zeros((S.shape[0], 3), np.float32)
+    lib().orc_mlp_forward(W.ctypes.data, S.ctypes.data, S.shape[0], out.ctypes.data, 1 if bf16 else 0)
+    return out
+
+
+def mlp_gradient(W, samples, bf16=True):
+    W = _f32(W)
+    S = _f32(samples).reshape(-1, 16)
+    dW = np.zeros(MLP_PARAMS, np.float32)
+    loss = lib().orc_mlp_gradient(W.ctypes.data, S.ctypes.data, S.shape[0], dW.ctypes.data, 1 if bf16 else 0)
+    return dW, loss
+
+
+def mlp_adam(W, dW, m, v, lr, t):
+    W, m, v = _f32(W).copy(), _f32(m).copy(), _f32(v).copy()
+    dW = _f32(dW)
+    lib().orc_mlp_adam(W.ctypes.data, dW.ctypes.data, m.ctypes.data, v.ctypes.data, lr, t)
+    return W, m, v

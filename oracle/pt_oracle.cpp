@@ -903,3 +903,127 @@ ORC_API void orc_frame(const float* in, uint32_t n, float* out) {
     }
 }
 ORC_API uint32_t orc_scene_bvh_nodes(void* sp) { return (uint32_t)((Scene*)sp)->nodes.size(); }
+
+// ===================================================== radiance-cache MLP ====
+// CPU restatement of the cache network (64 encoded inputs, 4 hidden ReLU
+// layers of 64, 3 outputs, no biases) with the same rounding points as the
+// tensor-core kernels when `bf16` is set: encoded features, hidden
+// activations, weights and back-propagated gradients are rounded to bfloat16
+// (round to nearest even) before each product; sums are fp32.  With `bf16`
+// clear it is plain fp32 (used for finite-difference checks).
+namespace orc {
+static float bf16r(float x, bool on) {
+    if (!on) return x;
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x7fffu + ((u >> 16) & 1u)) & 0xffff0000u;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
+static float mlp_feature(const float* raw, int f) {
+    if (f < 56) {
+        int d = f >> 3, k = (f & 7) >> 1;
+        float s, c;
+        sincos_turns(raw[d] * (float)(1 << k) * 0.5f, &s, &c);
+        return (f & 1) ? c : s;
+    }
+    int r = f - 56;
+    if (r < 5) return raw[7 + r];
+    return r == 5 ? 1.0f : 0.0f;
+}
+constexpr int kP = 4 * 4096 + 8 * 64;
+struct MlpAct { float e[64], a[4][64], y[8]; };
+static void mlp_fwd(const float* W, const float* raw, bool bf, MlpAct& A) {
+    for (int f = 0; f < 64; ++f) A.e[f] = bf16r(mlp_feature(raw, f), bf);
+    const float* in = A.e;
+    for (int l = 0; l < 4; ++l) {
+        const float* Wl = W + l * 4096;
+        for (int o = 0; o < 64; ++o) {
+            float z = 0.0f;
+            for (int i = 0; i < 64; ++i) z += bf16r(Wl[o * 64 + i], bf) * in[i];
+            A.a[l][o] = bf16r(std::fmax(z, 0.0f), bf);
+        }
+        in = A.a[l];
+    }
+    const float* W4 = W + 4 * 4096;
+    for (int o = 0; o < 8; ++o) {
+        float z = 0.0f;
+        for (int i = 0; i < 64; ++i) z += bf16r(W4[o * 64 + i], bf) * in[i];
+        A.y[o] = o < 3 ? z : 0.0f;
+    }
+}
+}  // namespace orc
+
+// samples: n x 16 floats (raw 12, target 3, pad); out: n x 3
+ORC_API void orc_mlp_forward(const float* W, const float* samples, uint32_t n, float* out, int bf16) {
+    for (uint32_t s = 0; s < n; ++s) {
+        orc::MlpAct A;
+        orc::mlp_fwd(W, samples + 16 * (size_t)s, bf16 != 0, A);
+        for (int c = 0; c < 3; ++c) out[3 * (size_t)s + c] = A.y[c];
+    }
+}
+
+// Gradient of the mean relative L2 loss  mean_{s,c} (y - t)^2 / (y^2 + 0.01)  (the y^2 in the
+// denominator is held constant, as in the kernels); returns the loss.
+ORC_API float orc_mlp_gradient(const float* W, const float* samples, uint32_t n, float* dW, int bf16) {
+    const bool bf = bf16 != 0;
+    for (int i = 0; i < orc::kP; ++i) dW[i] = 0.0f;
+    double loss = 0.0;
+    const float inv = 1.0f / (3.0f * (float)n);
+    for (uint32_t s = 0; s < n; ++s) {
+        const float* S = samples + 16 * (size_t)s;
+        orc::MlpAct A;
+        orc::mlp_fwd(W, S, bf, A);
+        float gy[8] = {0};
+        for (int c = 0; c < 3; ++c) {
+            float d = A.y[c] - S[12 + c], den = A.y[c] * A.y[c] + 0.01f;
+            loss += (double)(d * d / den * inv);
+            gy[c] = orc::bf16r(2.0f * d / den * inv, bf);
+        }
+        // output layer
+        const float* W4 = W + 4 * 4096;
+        float* dW4 = dW + 4 * 4096;
+        float g[64];
+        for (int i = 0; i < 64; ++i) {
+            float acc = 0.0f;
+            for (int o = 0; o < 8; ++o) {
+                dW4[o * 64 + i] += gy[o] * A.a[3][i];
+                acc += orc::bf16r(W4[o * 64 + i], bf) * gy[o];
+            }
+            g[i] = acc;
+        }
+        for (int l = 3; l >= 0; --l) {
+            float gz[64];
+            for (int i = 0; i < 64; ++i) gz[i] = orc::bf16r(A.a[l][i] > 0.0f ? g[i] : 0.0f, bf);
+            const float* prev = l > 0 ? A.a[l - 1] : A.e;
+            const float* Wl = W + l * 4096;
+            float* dWl = dW + l * 4096;
+            for (int o = 0; o < 64; ++o)
+                for (int i = 0; i < 64; ++i) dWl[o * 64 + i] += gz[o] * prev[i];
+            if (l > 0) {
+                for (int i = 0; i < 64; ++i) {
+                    float acc = 0.0f;
+                    for (int o = 0; o < 64; ++o) acc += orc::bf16r(Wl[o * 64 + i], bf) * gz[o];
+                    g[i] = acc;
+                }
+            }
+        }
+    }
+    return (float)loss;
+}
+
+// One Adam step (beta1 0.9, beta2 0.99, eps 1e-8) at 1-based step t; padded output rows stay zero.
+ORC_API void orc_mlp_adam(float* W, const float* dW, float* m, float* v, float lr, int t) {
+    const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
+    float bc1 = 1.0f - std::pow(b1, (float)t), bc2 = 1.0f - std::pow(b2, (float)t);
+    for (int i = 0; i < orc::kP; ++i) {
+        float g = dW[i];
+        m[i] = b1 * m[i] + (1.0f - b1) * g;
+        v[i] = b2 * v[i] + (1.0f - b2) * g * g;
+        float mh = m[i] / bc1, vh = v[i] / bc2;
+        float w = W[i] - lr * mh / (std::sqrt(vh) + eps);
+        if (i >= 4 * 4096 + 3 * 64) w = 0.0f;
+        W[i] = w;
+    }
+}

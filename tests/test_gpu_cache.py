@@ -1,0 +1,129 @@
+"""Radiance cache on the GPU.
+
+* the fused BF16 tensor-core forward and the training kernel's gradients against
+  the CPU oracle of the same network (same bf16 rounding points; sums in another
+  order), one Adam step against the oracle's Adam;
+* training on tracer-style samples lowers the loss; weights save and load;
+* the gain of the trained cache: with paths ending at their third vertex,
+  finishing them with the trained network is closer to a high-spp reference
+  (relMSE) than ending them without it."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def random_samples(n, seed):
+    rng = np.random.default_rng(seed)
+    s = np.zeros((n, 16), np.float32)
+    s[:, :12] = rng.uniform(0.0, 1.0, (n, 12))
+    s[:, 12:15] = rng.uniform(0.0, 2.0, (n, 3))
+    return s
+
+
+@pytest.fixture(scope="module")
+def cache(bsm, ctx):
+    c = bsm.RadianceCache(ctx, seed=7)
+    yield c
+    c.close()
+
+
+def test_forward_matches_oracle(cache, oracle):
+    S = random_samples(1000, 1)
+    W = cache.weights()
+    g = cache.predict(S)
+    o = oracle.mlp_forward(W, S, bf16=True)
+    scale = float(np.abs(o).max())
+    assert np.abs(g - o).max() <= 1e-2 * scale + 1e-5
+    assert np.median(np.abs(g - o)) <= 1e-3 * scale
+
+
+def test_gradient_matches_oracle(cache, oracle):
+    S = random_samples(777, 2)     # not a multiple of the 16-row tile
+    W = cache.weights()
+    dg, lg = cache.gradient(S)
+    do, lo = oracle.mlp_gradient(W, S, bf16=True)
+    assert abs(lg - lo) <= 1e-3 * abs(lo)
+    blocks = [(0, 4096), (4096, 8192), (8192, 12288), (12288, 16384), (16384, 16384 + 192)]
+    for a, b in blocks:
+        x, y = dg[a:b].astype(np.float64), do[a:b].astype(np.float64)
+        assert np.abs(x - y).max() <= 2e-2 * np.abs(y).max(), (a, np.abs(x - y).max(), np.abs(y).max())
+        cos = float(x @ y / (np.linalg.norm(x) * np.linalg.norm(y)))
+        assert cos > 0.999, (a, cos)
+    assert np.all(dg[16384 + 192:] == 0.0)
+
+
+def test_adam_step_matches_oracle(cache, oracle):
+    W0 = cache.weights()
+    cache.weights(W0)              # resets the Adam state
+    S = random_samples(512, 3)
+    dg, _ = cache.gradient(S)
+    cache.train(S, batch=512, lr=1e-2)
+    W1 = cache.weights()
+    W1o, _, _ = oracle.mlp_adam(W0, dg, np.zeros_like(W0), np.zeros_like(W0), 1e-2, 1)
+    ok = np.abs(dg) > 1e-6         # the first Adam step is lr * sign(g): skip gradients at the noise floor
+    assert np.abs(W1[ok] - W1o[ok]).max() <= 1e-5
+    assert np.all(W1[16384 + 192:] == 0.0)
+
+
+def test_training_lowers_loss(bsm, ctx):
+    c = bsm.RadianceCache(ctx, seed=11)
+    try:
+        S = random_samples(8192, 4)
+        # smooth target: radiance depending on position and normal
+        S[:, 12] = 0.5 + 0.4 * np.sin(3.0 * S[:, 0]) * S[:, 6]
+        S[:, 13] = 0.3 + 0.3 * S[:, 1] * S[:, 8]
+        S[:, 14] = 0.2 + 0.5 * S[:, 2] ** 2
+        first = c.train(S, batch=8192, lr=1e-2)
+        for _ in range(60):
+            last = c.train(S, batch=8192, lr=1e-2)
+        assert last < 0.25 * first, (first, last)
+    finally:
+        c.close()
+
+
+def test_save_load_roundtrip(bsm, ctx, cache, tmp_path):
+    path = str(tmp_path / "cache.bin")
+    W = cache.weights()
+    cache.save(path)
+    other = bsm.RadianceCache(ctx, seed=99)
+    try:
+        other.load(path)
+        assert np.array_equal(other.weights(), W)
+        S = random_samples(100, 5)
+        assert np.array_equal(other.predict(S), cache.predict(S))
+    finally:
+        other.close()
+
+
+def test_trained_cache_gains_over_the_method_without_it(bsm, ctx):
+    """Paths end at their third vertex in both renders; with the trained network
+    that vertex contributes the learned outgoing radiance, without it (a network
+    whose output layer is zero) it contributes nothing.  The trained cache must be
+    much closer to a 512-spp plain render."""
+    scene = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=41, spheres=24)
+    sid = ctx.load_scene(scene)
+    cam = bsm.make_camera(tuple(scene.camera.position), tuple(scene.camera.front), width=96, height=96)
+    refs, rst = ctx.render(sid, [cam], bsm.settings(spp=512, max_segments=8, seed=1000))
+    ref = refs[0]
+    assert rst.rays_per_segment[1] > 0
+    c = bsm.RadianceCache(ctx, seed=5)
+    off = bsm.RadianceCache(ctx, seed=5)
+    try:
+        w = off.weights()
+        w[4 * 4096:] = 0.0
+        off.weights(w)
+        cs = bsm.cache_settings(train_paths=16384, train_batch=8192, train_steps=2, cache_segment=2)
+        losses = [c.render(sid, cam, bsm.settings(spp=1, seed=f + 1), cs, outputs=False)[2] for f in range(60)]
+        cs_eval = bsm.cache_settings(train_steps=0, cache_segment=2)
+        cached, st, _ = c.render(sid, cam, bsm.settings(spp=64, seed=77), cs_eval)
+        without, _, _ = off.render(sid, cam, bsm.settings(spp=64, seed=77), cs_eval)
+        e_cached = bsm.rel_mse(cached, ref)
+        e_without = bsm.rel_mse(without, ref)
+        assert np.isfinite(cached).all()
+        assert st.rays_per_segment[3] == 0           # no path goes past the cache vertex
+        assert np.mean(losses[-10:]) < np.mean(losses[:10])
+        assert e_cached < 0.5 * e_without, (e_cached, e_without)
+    finally:
+        c.close()
+        off.close()
