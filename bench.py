@@ -57,6 +57,7 @@ def parse():
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--block", type=int, default=0, help="threads per block of the traversal kernels (0 = tuned)")
     p.add_argument("--capacity", type=int, default=0, help="wavefront paths per chunk (0 = automatic)")
+    p.add_argument("--regcap", type=int, default=-1, help="1/0: force the 64-register traversal kernels (-1: tuned)")
     p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "cache"],
                    help="plain: the single-frame pass (the bench line); batch: 256 uneven views in one wavefront "
                         "against a loop of plain renders")
@@ -251,6 +252,8 @@ def run_ours(a, dist: Dist):
     sid = ctx.upload(scene)
     bvh = ctx.build_bvh(sid)
     setup_s = time.perf_counter() - t0
+    if a.regcap >= 0:
+        ctx.set_tuning(sid, bsm.TuneParams(a.block or 128, a.capacity, 16, 8, a.regcap))
     cam = scene.camera
     seed = a.seed + 1000 * dist.rank
     flags_timed = bsm.BSM_PT_STAGE_TIMING
@@ -446,6 +449,7 @@ def run_batch(a, dist):
             "equal_relmse_check": {"views_compared": len(sample), "max_rel_diff": worst},
             "tune": {"block_size": tune.best.block_size, "wavefront_capacity": tune.best.wavefront_capacity,
                      "postpone_depth": tune.best.postpone_depth, "refill_lanes": tune.best.refill_lanes,
+                     "register_cap": tune.best.register_cap,
                      "best_ms": round(tune.best_ms, 3), "default_ms": round(tune.default_ms, 3),
                      "tried": tune.tried, "from_cache": tune.from_cache, "seconds": round(tune_s, 2)},
             "config": workload_config(a, scene.num_triangles)}
@@ -539,12 +543,26 @@ def run_cache(a, dist):
                              outputs=last)
     ref = imgs[0] if a.ref_spp > per else ctx.render(sid, [cam], bsm.settings(spp=per, max_segments=a.segments,
                                                                               seed=90000))[0][0]
-    spps = [1, 2, 4, 8, 16, 32]
+    spps = [1, 2, 4, 8, 16, 32, 64]
+    seeds = 3
+
+    def trimmed(img, r, q=0.999):
+        a = img[..., :3].astype(np.float64)
+        b = r[..., :3].astype(np.float64)
+        e = ((a - b) ** 2 / (b * b + 1e-2)).ravel()
+        return float(np.mean(np.sort(e)[: int(q * e.size)]))
+
     plain = []
     for spp in spps:
         ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=a.segments, seed=5 + spp), outputs=False)
-        img, st = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=a.segments, seed=7 + spp))
-        plain.append({"spp": spp, "relmse": bsm.rel_mse(img[0], ref), "ms": st.ms_total})
+        errs, terrs, ms = [], [], []
+        for k in range(seeds):
+            img, st = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=a.segments, seed=7 + 100 * k + spp))
+            errs.append(bsm.rel_mse(img[0], ref))
+            terrs.append(trimmed(img[0], ref))
+            ms.append(st.ms_total)
+        plain.append({"spp": spp, "relmse": float(np.mean(errs)), "relmse_trimmed": float(np.mean(terrs)),
+                      "ms": float(np.mean(ms))})
     cache = bsm.RadianceCache(ctx, seed=a.seed)
     cs = bsm.cache_settings()
     t0 = time.perf_counter()
@@ -555,35 +573,57 @@ def run_cache(a, dist):
     train_s = time.perf_counter() - t0
     cached = []
     for spp in spps:
-        ctx.sync()
-        w0 = time.perf_counter()
-        img, st, _ = cache.render(sid, cam, bsm.settings(spp=spp, seed=3000 + spp), cs)   # trains, then renders
-        wall = (time.perf_counter() - w0) * 1e3
-        cached.append({"spp": spp, "relmse": bsm.rel_mse(img, ref), "ms": wall, "ms_render": st.ms_total})
+        errs, terrs, ms, msr = [], [], [], []
+        for k in range(seeds):
+            ctx.sync()
+            w0 = time.perf_counter()
+            img, st, _ = cache.render(sid, cam, bsm.settings(spp=spp, seed=3000 + 100 * k + spp), cs)  # train + render
+            ms.append((time.perf_counter() - w0) * 1e3)
+            msr.append(st.ms_total)
+            errs.append(bsm.rel_mse(img, ref))
+            terrs.append(trimmed(img, ref))
+        cached.append({"spp": spp, "relmse": float(np.mean(errs)), "relmse_trimmed": float(np.mean(terrs)),
+                       "ms": float(np.mean(ms)), "ms_render": float(np.mean(msr))})
     cache.close()
     ctx.close()
 
-    def time_at(curve, target):
-        """Frame time needed to reach `target` relMSE (log-log interpolation; None if never reached)."""
-        pts = sorted((c["relmse"], c["ms"]) for c in curve)
-        for (e0, t0_), (e1, t1) in zip(pts[1:], pts[:-1]):
-            pass
-        xs = [c["relmse"] for c in curve]
-        ts = [c["ms"] for c in curve]
-        for i in range(len(curve) - 1):
-            e0, e1 = xs[i], xs[i + 1]
-            if (e0 - target) * (e1 - target) <= 0 and e0 != e1:
-                u = (np.log(target) - np.log(e0)) / (np.log(e1) - np.log(e0))
-                return float(np.exp(np.log(ts[i]) + u * (np.log(ts[i + 1]) - np.log(ts[i]))))
-        return None
-    equal = []
-    for c in cached:
-        tp = time_at(plain, c["relmse"])
-        equal.append({"relmse": round(c["relmse"], 6), "cached_fps": round(1e3 / c["ms"], 2),
-                      "plain_fps": round(1e3 / tp, 2) if tp else None,
-                      "speedup": round(tp / c["ms"], 3) if tp else None})
+    def fit_err(curve, key, biased):
+        """relMSE(spp) ~ V / spp (+ B for the biased cached estimator), least squares on the measured points."""
+        x = np.array([1.0 / c["spp"] for c in curve])
+        y = np.array([c[key] for c in curve])
+        if biased:
+            A = np.stack([x, np.ones_like(x)], 1)
+            (V, B), *_ = np.linalg.lstsq(A, y, rcond=None)
+            return float(V), float(max(B, 0.0))
+        return float((x @ y) / (x @ x)), 0.0
+
+    def fit_time(curve):
+        x = np.array([c["spp"] for c in curve], np.float64)
+        y = np.array([c["ms"] for c in curve])
+        A = np.stack([x, np.ones_like(x)], 1)
+        (t1, t0_), *_ = np.linalg.lstsq(A, y, rcond=None)
+        return float(t1), float(t0_)
+
+    equal = {}
+    for key in ("relmse", "relmse_trimmed"):
+        Vp, _ = fit_err(plain, key, False)
+        Vc, Bc = fit_err(cached, key, True)
+        tp1, tp0 = fit_time(plain)
+        tc1, tc0 = fit_time(cached)
+        rows = []
+        for ref_spp in (4, 16, 64):
+            target = Vp / ref_spp
+            spp_c = Vc / (target - Bc) if target > Bc else None
+            t_p = tp0 + tp1 * ref_spp
+            t_c = tc0 + tc1 * spp_c if spp_c else None
+            rows.append({"target_relmse": round(target, 6), "plain_spp": ref_spp, "plain_fps": round(1e3 / t_p, 2),
+                         "cached_spp": round(spp_c, 2) if spp_c else None,
+                         "cached_fps": round(1e3 / t_c, 2) if t_c else None,
+                         "speedup": round(t_p / t_c, 3) if t_c else None})
+        equal[key] = {"plain_fit": {"V": Vp}, "cached_fit": {"V": Vc, "B": Bc}, "at": rows}
     line = {"workload": "cache", "metric": "frames/s at equal relMSE, cached vs plain pass",
-            "reference_spp": a.ref_spp, "plain": plain, "cached": cached, "equal_relmse": equal,
+            "reference_spp": a.ref_spp, "seeds_per_point": seeds, "plain": plain, "cached": cached,
+            "equal_relmse": equal,
             "train": {"frames": a.train_frames, "seconds": round(train_s, 2),
                       "loss_first10": round(float(np.mean(losses[:10])), 4),
                       "loss_last10": round(float(np.mean(losses[-10:])), 4),

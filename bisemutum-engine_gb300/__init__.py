@@ -109,7 +109,7 @@ class ViewDesc(C.Structure):
 
 class TuneParams(C.Structure):
     _fields_ = [("block_size", C.c_uint32), ("wavefront_capacity", C.c_uint32), ("postpone_depth", C.c_uint32),
-                ("refill_lanes", C.c_uint32)]
+                ("refill_lanes", C.c_uint32), ("register_cap", C.c_uint32)]
 
 
 class TuneResult(C.Structure):

@@ -198,12 +198,14 @@ void build_sky_tables(const bsm_sky& sky, std::vector<float>& marg, std::vector<
         pdf[k] = total > 0.0 ? (float)(w[k] * (double)W * (double)H / total) : 0.0f;
 }
 
-bsm_status ensure_launch_cfg(bsm_context* ctx, uint32_t block) {
+bsm_status ensure_launch_cfg(bsm_context* ctx, uint32_t block, int regcap = 0) {
     int b = block ? (int)block : 128;
     if (b != 64 && b != 128 && b != 256) return fail(ctx, BSM_ERR_INVALID_ARG, "block_size must be 64, 128 or 256");
-    if (ctx->lc_block == b) return BSM_OK;
+    int key = b | (regcap << 16);
+    if (ctx->lc_block == key) return BSM_OK;
+    ctx->lc.regcap = regcap;
     query_launch_cfg(ctx->device, b, &ctx->lc);
-    ctx->lc_block = b;
+    ctx->lc_block = key;
     return BSM_OK;
 }
 
@@ -636,7 +638,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
     bsm_status st;
     // tuned parameters of this scene fill in what the settings leave at 0
     uint32_t block = s.block_size ? s.block_size : (sc->tuned ? sc->tune.block_size : 0u);
-    if ((st = ensure_launch_cfg(ctx, block))) return st;
+    if ((st = ensure_launch_cfg(ctx, block, sc->tuned ? (int)(sc->tune.register_cap != 0) : 0))) return st;
     ctx->lc.postpone_sp = sc->tuned ? (int)sc->tune.postpone_depth : 16;
     ctx->lc.refill_min = sc->tuned ? (int)sc->tune.refill_lanes : 8;
     const bsm_camera* views = nullptr;
@@ -874,7 +876,7 @@ namespace {
 bool valid_tune(const bsm_tune_params& p) {
     return (p.block_size == 64 || p.block_size == 128 || p.block_size == 256) &&
            (p.wavefront_capacity == 0 || p.wavefront_capacity >= 1024) && p.postpone_depth <= 16 &&
-           p.refill_lanes >= 1 && p.refill_lanes <= 32;
+           p.refill_lanes >= 1 && p.refill_lanes <= 32 && p.register_cap <= 1;
 }
 
 std::string tune_key(bsm_context* ctx, const Scene* sc, uint64_t paths) {
@@ -928,8 +930,9 @@ extern "C" bsm_status bsm_autotune(bsm_context* ctx, uint32_t scene_id, const bs
                 char k[400];
                 bsm_tune_params p{};
                 float ms = 0.0f;
-                if (std::sscanf(line, "%399s %u %u %u %u %f", k, &p.block_size, &p.wavefront_capacity,
-                                &p.postpone_depth, &p.refill_lanes, &ms) == 6 && key == k && valid_tune(p)) {
+                if (std::sscanf(line, "%399s %u %u %u %u %u %f", k, &p.block_size, &p.wavefront_capacity,
+                                &p.postpone_depth, &p.refill_lanes, &p.register_cap, &ms) == 7 && key == k &&
+                    valid_tune(p)) {
                     result->best = p;
                     result->best_ms = ms;
                     result->from_cache = 1;
@@ -966,7 +969,7 @@ extern "C" bsm_status bsm_autotune(bsm_context* ctx, uint32_t scene_id, const bs
         result->tried++;
         return BSM_OK;
     };
-    bsm_tune_params cur{128, 0, 16, 8};
+    bsm_tune_params cur{128, 0, 16, 8, 0};
     float cur_ms = 0.0f;
     bsm_status e = measure(cur, &cur_ms);
     if (e) { sc->tune = saved; sc->tuned = had; return e; }
@@ -993,6 +996,7 @@ extern "C" bsm_status bsm_autotune(bsm_context* ctx, uint32_t scene_id, const bs
         }
         for (uint32_t v : postpones) { if (e) break; if (v != cur.postpone_depth) { bsm_tune_params p = cur; p.postpone_depth = v; e = try_one(p); } }
         for (uint32_t v : refills) { if (e) break; if (v != cur.refill_lanes) { bsm_tune_params p = cur; p.refill_lanes = v; e = try_one(p); } }
+        if (!e) { bsm_tune_params p = cur; p.register_cap = cur.register_cap ^ 1u; e = try_one(p); }
         if (e) { sc->tune = saved; sc->tuned = had; return e; }
         if (!improved) break;
     }
@@ -1003,8 +1007,8 @@ extern "C" bsm_status bsm_autotune(bsm_context* ctx, uint32_t scene_id, const bs
     if (cache_path) {
         FILE* f = std::fopen(cache_path, "a");
         if (f) {
-            std::fprintf(f, "%s %u %u %u %u %.4f\n", key.c_str(), cur.block_size, cur.wavefront_capacity,
-                         cur.postpone_depth, cur.refill_lanes, cur_ms);
+            std::fprintf(f, "%s %u %u %u %u %u %.4f\n", key.c_str(), cur.block_size, cur.wavefront_capacity,
+                         cur.postpone_depth, cur.refill_lanes, cur.register_cap, cur_ms);
             std::fclose(f);
         }
     }

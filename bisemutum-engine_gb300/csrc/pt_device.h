@@ -8,7 +8,9 @@
 //                        PCG32 state low/high word
 //   thr[2][C]    float4  throughput.rgb, pdf of the sampled direction
 //   hit[C]       float4  t, leaf triangle index, u, v
-//   sh_o/sh_d/sh_c[(L+1) C] float4  shadow rays and their contributions
+//   sh_o/sh_d/sh_c[(L+1) C] float4  shadow rays and their contributions: sun
+//                rays fill the queue from the front, sky rays from the back, so
+//                a warp of the any-hit kernel traces rays of one kind
 //   counters     uint32  queue sizes per segment, work counters, error flags
 //   stats        uint64  rays per segment (summed over chunks)
 // All queues are structures of arrays read with 128-bit loads.
@@ -65,9 +67,10 @@ struct DevView {
 // counters[] word offsets
 enum : uint32_t {
     kCntQueue = 0,                 // [kMaxSeg + 1] extend queue size entering segment s
-    kCntShadow = kCntQueue + 17,   // [kMaxSeg] shadow queue size of segment s
+    kCntShadow = kCntQueue + 17,   // [kMaxSeg] sun shadow rays of segment s (queue front)
     kCntWork = kCntShadow + 16,    // [2 * kMaxSeg] persistent-kernel work counters
-    kCntCache = kCntWork + 32,     // radiance-cache queries of the chunk
+    kCntSky = kCntWork + 32,       // [kMaxSeg] sky shadow rays of segment s (queue back)
+    kCntCache = kCntSky + 16,      // radiance-cache queries of the chunk
     kCntError = kCntCache + 1,     // error flags (bit 0: queue overflow); words below it are cleared per chunk
     kCntWords = kCntError + 1
 };
@@ -102,6 +105,7 @@ struct LaunchCfg {
     int grid_shade;
     int postpone_sp = 16;   // traversal stack budget for postponed triangle groups
     int refill_min = 8;     // idle lanes that trigger a warp refill
+    int regcap = 0;         // 1: traversal kernels compiled for 4 blocks of 256 (64 registers)
 };
 
 // ---- launch wrappers (pt_kernels.cu) ----
@@ -133,7 +137,8 @@ cudaError_t launch_mlp_adam(cudaStream_t st, float* wm, void* wb, const float* d
 void launch_train_paths(cudaStream_t st, const DevScene& sc, const DevView* view, uint32_t n_paths, uint32_t frame,
                         uint32_t max_segments, float4* samples, uint32_t* count, uint32_t max_samples);
 
-// Fills the persistent-kernel grids from the device's SM count and occupancy.
+// Fills the persistent-kernel grids from the device's SM count and occupancy
+// (for the kernel variant lc->regcap selects).
 void query_launch_cfg(int device, int block_trace, LaunchCfg* lc);
 
 }  // namespace bsm

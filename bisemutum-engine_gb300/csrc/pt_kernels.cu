@@ -79,8 +79,8 @@ __global__ void k_camera(const DevView* __restrict__ views, uint32_t n_views, ui
 }
 
 // ---------------------------------------------------------------- extend ----
-template <bool kCount>
-__global__ void __launch_bounds__(256) k_extend(DevScene sc, const float4* __restrict__ ray_o,
+template <bool kCount, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) k_extend(DevScene sc, const float4* __restrict__ ray_o,
                                                 const float4* __restrict__ ray_d, float4* __restrict__ hit,
                                                 uint32_t* counters, unsigned long long* stats, uint32_t seg,
                                                 int postpone_sp, int refill_min) {
@@ -108,19 +108,24 @@ __global__ void __launch_bounds__(256) k_extend(DevScene sc, const float4* __res
 }
 
 // ---------------------------------------------------------------- shadow ----
-__global__ void __launch_bounds__(256) k_shadow(DevScene sc, Wavefront wf, uint32_t seg, float4* accum,
-                                                int postpone_sp, int refill_min) {
-    uint32_t n = wf.counters[kCntShadow + seg];
+template <int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) k_shadow(DevScene sc, Wavefront wf, uint32_t seg, float4* accum,
+                                                            int postpone_sp, int refill_min) {
+    const uint32_t n_sun = wf.counters[kCntShadow + seg], n_sky = wf.counters[kCntSky + seg];
+    const uint32_t sh_cap = wf.capacity * (sc.num_lights + 1u);
+    const uint32_t n = n_sun + n_sky;
     if (blockIdx.x == 0 && threadIdx.x == 0) wf.stats[kStatShadow + seg] += n;
     const float4* __restrict__ so = wf.sh_o;
     const float4* __restrict__ sd = wf.sh_d;
     const float4* __restrict__ scn = wf.sh_c;
+    // work index i < n_sun: sun ray i; otherwise sky ray at the back of the queue
+    auto slot = [=](uint32_t i) { return i < n_sun ? i : sh_cap - 1u - (i - n_sun); };
     trace_queue<true, false>(
         sc.nodes, sc.tris, n, wf.counters + kCntWork + 2 * seg + 1,
-        [&](uint32_t i, float4& o, float4& d) { o = so[i]; d = sd[i]; },
+        [&](uint32_t i, float4& o, float4& d) { uint32_t k = slot(i); o = so[k]; d = sd[k]; },
         [&](uint32_t i, uint32_t leaf, float, float, float) {
             if (leaf == kMissPrim) {
-                float4 c = scn[i];
+                float4 c = scn[slot(i)];
                 accum_add(accum, __float_as_uint(c.w), v3(c.x, c.y, c.z));
             }
         },
@@ -251,7 +256,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene sc, const DevView* __res
             }
             uint32_t slot = warp_alloc(emit, wf.counters + kCntShadow + seg);
             if (emit) {
-                if (slot < sh_cap) {
+                if (slot < cap * sc.num_lights) {
                     wf.sh_o[slot] = make_float4(org.x, org.y, org.z, tmin);
                     wf.sh_d[slot] = make_float4(L.x, L.y, L.z, ray_len);
                     wf.sh_c[slot] = make_float4(c.x, c.y, c.z, __uint_as_float(m4.x));
@@ -280,12 +285,13 @@ __global__ void __launch_bounds__(256) k_shade(DevScene sc, const DevView* __res
                     }
                 }
             }
-            uint32_t slot = warp_alloc(emit, wf.counters + kCntShadow + seg);
+            uint32_t slot = warp_alloc(emit, wf.counters + kCntSky + seg);
             if (emit) {
-                if (slot < sh_cap) {
-                    wf.sh_o[slot] = make_float4(org.x, org.y, org.z, tmin);
-                    wf.sh_d[slot] = make_float4(L.x, L.y, L.z, ray_len);
-                    wf.sh_c[slot] = make_float4(c.x, c.y, c.z, __uint_as_float(m4.x));
+                if (slot < cap) {
+                    uint32_t k = sh_cap - 1u - slot;   // sky rays fill the queue from the back
+                    wf.sh_o[k] = make_float4(org.x, org.y, org.z, tmin);
+                    wf.sh_d[k] = make_float4(L.x, L.y, L.z, ray_len);
+                    wf.sh_c[k] = make_float4(c.x, c.y, c.z, __uint_as_float(m4.x));
                 } else {
                     atomicOr(wf.counters + kCntError, 1u);
                 }
@@ -384,13 +390,17 @@ void launch_camera(const LaunchCfg& lc, cudaStream_t st, const DevView* views, u
 void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, int q,
                    uint32_t seg, bool count_traversal) {
     if (count_traversal)
-        k_extend<true><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
-                                                                        wf.counters, wf.stats, seg, lc.postpone_sp,
-                                                                        lc.refill_min);
+        k_extend<true, 1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
+                                                                           wf.counters, wf.stats, seg,
+                                                                           lc.postpone_sp, lc.refill_min);
+    else if (lc.regcap)
+        k_extend<false, 4><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
+                                                                            wf.counters, wf.stats, seg,
+                                                                            lc.postpone_sp, lc.refill_min);
     else
-        k_extend<false><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
-                                                                         wf.counters, wf.stats, seg, lc.postpone_sp,
-                                                                         lc.refill_min);
+        k_extend<false, 1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
+                                                                            wf.counters, wf.stats, seg,
+                                                                            lc.postpone_sp, lc.refill_min);
 }
 void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const DevView* views,
                   const Wavefront& wf, int q, uint32_t seg, float4* accum) {
@@ -398,7 +408,12 @@ void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, cons
 }
 void launch_shadow(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, uint32_t seg,
                    float4* accum) {
-    k_shadow<<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp, lc.refill_min);
+    if (lc.regcap)
+        k_shadow<4><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp,
+                                                                     lc.refill_min);
+    else
+        k_shadow<1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp,
+                                                                     lc.refill_min);
 }
 void launch_resolve(cudaStream_t st, const float4* accum, uint32_t width, uint32_t height, float inv_spp,
                     float4* out, uint32_t pitch_px) {
@@ -425,8 +440,13 @@ void query_launch_cfg(int device, int block_trace, LaunchCfg* lc) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int per_sm_ext = 0, per_sm_sh = 0, per_sm_shade = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false>, block_trace, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow, block_trace, 0);
+    if (lc->regcap) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, 4>, block_trace, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<4>, block_trace, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, 1>, block_trace, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<1>, block_trace, 0);
+    }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_shade, k_shade, 256, 0);
     int per_sm = per_sm_ext < per_sm_sh ? per_sm_ext : per_sm_sh;
     if (per_sm < 1) per_sm = 1;

@@ -133,9 +133,13 @@ __device__ __forceinline__ bool tri_test(const RayPre& r, float4 a, float4 b, fl
     return true;
 }
 
-// Byte k of w as a float: PRMT builds 2^23 + byte, the FADD removes 2^23 exactly.
+// Byte k of w as the float 2^23 + byte (one PRMT).  The slab constants below
+// absorb the 2^23 offset: t = (2^23 + q) s + (a - 2^23 s).  Rounding the folded
+// constant costs at most half a quantisation step of the plane, inside the one
+// step by which the builder pads every child box outward, so the test stays
+// conservative.
 __device__ __forceinline__ float qbyte(uint32_t w, uint32_t k) {
-    return __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7440u | k)) - 8388608.0f;
+    return __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7440u | k));
 }
 
 // Intersects the eight children of node `ni`; returns the group of internal
@@ -153,6 +157,9 @@ __device__ __forceinline__ void node_test(const RayPre& r, const CwNode* __restr
     float ax = (__uint_as_float(n0.x) - r.ox) * r.idx;
     float ay = (__uint_as_float(n0.y) - r.oy) * r.idy;
     float az = (__uint_as_float(n0.z) - r.oz) * r.idz;
+    ax = __fsub_rn(ax, 8388608.0f * sx);
+    ay = __fsub_rn(ay, 8388608.0f * sy);
+    az = __fsub_rn(az, 8388608.0f * sz);
     float sxf = sx * BSM_BOX_PAD, syf = sy * BSM_BOX_PAD, szf = sz * BSM_BOX_PAD;
     float axf = ax * BSM_BOX_PAD, ayf = ay * BSM_BOX_PAD, azf = az * BSM_BOX_PAD;
     uint32_t imask = ew >> 24;

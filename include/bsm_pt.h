@@ -252,6 +252,7 @@ typedef struct bsm_tune_params {
     uint32_t wavefront_capacity;  /* paths per chunk (queue capacity) */
     uint32_t postpone_depth;      /* traversal stack entries open to postponed triangle groups (0..16) */
     uint32_t refill_lanes;        /* idle lanes that make a warp fetch new rays (1..32) */
+    uint32_t register_cap;        /* 1: traversal kernels limited to 64 registers (more warps per SM) */
 } bsm_tune_params;
 
 typedef struct bsm_tune_result {

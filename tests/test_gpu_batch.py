@@ -73,7 +73,7 @@ def test_autotune_persists_and_keeps_results(bsm, ctx, scene, tmp_path):
     ref, _, _ = osc.render(cam.as_array(), spp=spp, max_segments=segs, seed=seed)
     assert rel_err(img[0], ref).max() <= RTOL
     # every tunable corner gives the same image
-    for p in [(64, 4096, 0, 1), (256, 1 << 20, 16, 32), (128, 1024, 4, 16)]:
+    for p in [(64, 4096, 0, 1, 0), (256, 1 << 20, 16, 32, 1), (128, 1024, 4, 16, 1)]:
         ctx.set_tuning(sid, bsm.TuneParams(*p))
         im, _ = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=segs, seed=seed))
         assert rel_err(im[0], ref).max() <= RTOL
@@ -83,6 +83,8 @@ def test_autotune_persists_and_keeps_results(bsm, ctx, scene, tmp_path):
 def test_set_tuning_rejects_bad_values(bsm, ctx, scene):
     sc, sid, osc = scene
     with pytest.raises(bsm.BsmError):
-        ctx.set_tuning(sid, bsm.TuneParams(100, 0, 16, 8))
+        ctx.set_tuning(sid, bsm.TuneParams(100, 0, 16, 8, 0))
     with pytest.raises(bsm.BsmError):
-        ctx.set_tuning(sid, bsm.TuneParams(128, 0, 17, 8))
+        ctx.set_tuning(sid, bsm.TuneParams(128, 0, 17, 8, 0))
+    with pytest.raises(bsm.BsmError):
+        ctx.set_tuning(sid, bsm.TuneParams(128, 0, 16, 8, 2))
