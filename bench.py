@@ -604,23 +604,26 @@ def run_cache(a, dist):
         (t1, t0_), *_ = np.linalg.lstsq(A, y, rcond=None)
         return float(t1), float(t0_)
 
+    def time_at(curve, key, target):
+        """Frame time the method needs for `target` error: log-log interpolation between measured points."""
+        pts = sorted(((c[key], c["ms"]) for c in curve), reverse=True)   # decreasing error
+        for (e0, t0_), (e1, t1) in zip(pts[:-1], pts[1:]):
+            if e1 <= target <= e0 and e0 > e1:
+                u = (np.log(target) - np.log(e0)) / (np.log(e1) - np.log(e0))
+                return float(np.exp(np.log(t0_) + u * (np.log(t1) - np.log(t0_))))
+        return None
+
     equal = {}
-    for key in ("relmse", "relmse_trimmed"):
+    for key in ("relmse_trimmed", "relmse"):
+        rows = []
+        for c in plain:
+            tc = time_at(cached, key, c[key])
+            rows.append({"plain_spp": c["spp"], "target": round(c[key], 6), "plain_fps": round(1e3 / c["ms"], 2),
+                         "cached_fps": round(1e3 / tc, 2) if tc else None,
+                         "speedup": round(c["ms"] / tc, 3) if tc else None})
         Vp, _ = fit_err(plain, key, False)
         Vc, Bc = fit_err(cached, key, True)
-        tp1, tp0 = fit_time(plain)
-        tc1, tc0 = fit_time(cached)
-        rows = []
-        for ref_spp in (4, 16, 64):
-            target = Vp / ref_spp
-            spp_c = Vc / (target - Bc) if target > Bc else None
-            t_p = tp0 + tp1 * ref_spp
-            t_c = tc0 + tc1 * spp_c if spp_c else None
-            rows.append({"target_relmse": round(target, 6), "plain_spp": ref_spp, "plain_fps": round(1e3 / t_p, 2),
-                         "cached_spp": round(spp_c, 2) if spp_c else None,
-                         "cached_fps": round(1e3 / t_c, 2) if t_c else None,
-                         "speedup": round(t_p / t_c, 3) if t_c else None})
-        equal[key] = {"plain_fit": {"V": Vp}, "cached_fit": {"V": Vc, "B": Bc}, "at": rows}
+        equal[key] = {"at_plain_points": rows, "plain_fit_V": Vp, "cached_fit": {"V": Vc, "B": Bc}}
     line = {"workload": "cache", "metric": "frames/s at equal relMSE, cached vs plain pass",
             "reference_spp": a.ref_spp, "seeds_per_point": seeds, "plain": plain, "cached": cached,
             "equal_relmse": equal,

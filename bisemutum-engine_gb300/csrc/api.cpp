@@ -638,7 +638,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
     bsm_status st;
     // tuned parameters of this scene fill in what the settings leave at 0
     uint32_t block = s.block_size ? s.block_size : (sc->tuned ? sc->tune.block_size : 0u);
-    if ((st = ensure_launch_cfg(ctx, block, sc->tuned ? (int)(sc->tune.register_cap != 0) : 0))) return st;
+    if ((st = ensure_launch_cfg(ctx, block, sc->tuned ? (int)(sc->tune.register_cap != 0) : 1))) return st;
     ctx->lc.postpone_sp = sc->tuned ? (int)sc->tune.postpone_depth : 16;
     ctx->lc.refill_min = sc->tuned ? (int)sc->tune.refill_lanes : 8;
     const bsm_camera* views = nullptr;
@@ -969,7 +969,7 @@ extern "C" bsm_status bsm_autotune(bsm_context* ctx, uint32_t scene_id, const bs
         result->tried++;
         return BSM_OK;
     };
-    bsm_tune_params cur{128, 0, 16, 8, 0};
+    bsm_tune_params cur{128, 0, 16, 8, 1};
     float cur_ms = 0.0f;
     bsm_status e = measure(cur, &cur_ms);
     if (e) { sc->tune = saved; sc->tuned = had; return e; }

@@ -105,7 +105,7 @@ struct LaunchCfg {
     int grid_shade;
     int postpone_sp = 16;   // traversal stack budget for postponed triangle groups
     int refill_min = 8;     // idle lanes that trigger a warp refill
-    int regcap = 0;         // 1: traversal kernels compiled for 4 blocks of 256 (64 registers)
+    int regcap = 1;         // 1: traversal kernels compiled for 4 blocks of 256 (64 registers); the default
 };
 
 // ---- launch wrappers (pt_kernels.cu) ----

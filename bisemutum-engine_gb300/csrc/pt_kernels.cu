@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_shadow(DevScene sc, Wavefro
 }
 
 // ----------------------------------------------------------------- shade ----
-__global__ void __launch_bounds__(256) k_shade(DevScene sc, const DevView* __restrict__ views, Wavefront wf,
+__global__ void __launch_bounds__(256, 3) k_shade(DevScene sc, const DevView* __restrict__ views, Wavefront wf,
                                                int q, uint32_t seg, float4* accum) {
     const uint32_t n = wf.counters[kCntQueue + seg];
     const uint32_t cap = wf.capacity;
@@ -244,7 +244,9 @@ __global__ void __launch_bounds__(256) k_shade(DevScene sc, const DevView* __res
         V3 lv = to_local(fr, V);
         float p_spec = spec_probability(surf, lv.z);
         // next-event estimation: directional lights (lights.hlsl:10-13, dir_light_eval)
-        for (uint32_t l = 0; l < sc.num_lights; ++l) {
+#pragma unroll
+        for (uint32_t l = 0; l < (uint32_t)kMaxLights; ++l) {
+            if (l >= sc.num_lights) break;
             V3 c = v3s(0.0f);
             V3 L = v3(sc.light_dir[l].x, sc.light_dir[l].y, sc.light_dir[l].z);
             bool emit = false;

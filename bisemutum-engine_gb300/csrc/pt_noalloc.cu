@@ -48,6 +48,7 @@ cudaError_t scratch_for_device(int dev, void** out) {
         g_scratch_addr[dev] = p;
     }
     if (!g_lc_valid[dev]) {
+        g_lc[dev].regcap = 1;
         query_launch_cfg(dev, 128, &g_lc[dev]);
         g_lc_valid[dev] = true;
     }

@@ -332,6 +332,7 @@ extern "C" bsm_status bsm_server_start(bsm_context* ctx, const bsm_server_opts* 
         ctx_set_error(ctx, "server options out of range (lanes <= 16, chunk_paths >= 1024, views <= 4096)");
         return BSM_ERR_INVALID_ARG;
     }
+    S->lc.regcap = 1;
     query_launch_cfg(S->device, 128, &S->lc);
     S->lights = std::max(ctx_max_lights(ctx), (uint32_t)kMaxLights);
     const size_t C = S->opts.chunk_paths, SH = C * (S->lights + 1);
