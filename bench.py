@@ -296,6 +296,7 @@ def run_ours(a, dist: Dist):
         shadow_rays += st.shadow_rays
         launches += st.chunks * (1 + 3 * a.segments)
         ext_launches = st.extend_launches
+        seg_rays = [int(st.rays_per_segment[k]) for k in range(a.segments)]
     ctx.sync()
     dist.barrier()
     wall = time.perf_counter() - wall0
@@ -367,7 +368,8 @@ def run_ours(a, dist: Dist):
                 "stages_ms_per_step": {"camera": round(ms_cam / a.steps, 3), "extend": round(ms_ext / a.steps, 3),
                                        "shade": round(ms_shade / a.steps, 3),
                                        "shadow": round(ms_shadow / a.steps, 3)},
-                "rays_per_step": {"extend": rays // a.steps, "shadow": shadow_rays // a.steps},
+                "rays_per_step": {"extend": rays // a.steps, "shadow": shadow_rays // a.steps,
+                                  "extend_per_segment": seg_rays},
                 "shadow_mrays_per_s": round(shadow_rays / (ms_shadow / 1e3) / 1e6, 1) if ms_shadow > 0 else None,
                 "bvh": {"build_s_host": round(bvh.build_ms / 1e3, 3), "nodes": bvh.num_nodes,
                         "depth": bvh.max_depth, "bytes": bvh.node_bytes + bvh.tri_bytes,

@@ -95,6 +95,11 @@ class ViewOutput(C.Structure):
     _fields_ = [("rgba", C.c_void_p), ("row_pitch_px", C.c_uint32), ("location", C.c_uint32)]
 
 
+class PrimaryOutput(C.Structure):
+    _fields_ = [("depth", C.c_void_p), ("gbuffer", C.c_void_p * 4), ("hit_positions", C.c_void_p),
+                ("location", C.c_uint32)]
+
+
 class RenderStats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("rays_per_segment", C.c_uint64 * 16), ("chunks", C.c_uint32), ("extend_launches", C.c_uint32),
@@ -188,6 +193,8 @@ _SIGS = {
     "bsm_trace_closest": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
     "bsm_trace_any": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
     "bsm_trace_counts": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "bsm_render_primary": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.POINTER(PtSettings), C.c_float,
+                                       C.c_float, C.POINTER(PrimaryOutput)]),
     "bsm_render_noalloc": (C.c_int32, [C.c_void_p, C.c_uint32, C.POINTER(Camera), C.POINTER(PtSettings),
                                        C.c_void_p]),
     "bsm_server_start": (C.c_int32, [C.c_void_p, C.POINTER(ServerOpts)]),
@@ -444,6 +451,24 @@ class Context:
         self.check(self._L.bsm_trace_counts(self.h, scene_id, rays.ctypes.data, rays.shape[0], cnt.ctypes.data))
         return cnt
 
+    def render_primary(self, scene_id: int, cam: Camera, s: PtSettings | None = None, near_z: float = 0.0,
+                       far_z: float = 0.0):
+        """Primary-hit outputs of one pixel-centre ray per pixel: (depth (H, W), G-buffer (4, H, W, 4) as
+        base_color, normal_roughness, fresnel, material_0, hit positions (H, W, 4))."""
+        h, w = cam.height, cam.width
+        depth = np.zeros((h, w), np.float32)
+        gb = np.zeros((4, h, w, 4), np.float32)
+        hp = np.zeros((h, w, 4), np.float32)
+        out = PrimaryOutput()
+        out.depth = depth.ctypes.data
+        for k in range(4):
+            out.gbuffer[k] = gb[k].ctypes.data
+        out.hit_positions = hp.ctypes.data
+        out.location = BSM_HOST
+        self.check(self._L.bsm_render_primary(self.h, scene_id, C.byref(cam), C.byref(s) if s is not None else None,
+                                              near_z, far_z, C.byref(out)))
+        return depth, gb, hp
+
     # render
     def render(self, scene_id: int, cameras, s: PtSettings, outputs: bool = True, stats: bool = True):
         """Renders views; returns (list of (H, W, 4) float32 images or None, RenderStats or None)."""
@@ -632,22 +657,43 @@ class PathTracingSettings:
     seed: int = 1
 
 
+@dataclass
+class GBufferTextures:
+    """GBufferTextures (renderer/context/gbuffer.hpp): the four packed planes of gbuffer.hlsl:6-11."""
+    base_color: np.ndarray
+    normal_roughness: np.ndarray
+    fresnel: np.ndarray
+    material_0: np.ndarray
+
+
 class PathTracingPass:
     """Mirror of PathTracingPass (path_tracing.hpp:13-35) on the GB300 pass.
 
     update_params() takes the lights and skybox the reference reads from its
     LightsContext / SkyboxContext; render() traces one camera and returns the
-    pass output's colour (the running mean over accumulated frames)."""
+    pass's OutputData: the colour (running mean over the accumulated frames),
+    the reverse-Z depth and the G-buffer of the primary hit, and no velocity
+    (invalid in the reference too, path_tracing.cpp:553-558).
+
+    History follows path_tracing.cpp:231-245: it continues only while the same
+    camera (position, orientation, field of view) and size are rendered on
+    consecutive frames.  Frames are counted by this object; a caller that skips
+    frames passes `frame_index` (the engine's frame count) and a gap resets
+    the history as the reference's `last_frame + 1 == frame_count` test does."""
 
     @dataclass
     class OutputData:
         color: np.ndarray
+        depth: np.ndarray | None = None
+        velocity: None = None
+        gbuffer: GBufferTextures | None = None
 
     def __init__(self, ctx: Context, scene: SceneData):
         self.ctx = ctx
         self.scene = scene
         self.scene_id = None
         self.frame = 0
+        self.last_frame = None
 
     def update_params(self, lights=None, skybox=None, settings_: PathTracingSettings | None = None):
         if lights is not None:
@@ -658,11 +704,20 @@ class PathTracingPass:
             self.ctx.release(self.scene_id)
         self.scene_id = self.ctx.load_scene(self.scene)
 
-    def render(self, camera: Camera, settings_: PathTracingSettings) -> "PathTracingPass.OutputData":
+    def render(self, camera: Camera, settings_: PathTracingSettings, frame_index: int | None = None,
+               near_z: float = 0.01, far_z: float = 10000.0, primary: bool = True) -> "PathTracingPass.OutputData":
         if self.scene_id is None:
             self.update_params()
+        frame = self.frame + 1 if frame_index is None else int(frame_index)
+        consecutive = self.last_frame is not None and self.last_frame + 1 == frame
         s = settings(spp=settings_.spp, max_bounces=settings_.max_bounces, seed=settings_.seed,
-                     ray_length=settings_.ray_length, accumulate=1 if settings_.accumulate else 0)
+                     ray_length=settings_.ray_length, accumulate=1 if settings_.accumulate and consecutive else 0)
         imgs, _ = self.ctx.render(self.scene_id, [camera], s, outputs=True, stats=False)
-        self.frame += 1
-        return PathTracingPass.OutputData(color=imgs[0])
+        self.frame = frame
+        self.last_frame = frame
+        out = PathTracingPass.OutputData(color=imgs[0])
+        if primary:
+            depth, gb, _ = self.ctx.render_primary(self.scene_id, camera, s, near_z, far_z)
+            out.depth = depth
+            out.gbuffer = GBufferTextures(gb[0], gb[1], gb[2], gb[3])
+        return out

@@ -1152,6 +1152,60 @@ extern "C" bsm_status bsm_trace_counts(bsm_context* ctx, uint32_t scene_id, cons
     return BSM_OK;
 }
 
+extern "C" bsm_status bsm_render_primary(bsm_context* ctx, uint32_t scene_id, const bsm_camera* camera,
+                                         const bsm_pt_settings* settings, float near_z, float far_z,
+                                         const bsm_primary_output* out) {
+    Scene* sc;
+    bsm_status st = stage_prep(ctx, scene_id, &sc);
+    if (st) return st;
+    if (!camera || !out) return fail(ctx, BSM_ERR_INVALID_ARG, "camera and out must not be NULL");
+    bsm_pt_settings s;
+    bsm_pt_settings_default(&s);
+    if (settings) s = *settings;
+    const bsm_camera& c = *camera;
+    if (c.width == 0 || c.height == 0) return fail(ctx, BSM_ERR_INVALID_ARG, "view size must be > 0");
+    if ((uint64_t)c.width * c.height >= (1ull << 31)) return fail(ctx, BSM_ERR_INVALID_ARG, "view too large");
+    if (!(c.yfov_deg > 0.0f && c.yfov_deg < 180.0f)) return fail(ctx, BSM_ERR_INVALID_ARG, "yfov_deg must be in (0, 180)");
+    if (!(s.ray_length > 0.0f)) return fail(ctx, BSM_ERR_INVALID_ARG, "ray_length must be > 0");
+    if (s.t_min < 0.0f) return fail(ctx, BSM_ERR_INVALID_ARG, "t_min must be >= 0");
+    if (near_z == 0.0f) near_z = 0.01f;   // camera.hpp:54-55
+    if (far_z == 0.0f) far_z = 10000.0f;
+    if (!(near_z > 0.0f && far_z > near_z)) return fail(ctx, BSM_ERR_INVALID_ARG, "need 0 < near_z < far_z");
+    if (out->location != BSM_HOST && out->location != BSM_DEVICE)
+        return fail(ctx, BSM_ERR_INVALID_ARG, "location must be BSM_HOST or BSM_DEVICE");
+    DevView v;
+    std::memset(&v, 0, sizeof(v));
+    make_view(c, v);
+    v.ray_length = s.ray_length;
+    v.t_min = s.t_min;
+    const size_t npix = (size_t)c.width * c.height;
+    // device targets: the caller's buffers, or one staging block for host outputs
+    float* dst[6] = {out->depth, out->gbuffer[0], out->gbuffer[1], out->gbuffer[2], out->gbuffer[3],
+                     out->hit_positions};
+    const size_t bytes[6] = {npix * 4, npix * 16, npix * 16, npix * 16, npix * 16, npix * 16};
+    float* dev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (out->location == BSM_DEVICE) {
+        for (int k = 0; k < 6; ++k) dev[k] = dst[k];
+    } else {
+        size_t total = 0;
+        for (int k = 0; k < 6; ++k)
+            if (dst[k]) total += bytes[k];
+        if (total == 0) return BSM_OK;
+        if ((st = dev_alloc(ctx, ctx->tmp, total))) return st;
+        char* b = (char*)ctx->tmp.ptr;
+        for (int k = 0; k < 6; ++k)
+            if (dst[k]) { dev[k] = (float*)b; b += bytes[k]; }
+    }
+    float4* gb[4] = {(float4*)dev[1], (float4*)dev[2], (float4*)dev[3], (float4*)dev[4]};
+    launch_primary(ctx->stream, sc->dev, v, near_z, far_z, dev[0], gb, (float4*)dev[5]);
+    CK(cudaGetLastError());
+    if (out->location == BSM_HOST)
+        for (int k = 0; k < 6; ++k)
+            if (dst[k]) CK(cudaMemcpyAsync(dst[k], dev[k], bytes[k], cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BSM_OK;
+}
+
 // ============================================ internals for other entry points ====
 namespace bsm {
 bool ctx_scene(bsm_context* ctx, uint32_t scene_id, DevScene* out) {

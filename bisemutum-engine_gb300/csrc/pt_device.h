@@ -124,6 +124,8 @@ void launch_trace_closest(cudaStream_t st, const DevScene& sc, const float4* ray
 void launch_trace_any(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint8_t* occluded,
                       int block);
 void launch_trace_count(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint2* counts);
+void launch_primary(cudaStream_t st, const DevScene& sc, const DevView& v, float near_z, float far_z, float* depth,
+                    float4* const gb[4], float4* hitpos);
 // radiance cache (mlp.cu)
 cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const float4* queries, const uint32_t* count,
                              uint32_t capacity, float4* accum);

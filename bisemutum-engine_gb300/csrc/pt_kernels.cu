@@ -20,6 +20,7 @@
 #include "pt_device.h"
 #include "pt_sky.cuh"
 #include "pt_trace.cuh"
+#include "pt_gbuffer.cuh"
 #include "mlp.cuh"
 
 namespace bsm {
@@ -40,6 +41,19 @@ __device__ __forceinline__ void accum_add(float4* accum, uint32_t idx, V3 c) {
 }
 
 // ---------------------------------------------------------------- camera ----
+// generate_camera_ray.hlsl:9-11 restated without the matrices: the inverse
+// reverse-Z projection of (ndc, 1, 1) is (ndc.x * aspect * tan, ndc.y * tan, -1),
+// rotated by the camera basis.  (jx, jy) is the position inside the pixel.
+__device__ __forceinline__ V3 camera_dir(const DevView& v, uint32_t px, uint32_t py, float jx, float jy) {
+    float uvx = ((float)px + jx) / (float)v.width;
+    float uvy = ((float)py + jy) / (float)v.height;
+    float ndx = uvx * 2.0f - 1.0f;
+    float ndy = 1.0f - uvy * 2.0f;
+    V3 dl = normalize(v3(ndx * v.aspect * v.tan_half, ndy * v.tan_half, -1.0f));
+    V3 s = v3(v.s[0], v.s[1], v.s[2]), u = v3(v.u[0], v.u[1], v.u[2]), f = v3(v.f[0], v.f[1], v.f[2]);
+    return normalize(s * dl.x + u * dl.y + (-f) * dl.z);
+}
+
 __global__ void k_camera(const DevView* __restrict__ views, uint32_t n_views, uint64_t path_begin,
                          uint32_t path_count, Wavefront wf, uint32_t max_segments_cap) {
     uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -61,15 +75,7 @@ __global__ void k_camera(const DevView* __restrict__ views, uint32_t n_views, ui
     Pcg g = pcg_seed(sample_initstate(v.seed, v.sample_offset + sample), (uint64_t)pixel);
     float jx = 0.5f, jy = 0.5f;
     if (v.flags & BSM_PT_JITTER) { jx = pcg_uniform(g); jy = pcg_uniform(g); }
-    // generate_camera_ray.hlsl:9-11 restated without the matrices: the inverse
-    // reverse-Z projection of (ndc, 1, 1) is (ndc.x * aspect * tan, ndc.y * tan, -1).
-    float uvx = ((float)px + jx) / (float)v.width;
-    float uvy = ((float)py + jy) / (float)v.height;
-    float ndx = uvx * 2.0f - 1.0f;
-    float ndy = 1.0f - uvy * 2.0f;
-    V3 dl = normalize(v3(ndx * v.aspect * v.tan_half, ndy * v.tan_half, -1.0f));
-    V3 s = v3(v.s[0], v.s[1], v.s[2]), u = v3(v.u[0], v.u[1], v.u[2]), f = v3(v.f[0], v.f[1], v.f[2]);
-    V3 dw = normalize(s * dl.x + u * dl.y + (-f) * dl.z);
+    V3 dw = camera_dir(v, px, py, jx, jy);
     uint32_t maxseg = v.max_segments < max_segments_cap ? v.max_segments : max_segments_cap;
     wf.ray_o[0][gid] = make_float4(v.pos[0], v.pos[1], v.pos[2], v.t_min);
     wf.ray_d[0][gid] = make_float4(dw.x, dw.y, dw.z, v.ray_length);
@@ -359,6 +365,57 @@ __global__ void __launch_bounds__(256) k_trace_closest(DevScene sc, const float4
     hits[i] = make_uint4(__float_as_uint(t), prim, __float_as_uint(u), __float_as_uint(v));
 }
 
+// ------------------------------------------------------ primary outputs ----
+// One pixel-centre camera ray per pixel and its closest hit, as the reference's
+// first trace of a frame (generate_camera_ray.hlsl:9-15, rt_gbuffer.hlsl:7-36),
+// written as the pass's primary-hit outputs: reverse-Z depth (pt_depth.hlsl:7-16),
+// the packed G-buffer (gbuffer.hlsl:18-31) and hit positions.  The normal is the
+// geometric one faced towards the ray (as k_shade), the tangent the triangle's
+// first edge.  A miss writes depth 0, hit position (direction, -1) and a zero
+// G-buffer.  Outputs are tightly packed width*height arrays; any may be null.
+__global__ void __launch_bounds__(256) k_primary(DevScene sc, DevView v, float near_z, float far_z,
+                                                 float* __restrict__ depth, float4* __restrict__ gb0,
+                                                 float4* __restrict__ gb1, float4* __restrict__ gb2,
+                                                 float4* __restrict__ gb3, float4* __restrict__ hitpos) {
+    uint32_t npix = v.width * v.height;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix) return;
+    uint32_t px = i % v.width, py = i / v.width;
+    V3 dw = camera_dir(v, px, py, 0.5f, 0.5f);
+    V3 eye = v3(v.pos[0], v.pos[1], v.pos[2]);
+    RayPre r = make_ray(make_float4(eye.x, eye.y, eye.z, v.t_min), make_float4(dw.x, dw.y, dw.z, v.ray_length));
+    float t, hu, hv;
+    uint32_t leaf = trace_ray<false, false>(r, v.ray_length, sc.nodes, sc.tris, t, hu, hv, nullptr);
+    float g[16];
+    float z = 0.0f;
+    float4 hp;
+    if (leaf == kMissPrim) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) g[k] = 0.0f;
+        hp = make_float4(dw.x, dw.y, dw.z, -1.0f);
+    } else {
+        const float4* tp = reinterpret_cast<const float4*>(sc.tris + leaf);
+        float4 a = tp[0], b = tp[1], c = tp[2];
+        V3 va = v3(a.x, a.y, a.z), vb = v3(b.x, b.y, b.z), vc = v3(c.x, c.y, c.z);
+        V3 ng = normalize(cross(vb - va, vc - va));
+        if (dot(ng, dw) > 0.0f) ng = -ng;
+        V3 T = normalize(vb - va);
+        uint32_t mi = __float_as_uint(b.w);
+        if (mi >= sc.num_materials) mi = 0;
+        float4 m0 = sc.materials[2 * mi], m1 = sc.materials[2 * mi + 1];
+        pack_gbuffer(ng, T, v3(m0.x, m0.y, m0.z), v3(m1.x, m1.y, m1.z), m0.w, g);
+        V3 P = eye + dw * t;
+        z = reverse_z_depth(eye, v3(v.f[0], v.f[1], v.f[2]), P, near_z, far_z);
+        hp = make_float4(P.x, P.y, P.z, t);
+    }
+    if (depth) depth[i] = z;
+    if (gb0) gb0[i] = make_float4(g[0], g[1], g[2], g[3]);
+    if (gb1) gb1[i] = make_float4(g[4], g[5], g[6], g[7]);
+    if (gb2) gb2[i] = make_float4(g[8], g[9], g[10], g[11]);
+    if (gb3) gb3[i] = make_float4(g[12], g[13], g[14], g[15]);
+    if (hitpos) hitpos[i] = hp;
+}
+
 __global__ void __launch_bounds__(256) k_trace_any(DevScene sc, const float4* __restrict__ rays, uint32_t n,
                                                    uint8_t* __restrict__ occluded) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -431,6 +488,12 @@ void launch_trace_any(cudaStream_t st, const DevScene& sc, const float4* rays, u
                       int block) {
     if (n == 0) return;
     k_trace_any<<<(n + block - 1) / block, block, 0, st>>>(sc, rays, n, occluded);
+}
+void launch_primary(cudaStream_t st, const DevScene& sc, const DevView& v, float near_z, float far_z, float* depth,
+                    float4* const gb[4], float4* hitpos) {
+    uint32_t npix = v.width * v.height;
+    if (npix == 0) return;
+    k_primary<<<(npix + 255) / 256, 256, 0, st>>>(sc, v, near_z, far_z, depth, gb[0], gb[1], gb[2], gb[3], hitpos);
 }
 void launch_trace_count(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint2* counts) {
     if (n == 0) return;

@@ -304,6 +304,34 @@ BSM_API bsm_status bsm_trace_any(bsm_context* ctx, uint32_t scene_id, const floa
 BSM_API bsm_status bsm_trace_counts(bsm_context* ctx, uint32_t scene_id, const float* rays, uint32_t n,
                                     uint32_t* counts);
 
+/* ---- primary-hit outputs (depth, G-buffer) ------------------------------ */
+
+/* The outputs of PathTracingPass::render besides the colour
+ * (path_tracing.hpp:20-25, OutputData{depth, velocity, gbuffer}; velocity is
+ * invalid there too).  Each array is width*height, row-major, tightly packed;
+ * a NULL pointer skips that output. */
+typedef struct bsm_primary_output {
+    float* depth;           /* f32 reverse-Z device depth of the primary hit, 0 on a miss
+                               (pt_depth.hlsl:7-16, depth.hlsl:3-4) */
+    float* gbuffer[4];      /* float4 each: base_color, normal_roughness, fresnel, material_0 as
+                               pack_surface_to_gbuffer packs them (renderer/gbuffer.hlsl:6-31);
+                               zero on a miss */
+    float* hit_positions;   /* float4: (position, t), or (direction, -1) on a miss (rt_gbuffer.hlsl:28-35) */
+    uint32_t location;      /* BSM_HOST or BSM_DEVICE */
+} bsm_primary_output;
+
+/* Traces one pixel-centre camera ray per pixel and writes the primary-hit
+ * outputs: the "PT Trace GBuffer #1" and "PT Depth" passes of
+ * PathTracingPass::render (path_tracing.cpp:362-395, 437-448).  The primary
+ * hit is the one the colour pass's first segment finds for an unjittered
+ * sample (same ray, same t_min / ray_length from `settings`; NULL = defaults).
+ * `near_z` / `far_z` are the camera's clip planes for the reverse-Z
+ * projection (camera.hpp:54-55; 0 = the reference defaults 0.01 / 10000).
+ * Synchronous. */
+BSM_API bsm_status bsm_render_primary(bsm_context* ctx, uint32_t scene_id, const bsm_camera* camera,
+                                      const bsm_pt_settings* settings, float near_z, float far_z,
+                                      const bsm_primary_output* out);
+
 /* Page-locked host memory for fast host<->device copies (cudaHostAlloc). */
 BSM_API bsm_status bsm_host_alloc(bsm_context* ctx, uint64_t bytes, void** ptr);
 BSM_API bsm_status bsm_host_free(bsm_context* ctx, void* ptr);

@@ -7,8 +7,9 @@ reference shader it follows) and, where the reference tree was present at
 build time, ``oracle/_ref/libref_bsdf.so`` (the reference's own HLSL material
 math compiled through a C++ shim; used only to generate golden vectors).
 
-Parity pins: BSDF / frame / sampler formulas against golden vectors produced
-from the reference's shader sources (tests/golden/bsdf_golden.npz); PCG32
+Parity pins: BSDF / frame / sampler formulas and the G-buffer packing against
+golden vectors produced from the reference's shader sources
+(tests/golden/bsdf_golden.npz, tests/golden/gbuffer_golden.npz); PCG32
 against the published pcg32 demo output.  Traversal and BVH: the reference's
 are inside the graphics driver, so closest-hit parity is pinned to this
 restatement of the published watertight test only.
@@ -51,6 +52,9 @@ def lib() -> C.CDLL:
         L.orc_mlp_gradient.argtypes = [vp, vp, u32, vp, i32]
         L.orc_mlp_gradient.restype = f32
         L.orc_mlp_adam.argtypes = [vp, vp, vp, vp, f32, i32]
+        L.orc_primary.argtypes = [vp, vp, f32, f32, f32, f32, vp, vp, vp, i32]
+        L.orc_primary.restype = i32
+        L.orc_gbuffer_pack.argtypes = [vp, u32, vp]
         L.orc_scene_bvh_nodes.argtypes = [vp]
         L.orc_scene_bvh_nodes.restype = u32
         _lib = L
@@ -66,7 +70,8 @@ def ref_lib() -> C.CDLL | None:
         if path is None:
             return None
         R = C.CDLL(path)
-        for fn in ("ref_eval_lit", "ref_vndf", "ref_frame", "ref_aniso", "ref_samplers"):
+        for fn in ("ref_eval_lit", "ref_vndf", "ref_frame", "ref_aniso", "ref_samplers", "ref_gbuffer",
+                   "ref_gbuffer_unpack"):
             getattr(R, fn).argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
         R.ref_inv_pi.restype = C.c_float
         _ref = R
@@ -129,6 +134,22 @@ class OracleScene:
         return out, stats, sec.value
 
 
+    def primary(self, camera: np.ndarray, ray_length: float = 100.0, t_min: float = 0.0, near_z: float = 0.01,
+                far_z: float = 10000.0, threads: int = 0):
+        """Primary-hit outputs of one pixel-centre ray per pixel: (depth (h, w), G-buffer (4, h, w, 4),
+        hit positions (h, w, 4))."""
+        cam = _f32(camera)
+        w, h = int(cam[10]), int(cam[11])
+        depth = np.zeros((h, w), np.float32)
+        gb = np.zeros((4, h, w, 4), np.float32)
+        hp = np.zeros((h, w, 4), np.float32)
+        st = self._L.orc_primary(self.h, cam.ctypes.data, ray_length, t_min, near_z, far_z, depth.ctypes.data,
+                                 gb.ctypes.data, hp.ctypes.data, threads)
+        if st != 0:
+            raise RuntimeError("orc_primary failed")
+        return depth, gb, hp
+
+
 def pcg32(initstate: int, initseq: int, n: int) -> np.ndarray:
     out = np.zeros(n, np.uint32)
     lib().orc_pcg32(initstate, initseq, n, out.ctypes.data)
@@ -155,6 +176,11 @@ def _batch(fn, a, cols_in, cols_out):
     o = np.zeros((a.shape[0], cols_out), np.float32)
     fn(a.ctypes.data, a.shape[0], o.ctypes.data)
     return o
+
+
+def gbuffer_pack(a):
+    """rows of V3 N3 T3 base3 f0_3 roughness -> the four packed G-buffer float4 (16 floats)."""
+    return _batch(lib().orc_gbuffer_pack, a, 16, 16)
 
 
 def eval_lit(a):

@@ -5,9 +5,12 @@
   rounds exactly like the CUDA kernels.
 * ``oracle/_ref/libref_bsdf.so`` — only where the reference tree is present:
   the reference's own shader math (math.hlsl, material/utils.hlsl,
-  material/lit.hlsl, utils/frame.hlsl, utils/sampling.hlsl) compiled with g++
-  through ``ref_shim/hlsl_shim.h``.  The sources are read in place; the only
-  rewrite is ``out T x`` / ``inout T x`` -> ``T& x`` (HLSL output parameters).
+  material/lit.hlsl, utils/frame.hlsl, utils/sampling.hlsl, and the G-buffer
+  packing functions of utils/pack.hlsl and renderer/gbuffer.hlsl) compiled
+  with g++ through ``ref_shim/hlsl_shim.h``.  The sources are read in place;
+  the only rewrite is ``out T x`` / ``inout T x`` -> ``T& x`` (HLSL output
+  parameters); of pack.hlsl and gbuffer.hlsl only the named functions and
+  structs are taken (the rest of those files uses HLSL the shim lacks).
   The generated translation unit and the library stay under ``oracle/_ref/``,
   which is not committed.
 """
@@ -28,6 +31,13 @@ REF_SHADERS = [
     "bisemutum/shaders/core/material/lit.hlsl",
     "bisemutum/shaders/core/utils/frame.hlsl",
     "bisemutum/shaders/core/utils/sampling.hlsl",
+]
+# (file, names of the functions / structs taken from it)
+REF_EXTRACTS = [
+    ("bisemutum/shaders/core/utils/pack.hlsl",
+     ["pack_u32_to_unorm16x2", "unpack_u32_from_unorm16x2", "pack_color_rg11b10", "unpack_color_rg11b10",
+      "oct_wrap", "oct_encode", "oct_decode", "pack_normal_and_tangent", "unpack_normal_and_tangent"]),
+    ("bisemutum/shaders/renderer/gbuffer.hlsl", ["GBuffer", "pack_surface_to_gbuffer", "unpack_gbuffer_to_surface"]),
 ]
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
@@ -58,15 +68,36 @@ def _translate_hlsl(text: str) -> str:
     return text
 
 
+def _extract(text: str, name: str) -> str:
+    """The definition of function or struct `name`: from its declaration line to the matching brace."""
+    m = re.search(r"^(struct\s+" + name + r"\b|[\w<>]+\s+" + name + r"\s*\()", text, flags=re.M)
+    if m is None:
+        raise RuntimeError(f"{name} not found")
+    i = text.index("{", m.start())
+    depth = 0
+    for j in range(i, len(text)):
+        depth += {"{": 1, "}": -1}.get(text[j], 0)
+        if depth == 0:
+            end = j + 1
+            if text.startswith("struct", m.start()):
+                end = text.index(";", end) + 1
+            return text[m.start():end] + "\n"
+    raise RuntimeError(f"unbalanced braces after {name}")
+
+
 def build_reference(verbose: bool = False) -> str | None:
     """Compiles the reference's shader math; returns None when the reference tree is absent."""
     srcs = [os.path.join(REFERENCE_ROOT, p) for p in REF_SHADERS]
-    if not all(os.path.exists(s) for s in srcs):
+    extracts = [(os.path.join(REFERENCE_ROOT, p), p, names) for p, names in REF_EXTRACTS]
+    if not all(os.path.exists(s) for s in srcs) or not all(os.path.exists(e[0]) for e in extracts):
         return None
     os.makedirs(REF_DIR, exist_ok=True)
     inc = os.path.join(REF_DIR, "ref_sources.inc")
     shim_dir = os.path.join(HERE, "ref_shim")
     body = "".join(f"// ---- {p} ----\n" + _translate_hlsl(open(s).read()) + "\n" for p, s in zip(REF_SHADERS, srcs))
+    for path, p, names in extracts:
+        text = _translate_hlsl(open(path).read())
+        body += f"// ---- {p}: {', '.join(names)} ----\n" + "".join(_extract(text, n) for n in names)
     if not os.path.exists(inc) or open(inc).read() != body:
         with open(inc, "w") as f:
             f.write(body)

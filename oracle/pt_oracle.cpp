@@ -16,6 +16,8 @@
 //   samplers         bisemutum/shaders/core/utils/sampling.hlsl:13-31
 //   next direction   sample_secondary_ray.hlsl:16-28 (termination), :51-64 (weight, NaN guard)
 //   accumulation     pt_accumulate.hlsl:3-11 (running mean = sum / samples)
+//   primary outputs  pt_depth.hlsl:7-16 (reverse-Z depth), renderer/gbuffer.hlsl:18-31 and
+//                    core/utils/pack.hlsl:6-16, 83-93, 113-121 (G-buffer packing)
 // and the decisions the CUDA pass takes where the reference has none (PCG32
 // streams keyed to pixel and sample, next-event estimation towards the sun
 // and the importance-sampled sky with MIS, lobe-mixture sampling).  It keeps
@@ -862,6 +864,107 @@ ORC_API int orc_render(void* sp, const float* camera, uint32_t spp, uint32_t max
     return 0;
 }
 
+// ---- primary-hit outputs: G-buffer packing and reverse-Z depth ----
+// pack.hlsl:6-8: 32 bits as two 16-bit fractions of 65536.
+static void unorm16x2(uint32_t x, float* o) {
+    o[0] = (float)(x & 0xffffu) / 65536.0f;
+    o[1] = (float)(x >> 16) / 65536.0f;
+}
+// pack.hlsl:14-16: 11/11/10 bits, truncated.
+static uint32_t rg11b10(F3 c) {
+    return (uint32_t)(c.x * 2047.0f) | ((uint32_t)(c.y * 2047.0f) << 11) | ((uint32_t)(c.z * 1023.0f) << 22);
+}
+// pack.hlsl:83-93: octahedral encoding (L1-normalise, fold the lower half).
+static void octahedral(F3 n, float* o) {
+    float l1 = std::fabs(n.x) + std::fabs(n.y) + std::fabs(n.z);
+    n = divs(n, l1);
+    if (n.z >= 0.0f) {
+        o[0] = n.x;
+        o[1] = n.y;
+    } else {
+        o[0] = (1.0f - std::fabs(n.y)) * (n.x >= 0.0f ? 1.0f : -1.0f);
+        o[1] = (1.0f - std::fabs(n.x)) * (n.y >= 0.0f ? 1.0f : -1.0f);
+    }
+}
+// renderer/gbuffer.hlsl:18-31 (lit model, f90 = 1, anisotropy 0, ior 1.5) with
+// pack_normal_and_tangent (pack.hlsl:113-121).  g: 4 x float4.
+static void gbuffer_pack(F3 N, F3 T, F3 base, F3 f0, float rough, float* g) {
+    g[0] = base.x; g[1] = base.y; g[2] = base.z; g[3] = 1.0f;
+    float oc[2];
+    octahedral(N, oc);
+    Frm fr = make_frame(N);
+    float px = dot3(T, fr.x), py = dot3(T, fr.y);
+    float l1 = std::fabs(px) + std::fabs(py);
+    px = px / l1;
+    py = py / l1;
+    float qx = px * 0.5f + 0.5f;
+    g[4] = oc[0]; g[5] = oc[1]; g[6] = py < 0.0f ? -qx : qx; g[7] = rough;
+    unorm16x2(rg11b10(f0), g + 8);
+    unorm16x2(rg11b10(f3(1.0f, 1.0f, 1.0f)), g + 10);
+    g[12] = 0.0f; g[13] = 1.0f / 1.5f; g[14] = 0.0f; g[15] = 1.0f / 256.0f;
+}
+// pt_depth.hlsl:13-15 with perspective_reverse_z (math.cpp:5-11): clip z / w.
+static float rz_depth(F3 eye, F3 f, F3 P, float near_z, float far_z) {
+    float inv = 1.0f / (far_z - near_z);
+    float m22 = near_z * inv;
+    float m32 = near_z * far_z * inv;
+    float zv = -dot3(f, sub(P, eye));
+    return (m22 * zv + m32) / -zv;
+}
+
+// One pixel-centre ray per pixel (generate_camera_ray.hlsl:9-15) and its closest
+// hit (rt_gbuffer.hlsl:17-35): depth (w*h), G-buffer planes gb (4 x w*h float4,
+// plane-major), hit positions (w*h float4; (direction, -1) on a miss).
+ORC_API int orc_primary(void* sp, const float* camera, float ray_length, float t_min, float near_z, float far_z,
+                        float* depth, float* gb, float* hitpos, int threads) {
+    const Scene& S = *(Scene*)sp;
+    Cam K = make_cam(camera);
+    const uint32_t npix = K.w * K.h;
+    int nt = nthreads(threads);
+    std::atomic<uint32_t> next{0};
+    auto work = [&]() {
+        while (true) {
+            uint32_t b = next.fetch_add(1024);
+            if (b >= npix) break;
+            uint32_t e = std::min(npix, b + 1024);
+            for (uint32_t p = b; p < e; ++p) {
+                uint32_t px = p % K.w, py = p / K.w;
+                float uvx = ((float)px + 0.5f) / (float)K.w;
+                float uvy = ((float)py + 0.5f) / (float)K.h;
+                float ndx = uvx * 2.0f - 1.0f, ndy = 1.0f - uvy * 2.0f;
+                F3 dl = norm3(f3(ndx * K.aspect * K.tan_half, ndy * K.tan_half, -1.0f));
+                F3 dw = norm3(add(add(muls(K.s, dl.x), muls(K.u, dl.y)), muls(neg(K.f), dl.z)));
+                Ray r = make_ray(K.pos, t_min, dw, ray_length);
+                float t, u, v;
+                uint32_t h = trace(S, r, false, t, u, v, nullptr);
+                float g[16] = {0};
+                float z = 0.0f, hp[4] = {dw.x, dw.y, dw.z, -1.0f};
+                if (h != UINT32_MAX) {
+                    const Tri& T = S.tris[h];
+                    F3 ng = norm3(cross3(sub(T.b, T.a), sub(T.c, T.a)));
+                    if (dot3(ng, dw) > 0.0f) ng = neg(ng);
+                    F3 tan = norm3(sub(T.b, T.a));
+                    uint32_t mi = T.mat < S.nmat ? T.mat : 0;
+                    const float* m = S.mats.data() + 8 * (size_t)mi;
+                    gbuffer_pack(ng, tan, f3(m[0], m[1], m[2]), f3(m[4], m[5], m[6]), m[3], g);
+                    F3 P = add(K.pos, muls(dw, t));
+                    z = rz_depth(K.pos, K.f, P, near_z, far_z);
+                    hp[0] = P.x; hp[1] = P.y; hp[2] = P.z; hp[3] = t;
+                }
+                if (depth) depth[p] = z;
+                if (gb)
+                    for (int k = 0; k < 4; ++k) std::memcpy(gb + 4 * ((size_t)k * npix + p), g + 4 * k, 16);
+                if (hitpos) std::memcpy(hitpos + 4 * (size_t)p, hp, 16);
+            }
+        }
+    };
+    std::vector<std::thread> ts;
+    for (int k = 1; k < nt; ++k) ts.emplace_back(work);
+    work();
+    for (auto& t : ts) t.join();
+    return 0;
+}
+
 // Building blocks exposed for the unit tests (known-answer checks).
 ORC_API void orc_pcg32(uint64_t initstate, uint64_t initseq, uint32_t n, uint32_t* out) {
     Pcg g = pcg_seed(initstate, initseq);
@@ -900,6 +1003,15 @@ ORC_API void orc_frame(const float* in, uint32_t n, float* out) {
         Frm f = make_frame(f3(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
         float* o = out + 6 * (size_t)i;
         o[0] = f.x.x; o[1] = f.x.y; o[2] = f.x.z; o[3] = f.y.x; o[4] = f.y.y; o[5] = f.y.z;
+    }
+}
+// in: V3 N3 T3 base3 f0_3 roughness (16 floats); out: the packed G-buffer (16 floats).
+// V is unused, as in pack_surface_to_gbuffer.
+ORC_API void orc_gbuffer_pack(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + 16 * (size_t)i;
+        gbuffer_pack(f3(a[3], a[4], a[5]), f3(a[6], a[7], a[8]), f3(a[9], a[10], a[11]), f3(a[12], a[13], a[14]),
+                     a[15], out + 16 * (size_t)i);
     }
 }
 ORC_API uint32_t orc_scene_bvh_nodes(void* sp) { return (uint32_t)((Scene*)sp)->nodes.size(); }

@@ -1,8 +1,10 @@
 // hlsl_shim.h — TEST INFRASTRUCTURE: the subset of HLSL that the reference's
-// material / frame / sampling shader files use, as C++ types and functions, so
-// that those files compile unmodified (apart from out/inout parameters turned
-// into references by oracle/build.py) with g++ and produce golden vectors.
-// Semantics follow the HLSL intrinsic definitions: componentwise vector ops,
+// material / frame / sampling / G-buffer packing shader code uses, as C++ types
+// and functions, so that it compiles unmodified (apart from out/inout
+// parameters turned into references by oracle/build.py) with g++ and produces
+// golden vectors.  Swizzles (.xy of float3, .yx of float2, .xy/.zw/.xyz of
+// float4) read, and two-component ones write, through a union.  Semantics
+// follow the HLSL intrinsic definitions: componentwise vector ops,
 // lerp(a, b, t) = a + t * (b - a), saturate = clamp to [0, 1],
 // reflect(i, n) = i - 2 * n * dot(i, n).
 #pragma once
@@ -14,28 +16,73 @@ typedef uint32_t uint;
 struct bool3 { bool x, y, z; };
 struct bool4 { bool x, y, z, w; };
 
+struct float2;
+// Two-component swizzle of an N-float vector (reads and writes, e.g. n.xy = ...).
+template <int N, int A, int B>
+struct Swizzle2 {
+    float v[N];
+    inline operator float2() const;
+    inline Swizzle2& operator=(const float2& o);
+};
+
 struct float2 {
-    float x, y;
-    float2() : x(0), y(0) {}
-    float2(double s) : x((float)s), y((float)s) {}
-    float2(float a, float b) : x(a), y(b) {}
+    union {
+        struct { float x, y; };
+        Swizzle2<2, 1, 0> yx;
+    };
+    float2() { x = 0; y = 0; }
+    float2(double s) { x = (float)s; y = (float)s; }
+    float2(float a, float b) { x = a; y = b; }
+    float2(const float2& o) { x = o.x; y = o.y; }
+    float2& operator=(const float2& o) { x = o.x; y = o.y; return *this; }
     float& operator[](int i) { return (&x)[i]; }
     float operator[](int i) const { return (&x)[i]; }
 };
+template <int N, int A, int B>
+inline Swizzle2<N, A, B>::operator float2() const { return float2(v[A], v[B]); }
+template <int N, int A, int B>
+inline Swizzle2<N, A, B>& Swizzle2<N, A, B>::operator=(const float2& o) { v[A] = o.x; v[B] = o.y; return *this; }
+
 struct float3 {
-    float x, y, z;
-    float3() : x(0), y(0), z(0) {}
-    float3(double s) : x((float)s), y((float)s), z((float)s) {}
-    float3(float a, float b, float c) : x(a), y(b), z(c) {}
+    union {
+        struct { float x, y, z; };
+        Swizzle2<3, 0, 1> xy;
+    };
+    float3() { x = 0; y = 0; z = 0; }
+    float3(double s) { x = (float)s; y = (float)s; z = (float)s; }
+    float3(float a, float b, float c) { x = a; y = b; z = c; }
+    float3(float2 v, float c) { x = v.x; y = v.y; z = c; }
+    float3(const float3& o) { x = o.x; y = o.y; z = o.z; }
+    float3& operator=(const float3& o) { x = o.x; y = o.y; z = o.z; return *this; }
     float& operator[](int i) { return (&x)[i]; }
     float operator[](int i) const { return (&x)[i]; }
 };
+struct uint2 {
+    uint x, y;
+    explicit uint2(float2 f) : x((uint)f.x), y((uint)f.y) {}
+};
+
+// Three-component read swizzle of a float4 (.xyz).
+template <int A, int B, int C>
+struct Swizzle3 {
+    float v[4];
+    operator float3() const { return float3(v[A], v[B], v[C]); }
+};
+
 struct float4 {
-    float x, y, z, w;
-    float4() : x(0), y(0), z(0), w(0) {}
-    float4(double s) : x((float)s), y((float)s), z((float)s), w((float)s) {}
-    float4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
-    float4(float3 v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
+    union {
+        struct { float x, y, z, w; };
+        Swizzle2<4, 0, 1> xy;
+        Swizzle2<4, 2, 3> zw;
+        Swizzle3<0, 1, 2> xyz;
+    };
+    float4() { x = 0; y = 0; z = 0; w = 0; }
+    float4(double s) { x = (float)s; y = (float)s; z = (float)s; w = (float)s; }
+    float4(float a, float b, float c, float d) { x = a; y = b; z = c; w = d; }
+    float4(float3 v, float d) { x = v.x; y = v.y; z = v.z; w = d; }
+    float4(float2 a, float2 b) { x = a.x; y = a.y; z = b.x; w = b.y; }
+    float4(const float4& o) { x = o.x; y = o.y; z = o.z; w = o.w; }
+    float4& operator=(const float4& o) { x = o.x; y = o.y; z = o.z; w = o.w; return *this; }
     float& operator[](int i) { return (&x)[i]; }
     float operator[](int i) const { return (&x)[i]; }
 };
@@ -55,6 +102,9 @@ SHIM_V4OP(+) SHIM_V4OP(-) SHIM_V4OP(*) SHIM_V4OP(/)
     inline float2 operator op(float2 a, float s) { return float2(a.x op s, a.y op s); }
 SHIM_V2OP(+) SHIM_V2OP(-) SHIM_V2OP(*) SHIM_V2OP(/)
 inline float3 operator-(float3 a) { return float3(-a.x, -a.y, -a.z); }
+inline float2 operator-(double s, float2 a) { return float2((float)s - a.x, (float)s - a.y); }
+inline float3& operator/=(float3& a, float s) { a = a / s; return a; }
+inline float2& operator/=(float2& a, float s) { a = a / s; return a; }
 inline float4 operator-(float4 a) { return float4(-a.x, -a.y, -a.z, -a.w); }
 inline float3 operator/(double s, float3 a) { return float3((float)s / a.x, (float)s / a.y, (float)s / a.z); }
 inline float4 operator/(double s, float4 a) { return float4((float)s / a.x, (float)s / a.y, (float)s / a.z, (float)s / a.w); }
@@ -95,7 +145,10 @@ inline float min(float a, double b) { return min(a, (float)b); }
 inline float min(double a, double b) { return min((float)a, (float)b); }
 inline float3 max(float3 a, float3 b) { return float3(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z)); }
 inline float4 max(float4 a, float4 b) { return float4(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z), max(a.w, b.w)); }
+inline float clamp(float x, double lo, double hi) { return min(max(x, (float)lo), (float)hi); }
 inline float saturate(float x) { return min(max(x, 0.0f), 1.0f); }
+inline float abs(float a) { return std::fabs(a); }
+inline float2 abs(float2 a) { return float2(std::fabs(a.x), std::fabs(a.y)); }
 inline float3 abs(float3 a) { return float3(std::fabs(a.x), std::fabs(a.y), std::fabs(a.z)); }
 inline float4 abs(float4 a) { return float4(std::fabs(a.x), std::fabs(a.y), std::fabs(a.z), std::fabs(a.w)); }
 inline float sqrt(float x) { return std::sqrt(x); }

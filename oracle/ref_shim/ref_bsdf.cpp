@@ -1,13 +1,14 @@
 // ref_bsdf.cpp — TEST INFRASTRUCTURE: compiles the reference's shader math
 // (bisemutum/shaders/core/utils/math.hlsl, core/material/utils.hlsl,
-// core/material/lit.hlsl, core/utils/frame.hlsl, core/utils/sampling.hlsl)
+// core/material/lit.hlsl, core/utils/frame.hlsl, core/utils/sampling.hlsl,
+// and the G-buffer packing of core/utils/pack.hlsl and renderer/gbuffer.hlsl)
 // through hlsl_shim.h and exposes it to the golden-vector generator.  The
 // sources are read where they lie in the reference tree by oracle/build.py,
 // which only rewrites `out T x` / `inout T x` parameters to `T& x`; the result
 // is built into oracle/_ref/ and never shipped.
 #include "hlsl_shim.h"
 
-#include "ref_sources.inc"  // generated: the five reference files, concatenated
+#include "ref_sources.inc"  // generated: the reference files and extracted functions, concatenated
 
 #define REF_API extern "C" __attribute__((visibility("default")))
 
@@ -61,3 +62,42 @@ REF_API void ref_samplers(const float* in, uint32_t n, float* out) {
     }
 }
 REF_API float ref_inv_pi(void) { return INV_PI; }
+// in: V3 N3 T3 base3 f0_3 roughness; out: the four float4 of
+// pack_surface_to_gbuffer (gbuffer.hlsl:18-31) for the lit surface model
+// (material.hlsl:4) with the default f90, anisotropy and ior (utils.hlsl:18-31).
+REF_API void ref_gbuffer(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + 16 * (size_t)i;
+        SurfaceData s = surface_data_default();
+        s.base_color = float3(a[9], a[10], a[11]);
+        s.f0_color = float3(a[12], a[13], a[14]);
+        s.roughness = a[15];
+        GBuffer g = pack_surface_to_gbuffer(float3(a[0], a[1], a[2]), float3(a[3], a[4], a[5]),
+                                            float3(a[6], a[7], a[8]), s, 1u);
+        const float4* q[4] = {&g.base_color, &g.normal_roughness, &g.fresnel, &g.material_0};
+        for (int k = 0; k < 4; ++k) {
+            float* o = out + 16 * (size_t)i + 4 * k;
+            o[0] = q[k]->x; o[1] = q[k]->y; o[2] = q[k]->z; o[3] = q[k]->w;
+        }
+    }
+}
+// in: the four float4 of a packed G-buffer; out: unpack_gbuffer_to_surface
+// (gbuffer.hlsl:33-45): N3 T3 base3 f0_3 f90_3 roughness anisotropy ior model, 0.
+REF_API void ref_gbuffer_unpack(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + 16 * (size_t)i;
+        GBuffer g;
+        g.base_color = float4(a[0], a[1], a[2], a[3]);
+        g.normal_roughness = float4(a[4], a[5], a[6], a[7]);
+        g.fresnel = float4(a[8], a[9], a[10], a[11]);
+        g.material_0 = float4(a[12], a[13], a[14], a[15]);
+        float3 N, T;
+        SurfaceData s;
+        uint model;
+        unpack_gbuffer_to_surface(g, N, T, s, model);
+        const float v[20] = {N.x, N.y, N.z, T.x, T.y, T.z, s.base_color.x, s.base_color.y, s.base_color.z,
+                             s.f0_color.x, s.f0_color.y, s.f0_color.z, s.f90_color.x, s.f90_color.y, s.f90_color.z,
+                             s.roughness, s.anisotropy, s.ior, (float)model, 0.0f};
+        for (int k = 0; k < 20; ++k) out[20 * (size_t)i + k] = v[k];
+    }
+}

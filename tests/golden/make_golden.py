@@ -1,12 +1,15 @@
-"""Generates tests/golden/bsdf_golden.npz from the reference's own shader math.
+"""Generates tests/golden/bsdf_golden.npz and gbuffer_golden.npz from the
+reference's own shader math.
 
 The reference's material / frame / sampling HLSL files (bisemutum/shaders/core/
 material/utils.hlsl, lit.hlsl, core/utils/frame.hlsl, sampling.hlsl, math.hlsl)
-are compiled from their sources by oracle/build.py (through a C++ HLSL shim)
-and evaluated here on a seeded grid of inputs.  Needs the reference tree;
-the committed .npz is what the tests read.
+and its G-buffer packing (renderer/gbuffer.hlsl pack_surface_to_gbuffer with
+the helpers of core/utils/pack.hlsl) are compiled from their sources by
+oracle/build.py (through a C++ HLSL shim) and evaluated here on seeded inputs.
+Needs the reference tree; the committed .npz files are what the tests read.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # both files
+    python tests/golden/make_golden.py gbuffer    # one of them
 """
 import ctypes as C
 import os
@@ -24,10 +27,58 @@ def unit(v):
     return v / np.linalg.norm(v, axis=-1, keepdims=True)
 
 
-def main():
+def store_gbuffer_formats(g):
+    """What the reference's G-buffer textures hold after a store of the packed floats: base colour and
+    normal/roughness rgba16_sfloat, fresnel rgba16_unorm, material_0 rgba8_unorm (round to nearest)."""
+    q = np.array(g, np.float32).reshape(-1, 16).copy()
+    q[:, 0:8] = q[:, 0:8].astype(np.float16).astype(np.float32)
+    q[:, 8:12] = (np.round(np.clip(q[:, 8:12], 0, 1) * 65535.0) / 65535.0).astype(np.float32)
+    q[:, 12:16] = (np.round(np.clip(q[:, 12:16], 0, 1) * 255.0) / 255.0).astype(np.float32)
+    return np.ascontiguousarray(q)
+
+
+def gbuffer(R):
+    """pack_surface_to_gbuffer on random surfaces plus the octahedral fold's edge cases."""
+    rng = np.random.default_rng(20240602)
+    n = 2048
+    N = unit(rng.normal(size=(n, 3)))
+    # edge cases: axes (both signs), the equator (z = 0), the fold's diagonals
+    special = np.array([[0, 0, 1], [0, 0, -1], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0],
+                        [1, 1, 0], [-1, 1, 0], [1, -1, 0], [-1, -1, 0], [1, 1, -1], [-1, -1, -1],
+                        [0.6, 0, -0.8], [0, -0.6, -0.8]], np.float64)
+    N[:len(special)] = unit(special)
+    V = unit(rng.normal(size=(n, 3)))
+    # tangents: in the plane of N (as a triangle edge is), some arbitrary, one per frame axis
+    R3 = unit(rng.normal(size=(n, 3)))
+    T = unit(R3 - np.sum(R3 * N, 1, keepdims=True) * N)
+    T[n // 2:n // 2 + 128] = R3[n // 2:n // 2 + 128]
+    base = rng.uniform(0.0, 1.0, (n, 3))
+    base[:8] = [[0, 0, 0], [1, 1, 1], [0.5, 0.5, 0.5], [1, 0, 0], [0, 1, 0], [0, 0, 1], [0.04, 0.04, 0.04],
+                [0.999, 0.001, 0.5]]
+    metal = (rng.uniform(size=(n, 1)) < 0.4).astype(np.float64)
+    f0 = 0.04 + (base - 0.04) * metal
+    rough = rng.uniform(0.0, 1.0, (n, 1))
+    g_in = np.concatenate([V, N, T, base, f0, rough], 1).astype(np.float32)
+    g_out = np.zeros((n, 16), np.float32)
+    R.ref_gbuffer(g_in.ctypes.data, n, g_out.ctypes.data)
+    # the reference's own decoder on its packing after the texture stores of its G-buffer formats
+    # (renderer/context/gbuffer.hpp:14-17): N T base f0 f90 roughness anisotropy ior model
+    q = store_gbuffer_formats(g_out)
+    unpacked = np.zeros((n, 20), np.float32)
+    R.ref_gbuffer_unpack(q.ctypes.data, n, unpacked.ctypes.data)
+    out = os.path.join(HERE, "gbuffer_golden.npz")
+    np.savez_compressed(out, gbuffer_in=g_in, gbuffer_out=g_out, unpacked=unpacked[:, :19])
+    print("wrote", out, os.path.getsize(out), "bytes")
+
+
+def main(which=("bsdf", "gbuffer")):
     R = oracle.ref_lib()
     if R is None:
         raise SystemExit("reference tree not present: cannot regenerate the golden vectors")
+    if "gbuffer" in which:
+        gbuffer(R)
+    if "bsdf" not in which:
+        return
     rng = np.random.default_rng(20240601)
     n = 4096
     # surface_eval_lit inputs: N, V, L on the upper side of N, base, f0, roughness
@@ -74,4 +125,4 @@ def main():
 
 if __name__ == "__main__":
     R_ = C  # keep ctypes imported for the loaded library's argtypes
-    main()
+    main(tuple(sys.argv[1:]) or ("bsdf", "gbuffer"))

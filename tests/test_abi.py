@@ -56,6 +56,7 @@ def test_null_context_calls_fail_cleanly(bsm):
     assert L.bsm_sync(None, 0) == -1
     assert L.bsm_render(None, 1, None, 0, None, None, None) == -1
     assert L.bsm_trace_closest(None, 1, None, 0, None, 0) == -1
+    assert L.bsm_render_primary(None, 1, None, None, 0.0, 0.0, None) == -1
     assert L.bsm_last_error(None) == b"null context"
     L.bsm_destroy(None)
 
