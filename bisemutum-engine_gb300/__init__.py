@@ -160,6 +160,31 @@ class SceneGenParams(C.Structure):
 # -------------------------------------------------------------- library ----
 _lib = None
 
+class Submesh(C.Structure):
+    _fields_ = [("base_vertex", C.c_uint32), ("index_offset", C.c_uint32), ("num_indices", C.c_uint32),
+                ("topology", C.c_uint32)]
+
+
+class MeshData(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("positions", C.POINTER(C.c_float)),
+                ("num_normals", C.c_uint32), ("normals", C.POINTER(C.c_float)),
+                ("num_tangents", C.c_uint32), ("tangents", C.POINTER(C.c_float)),
+                ("num_colors", C.c_uint32), ("colors", C.POINTER(C.c_float)),
+                ("num_texcoords", C.c_uint32), ("texcoords", C.POINTER(C.c_float)),
+                ("num_texcoords2", C.c_uint32), ("texcoords2", C.POINTER(C.c_float)),
+                ("num_indices", C.c_uint32), ("indices", C.POINTER(C.c_uint32)),
+                ("num_submeshes", C.c_uint32), ("submeshes", C.POINTER(Submesh)),
+                ("handle", C.c_void_p)]
+
+
+class ProjectInfo(C.Structure):
+    _fields_ = [("camera", Camera), ("near_z", C.c_float), ("far_z", C.c_float), ("has_camera", C.c_uint32),
+                ("camera_orthographic", C.c_uint32), ("settings", PtSettings), ("num_objects", C.c_uint32),
+                ("num_drawables", C.c_uint32), ("num_skipped_submeshes", C.c_uint32),
+                ("num_materials_approximated", C.c_uint32), ("num_non_opaque_materials", C.c_uint32),
+                ("num_unsupported_lights", C.c_uint32), ("has_skybox", C.c_uint32), ("error", C.c_char * 256)]
+
+
 _SIGS = {
     "bsm_create": (C.c_int32, [C.POINTER(C.c_void_p), C.c_int, C.c_uint64]),
     "bsm_destroy": (None, [C.c_void_p]),
@@ -219,6 +244,13 @@ _SIGS = {
                                       C.POINTER(C.c_float)]),
     "bsm_scene_generate": (C.c_int32, [C.POINTER(SceneGenParams), C.POINTER(SceneDesc), C.POINTER(Camera)]),
     "bsm_scene_gen_free": (None, [C.POINTER(SceneDesc)]),
+    "bsm_static_mesh_read": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(MeshData), C.c_char_p, C.c_uint32]),
+    "bsm_static_mesh_free": (None, [C.POINTER(MeshData)]),
+    "bsm_static_mesh_write": (C.c_int32, [C.POINTER(MeshData), C.c_uint32, C.c_void_p, C.c_uint64,
+                                          C.POINTER(C.c_uint64)]),
+    "bsm_project_load": (C.c_int32, [C.c_char_p, C.POINTER(SceneDesc), C.POINTER(ProjectInfo)]),
+    "bsm_project_free": (None, [C.POINTER(SceneDesc)]),
+    "bsm_toml_check": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_uint32]),
 }
 
 
@@ -332,6 +364,109 @@ def generate_scene(kind: int, seed: int = 1, grid: int = 0, spheres: int = 0, sk
         L.bsm_scene_gen_free(C.byref(d))
     cam.width, cam.height = width, height
     return SceneData(pos, idx, mids, mats, lights, sky_kind, sky_color, tex, cam)
+
+
+def _scene_from_desc(d: SceneDesc, cam: Camera | None) -> SceneData:
+    nv, nt, nm, nl = d.num_vertices, d.num_triangles, d.num_materials, d.num_dir_lights
+    pos = np.ctypeslib.as_array(d.positions, (nv, 3)).copy() if nv else np.zeros((0, 3), np.float32)
+    idx = np.ctypeslib.as_array(d.indices, (nt, 3)).copy() if d.indices else None
+    mids = np.ctypeslib.as_array(d.material_ids, (nt,)).copy() if nt else np.zeros(0, np.uint32)
+    mats = np.array([[*d.materials[i].base_color, d.materials[i].roughness, d.materials[i].metallic]
+                     for i in range(nm)], np.float32).reshape(-1, 5)
+    lights = np.array([[*d.dir_lights[i].direction, *d.dir_lights[i].emission] for i in range(nl)],
+                      np.float32).reshape(-1, 6)
+    tex = None
+    if d.sky.kind == BSM_SKY_EQUIRECT:
+        tex = np.ctypeslib.as_array(d.sky.rgba16f, (d.sky.height, d.sky.width, 4)).copy()
+    return SceneData(pos, idx, mids, mats, lights, d.sky.kind, tuple(d.sky.color), tex, cam)
+
+
+_MESH_ARRAYS = [("positions", "num_vertices", 3, np.float32), ("normals", "num_normals", 3, np.float32),
+                ("tangents", "num_tangents", 4, np.float32), ("colors", "num_colors", 3, np.float32),
+                ("texcoords", "num_texcoords", 2, np.float32), ("texcoords2", "num_texcoords2", 2, np.float32),
+                ("indices", "num_indices", 1, np.uint32)]
+
+
+def read_static_mesh(data: bytes) -> dict:
+    """A .static_mesh.biasset image (bsm_static_mesh_read) as numpy arrays: positions (V, 3), normals,
+    tangents (N, 4), colors, texcoords (N, 2), texcoords2, indices (I,), submeshes (S, 4) uint32
+    (base_vertex, index_offset, num_indices, topology)."""
+    L = lib()
+    buf = C.create_string_buffer(bytes(data), len(data))
+    m = MeshData()
+    err = C.create_string_buffer(256)
+    st = L.bsm_static_mesh_read(buf, len(data), C.byref(m), err, 256)
+    if st != BSM_OK:
+        raise BsmError(st, "bsm_static_mesh_read: " + err.value.decode())
+    try:
+        out = {}
+        for name, count, comps, dt in _MESH_ARRAYS:
+            n = getattr(m, count)
+            ptr = getattr(m, name)
+            shape = (n, comps) if comps > 1 else (n,)
+            out[name] = np.ctypeslib.as_array(ptr, shape).astype(dt).copy() if n and ptr else np.zeros(shape, dt)
+        sub = np.zeros((m.num_submeshes, 4), np.uint32)
+        for i in range(m.num_submeshes):
+            s = m.submeshes[i]
+            sub[i] = (s.base_vertex, s.index_offset, s.num_indices, s.topology)
+        out["submeshes"] = sub
+    finally:
+        L.bsm_static_mesh_free(C.byref(m))
+    return out
+
+
+def write_static_mesh(mesh: dict, version: int = 2) -> bytes:
+    """Writes a .static_mesh.biasset image (bsm_static_mesh_write) from arrays named as read_static_mesh's."""
+    L = lib()
+    m = MeshData()
+    keep = []
+    for name, count, comps, dt in _MESH_ARRAYS:
+        a = mesh.get(name)
+        if a is None or len(a) == 0:
+            continue
+        a = np.ascontiguousarray(a, dt).reshape(-1, comps) if comps > 1 else np.ascontiguousarray(a, dt).ravel()
+        keep.append(a)
+        setattr(m, count, a.shape[0])
+        setattr(m, name, a.ctypes.data_as(C.POINTER(C.c_float if dt == np.float32 else C.c_uint32)))
+    sub = np.ascontiguousarray(mesh.get("submeshes", np.zeros((0, 4))), np.uint32).reshape(-1, 4)
+    subs = (Submesh * max(1, sub.shape[0]))()
+    for i, r in enumerate(sub):
+        subs[i] = Submesh(*[int(x) for x in r])
+    m.num_submeshes = sub.shape[0]
+    m.submeshes = C.cast(subs, C.POINTER(Submesh))
+    size = C.c_uint64()
+    st = L.bsm_static_mesh_write(C.byref(m), version, None, 0, C.byref(size))
+    if st != BSM_OK:
+        raise BsmError(st, "bsm_static_mesh_write failed")
+    out = C.create_string_buffer(size.value)
+    st = L.bsm_static_mesh_write(C.byref(m), version, out, size.value, C.byref(size))
+    if st != BSM_OK:
+        raise BsmError(st, "bsm_static_mesh_write failed")
+    return out.raw[:size.value]
+
+
+def load_project(path: str):
+    """A reference project directory (bsm_project_load) -> (SceneData, ProjectInfo)."""
+    L = lib()
+    d = SceneDesc()
+    info = ProjectInfo()
+    st = L.bsm_project_load(os.fsencode(path), C.byref(d), C.byref(info))
+    if st != BSM_OK:
+        raise BsmError(st, "bsm_project_load: " + info.error.decode())
+    try:
+        cam = Camera.from_buffer_copy(info.camera)
+        scene = _scene_from_desc(d, cam if info.has_camera else None)
+    finally:
+        L.bsm_project_free(C.byref(d))
+    return scene, info
+
+
+def toml_check(text: str):
+    """Parses TOML text with the library's reader; raises BsmError with the reason on a syntax error."""
+    err = C.create_string_buffer(256)
+    st = lib().bsm_toml_check(text.encode(), err, 256)
+    if st != BSM_OK:
+        raise BsmError(st, err.value.decode())
 
 
 def bvh_build_host(scene: SceneData, sah_bins=0, max_leaf=0, threads=0):

@@ -455,6 +455,84 @@ BSM_API bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, const 
                                      const bsm_cache_settings* cache_settings, const bsm_view_output* output,
                                      bsm_render_stats* stats, float* train_loss);
 
+/* ---- the reference's on-disk formats ----------------------------------- */
+
+/* SubmeshDesc (graphics/mesh.hpp:16-22); topology 3 = triangle_list (rhi/pipeline.hpp:34-43). */
+typedef struct bsm_submesh {
+    uint32_t base_vertex;
+    uint32_t index_offset;
+    uint32_t num_indices;     /* with no index data: the number of vertices; ~0 = to the end */
+    uint32_t topology;
+} bsm_submesh;
+
+/* MeshData (graphics/mesh.hpp:24-80): the arrays of a StaticMesh asset.  Each
+ * attribute array has its own element count (0 / NULL when absent). */
+typedef struct bsm_mesh_data {
+    uint32_t num_vertices;
+    const float* positions;   /* 3 * num_vertices */
+    uint32_t num_normals;
+    const float* normals;     /* 3 * num_normals */
+    uint32_t num_tangents;
+    const float* tangents;    /* 4 * num_tangents */
+    uint32_t num_colors;
+    const float* colors;      /* 3 * num_colors */
+    uint32_t num_texcoords;
+    const float* texcoords;   /* 2 * num_texcoords */
+    uint32_t num_texcoords2;
+    const float* texcoords2;  /* 2 * num_texcoords2 */
+    uint32_t num_indices;
+    const uint32_t* indices;
+    uint32_t num_submeshes;
+    const bsm_submesh* submeshes;
+    void* handle;             /* owner of the arrays (bsm_static_mesh_free) */
+} bsm_mesh_data;
+
+/* Reads a .static_mesh.biasset file image (StaticMesh::load,
+ * scene_basic/static_mesh.cpp:10-31): magic 0x0b1a55e7, type name
+ * "StaticMesh", version 1 (raw MeshData stream) or 2 (zlib-compressed
+ * MeshData stream, prelude/byte_stream.cpp:28-41).  Truncated or corrupt
+ * files are rejected (the reference reads past them silently); `error`
+ * (may be NULL) receives the reason.  Arrays belong to the library until
+ * bsm_static_mesh_free. */
+BSM_API bsm_status bsm_static_mesh_read(const void* bytes, uint64_t size, bsm_mesh_data* mesh, char* error,
+                                        uint32_t error_len);
+BSM_API void bsm_static_mesh_free(bsm_mesh_data* mesh);
+/* Writes a .static_mesh.biasset image of `mesh` (StaticMesh::save,
+ * static_mesh.cpp:33-42), version 1 or 2 (zlib stream of stored blocks).
+ * With out == NULL only *out_size is set. */
+BSM_API bsm_status bsm_static_mesh_write(const bsm_mesh_data* mesh, uint32_t version, void* out,
+                                         uint64_t out_capacity, uint64_t* out_size);
+
+typedef struct bsm_project_info {
+    bsm_camera camera;                 /* first CameraComponent (camera_system.cpp:17-29) */
+    float near_z, far_z;               /* its clip planes (for bsm_render_primary) */
+    uint32_t has_camera;
+    uint32_t camera_orthographic;      /* orthographic cameras are not supported by the pass */
+    bsm_pt_settings settings;          /* defaults + the path_tracing block of a BasicRendererOverrideVolume */
+    uint32_t num_objects;
+    uint32_t num_drawables;            /* (object, submesh) pairs placed in the scene */
+    uint32_t num_skipped_submeshes;    /* non-triangle-list topologies */
+    uint32_t num_materials_approximated; /* material functions beyond constant assignments */
+    uint32_t num_non_opaque_materials; /* alpha-test / translucent blend modes (traced as opaque) */
+    uint32_t num_unsupported_lights;   /* point / spot / rect light components */
+    uint32_t has_skybox;               /* a SkyboxComponent (its cube texture is not read: sky is black) */
+    char error[256];                   /* reason of a failed load */
+} bsm_project_info;
+
+/* Loads a reference project directory (project.toml -> asset_metadata.toml,
+ * scene.toml; runtime/scene.cpp:103-135) into a scene description: every
+ * StaticMeshComponent + MeshRendererComponent object's submeshes
+ * (static_mesh_render_system.cpp:56-79) in world space (Transform,
+ * math/transform.cpp:120-124, parents applied), its materials from their
+ * TOML (scene_basic/material.cpp:12-53; constant base colour / roughness /
+ * f0 / metallic), DirectionalLightComponents as directional lights
+ * (renderer/context/lights.cpp:55-65), and the first camera.  Arrays belong
+ * to the library until bsm_project_free. */
+BSM_API bsm_status bsm_project_load(const char* project_dir, bsm_scene_desc* desc, bsm_project_info* info);
+BSM_API void bsm_project_free(bsm_scene_desc* desc);
+/* Parses a TOML text with the reader bsm_project_load uses (syntax check). */
+BSM_API bsm_status bsm_toml_check(const char* text, char* error, uint32_t error_len);
+
 /* ---- synthetic scenes --------------------------------------------------- */
 
 enum {
