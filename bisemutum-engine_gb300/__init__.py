@@ -43,9 +43,12 @@ class BsmError(RuntimeError):
 
 
 # ---------------------------------------------------------- C structures ----
+BSM_BLEND_OPAQUE, BSM_BLEND_ALPHA_TEST, BSM_BLEND_TRANSLUCENT = 0, 1, 2
+
+
 class Material(C.Structure):
     _fields_ = [("base_color", C.c_float * 3), ("roughness", C.c_float), ("metallic", C.c_float),
-                ("emission", C.c_float * 3)]
+                ("emission", C.c_float * 3), ("opacity", C.c_float), ("blend_mode", C.c_uint32)]
 
 
 class DirLight(C.Structure):
@@ -289,7 +292,7 @@ class SceneData:
     positions: np.ndarray             # (V, 3) float32
     indices: np.ndarray | None        # (T, 3) uint32
     material_ids: np.ndarray          # (T,) uint32
-    materials: np.ndarray             # (M, 5) float32: base rgb, roughness, metallic
+    materials: np.ndarray             # (M, 5) or (M, 7) float32: base rgb, roughness, metallic[, opacity, blend mode]
     lights: np.ndarray                # (L, 6) float32: direction to light, emission
     sky_kind: int = BSM_SKY_CONSTANT
     sky_color: tuple = (0.5, 0.5, 0.5)
@@ -310,6 +313,8 @@ class SceneData:
             mats[i].base_color[:] = [float(m[0]), float(m[1]), float(m[2])]
             mats[i].roughness = float(m[3])
             mats[i].metallic = float(m[4])
+            mats[i].opacity = float(m[5]) if len(m) > 5 else 1.0
+            mats[i].blend_mode = int(m[6]) if len(m) > 6 else BSM_BLEND_OPAQUE
         lights = (DirLight * max(1, len(self.lights)))()
         for i, l in enumerate(self.lights):
             lights[i].direction[:] = [float(x) for x in l[:3]]
@@ -352,8 +357,8 @@ def generate_scene(kind: int, seed: int = 1, grid: int = 0, spheres: int = 0, sk
         pos = np.ctypeslib.as_array(d.positions, (nv, 3)).copy()
         idx = np.ctypeslib.as_array(d.indices, (nt, 3)).copy() if d.indices else None
         mids = np.ctypeslib.as_array(d.material_ids, (nt,)).copy()
-        mats = np.array([[*d.materials[i].base_color, d.materials[i].roughness, d.materials[i].metallic]
-                         for i in range(nm)], np.float32)
+        mats = np.array([[*d.materials[i].base_color, d.materials[i].roughness, d.materials[i].metallic,
+                          d.materials[i].opacity, d.materials[i].blend_mode] for i in range(nm)], np.float32)
         lights = np.array([[*d.dir_lights[i].direction, *d.dir_lights[i].emission] for i in range(nl)], np.float32)
         tex = None
         if d.sky.kind == BSM_SKY_EQUIRECT:
@@ -371,8 +376,8 @@ def _scene_from_desc(d: SceneDesc, cam: Camera | None) -> SceneData:
     pos = np.ctypeslib.as_array(d.positions, (nv, 3)).copy() if nv else np.zeros((0, 3), np.float32)
     idx = np.ctypeslib.as_array(d.indices, (nt, 3)).copy() if d.indices else None
     mids = np.ctypeslib.as_array(d.material_ids, (nt,)).copy() if nt else np.zeros(0, np.uint32)
-    mats = np.array([[*d.materials[i].base_color, d.materials[i].roughness, d.materials[i].metallic]
-                     for i in range(nm)], np.float32).reshape(-1, 5)
+    mats = np.array([[*d.materials[i].base_color, d.materials[i].roughness, d.materials[i].metallic,
+                      d.materials[i].opacity, d.materials[i].blend_mode] for i in range(nm)], np.float32).reshape(-1, 7)
     lights = np.array([[*d.dir_lights[i].direction, *d.dir_lights[i].emission] for i in range(nl)],
                       np.float32).reshape(-1, 6)
     tex = None

@@ -43,6 +43,7 @@ struct Scene {
     std::vector<float> positions;
     std::vector<uint32_t> indices;
     std::vector<uint32_t> material_ids;
+    std::vector<float> transparency;  // per material: 0 opaque, else what the any-hit rule compares against
     uint32_t num_triangles = 0;
     float extent = 1.0f;
     bool has_bvh = false;
@@ -218,6 +219,7 @@ bsm_status ensure_wavefront(bsm_context* ctx, uint32_t capacity, uint32_t lights
     size_t o_ro0 = sz(C * 16), o_ro1 = sz(C * 16), o_rd0 = sz(C * 16), o_rd1 = sz(C * 16);
     size_t o_p0 = sz(C * 16), o_p1 = sz(C * 16), o_t0 = sz(C * 16), o_t1 = sz(C * 16);
     size_t o_hit = sz(C * 16), o_sho = sz(sh * 16), o_shd = sz(sh * 16), o_shc = sz(sh * 16), o_cq = sz(C * 64);
+    size_t o_shs = sz(sh * 4);
     size_t o_cnt = sz(kCntWords * 4), o_st = sz(kStatWords * 8);
     clear_graphs(ctx);  // graphs hold the old pointers
     dev_free(ctx, ctx->wf_buf);
@@ -232,6 +234,7 @@ bsm_status ensure_wavefront(bsm_context* ctx, uint32_t capacity, uint32_t lights
     w.thr[0] = (float4*)(b + o_t0); w.thr[1] = (float4*)(b + o_t1);
     w.hit = (float4*)(b + o_hit);
     w.sh_o = (float4*)(b + o_sho); w.sh_d = (float4*)(b + o_shd); w.sh_c = (float4*)(b + o_shc);
+    w.sh_seed = (uint32_t*)(b + o_shs);
     w.cache_q = (float4*)(b + o_cq);
     w.counters = (uint32_t*)(b + o_cnt);
     w.stats = (unsigned long long*)(b + o_st);
@@ -390,8 +393,16 @@ extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d
     sc->extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
     // materials: (base.rgb, roughness), (f0.rgb, metallic); f0 = lerp(0.04, base, metallic)
     std::vector<float4> mats(2 * (size_t)d->num_materials);
+    sc->transparency.assign(d->num_materials, 0.0f);
     for (uint32_t m = 0; m < d->num_materials; ++m) {
         const bsm_material& M = d->materials[m];
+        if (M.blend_mode > BSM_BLEND_TRANSLUCENT) return fail(ctx, BSM_ERR_INVALID_ARG, "unknown blend mode");
+        if (M.blend_mode != BSM_BLEND_OPAQUE && !(M.opacity >= 0.0f && M.opacity <= 1.0f))
+            return fail(ctx, BSM_ERR_INVALID_ARG, "opacity must be in [0, 1]");
+        // the any-hit rule (rt_gbuffer_hit.hlsl:20-35): alpha test drops the hit below the
+        // threshold (utils.hlsl:38), translucent drops it when u < 1 - opacity
+        if (M.blend_mode == BSM_BLEND_ALPHA_TEST) sc->transparency[m] = M.opacity < 0.01f ? 1.0f : 0.0f;
+        if (M.blend_mode == BSM_BLEND_TRANSLUCENT) sc->transparency[m] = 1.0f - M.opacity;
         float f0[3];
         for (int k = 0; k < 3; ++k) f0[k] = 0.04f + (M.base_color[k] - 0.04f) * M.metallic;
         mats[2 * m] = make_float4(M.base_color[0], M.base_color[1], M.base_color[2], M.roughness);
@@ -403,6 +414,9 @@ extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d
     DevScene& ds = sc->dev;
     ds.materials = (const float4*)sc->materials.ptr;
     ds.num_materials = d->num_materials;
+    ds.has_non_opaque = 0;
+    for (uint32_t t = 0; t < d->num_triangles; ++t)
+        if (sc->transparency[d->material_ids ? d->material_ids[t] : 0] != 0.0f) { ds.has_non_opaque = 1; break; }
     ds.num_lights = d->num_dir_lights;
     for (uint32_t l = 0; l < d->num_dir_lights; ++l) {
         const bsm_dir_light& L = d->dir_lights[l];
@@ -458,6 +472,10 @@ extern "C" bsm_status bsm_scene_build_bvh(bsm_context* ctx, uint32_t scene_id, c
         return fail(ctx, BSM_ERR_INVALID_ARG, "BVH build failed: " + err);
     if (r.max_depth > (uint32_t)kMaxTraversalDepth)
         return fail(ctx, BSM_ERR_UNSUPPORTED, "BVH deeper than the traversal stack (" + std::to_string(r.max_depth) + ")");
+    for (CwTri& t : r.tris) {  // the any-hit rule's operand rides in the spare word
+        float tr = t.material < sc->transparency.size() ? sc->transparency[t.material] : 0.0f;
+        std::memcpy(&t.pad, &tr, 4);
+    }
     bsm_status st;
     dev_free(ctx, sc->nodes);
     dev_free(ctx, sc->tris);
@@ -1178,6 +1196,8 @@ extern "C" bsm_status bsm_render_primary(bsm_context* ctx, uint32_t scene_id, co
     make_view(c, v);
     v.ray_length = s.ray_length;
     v.t_min = s.t_min;
+    v.seed = s.seed;
+    v.sample_offset = s.sample_offset;
     const size_t npix = (size_t)c.width * c.height;
     // device targets: the caller's buffers, or one staging block for host outputs
     float* dst[6] = {out->depth, out->gbuffer[0], out->gbuffer[1], out->gbuffer[2], out->gbuffer[3],

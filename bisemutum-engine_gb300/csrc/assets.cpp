@@ -778,7 +778,8 @@ bool load_toml(const std::string& path, TVal& root, std::string& err) {
 
 // Material TOML (material.cpp:12-53) to the pass's constant material.  The
 // material function is HLSL; assignments of a parameter or a literal to
-// surface.base_color / roughness / f0_color are evaluated, and a `metallic`
+// surface.base_color / roughness / f0_color / opacity are evaluated, the blend
+// mode selects the any-hit rule, and a `metallic`
 // parameter with no f0 assignment gives f0 = lerp(0.04, base, metallic)
 // (import_model.cpp:217-219).  Anything else (texture samples, expressions,
 // conditionals) leaves the surface_data_default value of that field
@@ -848,8 +849,14 @@ bool load_material(const std::string& path, MatResult& r, std::string& err) {
         }
     }
     const TVal* bm = root.get("blend_mode");
-    r.non_opaque = bm && bm->k == TVal::Str && bm->s != "opaque";
-    double base[3] = {0.5, 0.5, 0.5}, rough = 0.5, f0[3] = {0.04, 0.04, 0.04};
+    uint32_t blend = BSM_BLEND_OPAQUE;
+    if (bm && bm->k == TVal::Str) {
+        if (bm->s == "alpha_test") blend = BSM_BLEND_ALPHA_TEST;
+        else if (bm->s == "translucent") blend = BSM_BLEND_TRANSLUCENT;
+        else if (bm->s != "opaque") { err = path + ": unknown blend_mode '" + bm->s + "'"; return false; }
+    }
+    r.non_opaque = blend != BSM_BLEND_OPAQUE;
+    double base[3] = {0.5, 0.5, 0.5}, rough = 0.5, f0[3] = {0.04, 0.04, 0.04}, opacity = 1.0;
     bool has_f0 = false;
     const TVal* fn = root.get("material_function");
     std::string code = fn && fn->k == TVal::Str ? fn->s : "";
@@ -865,7 +872,8 @@ bool load_material(const std::string& path, MatResult& r, std::string& err) {
         if (ok && lhs == "surface.base_color" && v.size() >= 3) { for (int c = 0; c < 3; ++c) base[c] = v[c]; continue; }
         if (ok && lhs == "surface.roughness" && v.size() == 1) { rough = v[0]; continue; }
         if (ok && lhs == "surface.f0_color" && v.size() >= 3) { for (int c = 0; c < 3; ++c) f0[c] = v[c]; has_f0 = true; continue; }
-        if (ok && (lhs == "surface.opacity" || lhs == "surface.two_sided")) continue;  // opacity: blend mode
+        if (ok && lhs == "surface.opacity" && v.size() == 1) { opacity = v[0]; continue; }
+        if (lhs == "surface.two_sided") continue;  // the pass faces every normal towards the ray
         r.approximated = true;
     }
     double metallic = 0.0;
@@ -884,6 +892,8 @@ bool load_material(const std::string& path, MatResult& r, std::string& err) {
     for (int c = 0; c < 3; ++c) { r.m.base_color[c] = (float)base[c]; r.m.emission[c] = 0.0f; }
     r.m.roughness = (float)rough;
     r.m.metallic = (float)metallic;
+    r.m.opacity = (float)std::min(1.0, std::max(0.0, opacity));
+    r.m.blend_mode = blend;
     return true;
 }
 
@@ -1211,7 +1221,7 @@ bsm_status project_load(const char* project_dir, bsm_scene_desc* desc, bsm_proje
         }
     }
     if (own->mats.empty()) {  // a scene without drawables still needs one material
-        bsm_material m{{0.5f, 0.5f, 0.5f}, 0.5f, 0.0f, {0, 0, 0}};
+        bsm_material m{{0.5f, 0.5f, 0.5f}, 0.5f, 0.0f, {0, 0, 0}, 1.0f, BSM_BLEND_OPAQUE};
         own->mats.push_back(m);
     }
     std::memset(desc, 0, sizeof(*desc));

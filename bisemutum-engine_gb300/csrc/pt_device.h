@@ -11,6 +11,8 @@
 //   sh_o/sh_d/sh_c[(L+1) C] float4  shadow rays and their contributions: sun
 //                rays fill the queue from the front, sky rays from the back, so
 //                a warp of the any-hit kernel traces rays of one kind
+//   sh_seed[(L+1) C] uint32  opacity seed of each shadow ray (scenes with
+//                non-opaque triangles; extension rays use the path's PCG word)
 //   counters     uint32  queue sizes per segment, work counters, error flags
 //   stats        uint64  rays per segment (summed over chunks)
 // All queues are structures of arrays read with 128-bit loads.
@@ -44,6 +46,7 @@ struct DevScene {
     float4 light_dir[kMaxLights];
     float4 light_e[kMaxLights];
     DevSky sky;
+    uint32_t has_non_opaque;   // some triangle has a transparency (alpha test / translucent)
     float ray_offset;          // origin offset along the geometric normal
     float box_lo[3];           // scene bounds: radiance-cache inputs are normalised to them
     float box_inv[3];
@@ -93,6 +96,7 @@ struct Wavefront {
     float4* sh_o;
     float4* sh_d;
     float4* sh_c;
+    uint32_t* sh_seed;         // [(L+1) C] opacity seeds of the shadow rays (written for non-opaque scenes)
     float4* cache_q;           // radiance-cache queries (4 float4 each), capacity C; may be null
     uint32_t* counters;
     unsigned long long* stats;

@@ -87,9 +87,10 @@ __global__ void k_camera(const DevView* __restrict__ views, uint32_t n_views, ui
 // ---------------------------------------------------------------- extend ----
 template <bool kCount, int kMinBlocks>
 __global__ void __launch_bounds__(256, kMinBlocks) k_extend(DevScene sc, const float4* __restrict__ ray_o,
-                                                const float4* __restrict__ ray_d, float4* __restrict__ hit,
-                                                uint32_t* counters, unsigned long long* stats, uint32_t seg,
-                                                int postpone_sp, int refill_min) {
+                                                const float4* __restrict__ ray_d, const uint4* __restrict__ path,
+                                                float4* __restrict__ hit, uint32_t* counters,
+                                                unsigned long long* stats, uint32_t seg, int postpone_sp,
+                                                int refill_min) {
     uint32_t n = counters[kCntQueue + seg];
     if (blockIdx.x == 0 && threadIdx.x == 0) stats[kStatExtend + seg] += n;
     TraceCounters c{0, 0};
@@ -99,6 +100,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_extend(DevScene sc, const f
         [&](uint32_t i, uint32_t leaf, float t, float u, float v) {
             hit[i] = make_float4(t, __uint_as_float(leaf), u, v);
         },
+        [&](uint32_t i) { return path[i].z; },   // the path's PCG32 word
         &c, postpone_sp, refill_min);
     if (kCount) {
         uint32_t cn = c.nodes, ct = c.tris;
@@ -135,6 +137,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_shadow(DevScene sc, Wavefro
                 accum_add(accum, __float_as_uint(c.w), v3(c.x, c.y, c.z));
             }
         },
+        [&](uint32_t i) { return wf.sh_seed ? wf.sh_seed[slot(i)] : 0u; },
         nullptr, postpone_sp, refill_min);
 }
 
@@ -268,6 +271,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene sc, const DevView* __
                     wf.sh_o[slot] = make_float4(org.x, org.y, org.z, tmin);
                     wf.sh_d[slot] = make_float4(L.x, L.y, L.z, ray_len);
                     wf.sh_c[slot] = make_float4(c.x, c.y, c.z, __uint_as_float(m4.x));
+                    if (sc.has_non_opaque && wf.sh_seed) wf.sh_seed[slot] = (uint32_t)g.state;
                 } else {
                     atomicOr(wf.counters + kCntError, 1u);
                 }
@@ -300,6 +304,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene sc, const DevView* __
                     wf.sh_o[k] = make_float4(org.x, org.y, org.z, tmin);
                     wf.sh_d[k] = make_float4(L.x, L.y, L.z, ray_len);
                     wf.sh_c[k] = make_float4(c.x, c.y, c.z, __uint_as_float(m4.x));
+                    if (sc.has_non_opaque && wf.sh_seed) wf.sh_seed[k] = (uint32_t)g.state;
                 } else {
                     atomicOr(wf.counters + kCntError, 1u);
                 }
@@ -385,7 +390,9 @@ __global__ void __launch_bounds__(256) k_primary(DevScene sc, DevView v, float n
     V3 eye = v3(v.pos[0], v.pos[1], v.pos[2]);
     RayPre r = make_ray(make_float4(eye.x, eye.y, eye.z, v.t_min), make_float4(dw.x, dw.y, dw.z, v.ray_length));
     float t, hu, hv;
-    uint32_t leaf = trace_ray<false, false>(r, v.ray_length, sc.nodes, sc.tris, t, hu, hv, nullptr);
+    // opacity decisions of sample 0 of an unjittered render (its camera-ray PCG word)
+    Pcg pg = pcg_seed(sample_initstate(v.seed, v.sample_offset), (uint64_t)i);
+    uint32_t leaf = trace_ray<false, false>(r, v.ray_length, sc.nodes, sc.tris, t, hu, hv, nullptr, (uint32_t)pg.state);
     float g[16];
     float z = 0.0f;
     float4 hp;
@@ -449,15 +456,15 @@ void launch_camera(const LaunchCfg& lc, cudaStream_t st, const DevView* views, u
 void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, int q,
                    uint32_t seg, bool count_traversal) {
     if (count_traversal)
-        k_extend<true, 1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
+        k_extend<true, 1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit,
                                                                            wf.counters, wf.stats, seg,
                                                                            lc.postpone_sp, lc.refill_min);
     else if (lc.regcap)
-        k_extend<false, 4><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
+        k_extend<false, 4><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit,
                                                                             wf.counters, wf.stats, seg,
                                                                             lc.postpone_sp, lc.refill_min);
     else
-        k_extend<false, 1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.hit,
+        k_extend<false, 1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit,
                                                                             wf.counters, wf.stats, seg,
                                                                             lc.postpone_sp, lc.refill_min);
 }

@@ -13,6 +13,7 @@
 
 #include <stdint.h>
 #include <math.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #include <cuda_runtime.h>
@@ -30,6 +31,13 @@ namespace bsm {
 #define BSM_TWO_PI (2.0f * 3.14159265359f)
 #define BSM_INV_PI 0.318309873f
 #define BSM_INV_FOUR_PI 0.0795774683f
+
+// bit pattern of a float (memcpy: defined on the host, one move on the device)
+BSM_HD uint32_t f2u(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+}
 
 struct V3 { float x, y, z; };
 
@@ -153,6 +161,17 @@ BSM_HD uint64_t mix64(uint64_t z) {
 }
 BSM_HD uint64_t sample_initstate(uint64_t seed, uint32_t sample) {
     return mix64(seed + 0x9e3779b97f4a7c15ULL * ((uint64_t)sample + 1u));
+}
+
+// Per-ray uniform of the stochastic-opacity test.  As the reference's
+// gen_opacity_random_for (renderer/raytracing/hits/rt_gbuffer.hlsl:14-19) it
+// combines the bits of the ray's origin and direction with a seed (there: the
+// frame index; here: the path's PCG32 state, which differs per sample and
+// bounce), then hashes them: SplitMix64's finaliser, top 24 bits as [0, 1).
+BSM_HD float opacity_random(float ox, float oy, float oz, float dx, float dy, float dz, uint32_t seed) {
+    uint32_t h = f2u(ox) ^ f2u(oy) ^ f2u(oz) ^ f2u(dx) ^ f2u(dy) ^ f2u(dz);
+    uint64_t z = mix64(((uint64_t)h << 32) | (uint64_t)seed);
+    return (float)(uint32_t)(z >> 40) * 5.96046448e-08f;
 }
 
 }  // namespace bsm

@@ -69,12 +69,16 @@ __global__ void k_noalloc_mean(float4* acc, uint32_t n, float inv_spp) {
 // Scratch layout: counters | stats | view record | wavefront arrays.
 constexpr size_t kHeaderBytes = 3 * 256 + 2048;
 
-size_t bytes_per_path(uint32_t lights) { return 9 * 16 + 3 * 16 * (size_t)(lights + 1); }
+// 9 float4 path arrays, 3 float4 per shadow slot, and a 4-byte opacity seed per
+// shadow slot for scenes with non-opaque triangles
+size_t bytes_per_path(uint32_t lights, bool non_opaque) {
+    return 9 * 16 + (3 * 16 + (non_opaque ? 4 : 0)) * (size_t)(lights + 1);
+}
 
 }  // namespace
 
-uint32_t noalloc_max_paths(uint32_t lights) {
-    size_t c = (kNoAllocScratchBytes - kHeaderBytes - 16 * 256) / bytes_per_path(lights);
+uint32_t noalloc_max_paths(uint32_t lights, bool non_opaque) {
+    size_t c = (kNoAllocScratchBytes - kHeaderBytes - 16 * 256) / bytes_per_path(lights, non_opaque);
     return (uint32_t)(c & ~(size_t)255);
 }
 
@@ -109,7 +113,7 @@ extern "C" bsm_status bsm_render_noalloc(bsm_context* ctx, uint32_t scene_id, co
         return BSM_ERR_INVALID_ARG;
     }
     const uint32_t lights = std::max(sc.num_lights, 1u);
-    const uint32_t max_paths = noalloc_max_paths(lights);
+    const uint32_t max_paths = noalloc_max_paths(lights, sc.has_non_opaque != 0);
     if (s->wavefront_capacity > max_paths) {
         ctx_set_error(ctx, "bsm_render_noalloc: wavefront_capacity exceeds the fixed scratch "
                            "(64 MiB: at most noalloc_max_paths() paths per chunk)");
@@ -150,6 +154,7 @@ extern "C" bsm_status bsm_render_noalloc(bsm_context* ctx, uint32_t scene_id, co
     wf.sh_o = (float4*)take(SH * 16);
     wf.sh_d = (float4*)take(SH * 16);
     wf.sh_c = (float4*)take(SH * 16);
+    wf.sh_seed = sc.has_non_opaque ? (uint32_t*)take(SH * 4) : nullptr;
     if (off > kNoAllocScratchBytes) {  // cannot happen for capacity <= noalloc_max_paths
         ctx_set_error(ctx, "bsm_render_noalloc: scratch layout overflow");
         return BSM_ERR_INVALID_ARG;

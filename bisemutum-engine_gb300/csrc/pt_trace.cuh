@@ -19,11 +19,16 @@
 //     and the hit primitive are reproducible bit for bit on a CPU.
 // Ties at equal t resolve to the lower primitive id, which makes the closest
 // hit independent of the BVH's shape.
+// Non-opaque triangles carry their transparency (1 - opacity, or 1 / 0 for an
+// alpha-tested surface below / above the threshold) in the spare word of the
+// triangle record; a candidate hit on one is ignored when the ray's opacity
+// uniform is below it (the any-hit shader's IgnoreHit, rt_gbuffer_hit.hlsl:20-35).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "bvh_layout.h"
+#include "pt_math.cuh"
 
 namespace bsm {
 
@@ -204,10 +209,15 @@ struct TraceCounters { uint32_t nodes, tris; };
 
 // Single-ray closest / any hit (used by the stage entry points).  Returns the
 // leaf-ordered triangle index (kMissPrim on a miss); t = tmax on a miss.
+// Rule of a candidate hit on a triangle of transparency `tr` (0 = opaque).
+__device__ __forceinline__ bool keep_hit(const RayPre& r, float tr, uint32_t oseed) {
+    return tr == 0.0f || !(opacity_random(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, oseed) < tr);
+}
+
 template <bool kAnyHit, bool kCount>
 __device__ __forceinline__ uint32_t trace_ray(const RayPre& r, float tmax, const CwNode* __restrict__ nodes,
                                               const CwTri* __restrict__ tris, float& t_out, float& u_out,
-                                              float& v_out, TraceCounters* cnt) {
+                                              float& v_out, TraceCounters* cnt, uint32_t oseed = 0u) {
     float tbest = tmax;
     uint32_t best_leaf = kMissPrim, best_prim = kMissPrim;
     float bu = 0.0f, bv = 0.0f;
@@ -227,7 +237,7 @@ __device__ __forceinline__ uint32_t trace_ray(const RayPre& r, float tmax, const
             uint32_t prim = __float_as_uint(a.w);
             if (kCount) cnt->tris++;
             float t, u, v;
-            if (tri_test(r, a, b, c, tbest, prim, best_prim, t, u, v)) {
+            if (tri_test(r, a, b, c, tbest, prim, best_prim, t, u, v) && keep_hit(r, c.w, oseed)) {
                 if (kAnyHit) { t_out = t; u_out = u; v_out = v; return ti; }
                 tbest = t; best_leaf = ti; best_prim = prim; bu = u; bv = v;
             }
@@ -260,13 +270,14 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // the warp runs this loop together (all ballots use the full mask).  `load`
 // (index -> (origin/tmin, direction/tmax)) supplies rays; `finish(index, leaf,
 // t, u, v)` receives each result (leaf = kMissPrim on a miss; for any-hit the
-// first hit found).
+// first hit found); `seed(index)` gives the ray's opacity seed, read only when a
+// candidate hit lies on a non-opaque triangle.
 // `postpone_sp` (<= kPostponeMaxSp) is the stack depth below which triangle
 // groups may be postponed (0 disables postponing); `refill_min` is the number
 // of idle lanes that makes the warp fetch new rays.  Both are tuning knobs.
-template <bool kAnyHit, bool kCount, class Load, class Finish>
+template <bool kAnyHit, bool kCount, class Load, class Finish, class Seed>
 __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, const CwTri* __restrict__ tris,
-                                            uint32_t n, uint32_t* work, Load load, Finish finish,
+                                            uint32_t n, uint32_t* work, Load load, Finish finish, Seed seed,
                                             TraceCounters* cnt, int postpone_sp, int refill_min) {
     postpone_sp = postpone_sp < kPostponeMaxSp ? postpone_sp : kPostponeMaxSp;
     const uint32_t lane = threadIdx.x & 31u;
@@ -341,7 +352,8 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
                 uint32_t prim = __float_as_uint(a.w);
                 if (kCount) cnt->tris++;
                 float t, u, v;
-                if (tri_test(r, a, b, c, tbest, prim, best_prim, t, u, v)) {
+                if (tri_test(r, a, b, c, tbest, prim, best_prim, t, u, v) &&
+                    (c.w == 0.0f || keep_hit(r, c.w, seed(idx)))) {
                     tbest = t; best_leaf = ti; best_prim = prim; bu = u; bv = v;
                     if (kAnyHit) { T.y = 0u; G.y = 0u; sp = 0; }
                 }

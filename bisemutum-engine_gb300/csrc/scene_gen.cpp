@@ -56,6 +56,8 @@ struct Builder {
         for (int i = 0; i < 3; ++i) m.base_color[i] = (float)r.uniform(0.1, 0.9);
         m.roughness = (float)r.uniform(0.05, 1.0);
         m.metallic = r.uniform() < 0.3 ? 1.0f : 0.0f;
+        m.opacity = 1.0f;
+        m.blend_mode = BSM_BLEND_OPAQUE;
         mats.push_back(m);
         return (uint32_t)(mats.size() - 1);
     }

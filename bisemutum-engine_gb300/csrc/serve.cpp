@@ -356,7 +356,7 @@ extern "C" bsm_status bsm_server_start(bsm_context* ctx, const bsm_server_opts* 
         auto sz = [&](size_t n) { size_t off = bytes; bytes += (n + 255) & ~(size_t)255; return off; };
         size_t o_ro0 = sz(C * 16), o_ro1 = sz(C * 16), o_rd0 = sz(C * 16), o_rd1 = sz(C * 16);
         size_t o_p0 = sz(C * 16), o_p1 = sz(C * 16), o_t0 = sz(C * 16), o_t1 = sz(C * 16), o_hit = sz(C * 16);
-        size_t o_sho = sz(SH * 16), o_shd = sz(SH * 16), o_shc = sz(SH * 16);
+        size_t o_sho = sz(SH * 16), o_shd = sz(SH * 16), o_shc = sz(SH * 16), o_shs = sz(SH * 4);
         size_t o_cnt = sz(kCntWords * 4), o_st = sz(kStatWords * 8);
         size_t o_v = sz(S->opts.max_views_per_chunk * sizeof(DevView));
         if (cudaMalloc(&l.wf_mem, bytes) != cudaSuccess) return fail_cleanup("server: cannot allocate lane queues");
@@ -368,6 +368,7 @@ extern "C" bsm_status bsm_server_start(bsm_context* ctx, const bsm_server_opts* 
         l.wf.thr[0] = (float4*)(b + o_t0); l.wf.thr[1] = (float4*)(b + o_t1);
         l.wf.hit = (float4*)(b + o_hit);
         l.wf.sh_o = (float4*)(b + o_sho); l.wf.sh_d = (float4*)(b + o_shd); l.wf.sh_c = (float4*)(b + o_shc);
+        l.wf.sh_seed = (uint32_t*)(b + o_shs);
         l.wf.counters = (uint32_t*)(b + o_cnt);
         l.wf.stats = (unsigned long long*)(b + o_st);
         l.views_dev = (DevView*)(b + o_v);

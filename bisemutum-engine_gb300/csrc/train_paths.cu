@@ -48,7 +48,8 @@ __global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView*
     for (uint32_t seg = 0; seg < segs; ++seg) {
         RayPre r = make_ray(make_float4(o.x, o.y, o.z, v.t_min), make_float4(d.x, d.y, d.z, v.ray_length));
         float t, hu, hv;
-        uint32_t leaf = trace_ray<false, false>(r, v.ray_length, sc.nodes, sc.tris, t, hu, hv, nullptr);
+        uint32_t leaf = trace_ray<false, false>(r, v.ray_length, sc.nodes, sc.tris, t, hu, hv, nullptr,
+                                                (uint32_t)g.state);
         if (leaf == kMissPrim) {
             if (nv > 0) {
                 V3 le = sky_eval(sc.sky, d);
@@ -91,7 +92,8 @@ __global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView*
             if (max_comp(c) > 0.0f) {
                 RayPre sr = make_ray(make_float4(org.x, org.y, org.z, v.t_min), make_float4(L.x, L.y, L.z, v.ray_length));
                 float a, b2, c2;
-                if (trace_ray<true, false>(sr, v.ray_length, sc.nodes, sc.tris, a, b2, c2, nullptr) == kMissPrim)
+                if (trace_ray<true, false>(sr, v.ray_length, sc.nodes, sc.tris, a, b2, c2, nullptr,
+                                           (uint32_t)g.state) == kMissPrim)
                     contrib[k] = contrib[k] + c;
             }
         }
@@ -107,7 +109,8 @@ __global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView*
                     RayPre sr = make_ray(make_float4(org.x, org.y, org.z, v.t_min), make_float4(L.x, L.y, L.z, v.ray_length));
                     float a, b2, c2;
                     if (max_comp(c) > 0.0f &&
-                        trace_ray<true, false>(sr, v.ray_length, sc.nodes, sc.tris, a, b2, c2, nullptr) == kMissPrim)
+                        trace_ray<true, false>(sr, v.ray_length, sc.nodes, sc.tris, a, b2, c2, nullptr,
+                                               (uint32_t)g.state) == kMissPrim)
                         contrib[k] = contrib[k] + c;
                 }
             }

@@ -90,11 +90,20 @@ BSM_API bsm_status bsm_memcpy(bsm_context* ctx, void* dst, const void* src, uint
 
 /* ---- scene description (DirLightData, skybox, GPU scene buffers) ------ */
 
+/* BlendMode (graphics/material.hpp): opaque surfaces always stop rays; the
+ * others run the any-hit rule of rt_gbuffer_hit.hlsl:20-35 on every candidate
+ * hit: alpha test ignores the hit when opacity < 0.01 (utils.hlsl:38),
+ * translucent ignores it when a per-ray uniform u < 1 - opacity (stochastic
+ * opacity).  Shadow rays follow the same rule. */
+enum { BSM_BLEND_OPAQUE = 0, BSM_BLEND_ALPHA_TEST = 1, BSM_BLEND_TRANSLUCENT = 2 };
+
 typedef struct bsm_material {
     float base_color[3];   /* SurfaceData::base_color (utils.hlsl:5-16) */
     float roughness;       /* perceptual roughness, alpha = max(r^2, 1e-3) */
     float metallic;        /* f0 = lerp(0.04, base_color, metallic) (import_model.cpp:217-219) */
     float emission[3];     /* kept for the descriptor; the reference PT drops it (gbuffer.hlsl) */
+    float opacity;         /* SurfaceData::opacity in [0, 1]; used by the non-opaque blend modes */
+    uint32_t blend_mode;   /* BSM_BLEND_* (0 = opaque) */
 } bsm_material;
 
 typedef struct bsm_dir_light {
@@ -345,7 +354,8 @@ BSM_API bsm_status bsm_host_free(bsm_context* ctx, void* ptr);
  * (queue counters, the view record, the wavefront queues) is one fixed 64 MiB
  * device array inside the library, held by every GPU that loads it until the
  * process exits; it bounds a chunk to wavefront_capacity paths (0 = the
- * maximum, 279,552 paths for one light); a larger wavefront_capacity is
+ * maximum, 279,552 paths for one light in an opaque scene, 270,336 when
+ * some material is not opaque); a larger wavefront_capacity is
  * rejected with BSM_ERR_INVALID_ARG.  Any image size works: paths run in chunks.
  * `out_rgba` is a caller-owned device buffer of width*height RGBA floats,
  * tightly packed; it receives the per-pixel sums and then the mean.  The first
@@ -513,7 +523,7 @@ typedef struct bsm_project_info {
     uint32_t num_drawables;            /* (object, submesh) pairs placed in the scene */
     uint32_t num_skipped_submeshes;    /* non-triangle-list topologies */
     uint32_t num_materials_approximated; /* material functions beyond constant assignments */
-    uint32_t num_non_opaque_materials; /* alpha-test / translucent blend modes (traced as opaque) */
+    uint32_t num_non_opaque_materials; /* alpha-test / translucent blend modes (any-hit opacity rule) */
     uint32_t num_unsupported_lights;   /* point / spot / rect light components */
     uint32_t has_skybox;               /* a SkyboxComponent (its cube texture is not read: sky is black) */
     char error[256];                   /* reason of a failed load */
@@ -525,7 +535,7 @@ typedef struct bsm_project_info {
  * (static_mesh_render_system.cpp:56-79) in world space (Transform,
  * math/transform.cpp:120-124, parents applied), its materials from their
  * TOML (scene_basic/material.cpp:12-53; constant base colour / roughness /
- * f0 / metallic), DirectionalLightComponents as directional lights
+ * f0 / metallic / opacity, blend mode), DirectionalLightComponents as directional lights
  * (renderer/context/lights.cpp:55-65), and the first camera.  Arrays belong
  * to the library until bsm_project_free. */
 BSM_API bsm_status bsm_project_load(const char* project_dir, bsm_scene_desc* desc, bsm_project_info* info);

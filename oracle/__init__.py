@@ -52,7 +52,7 @@ def lib() -> C.CDLL:
         L.orc_mlp_gradient.argtypes = [vp, vp, u32, vp, i32]
         L.orc_mlp_gradient.restype = f32
         L.orc_mlp_adam.argtypes = [vp, vp, vp, vp, f32, i32]
-        L.orc_primary.argtypes = [vp, vp, f32, f32, f32, f32, vp, vp, vp, i32]
+        L.orc_primary.argtypes = [vp, vp, f32, f32, f32, f32, u64, u32, vp, vp, vp, i32]
         L.orc_primary.restype = i32
         L.orc_gbuffer_pack.argtypes = [vp, u32, vp]
         L.orc_scene_bvh_nodes.argtypes = [vp]
@@ -82,6 +82,15 @@ def _f32(a):
     return np.ascontiguousarray(a, np.float32)
 
 
+def material_rows(materials) -> np.ndarray:
+    """(M, 7) float32: base rgb, roughness, metallic, opacity, blend mode; 5-column input is opaque."""
+    m = np.asarray(materials, np.float32)
+    m = m.reshape(m.shape[0], -1)
+    if m.shape[1] == 5:
+        m = np.concatenate([m, np.ones((m.shape[0], 1), np.float32), np.zeros((m.shape[0], 1), np.float32)], 1)
+    return np.ascontiguousarray(m[:, :7], np.float32)
+
+
 class OracleScene:
     """A scene inside the oracle (own binary SAH BVH)."""
 
@@ -91,7 +100,7 @@ class OracleScene:
         pos = _f32(scene.positions)
         idx = None if scene.indices is None else np.ascontiguousarray(scene.indices, np.uint32)
         mids = np.ascontiguousarray(scene.material_ids, np.uint32)
-        mats = _f32(scene.materials)
+        mats = material_rows(scene.materials)
         lights = _f32(scene.lights).reshape(-1, 6)
         color = _f32(scene.sky_color)
         tex = None if scene.sky_texels is None else np.ascontiguousarray(scene.sky_texels, np.uint16)
@@ -135,7 +144,7 @@ class OracleScene:
 
 
     def primary(self, camera: np.ndarray, ray_length: float = 100.0, t_min: float = 0.0, near_z: float = 0.01,
-                far_z: float = 10000.0, threads: int = 0):
+                far_z: float = 10000.0, seed: int = 1, sample_offset: int = 0, threads: int = 0):
         """Primary-hit outputs of one pixel-centre ray per pixel: (depth (h, w), G-buffer (4, h, w, 4),
         hit positions (h, w, 4))."""
         cam = _f32(camera)
@@ -143,8 +152,8 @@ class OracleScene:
         depth = np.zeros((h, w), np.float32)
         gb = np.zeros((4, h, w, 4), np.float32)
         hp = np.zeros((h, w, 4), np.float32)
-        st = self._L.orc_primary(self.h, cam.ctypes.data, ray_length, t_min, near_z, far_z, depth.ctypes.data,
-                                 gb.ctypes.data, hp.ctypes.data, threads)
+        st = self._L.orc_primary(self.h, cam.ctypes.data, ray_length, t_min, near_z, far_z, seed, sample_offset,
+                                 depth.ctypes.data, gb.ctypes.data, hp.ctypes.data, threads)
         if st != 0:
             raise RuntimeError("orc_primary failed")
         return depth, gb, hp

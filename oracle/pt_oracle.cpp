@@ -236,7 +236,7 @@ static float mix_pdf(F3 lv, F3 ll, float rx, float ry, float ps) {
 }
 
 // ------------------------------------------------------------- scene ----
-struct Tri { F3 a, b, c; uint32_t prim, mat; };
+struct Tri { F3 a, b, c; uint32_t prim, mat; float tr; };  // tr: transparency of the any-hit rule (0 = opaque)
 struct BNode { float lo[3], hi[3]; uint32_t left_or_first, count; uint32_t axis; };  // count > 0: leaf
 
 struct Scene {
@@ -343,14 +343,15 @@ static uint32_t build_rec(Scene& S, std::vector<BuildRef>& refs, uint32_t b, uin
 struct Ray {
     F3 o, d;
     float tmin, tmax;
+    uint32_t oseed;   // opacity seed (the path's PCG32 word; 0 for the stage entry points)
     float id[3];
     int kx, ky, kz;
     float Sx, Sy, Sz;
 };
 static float comp(F3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
-static Ray make_ray(F3 o, float tmin, F3 d, float tmax) {
+static Ray make_ray(F3 o, float tmin, F3 d, float tmax, uint32_t oseed = 0) {
     Ray r;
-    r.o = o; r.d = d; r.tmin = tmin; r.tmax = tmax;
+    r.o = o; r.d = d; r.tmin = tmin; r.tmax = tmax; r.oseed = oseed;
     for (int k = 0; k < 3; ++k) {
         float dk = comp(d, k);
         r.id[k] = 1.0f / dk;
@@ -417,6 +418,19 @@ static bool box_hit(const Ray& r, const BNode& n, float tbest) {
 }
 struct Counts { uint64_t nodes = 0, tris = 0; };
 // returns index into S.tris (leaf order) or UINT32_MAX
+static uint32_t bits_of(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+// Stochastic-opacity uniform of a ray: the bits of its origin and direction
+// combined as gen_opacity_random_for does (hits/rt_gbuffer.hlsl:14-19), with
+// the path's PCG32 word as the seed, hashed by SplitMix64's finaliser.
+static float opacity_random(const Ray& r) {
+    uint32_t h = bits_of(r.o.x) ^ bits_of(r.o.y) ^ bits_of(r.o.z) ^ bits_of(r.d.x) ^ bits_of(r.d.y) ^ bits_of(r.d.z);
+    uint64_t z = mix64(((uint64_t)h << 32) | (uint64_t)r.oseed);
+    return (float)(uint32_t)(z >> 40) * 5.96046448e-08f;
+}
+// The any-hit rule (rt_gbuffer_hit.hlsl:20-35): a candidate on a triangle of
+// transparency tr is ignored when the ray's uniform is below tr.
+static bool keep_hit(const Ray& r, float tr) { return tr == 0.0f || !(opacity_random(r) < tr); }
+
 static uint32_t trace(const Scene& S, const Ray& r, bool any, float& to, float& uo, float& vo, Counts* cnt) {
     float tbest = r.tmax;
     uint32_t best = UINT32_MAX, best_prim = UINT32_MAX;
@@ -435,7 +449,7 @@ static uint32_t trace(const Scene& S, const Ray& r, bool any, float& to, float& 
                 const Tri& t = S.tris[n.left_or_first + i];
                 if (cnt) cnt->tris++;
                 float tt, u, v;
-                if (tri_hit(r, t, tbest, best_prim, tt, u, v)) {
+                if (tri_hit(r, t, tbest, best_prim, tt, u, v) && keep_hit(r, t.tr)) {
                     tbest = tt; best = n.left_or_first + i; best_prim = t.prim; bu = u; bv = v;
                     if (any) { to = tt; uo = u; vo = v; return best; }
                 }
@@ -587,8 +601,8 @@ struct PathQ {  // one wavefront queue in the oracle (structure of arrays)
 struct ShadowQ {
     std::vector<F3> o, d, c;
     std::vector<float> tmin, tmax;
-    std::vector<uint32_t> pix;
-    void clear() { o.clear(); d.clear(); c.clear(); tmin.clear(); tmax.clear(); pix.clear(); }
+    std::vector<uint32_t> pix, seed;
+    void clear() { o.clear(); d.clear(); c.clear(); tmin.clear(); tmax.clear(); pix.clear(); seed.clear(); }
 };
 
 // Renders pixels [pix_begin, pix_end) of one camera; `acc` receives RGB sums
@@ -618,7 +632,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
             sq.clear();
             for (size_t i = 0; i < q.size(); ++i) {
                 // extend
-                Ray r = make_ray(q.o[i], q.tmin[i], q.d[i], q.tmax[i]);
+                Ray r = make_ray(q.o[i], q.tmin[i], q.d[i], q.tmax[i], (uint32_t)q.rng[i].state);
                 float t, u, v;
                 uint32_t hit = trace(S, r, false, t, u, v, nullptr);
                 F3 d = q.d[i], thr = q.thr[i];
@@ -660,6 +674,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                     if (maxc(c) > 0.0f) {
                         sq.o.push_back(org); sq.tmin.push_back(st.t_min); sq.d.push_back(S.ldir[l]);
                         sq.tmax.push_back(st.ray_length); sq.c.push_back(c); sq.pix.push_back(q.pix[i]);
+                        sq.seed.push_back((uint32_t)g.state);
                     }
                 }
                 if (!(st.flags & F_NO_SKY)) {
@@ -677,6 +692,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                             if (maxc(c) > 0.0f) {
                                 sq.o.push_back(org); sq.tmin.push_back(st.t_min); sq.d.push_back(L);
                                 sq.tmax.push_back(st.ray_length); sq.c.push_back(c); sq.pix.push_back(q.pix[i]);
+                                sq.seed.push_back((uint32_t)g.state);
                             }
                         }
                     }
@@ -700,7 +716,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
             // shadow (any hit)
             sh_cnt[seg] += sq.o.size();
             for (size_t k = 0; k < sq.o.size(); ++k) {
-                Ray r = make_ray(sq.o[k], sq.tmin[k], sq.d[k], sq.tmax[k]);
+                Ray r = make_ray(sq.o[k], sq.tmin[k], sq.d[k], sq.tmax[k], sq.seed[k]);
                 float t, u, v;
                 if (trace(S, r, true, t, u, v, nullptr) == UINT32_MAX) {
                     float* a = acc + 3 * (size_t)(sq.pix[k] - pix_begin);
@@ -758,13 +774,18 @@ ORC_API int orc_scene_create(const float* pos, uint32_t nv, const uint32_t* idx,
     for (uint32_t i = 0; i < nt; ++i) S->tris[i] = soup[refs[i].t];
     S->nmat = nm;
     S->mats.resize(8 * (size_t)nm);
+    std::vector<float> trm(nm, 0.0f);
     for (uint32_t m = 0; m < nm; ++m) {
-        const float* M = materials + 5 * (size_t)m;  // base rgb, roughness, metallic
+        // base rgb, roughness, metallic, opacity, blend mode (0 opaque, 1 alpha test, 2 translucent)
+        const float* M = materials + 7 * (size_t)m;
+        if (M[6] == 1.0f) trm[m] = M[5] < 0.01f ? 1.0f : 0.0f;   // ALPHA_TEST_OPACITY_THRESHOLD (utils.hlsl:38)
+        if (M[6] == 2.0f) trm[m] = 1.0f - M[5];
         float* o = &S->mats[8 * (size_t)m];
         o[0] = M[0]; o[1] = M[1]; o[2] = M[2]; o[3] = M[3];
         for (int k = 0; k < 3; ++k) o[4 + k] = 0.04f + (M[k] - 0.04f) * M[4];  // lerp(0.04, base, metallic)
         o[7] = M[4];
     }
+    for (Tri& T : S->tris) T.tr = T.mat < nm ? trm[T.mat] : 0.0f;
     S->nlights = nl;
     for (uint32_t l = 0; l < nl; ++l) {
         S->ldir[l] = norm3(f3(lights[6 * l], lights[6 * l + 1], lights[6 * l + 2]));
@@ -916,7 +937,7 @@ static float rz_depth(F3 eye, F3 f, F3 P, float near_z, float far_z) {
 // hit (rt_gbuffer.hlsl:17-35): depth (w*h), G-buffer planes gb (4 x w*h float4,
 // plane-major), hit positions (w*h float4; (direction, -1) on a miss).
 ORC_API int orc_primary(void* sp, const float* camera, float ray_length, float t_min, float near_z, float far_z,
-                        float* depth, float* gb, float* hitpos, int threads) {
+                        uint64_t seed, uint32_t sample_offset, float* depth, float* gb, float* hitpos, int threads) {
     const Scene& S = *(Scene*)sp;
     Cam K = make_cam(camera);
     const uint32_t npix = K.w * K.h;
@@ -934,7 +955,9 @@ ORC_API int orc_primary(void* sp, const float* camera, float ray_length, float t
                 float ndx = uvx * 2.0f - 1.0f, ndy = 1.0f - uvy * 2.0f;
                 F3 dl = norm3(f3(ndx * K.aspect * K.tan_half, ndy * K.tan_half, -1.0f));
                 F3 dw = norm3(add(add(muls(K.s, dl.x), muls(K.u, dl.y)), muls(neg(K.f), dl.z)));
-                Ray r = make_ray(K.pos, t_min, dw, ray_length);
+                // opacity decisions of sample 0 of an unjittered render
+                Pcg pg = pcg_seed(sample_initstate(seed, sample_offset), (uint64_t)p);
+                Ray r = make_ray(K.pos, t_min, dw, ray_length, (uint32_t)pg.state);
                 float t, u, v;
                 uint32_t h = trace(S, r, false, t, u, v, nullptr);
                 float g[16] = {0};

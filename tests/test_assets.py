@@ -215,7 +215,7 @@ def write_project(root, bsm):
                 "[[params]]\nname = 'metallic'\nvalue = 1.0\n")
     with open(os.path.join(root, "materials", "fancy.toml"), "w") as f:
         f.write("blend_mode = 'translucent'\nmaterial_function = '''int g = int(vertex.position_world.x);\n"
-                "surface.base_color = (g & 1) == 1 ? PARAM_a : PARAM_a;\n'''\n"
+                "surface.base_color = (g & 1) == 1 ? PARAM_a : PARAM_a;\nsurface.opacity = 0.35;\n'''\n"
                 "[[params]]\nname = 'a'\nvalue = [ 0.2, 0.2, 0.2 ]\n")
     scene = """
 [[objects]]
@@ -329,9 +329,10 @@ def test_project_loads_into_world_space(bsm, tmp_path):
     assert np.allclose(tri[3], expect_child[[4, 5, 6]], atol=1e-5)
     mats = sc.materials
     red, gold, fancy = mats[sc.material_ids[0]], mats[sc.material_ids[2]], mats[sc.material_ids[3]]
-    assert np.allclose(red, [0.9, 0.1, 0.1, 0.25, 0.0])
-    assert np.allclose(gold, [1.0, 0.8, 0.3, 0.4, 1.0])
-    assert np.allclose(fancy, [0.5, 0.5, 0.5, 0.5, 0.0])           # approximated: surface defaults
+    # base rgb, roughness, metallic, opacity, blend mode
+    assert np.allclose(red, [0.9, 0.1, 0.1, 0.25, 0.0, 1.0, 0])
+    assert np.allclose(gold, [1.0, 0.8, 0.3, 0.4, 1.0, 1.0, 0])
+    assert np.allclose(fancy, [0.5, 0.5, 0.5, 0.5, 0.0, 0.35, 2])  # base approximated: surface defaults
     assert info.num_materials_approximated == 1 and info.num_non_opaque_materials == 1
     # lights: zero emission skipped; direction = R (0, 1, 0)
     assert sc.lights.shape == (1, 6)
