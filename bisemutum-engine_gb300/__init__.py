@@ -163,6 +163,21 @@ class SceneGenParams(C.Structure):
 # -------------------------------------------------------------- library ----
 _lib = None
 
+class GeometryDesc(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("positions", C.POINTER(C.c_float)), ("num_triangles", C.c_uint32),
+                ("indices", C.POINTER(C.c_uint32)), ("material_ids", C.POINTER(C.c_uint32))]
+
+
+class Instance(C.Structure):
+    _fields_ = [("geometry_id", C.c_uint32), ("material_id", C.c_uint32), ("transform", C.c_float * 12)]
+
+
+class InstancedSceneDesc(C.Structure):
+    _fields_ = [("num_instances", C.c_uint32), ("instances", C.POINTER(Instance)), ("num_materials", C.c_uint32),
+                ("materials", C.POINTER(Material)), ("num_dir_lights", C.c_uint32),
+                ("dir_lights", C.POINTER(DirLight)), ("sky", Sky)]
+
+
 class Submesh(C.Structure):
     _fields_ = [("base_vertex", C.c_uint32), ("index_offset", C.c_uint32), ("num_indices", C.c_uint32),
                 ("topology", C.c_uint32)]
@@ -247,6 +262,10 @@ _SIGS = {
                                       C.POINTER(C.c_float)]),
     "bsm_scene_generate": (C.c_int32, [C.POINTER(SceneGenParams), C.POINTER(SceneDesc), C.POINTER(Camera)]),
     "bsm_scene_gen_free": (None, [C.POINTER(SceneDesc)]),
+    "bsm_geometry_create": (C.c_int32, [C.c_void_p, C.POINTER(GeometryDesc), C.c_void_p, C.POINTER(C.c_uint32)]),
+    "bsm_geometry_release": (C.c_int32, [C.c_void_p, C.c_uint32]),
+    "bsm_scene_create_instanced": (C.c_int32, [C.c_void_p, C.POINTER(InstancedSceneDesc), C.POINTER(C.c_uint32)]),
+    "bsm_scene_update_instances": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
     "bsm_static_mesh_read": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(MeshData), C.c_char_p, C.c_uint32]),
     "bsm_static_mesh_free": (None, [C.POINTER(MeshData)]),
     "bsm_static_mesh_write": (C.c_int32, [C.POINTER(MeshData), C.c_uint32, C.c_void_p, C.c_uint64,
@@ -340,6 +359,136 @@ class SceneData:
         else:
             self._keep = [pos, idx, mids, mats, lights]
         return d
+
+
+def _materials_array(materials) -> "C.Array":
+    mats = (Material * len(materials))()
+    for i, m in enumerate(materials):
+        mats[i].base_color[:] = [float(m[0]), float(m[1]), float(m[2])]
+        mats[i].roughness = float(m[3])
+        mats[i].metallic = float(m[4])
+        mats[i].opacity = float(m[5]) if len(m) > 5 else 1.0
+        mats[i].blend_mode = int(m[6]) if len(m) > 6 else BSM_BLEND_OPAQUE
+    return mats
+
+
+@dataclass
+class GeometryData:
+    """An object-space mesh of a two-level scene (bsm_geometry_desc)."""
+    positions: np.ndarray             # (V, 3) float32
+    indices: np.ndarray | None        # (T, 3) uint32
+    material_ids: np.ndarray | None = None
+
+    @property
+    def num_triangles(self) -> int:
+        return int(self.indices.shape[0]) if self.indices is not None else int(self.positions.shape[0] // 3)
+
+
+@dataclass
+class InstancedSceneData:
+    """A two-level scene: geometries and their instances (bsm_instanced_scene_desc)."""
+    geometries: list
+    inst_geometry: np.ndarray         # (N,) index into geometries
+    inst_material: np.ndarray         # (N,) uint32 material of every triangle, or 0xffffffff
+    inst_transform: np.ndarray        # (N, 12) float32 object-to-world, row-major 3x4
+    materials: np.ndarray             # (M, 5) or (M, 7), as SceneData
+    lights: np.ndarray                # (L, 6)
+    sky_kind: int = BSM_SKY_CONSTANT
+    sky_color: tuple = (0.5, 0.5, 0.5)
+    sky_texels: np.ndarray | None = None
+    camera: Camera | None = None
+
+    @property
+    def num_triangles(self) -> int:
+        return int(sum(self.geometries[g].num_triangles for g in self.inst_geometry))
+
+    def flattened(self) -> SceneData:
+        """The same scene as one world-space mesh (each instance's triangles transformed in float64)."""
+        pos, idx, mids = [], [], []
+        base = 0
+        for g, m, xf in zip(self.inst_geometry, self.inst_material, self.inst_transform):
+            G = self.geometries[int(g)]
+            M = np.asarray(xf, np.float64).reshape(3, 4)
+            p = np.asarray(G.positions, np.float64) @ M[:, :3].T + M[:, 3]
+            ii = np.asarray(G.indices, np.uint32) if G.indices is not None else np.arange(len(p), dtype=np.uint32).reshape(-1, 3)
+            pos.append(p.astype(np.float32))
+            idx.append(ii + base)
+            t = len(ii)
+            if int(m) != 0xFFFFFFFF:
+                mids.append(np.full(t, int(m), np.uint32))
+            else:
+                mids.append(np.zeros(t, np.uint32) if G.material_ids is None else np.asarray(G.material_ids, np.uint32))
+            base += len(p)
+        return SceneData(np.concatenate(pos), np.concatenate(idx), np.concatenate(mids), self.materials, self.lights,
+                         self.sky_kind, self.sky_color, self.sky_texels, self.camera)
+
+
+def _uv_sphere(n_lat: int, n_lon: int):
+    th = np.linspace(0, np.pi, n_lat + 1)
+    ph = np.linspace(0, 2 * np.pi, n_lon, endpoint=False)
+    P = np.stack(np.meshgrid(th, ph, indexing="ij"), -1).reshape(-1, 2)
+    pos = np.stack([np.sin(P[:, 0]) * np.cos(P[:, 1]), np.cos(P[:, 0]), np.sin(P[:, 0]) * np.sin(P[:, 1])], 1)
+    tri = []
+    for i in range(n_lat):
+        for j in range(n_lon):
+            a, b = i * n_lon + j, i * n_lon + (j + 1) % n_lon
+            c, d = a + n_lon, b + n_lon
+            if i > 0:
+                tri.append((a, b, c))
+            if i < n_lat - 1:
+                tri.append((b, d, c))
+    return pos.astype(np.float32), np.array(tri, np.uint32)
+
+
+def generate_instanced_scene(seed: int = 1, instances: int = 200, width: int = 256, height: int = 256,
+                             sphere_res: int = 16, ground: int = 64) -> InstancedSceneData:
+    """A seeded two-level scene: a ground grid, a UV sphere, a box and a tetrahedron as geometries, the objects
+    instanced with random rotations, non-uniform scales and translations over the ground; a sun and a constant sky."""
+    rng = np.random.default_rng(seed)
+    g = np.linspace(-1.0, 1.0, ground + 1)
+    X, Z = np.meshgrid(g, g, indexing="ij")
+    Y = 0.05 * np.sin(3 * X) * np.cos(2 * Z)
+    gp = np.stack([X, Y, Z], -1).reshape(-1, 3).astype(np.float32)
+    gi = []
+    for i in range(ground):
+        for j in range(ground):
+            a, b, c, d = i * (ground + 1) + j, i * (ground + 1) + j + 1, (i + 1) * (ground + 1) + j, (i + 1) * (ground + 1) + j + 1
+            gi += [(a, b, d), (a, d, c)]
+    sp, si = _uv_sphere(sphere_res, 2 * sphere_res)
+    bp = np.array([[x, y, z] for x in (-1, 1) for y in (-1, 1) for z in (-1, 1)], np.float32)
+    bi = np.array([[0, 1, 3], [0, 3, 2], [4, 6, 7], [4, 7, 5], [0, 4, 5], [0, 5, 1], [2, 3, 7], [2, 7, 6],
+                   [0, 2, 6], [0, 6, 4], [1, 5, 7], [1, 7, 3]], np.uint32)
+    tp = np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], np.float32)
+    ti = np.array([[0, 1, 2], [0, 3, 1], [0, 2, 3], [1, 3, 2]], np.uint32)
+    geoms = [GeometryData(gp, np.array(gi, np.uint32), np.zeros(len(gi), np.uint32)),
+             GeometryData(sp, si, (np.arange(len(si)) % 2 + 1).astype(np.uint32)),
+             GeometryData(bp, bi, np.full(len(bi), 3, np.uint32)),
+             GeometryData(tp, ti, None)]
+    n_mat = 8
+    mats = np.zeros((n_mat, 7), np.float32)
+    mats[:, :3] = rng.uniform(0.1, 0.9, (n_mat, 3))
+    mats[:, 3] = rng.uniform(0.05, 1.0, n_mat)
+    mats[:, 4] = (rng.uniform(size=n_mat) < 0.3).astype(np.float32)
+    mats[:, 5] = 1.0
+    inst_g = [0]
+    inst_m = [0xFFFFFFFF]
+    xf = [np.array([[4, 0, 0, 0], [0, 1, 0, 0], [0, 0, 4, 0]], np.float32)]
+    for _ in range(instances):
+        kind = int(rng.integers(1, 4))
+        a, b, c = rng.uniform(0, 2 * np.pi, 3)
+        Rz = np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
+        Rx = np.array([[1, 0, 0], [0, np.cos(b), -np.sin(b)], [0, np.sin(b), np.cos(b)]])
+        Ry = np.array([[np.cos(c), 0, np.sin(c)], [0, 1, 0], [-np.sin(c), 0, np.cos(c)]])
+        S = np.diag(rng.uniform(0.05, 0.3, 3))
+        L = Rz @ Rx @ Ry @ S
+        t = np.array([rng.uniform(-3.5, 3.5), rng.uniform(0.1, 0.6), rng.uniform(-3.5, 3.5)])
+        xf.append(np.concatenate([L, t[:, None]], 1).astype(np.float32))
+        inst_g.append(kind)
+        inst_m.append(0xFFFFFFFF if rng.uniform() < 0.5 else int(rng.integers(4, n_mat)))
+    lights = np.array([[0.4, 0.8, 0.3, 3.0, 2.9, 2.7]], np.float32)
+    cam = make_camera((0.0, 2.5, 6.0), (0.0, -0.35, -1.0), yfov_deg=50.0, width=width, height=height)
+    return InstancedSceneData(geoms, np.array(inst_g, np.uint32), np.array(inst_m, np.uint32),
+                              np.stack(xf).reshape(-1, 12), mats, lights, BSM_SKY_CONSTANT, (0.4, 0.5, 0.6), None, cam)
 
 
 def generate_scene(kind: int, seed: int = 1, grid: int = 0, spheres: int = 0, sky_width: int = 0,
@@ -523,6 +672,7 @@ class Context:
         if st != BSM_OK:
             raise BsmError(st, "bsm_create failed (no CUDA device?)")
         self.h = h
+        self._scene_geoms = {}   # two-level scene id -> its geometry ids
 
     def close(self):
         if self.h:
@@ -558,6 +708,62 @@ class Context:
 
     def release(self, scene_id: int):
         self.check(self._L.bsm_scene_release(self.h, scene_id))
+        for gid in self._scene_geoms.pop(scene_id, []):
+            self._L.bsm_geometry_release(self.h, gid)
+
+    def create_geometry(self, g: GeometryData, sah_bins=0, max_leaf=0, threads=0) -> int:
+        pos = np.ascontiguousarray(g.positions, np.float32)
+        idx = None if g.indices is None else np.ascontiguousarray(g.indices, np.uint32)
+        mids = None if g.material_ids is None else np.ascontiguousarray(g.material_ids, np.uint32)
+        d = GeometryDesc(pos.shape[0], _ptr(pos), g.num_triangles, _ptr(idx, C.c_uint32) if idx is not None else None,
+                         _ptr(mids, C.c_uint32) if mids is not None else None)
+        o = BvhOpts(sah_bins, max_leaf, threads)
+        gid = C.c_uint32()
+        self.check(self._L.bsm_geometry_create(self.h, C.byref(d), C.byref(o), C.byref(gid)))
+        return gid.value
+
+    def load_instanced(self, scene: InstancedSceneData) -> int:
+        """Creates the scene's geometries and the two-level scene; returns the scene id (release() frees both)."""
+        gids = [self.create_geometry(g) for g in scene.geometries]
+        n = len(scene.inst_geometry)
+        insts = (Instance * n)()
+        xf = np.ascontiguousarray(scene.inst_transform, np.float32).reshape(n, 12)
+        for i in range(n):
+            insts[i].geometry_id = gids[int(scene.inst_geometry[i])]
+            insts[i].material_id = int(scene.inst_material[i])
+            insts[i].transform[:] = [float(x) for x in xf[i]]
+        mats = _materials_array(scene.materials)
+        lights = (DirLight * max(1, len(scene.lights)))()
+        for i, l in enumerate(scene.lights):
+            lights[i].direction[:] = [float(x) for x in l[:3]]
+            lights[i].emission[:] = [float(x) for x in l[3:6]]
+        d = InstancedSceneDesc()
+        d.num_instances = n
+        d.instances = insts
+        d.num_materials = len(scene.materials)
+        d.materials = mats
+        d.num_dir_lights = len(scene.lights)
+        d.dir_lights = lights
+        d.sky.kind = scene.sky_kind
+        d.sky.color[:] = list(scene.sky_color)
+        tex = None
+        if scene.sky_texels is not None:
+            tex = np.ascontiguousarray(scene.sky_texels, np.uint16)
+            d.sky.width, d.sky.height = tex.shape[1], tex.shape[0]
+            d.sky.rgba16f = _ptr(tex, C.c_uint16)
+        sid = C.c_uint32()
+        st = self._L.bsm_scene_create_instanced(self.h, C.byref(d), C.byref(sid))
+        if st != BSM_OK:
+            for gid in gids:
+                self._L.bsm_geometry_release(self.h, gid)
+            self.check(st)
+        self._scene_geoms[sid.value] = gids
+        return sid.value
+
+    def update_instances(self, scene_id: int, transforms: np.ndarray):
+        """New object-to-world transforms (N, 12); the TLAS is refitted on the GPU."""
+        xf = np.ascontiguousarray(transforms, np.float32).reshape(-1, 12)
+        self.check(self._L.bsm_scene_update_instances(self.h, scene_id, xf.ctypes.data, xf.shape[0]))
 
     def scene_bytes(self, scene_id: int) -> int:
         b = C.c_uint64()

@@ -51,7 +51,23 @@ struct Scene {
     bool tuned = false;
     bsm_tune_params tune{};
     DevBuf nodes, tris, materials, texels, cdf_marg, cdf_cond, pdf_tab;
+    // two-level scenes: instances (caller order), their TLAS leaves, refit data
+    bool instanced = false;
+    std::vector<bsm_instance> instances;
+    std::vector<uint32_t> leaf_of;          // caller index -> TLAS leaf (InstDev record)
+    std::vector<uint32_t> level_begin;      // TLAS breadth-first level boundaries (levels + 1 entries)
+    std::vector<InstDev> inst_host;         // records in leaf order
+    DevBuf insts, inst_box, node_box, mat_tr;
     DevScene dev{};
+};
+
+// An object-space geometry of two-level scenes: its own BLAS.
+struct Geometry {
+    DevBuf nodes, tris;
+    float lo[3], hi[3];                     // object-space bounds
+    uint32_t num_triangles = 0;
+    uint32_t max_material = 0;
+    uint32_t users = 0;                     // scenes that instance it
 };
 
 struct ViewHist {
@@ -76,6 +92,8 @@ struct bsm_context {
     std::string err;
     std::map<uint32_t, std::unique_ptr<Scene>> scenes;
     uint32_t next_scene = 1;
+    std::map<uint32_t, std::unique_ptr<Geometry>> geoms;
+    uint32_t next_geom = 1;
     LaunchCfg lc{};
     int lc_block = 0;
     // wavefront buffers
@@ -356,6 +374,96 @@ extern "C" bsm_status bsm_host_free(bsm_context* ctx, void* ptr) {
     return BSM_OK;
 }
 
+namespace {
+bsm_status build_tlas(bsm_context* ctx, Scene* sc);
+
+// Device buffers of a scene; an instanced scene also lets go of its geometries.
+void free_scene_buffers(bsm_context* ctx, Scene& sc) {
+    for (DevBuf* b : {&sc.nodes, &sc.tris, &sc.materials, &sc.texels, &sc.cdf_marg, &sc.cdf_cond, &sc.pdf_tab,
+                      &sc.insts, &sc.inst_box, &sc.node_box, &sc.mat_tr})
+        dev_free(ctx, *b);
+    if (sc.instanced)
+        for (const bsm_instance& in : sc.instances) {
+            auto it = ctx->geoms.find(in.geometry_id);
+            if (it != ctx->geoms.end() && it->second->users > 0) it->second->users--;
+        }
+    sc.instanced = false;
+    sc.instances.clear();
+}
+
+// Materials, lights, sky and the scene bounds of a scene (both kinds).
+bsm_status setup_shading(bsm_context* ctx, Scene* sc, const bsm_material* materials, uint32_t num_materials,
+                         const bsm_dir_light* dir_lights, uint32_t num_dir_lights, const bsm_sky& sky,
+                         const float lo[3], const float hi[3]) {
+    if (num_materials == 0 || !materials) return fail(ctx, BSM_ERR_INVALID_ARG, "scene needs at least one material");
+    if (num_dir_lights > (uint32_t)kMaxLights)
+        return fail(ctx, BSM_ERR_INVALID_ARG, "at most " + std::to_string(kMaxLights) + " directional lights");
+    if (num_dir_lights && !dir_lights) return fail(ctx, BSM_ERR_INVALID_ARG, "dir_lights is NULL");
+    if (sky.kind == BSM_SKY_EQUIRECT && (!sky.rgba16f || sky.width == 0 || sky.height == 0))
+        return fail(ctx, BSM_ERR_INVALID_ARG, "equirect sky needs texels");
+    if (sky.kind > BSM_SKY_EQUIRECT) return fail(ctx, BSM_ERR_INVALID_ARG, "unknown sky kind");
+    sc->extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
+    // materials: (base.rgb, roughness), (f0.rgb, metallic); f0 = lerp(0.04, base, metallic)
+    std::vector<float4> mats(2 * (size_t)num_materials);
+    sc->transparency.assign(num_materials, 0.0f);
+    for (uint32_t m = 0; m < num_materials; ++m) {
+        const bsm_material& M = materials[m];
+        if (M.blend_mode > BSM_BLEND_TRANSLUCENT) return fail(ctx, BSM_ERR_INVALID_ARG, "unknown blend mode");
+        if (M.blend_mode != BSM_BLEND_OPAQUE && !(M.opacity >= 0.0f && M.opacity <= 1.0f))
+            return fail(ctx, BSM_ERR_INVALID_ARG, "opacity must be in [0, 1]");
+        // the any-hit rule (rt_gbuffer_hit.hlsl:20-35): alpha test drops the hit below the
+        // threshold (utils.hlsl:38), translucent drops it when u < 1 - opacity
+        if (M.blend_mode == BSM_BLEND_ALPHA_TEST) sc->transparency[m] = M.opacity < 0.01f ? 1.0f : 0.0f;
+        if (M.blend_mode == BSM_BLEND_TRANSLUCENT) sc->transparency[m] = 1.0f - M.opacity;
+        float f0[3];
+        for (int k = 0; k < 3; ++k) f0[k] = 0.04f + (M.base_color[k] - 0.04f) * M.metallic;
+        mats[2 * m] = make_float4(M.base_color[0], M.base_color[1], M.base_color[2], M.roughness);
+        mats[2 * m + 1] = make_float4(f0[0], f0[1], f0[2], M.metallic);
+    }
+    bsm_status st;
+    if ((st = dev_alloc(ctx, sc->materials, mats.size() * sizeof(float4)))) return st;
+    CK(cudaMemcpy(sc->materials.ptr, mats.data(), mats.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    DevScene& ds = sc->dev;
+    ds.materials = (const float4*)sc->materials.ptr;
+    ds.num_materials = num_materials;
+    ds.num_lights = num_dir_lights;
+    for (uint32_t l = 0; l < num_dir_lights; ++l) {
+        const bsm_dir_light& L = dir_lights[l];
+        V3 dir = normalize(v3(L.direction[0], L.direction[1], L.direction[2]));
+        ds.light_dir[l] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+        ds.light_e[l] = make_float4(L.emission[0], L.emission[1], L.emission[2], 0.0f);
+    }
+    ds.sky.kind = sky.kind;
+    ds.sky.cr = sky.color[0]; ds.sky.cg = sky.color[1]; ds.sky.cb = sky.color[2];
+    if (sky.kind == BSM_SKY_EQUIRECT) {
+        const uint32_t W = sky.width, H = sky.height;
+        std::vector<float> marg, cond, pdf;
+        build_sky_tables(sky, marg, cond, pdf);
+        size_t tb = (size_t)W * H * 8;
+        if ((st = dev_alloc(ctx, sc->texels, tb))) return st;
+        if ((st = dev_alloc(ctx, sc->cdf_marg, marg.size() * 4))) return st;
+        if ((st = dev_alloc(ctx, sc->cdf_cond, cond.size() * 4))) return st;
+        if ((st = dev_alloc(ctx, sc->pdf_tab, pdf.size() * 4))) return st;
+        CK(cudaMemcpy(sc->texels.ptr, sky.rgba16f, tb, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->cdf_marg.ptr, marg.data(), marg.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->cdf_cond.ptr, cond.data(), cond.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->pdf_tab.ptr, pdf.data(), pdf.size() * 4, cudaMemcpyHostToDevice));
+        ds.sky.width = W; ds.sky.height = H;
+        ds.sky.texels = (const ushort4*)sc->texels.ptr;
+        ds.sky.cdf_marg = (const float*)sc->cdf_marg.ptr;
+        ds.sky.cdf_cond = (const float*)sc->cdf_cond.ptr;
+        ds.sky.pdf_tab = (const float*)sc->pdf_tab.ptr;
+    }
+    ds.ray_offset = 2e-5f * sc->extent;
+    for (int k = 0; k < 3; ++k) {
+        ds.box_lo[k] = lo[k];
+        ds.box_inv[k] = 1.0f / std::max(hi[k] - lo[k], 1e-6f);
+    }
+    return BSM_OK;
+}
+
+}  // namespace
+
 // ================================================================ scenes ====
 extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d, uint32_t* scene_id) {
     if (!ctx || !d || !scene_id) return BSM_ERR_INVALID_ARG;
@@ -390,67 +498,17 @@ extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d
             if (!std::isfinite(p)) return fail(ctx, BSM_ERR_INVALID_ARG, "non-finite vertex position");
             lo[k] = std::min(lo[k], p); hi[k] = std::max(hi[k], p);
         }
-    sc->extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
-    // materials: (base.rgb, roughness), (f0.rgb, metallic); f0 = lerp(0.04, base, metallic)
-    std::vector<float4> mats(2 * (size_t)d->num_materials);
-    sc->transparency.assign(d->num_materials, 0.0f);
-    for (uint32_t m = 0; m < d->num_materials; ++m) {
-        const bsm_material& M = d->materials[m];
-        if (M.blend_mode > BSM_BLEND_TRANSLUCENT) return fail(ctx, BSM_ERR_INVALID_ARG, "unknown blend mode");
-        if (M.blend_mode != BSM_BLEND_OPAQUE && !(M.opacity >= 0.0f && M.opacity <= 1.0f))
-            return fail(ctx, BSM_ERR_INVALID_ARG, "opacity must be in [0, 1]");
-        // the any-hit rule (rt_gbuffer_hit.hlsl:20-35): alpha test drops the hit below the
-        // threshold (utils.hlsl:38), translucent drops it when u < 1 - opacity
-        if (M.blend_mode == BSM_BLEND_ALPHA_TEST) sc->transparency[m] = M.opacity < 0.01f ? 1.0f : 0.0f;
-        if (M.blend_mode == BSM_BLEND_TRANSLUCENT) sc->transparency[m] = 1.0f - M.opacity;
-        float f0[3];
-        for (int k = 0; k < 3; ++k) f0[k] = 0.04f + (M.base_color[k] - 0.04f) * M.metallic;
-        mats[2 * m] = make_float4(M.base_color[0], M.base_color[1], M.base_color[2], M.roughness);
-        mats[2 * m + 1] = make_float4(f0[0], f0[1], f0[2], M.metallic);
-    }
-    bsm_status st;
-    if ((st = dev_alloc(ctx, sc->materials, mats.size() * sizeof(float4)))) return st;
-    CK(cudaMemcpy(sc->materials.ptr, mats.data(), mats.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    bsm_status st = setup_shading(ctx, sc.get(), d->materials, d->num_materials, d->dir_lights, d->num_dir_lights,
+                                  d->sky, lo, hi);
+    if (st) { free_scene_buffers(ctx, *sc); return st; }
     DevScene& ds = sc->dev;
-    ds.materials = (const float4*)sc->materials.ptr;
-    ds.num_materials = d->num_materials;
     ds.has_non_opaque = 0;
     for (uint32_t t = 0; t < d->num_triangles; ++t)
         if (sc->transparency[d->material_ids ? d->material_ids[t] : 0] != 0.0f) { ds.has_non_opaque = 1; break; }
-    ds.num_lights = d->num_dir_lights;
-    for (uint32_t l = 0; l < d->num_dir_lights; ++l) {
-        const bsm_dir_light& L = d->dir_lights[l];
-        V3 dir = normalize(v3(L.direction[0], L.direction[1], L.direction[2]));
-        ds.light_dir[l] = make_float4(dir.x, dir.y, dir.z, 0.0f);
-        ds.light_e[l] = make_float4(L.emission[0], L.emission[1], L.emission[2], 0.0f);
+    if (ctx->server) {
+        free_scene_buffers(ctx, *sc);
+        return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
     }
-    ds.sky.kind = d->sky.kind;
-    ds.sky.cr = d->sky.color[0]; ds.sky.cg = d->sky.color[1]; ds.sky.cb = d->sky.color[2];
-    if (d->sky.kind == BSM_SKY_EQUIRECT) {
-        const uint32_t W = d->sky.width, H = d->sky.height;
-        std::vector<float> marg, cond, pdf;
-        build_sky_tables(d->sky, marg, cond, pdf);
-        size_t tb = (size_t)W * H * 8;
-        if ((st = dev_alloc(ctx, sc->texels, tb))) return st;
-        if ((st = dev_alloc(ctx, sc->cdf_marg, marg.size() * 4))) return st;
-        if ((st = dev_alloc(ctx, sc->cdf_cond, cond.size() * 4))) return st;
-        if ((st = dev_alloc(ctx, sc->pdf_tab, pdf.size() * 4))) return st;
-        CK(cudaMemcpy(sc->texels.ptr, d->sky.rgba16f, tb, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(sc->cdf_marg.ptr, marg.data(), marg.size() * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(sc->cdf_cond.ptr, cond.data(), cond.size() * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(sc->pdf_tab.ptr, pdf.data(), pdf.size() * 4, cudaMemcpyHostToDevice));
-        ds.sky.width = W; ds.sky.height = H;
-        ds.sky.texels = (const ushort4*)sc->texels.ptr;
-        ds.sky.cdf_marg = (const float*)sc->cdf_marg.ptr;
-        ds.sky.cdf_cond = (const float*)sc->cdf_cond.ptr;
-        ds.sky.pdf_tab = (const float*)sc->pdf_tab.ptr;
-    }
-    ds.ray_offset = 2e-5f * sc->extent;
-    for (int k = 0; k < 3; ++k) {
-        ds.box_lo[k] = lo[k];
-        ds.box_inv[k] = 1.0f / std::max(hi[k] - lo[k], 1e-6f);
-    }
-    if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
     std::lock_guard<std::mutex> lk(ctx->mu);
     uint32_t id = ctx->next_scene++;
     ctx->scenes[id] = std::move(sc);
@@ -465,6 +523,12 @@ extern "C" bsm_status bsm_scene_build_bvh(bsm_context* ctx, uint32_t scene_id, c
     Scene* sc = find_scene(ctx, scene_id);
     if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
     if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
+    if (sc->instanced) {  // a full rebuild of the TLAS from the current transforms
+        cudaStreamSynchronize(ctx->stream);
+        bsm_status st = build_tlas(ctx, sc);
+        if (!st && stats) *stats = sc->bvh_stats;
+        return st;
+    }
     BvhBuildResult r;
     std::string err;
     if (!build_cwbvh(sc->positions.data(), sc->indices.empty() ? nullptr : sc->indices.data(), sc->num_triangles,
@@ -538,10 +602,293 @@ extern "C" bsm_status bsm_scene_release(bsm_context* ctx, uint32_t scene_id) {
     if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
     if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf* b : {&sc->nodes, &sc->tris, &sc->materials, &sc->texels, &sc->cdf_marg, &sc->cdf_cond, &sc->pdf_tab})
-        dev_free(ctx, *b);
+    free_scene_buffers(ctx, *sc);
     ctx->scenes.erase(scene_id);
     clear_graphs(ctx);
+    return BSM_OK;
+}
+
+// ============================================================ instancing ====
+namespace {
+
+// Object-to-world (row-major 3x4) -> world-to-object: the inverse in double
+// (cofactors, determinant along the first row), rounded to float.  The oracle
+// evaluates the same expressions in the same order.
+bool invert_affine(const float* m, float* inv) {
+    double L00 = m[0], L01 = m[1], L02 = m[2], t0 = m[3];
+    double L10 = m[4], L11 = m[5], L12 = m[6], t1 = m[7];
+    double L20 = m[8], L21 = m[9], L22 = m[10], t2 = m[11];
+    double c00 = L11 * L22 - L12 * L21, c01 = L02 * L21 - L01 * L22, c02 = L01 * L12 - L02 * L11;
+    double c10 = L12 * L20 - L10 * L22, c11 = L00 * L22 - L02 * L20, c12 = L02 * L10 - L00 * L12;
+    double c20 = L10 * L21 - L11 * L20, c21 = L01 * L20 - L00 * L21, c22 = L00 * L11 - L01 * L10;
+    double det = L00 * c00 + L01 * c10 + L02 * c20;
+    if (!std::isfinite(det) || !(std::fabs(det) > 1e-30)) return false;
+    double r[9] = {c00 / det, c01 / det, c02 / det, c10 / det, c11 / det, c12 / det, c20 / det, c21 / det, c22 / det};
+    for (int i = 0; i < 3; ++i) {
+        inv[4 * i] = (float)r[3 * i];
+        inv[4 * i + 1] = (float)r[3 * i + 1];
+        inv[4 * i + 2] = (float)r[3 * i + 2];
+        inv[4 * i + 3] = (float)(-(r[3 * i] * t0 + r[3 * i + 1] * t1 + r[3 * i + 2] * t2));
+    }
+    return true;
+}
+
+// World box of an instance: the eight transformed corners of the geometry's
+// box in double, padded by 1e-5 of the coordinates' magnitude (more than the
+// rounding of the float ray transform) and rounded outward to float.
+void instance_world_box(const float* m, const float glo[3], const float ghi[3], float lo[3], float hi[3]) {
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < 8; ++c) {
+        double p[3] = {(c & 1) ? ghi[0] : glo[0], (c & 2) ? ghi[1] : glo[1], (c & 4) ? ghi[2] : glo[2]};
+        for (int k = 0; k < 3; ++k) {
+            double w = (double)m[4 * k] * p[0] + (double)m[4 * k + 1] * p[1] + (double)m[4 * k + 2] * p[2] +
+                       (double)m[4 * k + 3];
+            mn[k] = std::min(mn[k], w);
+            mx[k] = std::max(mx[k], w);
+        }
+    }
+    double mag = 0.0;
+    for (int k = 0; k < 3; ++k) mag = std::max(mag, std::max(std::fabs(mn[k]), std::fabs(mx[k])));
+    double pad = 1e-5 * mag + 1e-30;
+    for (int k = 0; k < 3; ++k) {
+        float l = (float)(mn[k] - pad), h = (float)(mx[k] + pad);
+        while ((double)l > mn[k] - pad) l = std::nextafter(l, -INFINITY);
+        while ((double)h < mx[k] + pad) h = std::nextafter(h, INFINITY);
+        lo[k] = l;
+        hi[k] = h;
+    }
+}
+
+bool valid_transform(const float* m) {
+    for (int i = 0; i < 12; ++i)
+        if (!std::isfinite(m[i])) return false;
+    float inv[12];
+    return invert_affine(m, inv);
+}
+
+// Instance records (w2o, o2w, BLAS pointers) and world boxes of every instance, in leaf order.
+void fill_instances(bsm_context* ctx, Scene* sc, std::vector<float>& boxes) {
+    const uint32_t n = (uint32_t)sc->instances.size();
+    sc->inst_host.resize(n);
+    boxes.assign(6 * (size_t)n, 0.0f);
+    uint32_t prim_base = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const bsm_instance& in = sc->instances[i];
+        Geometry* g = ctx->geoms.at(in.geometry_id).get();
+        uint32_t leaf = sc->leaf_of[i];
+        InstDev& r = sc->inst_host[leaf];
+        std::memcpy(r.o2w, in.transform, sizeof(r.o2w));
+        invert_affine(in.transform, r.w2o);
+        r.nodes = (const CwNode*)g->nodes.ptr;
+        r.tris = (const CwTri*)g->tris.ptr;
+        r.prim_base = prim_base;
+        r.material = in.material_id;
+        r.id = i;
+        r.pad = 0;
+        prim_base += g->num_triangles;
+        instance_world_box(in.transform, g->lo, g->hi, &boxes[6 * (size_t)leaf], &boxes[6 * (size_t)leaf + 3]);
+    }
+}
+
+// Builds the TLAS of an instanced scene from its instances' current world boxes
+// (the same SAH builder, one instance per leaf) and uploads it with the records.
+bsm_status build_tlas(bsm_context* ctx, Scene* sc) {
+    const uint32_t n = (uint32_t)sc->instances.size();
+    std::vector<float> corners(6 * (size_t)n);
+    std::vector<uint32_t> idx(3 * (size_t)n);
+    sc->leaf_of.assign(n, 0);
+    for (uint32_t i = 0; i < n; ++i) {
+        const bsm_instance& in = sc->instances[i];
+        Geometry* g = ctx->geoms.at(in.geometry_id).get();
+        instance_world_box(in.transform, g->lo, g->hi, &corners[6 * (size_t)i], &corners[6 * (size_t)i + 3]);
+        idx[3 * i] = 2 * i; idx[3 * i + 1] = 2 * i + 1; idx[3 * i + 2] = 2 * i;  // a "triangle" spanning the box
+    }
+    bsm_bvh_opts opts{};
+    opts.max_leaf_tris = 1;
+    BvhBuildResult r;
+    std::string err;
+    if (!build_cwbvh(corners.data(), idx.data(), n, nullptr, &opts, r, err))
+        return fail(ctx, BSM_ERR_INVALID_ARG, "TLAS build failed: " + err);
+    if (r.max_depth > (uint32_t)kMaxTlasDepth)
+        return fail(ctx, BSM_ERR_UNSUPPORTED, "TLAS deeper than " + std::to_string(kMaxTlasDepth) + " levels");
+    for (uint32_t l = 0; l < n; ++l) sc->leaf_of[r.tris[l].prim] = l;
+    // breadth-first levels: nodes are emitted in BFS order, so each level is a contiguous range
+    std::vector<uint32_t> depth(r.nodes.size(), 0);
+    for (uint32_t ni = 0; ni < r.nodes.size(); ++ni) {
+        const CwNode& nd = r.nodes[ni];
+        uint32_t k = 0;
+        for (int s = 0; s < 8; ++s)
+            if (nd.imask & (1u << s)) depth[nd.child_base + k++] = depth[ni] + 1;
+    }
+    sc->level_begin.clear();
+    for (uint32_t ni = 0; ni < r.nodes.size(); ++ni)
+        if (ni == 0 || depth[ni] != depth[ni - 1]) sc->level_begin.push_back(ni);
+    sc->level_begin.push_back((uint32_t)r.nodes.size());
+    std::vector<float> boxes;
+    fill_instances(ctx, sc, boxes);
+    bsm_status st;
+    dev_free(ctx, sc->nodes);
+    if ((st = dev_alloc(ctx, sc->nodes, r.nodes.size() * sizeof(CwNode)))) return st;
+    if ((st = dev_alloc(ctx, sc->insts, (size_t)n * sizeof(InstDev)))) return st;
+    if ((st = dev_alloc(ctx, sc->inst_box, boxes.size() * 4))) return st;
+    if ((st = dev_alloc(ctx, sc->node_box, r.nodes.size() * 6 * 4))) return st;
+    CK(cudaMemcpy(sc->nodes.ptr, r.nodes.data(), r.nodes.size() * sizeof(CwNode), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sc->insts.ptr, sc->inst_host.data(), (size_t)n * sizeof(InstDev), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sc->inst_box.ptr, boxes.data(), boxes.size() * 4, cudaMemcpyHostToDevice));
+    DevScene& ds = sc->dev;
+    ds.nodes = (const CwNode*)sc->nodes.ptr;
+    ds.tris = nullptr;
+    ds.insts = (const InstDev*)sc->insts.ptr;
+    ds.num_instances = n;
+    bsm_bvh_stats bs{};
+    bs.num_nodes = (uint32_t)r.nodes.size();
+    bs.num_tris = n;
+    bs.max_depth = r.max_depth;
+    bs.build_ms = r.build_ms;
+    bs.sah_cost = r.sah_cost;
+    bs.node_bytes = r.nodes.size() * sizeof(CwNode);
+    bs.tri_bytes = (uint64_t)n * sizeof(InstDev);
+    sc->bvh_stats = bs;
+    sc->has_bvh = true;
+    clear_graphs(ctx);
+    return BSM_OK;
+}
+
+}  // namespace
+
+extern "C" bsm_status bsm_geometry_create(bsm_context* ctx, const bsm_geometry_desc* d, const bsm_bvh_opts* opts,
+                                          uint32_t* geometry_id) {
+    if (!ctx || !d || !geometry_id) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (d->num_triangles == 0 || !d->positions || d->num_vertices == 0)
+        return fail(ctx, BSM_ERR_INVALID_ARG, "geometry needs vertices and triangles");
+    if (d->indices) {
+        for (size_t i = 0; i < 3 * (size_t)d->num_triangles; ++i)
+            if (d->indices[i] >= d->num_vertices) return fail(ctx, BSM_ERR_INVALID_ARG, "vertex index out of range");
+    } else if ((size_t)d->num_vertices < 3 * (size_t)d->num_triangles) {
+        return fail(ctx, BSM_ERR_INVALID_ARG, "triangle soup needs 3 vertices per triangle");
+    }
+    auto g = std::make_unique<Geometry>();
+    for (int k = 0; k < 3; ++k) { g->lo[k] = INFINITY; g->hi[k] = -INFINITY; }
+    for (size_t i = 0; i < (size_t)d->num_vertices; ++i)
+        for (int k = 0; k < 3; ++k) {
+            float p = d->positions[3 * i + k];
+            if (!std::isfinite(p)) return fail(ctx, BSM_ERR_INVALID_ARG, "non-finite vertex position");
+            g->lo[k] = std::min(g->lo[k], p);
+            g->hi[k] = std::max(g->hi[k], p);
+        }
+    if (d->material_ids)
+        for (uint32_t t = 0; t < d->num_triangles; ++t) g->max_material = std::max(g->max_material, d->material_ids[t]);
+    BvhBuildResult r;
+    std::string err;
+    if (!build_cwbvh(d->positions, d->indices, d->num_triangles, d->material_ids, opts, r, err))
+        return fail(ctx, BSM_ERR_INVALID_ARG, "BVH build failed: " + err);
+    // two-level stack: (TLAS depth - 1) + 3 transition entries + (BLAS depth - 1) <= 11 + 3 + 23 < kStackSize
+    if (r.max_depth > (uint32_t)kMaxTraversalDepth)
+        return fail(ctx, BSM_ERR_UNSUPPORTED, "geometry BVH deeper than the traversal stack");
+    bsm_status st;
+    if ((st = dev_alloc(ctx, g->nodes, r.nodes.size() * sizeof(CwNode)))) return st;
+    if ((st = dev_alloc(ctx, g->tris, r.tris.size() * sizeof(CwTri)))) { dev_free(ctx, g->nodes); return st; }
+    CK(cudaMemcpy(g->nodes.ptr, r.nodes.data(), r.nodes.size() * sizeof(CwNode), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(g->tris.ptr, r.tris.data(), r.tris.size() * sizeof(CwTri), cudaMemcpyHostToDevice));
+    g->num_triangles = d->num_triangles;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    uint32_t id = ctx->next_geom++;
+    ctx->geoms[id] = std::move(g);
+    *geometry_id = id;
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_geometry_release(bsm_context* ctx, uint32_t geometry_id) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    auto it = ctx->geoms.find(geometry_id);
+    if (it == ctx->geoms.end()) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown geometry id");
+    if (it->second->users) return fail(ctx, BSM_ERR_BAD_STATE, "geometry is instanced by a scene");
+    cudaSetDevice(ctx->device);
+    dev_free(ctx, it->second->nodes);
+    dev_free(ctx, it->second->tris);
+    ctx->geoms.erase(it);
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_scene_create_instanced(bsm_context* ctx, const bsm_instanced_scene_desc* d,
+                                                 uint32_t* scene_id) {
+    if (!ctx || !d || !scene_id) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
+    if (d->num_instances == 0 || !d->instances) return fail(ctx, BSM_ERR_INVALID_ARG, "scene needs instances");
+    uint64_t total = 0;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = 0; i < d->num_instances; ++i) {
+        const bsm_instance& in = d->instances[i];
+        auto it = ctx->geoms.find(in.geometry_id);
+        if (it == ctx->geoms.end()) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown geometry id in instance " + std::to_string(i));
+        if (in.material_id != kMissPrim ? in.material_id >= d->num_materials : it->second->max_material >= d->num_materials)
+            return fail(ctx, BSM_ERR_INVALID_ARG, "material id out of range in instance " + std::to_string(i));
+        if (!valid_transform(in.transform))
+            return fail(ctx, BSM_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": transform not finite / invertible");
+        total += it->second->num_triangles;
+        float bl[3], bh[3];
+        instance_world_box(in.transform, it->second->lo, it->second->hi, bl, bh);
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], bl[k]); hi[k] = std::max(hi[k], bh[k]); }
+    }
+    if (total >= 0xffffffffull) return fail(ctx, BSM_ERR_INVALID_ARG, "more than 2^32 - 1 instanced triangles");
+    auto sc = std::make_unique<Scene>();
+    sc->instanced = true;
+    sc->instances.assign(d->instances, d->instances + d->num_instances);
+    sc->num_triangles = (uint32_t)total;
+    for (const bsm_instance& in : sc->instances) ctx->geoms[in.geometry_id]->users++;
+    bsm_status st = setup_shading(ctx, sc.get(), d->materials, d->num_materials, d->dir_lights, d->num_dir_lights,
+                                  d->sky, lo, hi);
+    if (!st) {
+        bool any = false;
+        for (float t : sc->transparency) any = any || t != 0.0f;
+        sc->dev.has_non_opaque = any ? 1u : 0u;
+        sc->dev.mat_tr = nullptr;
+        if (any) {
+            st = dev_alloc(ctx, sc->mat_tr, sc->transparency.size() * 4);
+            if (!st && cudaMemcpy(sc->mat_tr.ptr, sc->transparency.data(), sc->transparency.size() * 4,
+                                  cudaMemcpyHostToDevice) != cudaSuccess)
+                st = fail(ctx, BSM_ERR_CUDA, "material upload failed");
+            sc->dev.mat_tr = (const float*)sc->mat_tr.ptr;
+        }
+    }
+    if (!st) st = build_tlas(ctx, sc.get());
+    if (st) { free_scene_buffers(ctx, *sc); return st; }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    uint32_t id = ctx->next_scene++;
+    ctx->scenes[id] = std::move(sc);
+    *scene_id = id;
+    return BSM_OK;
+}
+
+extern "C" bsm_status bsm_scene_update_instances(bsm_context* ctx, uint32_t scene_id, const float* transforms,
+                                                 uint32_t num_instances) {
+    if (!ctx || !transforms) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Scene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
+    if (!sc->instanced) return fail(ctx, BSM_ERR_BAD_STATE, "not an instanced scene");
+    if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
+    if (num_instances != sc->instances.size())
+        return fail(ctx, BSM_ERR_INVALID_ARG, "transform count differs from the scene's instances");
+    for (uint32_t i = 0; i < num_instances; ++i)
+        if (!valid_transform(transforms + 12 * (size_t)i))
+            return fail(ctx, BSM_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": transform not finite / invertible");
+    for (uint32_t i = 0; i < num_instances; ++i)
+        std::memcpy(sc->instances[i].transform, transforms + 12 * (size_t)i, 12 * sizeof(float));
+    std::vector<float> boxes;
+    fill_instances(ctx, sc, boxes);
+    CK(cudaStreamSynchronize(ctx->stream));  // no render may read the records while they change
+    CK(cudaMemcpyAsync(sc->insts.ptr, sc->inst_host.data(), sc->inst_host.size() * sizeof(InstDev),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(sc->inst_box.ptr, boxes.data(), boxes.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    // refit bottom-up: one launch per breadth-first level, deepest first
+    for (size_t lv = sc->level_begin.size() - 1; lv-- > 0;)
+        launch_tlas_refit(ctx->stream, (CwNode*)sc->nodes.ptr, (float*)sc->node_box.ptr, (const float*)sc->inst_box.ptr,
+                          sc->level_begin[lv], sc->level_begin[lv + 1]);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
     return BSM_OK;
 }
 
@@ -550,7 +897,8 @@ extern "C" bsm_status bsm_scene_device_bytes(bsm_context* ctx, uint32_t scene_id
     Scene* sc = find_scene(ctx, scene_id);
     if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
     uint64_t b = 0;
-    for (DevBuf* x : {&sc->nodes, &sc->tris, &sc->materials, &sc->texels, &sc->cdf_marg, &sc->cdf_cond, &sc->pdf_tab})
+    for (DevBuf* x : {&sc->nodes, &sc->tris, &sc->materials, &sc->texels, &sc->cdf_marg, &sc->cdf_cond, &sc->pdf_tab,
+                      &sc->insts, &sc->inst_box, &sc->node_box, &sc->mat_tr})
         b += x->bytes;
     *bytes = b;
     return BSM_OK;
@@ -562,7 +910,10 @@ extern "C" bsm_status bsm_scene_download_bvh(bsm_context* ctx, uint32_t scene_id
     Scene* sc = find_scene(ctx, scene_id);
     if (!sc || !sc->has_bvh) return fail(ctx, BSM_ERR_NOT_FOUND, "scene has no BVH");
     if (nodes) CK(cudaMemcpy(nodes, sc->nodes.ptr, sc->bvh_stats.node_bytes, cudaMemcpyDeviceToHost));
-    if (tris) CK(cudaMemcpy(tris, sc->tris.ptr, sc->bvh_stats.tri_bytes, cudaMemcpyDeviceToHost));
+    if (tris) {  // a two-level scene's leaves are its instance records (InstDev, leaf order)
+        const void* src = sc->instanced ? sc->insts.ptr : sc->tris.ptr;
+        CK(cudaMemcpy(tris, src, sc->bvh_stats.tri_bytes, cudaMemcpyDeviceToHost));
+    }
     return BSM_OK;
 }
 
@@ -1158,6 +1509,7 @@ extern "C" bsm_status bsm_trace_counts(bsm_context* ctx, uint32_t scene_id, cons
     Scene* sc;
     bsm_status st = stage_prep(ctx, scene_id, &sc);
     if (st) return st;
+    if (sc->instanced) return fail(ctx, BSM_ERR_UNSUPPORTED, "traversal counters cover single-level scenes");
     if (n == 0) return BSM_OK;
     size_t rb = (size_t)n * 32, cb = (size_t)n * 8;
     if ((st = dev_alloc(ctx, ctx->tmp, rb + cb))) return st;

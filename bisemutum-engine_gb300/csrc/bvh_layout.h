@@ -35,7 +35,25 @@ struct alignas(16) CwTri {
 };
 static_assert(sizeof(CwTri) == 48, "CwTri must be 48 bytes");
 
+// One instance of a two-level scene, stored in the TLAS's leaf order (the
+// TLAS's leaf "triangle" index is the index of this record).  The world-to-
+// object transform (row-major 3x4) takes a world ray into the geometry's
+// space; t is the same in both spaces because the direction is not
+// renormalised.  Normals go back with the transpose of its 3x3 part.
+struct alignas(16) InstDev {
+    float w2o[12];
+    float o2w[12];           // object-to-world (tangents of the primary outputs)
+    const CwNode* nodes;     // the geometry's BLAS
+    const CwTri* tris;
+    uint32_t prim_base;      // global primitive id of the instance's triangle 0
+    uint32_t material;       // material for every triangle, or kMissPrim: the geometry's ids
+    uint32_t id;             // the caller's instance index
+    uint32_t pad;
+};
+static_assert(sizeof(InstDev) == 128, "InstDev must be 128 bytes");
+
 constexpr uint32_t kMissPrim = 0xffffffffu;
+constexpr int kMaxTlasDepth = 12;        // TLAS levels the two-level stack budget accepts
 constexpr int kMaxTraversalDepth = 24;   // deepest BVH the traversal stack accepts
 
 }  // namespace bsm

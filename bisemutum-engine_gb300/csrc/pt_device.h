@@ -38,8 +38,11 @@ struct DevSky {
 };
 
 struct DevScene {
-    const CwNode* nodes;
-    const CwTri* tris;
+    const CwNode* nodes;       // the BVH; in a two-level scene the TLAS
+    const CwTri* tris;         // leaf-ordered triangles (null in a two-level scene)
+    const InstDev* insts;      // two-level scene: instances in TLAS leaf order, else null
+    uint32_t num_instances;
+    const float* mat_tr;       // two-level scene with non-opaque materials: per-material transparency, else null
     const float4* materials;   // 2 per material: (base.rgb, roughness), (f0.rgb, metallic)
     uint32_t num_materials;
     uint32_t num_lights;
@@ -128,6 +131,8 @@ void launch_trace_closest(cudaStream_t st, const DevScene& sc, const float4* ray
 void launch_trace_any(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint8_t* occluded,
                       int block);
 void launch_trace_count(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint2* counts);
+void launch_tlas_refit(cudaStream_t st, CwNode* nodes, float* node_box, const float* inst_box, uint32_t begin,
+                       uint32_t end);
 void launch_primary(cudaStream_t st, const DevScene& sc, const DevView& v, float near_z, float far_z, float* depth,
                     float4* const gb[4], float4* hitpos);
 // radiance cache (mlp.cu)

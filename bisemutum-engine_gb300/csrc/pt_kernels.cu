@@ -20,7 +20,9 @@
 #include "pt_device.h"
 #include "pt_sky.cuh"
 #include "pt_trace.cuh"
+#include "pt_scene.cuh"
 #include "pt_gbuffer.cuh"
+#include "bvh_quant.h"
 #include "mlp.cuh"
 
 namespace bsm {
@@ -141,6 +143,46 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_shadow(DevScene sc, Wavefro
         nullptr, postpone_sp, refill_min);
 }
 
+// ------------------------------------------------- two-level extend / shadow ----
+// Two-level scenes: one ray per thread over the queue (grid-stride); the hit
+// record carries the instance in place of u.
+__global__ void __launch_bounds__(256) k_extend2(DevScene sc, const float4* __restrict__ ray_o,
+                                                 const float4* __restrict__ ray_d, const uint4* __restrict__ path,
+                                                 float4* __restrict__ hit, const uint32_t* counters,
+                                                 unsigned long long* stats, uint32_t seg) {
+    const uint32_t n = counters[kCntQueue + seg];
+    if (blockIdx.x == 0 && threadIdx.x == 0) stats[kStatExtend + seg] += n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 o = ray_o[i], d = ray_d[i];
+        RayPre r = make_ray(o, d);
+        float t, u, v;
+        uint32_t inst;
+        uint32_t leaf = trace_ray2<false>(r, d.w, sc.nodes, sc.insts, sc.mat_tr, t, u, v, inst,
+                                          sc.mat_tr ? path[i].z : 0u);
+        hit[i] = make_float4(t, __uint_as_float(leaf), __uint_as_float(inst), v);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_shadow2(DevScene sc, Wavefront wf, uint32_t seg, float4* accum) {
+    const uint32_t n_sun = wf.counters[kCntShadow + seg], n_sky = wf.counters[kCntSky + seg];
+    const uint32_t sh_cap = wf.capacity * (sc.num_lights + 1u);
+    const uint32_t n = n_sun + n_sky;
+    if (blockIdx.x == 0 && threadIdx.x == 0) wf.stats[kStatShadow + seg] += n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t k = i < n_sun ? i : sh_cap - 1u - (i - n_sun);
+        float4 o = wf.sh_o[k], d = wf.sh_d[k];
+        RayPre r = make_ray(o, d);
+        float t, u, v;
+        uint32_t inst;
+        uint32_t leaf = trace_ray2<true>(r, d.w, sc.nodes, sc.insts, sc.mat_tr, t, u, v, inst,
+                                         (sc.mat_tr && wf.sh_seed) ? wf.sh_seed[k] : 0u);
+        if (leaf == kMissPrim) {
+            float4 c = wf.sh_c[k];
+            accum_add(accum, __float_as_uint(c.w), v3(c.x, c.y, c.z));
+        }
+    }
+}
+
 // ----------------------------------------------------------------- shade ----
 __global__ void __launch_bounds__(256, 3) k_shade(DevScene sc, const DevView* __restrict__ views, Wavefront wf,
                                                int q, uint32_t seg, float4* accum) {
@@ -198,15 +240,12 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene sc, const DevView* __
         Surface surf;
         surf.base_color = v3s(0.5f); surf.f0 = v3s(0.04f); surf.f90 = v3s(1.0f); surf.roughness = 0.5f; surf.ior = 1.5f;
         if (is_hit) {
-            const float4* tp = reinterpret_cast<const float4*>(sc.tris + leaf);
-            float4 a = tp[0], b = tp[1], c = tp[2];
-            V3 va = v3(a.x, a.y, a.z), vb = v3(b.x, b.y, b.z), vc = v3(c.x, c.y, c.z);
-            V3 ng = normalize(cross(vb - va, vc - va));
+            V3 ng, edge;
+            uint32_t mi;
+            hit_geometry(sc, leaf, sc.insts ? __float_as_uint(h4.z) : kMissPrim, ng, edge, mi);
             if (dot(ng, d) > 0.0f) ng = -ng;
             N = ng;
             P = v3(o4.x, o4.y, o4.z) + d * h4.x;
-            uint32_t mi = __float_as_uint(b.w);
-            if (mi >= sc.num_materials) mi = 0;
             float4 m0 = sc.materials[2 * mi], m1 = sc.materials[2 * mi + 1];
             surf.base_color = v3(m0.x, m0.y, m0.z);
             surf.roughness = m0.w;
@@ -365,8 +404,11 @@ __global__ void __launch_bounds__(256) k_trace_closest(DevScene sc, const float4
     float4 o = rays[2 * (size_t)i], d = rays[2 * (size_t)i + 1];
     RayPre r = make_ray(o, d);
     float t, u, v;
-    uint32_t leaf = trace_ray<false, false>(r, d.w, sc.nodes, sc.tris, t, u, v, nullptr);
-    uint32_t prim = leaf == kMissPrim ? kMissPrim : sc.tris[leaf].prim;
+    uint32_t inst;
+    uint32_t leaf = trace_scene<false>(sc, r, d.w, t, u, v, inst, 0u);
+    uint32_t prim = kMissPrim;
+    if (leaf != kMissPrim)
+        prim = inst != kMissPrim ? sc.insts[inst].prim_base + sc.insts[inst].tris[leaf].prim : sc.tris[leaf].prim;
     hits[i] = make_uint4(__float_as_uint(t), prim, __float_as_uint(u), __float_as_uint(v));
 }
 
@@ -392,7 +434,8 @@ __global__ void __launch_bounds__(256) k_primary(DevScene sc, DevView v, float n
     float t, hu, hv;
     // opacity decisions of sample 0 of an unjittered render (its camera-ray PCG word)
     Pcg pg = pcg_seed(sample_initstate(v.seed, v.sample_offset), (uint64_t)i);
-    uint32_t leaf = trace_ray<false, false>(r, v.ray_length, sc.nodes, sc.tris, t, hu, hv, nullptr, (uint32_t)pg.state);
+    uint32_t inst;
+    uint32_t leaf = trace_scene<false>(sc, r, v.ray_length, t, hu, hv, inst, (uint32_t)pg.state);
     float g[16];
     float z = 0.0f;
     float4 hp;
@@ -401,14 +444,11 @@ __global__ void __launch_bounds__(256) k_primary(DevScene sc, DevView v, float n
         for (int k = 0; k < 16; ++k) g[k] = 0.0f;
         hp = make_float4(dw.x, dw.y, dw.z, -1.0f);
     } else {
-        const float4* tp = reinterpret_cast<const float4*>(sc.tris + leaf);
-        float4 a = tp[0], b = tp[1], c = tp[2];
-        V3 va = v3(a.x, a.y, a.z), vb = v3(b.x, b.y, b.z), vc = v3(c.x, c.y, c.z);
-        V3 ng = normalize(cross(vb - va, vc - va));
+        V3 ng, edge;
+        uint32_t mi;
+        hit_geometry(sc, leaf, inst, ng, edge, mi);
         if (dot(ng, dw) > 0.0f) ng = -ng;
-        V3 T = normalize(vb - va);
-        uint32_t mi = __float_as_uint(b.w);
-        if (mi >= sc.num_materials) mi = 0;
+        V3 T = normalize(edge);
         float4 m0 = sc.materials[2 * mi], m1 = sc.materials[2 * mi + 1];
         pack_gbuffer(ng, T, v3(m0.x, m0.y, m0.z), v3(m1.x, m1.y, m1.z), m0.w, g);
         V3 P = eye + dw * t;
@@ -430,7 +470,8 @@ __global__ void __launch_bounds__(256) k_trace_any(DevScene sc, const float4* __
     float4 o = rays[2 * (size_t)i], d = rays[2 * (size_t)i + 1];
     RayPre r = make_ray(o, d);
     float t, u, v;
-    uint32_t leaf = trace_ray<true, false>(r, d.w, sc.nodes, sc.tris, t, u, v, nullptr);
+    uint32_t inst;
+    uint32_t leaf = trace_scene<true>(sc, r, d.w, t, u, v, inst, 0u);
     occluded[i] = leaf == kMissPrim ? 0 : 1;
 }
 
@@ -446,7 +487,45 @@ __global__ void __launch_bounds__(256) k_trace_count(DevScene sc, const float4* 
     counts[i] = make_uint2(c.nodes, c.tris);
 }
 
+// ------------------------------------------------------------- TLAS refit ----
+// Refits the TLAS for new instance boxes, one BFS level per launch from the
+// deepest up (nodes of a level are contiguous in the builder's breadth-first
+// order).  A node's eight child boxes come from the instance boxes of its leaf
+// slots (TLAS leaves hold one instance) and from the boxes its internal
+// children wrote one launch earlier; the node's frame and bytes are then
+// quantised outward exactly as the host builder does (tlas_quantise).
+__global__ void k_tlas_refit(CwNode* __restrict__ nodes, float* __restrict__ node_box,
+                             const float* __restrict__ inst_box, uint32_t begin, uint32_t end) {
+    uint32_t ni = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (ni >= end) return;
+    CwNode n = nodes[ni];
+    float lo[8][3], hi[8][3];
+    uint32_t used = 0;
+    for (int s = 0; s < 8; ++s) {
+        uint8_t m = n.meta[s];
+        if (m == 0) continue;
+        used |= 1u << s;
+        const float* b;
+        if (n.imask & (1u << s)) {
+            uint32_t ci = n.child_base + (uint32_t)__popc((uint32_t)n.imask & ((1u << s) - 1u));
+            b = node_box + 6 * (size_t)ci;
+        } else {
+            b = inst_box + 6 * (size_t)(n.tri_base + (m & 0x1fu));
+        }
+        for (int k = 0; k < 3; ++k) { lo[s][k] = b[k]; hi[s][k] = b[3 + k]; }
+    }
+    float nlo[3], nhi[3];
+    tlas_quantise(n, lo, hi, used, nlo, nhi);
+    nodes[ni] = n;
+    for (int k = 0; k < 3; ++k) { node_box[6 * (size_t)ni + k] = nlo[k]; node_box[6 * (size_t)ni + 3 + k] = nhi[k]; }
+}
+
 // ------------------------------------------------------------ launchers ----
+void launch_tlas_refit(cudaStream_t st, CwNode* nodes, float* node_box, const float* inst_box, uint32_t begin,
+                       uint32_t end) {
+    if (end <= begin) return;
+    k_tlas_refit<<<(end - begin + 127) / 128, 128, 0, st>>>(nodes, node_box, inst_box, begin, end);
+}
 void launch_camera(const LaunchCfg& lc, cudaStream_t st, const DevView* views, uint32_t n_views,
                    uint64_t path_begin, uint32_t path_count, const Wavefront& wf, uint32_t max_segments) {
     uint32_t blocks = (path_count + lc.block_shade - 1) / lc.block_shade;
@@ -455,7 +534,10 @@ void launch_camera(const LaunchCfg& lc, cudaStream_t st, const DevView* views, u
 }
 void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, int q,
                    uint32_t seg, bool count_traversal) {
-    if (count_traversal)
+    if (sc.insts)
+        k_extend2<<<lc.grid_shade, 256, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit, wf.counters,
+                                                   wf.stats, seg);
+    else if (count_traversal)
         k_extend<true, 1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit,
                                                                            wf.counters, wf.stats, seg,
                                                                            lc.postpone_sp, lc.refill_min);
@@ -474,7 +556,9 @@ void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, cons
 }
 void launch_shadow(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, uint32_t seg,
                    float4* accum) {
-    if (lc.regcap)
+    if (sc.insts)
+        k_shadow2<<<lc.grid_shade, 256, 0, st>>>(sc, wf, seg, accum);
+    else if (lc.regcap)
         k_shadow<4><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp,
                                                                      lc.refill_min);
     else

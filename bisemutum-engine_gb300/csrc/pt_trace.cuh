@@ -260,6 +260,125 @@ __device__ __forceinline__ uint32_t trace_ray(const RayPre& r, float tmax, const
     return best_leaf;
 }
 
+// ---------------------------------------------------------- two-level ----
+// Row-major 3x4 transform of a point / direction, in a fixed operation order
+// (the oracle evaluates the same sums).
+__device__ __forceinline__ float4 xform_point(const float* m, float x, float y, float z, float w) {
+    return make_float4(__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], x), __fmul_rn(m[1], y)), __fmul_rn(m[2], z)), m[3]),
+                       __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[4], x), __fmul_rn(m[5], y)), __fmul_rn(m[6], z)), m[7]),
+                       __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[8], x), __fmul_rn(m[9], y)), __fmul_rn(m[10], z)), m[11]),
+                       w);
+}
+__device__ __forceinline__ float4 xform_dir(const float* m, float x, float y, float z, float w) {
+    return make_float4(__fadd_rn(__fadd_rn(__fmul_rn(m[0], x), __fmul_rn(m[1], y)), __fmul_rn(m[2], z)),
+                       __fadd_rn(__fadd_rn(__fmul_rn(m[4], x), __fmul_rn(m[5], y)), __fmul_rn(m[6], z)),
+                       __fadd_rn(__fadd_rn(__fmul_rn(m[8], x), __fmul_rn(m[9], y)), __fmul_rn(m[10], z)), w);
+}
+__device__ __forceinline__ void load_xform(const float* src, float* m) {
+    const float4* p = reinterpret_cast<const float4*>(src);
+    float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    m[0] = a.x; m[1] = a.y; m[2] = a.z; m[3] = a.w;
+    m[4] = b.x; m[5] = b.y; m[6] = b.z; m[7] = b.w;
+    m[8] = c.x; m[9] = c.y; m[10] = c.z; m[11] = c.w;
+}
+
+// Closest / any hit in a two-level scene (the reference's TLAS over per-mesh
+// BLASes, accel.cpp:104-132).  The TLAS's leaves are instances: entering one
+// pushes the rest of the current node's work and an exit marker, moves the
+// ray into the instance's space and traverses its BLAS on the same stack;
+// popping the marker restores the world ray.  Triangles are tested in object
+// space; ties resolve to the lower global primitive id (instance prim_base +
+// primitive).  `mat_tr` (per material: transparency of the any-hit rule, or
+// null when every material is opaque) and the world ray give the opacity
+// decision.  Returns the leaf triangle index within the instance's geometry
+// and the instance (TLAS leaf index) in `inst_out`.
+constexpr uint32_t kStackExit = 0xffffffffu;
+template <bool kAnyHit>
+__device__ __forceinline__ uint32_t trace_ray2(const RayPre& rw, float tmax, const CwNode* __restrict__ tlas,
+                                               const InstDev* __restrict__ insts, const float* __restrict__ mat_tr,
+                                               float& t_out, float& u_out, float& v_out, uint32_t& inst_out,
+                                               uint32_t oseed) {
+    float tbest = tmax, bu = 0.0f, bv = 0.0f;
+    uint32_t best_leaf = kMissPrim, best_prim = kMissPrim, best_inst = kMissPrim;
+    uint2 stack[kStackSize];
+    int sp = 0;
+    RayPre r = rw;
+    const CwNode* nodes = tlas;
+    const CwTri* tris = nullptr;
+    uint32_t inst = kMissPrim, prim_base = 0u, mat_override = kMissPrim;
+    bool zero = rw.dx == 0.0f && rw.dy == 0.0f && rw.dz == 0.0f;  // skipped as a miss (rt_gbuffer.hlsl:13-15)
+    uint2 G = make_uint2(0u, zero ? 0u : (0x80000000u | (1u << (7u ^ rw.oct_key))));
+    uint2 T = make_uint2(0u, 0u);
+    while (true) {
+        while (T.y != 0u) {
+            int bit = __ffs(T.y) - 1;
+            T.y &= T.y - 1u;
+            uint32_t ti = T.x + (uint32_t)bit;
+            if (inst == kMissPrim) {
+                // enter instance ti; this node's remaining work waits below an exit marker.
+                // The depth limits (TLAS <= kMaxTlasDepth, BLAS <= kMaxTraversalDepth) keep sp
+                // below kStackSize - kMaxTraversalDepth here; the guard only keeps writes in bounds.
+                if (sp > kStackSize - 3 - kMaxTraversalDepth) { T.y = 0u; G.y = 0u; sp = 0; break; }
+                if ((G.y & 0xff000000u) != 0u) stack[sp++] = G;
+                if (T.y != 0u) stack[sp++] = T;
+                stack[sp++] = make_uint2(kStackExit, 0u);
+                const InstDev* I = insts + ti;
+                float m[12];
+                load_xform(I->w2o, m);
+                r = make_ray(xform_point(m, rw.ox, rw.oy, rw.oz, rw.tmin), xform_dir(m, rw.dx, rw.dy, rw.dz, 0.0f));
+                nodes = I->nodes;
+                tris = I->tris;
+                prim_base = I->prim_base;
+                mat_override = I->material;
+                inst = ti;
+                G = make_uint2(0u, 0x80000000u | (1u << (7u ^ r.oct_key)));
+                T = make_uint2(0u, 0u);
+                break;
+            }
+            const float4* tp = reinterpret_cast<const float4*>(tris + ti);
+            float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            uint32_t prim = prim_base + __float_as_uint(a.w);
+            float t, u, v;
+            if (tri_test(r, a, b, c, tbest, prim, best_prim, t, u, v)) {
+                float tr = 0.0f;
+                if (mat_tr) tr = mat_tr[mat_override != kMissPrim ? mat_override : __float_as_uint(b.w)];
+                if (keep_hit(rw, tr, oseed)) {
+                    if (kAnyHit) { t_out = t; u_out = u; v_out = v; inst_out = inst; return ti; }
+                    tbest = t; best_leaf = ti; best_prim = prim; best_inst = inst; bu = u; bv = v;
+                }
+            }
+        }
+        if ((G.y & 0xff000000u) == 0u) {
+            if (T.y != 0u) continue;
+            if (sp == 0) break;
+            uint2 e = stack[--sp];
+            if (e.y == 0u) {  // exit marker: back to the world ray and the TLAS
+                r = rw;
+                nodes = tlas;
+                tris = nullptr;
+                inst = kMissPrim;
+                prim_base = 0u;
+                mat_override = kMissPrim;
+                G = make_uint2(0u, 0u);
+                continue;
+            }
+            if ((e.y & 0xff000000u) == 0u) { T = e; G = make_uint2(0u, 0u); continue; }  // instances of a leaf group
+            G = e;
+        }
+        uint32_t bit = 31u - (uint32_t)__clz(G.y & 0xff000000u);
+        G.y &= ~(1u << bit);
+        uint32_t slot = (bit - 24u) ^ r.oct_key;
+        uint32_t ni = G.x + (uint32_t)__popc(G.y & 0xffu & ((1u << slot) - 1u));
+        if ((G.y & 0xff000000u) != 0u && sp < kStackSize) stack[sp++] = G;
+        node_test(r, nodes, ni, tbest, G, T);
+    }
+    t_out = tbest;
+    u_out = bu;
+    v_out = bv;
+    inst_out = best_inst;
+    return best_leaf;
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

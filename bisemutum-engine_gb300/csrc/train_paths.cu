@@ -16,6 +16,7 @@
 #include "pt_device.h"
 #include "pt_sky.cuh"
 #include "pt_trace.cuh"
+#include "pt_scene.cuh"
 
 namespace bsm {
 
@@ -48,8 +49,8 @@ __global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView*
     for (uint32_t seg = 0; seg < segs; ++seg) {
         RayPre r = make_ray(make_float4(o.x, o.y, o.z, v.t_min), make_float4(d.x, d.y, d.z, v.ray_length));
         float t, hu, hv;
-        uint32_t leaf = trace_ray<false, false>(r, v.ray_length, sc.nodes, sc.tris, t, hu, hv, nullptr,
-                                                (uint32_t)g.state);
+        uint32_t inst;
+        uint32_t leaf = trace_scene<false>(sc, r, v.ray_length, t, hu, hv, inst, (uint32_t)g.state);
         if (leaf == kMissPrim) {
             if (nv > 0) {
                 V3 le = sky_eval(sc.sky, d);
@@ -59,12 +60,11 @@ __global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView*
             }
             break;
         }
-        const CwTri& tri = sc.tris[leaf];
-        V3 va = v3(tri.v0x, tri.v0y, tri.v0z), vb = v3(tri.v1x, tri.v1y, tri.v1z), vc = v3(tri.v2x, tri.v2y, tri.v2z);
-        V3 N = normalize(cross(vb - va, vc - va));
+        V3 N, edge;
+        uint32_t mi;
+        hit_geometry(sc, leaf, inst, N, edge, mi);
         if (dot(N, d) > 0.0f) N = -N;
         V3 P = o + d * t;
-        uint32_t mi = tri.material < sc.num_materials ? tri.material : 0u;
         float4 m0 = sc.materials[2 * mi], m1 = sc.materials[2 * mi + 1];
         Surface surf;
         surf.base_color = v3(m0.x, m0.y, m0.z);
@@ -92,8 +92,8 @@ __global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView*
             if (max_comp(c) > 0.0f) {
                 RayPre sr = make_ray(make_float4(org.x, org.y, org.z, v.t_min), make_float4(L.x, L.y, L.z, v.ray_length));
                 float a, b2, c2;
-                if (trace_ray<true, false>(sr, v.ray_length, sc.nodes, sc.tris, a, b2, c2, nullptr,
-                                           (uint32_t)g.state) == kMissPrim)
+                uint32_t si;
+                if (trace_scene<true>(sc, sr, v.ray_length, a, b2, c2, si, (uint32_t)g.state) == kMissPrim)
                     contrib[k] = contrib[k] + c;
             }
         }
@@ -108,9 +108,9 @@ __global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView*
                     V3 c = thr * le * f * ((pl * pl) / (pl * pl + pb * pb) / pl);
                     RayPre sr = make_ray(make_float4(org.x, org.y, org.z, v.t_min), make_float4(L.x, L.y, L.z, v.ray_length));
                     float a, b2, c2;
+                    uint32_t si;
                     if (max_comp(c) > 0.0f &&
-                        trace_ray<true, false>(sr, v.ray_length, sc.nodes, sc.tris, a, b2, c2, nullptr,
-                                               (uint32_t)g.state) == kMissPrim)
+                        trace_scene<true>(sc, sr, v.ray_length, a, b2, c2, si, (uint32_t)g.state) == kMissPrim)
                         contrib[k] = contrib[k] + c;
                 }
             }

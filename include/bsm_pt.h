@@ -465,6 +465,60 @@ BSM_API bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, const 
                                      const bsm_cache_settings* cache_settings, const bsm_view_output* output,
                                      bsm_render_stats* stats, float* train_loss);
 
+/* ---- instancing: two-level scenes --------------------------------------- */
+
+/* An object-space mesh with its own BVH (the reference's per-mesh BLAS,
+ * accel.cpp:11-87).  Material ids index the materials of the scenes that
+ * instance it. */
+typedef struct bsm_geometry_desc {
+    uint32_t num_vertices;
+    const float* positions;       /* 3 * num_vertices, object space */
+    uint32_t num_triangles;
+    const uint32_t* indices;      /* 3 * num_triangles, or NULL for a soup */
+    const uint32_t* material_ids; /* num_triangles, or NULL (all 0) */
+} bsm_geometry_desc;
+
+BSM_API bsm_status bsm_geometry_create(bsm_context* ctx, const bsm_geometry_desc* desc, const bsm_bvh_opts* opts,
+                                       uint32_t* geometry_id);
+/* Fails with BSM_ERR_BAD_STATE while a scene instances the geometry. */
+BSM_API bsm_status bsm_geometry_release(bsm_context* ctx, uint32_t geometry_id);
+
+/* One drawable of a two-level scene (the reference's TLAS instance,
+ * accel.cpp:104-132). */
+typedef struct bsm_instance {
+    uint32_t geometry_id;
+    uint32_t material_id;     /* material of every triangle, or 0xffffffff: the geometry's ids */
+    float transform[12];      /* object to world, row-major 3x4 (rows of Transform::matrix()) */
+} bsm_instance;
+
+typedef struct bsm_instanced_scene_desc {
+    uint32_t num_instances;
+    const bsm_instance* instances;
+    uint32_t num_materials;
+    const bsm_material* materials;
+    uint32_t num_dir_lights;
+    const bsm_dir_light* dir_lights;
+    bsm_sky sky;
+} bsm_instanced_scene_desc;
+
+/* Creates a scene over instances of geometries: a TLAS (the same compressed
+ * 8-wide BVH, one instance per leaf) over the instances' world boxes; rays
+ * enter an instance's BLAS in its object space.  The scene renders and
+ * traces like any other (bsm_render*, bsm_trace_*, the server, the cache);
+ * primitive ids are global: the sum of the earlier instances' triangle
+ * counts plus the triangle's index in its geometry.  bsm_scene_build_bvh on
+ * it rebuilds the TLAS from the current transforms. */
+BSM_API bsm_status bsm_scene_create_instanced(bsm_context* ctx, const bsm_instanced_scene_desc* desc,
+                                              uint32_t* scene_id);
+/* New object-to-world transforms (12 floats per instance, in creation order)
+ * and a refit of the TLAS on the GPU: the world boxes change, the tree's
+ * topology stays (the reference rebuilds its TLAS every frame,
+ * accel.cpp:139-158; a refit keeps the per-frame cost to one small kernel per
+ * TLAS level).  The scene bounds used for ray offsets stay those of creation.
+ * Synchronous. */
+BSM_API bsm_status bsm_scene_update_instances(bsm_context* ctx, uint32_t scene_id, const float* transforms,
+                                              uint32_t num_instances);
+
 /* ---- the reference's on-disk formats ----------------------------------- */
 
 /* SubmeshDesc (graphics/mesh.hpp:16-22); topology 3 = triangle_list (rhi/pipeline.hpp:34-43). */

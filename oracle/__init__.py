@@ -55,6 +55,11 @@ def lib() -> C.CDLL:
         L.orc_primary.argtypes = [vp, vp, f32, f32, f32, f32, u64, u32, vp, vp, vp, i32]
         L.orc_primary.restype = i32
         L.orc_gbuffer_pack.argtypes = [vp, u32, vp]
+        L.orc_geometry_create.argtypes = [vp, u32, vp, u32, vp, C.POINTER(vp)]
+        L.orc_geometry_create.restype = i32
+        L.orc_scene_create_instanced.argtypes = [vp, u32, vp, vp, vp, u32, vp, u32, vp, u32, u32, vp, u32, u32, vp,
+                                                 C.POINTER(vp)]
+        L.orc_scene_create_instanced.restype = i32
         L.orc_scene_bvh_nodes.argtypes = [vp]
         L.orc_scene_bvh_nodes.restype = u32
         _lib = L
@@ -97,6 +102,9 @@ class OracleScene:
     def __init__(self, scene):
         L = lib()
         self._L = L
+        if hasattr(scene, "geometries"):   # a two-level scene
+            self._init_instanced(scene)
+            return
         pos = _f32(scene.positions)
         idx = None if scene.indices is None else np.ascontiguousarray(scene.indices, np.uint32)
         mids = np.ascontiguousarray(scene.material_ids, np.uint32)
@@ -114,10 +122,44 @@ class OracleScene:
             raise RuntimeError("orc_scene_create failed")
         self.h = h
 
+    def _init_instanced(self, scene):
+        L = self._L
+        self._geoms = []
+        for g in scene.geometries:
+            pos = _f32(g.positions)
+            idx = None if g.indices is None else np.ascontiguousarray(g.indices, np.uint32)
+            mids = None if g.material_ids is None else np.ascontiguousarray(g.material_ids, np.uint32)
+            h = C.c_void_p()
+            nt = idx.shape[0] if idx is not None else pos.shape[0] // 3
+            if L.orc_geometry_create(pos.ctypes.data, pos.shape[0], None if idx is None else idx.ctypes.data, nt,
+                                     None if mids is None else mids.ctypes.data, C.byref(h)) != 0:
+                raise RuntimeError("orc_geometry_create failed")
+            self._geoms.append(h)
+        garr = (C.c_void_p * len(self._geoms))(*[g.value for g in self._geoms])
+        ig = np.ascontiguousarray(scene.inst_geometry, np.uint32)
+        im = np.ascontiguousarray(scene.inst_material, np.uint32)
+        ix = _f32(scene.inst_transform).reshape(-1, 12)
+        mats = material_rows(scene.materials)
+        lights = _f32(scene.lights).reshape(-1, 6)
+        color = _f32(scene.sky_color)
+        tex = None if scene.sky_texels is None else np.ascontiguousarray(scene.sky_texels, np.uint16)
+        h = C.c_void_p()
+        st = L.orc_scene_create_instanced(garr, len(self._geoms), ig.ctypes.data, im.ctypes.data, ix.ctypes.data,
+                                          ig.shape[0], mats.ctypes.data, mats.shape[0], lights.ctypes.data,
+                                          lights.shape[0], scene.sky_kind, color.ctypes.data,
+                                          0 if tex is None else tex.shape[1], 0 if tex is None else tex.shape[0],
+                                          None if tex is None else tex.ctypes.data, C.byref(h))
+        if st != 0:
+            raise RuntimeError("orc_scene_create_instanced failed")
+        self.h = h
+
     def __del__(self):
         if getattr(self, "h", None):
             self._L.orc_scene_destroy(self.h)
             self.h = None
+        for g in getattr(self, "_geoms", []):
+            self._L.orc_scene_destroy(g)
+        self._geoms = []
 
     def trace(self, rays: np.ndarray, any_hit: bool = False, threads: int = 0, counts: bool = False):
         rays = _f32(rays).reshape(-1, 8)

@@ -252,6 +252,16 @@ struct Scene {
     std::vector<uint16_t> texels;
     std::vector<float> cmarg, ccond, ptab;
     float extent = 1.0f, offset = 0.0f;
+    // two-level scenes: instances of geometries (each a Scene holding tris + BVH only)
+    struct Inst {
+        const struct Scene* geo;
+        uint32_t material;          // every triangle's material, or UINT32_MAX
+        float o2w[12], w2o[12];     // row-major 3x4
+        uint32_t prim_base;
+    };
+    std::vector<Inst> inst;
+    std::vector<float> trm;         // per material transparency (two-level scenes)
+    float glo[3], ghi[3];           // a geometry's bounds over all its vertices
 };
 
 // binned SAH binary BVH (16 bins, leaves of up to 4 triangles)
@@ -371,7 +381,8 @@ static Ray make_ray(F3 o, float tmin, F3 d, float tmax, uint32_t oseed = 0) {
     return r;
 }
 // Woop, Benthin, Wald 2013 watertight test (fp32, double fallback on zero edges)
-static bool tri_hit(const Ray& r, const Tri& t, float tbest, uint32_t best_prim, float& to, float& uo, float& vo) {
+static bool tri_hit(const Ray& r, const Tri& t, float tbest, uint32_t best_prim, float& to, float& uo, float& vo,
+                    uint32_t prim_base = 0) {
     F3 A = sub(t.a, r.o), B = sub(t.b, r.o), C = sub(t.c, r.o);
     float Akx = comp(A, r.kx), Aky = comp(A, r.ky), Akz = comp(A, r.kz);
     float Bkx = comp(B, r.kx), Bky = comp(B, r.ky), Bkz = comp(B, r.kz);
@@ -393,7 +404,7 @@ static bool tri_hit(const Ray& r, const Tri& t, float tbest, uint32_t best_prim,
     float rcp = 1.0f / det;
     float tt = T * rcp;
     if (!(tt > r.tmin)) return false;
-    if (!(tt < tbest || (tt == tbest && t.prim < best_prim))) return false;
+    if (!(tt < tbest || (tt == tbest && prim_base + t.prim < best_prim))) return false;
     to = tt; uo = U * rcp; vo = V * rcp;
     return true;
 }
@@ -431,28 +442,32 @@ static float opacity_random(const Ray& r) {
 // transparency tr is ignored when the ray's uniform is below tr.
 static bool keep_hit(const Ray& r, float tr) { return tr == 0.0f || !(opacity_random(r) < tr); }
 
-static uint32_t trace(const Scene& S, const Ray& r, bool any, float& to, float& uo, float& vo, Counts* cnt) {
-    float tbest = r.tmax;
-    uint32_t best = UINT32_MAX, best_prim = UINT32_MAX;
-    float bu = 0, bv = 0;
+// Closest / any hit in one BVH.  `r` is the ray in the BVH's space, `rw` the
+// world ray (opacity decisions); `prim_base` makes primitive ids global;
+// `trm` (two-level scenes) gives the transparency per effective material,
+// otherwise the triangle's own.  Updates the best hit; true when any-hit found one.
+struct Best { float t; uint32_t leaf, prim, inst; float u, v; };
+static bool trace_bvh(const Scene& G, const Ray& r, const Ray& rw, bool any, uint32_t prim_base, uint32_t mat_override,
+                      const float* trm, uint32_t inst, Best& b, Counts* cnt) {
     uint32_t stack[128];
     int sp = 0;
     // a zero direction is skipped as a miss (rt_gbuffer.hlsl:13-15)
-    if (!(r.d.x == 0.0f && r.d.y == 0.0f && r.d.z == 0.0f)) stack[sp++] = 0;
+    if (!(rw.d.x == 0.0f && rw.d.y == 0.0f && rw.d.z == 0.0f)) stack[sp++] = 0;
     while (sp) {
         uint32_t ni = stack[--sp];
-        const BNode& n = S.nodes[ni];
+        const BNode& n = G.nodes[ni];
         if (cnt) cnt->nodes++;
-        if (!box_hit(r, n, tbest)) continue;
+        if (!box_hit(r, n, b.t)) continue;
         if (n.count) {
             for (uint32_t i = 0; i < n.count; ++i) {
-                const Tri& t = S.tris[n.left_or_first + i];
+                const Tri& t = G.tris[n.left_or_first + i];
                 if (cnt) cnt->tris++;
                 float tt, u, v;
-                if (tri_hit(r, t, tbest, best_prim, tt, u, v) && keep_hit(r, t.tr)) {
-                    tbest = tt; best = n.left_or_first + i; best_prim = t.prim; bu = u; bv = v;
-                    if (any) { to = tt; uo = u; vo = v; return best; }
-                }
+                if (!tri_hit(r, t, b.t, b.prim, tt, u, v, prim_base)) continue;
+                float tr = trm ? trm[mat_override != UINT32_MAX ? mat_override : t.mat] : t.tr;
+                if (!keep_hit(rw, tr)) continue;
+                b.t = tt; b.leaf = n.left_or_first + i; b.prim = prim_base + t.prim; b.inst = inst; b.u = u; b.v = v;
+                if (any) return true;
             }
         } else {
             uint32_t l = ni + 1, rr = n.left_or_first;
@@ -461,8 +476,59 @@ static uint32_t trace(const Scene& S, const Ray& r, bool any, float& to, float& 
             if (neg) { stack[sp++] = l; stack[sp++] = rr; } else { stack[sp++] = rr; stack[sp++] = l; }
         }
     }
-    to = tbest; uo = bu; vo = bv;
-    return best;
+    return false;
+}
+
+// Row-major 3x4 transforms in the GPU's operation order.
+static F3 xf_point(const float* m, F3 p) {
+    return f3(((m[0] * p.x + m[1] * p.y) + m[2] * p.z) + m[3], ((m[4] * p.x + m[5] * p.y) + m[6] * p.z) + m[7],
+              ((m[8] * p.x + m[9] * p.y) + m[10] * p.z) + m[11]);
+}
+static F3 xf_dir(const float* m, F3 d) {
+    return f3((m[0] * d.x + m[1] * d.y) + m[2] * d.z, (m[4] * d.x + m[5] * d.y) + m[6] * d.z,
+              (m[8] * d.x + m[9] * d.y) + m[10] * d.z);
+}
+static F3 xf_normal(const float* m, F3 n) {  // transpose of the linear part
+    return f3((m[0] * n.x + m[4] * n.y) + m[8] * n.z, (m[1] * n.x + m[5] * n.y) + m[9] * n.z,
+              (m[2] * n.x + m[6] * n.y) + m[10] * n.z);
+}
+
+// Closest / any hit of a world ray.  Two-level scenes test every instance (no
+// TLAS: the checker does not depend on one) with the ray moved into the
+// instance's space; ties resolve to the lower global primitive id.  Returns the
+// leaf index (in the instance's geometry for two-level scenes), inst_out the instance.
+static uint32_t trace(const Scene& S, const Ray& r, bool any, float& to, float& uo, float& vo, Counts* cnt,
+                      uint32_t* inst_out = nullptr) {
+    Best b{r.tmax, UINT32_MAX, UINT32_MAX, UINT32_MAX, 0.0f, 0.0f};
+    if (S.inst.empty()) {
+        trace_bvh(S, r, r, any, 0, UINT32_MAX, nullptr, UINT32_MAX, b, cnt);
+    } else {
+        for (uint32_t i = 0; i < S.inst.size(); ++i) {
+            const Scene::Inst& I = S.inst[i];
+            Ray ro = make_ray(xf_point(I.w2o, r.o), r.tmin, xf_dir(I.w2o, r.d), r.tmax, r.oseed);
+            if (trace_bvh(*I.geo, ro, r, any, I.prim_base, I.material, S.trm.empty() ? nullptr : S.trm.data(), i, b,
+                          cnt))
+                break;
+        }
+    }
+    to = b.t; uo = b.u; vo = b.v;
+    if (inst_out) *inst_out = b.inst;
+    return b.leaf;
+}
+
+// Geometric normal (world, unit, not faced), first edge (world) and material of a hit.
+static void hit_geom(const Scene& S, uint32_t leaf, uint32_t inst, F3& ng, F3& edge, uint32_t& mat) {
+    const Tri& T = inst == UINT32_MAX ? S.tris[leaf] : S.inst[inst].geo->tris[leaf];
+    ng = norm3(cross3(sub(T.b, T.a), sub(T.c, T.a)));
+    edge = sub(T.b, T.a);
+    mat = T.mat;
+    if (inst != UINT32_MAX) {
+        const Scene::Inst& I = S.inst[inst];
+        ng = norm3(xf_normal(I.w2o, ng));
+        edge = xf_dir(I.o2w, edge);
+        if (I.material != UINT32_MAX) mat = I.material;
+    }
+    if (mat >= S.nmat) mat = 0;
 }
 
 // ------------------------------------------------------------------ sky ----
@@ -634,7 +700,8 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                 // extend
                 Ray r = make_ray(q.o[i], q.tmin[i], q.d[i], q.tmax[i], (uint32_t)q.rng[i].state);
                 float t, u, v;
-                uint32_t hit = trace(S, r, false, t, u, v, nullptr);
+                uint32_t hinst;
+                uint32_t hit = trace(S, r, false, t, u, v, nullptr, &hinst);
                 F3 d = q.d[i], thr = q.thr[i];
                 float* a = acc + 3 * (size_t)(q.pix[i] - pix_begin);
                 if (hit == UINT32_MAX) {  // deferred_lighting_secondary.hlsl:23-29
@@ -650,12 +717,13 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                     continue;
                 }
                 // shade
-                const Tri& T = S.tris[hit];
-                F3 ng = norm3(cross3(sub(T.b, T.a), sub(T.c, T.a)));
+                F3 ng, edge;
+                uint32_t mat;
+                hit_geom(S, hit, hinst, ng, edge, mat);
                 if (dot3(ng, d) > 0.0f) ng = neg(ng);
                 F3 N = ng;
                 F3 P = add(q.o[i], muls(d, t));
-                const float* m = &S.mats[8 * (size_t)T.mat];
+                const float* m = &S.mats[8 * (size_t)mat];
                 Surf surf{f3(m[0], m[1], m[2]), f3(m[4], m[5], m[6]), f3(1, 1, 1), m[3], 1.5f};
                 Frm fr = make_frame(N);
                 F3 V = neg(d);
@@ -737,19 +805,11 @@ static int nthreads(int req) {
 
 using namespace orc;
 
-ORC_API int orc_scene_create(const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt, const uint32_t* mat_ids,
-                             const float* materials, uint32_t nm, const float* lights, uint32_t nl, uint32_t sky_kind,
-                             const float* sky_color, uint32_t sky_w, uint32_t sky_h, const uint16_t* sky_texels,
-                             void** out) {
-    if (!pos || !nt || !materials || !nm || !out || nl > 4) return -1;
-    Scene* S = new Scene();
+// Triangles and the binary BVH of a mesh (a scene's or a two-level geometry's).
+static void build_geometry(Scene* S, const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
+                           const uint32_t* mat_ids) {
     std::vector<BuildRef> refs(nt);
     std::vector<Tri> soup(nt);
-    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (uint32_t i = 0; i < nv; ++i)
-        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], pos[3 * i + k]); hi[k] = std::max(hi[k], pos[3 * i + k]); }
-    S->extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
-    S->offset = 2e-5f * S->extent;
     for (uint32_t t = 0; t < nt; ++t) {
         uint32_t v[3];
         for (int c = 0; c < 3; ++c) v[c] = idx ? idx[3 * t + c] : 3 * t + c;
@@ -759,6 +819,7 @@ ORC_API int orc_scene_create(const float* pos, uint32_t nv, const uint32_t* idx,
         T.c = f3(pos[3 * v[2]], pos[3 * v[2] + 1], pos[3 * v[2] + 2]);
         T.prim = t;
         T.mat = mat_ids ? mat_ids[t] : 0;
+        T.tr = 0.0f;
         BuildRef& R = refs[t];
         const F3 vs[3] = {T.a, T.b, T.c};
         for (int k = 0; k < 3; ++k) {
@@ -768,24 +829,32 @@ ORC_API int orc_scene_create(const float* pos, uint32_t nv, const uint32_t* idx,
         }
         R.t = t;
     }
+    (void)nv;
     S->nodes.reserve(2 * (size_t)nt);
     build_rec(*S, refs, 0, nt);
     S->tris.resize(nt);
     for (uint32_t i = 0; i < nt; ++i) S->tris[i] = soup[refs[i].t];
+}
+
+// Materials (7 floats each: base rgb, roughness, metallic, opacity, blend mode),
+// lights, sky and the ray offset of a scene with bounds lo / hi.
+static bool setup_shading(Scene* S, const float* materials, uint32_t nm, const float* lights, uint32_t nl,
+                          uint32_t sky_kind, const float* sky_color, uint32_t sky_w, uint32_t sky_h,
+                          const uint16_t* sky_texels, const float lo[3], const float hi[3]) {
+    S->extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
+    S->offset = 2e-5f * S->extent;
     S->nmat = nm;
     S->mats.resize(8 * (size_t)nm);
-    std::vector<float> trm(nm, 0.0f);
+    S->trm.assign(nm, 0.0f);
     for (uint32_t m = 0; m < nm; ++m) {
-        // base rgb, roughness, metallic, opacity, blend mode (0 opaque, 1 alpha test, 2 translucent)
         const float* M = materials + 7 * (size_t)m;
-        if (M[6] == 1.0f) trm[m] = M[5] < 0.01f ? 1.0f : 0.0f;   // ALPHA_TEST_OPACITY_THRESHOLD (utils.hlsl:38)
-        if (M[6] == 2.0f) trm[m] = 1.0f - M[5];
+        if (M[6] == 1.0f) S->trm[m] = M[5] < 0.01f ? 1.0f : 0.0f;   // ALPHA_TEST_OPACITY_THRESHOLD (utils.hlsl:38)
+        if (M[6] == 2.0f) S->trm[m] = 1.0f - M[5];
         float* o = &S->mats[8 * (size_t)m];
         o[0] = M[0]; o[1] = M[1]; o[2] = M[2]; o[3] = M[3];
         for (int k = 0; k < 3; ++k) o[4 + k] = 0.04f + (M[k] - 0.04f) * M[4];  // lerp(0.04, base, metallic)
         o[7] = M[4];
     }
-    for (Tri& T : S->tris) T.tr = T.mat < nm ? trm[T.mat] : 0.0f;
     S->nlights = nl;
     for (uint32_t l = 0; l < nl; ++l) {
         S->ldir[l] = norm3(f3(lights[6 * l], lights[6 * l + 1], lights[6 * l + 2]));
@@ -794,11 +863,131 @@ ORC_API int orc_scene_create(const float* pos, uint32_t nv, const uint32_t* idx,
     S->sky_kind = sky_kind;
     S->sky_color = f3(sky_color[0], sky_color[1], sky_color[2]);
     if (sky_kind == 1) {
-        if (!sky_texels || !sky_w || !sky_h) { delete S; return -1; }
+        if (!sky_texels || !sky_w || !sky_h) return false;
         S->sw = sky_w; S->sh = sky_h;
         S->texels.assign(sky_texels, sky_texels + (size_t)sky_w * sky_h * 4);
         build_sky(*S);
     }
+    return true;
+}
+
+ORC_API int orc_scene_create(const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt, const uint32_t* mat_ids,
+                             const float* materials, uint32_t nm, const float* lights, uint32_t nl, uint32_t sky_kind,
+                             const float* sky_color, uint32_t sky_w, uint32_t sky_h, const uint16_t* sky_texels,
+                             void** out) {
+    if (!pos || !nt || !materials || !nm || !out || nl > 4) return -1;
+    Scene* S = new Scene();
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = 0; i < nv; ++i)
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], pos[3 * i + k]); hi[k] = std::max(hi[k], pos[3 * i + k]); }
+    build_geometry(S, pos, nv, idx, nt, mat_ids);
+    if (!setup_shading(S, materials, nm, lights, nl, sky_kind, sky_color, sky_w, sky_h, sky_texels, lo, hi)) {
+        delete S;
+        return -1;
+    }
+    for (Tri& T : S->tris) T.tr = T.mat < nm ? S->trm[T.mat] : 0.0f;
+    S->trm.clear();  // single-level: the triangles carry their transparency
+    *out = S;
+    return 0;
+}
+
+// A geometry of two-level scenes: triangles and BVH in object space.
+ORC_API int orc_geometry_create(const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
+                                const uint32_t* mat_ids, void** out) {
+    if (!pos || !nt || !out) return -1;
+    Scene* G = new Scene();
+    for (int k = 0; k < 3; ++k) { G->glo[k] = INFINITY; G->ghi[k] = -INFINITY; }
+    for (uint32_t i = 0; i < nv; ++i)
+        for (int k = 0; k < 3; ++k) {
+            G->glo[k] = std::min(G->glo[k], pos[3 * i + k]);
+            G->ghi[k] = std::max(G->ghi[k], pos[3 * i + k]);
+        }
+    build_geometry(G, pos, nv, idx, nt, mat_ids);
+    *out = G;
+    return 0;
+}
+
+// World-to-object transform: the inverse of the row-major 3x4 object-to-world
+// transform in double (cofactors, first-row determinant), rounded to float.
+static bool invert_affine(const float* m, float* inv) {
+    double L00 = m[0], L01 = m[1], L02 = m[2], t0 = m[3];
+    double L10 = m[4], L11 = m[5], L12 = m[6], t1 = m[7];
+    double L20 = m[8], L21 = m[9], L22 = m[10], t2 = m[11];
+    double c00 = L11 * L22 - L12 * L21, c01 = L02 * L21 - L01 * L22, c02 = L01 * L12 - L02 * L11;
+    double c10 = L12 * L20 - L10 * L22, c11 = L00 * L22 - L02 * L20, c12 = L02 * L10 - L00 * L12;
+    double c20 = L10 * L21 - L11 * L20, c21 = L01 * L20 - L00 * L21, c22 = L00 * L11 - L01 * L10;
+    double det = L00 * c00 + L01 * c10 + L02 * c20;
+    if (!std::isfinite(det) || !(std::fabs(det) > 1e-30)) return false;
+    double r[9] = {c00 / det, c01 / det, c02 / det, c10 / det, c11 / det, c12 / det, c20 / det, c21 / det, c22 / det};
+    for (int i = 0; i < 3; ++i) {
+        inv[4 * i] = (float)r[3 * i];
+        inv[4 * i + 1] = (float)r[3 * i + 1];
+        inv[4 * i + 2] = (float)r[3 * i + 2];
+        inv[4 * i + 3] = (float)(-(r[3 * i] * t0 + r[3 * i + 1] * t1 + r[3 * i + 2] * t2));
+    }
+    return true;
+}
+
+// An instance's world box: the transformed corners of the geometry's box in
+// double, padded by 1e-5 of the coordinates' magnitude, rounded outward (the
+// scene bounds, hence the ray offset, come from these boxes).
+static void instance_world_box(const float* m, const float glo[3], const float ghi[3], float lo[3], float hi[3]) {
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < 8; ++c) {
+        double p[3] = {(c & 1) ? ghi[0] : glo[0], (c & 2) ? ghi[1] : glo[1], (c & 4) ? ghi[2] : glo[2]};
+        for (int k = 0; k < 3; ++k) {
+            double w = (double)m[4 * k] * p[0] + (double)m[4 * k + 1] * p[1] + (double)m[4 * k + 2] * p[2] +
+                       (double)m[4 * k + 3];
+            mn[k] = std::min(mn[k], w);
+            mx[k] = std::max(mx[k], w);
+        }
+    }
+    double mag = 0.0;
+    for (int k = 0; k < 3; ++k) mag = std::max(mag, std::max(std::fabs(mn[k]), std::fabs(mx[k])));
+    double pad = 1e-5 * mag + 1e-30;
+    for (int k = 0; k < 3; ++k) {
+        float l = (float)(mn[k] - pad), h = (float)(mx[k] + pad);
+        while ((double)l > mn[k] - pad) l = std::nextafter(l, -INFINITY);
+        while ((double)h < mx[k] + pad) h = std::nextafter(h, INFINITY);
+        lo[k] = l;
+        hi[k] = h;
+    }
+}
+
+// A two-level scene over geometries: instance i uses geometry inst_geo[i],
+// material inst_mat[i] (UINT32_MAX: the geometry's ids) and the object-to-world
+// transform inst_xf[12 i .. 12 i + 11].
+ORC_API int orc_scene_create_instanced(void* const* geoms, uint32_t ng, const uint32_t* inst_geo,
+                                       const uint32_t* inst_mat, const float* inst_xf, uint32_t ni,
+                                       const float* materials, uint32_t nm, const float* lights, uint32_t nl,
+                                       uint32_t sky_kind, const float* sky_color, uint32_t sky_w, uint32_t sky_h,
+                                       const uint16_t* sky_texels, void** out) {
+    if (!geoms || !ni || !materials || !nm || !out || nl > 4) return -1;
+    Scene* S = new Scene();
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    uint32_t prim_base = 0;
+    for (uint32_t i = 0; i < ni; ++i) {
+        if (inst_geo[i] >= ng) { delete S; return -1; }
+        const Scene* G = (const Scene*)geoms[inst_geo[i]];
+        Scene::Inst I;
+        I.geo = G;
+        I.material = inst_mat[i];
+        std::memcpy(I.o2w, inst_xf + 12 * (size_t)i, sizeof(I.o2w));
+        if (!invert_affine(I.o2w, I.w2o)) { delete S; return -1; }
+        I.prim_base = prim_base;
+        prim_base += (uint32_t)G->tris.size();
+        float bl[3], bh[3];
+        instance_world_box(I.o2w, G->glo, G->ghi, bl, bh);
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], bl[k]); hi[k] = std::max(hi[k], bh[k]); }
+        S->inst.push_back(I);
+    }
+    if (!setup_shading(S, materials, nm, lights, nl, sky_kind, sky_color, sky_w, sky_h, sky_texels, lo, hi)) {
+        delete S;
+        return -1;
+    }
+    bool any = false;
+    for (float t : S->trm) any = any || t != 0.0f;
+    if (!any) S->trm.clear();
     *out = S;
     return 0;
 }
@@ -821,10 +1010,12 @@ ORC_API int orc_trace(void* sp, const float* rays, uint32_t n, uint32_t* hits, i
                 Ray r = make_ray(f3(R[0], R[1], R[2]), R[3], f3(R[4], R[5], R[6]), R[7]);
                 float t, u, v;
                 Counts c;
-                uint32_t h = trace(S, r, any != 0, t, u, v, counts ? &c : nullptr);
+                uint32_t hi;
+                uint32_t h = trace(S, r, any != 0, t, u, v, counts ? &c : nullptr, &hi);
                 uint32_t* H = hits + 4 * (size_t)i;
                 std::memcpy(&H[0], &t, 4);
-                H[1] = h == UINT32_MAX ? UINT32_MAX : S.tris[h].prim;
+                H[1] = h == UINT32_MAX ? UINT32_MAX
+                                       : (hi == UINT32_MAX ? S.tris[h].prim : S.inst[hi].prim_base + S.inst[hi].geo->tris[h].prim);
                 std::memcpy(&H[2], &u, 4);
                 std::memcpy(&H[3], &v, 4);
                 if (counts) { counts[2 * (size_t)i] = (uint32_t)c.nodes; counts[2 * (size_t)i + 1] = (uint32_t)c.tris; }
@@ -959,15 +1150,16 @@ ORC_API int orc_primary(void* sp, const float* camera, float ray_length, float t
                 Pcg pg = pcg_seed(sample_initstate(seed, sample_offset), (uint64_t)p);
                 Ray r = make_ray(K.pos, t_min, dw, ray_length, (uint32_t)pg.state);
                 float t, u, v;
-                uint32_t h = trace(S, r, false, t, u, v, nullptr);
+                uint32_t hi;
+                uint32_t h = trace(S, r, false, t, u, v, nullptr, &hi);
                 float g[16] = {0};
                 float z = 0.0f, hp[4] = {dw.x, dw.y, dw.z, -1.0f};
                 if (h != UINT32_MAX) {
-                    const Tri& T = S.tris[h];
-                    F3 ng = norm3(cross3(sub(T.b, T.a), sub(T.c, T.a)));
+                    F3 ng, edge;
+                    uint32_t mi;
+                    hit_geom(S, h, hi, ng, edge, mi);
                     if (dot3(ng, dw) > 0.0f) ng = neg(ng);
-                    F3 tan = norm3(sub(T.b, T.a));
-                    uint32_t mi = T.mat < S.nmat ? T.mat : 0;
+                    F3 tan = norm3(edge);
                     const float* m = S.mats.data() + 8 * (size_t)mi;
                     gbuffer_pack(ng, tan, f3(m[0], m[1], m[2]), f3(m[4], m[5], m[6]), m[3], g);
                     F3 P = add(K.pos, muls(dw, t));
