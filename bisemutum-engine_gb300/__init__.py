@@ -29,7 +29,7 @@ STATUS_NAMES = {
     -9: "BSM_ERR_DEVICE_CHECK", -10: "BSM_ERR_ADMISSION",
 }
 BSM_HOST, BSM_DEVICE = 0, 1
-BSM_SKY_CONSTANT, BSM_SKY_EQUIRECT = 0, 1
+BSM_SKY_CONSTANT, BSM_SKY_EQUIRECT, BSM_SKY_CUBEMAP = 0, 1, 2
 BSM_SCENE_ROOM, BSM_SCENE_TERRAIN = 0, 1
 BSM_PT_JITTER, BSM_PT_NO_SUN_NEE, BSM_PT_NO_SKY_NEE, BSM_PT_STAGE_TIMING, BSM_PT_NO_GRAPH = 1, 2, 4, 8, 16
 BSM_PT_COUNT_TRAVERSAL = 32
@@ -57,7 +57,18 @@ class DirLight(C.Structure):
 
 class Sky(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("color", C.c_float * 3), ("width", C.c_uint32), ("height", C.c_uint32),
-                ("rgba16f", C.POINTER(C.c_uint16))]
+                ("rgba16f", C.POINTER(C.c_uint16)), ("transform", C.c_float * 9)]
+
+
+class PointLight(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("emission", C.c_float * 3), ("range", C.c_float),
+                ("direction", C.c_float * 3), ("cos_inner", C.c_float), ("cos_outer", C.c_float)]
+
+
+class RectLight(C.Structure):
+    _fields_ = [("center", C.c_float * 3), ("axis_x", C.c_float * 3), ("axis_y", C.c_float * 3),
+                ("width", C.c_float), ("height", C.c_float), ("emission", C.c_float * 3),
+                ("two_sided", C.c_uint32)]
 
 
 class SceneDesc(C.Structure):
@@ -65,7 +76,9 @@ class SceneDesc(C.Structure):
                 ("num_triangles", C.c_uint32), ("indices", C.POINTER(C.c_uint32)),
                 ("material_ids", C.POINTER(C.c_uint32)), ("num_materials", C.c_uint32),
                 ("materials", C.POINTER(Material)), ("num_dir_lights", C.c_uint32),
-                ("dir_lights", C.POINTER(DirLight)), ("sky", Sky)]
+                ("dir_lights", C.POINTER(DirLight)), ("sky", Sky), ("num_point_lights", C.c_uint32),
+                ("point_lights", C.POINTER(PointLight)), ("num_rect_lights", C.c_uint32),
+                ("rect_lights", C.POINTER(RectLight))]
 
 
 class BvhOpts(C.Structure):
@@ -175,7 +188,9 @@ class Instance(C.Structure):
 class InstancedSceneDesc(C.Structure):
     _fields_ = [("num_instances", C.c_uint32), ("instances", C.POINTER(Instance)), ("num_materials", C.c_uint32),
                 ("materials", C.POINTER(Material)), ("num_dir_lights", C.c_uint32),
-                ("dir_lights", C.POINTER(DirLight)), ("sky", Sky)]
+                ("dir_lights", C.POINTER(DirLight)), ("sky", Sky), ("num_point_lights", C.c_uint32),
+                ("point_lights", C.POINTER(PointLight)), ("num_rect_lights", C.c_uint32),
+                ("rect_lights", C.POINTER(RectLight))]
 
 
 class Submesh(C.Structure):
@@ -315,9 +330,12 @@ class SceneData:
     lights: np.ndarray                # (L, 6) float32: direction to light, emission
     sky_kind: int = BSM_SKY_CONSTANT
     sky_color: tuple = (0.5, 0.5, 0.5)
-    sky_texels: np.ndarray | None = None  # (H, W, 4) uint16 IEEE half
+    sky_texels: np.ndarray | None = None  # (H, W, 4) uint16 IEEE half, or (6, S, S, 4) for a cubemap
     camera: Camera | None = None
     _keep: list = field(default_factory=list, repr=False)
+    point_lights: np.ndarray | None = None  # (P, 12): position, emission, range, direction to light, cos_inner, cos_outer
+    rect_lights: np.ndarray | None = None   # (R, 15): centre, axis x, axis y, width, height, emission, two_sided
+    sky_transform: np.ndarray | None = None  # (9,) cubemap lookup rotation, row-major
 
     @property
     def num_triangles(self) -> int:
@@ -348,17 +366,53 @@ class SceneData:
         d.materials = mats
         d.num_dir_lights = len(self.lights)
         d.dir_lights = lights
-        d.sky.kind = self.sky_kind
-        d.sky.color[:] = list(self.sky_color)
-        if self.sky_texels is not None:
-            tex = np.ascontiguousarray(self.sky_texels, np.uint16)
-            d.sky.width = tex.shape[1]
-            d.sky.height = tex.shape[0]
-            d.sky.rgba16f = _ptr(tex, C.c_uint16)
-            self._keep = [pos, idx, mids, mats, lights, tex]
-        else:
-            self._keep = [pos, idx, mids, mats, lights]
+        keep = [pos, idx, mids, mats, lights]
+        keep += _fill_sky_and_lights(d, self)
+        self._keep = keep
         return d
+
+
+def _fill_sky_and_lights(d, scene) -> list:
+    """Sets the sky and the point / rect lights of a scene descriptor; returns the arrays to keep alive."""
+    keep = []
+    d.sky.kind = scene.sky_kind
+    d.sky.color[:] = list(scene.sky_color)
+    if scene.sky_texels is not None:
+        tex = np.ascontiguousarray(scene.sky_texels, np.uint16)
+        if scene.sky_kind == BSM_SKY_CUBEMAP:
+            d.sky.width, d.sky.height = tex.shape[2], tex.shape[1]
+        else:
+            d.sky.width, d.sky.height = tex.shape[1], tex.shape[0]
+        d.sky.rgba16f = _ptr(tex, C.c_uint16)
+        keep.append(tex)
+    if getattr(scene, "sky_transform", None) is not None:
+        d.sky.transform[:] = [float(x) for x in np.asarray(scene.sky_transform).ravel()[:9]]
+    pl = getattr(scene, "point_lights", None)
+    if pl is not None and len(pl):
+        pl = np.asarray(pl, np.float32).reshape(-1, 12)
+        arr = (PointLight * len(pl))()
+        for i, r in enumerate(pl):
+            arr[i].position[:] = [float(x) for x in r[0:3]]
+            arr[i].emission[:] = [float(x) for x in r[3:6]]
+            arr[i].range = float(r[6])
+            arr[i].direction[:] = [float(x) for x in r[7:10]]
+            arr[i].cos_inner, arr[i].cos_outer = float(r[10]), float(r[11])
+        d.num_point_lights, d.point_lights = len(pl), arr
+        keep.append(arr)
+    rl = getattr(scene, "rect_lights", None)
+    if rl is not None and len(rl):
+        rl = np.asarray(rl, np.float32).reshape(-1, 15)
+        arr = (RectLight * len(rl))()
+        for i, r in enumerate(rl):
+            arr[i].center[:] = [float(x) for x in r[0:3]]
+            arr[i].axis_x[:] = [float(x) for x in r[3:6]]
+            arr[i].axis_y[:] = [float(x) for x in r[6:9]]
+            arr[i].width, arr[i].height = float(r[9]), float(r[10])
+            arr[i].emission[:] = [float(x) for x in r[11:14]]
+            arr[i].two_sided = int(r[14])
+        d.num_rect_lights, d.rect_lights = len(rl), arr
+        keep.append(arr)
+    return keep
 
 
 def _materials_array(materials) -> "C.Array":
@@ -397,6 +451,9 @@ class InstancedSceneData:
     sky_color: tuple = (0.5, 0.5, 0.5)
     sky_texels: np.ndarray | None = None
     camera: Camera | None = None
+    point_lights: np.ndarray | None = None
+    rect_lights: np.ndarray | None = None
+    sky_transform: np.ndarray | None = None
 
     @property
     def num_triangles(self) -> int:
@@ -420,7 +477,8 @@ class InstancedSceneData:
                 mids.append(np.zeros(t, np.uint32) if G.material_ids is None else np.asarray(G.material_ids, np.uint32))
             base += len(p)
         return SceneData(np.concatenate(pos), np.concatenate(idx), np.concatenate(mids), self.materials, self.lights,
-                         self.sky_kind, self.sky_color, self.sky_texels, self.camera)
+                         self.sky_kind, self.sky_color, self.sky_texels, self.camera, point_lights=self.point_lights,
+                         rect_lights=self.rect_lights, sky_transform=self.sky_transform)
 
 
 def _uv_sphere(n_lat: int, n_lon: int):
@@ -532,7 +590,12 @@ def _scene_from_desc(d: SceneDesc, cam: Camera | None) -> SceneData:
     tex = None
     if d.sky.kind == BSM_SKY_EQUIRECT:
         tex = np.ctypeslib.as_array(d.sky.rgba16f, (d.sky.height, d.sky.width, 4)).copy()
-    return SceneData(pos, idx, mids, mats, lights, d.sky.kind, tuple(d.sky.color), tex, cam)
+    pts = np.array([[*p.position, *p.emission, p.range, *p.direction, p.cos_inner, p.cos_outer]
+                    for p in (d.point_lights[i] for i in range(d.num_point_lights))], np.float32).reshape(-1, 12)
+    rects = np.array([[*r.center, *r.axis_x, *r.axis_y, r.width, r.height, *r.emission, r.two_sided]
+                      for r in (d.rect_lights[i] for i in range(d.num_rect_lights))], np.float32).reshape(-1, 15)
+    return SceneData(pos, idx, mids, mats, lights, d.sky.kind, tuple(d.sky.color), tex, cam, point_lights=pts,
+                     rect_lights=rects)
 
 
 _MESH_ARRAYS = [("positions", "num_vertices", 3, np.float32), ("normals", "num_normals", 3, np.float32),
@@ -744,13 +807,7 @@ class Context:
         d.materials = mats
         d.num_dir_lights = len(scene.lights)
         d.dir_lights = lights
-        d.sky.kind = scene.sky_kind
-        d.sky.color[:] = list(scene.sky_color)
-        tex = None
-        if scene.sky_texels is not None:
-            tex = np.ascontiguousarray(scene.sky_texels, np.uint16)
-            d.sky.width, d.sky.height = tex.shape[1], tex.shape[0]
-            d.sky.rgba16f = _ptr(tex, C.c_uint16)
+        keep = _fill_sky_and_lights(d, scene)
         sid = C.c_uint32()
         st = self._L.bsm_scene_create_instanced(self.h, C.byref(d), C.byref(sid))
         if st != BSM_OK:

@@ -392,16 +392,100 @@ void free_scene_buffers(bsm_context* ctx, Scene& sc) {
 }
 
 // Materials, lights, sky and the scene bounds of a scene (both kinds).
+// IEEE half of a float, round to nearest even (for resampled sky texels).
+uint16_t float_to_half(float f) {
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    uint32_t sign = (x >> 16) & 0x8000u;
+    uint32_t exp = (x >> 23) & 0xffu;
+    uint32_t man = x & 0x7fffffu;
+    if (exp == 0xffu) return (uint16_t)(sign | 0x7c00u | (man ? 0x200u : 0u));
+    int e = (int)exp - 127 + 15;
+    if (e >= 31) return (uint16_t)(sign | 0x7c00u);
+    if (e <= 0) {  // subnormal half
+        if (e < -10) return (uint16_t)sign;
+        man |= 0x800000u;
+        uint32_t shift = (uint32_t)(14 - e);
+        uint32_t h = man >> shift;
+        uint32_t rem = man & ((1u << shift) - 1u), half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (h & 1u))) ++h;
+        return (uint16_t)(sign | h);
+    }
+    uint32_t h = ((uint32_t)e << 10) | (man >> 13);
+    uint32_t rem = man & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;  // may carry into the exponent: still correct
+    return (uint16_t)(sign | h);
+}
+
+// A cubemap sky (6 faces +X -X +Y -Y +Z -Z, RGBA16F) resampled to the equirect
+// layout of the sky sampler (4 size x 2 size): per texel centre the direction,
+// rotated by the sky transform, picks a face by the standard cube face table
+// (major axis; +X: (-z, -y), -X: (z, -y), +Y: (x, z), -Y: (x, -z), +Z: (x, -y),
+// -Z: (-x, -y)) and is filtered bilinearly inside that face.
+void cube_to_equirect(const bsm_sky& sky, std::vector<uint16_t>& out, uint32_t& W, uint32_t& H) {
+    const uint32_t S = sky.width;
+    W = 4 * S;
+    H = 2 * S;
+    out.assign((size_t)W * H * 4, 0);
+    double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    bool any = false;
+    for (int k = 0; k < 9; ++k) any = any || sky.transform[k] != 0.0f;
+    if (any)
+        for (int k = 0; k < 9; ++k) R[k] = sky.transform[k];
+    const double pi = 3.14159265358979323846;
+    for (uint32_t i = 0; i < H; ++i) {
+        double th = pi * (i + 0.5) / H;
+        for (uint32_t j = 0; j < W; ++j) {
+            double ph = 2.0 * pi * ((j + 0.5) / W - 0.5);
+            double d0[3] = {std::sin(th) * std::cos(ph), std::cos(th), std::sin(th) * std::sin(ph)};
+            double d[3];
+            for (int k = 0; k < 3; ++k) d[k] = R[3 * k] * d0[0] + R[3 * k + 1] * d0[1] + R[3 * k + 2] * d0[2];
+            double ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+            int face;
+            double sc, tc, ma;
+            if (ax >= ay && ax >= az) { face = d[0] > 0 ? 0 : 1; ma = ax; sc = d[0] > 0 ? -d[2] : d[2]; tc = -d[1]; }
+            else if (ay >= az) { face = d[1] > 0 ? 2 : 3; ma = ay; sc = d[0]; tc = d[1] > 0 ? d[2] : -d[2]; }
+            else { face = d[2] > 0 ? 4 : 5; ma = az; sc = d[2] > 0 ? d[0] : -d[0]; tc = -d[1]; }
+            double x = ((sc / ma + 1.0) * 0.5) * S - 0.5, y = ((tc / ma + 1.0) * 0.5) * S - 0.5;
+            x = std::min(std::max(x, 0.0), (double)S - 1);
+            y = std::min(std::max(y, 0.0), (double)S - 1);
+            uint32_t x0 = (uint32_t)x, y0 = (uint32_t)y;
+            uint32_t x1 = std::min(x0 + 1, S - 1), y1 = std::min(y0 + 1, S - 1);
+            double fx = x - x0, fy = y - y0;
+            const uint16_t* F = sky.rgba16f + (size_t)face * S * S * 4;
+            for (int c = 0; c < 4; ++c) {
+                auto at = [&](uint32_t xx, uint32_t yy) { return (double)half_to_float(F[((size_t)yy * S + xx) * 4 + c]); };
+                double v = (at(x0, y0) * (1 - fx) + at(x1, y0) * fx) * (1 - fy) + (at(x0, y1) * (1 - fx) + at(x1, y1) * fx) * fy;
+                out[((size_t)i * W + j) * 4 + c] = float_to_half((float)v);
+            }
+        }
+    }
+}
+
 bsm_status setup_shading(bsm_context* ctx, Scene* sc, const bsm_material* materials, uint32_t num_materials,
-                         const bsm_dir_light* dir_lights, uint32_t num_dir_lights, const bsm_sky& sky,
-                         const float lo[3], const float hi[3]) {
+                         const bsm_dir_light* dir_lights, uint32_t num_dir_lights, const bsm_point_light* point_lights,
+                         uint32_t num_point_lights, const bsm_rect_light* rect_lights, uint32_t num_rect_lights,
+                         const bsm_sky& sky_in, const float lo[3], const float hi[3]) {
     if (num_materials == 0 || !materials) return fail(ctx, BSM_ERR_INVALID_ARG, "scene needs at least one material");
-    if (num_dir_lights > (uint32_t)kMaxLights)
-        return fail(ctx, BSM_ERR_INVALID_ARG, "at most " + std::to_string(kMaxLights) + " directional lights");
-    if (num_dir_lights && !dir_lights) return fail(ctx, BSM_ERR_INVALID_ARG, "dir_lights is NULL");
-    if (sky.kind == BSM_SKY_EQUIRECT && (!sky.rgba16f || sky.width == 0 || sky.height == 0))
-        return fail(ctx, BSM_ERR_INVALID_ARG, "equirect sky needs texels");
-    if (sky.kind > BSM_SKY_EQUIRECT) return fail(ctx, BSM_ERR_INVALID_ARG, "unknown sky kind");
+    if ((uint64_t)num_dir_lights + num_point_lights + num_rect_lights > (uint64_t)kMaxLights)
+        return fail(ctx, BSM_ERR_INVALID_ARG, "at most " + std::to_string(kMaxLights) + " lights in all");
+    if ((num_dir_lights && !dir_lights) || (num_point_lights && !point_lights) || (num_rect_lights && !rect_lights))
+        return fail(ctx, BSM_ERR_INVALID_ARG, "light array is NULL");
+    if (sky_in.kind > BSM_SKY_CUBEMAP) return fail(ctx, BSM_ERR_INVALID_ARG, "unknown sky kind");
+    if (sky_in.kind != BSM_SKY_CONSTANT && (!sky_in.rgba16f || sky_in.width == 0 || sky_in.height == 0))
+        return fail(ctx, BSM_ERR_INVALID_ARG, "sky map needs texels");
+    if (sky_in.kind == BSM_SKY_CUBEMAP && sky_in.width != sky_in.height)
+        return fail(ctx, BSM_ERR_INVALID_ARG, "cubemap faces must be square");
+    bsm_sky sky = sky_in;
+    std::vector<uint16_t> cube_eq;
+    if (sky_in.kind == BSM_SKY_CUBEMAP) {  // resampled once into the sampler's equirect layout
+        uint32_t W, H;
+        cube_to_equirect(sky_in, cube_eq, W, H);
+        sky.kind = BSM_SKY_EQUIRECT;
+        sky.width = W;
+        sky.height = H;
+        sky.rgba16f = cube_eq.data();
+    }
     sc->extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
     // materials: (base.rgb, roughness), (f0.rgb, metallic); f0 = lerp(0.04, base, metallic)
     std::vector<float4> mats(2 * (size_t)num_materials);
@@ -426,13 +510,41 @@ bsm_status setup_shading(bsm_context* ctx, Scene* sc, const bsm_material* materi
     DevScene& ds = sc->dev;
     ds.materials = (const float4*)sc->materials.ptr;
     ds.num_materials = num_materials;
-    ds.num_lights = num_dir_lights;
+    uint32_t nl = 0;
+    auto kind_bits = [](uint32_t k) { float f; std::memcpy(&f, &k, 4); return f; };
     for (uint32_t l = 0; l < num_dir_lights; ++l) {
         const bsm_dir_light& L = dir_lights[l];
         V3 dir = normalize(v3(L.direction[0], L.direction[1], L.direction[2]));
-        ds.light_dir[l] = make_float4(dir.x, dir.y, dir.z, 0.0f);
-        ds.light_e[l] = make_float4(L.emission[0], L.emission[1], L.emission[2], 0.0f);
+        DevLight& d = ds.lights[nl++];
+        d.a = make_float4(dir.x, dir.y, dir.z, kind_bits(kLightDir));
+        d.b = make_float4(L.emission[0], L.emission[1], L.emission[2], 0.0f);
+        d.c = d.d = make_float4(0, 0, 0, 0);
     }
+    for (uint32_t l = 0; l < num_point_lights; ++l) {
+        const bsm_point_light& L = point_lights[l];
+        if (!(L.range > 0.0f)) return fail(ctx, BSM_ERR_INVALID_ARG, "point light range must be > 0");
+        V3 dir = normalize(v3(L.direction[0], L.direction[1], L.direction[2]));
+        if (!(L.cos_inner > L.cos_outer)) dir = v3(0.0f, 0.0f, 1.0f);
+        DevLight& d = ds.lights[nl++];
+        d.a = make_float4(L.position[0], L.position[1], L.position[2], kind_bits(kLightPoint));
+        d.b = make_float4(L.emission[0], L.emission[1], L.emission[2], 1.0f / (L.range * L.range));
+        d.c = make_float4(dir.x, dir.y, dir.z, L.cos_inner);
+        d.d = make_float4(L.cos_outer, 0.0f, 0.0f, 0.0f);
+    }
+    for (uint32_t l = 0; l < num_rect_lights; ++l) {
+        const bsm_rect_light& L = rect_lights[l];
+        if (!(L.width > 0.0f && L.height > 0.0f)) return fail(ctx, BSM_ERR_INVALID_ARG, "rect light size must be > 0");
+        V3 ax = v3(L.axis_x[0], L.axis_x[1], L.axis_x[2]), ay = v3(L.axis_y[0], L.axis_y[1], L.axis_y[2]);
+        V3 c = v3(L.center[0], L.center[1], L.center[2]);
+        V3 eu = ax * L.width, ev = ay * L.height;
+        V3 corner = c - ax * (0.5f * L.width) - ay * (0.5f * L.height);
+        DevLight& d = ds.lights[nl++];
+        d.a = make_float4(corner.x, corner.y, corner.z, kind_bits(kLightRect));
+        d.b = make_float4(L.emission[0], L.emission[1], L.emission[2], kind_bits(L.two_sided ? 1u : 0u));
+        d.c = make_float4(eu.x, eu.y, eu.z, L.width * L.height);
+        d.d = make_float4(ev.x, ev.y, ev.z, 0.0f);
+    }
+    ds.num_lights = nl;
     ds.sky.kind = sky.kind;
     ds.sky.cr = sky.color[0]; ds.sky.cg = sky.color[1]; ds.sky.cb = sky.color[2];
     if (sky.kind == BSM_SKY_EQUIRECT) {
@@ -471,11 +583,6 @@ extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d
     if (d->num_triangles == 0 || !d->positions || d->num_vertices == 0)
         return fail(ctx, BSM_ERR_INVALID_ARG, "scene needs vertices and triangles");
     if (d->num_materials == 0 || !d->materials) return fail(ctx, BSM_ERR_INVALID_ARG, "scene needs at least one material");
-    if (d->num_dir_lights > (uint32_t)kMaxLights)
-        return fail(ctx, BSM_ERR_INVALID_ARG, "at most " + std::to_string(kMaxLights) + " directional lights");
-    if (d->sky.kind == BSM_SKY_EQUIRECT && (!d->sky.rgba16f || d->sky.width == 0 || d->sky.height == 0))
-        return fail(ctx, BSM_ERR_INVALID_ARG, "equirect sky needs texels");
-    if (d->sky.kind > BSM_SKY_EQUIRECT) return fail(ctx, BSM_ERR_INVALID_ARG, "unknown sky kind");
     auto sc = std::make_unique<Scene>();
     sc->positions.assign(d->positions, d->positions + 3 * (size_t)d->num_vertices);
     if (d->indices) {
@@ -499,7 +606,8 @@ extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d
             lo[k] = std::min(lo[k], p); hi[k] = std::max(hi[k], p);
         }
     bsm_status st = setup_shading(ctx, sc.get(), d->materials, d->num_materials, d->dir_lights, d->num_dir_lights,
-                                  d->sky, lo, hi);
+                                  d->point_lights, d->num_point_lights, d->rect_lights, d->num_rect_lights, d->sky, lo,
+                                  hi);
     if (st) { free_scene_buffers(ctx, *sc); return st; }
     DevScene& ds = sc->dev;
     ds.has_non_opaque = 0;
@@ -839,7 +947,8 @@ extern "C" bsm_status bsm_scene_create_instanced(bsm_context* ctx, const bsm_ins
     sc->num_triangles = (uint32_t)total;
     for (const bsm_instance& in : sc->instances) ctx->geoms[in.geometry_id]->users++;
     bsm_status st = setup_shading(ctx, sc.get(), d->materials, d->num_materials, d->dir_lights, d->num_dir_lights,
-                                  d->sky, lo, hi);
+                                  d->point_lights, d->num_point_lights, d->rect_lights, d->num_rect_lights, d->sky, lo,
+                                  hi);
     if (!st) {
         bool any = false;
         for (float t : sc->transparency) any = any || t != 0.0f;

@@ -755,6 +755,8 @@ struct ProjectOwned {
     std::vector<uint32_t> idx, mat;
     std::vector<bsm_material> mats;
     std::vector<bsm_dir_light> lights;
+    std::vector<bsm_point_light> points;
+    std::vector<bsm_rect_light> rects;
 };
 std::mutex g_proj_mu;
 std::unordered_map<const void*, ProjectOwned*> g_proj;  // keyed by desc->positions
@@ -1136,8 +1138,60 @@ bsm_status project_load(const char* project_dir, bsm_scene_desc* desc, bsm_proje
                 rend_c = val;
             } else if (t == "SkyboxComponent") {
                 info->has_skybox = 1;
-            } else if (t == "PointLightComponent" || t == "SpotLightComponent" || t == "RectLightComponent") {
-                info->num_unsupported_lights++;
+            } else if (t == "PointLightComponent") {
+                // lights.cpp:120-139: position = translation, direction = rotation * (0, 1, 0),
+                // spot cone cosines, 1 / range^2 attenuation
+                double col[3] = {1, 1, 1};
+                vec_of(val->get("color"), 3, col);
+                double strength = num_or(val->get("strength"), 1.0);
+                bsm_point_light pl{};
+                bool zero = true;
+                for (int k = 0; k < 3; ++k) {
+                    pl.emission[k] = (float)(col[k] * strength);
+                    zero = zero && pl.emission[k] == 0.0f;
+                }
+                if (zero) continue;
+                double o0[3] = {0, 0, 0}, pw[3], y[3] = {0, 1, 0}, d[3];
+                world[i].apply(o0, pw);
+                world[i].rotate(y, d);
+                double n = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                for (int k = 0; k < 3; ++k) { pl.position[k] = (float)pw[k]; pl.direction[k] = (float)(d[k] / n); }
+                pl.range = (float)num_or(val->get("range"), 30.0);
+                const TVal* spot = val->get("spot");
+                if (spot && spot->k == TVal::Bool && spot->b) {
+                    const double d2r = 3.14159265358979323846 / 180.0;
+                    pl.cos_inner = (float)std::cos(num_or(val->get("spot_inner_angle"), 30.0) * d2r);
+                    pl.cos_outer = (float)std::cos(num_or(val->get("spot_outer_angle"), 60.0) * d2r);
+                }
+                own->points.push_back(pl);
+            } else if (t == "RectLightComponent") {
+                // lights.cpp:210-228: centre = translation, corners along rotation * (+-w/2, +-h/2, 0)
+                double col[3] = {1, 1, 1};
+                vec_of(val->get("color"), 3, col);
+                double strength = num_or(val->get("strength"), 1.0);
+                bsm_rect_light rl{};
+                bool zero = true;
+                for (int k = 0; k < 3; ++k) {
+                    rl.emission[k] = (float)(col[k] * strength);
+                    zero = zero && rl.emission[k] == 0.0f;
+                }
+                if (zero) continue;
+                double o0[3] = {0, 0, 0}, pw[3], x[3] = {1, 0, 0}, y[3] = {0, 1, 0}, ax[3], ay[3];
+                world[i].apply(o0, pw);
+                world[i].rotate(x, ax);
+                world[i].rotate(y, ay);
+                for (int k = 0; k < 3; ++k) {
+                    rl.center[k] = (float)pw[k];
+                    rl.axis_x[k] = (float)ax[k];
+                    rl.axis_y[k] = (float)ay[k];
+                }
+                rl.width = (float)num_or(val->get("width"), 1.0);
+                rl.height = (float)num_or(val->get("height"), 1.0);
+                const TVal* ts = val->get("two_sided");
+                rl.two_sided = ts && ts->k == TVal::Bool && ts->b ? 1u : 0u;
+                if (const TVal* tex = val->get("texture"); tex && tex->k == TVal::Tab && tex->get("asset_id"))
+                    info->num_unsupported_lights++;  // textured rect light: traced with its constant emission
+                own->rects.push_back(rl);
             } else if (t == "BasicRendererOverrideVolume") {
                 const TVal* st = val->get("settings");
                 const TVal* pt = st ? st->get("path_tracing") : nullptr;
@@ -1234,6 +1288,10 @@ bsm_status project_load(const char* project_dir, bsm_scene_desc* desc, bsm_proje
     desc->materials = own->mats.data();
     desc->num_dir_lights = (uint32_t)own->lights.size();
     desc->dir_lights = own->lights.empty() ? nullptr : own->lights.data();
+    desc->num_point_lights = (uint32_t)own->points.size();
+    desc->point_lights = own->points.empty() ? nullptr : own->points.data();
+    desc->num_rect_lights = (uint32_t)own->rects.size();
+    desc->rect_lights = own->rects.empty() ? nullptr : own->rects.data();
     // no SkyboxComponent texture support: the reference's black 1x1 cube when none is set
     // (skybox.cpp:47-50)
     desc->sky.kind = BSM_SKY_CONSTANT;

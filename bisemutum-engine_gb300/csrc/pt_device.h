@@ -24,7 +24,16 @@
 
 namespace bsm {
 
-constexpr int kMaxLights = 4;
+constexpr int kMaxLights = 8;     // directional + point/spot + rect lights of a scene
+
+// A light of the scene, four float4 (kind in a.w's bits):
+//   directional: a = (direction to the light, 0), b = (emission, 0)
+//   point/spot:  a = (position, 1), b = (emission, 1 / range^2), c = (direction to the light, cos_inner),
+//                d = (cos_outer, 0, 0, 0)
+//   rect:        a = (corner (-w, -h), 2), b = (emission, two_sided), c = (edge along x, area),
+//                d = (edge along y, 0); the unit normal (local +z) is normalize(cross(c, d))
+enum : uint32_t { kLightDir = 0, kLightPoint = 1, kLightRect = 2 };
+struct DevLight { float4 a, b, c, d; };
 constexpr int kMaxSeg = 16;
 
 struct DevSky {
@@ -45,9 +54,8 @@ struct DevScene {
     const float* mat_tr;       // two-level scene with non-opaque materials: per-material transparency, else null
     const float4* materials;   // 2 per material: (base.rgb, roughness), (f0.rgb, metallic)
     uint32_t num_materials;
-    uint32_t num_lights;
-    float4 light_dir[kMaxLights];
-    float4 light_e[kMaxLights];
+    uint32_t num_lights;       // all kinds; the shadow queue has num_lights + 1 slots per path
+    DevLight lights[kMaxLights];
     DevSky sky;
     uint32_t has_non_opaque;   // some triangle has a transparency (alpha test / translucent)
     float ray_offset;          // origin offset along the geometric normal

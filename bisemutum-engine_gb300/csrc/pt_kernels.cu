@@ -21,6 +21,7 @@
 #include "pt_sky.cuh"
 #include "pt_trace.cuh"
 #include "pt_scene.cuh"
+#include "pt_lights.cuh"
 #include "pt_gbuffer.cuh"
 #include "bvh_quant.h"
 #include "mlp.cuh"
@@ -87,7 +88,7 @@ __global__ void k_camera(const DevView* __restrict__ views, uint32_t n_views, ui
 }
 
 // ---------------------------------------------------------------- extend ----
-template <bool kCount, int kMinBlocks>
+template <bool kCount, int kMinBlocks, bool kOpacity>
 __global__ void __launch_bounds__(256, kMinBlocks) k_extend(DevScene sc, const float4* __restrict__ ray_o,
                                                 const float4* __restrict__ ray_d, const uint4* __restrict__ path,
                                                 float4* __restrict__ hit, uint32_t* counters,
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_extend(DevScene sc, const f
     uint32_t n = counters[kCntQueue + seg];
     if (blockIdx.x == 0 && threadIdx.x == 0) stats[kStatExtend + seg] += n;
     TraceCounters c{0, 0};
-    trace_queue<false, kCount>(
+    trace_queue<false, kCount, kOpacity>(
         sc.nodes, sc.tris, n, counters + kCntWork + 2 * seg,
         [&](uint32_t i, float4& o, float4& d) { o = ray_o[i]; d = ray_d[i]; },
         [&](uint32_t i, uint32_t leaf, float t, float u, float v) {
@@ -118,7 +119,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_extend(DevScene sc, const f
 }
 
 // ---------------------------------------------------------------- shadow ----
-template <int kMinBlocks>
+template <int kMinBlocks, bool kOpacity>
 __global__ void __launch_bounds__(256, kMinBlocks) k_shadow(DevScene sc, Wavefront wf, uint32_t seg, float4* accum,
                                                             int postpone_sp, int refill_min) {
     const uint32_t n_sun = wf.counters[kCntShadow + seg], n_sky = wf.counters[kCntSky + seg];
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_shadow(DevScene sc, Wavefro
     const float4* __restrict__ scn = wf.sh_c;
     // work index i < n_sun: sun ray i; otherwise sky ray at the back of the queue
     auto slot = [=](uint32_t i) { return i < n_sun ? i : sh_cap - 1u - (i - n_sun); };
-    trace_queue<true, false>(
+    trace_queue<true, false, kOpacity>(
         sc.nodes, sc.tris, n, wf.counters + kCntWork + 2 * seg + 1,
         [&](uint32_t i, float4& o, float4& d) { uint32_t k = slot(i); o = so[k]; d = sd[k]; },
         [&](uint32_t i, uint32_t leaf, float, float, float) {
@@ -291,24 +292,30 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene sc, const DevView* __
         aniso_roughness(surf.roughness, &rx, &ry);
         V3 lv = to_local(fr, V);
         float p_spec = spec_probability(surf, lv.z);
-        // next-event estimation: directional lights (lights.hlsl:10-13, dir_light_eval)
-#pragma unroll
+        // next-event estimation towards the lights (lights.hlsl:10-25; rect lights sampled by area),
+        // deferred_lighting_secondary.hlsl:51-96.  Rect lights draw their two uniforms here, after
+        // the vertex's five, in light order.
         for (uint32_t l = 0; l < (uint32_t)kMaxLights; ++l) {
             if (l >= sc.num_lights) break;
-            V3 c = v3s(0.0f);
-            V3 L = v3(sc.light_dir[l].x, sc.light_dir[l].y, sc.light_dir[l].z);
+            const DevLight& lt = sc.lights[l];
+            V3 c = v3s(0.0f), L = v3s(0.0f);
+            float smax = ray_len;
+            float ur0 = 0.0f, ur1 = 0.0f;
+            if (is_hit && __float_as_uint(lt.a.w) == kLightRect) { ur0 = pcg_uniform(g); ur1 = pcg_uniform(g); }
             bool emit = false;
             if (is_hit && (vflags & BSM_PT_NO_SUN_NEE) == 0u) {
-                V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
-                V3 e = v3(sc.light_e[l].x, sc.light_e[l].y, sc.light_e[l].z);
-                c = thr * e * f;
-                emit = max_comp(c) > 0.0f;
+                V3 e;
+                if (light_sample(lt, P, ur0, ur1, ray_len, L, smax, e)) {
+                    V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
+                    c = thr * e * f;
+                    emit = max_comp(c) > 0.0f;
+                }
             }
             uint32_t slot = warp_alloc(emit, wf.counters + kCntShadow + seg);
             if (emit) {
                 if (slot < cap * sc.num_lights) {
                     wf.sh_o[slot] = make_float4(org.x, org.y, org.z, tmin);
-                    wf.sh_d[slot] = make_float4(L.x, L.y, L.z, ray_len);
+                    wf.sh_d[slot] = make_float4(L.x, L.y, L.z, smax);
                     wf.sh_c[slot] = make_float4(c.x, c.y, c.z, __uint_as_float(m4.x));
                     if (sc.has_non_opaque && wf.sh_seed) wf.sh_seed[slot] = (uint32_t)g.state;
                 } else {
@@ -534,21 +541,18 @@ void launch_camera(const LaunchCfg& lc, cudaStream_t st, const DevView* views, u
 }
 void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, int q,
                    uint32_t seg, bool count_traversal) {
+#define BSM_EXTEND(C, B, O)                                                                                    \
+    k_extend<C, B, O><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], \
+                                                                     wf.hit, wf.counters, wf.stats, seg,        \
+                                                                     lc.postpone_sp, lc.refill_min)
+    const bool op = sc.has_non_opaque != 0;
     if (sc.insts)
         k_extend2<<<lc.grid_shade, 256, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit, wf.counters,
                                                    wf.stats, seg);
-    else if (count_traversal)
-        k_extend<true, 1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit,
-                                                                           wf.counters, wf.stats, seg,
-                                                                           lc.postpone_sp, lc.refill_min);
-    else if (lc.regcap)
-        k_extend<false, 4><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit,
-                                                                            wf.counters, wf.stats, seg,
-                                                                            lc.postpone_sp, lc.refill_min);
-    else
-        k_extend<false, 1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit,
-                                                                            wf.counters, wf.stats, seg,
-                                                                            lc.postpone_sp, lc.refill_min);
+    else if (count_traversal) { if (op) BSM_EXTEND(true, 1, true); else BSM_EXTEND(true, 1, false); }
+    else if (lc.regcap) { if (op) BSM_EXTEND(false, 4, true); else BSM_EXTEND(false, 4, false); }
+    else { if (op) BSM_EXTEND(false, 1, true); else BSM_EXTEND(false, 1, false); }
+#undef BSM_EXTEND
 }
 void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const DevView* views,
                   const Wavefront& wf, int q, uint32_t seg, float4* accum) {
@@ -556,14 +560,14 @@ void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, cons
 }
 void launch_shadow(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, uint32_t seg,
                    float4* accum) {
+#define BSM_SHADOW(B, O) \
+    k_shadow<B, O><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp, lc.refill_min)
+    const bool op = sc.has_non_opaque != 0;
     if (sc.insts)
         k_shadow2<<<lc.grid_shade, 256, 0, st>>>(sc, wf, seg, accum);
-    else if (lc.regcap)
-        k_shadow<4><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp,
-                                                                     lc.refill_min);
-    else
-        k_shadow<1><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp,
-                                                                     lc.refill_min);
+    else if (lc.regcap) { if (op) BSM_SHADOW(4, true); else BSM_SHADOW(4, false); }
+    else { if (op) BSM_SHADOW(1, true); else BSM_SHADOW(1, false); }
+#undef BSM_SHADOW
 }
 void launch_resolve(cudaStream_t st, const float4* accum, uint32_t width, uint32_t height, float inv_spp,
                     float4* out, uint32_t pitch_px) {
@@ -597,11 +601,11 @@ void query_launch_cfg(int device, int block_trace, LaunchCfg* lc) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int per_sm_ext = 0, per_sm_sh = 0, per_sm_shade = 0;
     if (lc->regcap) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, 4>, block_trace, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<4>, block_trace, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, 4, true>, block_trace, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<4, true>, block_trace, 0);
     } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, 1>, block_trace, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<1>, block_trace, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, 1, true>, block_trace, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<1, true>, block_trace, 0);
     }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_shade, k_shade, 256, 0);
     int per_sm = per_sm_ext < per_sm_sh ? per_sm_ext : per_sm_sh;

@@ -389,12 +389,13 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // the warp runs this loop together (all ballots use the full mask).  `load`
 // (index -> (origin/tmin, direction/tmax)) supplies rays; `finish(index, leaf,
 // t, u, v)` receives each result (leaf = kMissPrim on a miss; for any-hit the
-// first hit found); `seed(index)` gives the ray's opacity seed, read only when a
-// candidate hit lies on a non-opaque triangle.
+// first hit found); with kOpacity, `seed(index)` gives the ray's opacity seed,
+// read only when a candidate hit lies on a non-opaque triangle (scenes without
+// one use the kOpacity = false instantiation, which skips the rule).
 // `postpone_sp` (<= kPostponeMaxSp) is the stack depth below which triangle
 // groups may be postponed (0 disables postponing); `refill_min` is the number
 // of idle lanes that makes the warp fetch new rays.  Both are tuning knobs.
-template <bool kAnyHit, bool kCount, class Load, class Finish, class Seed>
+template <bool kAnyHit, bool kCount, bool kOpacity, class Load, class Finish, class Seed>
 __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, const CwTri* __restrict__ tris,
                                             uint32_t n, uint32_t* work, Load load, Finish finish, Seed seed,
                                             TraceCounters* cnt, int postpone_sp, int refill_min) {
@@ -472,7 +473,7 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
                 if (kCount) cnt->tris++;
                 float t, u, v;
                 if (tri_test(r, a, b, c, tbest, prim, best_prim, t, u, v) &&
-                    (c.w == 0.0f || keep_hit(r, c.w, seed(idx)))) {
+                    (!kOpacity || c.w == 0.0f || keep_hit(r, c.w, seed(idx)))) {
                     tbest = t; best_leaf = ti; best_prim = prim; bu = u; bv = v;
                     if (kAnyHit) { T.y = 0u; G.y = 0u; sp = 0; }
                 }

@@ -17,6 +17,7 @@
 #include "pt_sky.cuh"
 #include "pt_trace.cuh"
 #include "pt_scene.cuh"
+#include "pt_lights.cuh"
 
 namespace bsm {
 
@@ -86,14 +87,19 @@ __global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView*
         V3 lv = to_local(fr, V);
         float p_spec = spec_probability(surf, lv.z);
         for (uint32_t l = 0; l < sc.num_lights; ++l) {
-            V3 L = v3(sc.light_dir[l].x, sc.light_dir[l].y, sc.light_dir[l].z);
+            const DevLight& lt = sc.lights[l];
+            float ur0 = 0.0f, ur1 = 0.0f;
+            if (__float_as_uint(lt.a.w) == kLightRect) { ur0 = pcg_uniform(g); ur1 = pcg_uniform(g); }
+            V3 L, e;
+            float smax;
+            if (!light_sample(lt, P, ur0, ur1, v.ray_length, L, smax, e)) continue;
             V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
-            V3 c = thr * v3(sc.light_e[l].x, sc.light_e[l].y, sc.light_e[l].z) * f;
+            V3 c = thr * e * f;
             if (max_comp(c) > 0.0f) {
-                RayPre sr = make_ray(make_float4(org.x, org.y, org.z, v.t_min), make_float4(L.x, L.y, L.z, v.ray_length));
+                RayPre sr = make_ray(make_float4(org.x, org.y, org.z, v.t_min), make_float4(L.x, L.y, L.z, smax));
                 float a, b2, c2;
                 uint32_t si;
-                if (trace_scene<true>(sc, sr, v.ray_length, a, b2, c2, si, (uint32_t)g.state) == kMissPrim)
+                if (trace_scene<true>(sc, sr, smax, a, b2, c2, si, (uint32_t)g.state) == kMissPrim)
                     contrib[k] = contrib[k] + c;
             }
         }

@@ -111,12 +111,38 @@ typedef struct bsm_dir_light {
     float emission[3];     /* colour * strength; the radiance term of dir_light_eval (lights.hlsl:10-13) */
 } bsm_dir_light;
 
-enum { BSM_SKY_CONSTANT = 0, BSM_SKY_EQUIRECT = 1 };
+/* PointLightData (renderer/context/lights.hpp:24-36): a point light, or a
+ * spot light when cos_inner > cos_outer; point_light_eval (lights.hlsl:15-25). */
+typedef struct bsm_point_light {
+    float position[3];
+    float emission[3];      /* colour * strength */
+    float range;            /* attenuation range (saturate(1 - (d^2 / range^2)^2) / max(d^2, 0.001)) */
+    float direction[3];     /* unit vector pointing TO the light (the spot's axis reversed) */
+    float cos_inner;        /* spot: cos of the inner / outer half angles; point light: both 0 */
+    float cos_outer;
+} bsm_point_light;
+
+/* RectLightData (lights.hpp:38-53): a rectangle with corners c + R(+-w, +-h, 0).
+ * It emits towards its local -z (the side from which the corners run
+ * counter-clockwise, which the reference's LTC integral counts positive,
+ * lights.hlsl:421), or both sides when two_sided.  Untextured. */
+typedef struct bsm_rect_light {
+    float center[3];
+    float axis_x[3];        /* unit local x (width direction) in world space */
+    float axis_y[3];        /* unit local y (height direction) */
+    float width, height;
+    float emission[3];      /* colour * strength: radiance of the surface */
+    uint32_t two_sided;
+} bsm_rect_light;
+
+enum { BSM_SKY_CONSTANT = 0, BSM_SKY_EQUIRECT = 1, BSM_SKY_CUBEMAP = 2 };
 typedef struct bsm_sky {
-    uint32_t kind;          /* BSM_SKY_CONSTANT or BSM_SKY_EQUIRECT */
+    uint32_t kind;          /* BSM_SKY_* */
     float color[3];         /* constant radiance, or a multiplier of the map (skybox_color) */
-    uint32_t width, height; /* equirect size; row 0 looks at +y, column 0 at azimuth -pi */
-    const uint16_t* rgba16f;/* width*height RGBA IEEE half texels (host) */
+    uint32_t width, height; /* equirect size (row 0 looks at +y, column 0 at azimuth -pi), or the cube face size */
+    const uint16_t* rgba16f;/* RGBA IEEE half texels (host): width*height, or 6 faces +X -X +Y -Y +Z -Z */
+    float transform[9];     /* cubemap: row-major rotation applied to a direction before the lookup
+                               (skybox_transform, deferred_lighting_secondary.hlsl:25); zeros = identity */
 } bsm_sky;
 
 typedef struct bsm_scene_desc {
@@ -130,6 +156,10 @@ typedef struct bsm_scene_desc {
     uint32_t num_dir_lights;
     const bsm_dir_light* dir_lights;
     bsm_sky sky;
+    uint32_t num_point_lights;        /* dir + point + rect lights: at most 8 */
+    const bsm_point_light* point_lights;
+    uint32_t num_rect_lights;
+    const bsm_rect_light* rect_lights;
 } bsm_scene_desc;
 
 typedef struct bsm_bvh_opts {
@@ -499,6 +529,10 @@ typedef struct bsm_instanced_scene_desc {
     uint32_t num_dir_lights;
     const bsm_dir_light* dir_lights;
     bsm_sky sky;
+    uint32_t num_point_lights;
+    const bsm_point_light* point_lights;
+    uint32_t num_rect_lights;
+    const bsm_rect_light* rect_lights;
 } bsm_instanced_scene_desc;
 
 /* Creates a scene over instances of geometries: a TLAS (the same compressed
@@ -578,7 +612,7 @@ typedef struct bsm_project_info {
     uint32_t num_skipped_submeshes;    /* non-triangle-list topologies */
     uint32_t num_materials_approximated; /* material functions beyond constant assignments */
     uint32_t num_non_opaque_materials; /* alpha-test / translucent blend modes (any-hit opacity rule) */
-    uint32_t num_unsupported_lights;   /* point / spot / rect light components */
+    uint32_t num_unsupported_lights;   /* textured rect lights (traced with their constant emission) */
     uint32_t has_skybox;               /* a SkyboxComponent (its cube texture is not read: sky is black) */
     char error[256];                   /* reason of a failed load */
 } bsm_project_info;
@@ -589,8 +623,9 @@ typedef struct bsm_project_info {
  * (static_mesh_render_system.cpp:56-79) in world space (Transform,
  * math/transform.cpp:120-124, parents applied), its materials from their
  * TOML (scene_basic/material.cpp:12-53; constant base colour / roughness /
- * f0 / metallic / opacity, blend mode), DirectionalLightComponents as directional lights
- * (renderer/context/lights.cpp:55-65), and the first camera.  Arrays belong
+ * f0 / metallic / opacity, blend mode), directional, point / spot and rect
+ * light components (renderer/context/lights.cpp:55-65, 120-139, 210-228), and
+ * the first camera.  Arrays belong
  * to the library until bsm_project_free. */
 BSM_API bsm_status bsm_project_load(const char* project_dir, bsm_scene_desc* desc, bsm_project_info* info);
 BSM_API void bsm_project_free(bsm_scene_desc* desc);

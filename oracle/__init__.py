@@ -33,7 +33,7 @@ def lib() -> C.CDLL:
         path = _b.build_oracle()
         L = C.CDLL(path)
         vp, u32, u64, f32, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_int
-        L.orc_scene_create.argtypes = [vp, u32, vp, u32, vp, vp, u32, vp, u32, u32, vp, u32, u32, vp,
+        L.orc_scene_create.argtypes = [vp, u32, vp, u32, vp, vp, u32, vp, u32, u32, vp, u32, u32, vp, vp,
                                        C.POINTER(vp)]
         L.orc_scene_create.restype = i32
         L.orc_scene_destroy.argtypes = [vp]
@@ -58,7 +58,7 @@ def lib() -> C.CDLL:
         L.orc_geometry_create.argtypes = [vp, u32, vp, u32, vp, C.POINTER(vp)]
         L.orc_geometry_create.restype = i32
         L.orc_scene_create_instanced.argtypes = [vp, u32, vp, vp, vp, u32, vp, u32, vp, u32, u32, vp, u32, u32, vp,
-                                                 C.POINTER(vp)]
+                                                 vp, C.POINTER(vp)]
         L.orc_scene_create_instanced.restype = i32
         L.orc_scene_bvh_nodes.argtypes = [vp]
         L.orc_scene_bvh_nodes.restype = u32
@@ -87,6 +87,31 @@ def _f32(a):
     return np.ascontiguousarray(a, np.float32)
 
 
+def light_rows(scene) -> np.ndarray:
+    """(L, 16) float32 rows of the oracle's lights: kind, then the light's fields (pt_oracle.cpp setup_shading)."""
+    rows = []
+    for l in np.asarray(scene.lights, np.float32).reshape(-1, 6):
+        rows.append([0, *l] + [0] * 9)
+    for l in np.asarray(getattr(scene, "point_lights", None) if getattr(scene, "point_lights", None) is not None
+                        else np.zeros((0, 12)), np.float32).reshape(-1, 12):
+        rows.append([1, *l] + [0] * 3)
+    for l in np.asarray(getattr(scene, "rect_lights", None) if getattr(scene, "rect_lights", None) is not None
+                        else np.zeros((0, 15)), np.float32).reshape(-1, 15):
+        rows.append([2, *l])
+    return np.ascontiguousarray(np.array(rows, np.float32).reshape(-1, 16))
+
+
+def sky_args(scene):
+    """(texels or None, width, height, transform[9]) of a scene's sky (cubemaps: 6 faces, face size)."""
+    tex = None if scene.sky_texels is None else np.ascontiguousarray(scene.sky_texels, np.uint16)
+    xf = np.zeros(9, np.float32) if getattr(scene, "sky_transform", None) is None else _f32(scene.sky_transform)
+    if tex is None:
+        return None, 0, 0, xf
+    if scene.sky_kind == 2:                  # (6, S, S, 4)
+        return tex, tex.shape[2], tex.shape[1], xf
+    return tex, tex.shape[1], tex.shape[0], xf
+
+
 def material_rows(materials) -> np.ndarray:
     """(M, 7) float32: base rgb, roughness, metallic, opacity, blend mode; 5-column input is opaque."""
     m = np.asarray(materials, np.float32)
@@ -109,15 +134,14 @@ class OracleScene:
         idx = None if scene.indices is None else np.ascontiguousarray(scene.indices, np.uint32)
         mids = np.ascontiguousarray(scene.material_ids, np.uint32)
         mats = material_rows(scene.materials)
-        lights = _f32(scene.lights).reshape(-1, 6)
+        lights = light_rows(scene)
         color = _f32(scene.sky_color)
-        tex = None if scene.sky_texels is None else np.ascontiguousarray(scene.sky_texels, np.uint16)
+        tex, sw, sh, sxf = sky_args(scene)
         h = C.c_void_p()
         st = L.orc_scene_create(pos.ctypes.data, pos.shape[0], None if idx is None else idx.ctypes.data,
                                 mids.shape[0], mids.ctypes.data, mats.ctypes.data, mats.shape[0],
                                 lights.ctypes.data, lights.shape[0], scene.sky_kind, color.ctypes.data,
-                                0 if tex is None else tex.shape[1], 0 if tex is None else tex.shape[0],
-                                None if tex is None else tex.ctypes.data, C.byref(h))
+                                sw, sh, None if tex is None else tex.ctypes.data, sxf.ctypes.data, C.byref(h))
         if st != 0:
             raise RuntimeError("orc_scene_create failed")
         self.h = h
@@ -140,15 +164,14 @@ class OracleScene:
         im = np.ascontiguousarray(scene.inst_material, np.uint32)
         ix = _f32(scene.inst_transform).reshape(-1, 12)
         mats = material_rows(scene.materials)
-        lights = _f32(scene.lights).reshape(-1, 6)
+        lights = light_rows(scene)
         color = _f32(scene.sky_color)
-        tex = None if scene.sky_texels is None else np.ascontiguousarray(scene.sky_texels, np.uint16)
+        tex, sw, sh, sxf = sky_args(scene)
         h = C.c_void_p()
         st = L.orc_scene_create_instanced(garr, len(self._geoms), ig.ctypes.data, im.ctypes.data, ix.ctypes.data,
                                           ig.shape[0], mats.ctypes.data, mats.shape[0], lights.ctypes.data,
-                                          lights.shape[0], scene.sky_kind, color.ctypes.data,
-                                          0 if tex is None else tex.shape[1], 0 if tex is None else tex.shape[0],
-                                          None if tex is None else tex.ctypes.data, C.byref(h))
+                                          lights.shape[0], scene.sky_kind, color.ctypes.data, sw, sh,
+                                          None if tex is None else tex.ctypes.data, sxf.ctypes.data, C.byref(h))
         if st != 0:
             raise RuntimeError("orc_scene_create_instanced failed")
         self.h = h

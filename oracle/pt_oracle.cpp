@@ -244,8 +244,12 @@ struct Scene {
     std::vector<BNode> nodes;
     std::vector<float> mats;       // 8 per material: base rgb, rough, f0 rgb, metallic
     uint32_t nmat = 0;
+    // lights: 0 directional (a = direction, b = emission), 1 point/spot (a = position, b = emission,
+    // bw = 1 / range^2, c = direction to the light, cw = cos_inner, dx = cos_outer), 2 rect (a = corner,
+    // b = emission, bw = two_sided, c / d = edges, cw = area)
+    struct Light { uint32_t kind; F3 a, b, c, d; float bw, cw, dx; };
     uint32_t nlights = 0;
-    F3 ldir[4], le[4];
+    Light lights[8];
     uint32_t sky_kind = 0;
     F3 sky_color{0, 0, 0};
     uint32_t sw = 0, sh = 0;
@@ -671,6 +675,35 @@ struct ShadowQ {
     void clear() { o.clear(); d.clear(); c.clear(); tmin.clear(); tmax.clear(); pix.clear(); seed.clear(); }
 };
 
+// Next-event sample of a light from P (point_light_eval, lights.hlsl:15-25;
+// rect lights sampled uniformly by area): direction, shadow-ray length and the
+// radiance arriving along the direction (before the BSDF).
+static bool light_sample(const Scene::Light& L, F3 P, float u0, float u1, float ray_len, F3& dir, float& tmax, F3& e) {
+    if (L.kind == 0) { dir = L.a; e = L.b; tmax = ray_len; return true; }
+    F3 lvec = L.kind == 1 ? sub(L.a, P) : sub(add(add(L.a, muls(L.c, u0)), muls(L.d, u1)), P);
+    float d2 = dot3(lvec, lvec);
+    if (!(d2 > 0.0f)) return false;
+    float dist = std::sqrt(d2);
+    dir = divs(lvec, dist);
+    tmax = std::fmin(dist, ray_len);
+    if (L.kind == 1) {
+        float x = d2 * L.bw;
+        float att = std::fmin(std::fmax(1.0f - x * x, 0.0f), 1.0f) / std::fmax(d2, 0.001f);
+        if (L.cw > L.dx) {
+            float ct = std::fmin(std::fmax(dot3(dir, L.c), L.dx), L.cw);
+            att = att * ((ct - L.dx) / std::fmax(L.cw - L.dx, 0.001f));
+        }
+        e = muls(L.b, att);
+        return att > 0.0f;
+    }
+    F3 n = norm3(cross3(L.c, L.d));
+    float cl = dot3(dir, n);  // the rectangle emits towards -n
+    if (L.bw != 0.0f) cl = std::fabs(cl);
+    if (!(cl > 0.0f)) return false;
+    e = muls(L.b, cl * L.cw / d2);
+    return true;
+}
+
 // Renders pixels [pix_begin, pix_end) of one camera; `acc` receives RGB sums
 // (3 floats per pixel, indexed from pix_begin).
 static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32_t pix_begin, uint32_t pix_end,
@@ -735,13 +768,19 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                 aniso_rough(surf.rough, &rx, &ry);
                 F3 lv = local_of(fr, V);
                 float ps = spec_prob(surf, lv.z);
-                for (uint32_t l = 0; l < S.nlights; ++l) {  // deferred_lighting_secondary.hlsl:51-60
-                    if (st.flags & F_NO_SUN) break;
-                    F3 f = eval_lit(N, fr.x, fr.y, V, S.ldir[l], surf);
-                    F3 c = mul(mul(thr, S.le[l]), f);
+                for (uint32_t l = 0; l < S.nlights; ++l) {  // deferred_lighting_secondary.hlsl:51-96
+                    const Scene::Light& Lt = S.lights[l];
+                    float ur0 = 0.0f, ur1 = 0.0f;
+                    if (Lt.kind == 2) { ur0 = pcg_uniform(g); ur1 = pcg_uniform(g); }  // after the vertex's five
+                    if (st.flags & F_NO_SUN) continue;
+                    F3 L, e;
+                    float smax;
+                    if (!light_sample(Lt, P, ur0, ur1, st.ray_length, L, smax, e)) continue;
+                    F3 f = eval_lit(N, fr.x, fr.y, V, L, surf);
+                    F3 c = mul(mul(thr, e), f);
                     if (maxc(c) > 0.0f) {
-                        sq.o.push_back(org); sq.tmin.push_back(st.t_min); sq.d.push_back(S.ldir[l]);
-                        sq.tmax.push_back(st.ray_length); sq.c.push_back(c); sq.pix.push_back(q.pix[i]);
+                        sq.o.push_back(org); sq.tmin.push_back(st.t_min); sq.d.push_back(L);
+                        sq.tmax.push_back(smax); sq.c.push_back(c); sq.pix.push_back(q.pix[i]);
                         sq.seed.push_back((uint32_t)g.state);
                     }
                 }
@@ -838,9 +877,74 @@ static void build_geometry(Scene* S, const float* pos, uint32_t nv, const uint32
 
 // Materials (7 floats each: base rgb, roughness, metallic, opacity, blend mode),
 // lights, sky and the ray offset of a scene with bounds lo / hi.
+// IEEE half of a float, round to nearest even.
+static uint16_t float_to_half(float f) {
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    uint32_t sign = (x >> 16) & 0x8000u, exp = (x >> 23) & 0xffu, man = x & 0x7fffffu;
+    if (exp == 0xffu) return (uint16_t)(sign | 0x7c00u | (man ? 0x200u : 0u));
+    int e = (int)exp - 112;
+    if (e >= 31) return (uint16_t)(sign | 0x7c00u);
+    if (e <= 0) {
+        if (e < -10) return (uint16_t)sign;
+        man |= 0x800000u;
+        uint32_t shift = (uint32_t)(14 - e), h = man >> shift;
+        uint32_t rem = man & ((1u << shift) - 1u), half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (h & 1u))) ++h;
+        return (uint16_t)(sign | h);
+    }
+    uint32_t h = ((uint32_t)e << 10) | (man >> 13), rem = man & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
+    return (uint16_t)(sign | h);
+}
+
+// A cubemap (faces +X -X +Y -Y +Z -Z of size S) resampled to a 4S x 2S equirect
+// map: texel-centre direction, the sky rotation, the standard cube face table,
+// bilinear inside the face.
+static void cube_to_equirect(const uint16_t* faces, uint32_t S, const float* xf, std::vector<uint16_t>& out) {
+    const uint32_t W = 4 * S, H = 2 * S;
+    out.assign((size_t)W * H * 4, 0);
+    double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    bool any = false;
+    for (int k = 0; k < 9; ++k) any = any || xf[k] != 0.0f;
+    if (any)
+        for (int k = 0; k < 9; ++k) R[k] = xf[k];
+    const double pi = 3.14159265358979323846;
+    for (uint32_t i = 0; i < H; ++i) {
+        double th = pi * (i + 0.5) / H;
+        for (uint32_t j = 0; j < W; ++j) {
+            double ph = 2.0 * pi * ((j + 0.5) / W - 0.5);
+            double d0[3] = {std::sin(th) * std::cos(ph), std::cos(th), std::sin(th) * std::sin(ph)};
+            double d[3];
+            for (int k = 0; k < 3; ++k) d[k] = R[3 * k] * d0[0] + R[3 * k + 1] * d0[1] + R[3 * k + 2] * d0[2];
+            double ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+            int face;
+            double sc, tc, ma;
+            if (ax >= ay && ax >= az) { face = d[0] > 0 ? 0 : 1; ma = ax; sc = d[0] > 0 ? -d[2] : d[2]; tc = -d[1]; }
+            else if (ay >= az) { face = d[1] > 0 ? 2 : 3; ma = ay; sc = d[0]; tc = d[1] > 0 ? d[2] : -d[2]; }
+            else { face = d[2] > 0 ? 4 : 5; ma = az; sc = d[2] > 0 ? d[0] : -d[0]; tc = -d[1]; }
+            double x = ((sc / ma + 1.0) * 0.5) * S - 0.5, y = ((tc / ma + 1.0) * 0.5) * S - 0.5;
+            x = std::min(std::max(x, 0.0), (double)S - 1);
+            y = std::min(std::max(y, 0.0), (double)S - 1);
+            uint32_t x0 = (uint32_t)x, y0 = (uint32_t)y;
+            uint32_t x1 = std::min(x0 + 1, S - 1), y1 = std::min(y0 + 1, S - 1);
+            double fx = x - x0, fy = y - y0;
+            const uint16_t* F = faces + (size_t)face * S * S * 4;
+            for (int c = 0; c < 4; ++c) {
+                auto at = [&](uint32_t xx, uint32_t yy) { return (double)half_to_float(F[((size_t)yy * S + xx) * 4 + c]); };
+                double v = (at(x0, y0) * (1 - fx) + at(x1, y0) * fx) * (1 - fy) + (at(x0, y1) * (1 - fx) + at(x1, y1) * fx) * fy;
+                out[((size_t)i * W + j) * 4 + c] = float_to_half((float)v);
+            }
+        }
+    }
+}
+
+// Lights: 16 floats each, the first the kind.  0: direction, emission;
+// 1: position, emission, range, direction to the light, cos_inner, cos_outer;
+// 2: centre, axis x, axis y, width, height, emission, two_sided.
 static bool setup_shading(Scene* S, const float* materials, uint32_t nm, const float* lights, uint32_t nl,
                           uint32_t sky_kind, const float* sky_color, uint32_t sky_w, uint32_t sky_h,
-                          const uint16_t* sky_texels, const float lo[3], const float hi[3]) {
+                          const uint16_t* sky_texels, const float* sky_xf, const float lo[3], const float hi[3]) {
     S->extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
     S->offset = 2e-5f * S->extent;
     S->nmat = nm;
@@ -855,17 +959,45 @@ static bool setup_shading(Scene* S, const float* materials, uint32_t nm, const f
         for (int k = 0; k < 3; ++k) o[4 + k] = 0.04f + (M[k] - 0.04f) * M[4];  // lerp(0.04, base, metallic)
         o[7] = M[4];
     }
+    if (nl > 8) return false;
     S->nlights = nl;
     for (uint32_t l = 0; l < nl; ++l) {
-        S->ldir[l] = norm3(f3(lights[6 * l], lights[6 * l + 1], lights[6 * l + 2]));
-        S->le[l] = f3(lights[6 * l + 3], lights[6 * l + 4], lights[6 * l + 5]);
+        const float* r = lights + 16 * (size_t)l;
+        Scene::Light& L = S->lights[l];
+        L = Scene::Light{};
+        L.kind = (uint32_t)r[0];
+        if (L.kind == 0) {
+            L.a = norm3(f3(r[1], r[2], r[3]));
+            L.b = f3(r[4], r[5], r[6]);
+        } else if (L.kind == 1) {
+            L.a = f3(r[1], r[2], r[3]);
+            L.b = f3(r[4], r[5], r[6]);
+            L.bw = 1.0f / (r[7] * r[7]);
+            L.cw = r[11];
+            L.dx = r[12];
+            L.c = L.cw > L.dx ? norm3(f3(r[8], r[9], r[10])) : f3(0.0f, 0.0f, 1.0f);
+        } else {
+            F3 c = f3(r[1], r[2], r[3]), ax = f3(r[4], r[5], r[6]), ay = f3(r[7], r[8], r[9]);
+            float w = r[10], h = r[11];
+            L.a = sub(sub(c, muls(ax, 0.5f * w)), muls(ay, 0.5f * h));
+            L.b = f3(r[12], r[13], r[14]);
+            L.bw = r[15] != 0.0f ? 1.0f : 0.0f;
+            L.c = muls(ax, w);
+            L.d = muls(ay, h);
+            L.cw = w * h;
+        }
     }
-    S->sky_kind = sky_kind;
+    S->sky_kind = sky_kind == 2 ? 1 : sky_kind;
     S->sky_color = f3(sky_color[0], sky_color[1], sky_color[2]);
-    if (sky_kind == 1) {
+    if (sky_kind == 1 || sky_kind == 2) {
         if (!sky_texels || !sky_w || !sky_h) return false;
-        S->sw = sky_w; S->sh = sky_h;
-        S->texels.assign(sky_texels, sky_texels + (size_t)sky_w * sky_h * 4);
+        if (sky_kind == 2) {  // cubemap: resampled to the equirect layout, as the library does on upload
+            cube_to_equirect(sky_texels, sky_w, sky_xf, S->texels);
+            S->sw = 4 * sky_w; S->sh = 2 * sky_w;
+        } else {
+            S->sw = sky_w; S->sh = sky_h;
+            S->texels.assign(sky_texels, sky_texels + (size_t)sky_w * sky_h * 4);
+        }
         build_sky(*S);
     }
     return true;
@@ -874,14 +1006,14 @@ static bool setup_shading(Scene* S, const float* materials, uint32_t nm, const f
 ORC_API int orc_scene_create(const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt, const uint32_t* mat_ids,
                              const float* materials, uint32_t nm, const float* lights, uint32_t nl, uint32_t sky_kind,
                              const float* sky_color, uint32_t sky_w, uint32_t sky_h, const uint16_t* sky_texels,
-                             void** out) {
-    if (!pos || !nt || !materials || !nm || !out || nl > 4) return -1;
+                             const float* sky_xf, void** out) {
+    if (!pos || !nt || !materials || !nm || !out || nl > 8) return -1;
     Scene* S = new Scene();
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint32_t i = 0; i < nv; ++i)
         for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], pos[3 * i + k]); hi[k] = std::max(hi[k], pos[3 * i + k]); }
     build_geometry(S, pos, nv, idx, nt, mat_ids);
-    if (!setup_shading(S, materials, nm, lights, nl, sky_kind, sky_color, sky_w, sky_h, sky_texels, lo, hi)) {
+    if (!setup_shading(S, materials, nm, lights, nl, sky_kind, sky_color, sky_w, sky_h, sky_texels, sky_xf, lo, hi)) {
         delete S;
         return -1;
     }
@@ -961,8 +1093,8 @@ ORC_API int orc_scene_create_instanced(void* const* geoms, uint32_t ng, const ui
                                        const uint32_t* inst_mat, const float* inst_xf, uint32_t ni,
                                        const float* materials, uint32_t nm, const float* lights, uint32_t nl,
                                        uint32_t sky_kind, const float* sky_color, uint32_t sky_w, uint32_t sky_h,
-                                       const uint16_t* sky_texels, void** out) {
-    if (!geoms || !ni || !materials || !nm || !out || nl > 4) return -1;
+                                       const uint16_t* sky_texels, const float* sky_xf, void** out) {
+    if (!geoms || !ni || !materials || !nm || !out || nl > 8) return -1;
     Scene* S = new Scene();
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     uint32_t prim_base = 0;
@@ -981,7 +1113,7 @@ ORC_API int orc_scene_create_instanced(void* const* geoms, uint32_t ng, const ui
         for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], bl[k]); hi[k] = std::max(hi[k], bh[k]); }
         S->inst.push_back(I);
     }
-    if (!setup_shading(S, materials, nm, lights, nl, sky_kind, sky_color, sky_w, sky_h, sky_texels, lo, hi)) {
+    if (!setup_shading(S, materials, nm, lights, nl, sky_kind, sky_color, sky_w, sky_h, sky_texels, sky_xf, lo, hi)) {
         delete S;
         return -1;
     }

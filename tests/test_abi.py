@@ -91,3 +91,42 @@ def test_no_cpu_fallback_without_device(bsm):
         pytest.skip("a CUDA device is present")
     with pytest.raises(bsm.BsmError):
         bsm.Context(0)
+
+
+STRUCTS = {"Material": "bsm_material", "DirLight": "bsm_dir_light", "PointLight": "bsm_point_light",
+           "RectLight": "bsm_rect_light", "Sky": "bsm_sky", "SceneDesc": "bsm_scene_desc", "BvhOpts": "bsm_bvh_opts",
+           "BvhStats": "bsm_bvh_stats", "Camera": "bsm_camera", "PtSettings": "bsm_pt_settings",
+           "ViewOutput": "bsm_view_output", "PrimaryOutput": "bsm_primary_output", "RenderStats": "bsm_render_stats",
+           "ViewDesc": "bsm_view_desc", "TuneParams": "bsm_tune_params", "TuneResult": "bsm_tune_result",
+           "ServerOpts": "bsm_server_opts", "Request": "bsm_request", "RequestStatus": "bsm_request_status",
+           "ServerStats": "bsm_server_stats", "CacheSettings": "bsm_cache_settings",
+           "SceneGenParams": "bsm_scene_gen_params", "GeometryDesc": "bsm_geometry_desc", "Instance": "bsm_instance",
+           "InstancedSceneDesc": "bsm_instanced_scene_desc", "Submesh": "bsm_submesh", "MeshData": "bsm_mesh_data",
+           "ProjectInfo": "bsm_project_info"}
+
+
+def test_python_structures_match_the_header(bsm, tmp_path):
+    """Every ctypes mirror has the size and field offsets the C compiler gives the header's struct."""
+    import shutil
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "bsm_pt.h"', "int main(void) {"]
+    for py, c in STRUCTS.items():
+        lines.append(f'printf("{py} size %zu\\n", sizeof({c}));')
+        for fname, _ in getattr(bsm, py)._fields_:
+            lines.append(f'printf("{py} {fname} %zu\\n", offsetof({c}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "sizes.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "sizes"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    bad = []
+    for line in filter(None, out):
+        py, what, val = line.split()
+        cls = getattr(bsm, py)
+        got = C.sizeof(cls) if what == "size" else getattr(cls, what).offset
+        if got != int(val):
+            bad.append((py, what, got, int(val)))
+    assert not bad, bad

@@ -293,6 +293,37 @@ parent = 3
             [[objects.components.value.materials]]
             asset_id = 1
 [[objects]]
+name = 'Spot'
+    [[objects.components]]
+    type = 'Transform'
+        [objects.components.value]
+        rotation = [ 0.0, 0.0, 180.0 ]
+        translation = [ 0.0, 4.0, 0.0 ]
+    [[objects.components]]
+    type = 'PointLightComponent'
+        [objects.components.value]
+        color = [ 1.0, 1.0, 1.0 ]
+        strength = 10.0
+        range = 12.0
+        spot = true
+        spot_inner_angle = 20.0
+        spot_outer_angle = 40.0
+[[objects]]
+name = 'Panel'
+    [[objects.components]]
+    type = 'Transform'
+        [objects.components.value]
+        rotation = [ 90.0, 0.0, 0.0 ]
+        translation = [ 1.0, 3.0, 1.0 ]
+    [[objects.components]]
+    type = 'RectLightComponent'
+        [objects.components.value]
+        color = [ 0.5, 0.5, 1.0 ]
+        strength = 2.0
+        width = 2.0
+        height = 0.5
+        two_sided = true
+[[objects]]
 name = 'Override'
     [[objects.components]]
     type = 'BasicRendererOverrideVolume'
@@ -318,7 +349,7 @@ def test_project_loads_into_world_space(bsm, tmp_path):
     P = affine([1, 0, 0], [0, 90, 0], [2, 1, 2])
     Cw = P @ affine([0, 3, 0], [0, 0, 45], [1, 1, 1])
     # parent: submesh 0 (red) and 1 (gold); child: submesh 1 only (materials beyond the submeshes dropped)
-    assert info.num_objects == 6 and info.num_drawables == 3
+    assert info.num_objects == 8 and info.num_drawables == 3
     assert sc.num_triangles == 2 + 1 + 1
     hom = np.c_[q["positions"], np.ones(7)]
     expect_parent = (hom @ P.T)[:, :3]
@@ -338,6 +369,17 @@ def test_project_loads_into_world_space(bsm, tmp_path):
     assert sc.lights.shape == (1, 6)
     assert np.allclose(sc.lights[0, :3], euler_zxy([10, 0, -30]) @ [0, 1, 0], atol=1e-6)
     assert np.allclose(sc.lights[0, 3:], [4.0, 3.6, 3.2])
+    # spot: position = translation, direction = R (0, 1, 0), cone cosines; rect: centre, axes R x / R y
+    assert sc.point_lights.shape == (1, 12)
+    p = sc.point_lights[0]
+    assert np.allclose(p[0:3], [0, 4, 0]) and np.allclose(p[3:6], 10.0) and p[6] == 12.0
+    assert np.allclose(p[7:10], euler_zxy([0, 0, 180]) @ [0, 1, 0], atol=1e-6)
+    assert np.allclose(p[10:12], np.cos(np.radians([20.0, 40.0])))
+    r = sc.rect_lights[0]
+    Rr = euler_zxy([90, 0, 0])
+    assert np.allclose(r[0:3], [1, 3, 1]) and np.allclose(r[3:6], Rr @ [1, 0, 0], atol=1e-6)
+    assert np.allclose(r[6:9], Rr @ [0, 1, 0], atol=1e-6) and tuple(r[9:11]) == (2.0, 0.5)
+    assert np.allclose(r[11:14], [1.0, 1.0, 2.0]) and r[14] == 1
     # camera
     R = euler_zxy([-10, 20, 0])
     assert info.has_camera == 1
@@ -362,7 +404,7 @@ def test_project_errors(bsm, tmp_path):
     root2 = str(tmp_path / "p2")
     write_project(root2, bsm)
     with open(os.path.join(root2, "scene.toml"), "a") as f:
-        f.write("[[objects]]\nname = 'Loop'\nparent = 6\n")   # its own parent
+        f.write("[[objects]]\nname = 'Loop'\nparent = 8\n")   # its own parent (the ninth object)
     with pytest.raises(bsm.BsmError) as e:
         bsm.load_project(root2)
     assert "cycle" in str(e.value)
