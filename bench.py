@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--block", type=int, default=0, help="threads per block of the traversal kernels (0 = tuned)")
     p.add_argument("--capacity", type=int, default=0, help="wavefront paths per chunk (0 = automatic)")
     p.add_argument("--regcap", type=int, default=-1, help="1/0: force the 64-register traversal kernels (-1: tuned)")
+    p.add_argument("--collapse", type=int, default=0, help="BVH collapse: 0 SAH-optimal, 1 greedy")
     p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "cache"],
                    help="plain: the single-frame pass (the bench line); batch: 256 uneven views in one wavefront "
                         "against a loop of plain renders")
@@ -250,7 +251,7 @@ def run_ours(a, dist: Dist):
     ctx = bsm.Context(dist.local)
     t0 = time.perf_counter()
     sid = ctx.upload(scene)
-    bvh = ctx.build_bvh(sid)
+    bvh = ctx.build_bvh(sid, collapse=a.collapse)
     setup_s = time.perf_counter() - t0
     if a.regcap >= 0:
         ctx.set_tuning(sid, bsm.TuneParams(a.block or 128, a.capacity, 16, 8, a.regcap))
@@ -371,7 +372,8 @@ def run_ours(a, dist: Dist):
                 "rays_per_step": {"extend": rays // a.steps, "shadow": shadow_rays // a.steps,
                                   "extend_per_segment": seg_rays},
                 "shadow_mrays_per_s": round(shadow_rays / (ms_shadow / 1e3) / 1e6, 1) if ms_shadow > 0 else None,
-                "bvh": {"build_s_host": round(bvh.build_ms / 1e3, 3), "nodes": bvh.num_nodes,
+                "bvh": {"collapse": "sah-optimal" if a.collapse == 0 else "greedy",
+                        "build_s_host": round(bvh.build_ms / 1e3, 3), "nodes": bvh.num_nodes,
                         "depth": bvh.max_depth, "bytes": bvh.node_bytes + bvh.tri_bytes,
                         "upload_and_build_s": round(setup_s, 3)},
                 "wall_s_timed": round(wall, 3)}

@@ -81,8 +81,12 @@ class SceneDesc(C.Structure):
                 ("rect_lights", C.POINTER(RectLight))]
 
 
+BSM_COLLAPSE_SAH_OPTIMAL, BSM_COLLAPSE_GREEDY = 0, 1
+
+
 class BvhOpts(C.Structure):
-    _fields_ = [("sah_bins", C.c_uint32), ("max_leaf_tris", C.c_uint32), ("num_threads", C.c_uint32)]
+    _fields_ = [("sah_bins", C.c_uint32), ("max_leaf_tris", C.c_uint32), ("num_threads", C.c_uint32),
+                ("collapse", C.c_uint32)]
 
 
 class BvhStats(C.Structure):
@@ -686,11 +690,11 @@ def toml_check(text: str):
         raise BsmError(st, err.value.decode())
 
 
-def bvh_build_host(scene: SceneData, sah_bins=0, max_leaf=0, threads=0):
+def bvh_build_host(scene: SceneData, sah_bins=0, max_leaf=0, threads=0, collapse=0):
     """Host build of the compressed 8-wide BVH: returns (nodes bytes, tris bytes, BvhStats)."""
     L = lib()
     d = scene.desc()
-    o = BvhOpts(sah_bins, max_leaf, threads)
+    o = BvhOpts(sah_bins, max_leaf, threads, collapse)
     s = BvhStats()
     st = L.bsm_bvh_build_host(C.byref(d), C.byref(o), None, 0, None, 0, C.byref(s))
     if st != BSM_OK:
@@ -758,15 +762,15 @@ class Context:
         self.check(self._L.bsm_scene_upload(self.h, C.byref(scene.desc()), C.byref(sid)))
         return sid.value
 
-    def build_bvh(self, scene_id: int, sah_bins=0, max_leaf=0, threads=0) -> BvhStats:
-        o = BvhOpts(sah_bins, max_leaf, threads)
+    def build_bvh(self, scene_id: int, sah_bins=0, max_leaf=0, threads=0, collapse=0) -> BvhStats:
+        o = BvhOpts(sah_bins, max_leaf, threads, collapse)
         s = BvhStats()
         self.check(self._L.bsm_scene_build_bvh(self.h, scene_id, C.byref(o), C.byref(s)))
         return s
 
-    def load_scene(self, scene: SceneData) -> int:
+    def load_scene(self, scene: SceneData, collapse: int = 0) -> int:
         sid = self.upload(scene)
-        self.build_bvh(sid)
+        self.build_bvh(sid, collapse=collapse)
         return sid
 
     def release(self, scene_id: int):

@@ -165,6 +165,72 @@ double sah_cost(const std::vector<BNode>& nodes, uint32_t root) {
     return c;
 }
 
+// SAH-optimal collapse of a binary BVH into an 8-wide one (Ylitie, Karras,
+// Laine 2017, section 3.1): cost(n, i) is the least SAH cost of representing
+// n's subtree as at most i child slots of a wide node,
+//   cost(n, 1) = min(leaf(n), internal(n)),
+//   cost(n, i) = min(cost(n, i - 1), dist(n, i))               for i > 1,
+//   dist(n, j) = min over k of cost(left, k) + cost(right, j - k),
+//   internal(n) = area(n) * kNodeCost + dist(n, 8),
+//   leaf(n) = area(n) * count(n) * kTriCost   (count <= max_leaf).
+// The decisions are kept to expand each wide node's children afterwards.
+struct Collapse {
+    static constexpr double kNodeCost = 1.0;
+    static constexpr double kTriCost = 0.3;   // a triangle test against an 8-child node test
+    static constexpr uint8_t kLeaf = 0xff, kInner = 0xfe, kSame = 0xfd;
+    std::vector<double> cost;                 // 8 per binary node
+    std::vector<uint8_t> dec;                 // 8 per binary node: kLeaf / kInner (slot 0), kSame or k (left share)
+    std::vector<uint8_t> inner_split;         // k of dist(n, 8) for wide nodes
+
+    void run(const std::vector<BNode>& nodes, uint32_t max_leaf) {
+        const size_t n = nodes.size();
+        cost.assign(8 * n, INFINITY);
+        dec.assign(8 * n, kSame);
+        inner_split.assign(n, 4);
+        // children are allocated after their parent: reverse index order is a post-order
+        for (size_t x = n; x-- > 0;) {
+            const BNode& b = nodes[x];
+            double a = b.box.area();
+            double leaf = b.count <= max_leaf ? a * b.count * kTriCost : INFINITY;
+            double* c = &cost[8 * x];
+            uint8_t* d = &dec[8 * x];
+            if (b.leaf) {
+                for (int i = 0; i < 8; ++i) { c[i] = leaf; d[i] = i == 0 ? kLeaf : kSame; }
+                continue;
+            }
+            const double* cl = &cost[8 * (size_t)b.left];
+            const double* cr = &cost[8 * (size_t)b.right];
+            double dist[9];
+            uint8_t arg[9];
+            for (int j = 2; j <= 8; ++j) {
+                dist[j] = INFINITY;
+                arg[j] = 1;
+                for (int k = 1; k < j; ++k) {
+                    double v = cl[k - 1] + cr[j - k - 1];
+                    if (v < dist[j]) { dist[j] = v; arg[j] = (uint8_t)k; }
+                }
+            }
+            double inner = a * kNodeCost + dist[8];
+            inner_split[x] = arg[8];
+            if (leaf <= inner) { c[0] = leaf; d[0] = kLeaf; }
+            else { c[0] = inner; d[0] = kInner; }
+            for (int i = 2; i <= 8; ++i) {
+                if (c[i - 2] <= dist[i]) { c[i - 1] = c[i - 2]; d[i - 1] = kSame; }
+                else { c[i - 1] = dist[i]; d[i - 1] = arg[i]; }
+            }
+        }
+    }
+    // the binary nodes that fill up to i slots for subtree x
+    void gather(const std::vector<BNode>& nodes, uint32_t x, int i, std::vector<uint32_t>& out) const {
+        while (i > 1 && dec[8 * (size_t)x + i - 1] == kSame) --i;
+        if (i == 1) { out.push_back(x); return; }
+        int k = dec[8 * (size_t)x + i - 1];
+        gather(nodes, nodes[x].left, k, out);
+        gather(nodes, nodes[x].right, i - k, out);
+    }
+    bool is_leaf(uint32_t x) const { return dec[8 * (size_t)x] == kLeaf; }
+};
+
 // smallest e with 253 * 2^e >= extent (two steps of margin for the outward
 // padding); returns the biased exponent byte
 int quant_exponent(float extent) {
@@ -187,6 +253,7 @@ bool build_cwbvh(const float* positions, const uint32_t* indices, uint32_t num_t
     if (opts_in) opts = *opts_in;
     uint32_t bins = opts.sah_bins ? std::min(std::max(opts.sah_bins, 4u), 256u) : 32u;
     uint32_t max_leaf = opts.max_leaf_tris ? std::min(opts.max_leaf_tris, 3u) : 3u;
+    const bool optimal = opts.collapse == BSM_COLLAPSE_SAH_OPTIMAL;
     uint32_t threads = opts.num_threads ? opts.num_threads : std::max(1u, std::thread::hardware_concurrency());
 
     auto vtx = [&](uint32_t t, int c, float p[3]) {
@@ -211,12 +278,18 @@ bool build_cwbvh(const float* positions, const uint32_t* indices, uint32_t num_t
     std::vector<BNode> nodes(2 * (size_t)num_tris);
     Builder bld{tri_box, cen, refs, nodes};
     bld.bins = bins;
-    bld.max_leaf = max_leaf;
+    bld.max_leaf = optimal ? 1u : max_leaf;  // the collapse chooses the leaves itself
     bld.threads_free = (int)threads - 1;
     uint32_t root = bld.alloc();
     bld.build(root, 0, num_tris);
     nodes.resize(bld.node_count.load());
     out.sah_cost = sah_cost(nodes, root);
+    Collapse dp;
+    if (optimal) dp.run(nodes, max_leaf);
+    // a binary node becomes one leaf slot
+    auto as_leaf_node = [&](uint32_t x) {
+        return optimal ? dp.is_leaf(x) : (nodes[x].leaf || nodes[x].count <= max_leaf);
+    };
 
     // subtree triangle counts (count is set for every node by build())
     // collapse into 8-wide nodes, breadth first
@@ -250,9 +323,16 @@ bool build_cwbvh(const float* positions, const uint32_t* indices, uint32_t num_t
         // gather up to 8 children
         std::vector<uint32_t> ch;
         const BNode& bn = nodes[it.bnode];
-        if (bn.leaf || bn.count <= max_leaf) ch.push_back(it.bnode);  // root that is a single leaf
-        else { ch.push_back(bn.left); ch.push_back(bn.right); }
-        while (ch.size() < 8) {
+        if (as_leaf_node(it.bnode)) {
+            ch.push_back(it.bnode);  // root that is a single leaf
+        } else if (optimal) {
+            dp.gather(nodes, bn.left, dp.inner_split[it.bnode], ch);
+            dp.gather(nodes, bn.right, 8 - dp.inner_split[it.bnode], ch);
+        } else {
+            ch.push_back(bn.left);
+            ch.push_back(bn.right);
+        }
+        while (!optimal && ch.size() < 8) {
             int best = -1;
             double best_area = -1.0;
             for (size_t i = 0; i < ch.size(); ++i) {
@@ -335,7 +415,7 @@ bool build_cwbvh(const float* positions, const uint32_t* indices, uint32_t num_t
                 qlo[k][s] = (uint8_t)lo;
                 qhi[k][s] = (uint8_t)hi;
             }
-            bool as_leaf = c.leaf || c.count <= max_leaf;
+            bool as_leaf = as_leaf_node(ci);
             if (as_leaf) {
                 uint32_t cnt = c.count;
                 if (cnt == 0 || cnt > 3) { err = "internal error: leaf size"; return false; }
