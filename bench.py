@@ -59,6 +59,9 @@ def parse():
     p.add_argument("--capacity", type=int, default=0, help="wavefront paths per chunk (0 = automatic)")
     p.add_argument("--regcap", type=int, default=-1, help="1/0: force the 64-register traversal kernels (-1: tuned)")
     p.add_argument("--collapse", type=int, default=0, help="BVH collapse: 0 SAH-optimal, 1 greedy")
+    p.add_argument("--tri-cost", type=float, default=0.0, help="SAH-optimal collapse: triangle / node test cost")
+    p.add_argument("--bins", type=int, default=0, help="binned SAH bins (0 = 32)")
+    p.add_argument("--max-leaf", type=int, default=0, help="largest leaf (triangles, 1..3; 0 = 3)")
     p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "cache"],
                    help="plain: the single-frame pass (the bench line); batch: 256 uneven views in one wavefront "
                         "against a loop of plain renders")
@@ -251,7 +254,7 @@ def run_ours(a, dist: Dist):
     ctx = bsm.Context(dist.local)
     t0 = time.perf_counter()
     sid = ctx.upload(scene)
-    bvh = ctx.build_bvh(sid, collapse=a.collapse)
+    bvh = ctx.build_bvh(sid, sah_bins=a.bins, max_leaf=a.max_leaf, collapse=a.collapse, tri_cost=a.tri_cost)
     setup_s = time.perf_counter() - t0
     if a.regcap >= 0:
         ctx.set_tuning(sid, bsm.TuneParams(a.block or 128, a.capacity, 16, 8, a.regcap))

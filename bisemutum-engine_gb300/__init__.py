@@ -86,7 +86,7 @@ BSM_COLLAPSE_SAH_OPTIMAL, BSM_COLLAPSE_GREEDY = 0, 1
 
 class BvhOpts(C.Structure):
     _fields_ = [("sah_bins", C.c_uint32), ("max_leaf_tris", C.c_uint32), ("num_threads", C.c_uint32),
-                ("collapse", C.c_uint32)]
+                ("collapse", C.c_uint32), ("tri_cost", C.c_float)]
 
 
 class BvhStats(C.Structure):
@@ -762,8 +762,8 @@ class Context:
         self.check(self._L.bsm_scene_upload(self.h, C.byref(scene.desc()), C.byref(sid)))
         return sid.value
 
-    def build_bvh(self, scene_id: int, sah_bins=0, max_leaf=0, threads=0, collapse=0) -> BvhStats:
-        o = BvhOpts(sah_bins, max_leaf, threads, collapse)
+    def build_bvh(self, scene_id: int, sah_bins=0, max_leaf=0, threads=0, collapse=0, tri_cost=0.0) -> BvhStats:
+        o = BvhOpts(sah_bins, max_leaf, threads, collapse, tri_cost)
         s = BvhStats()
         self.check(self._L.bsm_scene_build_bvh(self.h, scene_id, C.byref(o), C.byref(s)))
         return s

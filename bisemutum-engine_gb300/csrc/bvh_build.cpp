@@ -176,7 +176,8 @@ double sah_cost(const std::vector<BNode>& nodes, uint32_t root) {
 // The decisions are kept to expand each wide node's children afterwards.
 struct Collapse {
     static constexpr double kNodeCost = 1.0;
-    static constexpr double kTriCost = 0.3;   // a triangle test against an 8-child node test
+    double kTriCost = 1.0;                    // a triangle test against an 8-child node test (measured optimum
+                                              // 0.7-1.4 on the 1.48 M-triangle terrain)
     static constexpr uint8_t kLeaf = 0xff, kInner = 0xfe, kSame = 0xfd;
     std::vector<double> cost;                 // 8 per binary node
     std::vector<uint8_t> dec;                 // 8 per binary node: kLeaf / kInner (slot 0), kSame or k (left share)
@@ -285,6 +286,7 @@ bool build_cwbvh(const float* positions, const uint32_t* indices, uint32_t num_t
     nodes.resize(bld.node_count.load());
     out.sah_cost = sah_cost(nodes, root);
     Collapse dp;
+    if (opts.tri_cost > 0.0f) dp.kTriCost = opts.tri_cost;
     if (optimal) dp.run(nodes, max_leaf);
     // a binary node becomes one leaf slot
     auto as_leaf_node = [&](uint32_t x) {

@@ -170,6 +170,7 @@ typedef struct bsm_bvh_opts {
     uint32_t collapse;        /* binary -> 8-wide: BSM_COLLAPSE_SAH_OPTIMAL (dynamic programming over a
                                  binary tree of single-triangle leaves) or BSM_COLLAPSE_GREEDY (open the
                                  largest child) */
+    float tri_cost;           /* SAH-optimal collapse: cost of a triangle test relative to a node test; 0 = 1.0 */
 } bsm_bvh_opts;
 
 typedef struct bsm_bvh_stats {
