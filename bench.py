@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--block", type=int, default=0, help="threads per block of the traversal kernels (0 = tuned)")
     p.add_argument("--capacity", type=int, default=0, help="wavefront paths per chunk (0 = automatic)")
     p.add_argument("--regcap", type=int, default=-1, help="1/0: force the 64-register traversal kernels (-1: tuned)")
+    p.add_argument("--postpone", type=int, default=-1, help="traversal stack budget for postponed triangle groups")
+    p.add_argument("--refill", type=int, default=-1, help="idle lanes that make a warp fetch new rays")
     p.add_argument("--collapse", type=int, default=0, help="BVH collapse: 0 SAH-optimal, 1 greedy")
     p.add_argument("--tri-cost", type=float, default=0.0, help="SAH-optimal collapse: triangle / node test cost")
     p.add_argument("--bins", type=int, default=0, help="binned SAH bins (0 = 32)")
@@ -256,8 +258,9 @@ def run_ours(a, dist: Dist):
     sid = ctx.upload(scene)
     bvh = ctx.build_bvh(sid, sah_bins=a.bins, max_leaf=a.max_leaf, collapse=a.collapse, tri_cost=a.tri_cost)
     setup_s = time.perf_counter() - t0
-    if a.regcap >= 0:
-        ctx.set_tuning(sid, bsm.TuneParams(a.block or 128, a.capacity, 16, 8, a.regcap))
+    if a.regcap >= 0 or a.postpone >= 0 or a.refill >= 0:
+        ctx.set_tuning(sid, bsm.TuneParams(a.block or 128, a.capacity, a.postpone if a.postpone >= 0 else 16,
+                                           a.refill if a.refill >= 0 else 8, a.regcap if a.regcap >= 0 else 1))
     cam = scene.camera
     seed = a.seed + 1000 * dist.rank
     flags_timed = bsm.BSM_PT_STAGE_TIMING

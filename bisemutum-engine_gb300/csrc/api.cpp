@@ -50,7 +50,7 @@ struct Scene {
     bsm_bvh_stats bvh_stats{};
     bool tuned = false;
     bsm_tune_params tune{};
-    DevBuf nodes, tris, materials, texels, cdf_marg, cdf_cond, pdf_tab;
+    DevBuf nodes, tris, materials, texels, sky_alias, pdf_tab;
     // two-level scenes: instances (caller order), their TLAS leaves, refit data
     bool instanced = false;
     std::vector<bsm_instance> instances;
@@ -177,11 +177,16 @@ bool same_camera(const bsm_camera& a, const bsm_camera& b) { return std::memcmp(
 
 // Sky sampling tables: weights (r + g + b) * sin(theta at the row centre),
 // prefix sums in double, stored as float.
-void build_sky_tables(const bsm_sky& sky, std::vector<float>& marg, std::vector<float>& cond, std::vector<float>& pdf) {
+// Sky sampling tables: texel weights (r + g + b) * sin(theta at the row centre),
+// the pdf of each texel in (u, v) space, and an alias table over the texels
+// (Walker's method with Vose's construction): entry k keeps texel k with
+// probability prob[k] and otherwise gives its alias.  Two words per entry:
+// the bits of prob, the alias.  Sampling is two dependent loads instead of two
+// binary searches over CDFs.
+void build_sky_tables(const bsm_sky& sky, std::vector<uint32_t>& alias, std::vector<float>& pdf) {
     const uint32_t W = sky.width, H = sky.height;
-    marg.assign(H + 1, 0.0f);
-    cond.assign((size_t)H * (W + 1), 0.0f);
-    pdf.assign((size_t)H * W, 0.0f);
+    const size_t N = (size_t)W * H;
+    pdf.assign(N, 0.0f);
     std::vector<double> w((size_t)H * W), rows(H);
     double total = 0.0;
     for (uint32_t i = 0; i < H; ++i) {
@@ -198,23 +203,33 @@ void build_sky_tables(const bsm_sky& sky, std::vector<float>& marg, std::vector<
         rows[i] = rs;
         total += rs;
     }
-    for (uint32_t i = 0; i < H; ++i) {
-        float* c = &cond[(size_t)i * (W + 1)];
-        double acc = 0.0;
-        for (uint32_t j = 0; j < W; ++j) {
-            c[j] = rows[i] > 0.0 ? (float)(acc / rows[i]) : (float)j / (float)W;
-            acc += w[(size_t)i * W + j];
-        }
-        c[W] = 1.0f;
-    }
-    double acc = 0.0;
-    for (uint32_t i = 0; i < H; ++i) {
-        marg[i] = total > 0.0 ? (float)(acc / total) : (float)i / (float)H;
-        acc += rows[i];
-    }
-    marg[H] = 1.0f;
-    for (size_t k = 0; k < (size_t)H * W; ++k)
+    for (size_t k = 0; k < N; ++k)
         pdf[k] = total > 0.0 ? (float)(w[k] * (double)W * (double)H / total) : 0.0f;
+    // Vose: scaled weights q = N w / total; small (q < 1) entries take a large one's excess
+    alias.assign(2 * N, 0u);
+    std::vector<double> q(N);
+    std::vector<uint32_t> small, large;
+    for (size_t k = 0; k < N; ++k) {
+        q[k] = total > 0.0 ? w[k] * (double)N / total : 1.0;
+        (q[k] < 1.0 ? small : large).push_back((uint32_t)k);
+    }
+    auto put = [&](uint32_t k, float prob, uint32_t a) {
+        std::memcpy(&alias[2 * (size_t)k], &prob, 4);
+        alias[2 * (size_t)k + 1] = a;
+    };
+    while (!small.empty() && !large.empty()) {
+        uint32_t sm = small.back();
+        small.pop_back();
+        uint32_t lg = large.back();
+        put(sm, (float)q[sm], lg);
+        q[lg] = (q[lg] + q[sm]) - 1.0;
+        if (q[lg] < 1.0) {
+            large.pop_back();
+            small.push_back(lg);
+        }
+    }
+    for (uint32_t k : large) put(k, 1.0f, k);
+    for (uint32_t k : small) put(k, 1.0f, k);  // rounding leftovers
 }
 
 bsm_status ensure_launch_cfg(bsm_context* ctx, uint32_t block, int regcap = 0) {
@@ -303,7 +318,7 @@ extern "C" void bsm_destroy(bsm_context* ctx) {
     for (auto& g : ctx->graphs) if (g.exec) cudaGraphExecDestroy(g.exec);
     for (auto& kv : ctx->scenes) {
         Scene* s = kv.second.get();
-        for (DevBuf* b : {&s->nodes, &s->tris, &s->materials, &s->texels, &s->cdf_marg, &s->cdf_cond, &s->pdf_tab})
+        for (DevBuf* b : {&s->nodes, &s->tris, &s->materials, &s->texels, &s->sky_alias, &s->pdf_tab})
             dev_free(ctx, *b);
     }
     dev_free(ctx, ctx->wf_buf);
@@ -379,7 +394,7 @@ bsm_status build_tlas(bsm_context* ctx, Scene* sc);
 
 // Device buffers of a scene; an instanced scene also lets go of its geometries.
 void free_scene_buffers(bsm_context* ctx, Scene& sc) {
-    for (DevBuf* b : {&sc.nodes, &sc.tris, &sc.materials, &sc.texels, &sc.cdf_marg, &sc.cdf_cond, &sc.pdf_tab,
+    for (DevBuf* b : {&sc.nodes, &sc.tris, &sc.materials, &sc.texels, &sc.sky_alias, &sc.pdf_tab,
                       &sc.insts, &sc.inst_box, &sc.node_box, &sc.mat_tr})
         dev_free(ctx, *b);
     if (sc.instanced)
@@ -549,21 +564,19 @@ bsm_status setup_shading(bsm_context* ctx, Scene* sc, const bsm_material* materi
     ds.sky.cr = sky.color[0]; ds.sky.cg = sky.color[1]; ds.sky.cb = sky.color[2];
     if (sky.kind == BSM_SKY_EQUIRECT) {
         const uint32_t W = sky.width, H = sky.height;
-        std::vector<float> marg, cond, pdf;
-        build_sky_tables(sky, marg, cond, pdf);
+        std::vector<uint32_t> alias;
+        std::vector<float> pdf;
+        build_sky_tables(sky, alias, pdf);
         size_t tb = (size_t)W * H * 8;
         if ((st = dev_alloc(ctx, sc->texels, tb))) return st;
-        if ((st = dev_alloc(ctx, sc->cdf_marg, marg.size() * 4))) return st;
-        if ((st = dev_alloc(ctx, sc->cdf_cond, cond.size() * 4))) return st;
+        if ((st = dev_alloc(ctx, sc->sky_alias, alias.size() * 4))) return st;
         if ((st = dev_alloc(ctx, sc->pdf_tab, pdf.size() * 4))) return st;
         CK(cudaMemcpy(sc->texels.ptr, sky.rgba16f, tb, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(sc->cdf_marg.ptr, marg.data(), marg.size() * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(sc->cdf_cond.ptr, cond.data(), cond.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->sky_alias.ptr, alias.data(), alias.size() * 4, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(sc->pdf_tab.ptr, pdf.data(), pdf.size() * 4, cudaMemcpyHostToDevice));
         ds.sky.width = W; ds.sky.height = H;
         ds.sky.texels = (const ushort4*)sc->texels.ptr;
-        ds.sky.cdf_marg = (const float*)sc->cdf_marg.ptr;
-        ds.sky.cdf_cond = (const float*)sc->cdf_cond.ptr;
+        ds.sky.alias = (const uint2*)sc->sky_alias.ptr;
         ds.sky.pdf_tab = (const float*)sc->pdf_tab.ptr;
     }
     ds.ray_offset = 2e-5f * sc->extent;
@@ -1006,7 +1019,7 @@ extern "C" bsm_status bsm_scene_device_bytes(bsm_context* ctx, uint32_t scene_id
     Scene* sc = find_scene(ctx, scene_id);
     if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
     uint64_t b = 0;
-    for (DevBuf* x : {&sc->nodes, &sc->tris, &sc->materials, &sc->texels, &sc->cdf_marg, &sc->cdf_cond, &sc->pdf_tab,
+    for (DevBuf* x : {&sc->nodes, &sc->tris, &sc->materials, &sc->texels, &sc->sky_alias, &sc->pdf_tab,
                       &sc->insts, &sc->inst_box, &sc->node_box, &sc->mat_tr})
         b += x->bytes;
     *bytes = b;

@@ -41,8 +41,7 @@ struct DevSky {
     uint32_t width, height;
     float cr, cg, cb;          // colour / multiplier
     const ushort4* texels;     // width*height RGBA16F
-    const float* cdf_marg;     // height + 1
-    const float* cdf_cond;     // height * (width + 1)
+    const uint2* alias;        // height * width alias entries (bits of the keep probability, alias texel)
     const float* pdf_tab;      // height * width: pdf in (u,v) space
 };
 

@@ -257,9 +257,9 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene sc, const DevView* __
         Pcg g;
         g.state = ((uint64_t)m4.w << 32) | m4.z;
         g.inc = ((uint64_t)stream << 1) | 1u;
-        float u_sky0 = 0.0f, u_sky1 = 0.0f, u_lobe = 0.0f, u_b0 = 0.0f, u_b1 = 0.0f;
+        float u_sky0 = 0.0f, u_sky1 = 0.0f, u_sky2 = 0.0f, u_lobe = 0.0f, u_b0 = 0.0f, u_b1 = 0.0f;
         if (is_hit) {
-            u_sky0 = pcg_uniform(g); u_sky1 = pcg_uniform(g); u_lobe = pcg_uniform(g);
+            u_sky0 = pcg_uniform(g); u_sky1 = pcg_uniform(g); u_sky2 = pcg_uniform(g); u_lobe = pcg_uniform(g);
             u_b0 = pcg_uniform(g); u_b1 = pcg_uniform(g);
         }
         // radiance cache: a hit of the cache segment becomes a query (NRC-style
@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene sc, const DevView* __
         float p_spec = spec_probability(surf, lv.z);
         // next-event estimation towards the lights (lights.hlsl:10-25; rect lights sampled by area),
         // deferred_lighting_secondary.hlsl:51-96.  Rect lights draw their two uniforms here, after
-        // the vertex's five, in light order.
+        // the vertex's six, in light order.
         for (uint32_t l = 0; l < (uint32_t)kMaxLights; ++l) {
             if (l >= sc.num_lights) break;
             const DevLight& lt = sc.lights[l];
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(DevScene sc, const DevView* __
             if (is_hit && sky_nee) {
                 float pl;
                 V3 le;
-                L = sky_sample(sc.sky, u_sky0, u_sky1, pl, le);
+                L = sky_sample(sc.sky, u_sky0, u_sky1, u_sky2, pl, le);
                 if (pl > 0.0f) {
                     V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
                     if (max_comp(f) > 0.0f) {

@@ -6,9 +6,9 @@
 // rays and adds next-event estimation towards the sky:
 //   constant sky: uniform sphere directions, pdf 1 / (4 pi);
 //   equirect sky: piecewise-constant 2-D distribution over texels weighted by
-//     (r + g + b) * sin(theta at the row centre); the marginal CDF picks a row,
-//     the row's conditional CDF a column, and the remainders place the
-//     direction inside the texel.  pdf(omega) = p_uv / (2 pi^2 sin theta).
+//     (r + g + b) * sin(theta at the row centre); an alias table (Walker,
+//     Vose's construction) picks a texel in two loads, and two uniforms place
+//     the direction inside it.  pdf(omega) = p_uv / (2 pi^2 sin theta).
 // Equirect convention: row 0 looks at +y, column j spans azimuth
 // phi = 2 pi (j / W - 0.5) .. 2 pi ((j + 1) / W - 0.5), phi = atan2(z, x).
 #pragma once
@@ -18,22 +18,6 @@
 namespace bsm {
 
 #define BSM_TWO_PI_SQR 19.7392082f
-
-BSM_HD uint32_t cdf_search(const float* cdf, uint32_t n, float u) {
-    // largest i in [0, n-1] with cdf[i] <= u (cdf has n + 1 entries, cdf[0] = 0, cdf[n] = 1)
-    uint32_t lo = 0, hi = n - 1;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi + 1) >> 1;
-        if (cdf[mid] <= u) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
-BSM_HD float cdf_remainder(const float* cdf, uint32_t i, float u) {
-    float w = cdf[i + 1] - cdf[i];
-    float f = w > 0.0f ? (u - cdf[i]) / w : 0.5f;
-    return fminf(fmaxf(f, 0.0f), 0.99999994f);
-}
 
 __device__ __forceinline__ V3 texel_rgb(const DevSky& s, uint32_t i, uint32_t j) {
     ushort4 t = s.texels[(size_t)i * s.width + j];
@@ -69,18 +53,33 @@ __device__ __forceinline__ float sky_pdf(const DevSky& s, V3 d) {
     return s.pdf_tab[(size_t)i * s.width + j] / (BSM_TWO_PI_SQR * st);
 }
 
-// Samples a sky direction; returns pdf 0 when nothing can be sampled.
-__device__ __forceinline__ V3 sky_sample(const DevSky& s, float u0, float u1, float& pdf, V3& le) {
+// Samples a sky direction; returns pdf 0 when nothing can be sampled.  An
+// equirect sky picks a texel with the alias table (u0: the entry, u1: keep or
+// alias, its remainder the row position inside the texel; u2: the column
+// position), then the direction inside the texel.
+__device__ __forceinline__ V3 sky_sample(const DevSky& s, float u0, float u1, float u2, float& pdf, V3& le) {
     if (s.kind == 0u) {
         pdf = BSM_INV_FOUR_PI;
         le = v3(s.cr, s.cg, s.cb);
         return uniform_sphere_sample(u0, u1);
     }
-    uint32_t i = cdf_search(s.cdf_marg, s.height, u0);
-    float fy = cdf_remainder(s.cdf_marg, i, u0);
-    const float* row = s.cdf_cond + (size_t)i * (s.width + 1);
-    uint32_t j = cdf_search(row, s.width, u1);
-    float fx = cdf_remainder(row, j, u1);
+    const uint32_t n = s.width * s.height;
+    uint32_t k = (uint32_t)(u0 * (float)n);
+    k = k < n ? k : n - 1u;
+    uint2 e = s.alias[k];
+    float keep = __uint_as_float(e.x);
+    uint32_t t;
+    float fy;
+    if (u1 < keep) {
+        t = k;
+        fy = u1 / keep;
+    } else {
+        t = e.y;
+        fy = (u1 - keep) / (1.0f - keep);
+    }
+    fy = fminf(fmaxf(fy, 0.0f), 0.99999994f);
+    float fx = u2;
+    uint32_t i = t / s.width, j = t - i * s.width;
     float st, ct, sp, cp;
     sincos_turns(((float)i + fy) / (2.0f * (float)s.height), &st, &ct);
     sincos_turns(((float)j + fx) / (float)s.width - 0.5f, &sp, &cp);

@@ -80,8 +80,8 @@ __global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView*
         int k = nv++;
         Frame fr = create_frame(N);
         V3 org = P + N * sc.ray_offset;
-        float u_sky0 = pcg_uniform(g), u_sky1 = pcg_uniform(g), u_lobe = pcg_uniform(g), u_b0 = pcg_uniform(g),
-              u_b1 = pcg_uniform(g);
+        float u_sky0 = pcg_uniform(g), u_sky1 = pcg_uniform(g), u_sky2 = pcg_uniform(g), u_lobe = pcg_uniform(g),
+              u_b0 = pcg_uniform(g), u_b1 = pcg_uniform(g);
         float rx, ry;
         aniso_roughness(surf.roughness, &rx, &ry);
         V3 lv = to_local(fr, V);
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView*
         {
             float pl;
             V3 le;
-            V3 L = sky_sample(sc.sky, u_sky0, u_sky1, pl, le);
+            V3 L = sky_sample(sc.sky, u_sky0, u_sky1, u_sky2, pl, le);
             if (pl > 0.0f) {
                 V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
                 if (max_comp(f) > 0.0f) {

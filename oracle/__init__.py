@@ -60,6 +60,7 @@ def lib() -> C.CDLL:
         L.orc_scene_create_instanced.argtypes = [vp, u32, vp, vp, vp, u32, vp, u32, vp, u32, u32, vp, u32, u32, vp,
                                                  vp, C.POINTER(vp)]
         L.orc_scene_create_instanced.restype = i32
+        L.orc_sky_sample.argtypes = [vp, vp, u32, vp]
         L.orc_scene_bvh_nodes.argtypes = [vp]
         L.orc_scene_bvh_nodes.restype = u32
         _lib = L
@@ -222,6 +223,14 @@ class OracleScene:
         if st != 0:
             raise RuntimeError("orc_primary failed")
         return depth, gb, hp
+
+
+    def sky_sample(self, u: np.ndarray) -> np.ndarray:
+        """(n, 3) uniforms -> (n, 5): sampled direction, its pdf, and sky_pdf of that direction."""
+        u = _f32(u).reshape(-1, 3)
+        out = np.zeros((u.shape[0], 5), np.float32)
+        self._L.orc_sky_sample(self.h, u.ctypes.data, u.shape[0], out.ctypes.data)
+        return out
 
 
 def pcg32(initstate: int, initseq: int, n: int) -> np.ndarray:

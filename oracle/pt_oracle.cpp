@@ -254,7 +254,8 @@ struct Scene {
     F3 sky_color{0, 0, 0};
     uint32_t sw = 0, sh = 0;
     std::vector<uint16_t> texels;
-    std::vector<float> cmarg, ccond, ptab;
+    std::vector<float> ptab, aprob;   // sky: pdf per texel, alias keep probability
+    std::vector<uint32_t> alias;
     float extent = 1.0f, offset = 0.0f;
     // two-level scenes: instances of geometries (each a Scene holding tris + BVH only)
     struct Inst {
@@ -536,19 +537,6 @@ static void hit_geom(const Scene& S, uint32_t leaf, uint32_t inst, F3& ng, F3& e
 }
 
 // ------------------------------------------------------------------ sky ----
-static uint32_t cdf_search(const float* cdf, uint32_t n, float u) {
-    uint32_t lo = 0, hi = n - 1;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi + 1) >> 1;
-        if (cdf[mid] <= u) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-static float cdf_rem(const float* cdf, uint32_t i, float u) {
-    float w = cdf[i + 1] - cdf[i];
-    float f = w > 0.0f ? (u - cdf[i]) / w : 0.5f;
-    return std::fmin(std::fmax(f, 0.0f), 0.99999994f);
-}
 static F3 texel(const Scene& S, uint32_t i, uint32_t j) {
     const uint16_t* t = &S.texels[((size_t)i * S.sw + j) * 4];
     return f3(half_to_float(t[0]) * S.sky_color.x, half_to_float(t[1]) * S.sky_color.y, half_to_float(t[2]) * S.sky_color.z);
@@ -578,13 +566,21 @@ static float sky_pdf(const Scene& S, F3 d) {
     if (!(st > 0.0f)) return 0.0f;
     return S.ptab[(size_t)i * S.sw + j] / (kTwoPiSq * st);
 }
-static F3 sky_sample(const Scene& S, float u0, float u1, float& pdf, F3& le) {
+// Equirect sky: the alias table picks a texel (u0: entry, u1: keep or alias and,
+// rescaled, the row position in the texel; u2: the column position).
+static F3 sky_sample(const Scene& S, float u0, float u1, float u2, float& pdf, F3& le) {
     if (S.sky_kind == 0) { pdf = 0.0795774683f; le = S.sky_color; return sphere_sample(u0, u1); }
-    uint32_t i = cdf_search(S.cmarg.data(), S.sh, u0);
-    float fy = cdf_rem(S.cmarg.data(), i, u0);
-    const float* row = S.ccond.data() + (size_t)i * (S.sw + 1);
-    uint32_t j = cdf_search(row, S.sw, u1);
-    float fx = cdf_rem(row, j, u1);
+    const uint32_t n = S.sw * S.sh;
+    uint32_t k = (uint32_t)(u0 * (float)n);
+    k = k < n ? k : n - 1u;
+    float keep = S.aprob[k];
+    uint32_t t;
+    float fy;
+    if (u1 < keep) { t = k; fy = u1 / keep; }
+    else { t = S.alias[k]; fy = (u1 - keep) / (1.0f - keep); }
+    fy = std::fmin(std::fmax(fy, 0.0f), 0.99999994f);
+    float fx = u2;
+    uint32_t i = t / S.sw, j = t - i * S.sw;
     float st, ct, sp, cp;
     sincos_turns(((float)i + fy) / (2.0f * (float)S.sh), &st, &ct);
     sincos_turns(((float)j + fx) / (float)S.sw - 0.5f, &sp, &cp);
@@ -594,11 +590,13 @@ static F3 sky_sample(const Scene& S, float u0, float u1, float& pdf, F3& le) {
     le = texel(S, i, j);
     return d;
 }
+// Texel weights (r + g + b) sin(theta), pdf table, and the alias table (Walker's
+// method, Vose's construction: small entries, taken from the back, borrow the
+// excess of the last large one).
 static void build_sky(Scene& S) {
     const uint32_t W = S.sw, H = S.sh;
-    S.cmarg.assign(H + 1, 0.0f);
-    S.ccond.assign((size_t)H * (W + 1), 0.0f);
-    S.ptab.assign((size_t)H * W, 0.0f);
+    const size_t N = (size_t)W * H;
+    S.ptab.assign(N, 0.0f);
     std::vector<double> w((size_t)H * W), rows(H);
     double total = 0.0;
     for (uint32_t i = 0; i < H; ++i) {
@@ -615,23 +613,29 @@ static void build_sky(Scene& S) {
         rows[i] = rs;
         total += rs;
     }
-    for (uint32_t i = 0; i < H; ++i) {
-        float* c = &S.ccond[(size_t)i * (W + 1)];
-        double acc = 0.0;
-        for (uint32_t j = 0; j < W; ++j) {
-            c[j] = rows[i] > 0.0 ? (float)(acc / rows[i]) : (float)j / (float)W;
-            acc += w[(size_t)i * W + j];
-        }
-        c[W] = 1.0f;
-    }
-    double acc = 0.0;
-    for (uint32_t i = 0; i < H; ++i) {
-        S.cmarg[i] = total > 0.0 ? (float)(acc / total) : (float)i / (float)H;
-        acc += rows[i];
-    }
-    S.cmarg[H] = 1.0f;
-    for (size_t k = 0; k < (size_t)H * W; ++k)
+    for (size_t k = 0; k < N; ++k)
         S.ptab[k] = total > 0.0 ? (float)(w[k] * (double)W * (double)H / total) : 0.0f;
+    S.aprob.assign(N, 1.0f);
+    S.alias.assign(N, 0u);
+    std::vector<double> q(N);
+    std::vector<uint32_t> small, large;
+    for (size_t k = 0; k < N; ++k) {
+        q[k] = total > 0.0 ? w[k] * (double)N / total : 1.0;
+        (q[k] < 1.0 ? small : large).push_back((uint32_t)k);
+        S.alias[k] = (uint32_t)k;
+    }
+    while (!small.empty() && !large.empty()) {
+        uint32_t sm = small.back();
+        small.pop_back();
+        uint32_t lg = large.back();
+        S.aprob[sm] = (float)q[sm];
+        S.alias[sm] = lg;
+        q[lg] = (q[lg] + q[sm]) - 1.0;
+        if (q[lg] < 1.0) {
+            large.pop_back();
+            small.push_back(lg);
+        }
+    }
 }
 
 // --------------------------------------------------------- wavefront ----
@@ -761,8 +765,8 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                 Frm fr = make_frame(N);
                 F3 V = neg(d);
                 Pcg g = q.rng[i];
-                float us0 = pcg_uniform(g), us1 = pcg_uniform(g), ul = pcg_uniform(g), ub0 = pcg_uniform(g),
-                      ub1 = pcg_uniform(g);
+                float us0 = pcg_uniform(g), us1 = pcg_uniform(g), us2 = pcg_uniform(g), ul = pcg_uniform(g),
+                      ub0 = pcg_uniform(g), ub1 = pcg_uniform(g);
                 F3 org = add(P, muls(N, S.offset));
                 float rx, ry;
                 aniso_rough(surf.rough, &rx, &ry);
@@ -771,7 +775,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                 for (uint32_t l = 0; l < S.nlights; ++l) {  // deferred_lighting_secondary.hlsl:51-96
                     const Scene::Light& Lt = S.lights[l];
                     float ur0 = 0.0f, ur1 = 0.0f;
-                    if (Lt.kind == 2) { ur0 = pcg_uniform(g); ur1 = pcg_uniform(g); }  // after the vertex's five
+                    if (Lt.kind == 2) { ur0 = pcg_uniform(g); ur1 = pcg_uniform(g); }  // after the vertex's six
                     if (st.flags & F_NO_SUN) continue;
                     F3 L, e;
                     float smax;
@@ -787,7 +791,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                 if (!(st.flags & F_NO_SKY)) {
                     float pl;
                     F3 le;
-                    F3 L = sky_sample(S, us0, us1, pl, le);
+                    F3 L = sky_sample(S, us0, us1, us2, pl, le);
                     if (pl > 0.0f) {
                         F3 f = eval_lit(N, fr.x, fr.y, V, L, surf);
                         if (maxc(f) > 0.0f) {
@@ -1361,6 +1365,19 @@ ORC_API void orc_gbuffer_pack(const float* in, uint32_t n, float* out) {
                      a[15], out + 16 * (size_t)i);
     }
 }
+// Sky samples for the unit tests: u (n x 3 uniforms) -> direction, pdf, and the
+// pdf the sky reports for that direction (n x 5).
+ORC_API void orc_sky_sample(void* sp, const float* u, uint32_t n, float* out) {
+    const Scene& S = *(const Scene*)sp;
+    for (uint32_t i = 0; i < n; ++i) {
+        float pdf;
+        F3 le;
+        F3 d = sky_sample(S, u[3 * i], u[3 * i + 1], u[3 * i + 2], pdf, le);
+        float* o = out + 5 * (size_t)i;
+        o[0] = d.x; o[1] = d.y; o[2] = d.z; o[3] = pdf; o[4] = sky_pdf(S, d);
+    }
+}
+
 ORC_API uint32_t orc_scene_bvh_nodes(void* sp) { return (uint32_t)((Scene*)sp)->nodes.size(); }
 
 // ===================================================== radiance-cache MLP ====

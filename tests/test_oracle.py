@@ -194,3 +194,33 @@ def test_oracle_ties_at_shared_vertices_equal_brute_force(bsm, oracle):
     h = oracle.OracleScene(sc).trace(rays)
     t, p = watertight_brute(sc.positions[sc.indices].astype(np.float32), rays)
     assert np.array_equal(h[:, 1], p)
+
+
+def test_sky_alias_sampling_matches_its_pdf(bsm, oracle):
+    """Texels are chosen with the probabilities the sky's weights give (chi-square over texels), and the
+    returned pdf equals sky_pdf of the sampled direction."""
+    sc = bsm.generate_scene(bsm.BSM_SCENE_TERRAIN, seed=5, grid=16, spheres=4, sky_width=32, sky_height=16)
+    osc = oracle.OracleScene(sc)
+    n = 400000
+    u = np.random.default_rng(1).uniform(0.0, 1.0, (n, 3)).astype(np.float32)
+    s = osc.sky_sample(u)
+    d, pdf, pdf2 = s[:, :3].astype(np.float64), s[:, 3], s[:, 4]
+    ok = pdf > 0
+    assert ok.mean() > 0.999
+    # a direction rounded onto a texel boundary may be looked up in the neighbouring texel
+    assert np.mean(np.abs(pdf[ok] - pdf2[ok]) > 1e-5 * pdf2[ok]) < 1e-4
+    # texel of each direction (row from theta about +y, column from phi = atan2(z, x))
+    H, W = 16, 32
+    th = np.arccos(np.clip(d[:, 1], -1, 1))
+    ph = np.arctan2(d[:, 2], d[:, 0])
+    i = np.clip((th / np.pi * H).astype(int), 0, H - 1)
+    j = np.clip(((ph / (2 * np.pi) + 0.5) * W).astype(int), 0, W - 1)
+    counts = np.bincount(i * W + j, minlength=H * W).astype(np.float64)
+    # texel probabilities from the sky's own weights (r + g + b) * sin(theta at the row centre)
+    tex = sc.sky_texels.view(np.float16).astype(np.float64)
+    w = tex[..., :3].sum(-1) * np.sin(np.pi * (np.arange(H) + 0.5) / H)[:, None]
+    p = (w / w.sum()).ravel()
+    expect = p * n
+    m = expect > 20
+    chi2 = float(((counts[m] - expect[m]) ** 2 / expect[m]).sum())
+    assert chi2 < 1.3 * m.sum(), (chi2, m.sum())
