@@ -556,11 +556,8 @@ def run_cache(a, dist):
     spps = [1, 2, 4, 8, 16, 32, 64]
     seeds = 3
 
-    def trimmed(img, r, q=0.999):
-        a = img[..., :3].astype(np.float64)
-        b = r[..., :3].astype(np.float64)
-        e = ((a - b) ** 2 / (b * b + 1e-2)).ravel()
-        return float(np.mean(np.sort(e)[: int(q * e.size)]))
+    def trimmed(img, r):
+        return bsm.rel_mse(img, r, trim=0.001)
 
     plain = []
     for spp in spps:

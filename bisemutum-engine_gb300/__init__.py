@@ -1045,11 +1045,15 @@ class RadianceCache:
         return img, st, loss.value
 
 
-def rel_mse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
-    """Relative MSE over pixels and RGB: mean((I - R)^2 / (R^2 + eps))."""
+def rel_mse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2, trim: float = 0.0) -> float:
+    """Relative MSE over pixels and RGB: mean((I - R)^2 / (R^2 + eps)); `trim` drops that fraction of the
+    largest per-value errors first (fireflies dominate single-frame relMSE)."""
     a = img[..., :3].astype(np.float64)
     b = ref[..., :3].astype(np.float64)
-    return float(np.mean((a - b) ** 2 / (b * b + eps)))
+    e = ((a - b) ** 2 / (b * b + eps)).ravel()
+    if trim > 0.0:
+        e = np.sort(e)[: max(1, int(round(e.size * (1.0 - trim))))]
+    return float(np.mean(e))
 
 
 # -------------------------------------------------- reference-shaped API ----

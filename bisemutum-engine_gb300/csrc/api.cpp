@@ -1001,7 +1001,28 @@ extern "C" bsm_status bsm_scene_update_instances(bsm_context* ctx, uint32_t scen
         std::memcpy(sc->instances[i].transform, transforms + 12 * (size_t)i, 12 * sizeof(float));
     std::vector<float> boxes;
     fill_instances(ctx, sc, boxes);
+    // the scene bounds (ray offset, radiance-cache normalisation) follow the instances, as a rebuild's would
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t l = 0; l < sc->inst_host.size(); ++l)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], boxes[6 * l + k]);
+            hi[k] = std::max(hi[k], boxes[6 * l + 3 + k]);
+        }
+    float extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
+    DevScene& ds = sc->dev;
+    bool moved_bounds = extent != sc->extent;
+    for (int k = 0; k < 3; ++k)
+        moved_bounds = moved_bounds || ds.box_lo[k] != lo[k] || ds.box_inv[k] != 1.0f / std::max(hi[k] - lo[k], 1e-6f);
     CK(cudaStreamSynchronize(ctx->stream));  // no render may read the records while they change
+    if (moved_bounds) {
+        sc->extent = extent;
+        ds.ray_offset = 2e-5f * extent;
+        for (int k = 0; k < 3; ++k) {
+            ds.box_lo[k] = lo[k];
+            ds.box_inv[k] = 1.0f / std::max(hi[k] - lo[k], 1e-6f);
+        }
+        clear_graphs(ctx);  // captured launches hold the scene record by value
+    }
     CK(cudaMemcpyAsync(sc->insts.ptr, sc->inst_host.data(), sc->inst_host.size() * sizeof(InstDev),
                        cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(sc->inst_box.ptr, boxes.data(), boxes.size() * 4, cudaMemcpyHostToDevice, ctx->stream));

@@ -553,8 +553,9 @@ BSM_API bsm_status bsm_scene_create_instanced(bsm_context* ctx, const bsm_instan
  * and a refit of the TLAS on the GPU: the world boxes change, the tree's
  * topology stays (the reference rebuilds its TLAS every frame,
  * accel.cpp:139-158; a refit keeps the per-frame cost to one small kernel per
- * TLAS level).  The scene bounds used for ray offsets stay those of creation.
- * Synchronous. */
+ * TLAS level).  The scene bounds (ray offsets, radiance-cache inputs) follow
+ * the new instance boxes, as after a rebuild; when they change, the next
+ * render re-captures its CUDA graph.  Synchronous. */
 BSM_API bsm_status bsm_scene_update_instances(bsm_context* ctx, uint32_t scene_id, const float* transforms,
                                               uint32_t num_instances);
 

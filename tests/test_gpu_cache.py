@@ -100,7 +100,8 @@ def test_trained_cache_gains_over_the_method_without_it(bsm, ctx):
     """Paths end at their third vertex in both renders; with the trained network
     that vertex contributes the learned outgoing radiance, without it (a network
     whose output layer is zero) it contributes nothing.  The trained cache must be
-    much closer to a 512-spp plain render."""
+    much closer to a 512-spp plain render (relMSE with the largest 0.1 % of the
+    errors dropped)."""
     scene = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=41, spheres=24)
     sid = ctx.load_scene(scene)
     cam = bsm.make_camera(tuple(scene.camera.position), tuple(scene.camera.front), width=96, height=96)
@@ -118,8 +119,10 @@ def test_trained_cache_gains_over_the_method_without_it(bsm, ctx):
         cs_eval = bsm.cache_settings(train_steps=0, cache_segment=2)
         cached, st, _ = c.render(sid, cam, bsm.settings(spp=64, seed=77), cs_eval)
         without, _, _ = off.render(sid, cam, bsm.settings(spp=64, seed=77), cs_eval)
-        e_cached = bsm.rel_mse(cached, ref)
-        e_without = bsm.rel_mse(without, ref)
+        # trimmed relMSE: a single firefly shared by both renders (same paths up to the cache vertex)
+        # otherwise decides the comparison
+        e_cached = bsm.rel_mse(cached, ref, trim=0.001)
+        e_without = bsm.rel_mse(without, ref, trim=0.001)
         assert np.isfinite(cached).all()
         assert st.rays_per_segment[3] == 0           # no path goes past the cache vertex
         assert np.mean(losses[-10:]) < np.mean(losses[:10])
