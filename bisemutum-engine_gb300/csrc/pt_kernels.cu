@@ -75,7 +75,7 @@ __global__ void k_camera(const DevView* __restrict__ views, uint32_t n_views, ui
     uint32_t sample = (uint32_t)(local / npix);
     uint32_t pixel = (uint32_t)(local - (uint64_t)sample * npix);
     uint32_t px = pixel % v.width, py = pixel / v.width;
-    Pcg g = pcg_seed(sample_initstate(v.seed, v.sample_offset + sample), (uint64_t)pixel);
+    Pcg g = pcg_seed(path_initstate(v.seed, v.sample_offset + sample, pixel), (uint64_t)pixel);
     float jx = 0.5f, jy = 0.5f;
     if (v.flags & BSM_PT_JITTER) { jx = pcg_uniform(g); jy = pcg_uniform(g); }
     V3 dw = camera_dir(v, px, py, jx, jy);
@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(256) k_primary(DevScene sc, DevView v, float n
     RayPre r = make_ray(make_float4(eye.x, eye.y, eye.z, v.t_min), make_float4(dw.x, dw.y, dw.z, v.ray_length));
     float t, hu, hv;
     // opacity decisions of sample 0 of an unjittered render (its camera-ray PCG word)
-    Pcg pg = pcg_seed(sample_initstate(v.seed, v.sample_offset), (uint64_t)i);
+    Pcg pg = pcg_seed(path_initstate(v.seed, v.sample_offset, i), (uint64_t)i);
     uint32_t inst;
     uint32_t leaf = trace_scene<false>(sc, r, v.ray_length, t, hu, hv, inst, (uint32_t)pg.state);
     float g[16];

@@ -124,6 +124,10 @@ static uint64_t mix64(uint64_t z) {
 static uint64_t sample_initstate(uint64_t seed, uint32_t sample) {
     return mix64(seed + 0x9e3779b97f4a7c15ULL * ((uint64_t)sample + 1u));
 }
+// per-path start state: the pixel mixed into the sample's state (decorrelates the streams)
+static uint64_t path_initstate(uint64_t seed, uint32_t sample, uint64_t pixel) {
+    return mix64(sample_initstate(seed, sample) ^ mix64(pixel * 0x9e3779b97f4a7c15ULL + 0x632be59bd9b4e019ULL));
+}
 
 // -------------------------------------------------- reference BSDF ----
 static const float kInvPi = 0.318309873f;
@@ -719,7 +723,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
         // camera (generate_camera_ray.hlsl:9-15)
         for (uint32_t p = pix_begin; p < pix_end; ++p) {
             uint32_t px = p % K.w, py = p / K.w;
-            Pcg g = pcg_seed(sample_initstate(st.seed, st.sample_offset + s), (uint64_t)p);
+            Pcg g = pcg_seed(path_initstate(st.seed, st.sample_offset + s, p), (uint64_t)p);
             float jx = 0.5f, jy = 0.5f;
             if (st.flags & F_JITTER) { jx = pcg_uniform(g); jy = pcg_uniform(g); }
             float uvx = ((float)px + jx) / (float)K.w;
@@ -1283,7 +1287,7 @@ ORC_API int orc_primary(void* sp, const float* camera, float ray_length, float t
                 F3 dl = norm3(f3(ndx * K.aspect * K.tan_half, ndy * K.tan_half, -1.0f));
                 F3 dw = norm3(add(add(muls(K.s, dl.x), muls(K.u, dl.y)), muls(neg(K.f), dl.z)));
                 // opacity decisions of sample 0 of an unjittered render
-                Pcg pg = pcg_seed(sample_initstate(seed, sample_offset), (uint64_t)p);
+                Pcg pg = pcg_seed(path_initstate(seed, sample_offset, p), (uint64_t)p);
                 Ray r = make_ray(K.pos, t_min, dw, ray_length, (uint32_t)pg.state);
                 float t, u, v;
                 uint32_t hi;
