@@ -83,7 +83,7 @@ def workload_config(a, tris=None):
     return {"workload": f"terrain fBm {a.grid}x{a.grid} + {a.spheres} UV spheres, {a.width}x{a.height}, "
                         f"{a.spp} spp, {a.segments} segments",
             "scene_triangles": tris, "width": a.width, "height": a.height, "spp": a.spp,
-            "max_segments": a.segments, "sky": "1024x512 RGBA16F equirect + 2-D CDF", "seed": a.seed,
+            "max_segments": a.segments, "sky": "1024x512 RGBA16F equirect + alias table", "seed": a.seed,
             "parallelism": "replicas" if a.gpus > 1 else "single GPU",
             "l2": "inputs larger than L2 (wavefront queues ~2 GB per chunk) and a 512 MB device copy "
                   "between timed steps flushes L2"}
