@@ -3,7 +3,7 @@
 
 Workload (the plain pass at scale): the procedural terrain scene of 1,482,242
 triangles (512 x 512-vertex fBm heightfield + 2000 UV spheres, gradient sky
-baked to a 1024 x 512 RGBA16F equirect map with an importance-sampling CDF, one
+baked to a 1024 x 512 RGBA16F equirect map with an importance-sampling alias table, one
 sun), rendered at 1920 x 1080, 64 spp, 8 extend segments (primary + 7
 bounces), fp32 accumulation.  A step is one full frame.  Inputs are synthetic
 and seeded (no dataset exists for this pass).
@@ -521,15 +521,56 @@ def run_serve(a, dist):
                         "p99_ms": round(float(np.percentile(lat, 99)), 2),
                         "mean_ms": round(float(lat.mean()), 2), "completed_req_s": round(n / wall, 2),
                         "mrays_per_s": round(ss.extend_rays / wall / 1e6, 1), "wall_s": round(wall, 2)})
+    saturated = serve_saturated(a, bsm, ctx, ids, scenes, rng)
     ctx.close()
     line = {"workload": "serve", "metric": "p50/p99 request latency and rays/s per Poisson arrival rate",
-            "scenes_triangles": tris, "setup_s": round(setup_s, 1), "results": results,
+            "scenes_triangles": tris, "setup_s": round(setup_s, 1), "results": results, "saturated": saturated,
             "request_mix": "scene uniform, resolution log-uniform 128x128..1920x1080, spp {1,4,16,32}, "
                            "bounces {2,4,8}", "server": {"pool_bytes": 16 << 30, "chunk_paths": 1 << 21,
                                                           "lanes": 4}}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def serve_saturated(a, bsm, ctx, ids, scenes, rng, n=240):
+    """Serving efficiency at saturation: n requests of the same mix submitted at once, against the same
+    views rendered by one bsm_render_batch call per scene (same spp, bounces and seeds, so the same paths);
+    both include the copy of every result to host memory."""
+    reqs = []
+    for i in range(n):
+        k = int(rng.integers(0, 4))
+        u = float(rng.uniform())
+        w = int(round(128 * (1920 / 128) ** u))
+        h = int(round(128 * (1080 / 128) ** u))
+        base = scenes[k].camera
+        cam = bsm.make_camera(tuple(base.position), tuple(base.front), width=w, height=h)
+        reqs.append((k, cam, int(rng.choice([1, 4, 16, 32])), int(rng.choice([2, 4, 8])), int(i + 1)))
+    ctx.server_start(pool_bytes=16 << 30, chunk_paths=1 << 21, lanes=4)
+    ctx.sync()
+    t0 = time.perf_counter()
+    rids = [ctx.submit(ids[k], cam, spp, segs, seed)[0] for k, cam, spp, segs, seed in reqs]
+    for rid in rids:
+        ctx.wait(rid, timeout_ms=600000)
+    serve_s = time.perf_counter() - t0
+    rays = ctx.server_stats().extend_rays
+    ctx.server_stop()
+    s = bsm.settings(spp=1, max_segments=8)
+    groups = [[(cam, spp, segs, seed) for k2, cam, spp, segs, seed in reqs if k2 == k] for k in range(4)]
+    for k in range(4):  # warm-up: graphs and buffers of each scene
+        if groups[k]:
+            ctx.render_batch(ids[k], groups[k][:2], s, outputs=False)
+    ctx.sync()
+    t0 = time.perf_counter()
+    brays = 0
+    for k in range(4):
+        if groups[k]:
+            _, st = ctx.render_batch(ids[k], groups[k], s)
+            brays += st.extend_rays
+    batch_s = time.perf_counter() - t0
+    return {"requests": n, "serve_s": round(serve_s, 3), "serve_mrays_per_s": round(rays / serve_s / 1e6, 1),
+            "batch_s": round(batch_s, 3), "batch_mrays_per_s": round(brays / batch_s / 1e6, 1),
+            "same_rays": bool(rays == brays), "efficiency": round(batch_s / serve_s, 3)}
 
 
 # ----------------------------------------------------------------- cache ----

@@ -62,6 +62,8 @@ def lib() -> C.CDLL:
         L.orc_scene_create_instanced.restype = i32
         L.orc_sky_sample.argtypes = [vp, vp, u32, vp]
         L.orc_scene_bvh_nodes.argtypes = [vp]
+        L.orc_cwbvh_trace.argtypes = [vp, u64, vp, u64, vp, u32, i32, vp, vp, i32]
+        L.orc_cwbvh_trace.restype = i32
         L.orc_scene_bvh_nodes.restype = u32
         _lib = L
     return _lib
@@ -231,6 +233,24 @@ class OracleScene:
         out = np.zeros((u.shape[0], 5), np.float32)
         self._L.orc_sky_sample(self.h, u.ctypes.data, u.shape[0], out.ctypes.data)
         return out
+
+
+def cwbvh_trace(nodes: np.ndarray, tris: np.ndarray, rays: np.ndarray, any_hit: bool = False, threads: int = 0):
+    """Traverses the product's compressed BVH (raw node and triangle bytes) with
+    the device kernel's arithmetic; returns (hits n x 4 u32, counts n x 2 u32:
+    nodes visited, triangles tested)."""
+    nodes = np.ascontiguousarray(nodes).view(np.uint8)
+    tris = np.ascontiguousarray(tris).view(np.uint8)
+    assert nodes.size % 80 == 0 and tris.size % 48 == 0
+    rays = _f32(rays).reshape(-1, 8)
+    hits = np.zeros((rays.shape[0], 4), np.uint32)
+    cnt = np.zeros((rays.shape[0], 2), np.uint32)
+    st = lib().orc_cwbvh_trace(nodes.ctypes.data, nodes.size // 80, tris.ctypes.data, tris.size // 48,
+                               rays.ctypes.data, rays.shape[0], 1 if any_hit else 0, hits.ctypes.data,
+                               cnt.ctypes.data, threads)
+    if st != 0:
+        raise RuntimeError("orc_cwbvh_trace failed")
+    return hits, cnt
 
 
 def pcg32(initstate: int, initseq: int, n: int) -> np.ndarray:

@@ -1384,6 +1384,166 @@ ORC_API void orc_sky_sample(void* sp, const float* u, uint32_t n, float* out) {
 
 ORC_API uint32_t orc_scene_bvh_nodes(void* sp) { return (uint32_t)((Scene*)sp)->nodes.size(); }
 
+// ============================================ compressed-BVH traversal ====
+// Restatement of the product's single-ray traversal of its compressed 8-wide
+// BVH, used to count the nodes visited and triangles tested per ray on the
+// product's own tree (the traversal-bytes figure: 80 B per node, 48 B per
+// triangle) and to check that the quantised boxes never cull a hit.  Layout
+// of one 80-byte node: frame origin p (3 x f32), biased exponents e (3 x u8),
+// internal-child mask, child_base, tri_base, 8 meta bytes (0: empty slot;
+// internal child: 24 + slot in the low 5 bits; leaf: triangle offset in the
+// low 5 bits and a unary triangle count in the top 3), then the low planes
+// x/y/z and the high planes x/y/z, 8 bytes each.  A triangle is 48 bytes:
+// v0, prim, v1, material, v2, transparency bits.
+//
+// Arithmetic, in this order, as the device kernel evaluates it: per axis the
+// slab scale s = 2^(e-127) / d and offset a = (p - o) / d - 2^23 s; the plane
+// of byte q is at fma(2^23 + q, s, a) (near) or fma(2^23 + q, s PAD, a PAD)
+// (far), PAD = 1.00000095; a child is hit when max(near x/y/z, tmin) <=
+// min(far x/y/z, t_best).  Children are visited nearest-octant first
+// (descending slot ^ (7 ^ octant)), a leaf's triangles in ascending offset,
+// all of a node's triangles before its next child.
+namespace orc {
+struct CwNodeO {
+    float p[3];
+    uint8_t e[3], imask;
+    uint32_t child_base, tri_base;
+    uint8_t meta[8];
+    uint8_t qlo[3][8], qhi[3][8];
+};
+static_assert(sizeof(CwNodeO) == 80, "node layout");
+struct CwTriO { float v0[3]; uint32_t prim; float v1[3]; uint32_t mat; float v2[3]; uint32_t tr; };
+static_assert(sizeof(CwTriO) == 48, "triangle layout");
+
+static float pow2_biased(uint8_t e) { uint32_t u = (uint32_t)e << 23; float f; std::memcpy(&f, &u, 4); return f; }
+
+// Hit bits of node `n`: internal children at bit 24 + (slot ^ key), triangles
+// at tri offset .. offset + count - 1.
+static uint32_t cw_node_hits(const Ray& r, const CwNodeO& n, uint32_t key, float tbest) {
+    const float PAD = 1.00000095f;
+    float o[3] = {r.o.x, r.o.y, r.o.z};
+    float s[3], a[3], sf[3], af[3];
+    for (int k = 0; k < 3; ++k) {
+        s[k] = pow2_biased(n.e[k]) * r.id[k];
+        a[k] = (n.p[k] - o[k]) * r.id[k];
+        a[k] = a[k] - 8388608.0f * s[k];
+        sf[k] = s[k] * PAD;
+        af[k] = a[k] * PAD;
+    }
+    uint32_t hits = 0;
+    for (int c = 0; c < 8; ++c) {
+        uint8_t m = n.meta[c];
+        if (m == 0) continue;
+        float tnear[3], tfar[3];
+        for (int k = 0; k < 3; ++k) {
+            bool neg = r.id[k] < 0.0f;
+            float qn = 8388608.0f + (float)(neg ? n.qhi[k][c] : n.qlo[k][c]);
+            float qf = 8388608.0f + (float)(neg ? n.qlo[k][c] : n.qhi[k][c]);
+            tnear[k] = std::fmaf(qn, s[k], a[k]);
+            tfar[k] = std::fmaf(qf, sf[k], af[k]);
+        }
+        float tn = std::fmax(std::fmax(tnear[0], tnear[1]), std::fmax(tnear[2], r.tmin));
+        float tf = std::fmin(std::fmin(tfar[0], tfar[1]), std::fmin(tfar[2], tbest));
+        if (!(tn <= tf)) continue;
+        if ((n.imask >> c) & 1u) hits |= 1u << (24 + ((uint32_t)c ^ key));
+        else hits |= (uint32_t)(m >> 5) << (m & 31u);
+    }
+    return hits;
+}
+
+static uint32_t cw_trace(const CwNodeO* nodes, const CwTriO* tris, const Ray& r, bool any, float& to, float& uo,
+                         float& vo, uint32_t& prim_out, Counts* cnt) {
+    uint32_t oct = (r.id[0] < 0.0f ? 1u : 0u) | (r.id[1] < 0.0f ? 2u : 0u) | (r.id[2] < 0.0f ? 4u : 0u);
+    uint32_t key = 7u ^ oct;
+    float tbest = r.tmax, bu = 0.0f, bv = 0.0f;
+    uint32_t best_leaf = UINT32_MAX, best_prim = UINT32_MAX;
+    struct Group { uint32_t base, bits; };
+    std::vector<Group> stack;
+    // a zero direction is skipped as a miss (rt_gbuffer.hlsl:13-15)
+    bool zero = r.d.x == 0.0f && r.d.y == 0.0f && r.d.z == 0.0f;
+    Group G{0u, zero ? 0u : (0x80000000u | (1u << (7u ^ key)))};  // the root: slot 7 ^ key of a virtual parent
+    Group T{0u, 0u};
+    while (true) {
+        while (T.bits) {
+            uint32_t bit = (uint32_t)__builtin_ctz(T.bits);
+            T.bits &= T.bits - 1u;
+            uint32_t ti = T.base + bit;
+            const CwTriO& ct = tris[ti];
+            if (cnt) cnt->tris++;
+            Tri t;
+            t.a = f3(ct.v0[0], ct.v0[1], ct.v0[2]);
+            t.b = f3(ct.v1[0], ct.v1[1], ct.v1[2]);
+            t.c = f3(ct.v2[0], ct.v2[1], ct.v2[2]);
+            t.prim = ct.prim;
+            t.mat = ct.mat;
+            std::memcpy(&t.tr, &ct.tr, 4);
+            float tt, u, v;
+            if (!tri_hit(r, t, tbest, best_prim, tt, u, v)) continue;
+            if (!keep_hit(r, t.tr)) continue;
+            tbest = tt; best_leaf = ti; best_prim = t.prim; bu = u; bv = v;
+            if (any) { to = tt; uo = u; vo = v; prim_out = t.prim; return ti; }
+        }
+        if ((G.bits & 0xff000000u) == 0u) {
+            if (stack.empty()) break;
+            G = stack.back();
+            stack.pop_back();
+        }
+        uint32_t bit = 31u - (uint32_t)__builtin_clz(G.bits & 0xff000000u);
+        G.bits &= ~(1u << bit);
+        uint32_t slot = (bit - 24u) ^ key;
+        uint32_t ni = G.base + (uint32_t)__builtin_popcount(G.bits & 0xffu & ((1u << slot) - 1u));
+        if (G.bits & 0xff000000u) stack.push_back(G);
+        if (cnt) cnt->nodes++;
+        const CwNodeO& n = nodes[ni];
+        uint32_t h = cw_node_hits(r, n, key, tbest);
+        G = Group{n.child_base, (h & 0xff000000u) | n.imask};
+        T = Group{n.tri_base, h & 0x00ffffffu};
+    }
+    to = tbest; uo = bu; vo = bv;
+    prim_out = best_prim;
+    return best_leaf;
+}
+}  // namespace orc
+
+// rays: n x 8 floats (origin, tmin, direction, tmax); hits: n x 4 words (t bits,
+// primitive id or 0xffffffff, u bits, v bits); counts (optional): n x 2 (nodes
+// visited, triangles tested).
+ORC_API int orc_cwbvh_trace(const void* nodes, uint64_t num_nodes, const void* tris, uint64_t num_tris,
+                            const float* rays, uint32_t n, int any, uint32_t* hits, uint32_t* counts, int threads) {
+    if (!nodes || !tris || num_nodes == 0) return -1;
+    const CwNodeO* N = (const CwNodeO*)nodes;
+    const CwTriO* T = (const CwTriO*)tris;
+    (void)num_tris;
+    int nt = nthreads(threads);
+    std::atomic<uint32_t> next{0};
+    auto work = [&]() {
+        while (true) {
+            uint32_t b = next.fetch_add(1024);
+            if (b >= n) break;
+            uint32_t e = std::min(n, b + 1024);
+            for (uint32_t i = b; i < e; ++i) {
+                const float* R = rays + 8 * (size_t)i;
+                Ray r = make_ray(f3(R[0], R[1], R[2]), R[3], f3(R[4], R[5], R[6]), R[7]);
+                float t, u, v;
+                uint32_t prim;
+                Counts c;
+                cw_trace(N, T, r, any != 0, t, u, v, prim, counts ? &c : nullptr);
+                uint32_t* H = hits + 4 * (size_t)i;
+                std::memcpy(&H[0], &t, 4);
+                H[1] = prim;
+                std::memcpy(&H[2], &u, 4);
+                std::memcpy(&H[3], &v, 4);
+                if (counts) { counts[2 * (size_t)i] = (uint32_t)c.nodes; counts[2 * (size_t)i + 1] = (uint32_t)c.tris; }
+            }
+        }
+    };
+    std::vector<std::thread> ts;
+    for (int k = 1; k < nt; ++k) ts.emplace_back(work);
+    work();
+    for (auto& t : ts) t.join();
+    return 0;
+}
+
 // ===================================================== radiance-cache MLP ====
 // CPU restatement of the cache network (64 encoded inputs, 4 hidden ReLU
 // layers of 64, 3 outputs, no biases) with the same rounding points as the

@@ -132,3 +132,31 @@ def test_octant_traversal_finds_oracle_hits(bsm, oracle, built):
                         if t[0] < best_t or (t[0] == best_t and prim < best_p):
                             best_t, best_p = float(t[0]), prim
         assert best_p == ref[i, 1], f"ray {i}"
+
+
+@pytest.mark.parametrize("collapse", [0, 1])
+@pytest.mark.parametrize("kind", ["room", "terrain"])
+def test_kernel_arithmetic_traversal_finds_oracle_hits(bsm, oracle, kind, collapse):
+    """The oracle's restatement of the device traversal (quantised slab
+    arithmetic in float, octant order) over the host-built tree finds the
+    closest and any hits of the oracle's own binary BVH, bit for bit, for
+    both collapse modes; the per-ray counts are positive and bounded."""
+    if kind == "room":
+        sc = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=6, spheres=16, width=32, height=32)
+        rays = random_rays(3000, -0.2, 1.2, seed=22)
+    else:
+        sc = bsm.generate_scene(bsm.BSM_SCENE_TERRAIN, seed=2, grid=64, spheres=40, width=32, height=32)
+        rays = random_rays(3000, -1.0, 1.0, seed=23)
+    nb, tb, st = bsm.bvh_build_host(sc, collapse=collapse)
+    osc = oracle.OracleScene(sc)
+    ref = osc.trace(rays)
+    hits, cnt = oracle.cwbvh_trace(nb, tb, rays)
+    assert np.array_equal(hits[:, 1], ref[:, 1])
+    hit = ref[:, 1] != 0xFFFFFFFF
+    assert hit.sum() > 100
+    assert np.array_equal(hits[hit, 0], ref[hit, 0]) and np.array_equal(hits[hit, 2:], ref[hit, 2:])
+    assert (cnt[:, 0] >= 1).all() and (cnt[:, 0] <= st.num_nodes).all()
+    assert (cnt[hit, 1] >= 1).all()
+    occ_ref = osc.trace(rays, any_hit=True)[:, 1] != 0xFFFFFFFF
+    occ, _ = oracle.cwbvh_trace(nb, tb, rays, any_hit=True)
+    assert np.array_equal(occ[:, 1] != 0xFFFFFFFF, occ_ref)
