@@ -195,7 +195,8 @@ def profile_traffic():
 
 # -------------------------------------------------------------- CPU legs ----
 def cpu_sample(scene, cam_arr, a, budget_s: float, threads: int = 0):
-    """Times the oracle on whole rows of the frame at 1 spp, sized to about budget_s seconds."""
+    """Times the oracle on whole rows of the frame, sized to about budget_s seconds: a band of rows at 1 spp,
+    or the whole frame at as many samples per pixel (up to the workload's) as the budget holds."""
     import oracle
     osc = oracle.OracleScene(scene)
     h = a.height
@@ -204,11 +205,12 @@ def cpu_sample(scene, cam_arr, a, budget_s: float, threads: int = 0):
     _, st, sec = osc.render(cam_arr, spp=1, max_segments=a.segments, seed=a.seed, rows=probe, threads=threads)
     per_row = max(sec / 8.0, 1e-4)
     rows = int(min(h, max(8, budget_s / per_row)))
+    spp = int(max(1, min(a.spp, budget_s / (per_row * h)))) if rows == h else 1
     r0 = max(0, mid - rows // 2)
     r1 = min(h, r0 + rows)
-    _, st, sec = osc.render(cam_arr, spp=1, max_segments=a.segments, seed=a.seed, rows=(r0, r1), threads=threads)
+    _, st, sec = osc.render(cam_arr, spp=spp, max_segments=a.segments, seed=a.seed, rows=(r0, r1), threads=threads)
     rays = int(st[:16].sum())
-    return {"rays": rays, "seconds": sec, "rows": (r0, r1), "shadow_rays": int(st[16:].sum())}
+    return {"rays": rays, "seconds": sec, "rows": (r0, r1), "spp": spp, "shadow_rays": int(st[16:].sum())}
 
 
 def nthreads():
@@ -231,10 +233,10 @@ def run_reference(a, dist: Dist):
         r = cpu_sample(scene, cam, a, budget)
         rays += r["rays"]
         secs += r["seconds"]
-        rows = r["rows"]
+        rows, spp = r["rows"], r["spp"]
     value = rays / secs / 1e6
     cores = nthreads()
-    sample = f"rows {rows[0]}-{rows[1]} of the {a.width}x{a.height} frame at 1 spp per step, {a.segments} segments"
+    sample = f"rows {rows[0]}-{rows[1]} of the {a.width}x{a.height} frame at {spp} spp per step, {a.segments} segments"
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": a.gpus,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(secs / a.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -360,7 +362,7 @@ def run_ours(a, dist: Dist):
             r = cpu_sample(scene, cam.as_array(), a, a.cpu_seconds)
             cpu = {"value": round(r["rays"] / r["seconds"] / 1e6, 3), "unit": "Mrays/s", "cores": nthreads(),
                    "kind": "port",
-                   "sample": f"rows {r['rows'][0]}-{r['rows'][1]} of the frame at 1 spp ({r['rays']} extend rays, "
+                   "sample": f"rows {r['rows'][0]}-{r['rows'][1]} of the frame at {r['spp']} spp ({r['rays']} extend rays, "
                              f"{r['seconds']:.1f} s)"}
         line = {"metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": a.gpus, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,

@@ -173,6 +173,24 @@ void make_view(const bsm_camera& c, DevView& v) {
     v.height = c.height;
 }
 
+// Why a camera cannot be rendered, or nullptr: a view needs a size, a field of
+// view in (0, 180) degrees, finite vectors, and a front that is neither zero
+// nor parallel to up (the view basis is built from front x up).
+const char* camera_problem(const bsm_camera& c) {
+    if (c.width == 0 || c.height == 0) return "view size must be > 0";
+    if (!(c.yfov_deg > 0.0f && c.yfov_deg < 180.0f)) return "yfov_deg must be in (0, 180)";
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(c.position[k]) || !std::isfinite(c.front[k]) || !std::isfinite(c.up[k]))
+            return "camera position, front and up must be finite";
+    double f[3] = {c.front[0], c.front[1], c.front[2]}, u[3] = {c.up[0], c.up[1], c.up[2]};
+    double x[3] = {f[1] * u[2] - f[2] * u[1], f[2] * u[0] - f[0] * u[2], f[0] * u[1] - f[1] * u[0]};
+    double ff = f[0] * f[0] + f[1] * f[1] + f[2] * f[2], uu = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    double xx = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+    if (!(ff > 0.0) || !(uu > 0.0)) return "camera front and up must not be zero";
+    if (!(xx > 1e-12 * ff * uu)) return "camera front must not be parallel to up";
+    return nullptr;
+}
+
 bool same_camera(const bsm_camera& a, const bsm_camera& b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
 
 // Sky sampling tables: weights (r + g + b) * sin(theta at the row centre),
@@ -1165,9 +1183,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         relayout = ctx->layout[v].first != views[v].width || ctx->layout[v].second != views[v].height;
     uint64_t total_px = 0;
     for (uint32_t v = 0; v < n_views; ++v) {
-        if (views[v].width == 0 || views[v].height == 0) return fail(ctx, BSM_ERR_INVALID_ARG, "view size must be > 0");
-        if (!(views[v].yfov_deg > 0.0f && views[v].yfov_deg < 180.0f))
-            return fail(ctx, BSM_ERR_INVALID_ARG, "yfov_deg must be in (0, 180)");
+        if (const char* why = camera_problem(views[v])) return fail(ctx, BSM_ERR_INVALID_ARG, why);
         total_px += (uint64_t)views[v].width * views[v].height;
     }
     if (total_px >= (1ull << 32)) return fail(ctx, BSM_ERR_INVALID_ARG, "too many pixels in one call");
@@ -1348,6 +1364,7 @@ extern "C" bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, con
     Scene* sc = find_scene(ctx, scene_id);
     if (!sc || !sc->has_bvh) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene or BVH not built");
     if (cache->ctx != ctx) return fail(ctx, BSM_ERR_INVALID_ARG, "cache belongs to another context");
+    if (const char* why = camera_problem(*cam)) return fail(ctx, BSM_ERR_INVALID_ARG, why);
     bsm_cache_settings cs;
     if (cs_in) cs = *cs_in; else bsm_cache_settings_default(&cs);
     if (cs.cache_segment == 0 || cs.cache_segment >= (uint32_t)kMaxSeg)
@@ -1676,9 +1693,8 @@ extern "C" bsm_status bsm_render_primary(bsm_context* ctx, uint32_t scene_id, co
     bsm_pt_settings_default(&s);
     if (settings) s = *settings;
     const bsm_camera& c = *camera;
-    if (c.width == 0 || c.height == 0) return fail(ctx, BSM_ERR_INVALID_ARG, "view size must be > 0");
+    if (const char* why = camera_problem(c)) return fail(ctx, BSM_ERR_INVALID_ARG, why);
     if ((uint64_t)c.width * c.height >= (1ull << 31)) return fail(ctx, BSM_ERR_INVALID_ARG, "view too large");
-    if (!(c.yfov_deg > 0.0f && c.yfov_deg < 180.0f)) return fail(ctx, BSM_ERR_INVALID_ARG, "yfov_deg must be in (0, 180)");
     if (!(s.ray_length > 0.0f)) return fail(ctx, BSM_ERR_INVALID_ARG, "ray_length must be > 0");
     if (s.t_min < 0.0f) return fail(ctx, BSM_ERR_INVALID_ARG, "t_min must be >= 0");
     if (near_z == 0.0f) near_z = 0.01f;   // camera.hpp:54-55
@@ -1734,6 +1750,7 @@ cudaStream_t ctx_stream(bsm_context* ctx) { return ctx->stream; }
 int ctx_device(bsm_context* ctx) { return ctx->device; }
 void ctx_set_error(bsm_context* ctx, const char* msg) { ctx->err = msg; }
 void ctx_make_view(const bsm_camera* c, DevView* v) { make_view(*c, *v); }
+const char* ctx_camera_problem(const bsm_camera* c) { return camera_problem(*c); }
 void*& ctx_server_slot(bsm_context* ctx) { return ctx->server; }
 uint32_t ctx_max_lights(bsm_context* ctx) {
     uint32_t m = 1;

@@ -171,6 +171,7 @@ cudaStream_t ctx_stream(bsm_context* ctx);
 int ctx_device(bsm_context* ctx);
 void ctx_set_error(bsm_context* ctx, const char* msg);
 void ctx_make_view(const bsm_camera* c, DevView* v);
+const char* ctx_camera_problem(const bsm_camera* c);   // nullptr when the camera can be rendered
 void*& ctx_server_slot(bsm_context* ctx);
 uint32_t ctx_max_lights(bsm_context* ctx);
 

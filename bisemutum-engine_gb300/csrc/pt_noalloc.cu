@@ -97,8 +97,7 @@ extern "C" bsm_status bsm_render_noalloc(bsm_context* ctx, uint32_t scene_id, co
         ctx_set_error(ctx, "bsm_render_noalloc: unknown scene id or BVH not built");
         return BSM_ERR_NOT_FOUND;
     }
-    if (cam->width == 0 || cam->height == 0 || !(cam->yfov_deg > 0.0f && cam->yfov_deg < 180.0f) || s->spp == 0 ||
-        !(s->ray_length > 0.0f) || s->t_min < 0.0f) {
+    if (ctx_camera_problem(cam) || s->spp == 0 || !(s->ray_length > 0.0f) || s->t_min < 0.0f) {
         ctx_set_error(ctx, "bsm_render_noalloc: invalid camera or settings");
         return BSM_ERR_INVALID_ARG;
     }

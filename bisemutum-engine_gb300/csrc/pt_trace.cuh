@@ -90,6 +90,17 @@ __device__ __forceinline__ RayPre make_ray(float4 o, float4 d) {
     return r;
 }
 
+// Rays that are traced: origin and direction finite, direction not zero (a
+// zero direction is skipped as a miss, rt_gbuffer.hlsl:13-15) and tmin <= tmax.
+// Every other ray (a NaN or infinite component, an empty or NaN interval) is a
+// miss without traversal.
+__device__ __forceinline__ bool finite_bits(float x) { return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u; }
+__device__ __forceinline__ bool ray_traceable(const RayPre& r, float tmax) {
+    bool fin = finite_bits(r.ox) & finite_bits(r.oy) & finite_bits(r.oz) & finite_bits(r.dx) & finite_bits(r.dy) &
+               finite_bits(r.dz);
+    return fin && !(r.dx == 0.0f && r.dy == 0.0f && r.dz == 0.0f) && r.tmin <= tmax;
+}
+
 // Watertight test.  Returns true and writes t/u/v when the triangle is hit at
 // t in (tmin, tbest], preferring the lower primitive id on a tie at tbest.
 __device__ __forceinline__ bool tri_test(const RayPre& r, float4 a, float4 b, float4 c, float tbest,
@@ -224,8 +235,7 @@ __device__ __forceinline__ uint32_t trace_ray(const RayPre& r, float tmax, const
     uint2 stack[kStackSize];
     int sp = 0;
     uint32_t root_slot = 7u ^ r.oct_key;
-    bool zero = r.dx == 0.0f && r.dy == 0.0f && r.dz == 0.0f;  // skipped as a miss (rt_gbuffer.hlsl:13-15)
-    uint2 G = make_uint2(0u, zero ? 0u : (0x80000000u | (1u << root_slot)));
+    uint2 G = make_uint2(0u, ray_traceable(r, tmax) ? (0x80000000u | (1u << root_slot)) : 0u);
     uint2 T = make_uint2(0u, 0u);
     while (true) {
         while (T.y != 0u) {
@@ -306,8 +316,7 @@ __device__ __forceinline__ uint32_t trace_ray2(const RayPre& rw, float tmax, con
     const CwNode* nodes = tlas;
     const CwTri* tris = nullptr;
     uint32_t inst = kMissPrim, prim_base = 0u, mat_override = kMissPrim;
-    bool zero = rw.dx == 0.0f && rw.dy == 0.0f && rw.dz == 0.0f;  // skipped as a miss (rt_gbuffer.hlsl:13-15)
-    uint2 G = make_uint2(0u, zero ? 0u : (0x80000000u | (1u << (7u ^ rw.oct_key))));
+    uint2 G = make_uint2(0u, ray_traceable(rw, tmax) ? (0x80000000u | (1u << (7u ^ rw.oct_key))) : 0u);
     uint2 T = make_uint2(0u, 0u);
     while (true) {
         while (T.y != 0u) {
@@ -425,9 +434,7 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
                     r = make_ray(o, d);
                     tbest = d.w;
                     best_leaf = kMissPrim; best_prim = kMissPrim; bu = 0.0f; bv = 0.0f;
-                    // a zero direction is skipped as a miss (rt_gbuffer.hlsl:13-15)
-                    bool zero = d.x == 0.0f && d.y == 0.0f && d.z == 0.0f;
-                    G = make_uint2(0u, zero ? 0u : (0x80000000u | (1u << (7u ^ r.oct_key))));
+                    G = make_uint2(0u, ray_traceable(r, d.w) ? (0x80000000u | (1u << (7u ^ r.oct_key))) : 0u);
                     T = make_uint2(0u, 0u);
                     sp = 0;
                     idx = i;

@@ -404,6 +404,7 @@ extern "C" bsm_status bsm_server_submit(bsm_context* ctx, const bsm_request* r, 
         ctx_set_error(ctx, "invalid request");
         return BSM_ERR_INVALID_ARG;
     }
+    if (const char* why = ctx_camera_problem(&r->camera)) { ctx_set_error(ctx, why); return BSM_ERR_INVALID_ARG; }
     uint32_t segs = r->max_segments ? r->max_segments : 8;
     if (segs > (uint32_t)kMaxSeg) { ctx_set_error(ctx, "max_segments must be 1..16"); return BSM_ERR_INVALID_ARG; }
     uint64_t px = (uint64_t)r->camera.width * r->camera.height;

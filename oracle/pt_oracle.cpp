@@ -439,6 +439,15 @@ static bool box_hit(const Ray& r, const BNode& n, float tbest) {
 struct Counts { uint64_t nodes = 0, tris = 0; };
 // returns index into S.tris (leaf order) or UINT32_MAX
 static uint32_t bits_of(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+// Rays that are traced (the device traversal's rule): origin and direction
+// finite, direction not zero (a zero direction is skipped as a miss,
+// rt_gbuffer.hlsl:13-15) and tmin <= tmax; every other ray is a miss.
+static bool finite_bits(float x) { return (bits_of(x) & 0x7f800000u) != 0x7f800000u; }
+static bool ray_traceable(const Ray& r) {
+    bool fin = finite_bits(r.o.x) && finite_bits(r.o.y) && finite_bits(r.o.z) && finite_bits(r.d.x) &&
+               finite_bits(r.d.y) && finite_bits(r.d.z);
+    return fin && !(r.d.x == 0.0f && r.d.y == 0.0f && r.d.z == 0.0f) && r.tmin <= r.tmax;
+}
 // Stochastic-opacity uniform of a ray: the bits of its origin and direction
 // combined as gen_opacity_random_for does (hits/rt_gbuffer.hlsl:14-19), with
 // the path's PCG32 word as the seed, hashed by SplitMix64's finaliser.
@@ -460,8 +469,7 @@ static bool trace_bvh(const Scene& G, const Ray& r, const Ray& rw, bool any, uin
                       const float* trm, uint32_t inst, Best& b, Counts* cnt) {
     uint32_t stack[128];
     int sp = 0;
-    // a zero direction is skipped as a miss (rt_gbuffer.hlsl:13-15)
-    if (!(rw.d.x == 0.0f && rw.d.y == 0.0f && rw.d.z == 0.0f)) stack[sp++] = 0;
+    if (ray_traceable(rw)) stack[sp++] = 0;
     while (sp) {
         uint32_t ni = stack[--sp];
         const BNode& n = G.nodes[ni];
@@ -1459,9 +1467,7 @@ static uint32_t cw_trace(const CwNodeO* nodes, const CwTriO* tris, const Ray& r,
     uint32_t best_leaf = UINT32_MAX, best_prim = UINT32_MAX;
     struct Group { uint32_t base, bits; };
     std::vector<Group> stack;
-    // a zero direction is skipped as a miss (rt_gbuffer.hlsl:13-15)
-    bool zero = r.d.x == 0.0f && r.d.y == 0.0f && r.d.z == 0.0f;
-    Group G{0u, zero ? 0u : (0x80000000u | (1u << (7u ^ key)))};  // the root: slot 7 ^ key of a virtual parent
+    Group G{0u, ray_traceable(r) ? (0x80000000u | (1u << (7u ^ key))) : 0u};  // the root: slot 7 ^ key of a virtual parent
     Group T{0u, 0u};
     while (true) {
         while (T.bits) {

@@ -224,3 +224,40 @@ def test_sky_alias_sampling_matches_its_pdf(bsm, oracle):
     m = expect > 20
     chi2 = float(((counts[m] - expect[m]) ** 2 / expect[m]).sum())
     assert chi2 < 1.3 * m.sum(), (chi2, m.sum())
+
+
+def test_edge_cases_of_the_traversal(bsm, oracle):
+    """Coincident triangles resolve to the lower primitive id, zero-area
+    triangles are never hit, shared edges and vertices do not leak, and rays
+    with a non-finite component or an empty interval are misses — in the
+    oracle's binary BVH and in its restatement of the device traversal over
+    the product's compressed BVH alike."""
+    from edge_scenes import MISS, coincident_scene, edge_rays, grid_scene, invalid_rays, rays_along_z
+    sc = coincident_scene(bsm)
+    osc = oracle.OracleScene(sc)
+    nb, tb, _ = bsm.bvh_build_host(sc)
+    rays = rays_along_z(4000, seed=3)
+    h = osc.trace(rays)
+    hc, _ = oracle.cwbvh_trace(nb, tb, rays)
+    assert np.array_equal(h[:, :2], hc[:, :2])
+    in_front = rays[:, 0] + rays[:, 1] < 1.0           # inside the front triangle
+    assert (h[in_front, 1] == 1).all()
+    assert set(np.unique(h[~in_front, 1]).tolist()) <= {0, 5, 1}
+    assert not np.isin(h[:, 1], [2, 3, 4]).any()
+    occ = osc.trace(rays, any_hit=True)[:, 1] != MISS
+    assert occ.all()
+    g = grid_scene(bsm)
+    er = edge_rays()
+    og = oracle.OracleScene(g)
+    gh = og.trace(er)
+    assert (gh[:, 1] != MISS).all(), "a ray through a shared edge or vertex leaked"
+    gnb, gtb, _ = bsm.bvh_build_host(g)
+    assert np.array_equal(oracle.cwbvh_trace(gnb, gtb, er)[0][:, :2], gh[:, :2])
+    bad = invalid_rays()
+    assert (osc.trace(bad)[:, 1] == MISS).all()
+    assert (osc.trace(bad, any_hit=True)[:, 1] == MISS).all()
+    assert (oracle.cwbvh_trace(nb, tb, bad)[0][:, 1] == MISS).all()
+    # an infinite tmax is a valid interval
+    inf_tmax = rays_along_z(100, seed=4)
+    inf_tmax[:, 7] = np.inf
+    assert np.array_equal(osc.trace(inf_tmax)[:, 1], osc.trace(rays_along_z(100, seed=4))[:, 1])
