@@ -63,7 +63,7 @@ def parse():
     p.add_argument("--collapse", type=int, default=0, help="BVH collapse: 0 SAH-optimal, 1 greedy")
     p.add_argument("--tri-cost", type=float, default=0.0, help="SAH-optimal collapse: triangle / node test cost")
     p.add_argument("--bins", type=int, default=0, help="binned SAH bins (0 = 32)")
-    p.add_argument("--max-leaf", type=int, default=0, help="largest leaf (triangles, 1..3; 0 = 3)")
+    p.add_argument("--max-leaf", type=int, default=0, help="largest leaf (triangles, 1..2; 0 = 2)")
     p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "cache"],
                    help="plain: the single-frame pass (the bench line); batch: 256 uneven views in one wavefront "
                         "against a loop of plain renders")

@@ -250,10 +250,12 @@ bool build_cwbvh(const float* positions, const uint32_t* indices, uint32_t num_t
                  const bsm_bvh_opts* opts_in, BvhBuildResult& out, std::string& err) {
     auto t0 = std::chrono::steady_clock::now();
     if (num_tris == 0) { err = "scene has no triangles"; return false; }
+    // node and triangle bases share their top bit with the traversal's triangle-group flag
+    if (num_tris >= kTriGroupFlag) { err = "more than 2^31 - 1 triangles in one BVH"; return false; }
     bsm_bvh_opts opts{};
     if (opts_in) opts = *opts_in;
     uint32_t bins = opts.sah_bins ? std::min(std::max(opts.sah_bins, 4u), 256u) : 32u;
-    uint32_t max_leaf = opts.max_leaf_tris ? std::min(opts.max_leaf_tris, 3u) : 3u;
+    uint32_t max_leaf = opts.max_leaf_tris ? std::min(opts.max_leaf_tris, kMaxLeafTris) : kMaxLeafTris;
     const bool optimal = opts.collapse == BSM_COLLAPSE_SAH_OPTIMAL;
     uint32_t threads = opts.num_threads ? opts.num_threads : std::max(1u, std::thread::hardware_concurrency());
 
@@ -420,7 +422,7 @@ bool build_cwbvh(const float* positions, const uint32_t* indices, uint32_t num_t
             bool as_leaf = as_leaf_node(ci);
             if (as_leaf) {
                 uint32_t cnt = c.count;
-                if (cnt == 0 || cnt > 3) { err = "internal error: leaf size"; return false; }
+                if (cnt == 0 || cnt > kMaxLeafTris) { err = "internal error: leaf size"; return false; }
                 // gather the subtree's triangles (a small internal subtree becomes one leaf)
                 std::vector<uint32_t> st{ci};
                 while (!st.empty()) {
@@ -429,16 +431,14 @@ bool build_cwbvh(const float* positions, const uint32_t* indices, uint32_t num_t
                     if (nodes[x].leaf) emit_leaf_tris(x);
                     else { st.push_back(nodes[x].right); st.push_back(nodes[x].left); }
                 }
-                uint8_t unary = (uint8_t)((1u << cnt) - 1u);
-                node.meta[s] = (uint8_t)((unary << 5) | tri_off);
+                node.tri_mask |= (uint16_t)(((1u << cnt) - 1u) << (2 * s));
                 tri_off += cnt;
             } else {
                 node.imask |= (uint8_t)(1u << s);
-                node.meta[s] = (uint8_t)(0x20u | (24u + (uint32_t)s));
                 internal_children.push_back(ci);
             }
         }
-        if (tri_off > 24) { err = "internal error: more than 24 triangles in a node"; return false; }
+        if (tri_off > 2 * 8) { err = "internal error: more than 16 triangles in a node"; return false; }
         for (uint32_t ci : internal_children) {
             uint32_t wi = (uint32_t)out.nodes.size();
             out.nodes.emplace_back();

@@ -6,7 +6,10 @@
 // published compressed wide BVH of Ylitie, Karras and Laine, "Efficient
 // Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs" (HPG 2017):
 // one 80-byte node holds the quantisation frame of its box and eight child
-// boxes quantised outward to 8 bits per plane.
+// boxes quantised outward to 8 bits per plane.  Where the paper keeps a meta
+// byte per child (triangle offset and count), this layout keeps one 16-bit
+// mask of two bits per slot, so that a node test turns its 8-bit child hit
+// mask into the triangle hits with one table lookup and one AND.
 #pragma once
 #include <stdint.h>
 
@@ -18,13 +21,16 @@ struct alignas(16) CwNode {
     uint8_t ex, ey, ez;      // per-axis scale 2^(e - 127)
     uint8_t imask;           // bit s: child slot s is an internal node
     uint32_t child_base;     // index of the first internal child (children stored in slot order)
-    uint32_t tri_base;       // index of the first triangle referenced by this node's leaves
-    uint8_t meta[8];         // per slot: 0 = empty; internal: 0x20 | (24 + slot);
-                             //           leaf: (unary triangle count << 5) | triangle offset (0..23)
+    uint32_t tri_base;       // index of the first triangle of this node's leaf slots (stored in slot order)
+    uint16_t tri_mask;       // bits 2s, 2s + 1: leaf slot s holds a first / a second triangle; the triangle
+                             // of bit b is tri_base + popc(tri_mask & ((1 << b) - 1))
+    uint8_t pad[6];
     uint8_t qlo_x[8], qlo_y[8], qlo_z[8];
     uint8_t qhi_x[8], qhi_y[8], qhi_z[8];
 };
 static_assert(sizeof(CwNode) == 80, "CwNode must be 80 bytes");
+constexpr uint32_t kMaxLeafTris = 2;          // triangles per leaf slot (the tri_mask has two bits per slot)
+constexpr uint32_t kTriGroupFlag = 0x80000000u;  // marks a triangle group on a traversal stack (bases < 2^31)
 
 // Leaf-ordered triangle: three float4 (48 bytes).  w of the first vertex holds
 // the primitive id (input triangle index) and w of the second the material id.

@@ -29,7 +29,7 @@ BSM_QHD int quant_exponent_hd(float extent) {
 
 // Rewrites the frame (px..pz, ex..ez) and the child bytes of node `n` for the
 // child boxes of the slots in `used`; returns the node box.  Topology fields
-// (imask, meta, child_base, tri_base) are kept.
+// (imask, tri_mask, child_base, tri_base) are kept.
 BSM_QHD void tlas_quantise(CwNode& n, const float lo[8][3], const float hi[8][3], uint32_t used, float nlo[3],
                            float nhi[3]) {
     for (int k = 0; k < 3; ++k) { nlo[k] = INFINITY; nhi[k] = -INFINITY; }

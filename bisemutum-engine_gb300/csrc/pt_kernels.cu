@@ -509,15 +509,15 @@ __global__ void k_tlas_refit(CwNode* __restrict__ nodes, float* __restrict__ nod
     float lo[8][3], hi[8][3];
     uint32_t used = 0;
     for (int s = 0; s < 8; ++s) {
-        uint8_t m = n.meta[s];
-        if (m == 0) continue;
+        bool inner = (n.imask >> s) & 1u;
+        if (!inner && ((n.tri_mask >> (2 * s)) & 3u) == 0u) continue;
         used |= 1u << s;
         const float* b;
-        if (n.imask & (1u << s)) {
+        if (inner) {
             uint32_t ci = n.child_base + (uint32_t)__popc((uint32_t)n.imask & ((1u << s) - 1u));
             b = node_box + 6 * (size_t)ci;
         } else {
-            b = inst_box + 6 * (size_t)(n.tri_base + (m & 0x1fu));
+            b = inst_box + 6 * (size_t)(n.tri_base + (uint32_t)__popc((uint32_t)n.tri_mask & ((1u << (2 * s)) - 1u)));
         }
         for (int k = 0; k < 3; ++k) { lo[s][k] = b[k]; hi[s][k] = b[3 + k]; }
     }

@@ -3,11 +3,11 @@
 // Replaces TraceRay on the RT cores (bisemutum/shaders/renderer/raytracing/
 // rt_gbuffer.hlsl:17-25) with a software traversal:
 //   * node test: eight quantised child boxes per 80-byte node; a plane is
-//     rebuilt from its byte with one PRMT and one exact FADD, then one fused
-//     multiply-add gives its slab distance; three-input min/max close the
-//     slabs; the child hit bits of four children are decoded at once from the
-//     packed meta bytes, octant-ordered so the highest bit is the nearest
-//     child (Ylitie, Karras, Laine, HPG 2017);
+//     rebuilt from its byte with one PRMT, then one fused multiply-add gives
+//     its slab distance; three-input min/max close the slabs into an 8-bit
+//     child hit mask.  Two table lookups turn the mask into the internal
+//     children in octant order (the highest bit is the nearest child; Ylitie,
+//     Karras, Laine, HPG 2017) and into the hit triangles (two bits per slot);
 //   * node groups (base index + hit bits) on a per-thread stack; triangle
 //     groups are postponed onto the stack while few lanes of the warp have
 //     triangles, so node and triangle work stay converged;
@@ -149,6 +149,36 @@ __device__ __forceinline__ bool tri_test(const RayPre& r, float4 a, float4 b, fl
     return true;
 }
 
+// Lookup tables of the node test, in global memory (read through L1):
+// child_perm[key][m] moves bit s of m to bit s ^ key (octant order of the
+// internal children); spread2[m] moves bit s of m to bit 2s (the first
+// triangle bit of slot s).
+struct ChildPermTable { uint8_t v[8 * 256]; };
+struct Spread2Table { uint16_t v[256]; };
+constexpr ChildPermTable make_child_perm() {
+    ChildPermTable t{};
+    for (int k = 0; k < 8; ++k)
+        for (int m = 0; m < 256; ++m) {
+            int y = 0;
+            for (int b = 0; b < 8; ++b)
+                if ((m >> b) & 1) y |= 1 << (b ^ k);
+            t.v[k * 256 + m] = (uint8_t)y;
+        }
+    return t;
+}
+constexpr Spread2Table make_spread2() {
+    Spread2Table t{};
+    for (int m = 0; m < 256; ++m) {
+        int y = 0;
+        for (int b = 0; b < 8; ++b)
+            if ((m >> b) & 1) y |= 1 << (2 * b);
+        t.v[m] = (uint16_t)y;
+    }
+    return t;
+}
+static __device__ ChildPermTable g_child_perm = make_child_perm();
+static __device__ Spread2Table g_spread2 = make_spread2();
+
 // Byte k of w as the float 2^23 + byte (one PRMT).  The slab constants below
 // absorb the 2^23 offset: t = (2^23 + q) s + (a - 2^23 s).  Rounding the folded
 // constant costs at most half a quantisation step of the plane, inside the one
@@ -159,8 +189,9 @@ __device__ __forceinline__ float qbyte(uint32_t w, uint32_t k) {
 }
 
 // Intersects the eight children of node `ni`; returns the group of internal
-// children hit (base index, hit bits 24..31 in octant order | imask) and the
-// group of triangles hit (base index, bits 0..23).
+// children hit (child base, hit bits 24..31 in octant order | imask) and the
+// group of triangles hit (triangle base, hit bits 0..15 | the node's
+// tri_mask in bits 16..31, which locates each triangle: next_tri).
 __device__ __forceinline__ void node_test(const RayPre& r, const CwNode* __restrict__ nodes, uint32_t ni, float tbest,
                                           uint2& G, uint2& T) {
     const uint4* p = reinterpret_cast<const uint4*>(nodes + ni);
@@ -186,14 +217,7 @@ __device__ __forceinline__ void node_test(const RayPre& r, const CwNode* __restr
     uint32_t nfy0 = ny ? n2.z : n4.x, nfy1 = ny ? n2.w : n4.y;
     uint32_t nlz0 = nz ? n4.z : n3.x, nlz1 = nz ? n4.w : n3.y;
     uint32_t nfz0 = nz ? n3.x : n4.z, nfz1 = nz ? n3.y : n4.w;
-    // meta decode, four children per word: inner children have bits 4 and 3 set
-    uint32_t oct4 = r.oct_key * 0x01010101u;
-    uint32_t m0 = n1.z, m1 = n1.w;
-    uint32_t in0 = ((m0 & (m0 << 1)) & 0x10101010u) >> 4, in1 = ((m1 & (m1 << 1)) & 0x10101010u) >> 4;
-    uint32_t bi0 = (m0 ^ (oct4 & (in0 * 0xffu))) & 0x1f1f1f1fu;
-    uint32_t bi1 = (m1 ^ (oct4 & (in1 * 0xffu))) & 0x1f1f1f1fu;
-    uint32_t cb0 = (m0 >> 5) & 0x07070707u, cb1 = (m1 >> 5) & 0x07070707u;
-    uint32_t hits = 0;
+    uint32_t hm = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const uint32_t k = (uint32_t)(c & 3);
@@ -206,15 +230,24 @@ __device__ __forceinline__ void node_test(const RayPre& r, const CwNode* __restr
         float tfz = __fmaf_rn(qbyte(lo ? nfz0 : nfz1, k), szf, azf);
         float tn = max3f(tnx, tny, fmaxf(tnz, r.tmin));
         float tf = min3f(tfx, tfy, fminf(tfz, tbest));
-        if (tn <= tf) {
-            uint32_t bits = ((lo ? cb0 : cb1) >> (8 * k)) & 0xffu;
-            uint32_t pos = ((lo ? bi0 : bi1) >> (8 * k)) & 0xffu;
-            hits |= bits << pos;
-        }
+        hm |= (tn <= tf) ? (1u << c) : 0u;
     }
-    G = make_uint2(n1.x, (hits & 0xff000000u) | imask);
-    T = make_uint2(n1.y, hits & 0x00ffffffu);
+    // hit slots that are empty have neither an imask nor a tri_mask bit, so they drop out here
+    uint32_t inner = __ldg(&g_child_perm.v[r.oct_key * 256u + (hm & imask)]);
+    uint32_t tm = n1.z & 0xffffu;
+    uint32_t th = ((uint32_t)__ldg(&g_spread2.v[hm]) * 3u) & tm;
+    G = make_uint2(n1.x, (inner << 24) | imask);
+    T = make_uint2(n1.y, th | (tm << 16));
 }
+
+// Takes the next (lowest) hit triangle of group T, whose hit bits 0..15 must
+// not be empty, and returns its index.
+__device__ __forceinline__ uint32_t next_tri(uint2& T) {
+    uint32_t bit = (uint32_t)__ffs(T.y) - 1u;
+    T.y &= T.y - 1u;
+    return T.x + (uint32_t)__popc((T.y >> 16) & ((1u << bit) - 1u));
+}
+__device__ __forceinline__ bool has_tris(const uint2& T) { return (T.y & 0xffffu) != 0u; }
 
 struct TraceCounters { uint32_t nodes, tris; };
 
@@ -238,10 +271,8 @@ __device__ __forceinline__ uint32_t trace_ray(const RayPre& r, float tmax, const
     uint2 G = make_uint2(0u, ray_traceable(r, tmax) ? (0x80000000u | (1u << root_slot)) : 0u);
     uint2 T = make_uint2(0u, 0u);
     while (true) {
-        while (T.y != 0u) {
-            int bit = __ffs(T.y) - 1;
-            T.y &= T.y - 1u;
-            uint32_t ti = T.x + (uint32_t)bit;
+        while (has_tris(T)) {
+            uint32_t ti = next_tri(T);
             const float4* tp = reinterpret_cast<const float4*>(tris + ti);
             float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
             uint32_t prim = __float_as_uint(a.w);
@@ -319,17 +350,15 @@ __device__ __forceinline__ uint32_t trace_ray2(const RayPre& rw, float tmax, con
     uint2 G = make_uint2(0u, ray_traceable(rw, tmax) ? (0x80000000u | (1u << (7u ^ rw.oct_key))) : 0u);
     uint2 T = make_uint2(0u, 0u);
     while (true) {
-        while (T.y != 0u) {
-            int bit = __ffs(T.y) - 1;
-            T.y &= T.y - 1u;
-            uint32_t ti = T.x + (uint32_t)bit;
+        while (has_tris(T)) {
+            uint32_t ti = next_tri(T);
             if (inst == kMissPrim) {
                 // enter instance ti; this node's remaining work waits below an exit marker.
                 // The depth limits (TLAS <= kMaxTlasDepth, BLAS <= kMaxTraversalDepth) keep sp
                 // below kStackSize - kMaxTraversalDepth here; the guard only keeps writes in bounds.
                 if (sp > kStackSize - 3 - kMaxTraversalDepth) { T.y = 0u; G.y = 0u; sp = 0; break; }
                 if ((G.y & 0xff000000u) != 0u) stack[sp++] = G;
-                if (T.y != 0u) stack[sp++] = T;
+                if (has_tris(T)) stack[sp++] = make_uint2(T.x | kTriGroupFlag, T.y);
                 stack[sp++] = make_uint2(kStackExit, 0u);
                 const InstDev* I = insts + ti;
                 float m[12];
@@ -358,7 +387,7 @@ __device__ __forceinline__ uint32_t trace_ray2(const RayPre& rw, float tmax, con
             }
         }
         if ((G.y & 0xff000000u) == 0u) {
-            if (T.y != 0u) continue;
+            if (has_tris(T)) continue;
             if (sp == 0) break;
             uint2 e = stack[--sp];
             if (e.y == 0u) {  // exit marker: back to the world ray and the TLAS
@@ -371,7 +400,11 @@ __device__ __forceinline__ uint32_t trace_ray2(const RayPre& rw, float tmax, con
                 G = make_uint2(0u, 0u);
                 continue;
             }
-            if ((e.y & 0xff000000u) == 0u) { T = e; G = make_uint2(0u, 0u); continue; }  // instances of a leaf group
+            if (e.x & kTriGroupFlag) {  // instances of a leaf group
+                T = make_uint2(e.x & ~kTriGroupFlag, e.y);
+                G = make_uint2(0u, 0u);
+                continue;
+            }
             G = e;
         }
         uint32_t bit = 31u - (uint32_t)__clz(G.y & 0xff000000u);
@@ -446,7 +479,10 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
         if (__ballot_sync(0xffffffffu, has) == 0u) break;
         // node step
         if (has) {
-            if ((G.y & 0xff000000u) != 0u) {
+            if (G.x & kTriGroupFlag) {
+                T = make_uint2(G.x & ~kTriGroupFlag, G.y);  // a postponed triangle group popped from the stack
+                G = make_uint2(0u, 0u);
+            } else if ((G.y & 0xff000000u) != 0u) {
                 uint32_t bit = 31u - (uint32_t)__clz(G.y & 0xff000000u);
                 G.y &= ~(1u << bit);
                 uint32_t slot = (bit - 24u) ^ r.oct_key;
@@ -454,26 +490,21 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
                 if ((G.y & 0xff000000u) != 0u) stack[sp++] = G;
                 if (kCount) cnt->nodes++;
                 node_test(r, nodes, ni, tbest, G, T);
-            } else {
-                T = G;  // a postponed triangle group popped from the stack
-                G = make_uint2(0u, 0u);
             }
         }
         // triangle steps, postponed while fewer than 1/4 of the active lanes have triangles
         while (true) {
-            bool want = has && T.y != 0u;
+            bool want = has && has_tris(T);
             uint32_t m = __ballot_sync(0xffffffffu, want);
             if (m == 0u) break;
             uint32_t act = __ballot_sync(0xffffffffu, has);
             if (__popc(m) * 4 < __popc(act)) {
-                if (want && sp < postpone_sp) { stack[sp++] = T; T.y = 0u; }
-                if (__ballot_sync(0xffffffffu, has && T.y != 0u) == 0u) break;
-                want = has && T.y != 0u;
+                if (want && sp < postpone_sp) { stack[sp++] = make_uint2(T.x | kTriGroupFlag, T.y); T.y = 0u; }
+                if (__ballot_sync(0xffffffffu, has && has_tris(T)) == 0u) break;
+                want = has && has_tris(T);
             }
             if (want) {
-                int bit = __ffs(T.y) - 1;
-                T.y &= T.y - 1u;
-                uint32_t ti = T.x + (uint32_t)bit;
+                uint32_t ti = next_tri(T);
                 const float4* tp = reinterpret_cast<const float4*>(tris + ti);
                 float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
                 uint32_t prim = __float_as_uint(a.w);
@@ -487,7 +518,7 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
             }
         }
         // next group, or done
-        if (has && (G.y & 0xff000000u) == 0u && T.y == 0u) {
+        if (has && (G.y & 0xff000000u) == 0u && !has_tris(T)) {
             if (sp > 0 && !(kAnyHit && best_leaf != kMissPrim)) {
                 G = stack[--sp];
             } else {

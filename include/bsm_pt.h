@@ -165,7 +165,7 @@ typedef struct bsm_scene_desc {
 enum { BSM_COLLAPSE_SAH_OPTIMAL = 0, BSM_COLLAPSE_GREEDY = 1 };
 typedef struct bsm_bvh_opts {
     uint32_t sah_bins;        /* 0 = 32 */
-    uint32_t max_leaf_tris;   /* 1..3, 0 = 3 */
+    uint32_t max_leaf_tris;   /* 1..2, 0 = 2 */
     uint32_t num_threads;     /* 0 = hardware concurrency */
     uint32_t collapse;        /* binary -> 8-wide: BSM_COLLAPSE_SAH_OPTIMAL (dynamic programming over a
                                  binary tree of single-triangle leaves) or BSM_COLLAPSE_GREEDY (open the

@@ -1398,9 +1398,9 @@ ORC_API uint32_t orc_scene_bvh_nodes(void* sp) { return (uint32_t)((Scene*)sp)->
 // product's own tree (the traversal-bytes figure: 80 B per node, 48 B per
 // triangle) and to check that the quantised boxes never cull a hit.  Layout
 // of one 80-byte node: frame origin p (3 x f32), biased exponents e (3 x u8),
-// internal-child mask, child_base, tri_base, 8 meta bytes (0: empty slot;
-// internal child: 24 + slot in the low 5 bits; leaf: triangle offset in the
-// low 5 bits and a unary triangle count in the top 3), then the low planes
+// internal-child mask, child_base, tri_base, a 16-bit triangle mask (bits
+// 2s and 2s + 1: leaf slot s holds a first / a second triangle, triangles
+// stored from tri_base in slot order) and 6 pad bytes, then the low planes
 // x/y/z and the high planes x/y/z, 8 bytes each.  A triangle is 48 bytes:
 // v0, prim, v1, material, v2, transparency bits.
 //
@@ -1409,14 +1409,15 @@ ORC_API uint32_t orc_scene_bvh_nodes(void* sp) { return (uint32_t)((Scene*)sp)->
 // of byte q is at fma(2^23 + q, s, a) (near) or fma(2^23 + q, s PAD, a PAD)
 // (far), PAD = 1.00000095; a child is hit when max(near x/y/z, tmin) <=
 // min(far x/y/z, t_best).  Children are visited nearest-octant first
-// (descending slot ^ (7 ^ octant)), a leaf's triangles in ascending offset,
+// (descending slot ^ (7 ^ octant)), the hit triangles in ascending index,
 // all of a node's triangles before its next child.
 namespace orc {
 struct CwNodeO {
     float p[3];
     uint8_t e[3], imask;
     uint32_t child_base, tri_base;
-    uint8_t meta[8];
+    uint16_t tri_mask;
+    uint8_t pad[6];
     uint8_t qlo[3][8], qhi[3][8];
 };
 static_assert(sizeof(CwNodeO) == 80, "node layout");
@@ -1425,8 +1426,8 @@ static_assert(sizeof(CwTriO) == 48, "triangle layout");
 
 static float pow2_biased(uint8_t e) { uint32_t u = (uint32_t)e << 23; float f; std::memcpy(&f, &u, 4); return f; }
 
-// Hit bits of node `n`: internal children at bit 24 + (slot ^ key), triangles
-// at tri offset .. offset + count - 1.
+// Hit bits of node `n`: internal children at bit 24 + (slot ^ key), the
+// triangles of a hit leaf slot s at its tri_mask bits 2s, 2s + 1.
 static uint32_t cw_node_hits(const Ray& r, const CwNodeO& n, uint32_t key, float tbest) {
     const float PAD = 1.00000095f;
     float o[3] = {r.o.x, r.o.y, r.o.z};
@@ -1440,8 +1441,9 @@ static uint32_t cw_node_hits(const Ray& r, const CwNodeO& n, uint32_t key, float
     }
     uint32_t hits = 0;
     for (int c = 0; c < 8; ++c) {
-        uint8_t m = n.meta[c];
-        if (m == 0) continue;
+        bool inner = (n.imask >> c) & 1u;
+        uint32_t tm = ((uint32_t)n.tri_mask >> (2 * c)) & 3u;
+        if (!inner && tm == 0u) continue;   // an empty slot
         float tnear[3], tfar[3];
         for (int k = 0; k < 3; ++k) {
             bool neg = r.id[k] < 0.0f;
@@ -1453,8 +1455,8 @@ static uint32_t cw_node_hits(const Ray& r, const CwNodeO& n, uint32_t key, float
         float tn = std::fmax(std::fmax(tnear[0], tnear[1]), std::fmax(tnear[2], r.tmin));
         float tf = std::fmin(std::fmin(tfar[0], tfar[1]), std::fmin(tfar[2], tbest));
         if (!(tn <= tf)) continue;
-        if ((n.imask >> c) & 1u) hits |= 1u << (24 + ((uint32_t)c ^ key));
-        else hits |= (uint32_t)(m >> 5) << (m & 31u);
+        if (inner) hits |= 1u << (24 + ((uint32_t)c ^ key));
+        else hits |= tm << (2 * c);
     }
     return hits;
 }
@@ -1465,15 +1467,15 @@ static uint32_t cw_trace(const CwNodeO* nodes, const CwTriO* tris, const Ray& r,
     uint32_t key = 7u ^ oct;
     float tbest = r.tmax, bu = 0.0f, bv = 0.0f;
     uint32_t best_leaf = UINT32_MAX, best_prim = UINT32_MAX;
-    struct Group { uint32_t base, bits; };
+    struct Group { uint32_t base, bits, mask; };
     std::vector<Group> stack;
-    Group G{0u, ray_traceable(r) ? (0x80000000u | (1u << (7u ^ key))) : 0u};  // the root: slot 7 ^ key of a virtual parent
-    Group T{0u, 0u};
+    Group G{0u, ray_traceable(r) ? (0x80000000u | (1u << (7u ^ key))) : 0u, 0u};  // the root: slot 7 ^ key of a virtual parent
+    Group T{0u, 0u, 0u};
     while (true) {
         while (T.bits) {
             uint32_t bit = (uint32_t)__builtin_ctz(T.bits);
             T.bits &= T.bits - 1u;
-            uint32_t ti = T.base + bit;
+            uint32_t ti = T.base + (uint32_t)__builtin_popcount(T.mask & ((1u << bit) - 1u));
             const CwTriO& ct = tris[ti];
             if (cnt) cnt->tris++;
             Tri t;
@@ -1502,8 +1504,8 @@ static uint32_t cw_trace(const CwNodeO* nodes, const CwTriO* tris, const Ray& r,
         if (cnt) cnt->nodes++;
         const CwNodeO& n = nodes[ni];
         uint32_t h = cw_node_hits(r, n, key, tbest);
-        G = Group{n.child_base, (h & 0xff000000u) | n.imask};
-        T = Group{n.tri_base, h & 0x00ffffffu};
+        G = Group{n.child_base, (h & 0xff000000u) | n.imask, 0u};
+        T = Group{n.tri_base, h & 0x0000ffffu, n.tri_mask};
     }
     to = tbest; uo = bu; vo = bv;
     prim_out = best_prim;

@@ -1,7 +1,7 @@
 """The compressed 8-wide BVH built by the product (host build, no GPU).
 
-Invariants: every triangle referenced exactly once; leaves hold 1..3
-triangles and at most 24 per node; every quantised child box, decoded in
+Invariants: every triangle referenced exactly once; leaves hold 1..2
+triangles and at most 16 per node; every quantised child box, decoded in
 double precision, encloses all triangles of its subtree; depth within the
 traversal stack.  A numpy restatement of the octant-ordered traversal over
 the decoded boxes finds the same closest hits as the oracle."""
@@ -11,7 +11,7 @@ import pytest
 from conftest import random_rays
 
 NODE_DT = np.dtype([("p", "<f4", 3), ("e", "u1", 3), ("imask", "u1"), ("child_base", "<u4"), ("tri_base", "<u4"),
-                    ("meta", "u1", 8), ("qlo", "u1", (3, 8)), ("qhi", "u1", (3, 8))])
+                    ("tri_mask", "<u2"), ("pad", "u1", 6), ("qlo", "u1", (3, 8)), ("qhi", "u1", (3, 8))])
 TRI_DT = np.dtype([("v0", "<f4", 3), ("prim", "<u4"), ("v1", "<f4", 3), ("mat", "<u4"), ("v2", "<f4", 3),
                    ("pad", "<u4")])
 
@@ -25,20 +25,21 @@ def children(node):
     """Yields (slot, is_internal, child index or (first tri, count), lo(3), hi(3)) in double precision."""
     scale = np.ldexp(1.0, node["e"].astype(np.int64) - 127)
     p = node["p"].astype(np.float64)
-    internal_seen = 0
+    tmask = int(node["tri_mask"])
     for s in range(8):
-        m = int(node["meta"][s])
-        if m == 0:
+        inner = (int(node["imask"]) >> s) & 1
+        tm = (tmask >> (2 * s)) & 3
+        if not inner and tm == 0:
             continue
         lo = p + node["qlo"][:, s] * scale
         hi = p + node["qhi"][:, s] * scale
-        if (node["imask"] >> s) & 1:
+        if inner:
             rel = bin(int(node["imask"]) & ((1 << s) - 1)).count("1")
             yield s, True, int(node["child_base"]) + rel, lo, hi
-            internal_seen += 1
         else:
-            cnt = bin(m >> 5).count("1")
-            yield s, False, (int(node["tri_base"]) + (m & 31), cnt), lo, hi
+            assert tm in (1, 3), "a slot's second triangle without a first"
+            first = int(node["tri_base"]) + bin(tmask & ((1 << (2 * s)) - 1)).count("1")
+            yield s, False, (first, bin(tm).count("1")), lo, hi
 
 
 @pytest.fixture(scope="module")
@@ -83,12 +84,12 @@ def test_boxes_enclose_subtrees_and_leaf_sizes(built):
         for s, internal, ref, lo, hi in children(n):
             idx = subtree_tris(ref) if internal else list(range(ref[0], ref[0] + ref[1]))
             if not internal:
-                assert 1 <= ref[1] <= 3
+                assert 1 <= ref[1] <= 2
                 total += ref[1]
                 seen[idx] += 1
             v = np.concatenate([tris["v0"][idx], tris["v1"][idx], tris["v2"][idx]]).astype(np.float64)
             assert (v >= lo).all() and (v <= hi).all(), f"node {ni} slot {s} box does not enclose its triangles"
-        assert total <= 24
+        assert total <= 16
     assert (seen == 1).all()
 
 
