@@ -42,7 +42,7 @@ constexpr int kPostponeMaxSp = 16;    // largest stack budget for postponed tria
 struct RayPre {
     float ox, oy, oz, tmin;
     float dx, dy, dz;
-    float idx, idy, idz;     // 1 / direction (+-inf for a zero component)
+    float idx, idy, idz;     // 1 / direction, a component below 1e-20 in magnitude taken as +-1e-20
     uint32_t oct_key;        // 7 ^ (sign bits): child visiting key = slot ^ oct_key
     int kx, ky, kz;          // watertight axis permutation
     float Sx, Sy, Sz;        // watertight shear
@@ -62,16 +62,24 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
     return r;
 }
 
+__device__ __forceinline__ float box_dir(float x) { return fabsf(x) < 1e-20f ? copysignf(1e-20f, x) : x; }
+
 __device__ __forceinline__ RayPre make_ray(float4 o, float4 d) {
     RayPre r;
     r.ox = o.x; r.oy = o.y; r.oz = o.z; r.tmin = o.w;
     r.dx = d.x; r.dy = d.y; r.dz = d.z;
-    // a zero component gives an infinite reciprocal: its slab is then either
-    // (-inf, inf), or empty, or NaN when the origin lies on the plane, and the
-    // NaN is dropped by min/max — the test stays conservative.
-    r.idx = __fdiv_rn(1.0f, d.x);
-    r.idy = __fdiv_rn(1.0f, d.y);
-    r.idz = __fdiv_rn(1.0f, d.z);
+    // The box test's reciprocals: a zero (or tiny) component is taken as
+    // +-1e-20, which keeps every slab constant finite.  An infinite reciprocal
+    // would make the folded slab constants inf - inf = NaN, which min/max drop:
+    // the slab would stop culling, and a ray parallel to an axis (a sky sample
+    // at the zenith, for instance) would visit every node its other slabs
+    // allow.  The 1e-20 slope moves the ray by at most 1e-20 t across the
+    // slab, far inside the half quantisation step of padding left for a hit at
+    // t below 1e17 times the node's extent.  The triangle test uses the true
+    // direction.
+    r.idx = __fdiv_rn(1.0f, box_dir(d.x));
+    r.idy = __fdiv_rn(1.0f, box_dir(d.y));
+    r.idz = __fdiv_rn(1.0f, box_dir(d.z));
     uint32_t oct = (r.idx < 0.0f ? 1u : 0u) | (r.idy < 0.0f ? 2u : 0u) | (r.idz < 0.0f ? 4u : 0u);
     r.oct_key = 7u ^ oct;
     float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);

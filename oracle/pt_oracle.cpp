@@ -364,6 +364,7 @@ struct Ray {
     float tmin, tmax;
     uint32_t oseed;   // opacity seed (the path's PCG32 word; 0 for the stage entry points)
     float id[3];
+    float idc[3];     // reciprocals of the compressed-BVH box test: |d| below 1e-20 taken as +-1e-20
     int kx, ky, kz;
     float Sx, Sy, Sz;
 };
@@ -374,6 +375,7 @@ static Ray make_ray(F3 o, float tmin, F3 d, float tmax, uint32_t oseed = 0) {
     for (int k = 0; k < 3; ++k) {
         float dk = comp(d, k);
         r.id[k] = 1.0f / dk;
+        r.idc[k] = 1.0f / (std::fabs(dk) < 1e-20f ? std::copysign(1e-20f, dk) : dk);
     }
     float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
     int kz = 0;
@@ -1405,7 +1407,8 @@ ORC_API uint32_t orc_scene_bvh_nodes(void* sp) { return (uint32_t)((Scene*)sp)->
 // v0, prim, v1, material, v2, transparency bits.
 //
 // Arithmetic, in this order, as the device kernel evaluates it: per axis the
-// slab scale s = 2^(e-127) / d and offset a = (p - o) / d - 2^23 s; the plane
+// slab scale s = 2^(e-127) / d and offset a = (p - o) / d - 2^23 s (a component
+// d below 1e-20 in magnitude taken as +-1e-20, as the device does); the plane
 // of byte q is at fma(2^23 + q, s, a) (near) or fma(2^23 + q, s PAD, a PAD)
 // (far), PAD = 1.00000095; a child is hit when max(near x/y/z, tmin) <=
 // min(far x/y/z, t_best).  Children are visited nearest-octant first
@@ -1433,8 +1436,8 @@ static uint32_t cw_node_hits(const Ray& r, const CwNodeO& n, uint32_t key, float
     float o[3] = {r.o.x, r.o.y, r.o.z};
     float s[3], a[3], sf[3], af[3];
     for (int k = 0; k < 3; ++k) {
-        s[k] = pow2_biased(n.e[k]) * r.id[k];
-        a[k] = (n.p[k] - o[k]) * r.id[k];
+        s[k] = pow2_biased(n.e[k]) * r.idc[k];
+        a[k] = (n.p[k] - o[k]) * r.idc[k];
         a[k] = a[k] - 8388608.0f * s[k];
         sf[k] = s[k] * PAD;
         af[k] = a[k] * PAD;
@@ -1446,7 +1449,7 @@ static uint32_t cw_node_hits(const Ray& r, const CwNodeO& n, uint32_t key, float
         if (!inner && tm == 0u) continue;   // an empty slot
         float tnear[3], tfar[3];
         for (int k = 0; k < 3; ++k) {
-            bool neg = r.id[k] < 0.0f;
+            bool neg = r.idc[k] < 0.0f;
             float qn = 8388608.0f + (float)(neg ? n.qhi[k][c] : n.qlo[k][c]);
             float qf = 8388608.0f + (float)(neg ? n.qlo[k][c] : n.qhi[k][c]);
             tnear[k] = std::fmaf(qn, s[k], a[k]);
@@ -1463,7 +1466,7 @@ static uint32_t cw_node_hits(const Ray& r, const CwNodeO& n, uint32_t key, float
 
 static uint32_t cw_trace(const CwNodeO* nodes, const CwTriO* tris, const Ray& r, bool any, float& to, float& uo,
                          float& vo, uint32_t& prim_out, Counts* cnt) {
-    uint32_t oct = (r.id[0] < 0.0f ? 1u : 0u) | (r.id[1] < 0.0f ? 2u : 0u) | (r.id[2] < 0.0f ? 4u : 0u);
+    uint32_t oct = (r.idc[0] < 0.0f ? 1u : 0u) | (r.idc[1] < 0.0f ? 2u : 0u) | (r.idc[2] < 0.0f ? 4u : 0u);
     uint32_t key = 7u ^ oct;
     float tbest = r.tmax, bu = 0.0f, bv = 0.0f;
     uint32_t best_leaf = UINT32_MAX, best_prim = UINT32_MAX;

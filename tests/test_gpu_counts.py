@@ -22,7 +22,10 @@ def test_counts_and_hits_match_oracle_traversal(bsm, ctx, oracle, collapse):
     nb, tb = ctx.download_bvh(sid, st)
     short = random_rays(20000, -1.0, 1.0, seed=32, tmax=0.5)
     short[:, 3] = 1e-3
-    rays = np.concatenate([random_rays(20000, -1.0, 1.0, seed=31), short])
+    # rays along the axes (exactly zero direction components)
+    axis = random_rays(3000, -1.0, 1.0, seed=33)
+    axis[:, 4:7] = np.eye(3, dtype=np.float32)[np.arange(3000) % 3] * np.where(np.arange(3000) % 2, 1, -1)[:, None]
+    rays = np.concatenate([random_rays(20000, -1.0, 1.0, seed=31), short, axis])
     g_cnt = ctx.trace_counts(sid, rays)
     g_hit = ctx.trace_closest(sid, rays)
     o_hit, o_cnt = oracle.cwbvh_trace(nb, tb, rays)
