@@ -85,8 +85,8 @@ def workload_config(a, tris=None):
             "scene_triangles": tris, "width": a.width, "height": a.height, "spp": a.spp,
             "max_segments": a.segments, "sky": "1024x512 RGBA16F equirect + alias table", "seed": a.seed,
             "parallelism": "replicas" if a.gpus > 1 else "single GPU",
-            "l2": "inputs larger than L2 (wavefront queues ~2 GB per chunk) and a 512 MB device copy "
-                  "between timed steps flushes L2"}
+            "l2": "inputs larger than L2 (the wavefront queues hold up to 2^27 paths, 312 B each: 41 GB for "
+                  "the 1920x1080x64 frame) and a 512 MB device copy between timed steps flushes L2"}
 
 
 # ----------------------------------------------------------- distributed ----

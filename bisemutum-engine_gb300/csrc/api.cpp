@@ -261,8 +261,29 @@ bsm_status ensure_launch_cfg(bsm_context* ctx, uint32_t block, int regcap = 0) {
     return BSM_OK;
 }
 
+// Device bytes of the wavefront per path slot (the layout of ensure_wavefront):
+// 9 arrays of 16 B (rays, paths and throughputs ping-pong, hits), 64 B of cache
+// query, and (lights + 1) shadow records of 3 x 16 B + a 4 B opacity seed.
+uint64_t wavefront_bytes_per_path(uint32_t lights) { return 9 * 16 + 64 + (uint64_t)(lights + 1) * (3 * 16 + 4); }
+
+// Paths per chunk when the caller leaves it open: the whole call up to 2^27
+// paths (one chunk for a 1920x1080 frame at 64 spp), within half of the device
+// memory the context's budget has left.  Bigger chunks keep the late, short
+// segments of a frame wide enough to fill the GPU (measured on the terrain at
+// 64 spp: 1154 Mrays/s with 2^23-path chunks, 1216 with 2^24, 1249 with 2^25,
+// 1273 with one chunk).
+uint32_t default_capacity(const bsm_context* ctx, uint64_t total_paths, uint32_t lights) {
+    uint64_t left = ctx->budget > ctx->used ? ctx->budget - ctx->used + ctx->wf_buf.bytes : ctx->wf_buf.bytes;
+    uint64_t by_mem = left / 2 / wavefront_bytes_per_path(lights);
+    uint64_t c = std::min<uint64_t>(std::min<uint64_t>(total_paths, 1ull << 27), by_mem);
+    return (uint32_t)std::max<uint64_t>(c, 1024);
+}
+
 bsm_status ensure_wavefront(bsm_context* ctx, uint32_t capacity, uint32_t lights) {
     if (ctx->wf.capacity >= capacity && ctx->wf_lights >= lights && ctx->wf_buf.ptr) return BSM_OK;
+    // queue slots are 32-bit: the shadow queue holds (lights + 1) records per path
+    if ((uint64_t)capacity * (lights + 1) >= (1ull << 32))
+        return fail(ctx, BSM_ERR_INVALID_ARG, "wavefront_capacity x (lights + 1) must stay below 2^32");
     size_t C = capacity;
     size_t sh = C * (lights + 1);
     size_t bytes = 0;
@@ -1230,7 +1251,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         total_paths += (uint64_t)views[v].width * views[v].height * req[v].spp;
     }
     uint32_t cap_req = s.wavefront_capacity ? s.wavefront_capacity : (sc->tuned ? sc->tune.wavefront_capacity : 0u);
-    uint32_t capacity = cap_req ? cap_req : (uint32_t)std::min<uint64_t>(total_paths, 1u << 23);
+    uint32_t capacity = cap_req ? cap_req : default_capacity(ctx, total_paths, std::max(sc->dev.num_lights, 1u));
     capacity = std::max(capacity, 1024u);
     if ((st = ensure_wavefront(ctx, capacity, std::max(sc->dev.num_lights, 1u)))) return st;
     capacity = std::min(capacity, ctx->wf.capacity);
@@ -1504,7 +1525,8 @@ extern "C" bsm_status bsm_autotune(bsm_context* ctx, uint32_t scene_id, const bs
     if (e) { sc->tune = saved; sc->tuned = had; return e; }
     result->default_ms = cur_ms;
     const uint32_t blocks[] = {64, 128, 256};
-    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
+    const uint32_t caps[] = {1u << 20, 1u << 22, 1u << 24, 1u << 25, 1u << 26, 1u << 27};
+    const uint64_t cap_mem = default_capacity(ctx, ~0ull, std::max(sc->dev.num_lights, 1u));
     const uint32_t postpones[] = {0, 4, 8, 16};
     const uint32_t refills[] = {4, 8, 16, 24};
     for (int pass = 0; pass < 2; ++pass) {
@@ -1519,7 +1541,7 @@ extern "C" bsm_status bsm_autotune(bsm_context* ctx, uint32_t scene_id, const bs
         for (uint32_t b : blocks) if (b != cur.block_size) { bsm_tune_params p = cur; p.block_size = b; if ((e = try_one(p))) break; }
         for (uint32_t c : caps) {
             if (e) break;
-            if ((uint64_t)c > paths * 2 || c == cur.wavefront_capacity) continue;
+            if ((uint64_t)c > paths * 2 || c > cap_mem || c == cur.wavefront_capacity) continue;
             bsm_tune_params p = cur; p.wavefront_capacity = c;
             e = try_one(p);
         }

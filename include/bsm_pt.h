@@ -235,7 +235,8 @@ typedef struct bsm_pt_settings {
     uint32_t flags;            /* BSM_PT_* */
     float t_min;               /* ray TMin; 0 = default 0 (origins are offset instead) */
     float ray_offset;          /* origin offset along the geometric normal; 0 = 2e-5 * scene extent */
-    uint32_t wavefront_capacity; /* paths in flight per chunk; 0 = automatic */
+    uint32_t wavefront_capacity; /* paths in flight per chunk; 0 = the whole call up to 2^27 paths, within
+                                    half of the device memory the budget has left */
     uint32_t block_size;       /* threads per block of the traversal kernels; 0 = tuned default */
 } bsm_pt_settings;
 
