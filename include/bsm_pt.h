@@ -463,7 +463,8 @@ BSM_API bsm_status bsm_server_stop(bsm_context* ctx);
  * FP32 accumulation on the tensor cores) trained online on the path vertices
  * the tracer generates.  Paths terminate into it after a short prefix.  No
  * reference counterpart: the engine's DDGI probes (ddgi_update.cpp) are its
- * closest relative, and the plain pass stays the fallback and the judge. */
+ * closest relative, and the plain pass stays the fallback and the yardstick
+ * of its error. */
 typedef struct bsm_cache bsm_cache;
 
 typedef struct bsm_cache_settings {

@@ -3,8 +3,8 @@
 The pass does not shard beyond replicas: every rank renders its own frame and
 the only cross-rank steps are the barriers around the timed region, the max
 of the ranks' times and the sum of their rays.  These run here over gloo:
-the reductions of bench.Dist, and the reference arm launched the way the
-driver launches it (torchrun, two ranks: rank 0 prints one line, rank 1 exits
+the reductions of bench.Dist, and the reference arm launched as a multi-rank
+job is launched (torchrun, two ranks: rank 0 prints one line, rank 1 exits
 0 without work)."""
 import json
 import os
