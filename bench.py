@@ -73,6 +73,8 @@ def parse():
     p.add_argument("--max-requests", type=int, default=600, help="serve: cap on requests per rate")
     p.add_argument("--ref-spp", type=int, default=4096, help="cache: spp of the plain reference render")
     p.add_argument("--train-frames", type=int, default=120, help="cache: online training frames before timing")
+    p.add_argument("--ema", type=float, default=-1.0, help="cache: weight moving-average decay (-1: library default)")
+    p.add_argument("--cache-lr", type=float, default=-1.0, help="cache: Adam learning rate (-1: library default)")
     p.add_argument("--tune-cache", default=None, help="autotuner cache file (batch workload)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -615,6 +617,10 @@ def run_cache(a, dist):
                       "ms": float(np.mean(ms))})
     cache = bsm.RadianceCache(ctx, seed=a.seed)
     cs = bsm.cache_settings()
+    if a.ema >= 0.0:
+        cs.ema_decay = a.ema
+    if a.cache_lr > 0.0:
+        cs.lr = a.cache_lr
     t0 = time.perf_counter()
     losses = []
     for f in range(a.train_frames):
@@ -680,7 +686,8 @@ def run_cache(a, dist):
             "train": {"frames": a.train_frames, "seconds": round(train_s, 2),
                       "loss_first10": round(float(np.mean(losses[:10])), 4),
                       "loss_last10": round(float(np.mean(losses[-10:])), 4),
-                      "per_frame": "65536 training paths, 4 Adam steps of 16384 vertices, lr 1e-2"},
+                      "per_frame": f"65536 training paths, 4 Adam steps of 16384 vertices, lr {cs.lr:g}",
+                      "ema_decay": round(float(cs.ema_decay), 4)},
             "config": workload_config(a, scene.num_triangles)}
     line["config"]["workload"] = f"radiance cache on the terrain scene, {a.width}x{a.height}, cache after 2 bounces"
     if dist.rank == 0:

@@ -169,7 +169,8 @@ BSM_REQ_QUEUED, BSM_REQ_RUNNING, BSM_REQ_DONE, BSM_REQ_FAILED = 0, 1, 2, 3
 
 class CacheSettings(C.Structure):
     _fields_ = [("cache_segment", C.c_uint32), ("train_paths", C.c_uint32), ("train_segments", C.c_uint32),
-                ("train_batch", C.c_uint32), ("train_steps", C.c_uint32), ("lr", C.c_float)]
+                ("train_batch", C.c_uint32), ("train_steps", C.c_uint32), ("lr", C.c_float),
+                ("ema_decay", C.c_float)]
 
 
 class SceneGenParams(C.Structure):
@@ -270,6 +271,7 @@ _SIGS = {
     "bsm_cache_create": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
     "bsm_cache_destroy": (None, [C.c_void_p]),
     "bsm_cache_weights": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "bsm_cache_render_weights": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "bsm_cache_predict": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "bsm_cache_gradient": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)]),
     "bsm_cache_train": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,
@@ -1002,6 +1004,12 @@ class RadianceCache:
         src = None if set_to is None else np.ascontiguousarray(set_to, np.float32)
         self._st(self._L.bsm_cache_weights(self.h, w.ctypes.data, None if src is None else src.ctypes.data))
         return w if set_to is None else src
+
+    def render_weights(self) -> np.ndarray:
+        """The weights renders use: the bias-corrected moving average (ema_decay > 0), else the master weights."""
+        w = np.zeros(self.nparams, np.float32)
+        self._st(self._L.bsm_cache_render_weights(self.h, w.ctypes.data))
+        return w
 
     def predict(self, samples: np.ndarray) -> np.ndarray:
         s = np.ascontiguousarray(samples, np.float32).reshape(-1, 16)

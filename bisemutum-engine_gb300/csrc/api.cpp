@@ -1403,7 +1403,7 @@ extern "C" bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, con
     }
     std::vector<ViewReq> req(1);
     req[0] = ViewReq{*cam, settings->spp, cs.cache_segment + 1, settings->seed};
-    return render_impl(ctx, scene_id, req, *settings, output, stats, cache->w_bf16, cs.cache_segment);
+    return render_impl(ctx, scene_id, req, *settings, output, stats, cache_render_weights(cache), cs.cache_segment);
 }
 
 extern "C" bsm_status bsm_render_batch(bsm_context* ctx, uint32_t scene_id, const bsm_view_desc* views,

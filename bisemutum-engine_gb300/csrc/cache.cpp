@@ -35,7 +35,10 @@ void upload_weights(bsm_cache* c, const float* w) {
     cudaMemcpy(c->w_bf16, b.data(), kMlpParams * 2, cudaMemcpyHostToDevice);
     cudaMemset(c->adam_m, 0, kMlpParams * 4);
     cudaMemset(c->adam_v, 0, kMlpParams * 4);
+    cudaMemset(c->w_ema, 0, kMlpParams * 4);
     c->step = 0;
+    c->ema_steps = 0;
+    c->ema_decay = 0.0f;
 }
 
 }  // namespace
@@ -48,6 +51,7 @@ extern "C" void bsm_cache_settings_default(bsm_cache_settings* cs) {
     cs->train_batch = 16384;
     cs->train_steps = 4;
     cs->lr = 1e-2f;
+    cs->ema_decay = 0.99f;
 }
 
 extern "C" uint32_t bsm_cache_param_count(void) { return (uint32_t)kMlpParams; }
@@ -61,6 +65,8 @@ extern "C" bsm_status bsm_cache_create(bsm_context* ctx, uint64_t seed, bsm_cach
     cudaSetDevice(c->device);
     bool ok = cudaMalloc((void**)&c->w_master, kMlpParams * 4) == cudaSuccess &&
               cudaMalloc(&c->w_bf16, kMlpParams * 2) == cudaSuccess &&
+              cudaMalloc((void**)&c->w_ema, kMlpParams * 4) == cudaSuccess &&
+              cudaMalloc(&c->w_ema_bf16, kMlpParams * 2) == cudaSuccess &&
               cudaMalloc((void**)&c->adam_m, kMlpParams * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->adam_v, kMlpParams * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->dW, kMlpParams * 4) == cudaSuccess &&
@@ -91,7 +97,7 @@ extern "C" void bsm_cache_destroy(bsm_cache* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
-    for (void* p : {(void*)c->w_master, c->w_bf16, (void*)c->adam_m, (void*)c->adam_v, (void*)c->dW, (void*)c->loss,
+    for (void* p : {(void*)c->w_master, c->w_bf16, (void*)c->w_ema, c->w_ema_bf16, (void*)c->adam_m, (void*)c->adam_v, (void*)c->dW, (void*)c->loss,
                     (void*)c->samples, (void*)c->sample_count, (void*)c->view_dev, (void*)c->io})
         if (p) cudaFree(p);
     delete c;
@@ -103,6 +109,17 @@ extern "C" bsm_status bsm_cache_weights(bsm_cache* c, float* get, const float* s
     if (get && cudaMemcpy(get, c->w_master, kMlpParams * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BSM_ERR_CUDA;
     if (set) upload_weights(c, set);
     return cudaGetLastError() == cudaSuccess ? BSM_OK : BSM_ERR_CUDA;
+}
+
+extern "C" bsm_status bsm_cache_render_weights(bsm_cache* c, float* out) {
+    if (!c || !out) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    if (c->ema_steps == 0) return cudaMemcpy(out, c->w_master, kMlpParams * 4, cudaMemcpyDeviceToHost) == cudaSuccess
+                                      ? BSM_OK : BSM_ERR_CUDA;
+    if (cudaMemcpy(out, c->w_ema, kMlpParams * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BSM_ERR_CUDA;
+    double corr = 1.0 / (1.0 - std::pow((double)c->ema_decay, (double)c->ema_steps));
+    for (int i = 0; i < kMlpParams; ++i) out[i] = (float)(out[i] * corr);
+    return BSM_OK;
 }
 
 extern "C" bsm_status bsm_cache_predict(bsm_cache* c, const float* samples, uint32_t n, float* out) {
@@ -136,7 +153,12 @@ extern "C" bsm_status bsm_cache_gradient(bsm_cache* c, const float* samples, uin
 
 namespace {
 bsm_status train_device(bsm_cache* c, const float4* samples, uint32_t n, uint32_t batch, float lr, cudaStream_t st,
-                        float* mean_loss) {
+                        float* mean_loss, float ema_decay = 0.0f) {
+    if (ema_decay != c->ema_decay) {  // a new decay starts a new average
+        cudaMemsetAsync(c->w_ema, 0, kMlpParams * 4, st);
+        c->ema_steps = 0;
+        c->ema_decay = ema_decay;
+    }
     if (batch == 0) batch = 16384;
     double loss_sum = 0.0;
     uint32_t steps = 0;
@@ -147,7 +169,9 @@ bsm_status train_device(bsm_cache* c, const float4* samples, uint32_t n, uint32_
         if (launch_mlp_train(c->device, st, c->w_bf16, samples + 4 * (size_t)off, nb, c->dW, c->loss) != cudaSuccess)
             return BSM_ERR_CUDA;
         c->step++;
-        if (launch_mlp_adam(st, c->w_master, c->w_bf16, c->dW, c->adam_m, c->adam_v, lr, c->step) != cudaSuccess)
+        if (ema_decay > 0.0f) c->ema_steps++;
+        if (launch_mlp_adam(st, c->w_master, c->w_bf16, c->dW, c->adam_m, c->adam_v, lr, c->step, c->w_ema,
+                            c->w_ema_bf16, ema_decay, c->ema_steps) != cudaSuccess)
             return BSM_ERR_CUDA;
         float l = 0.0f;
         cudaMemcpyAsync(&l, c->loss, 4, cudaMemcpyDeviceToHost, st);
@@ -228,6 +252,6 @@ bsm_status cache_train_frame(bsm_cache* c, const DevScene& sc, const DevView& vi
     n = std::min(n, c->sample_cap);
     uint32_t use = std::min(n, cs.train_batch * cs.train_steps);
     if (samples_out) *samples_out = n;
-    return train_device(c, c->samples, use, cs.train_batch, cs.lr, st, loss_out);
+    return train_device(c, c->samples, use, cs.train_batch, cs.lr, st, loss_out, cs.ema_decay);
 }
 }  // namespace bsm

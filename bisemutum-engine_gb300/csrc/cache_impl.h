@@ -12,6 +12,10 @@ struct bsm_cache {
     int device = 0;
     float* w_master = nullptr;   // fp32 master weights (kMlpParams)
     void* w_bf16 = nullptr;      // bf16 copy read by the kernels
+    float* w_ema = nullptr;      // moving average of the master weights (zero-started, bias-corrected on use)
+    void* w_ema_bf16 = nullptr;  // bf16 copy of the corrected average, read by renders
+    int ema_steps = 0;           // Adam steps averaged (0: renders read w_bf16)
+    float ema_decay = 0.0f;      // decay of the running average
     float* adam_m = nullptr;
     float* adam_v = nullptr;
     float* dW = nullptr;
@@ -27,6 +31,8 @@ struct bsm_cache {
 };
 
 namespace bsm {
+// The bf16 weights renders read: the corrected moving average once it holds a step, else the current ones.
+inline const void* cache_render_weights(const bsm_cache* c) { return c->ema_steps > 0 ? c->w_ema_bf16 : c->w_bf16; }
 // Runs train paths + Adam steps for one camera (cache.cpp).
 bsm_status cache_train_frame(bsm_cache* c, const DevScene& sc, const DevView& view, const bsm_cache_settings& cs,
                              cudaStream_t st, float* loss_out, uint32_t* samples_out);

@@ -149,8 +149,10 @@ cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, cons
                                float* out);
 cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
                              float* dW, float* loss);
+// Adam step; with ema_decay > 0 also updates the weights' moving average `ema` and writes its
+// bias-corrected bf16 copy `ema_b` (ema_step: steps averaged, this one included)
 cudaError_t launch_mlp_adam(cudaStream_t st, float* wm, void* wb, const float* dW, float* m, float* v, float lr,
-                            int step);
+                            int step, float* ema, void* ema_b, float ema_decay, int ema_step);
 // training paths (train_paths.cu): full-length paths that record per-vertex cache samples
 void launch_train_paths(cudaStream_t st, const DevScene& sc, const DevView* view, uint32_t n_paths, uint32_t frame,
                         uint32_t max_segments, float4* samples, uint32_t* count, uint32_t max_samples);

@@ -474,6 +474,8 @@ typedef struct bsm_cache_settings {
     uint32_t train_batch;     /* samples per Adam step (16384) */
     uint32_t train_steps;     /* Adam steps per frame (4); 0 = render only */
     float lr;                 /* Adam learning rate (1e-2) */
+    float ema_decay;          /* renders read an exponential moving average of the weights with this
+                                 decay per Adam step (bias-corrected); 0 = the current weights */
 } bsm_cache_settings;
 
 BSM_API void bsm_cache_settings_default(bsm_cache_settings* cs);
@@ -484,6 +486,9 @@ BSM_API bsm_status bsm_cache_create(bsm_context* ctx, uint64_t seed, bsm_cache**
 BSM_API void bsm_cache_destroy(bsm_cache* cache);
 /* Reads (get != NULL) and/or writes (set != NULL) the fp32 master weights; a write resets Adam. */
 BSM_API bsm_status bsm_cache_weights(bsm_cache* cache, float* get, const float* set);
+/* Reads the weights renders use (bsm_cache_param_count floats): the bias-corrected moving average of the
+ * master weights over the Adam steps taken with ema_decay > 0, or the master weights before any. */
+BSM_API bsm_status bsm_cache_render_weights(bsm_cache* cache, float* out);
 /* samples: n x 16 floats (12 raw inputs, 3 target radiance, 1 unused), host memory.
  * Prediction (n x 3) / gradient of the mean relative L2 loss (bsm_cache_param_count floats). */
 BSM_API bsm_status bsm_cache_predict(bsm_cache* cache, const float* samples, uint32_t n, float* out);

@@ -130,3 +130,28 @@ def test_trained_cache_gains_over_the_method_without_it(bsm, ctx):
     finally:
         c.close()
         off.close()
+
+
+def test_renders_read_the_corrected_moving_average(bsm, ctx):
+    """With ema_decay d the weights renders read are e_k / (1 - d^k), e_k = d e_(k-1) + (1 - d) w_k over the
+    master weights w_k after each Adam step (e_0 = 0); before any averaged step they are the master weights."""
+    scene = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=41, spheres=8)
+    sid = ctx.load_scene(scene)
+    cam = bsm.make_camera(tuple(scene.camera.position), tuple(scene.camera.front), width=32, height=32)
+    c = bsm.RadianceCache(ctx, seed=9)
+    try:
+        d = 0.9
+        cs = bsm.cache_settings(train_paths=4096, train_batch=8192, train_steps=1, cache_segment=2, ema_decay=d)
+        assert np.array_equal(c.render_weights(), c.weights())
+        e = np.zeros(c.nparams, np.float64)
+        for k in range(1, 7):
+            c.render(sid, cam, bsm.settings(spp=1, seed=k), cs, outputs=False)
+            e = d * e + (1.0 - d) * c.weights().astype(np.float64)
+            np.testing.assert_allclose(c.render_weights(), e / (1.0 - d ** k), rtol=2e-5, atol=2e-7)
+        # a cache whose weights are set again renders with them until it trains
+        w = c.weights()
+        c.weights(w)
+        assert np.array_equal(c.render_weights(), w)
+    finally:
+        c.close()
+    ctx.release(sid)
