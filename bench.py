@@ -71,6 +71,8 @@ def parse():
     p.add_argument("--rates", default="10,50,100,200,500,1000,2000", help="serve: Poisson arrival rates (req/s)")
     p.add_argument("--serve-seconds", type=float, default=6.0, help="serve: arrival window per rate")
     p.add_argument("--max-requests", type=int, default=600, help="serve: cap on requests per rate")
+    p.add_argument("--serve-chunk", type=int, default=1 << 21, help="serve: paths per chunk")
+    p.add_argument("--serve-lanes", type=int, default=4, help="serve: lanes (streams)")
     p.add_argument("--ref-spp", type=int, default=4096, help="cache: spp of the plain reference render")
     p.add_argument("--train-frames", type=int, default=120, help="cache: online training frames before timing")
     p.add_argument("--ema", type=float, default=-1.0, help="cache: weight moving-average decay (-1: library default)")
@@ -495,7 +497,7 @@ def run_serve(a, dist):
     results = []
     for lam in [float(x) for x in a.rates.split(",")]:
         n = int(min(a.max_requests, max(20, lam * a.serve_seconds)))
-        ctx.server_start(pool_bytes=16 << 30, chunk_paths=1 << 21, lanes=4)
+        ctx.server_start(pool_bytes=16 << 30, chunk_paths=a.serve_chunk, lanes=a.serve_lanes)
         arrivals = np.cumsum(rng.exponential(1.0 / lam, n))
         reqs = []
         for i in range(n):
@@ -530,8 +532,8 @@ def run_serve(a, dist):
     line = {"workload": "serve", "metric": "p50/p99 request latency and rays/s per Poisson arrival rate",
             "scenes_triangles": tris, "setup_s": round(setup_s, 1), "results": results, "saturated": saturated,
             "request_mix": "scene uniform, resolution log-uniform 128x128..1920x1080, spp {1,4,16,32}, "
-                           "bounces {2,4,8}", "server": {"pool_bytes": 16 << 30, "chunk_paths": 1 << 21,
-                                                          "lanes": 4}}
+                           "bounces {2,4,8}", "server": {"pool_bytes": 16 << 30, "chunk_paths": a.serve_chunk,
+                                                          "lanes": a.serve_lanes}}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -550,7 +552,7 @@ def serve_saturated(a, bsm, ctx, ids, scenes, rng, n=240):
         base = scenes[k].camera
         cam = bsm.make_camera(tuple(base.position), tuple(base.front), width=w, height=h)
         reqs.append((k, cam, int(rng.choice([1, 4, 16, 32])), int(rng.choice([2, 4, 8])), int(i + 1)))
-    ctx.server_start(pool_bytes=16 << 30, chunk_paths=1 << 21, lanes=4)
+    ctx.server_start(pool_bytes=16 << 30, chunk_paths=a.serve_chunk, lanes=a.serve_lanes)
     ctx.sync()
     t0 = time.perf_counter()
     rids = [ctx.submit(ids[k], cam, spp, segs, seed)[0] for k, cam, spp, segs, seed in reqs]
