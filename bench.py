@@ -64,7 +64,7 @@ def parse():
     p.add_argument("--tri-cost", type=float, default=0.0, help="SAH-optimal collapse: triangle / node test cost")
     p.add_argument("--bins", type=int, default=0, help="binned SAH bins (0 = 32)")
     p.add_argument("--max-leaf", type=int, default=0, help="largest leaf (triangles, 1..2; 0 = 2)")
-    p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "cache"],
+    p.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "cache", "instanced"],
                    help="plain: the single-frame pass (the bench line); batch: 256 uneven views in one wavefront "
                         "against a loop of plain renders")
     p.add_argument("--views", type=int, default=256)
@@ -579,6 +579,43 @@ def serve_saturated(a, bsm, ctx, ids, scenes, rng, n=240):
             "same_rays": bool(rays == brays), "efficiency": round(batch_s / serve_s, 3)}
 
 
+# ------------------------------------------------------------- instanced ----
+def run_instanced(a, dist):
+    """Two-level scene (the reference's TLAS of drawables): a 512x512 ground grid and 4,000 instances of a UV
+    sphere, a box and a tetrahedron, rendered through the TLAS + BLAS traversal and, for comparison, as the same
+    triangles flattened into one world-space BVH; 1920x1080, 16 spp, 8 segments."""
+    bsm = importlib.import_module("bisemutum-engine_gb300")
+    ctx = bsm.Context(dist.local)
+    inst = bsm.generate_instanced_scene(seed=a.seed, instances=4000, ground=512, width=a.width, height=a.height)
+    flat = inst.flattened()
+    spp = 16
+    out = {}
+    for name, sid in (("two_level", ctx.load_instanced(inst)), ("flat", ctx.load_scene(flat))):
+        s = bsm.settings(spp=spp, max_segments=a.segments, seed=a.seed, flags=bsm.BSM_PT_STAGE_TIMING)
+        for _ in range(a.warmup):
+            ctx.render(sid, [inst.camera], s, outputs=False)
+        ms, rays, stages = 0.0, 0, None
+        for _ in range(a.steps):
+            _, st = ctx.render(sid, [inst.camera], s, outputs=False)
+            ms += st.ms_total
+            rays += st.extend_rays
+            stages = {"extend": round(st.ms_extend, 3), "shadow": round(st.ms_shadow, 3),
+                      "shade": round(st.ms_shade, 3)}
+        out[name] = {"mrays_per_s": round(rays / ms / 1e3, 1), "ms_per_frame": round(ms / a.steps, 2),
+                     "stages_ms": stages}
+        ctx.release(sid)
+    ctx.close()
+    line = {"workload": "instanced", "metric": "Mrays/s, two-level scene vs the same triangles flattened",
+            "triangles": int(flat.num_triangles), "instances": int(len(inst.inst_geometry)),
+            "two_level": out["two_level"], "flat": out["flat"],
+            "ratio": round(out["two_level"]["mrays_per_s"] / out["flat"]["mrays_per_s"], 3),
+            "config": {"workload": f"instanced ground + 4000 objects, {a.width}x{a.height}, {spp} spp, "
+                                   f"{a.segments} segments", "seed": a.seed}}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 # ----------------------------------------------------------------- cache ----
 def run_cache(a, dist):
     """Radiance cache on the terrain scene: relMSE against a high-spp plain render and device time per frame,
@@ -711,6 +748,8 @@ def main():
             return run_serve(a, dist)
         if a.workload == "cache":
             return run_cache(a, dist)
+        if a.workload == "instanced":
+            return run_instanced(a, dist)
         return run_ours(a, dist)
     finally:
         dist.close()

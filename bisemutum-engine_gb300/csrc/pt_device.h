@@ -114,6 +114,7 @@ struct Wavefront {
 
 struct LaunchCfg {
     int grid_persistent;    // blocks for the persistent traversal kernels
+    int grid_persistent2;   // blocks for the persistent two-level traversal kernels
     int block_trace;        // threads per block, traversal
     int block_shade;        // threads per block, shading / camera
     int grid_shade;

@@ -145,43 +145,48 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_shadow(DevScene sc, Wavefro
 }
 
 // ------------------------------------------------- two-level extend / shadow ----
-// Two-level scenes: one ray per thread over the queue (grid-stride); the hit
-// record carries the instance in place of u.
-__global__ void __launch_bounds__(256) k_extend2(DevScene sc, const float4* __restrict__ ray_o,
-                                                 const float4* __restrict__ ray_d, const uint4* __restrict__ path,
-                                                 float4* __restrict__ hit, const uint32_t* counters,
-                                                 unsigned long long* stats, uint32_t seg) {
+// Two-level scenes: persistent warps over the queue with trace_queue2 (TLAS
+// leaves enter instances).  The hit record carries the instance in place of u.
+template <bool kOpacity>
+__global__ void __launch_bounds__(256, 2) k_extend2(DevScene sc, const float4* __restrict__ ray_o,
+                                                    const float4* __restrict__ ray_d, const uint4* __restrict__ path,
+                                                    float4* __restrict__ hit, uint32_t* counters,
+                                                    unsigned long long* stats, uint32_t seg, int postpone_sp,
+                                                    int refill_min) {
     const uint32_t n = counters[kCntQueue + seg];
     if (blockIdx.x == 0 && threadIdx.x == 0) stats[kStatExtend + seg] += n;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 o = ray_o[i], d = ray_d[i];
-        RayPre r = make_ray(o, d);
-        float t, u, v;
-        uint32_t inst;
-        uint32_t leaf = trace_ray2<false>(r, d.w, sc.nodes, sc.insts, sc.mat_tr, t, u, v, inst,
-                                          sc.mat_tr ? path[i].z : 0u);
-        hit[i] = make_float4(t, __uint_as_float(leaf), __uint_as_float(inst), v);
-    }
+    trace_queue2<false, kOpacity>(
+        sc.nodes, sc.insts, sc.mat_tr, n, counters + kCntWork + 2 * seg,
+        [&](uint32_t i, float4& o, float4& d) { o = ray_o[i]; d = ray_d[i]; },
+        [&](uint32_t i, uint32_t leaf, float t, float, float v, uint32_t inst) {
+            hit[i] = make_float4(t, __uint_as_float(leaf), __uint_as_float(inst), v);
+        },
+        [&](uint32_t i) { return path[i].z; },   // the path's PCG32 word
+        postpone_sp, refill_min);
 }
 
-__global__ void __launch_bounds__(256) k_shadow2(DevScene sc, Wavefront wf, uint32_t seg, float4* accum) {
+template <bool kOpacity>
+__global__ void __launch_bounds__(256, 2) k_shadow2(DevScene sc, Wavefront wf, uint32_t seg, float4* accum,
+                                                    int postpone_sp, int refill_min) {
     const uint32_t n_sun = wf.counters[kCntShadow + seg], n_sky = wf.counters[kCntSky + seg];
     const uint32_t sh_cap = wf.capacity * (sc.num_lights + 1u);
     const uint32_t n = n_sun + n_sky;
     if (blockIdx.x == 0 && threadIdx.x == 0) wf.stats[kStatShadow + seg] += n;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t k = i < n_sun ? i : sh_cap - 1u - (i - n_sun);
-        float4 o = wf.sh_o[k], d = wf.sh_d[k];
-        RayPre r = make_ray(o, d);
-        float t, u, v;
-        uint32_t inst;
-        uint32_t leaf = trace_ray2<true>(r, d.w, sc.nodes, sc.insts, sc.mat_tr, t, u, v, inst,
-                                         (sc.mat_tr && wf.sh_seed) ? wf.sh_seed[k] : 0u);
-        if (leaf == kMissPrim) {
-            float4 c = wf.sh_c[k];
-            accum_add(accum, __float_as_uint(c.w), v3(c.x, c.y, c.z));
-        }
-    }
+    const float4* __restrict__ so = wf.sh_o;
+    const float4* __restrict__ sd = wf.sh_d;
+    const float4* __restrict__ scn = wf.sh_c;
+    auto slot = [=](uint32_t i) { return i < n_sun ? i : sh_cap - 1u - (i - n_sun); };
+    trace_queue2<true, kOpacity>(
+        sc.nodes, sc.insts, sc.mat_tr, n, wf.counters + kCntWork + 2 * seg + 1,
+        [&](uint32_t i, float4& o, float4& d) { uint32_t k = slot(i); o = so[k]; d = sd[k]; },
+        [&](uint32_t i, uint32_t leaf, float, float, float, uint32_t) {
+            if (leaf == kMissPrim) {
+                float4 c = scn[slot(i)];
+                accum_add(accum, __float_as_uint(c.w), v3(c.x, c.y, c.z));
+            }
+        },
+        [&](uint32_t i) { return wf.sh_seed ? wf.sh_seed[slot(i)] : 0u; },
+        postpone_sp, refill_min);
 }
 
 // ----------------------------------------------------------------- shade ----
@@ -546,9 +551,16 @@ void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, con
                                                                      wf.hit, wf.counters, wf.stats, seg,        \
                                                                      lc.postpone_sp, lc.refill_min)
     const bool op = sc.has_non_opaque != 0;
-    if (sc.insts)
-        k_extend2<<<lc.grid_shade, 256, 0, st>>>(sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit, wf.counters,
-                                                   wf.stats, seg);
+    if (sc.insts) {
+        if (op)
+            k_extend2<true><<<lc.grid_persistent2, lc.block_trace, 0, st>>>(
+                sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit, wf.counters, wf.stats, seg, lc.postpone_sp,
+                lc.refill_min);
+        else
+            k_extend2<false><<<lc.grid_persistent2, lc.block_trace, 0, st>>>(
+                sc, wf.ray_o[q], wf.ray_d[q], wf.path[q], wf.hit, wf.counters, wf.stats, seg, lc.postpone_sp,
+                lc.refill_min);
+    }
     else if (count_traversal) { if (op) BSM_EXTEND(true, 1, true); else BSM_EXTEND(true, 1, false); }
     else if (lc.regcap) { if (op) BSM_EXTEND(false, 4, true); else BSM_EXTEND(false, 4, false); }
     else { if (op) BSM_EXTEND(false, 1, true); else BSM_EXTEND(false, 1, false); }
@@ -563,9 +575,14 @@ void launch_shadow(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, con
 #define BSM_SHADOW(B, O) \
     k_shadow<B, O><<<lc.grid_persistent, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp, lc.refill_min)
     const bool op = sc.has_non_opaque != 0;
-    if (sc.insts)
-        k_shadow2<<<lc.grid_shade, 256, 0, st>>>(sc, wf, seg, accum);
-    else if (lc.regcap) { if (op) BSM_SHADOW(4, true); else BSM_SHADOW(4, false); }
+    if (sc.insts) {
+        if (op)
+            k_shadow2<true><<<lc.grid_persistent2, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp,
+                                                                            lc.refill_min);
+        else
+            k_shadow2<false><<<lc.grid_persistent2, lc.block_trace, 0, st>>>(sc, wf, seg, accum, lc.postpone_sp,
+                                                                             lc.refill_min);
+    } else if (lc.regcap) { if (op) BSM_SHADOW(4, true); else BSM_SHADOW(4, false); }
     else { if (op) BSM_SHADOW(1, true); else BSM_SHADOW(1, false); }
 #undef BSM_SHADOW
 }
@@ -608,6 +625,12 @@ void query_launch_cfg(int device, int block_trace, LaunchCfg* lc) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<1, true>, block_trace, 0);
     }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_shade, k_shade, 256, 0);
+    int per_sm2_ext = 0, per_sm2_sh = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2_ext, k_extend2<true>, block_trace, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2_sh, k_shadow2<true>, block_trace, 0);
+    int per_sm2 = per_sm2_ext < per_sm2_sh ? per_sm2_ext : per_sm2_sh;
+    if (per_sm2 < 1) per_sm2 = 1;
+    lc->grid_persistent2 = sms * per_sm2;
     int per_sm = per_sm_ext < per_sm_sh ? per_sm_ext : per_sm_sh;
     if (per_sm < 1) per_sm = 1;
     if (per_sm_shade < 1) per_sm_shade = 1;

@@ -538,3 +538,161 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
 }
 
 }  // namespace bsm
+
+namespace bsm {
+
+constexpr int kStackSize2 = 64;   // two-level: TLAS groups (<= 12 + 1) + exit marker + BLAS groups + postponed
+static_assert(kMaxTlasDepth + 3 + kMaxTraversalDepth + kPostponeMaxSp <= kStackSize2, "two-level stack budget");
+
+// Persistent, warp-synchronous traversal of a queue of rays through a two-level
+// scene (TLAS over per-geometry BLASes), with trace_queue's refill and
+// triangle postponing.  A TLAS leaf "triangle" is an instance: a lane that
+// reaches one pushes the rest of its TLAS work and an exit marker, moves its
+// ray into the instance's space and continues in the BLAS on the same stack;
+// popping the marker reloads the world ray (`load`) and returns to the TLAS.
+// Triangle groups are postponed only inside a BLAS, at most `postpone_sp`
+// entries above the BLAS's exit marker, so the stack stays within
+// kStackSize2 (TLAS depth <= kMaxTlasDepth, BLAS depth <= kMaxTraversalDepth).
+// Results and the opacity rule are those of trace_ray2: object-space
+// triangle tests with t unchanged, ties to the lower global primitive id,
+// candidate hits on non-opaque triangles decided with the world ray.
+// `finish(index, leaf, t, u, v, instance)`.
+template <bool kAnyHit, bool kOpacity, class Load, class Finish, class Seed>
+__device__ __forceinline__ void trace_queue2(const CwNode* __restrict__ tlas, const InstDev* __restrict__ insts,
+                                             const float* __restrict__ mat_tr, uint32_t n, uint32_t* work, Load load,
+                                             Finish finish, Seed seed, int postpone_sp, int refill_min) {
+    postpone_sp = postpone_sp < kPostponeMaxSp ? postpone_sp : kPostponeMaxSp;
+    const uint32_t lane = threadIdx.x & 31u;
+    bool has = false;
+    bool exhausted = false;  // warp-uniform
+    RayPre r;
+    float tbest = 0.0f, bu = 0.0f, bv = 0.0f;
+    uint32_t best_leaf = kMissPrim, best_prim = kMissPrim, best_inst = kMissPrim, idx = 0;
+    const CwNode* nodes = tlas;
+    const CwTri* tris = nullptr;   // nullptr: traversing the TLAS
+    uint32_t inst = kMissPrim, prim_base = 0u, mat_override = kMissPrim;
+    uint2 G = make_uint2(0, 0), T = make_uint2(0, 0);
+    uint2 stack[kStackSize2];
+    int sp = 0, sp_blas = 0;       // sp_blas: stack depth just above the current BLAS's exit marker
+    while (true) {
+        uint32_t idle = __ballot_sync(0xffffffffu, !has);
+        if (!exhausted && (__popc(idle) >= refill_min || idle == 0xffffffffu)) {
+            uint32_t cntn = (uint32_t)__popc(idle);
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(work, cntn);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (!has) {
+                uint32_t i = base + (uint32_t)__popc(idle & lanemask_lt());
+                if (i < n) {
+                    float4 o, d;
+                    load(i, o, d);
+                    r = make_ray(o, d);
+                    tbest = d.w;
+                    best_leaf = kMissPrim; best_prim = kMissPrim; best_inst = kMissPrim; bu = 0.0f; bv = 0.0f;
+                    nodes = tlas; tris = nullptr; inst = kMissPrim; prim_base = 0u; mat_override = kMissPrim;
+                    G = make_uint2(0u, ray_traceable(r, d.w) ? (0x80000000u | (1u << (7u ^ r.oct_key))) : 0u);
+                    T = make_uint2(0u, 0u);
+                    sp = 0;
+                    sp_blas = 0;
+                    idx = i;
+                    has = true;
+                }
+            }
+            if (base + cntn >= n) exhausted = true;
+        }
+        const uint32_t act = __ballot_sync(0xffffffffu, has);
+        if (act == 0u) break;
+        // node step
+        if (has) {
+            if (G.x & kTriGroupFlag) {
+                T = make_uint2(G.x & ~kTriGroupFlag, G.y);  // a postponed triangle group popped from the stack
+                G = make_uint2(0u, 0u);
+            } else if ((G.y & 0xff000000u) != 0u) {
+                uint32_t bit = 31u - (uint32_t)__clz(G.y & 0xff000000u);
+                G.y &= ~(1u << bit);
+                uint32_t slot = (bit - 24u) ^ r.oct_key;
+                uint32_t ni = G.x + (uint32_t)__popc(G.y & 0xffu & ((1u << slot) - 1u));
+                if ((G.y & 0xff000000u) != 0u) stack[sp++] = G;
+                node_test(r, nodes, ni, tbest, G, T);
+            }
+        }
+        // leaf steps: instances in the TLAS, triangles (postponed while few lanes have them) in a BLAS
+        while (true) {
+            bool want = has && has_tris(T);
+            uint32_t m = __ballot_sync(0xffffffffu, want);
+            if (m == 0u) break;
+            if (__popc(m) * 4 < __popc(act)) {
+                if (want && tris != nullptr && sp < sp_blas + postpone_sp) {
+                    stack[sp++] = make_uint2(T.x | kTriGroupFlag, T.y);
+                    T.y = 0u;
+                }
+                if (__ballot_sync(0xffffffffu, has && has_tris(T)) == 0u) break;
+                want = has && has_tris(T);
+            }
+            if (!want) continue;
+            uint32_t ti = next_tri(T);
+            if (tris == nullptr) {
+                // enter instance ti: this node's remaining work waits below an exit marker
+                if ((G.y & 0xff000000u) != 0u) stack[sp++] = G;
+                if (has_tris(T)) stack[sp++] = make_uint2(T.x | kTriGroupFlag, T.y);
+                stack[sp++] = make_uint2(kStackExit, 0u);
+                sp_blas = sp;
+                const InstDev* I = insts + ti;
+                float mx[12];
+                load_xform(I->w2o, mx);
+                r = make_ray(xform_point(mx, r.ox, r.oy, r.oz, r.tmin), xform_dir(mx, r.dx, r.dy, r.dz, 0.0f));
+                nodes = I->nodes;
+                tris = I->tris;
+                prim_base = I->prim_base;
+                mat_override = I->material;
+                inst = ti;
+                G = make_uint2(0u, 0x80000000u | (1u << (7u ^ r.oct_key)));
+                T = make_uint2(0u, 0u);
+                continue;
+            }
+            const float4* tp = reinterpret_cast<const float4*>(tris + ti);
+            float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            uint32_t prim = prim_base + __float_as_uint(a.w);
+            float t, u, v;
+            if (tri_test(r, a, b, c, tbest, prim, best_prim, t, u, v)) {
+                bool keep = true;
+                if (kOpacity && mat_tr) {
+                    float tr = mat_tr[mat_override != kMissPrim ? mat_override : __float_as_uint(b.w)];
+                    if (tr != 0.0f) {   // the rule reads the world ray
+                        float4 o4, d4;
+                        load(idx, o4, d4);
+                        keep = keep_hit(make_ray(o4, d4), tr, seed(idx));
+                    }
+                }
+                if (keep) {
+                    tbest = t; best_leaf = ti; best_prim = prim; best_inst = inst; bu = u; bv = v;
+                    if (kAnyHit) { T.y = 0u; G.y = 0u; sp = 0; }
+                }
+            }
+        }
+        // next group, or done
+        if (has && (G.y & 0xff000000u) == 0u && !has_tris(T)) {
+            const bool done = kAnyHit && best_leaf != kMissPrim;
+            uint2 e = make_uint2(0u, 0u);
+            if (!done && sp > 0) {
+                e = stack[--sp];
+                if (e.y == 0u) {  // exit marker: back to the world ray and the TLAS
+                    float4 o4, d4;
+                    load(idx, o4, d4);
+                    r = make_ray(o4, d4);
+                    nodes = tlas; tris = nullptr; inst = kMissPrim; prim_base = 0u; mat_override = kMissPrim;
+                    sp_blas = 0;
+                    e = sp > 0 ? stack[--sp] : make_uint2(0u, 0u);
+                }
+            }
+            if (e.y != 0u) {
+                G = e;
+            } else {
+                finish(idx, best_leaf, tbest, bu, bv, best_inst);
+                has = false;
+            }
+        }
+    }
+}
+
+}  // namespace bsm
