@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_shadow(DevScene sc, Wavefro
 // Two-level scenes: persistent warps over the queue with trace_queue2 (TLAS
 // leaves enter instances).  The hit record carries the instance in place of u.
 template <bool kOpacity>
-__global__ void __launch_bounds__(256, 2) k_extend2(DevScene sc, const float4* __restrict__ ray_o,
+__global__ void __launch_bounds__(256, 4) k_extend2(DevScene sc, const float4* __restrict__ ray_o,
                                                     const float4* __restrict__ ray_d, const uint4* __restrict__ path,
                                                     float4* __restrict__ hit, uint32_t* counters,
                                                     unsigned long long* stats, uint32_t seg, int postpone_sp,
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256, 2) k_extend2(DevScene sc, const float4* _
 }
 
 template <bool kOpacity>
-__global__ void __launch_bounds__(256, 2) k_shadow2(DevScene sc, Wavefront wf, uint32_t seg, float4* accum,
+__global__ void __launch_bounds__(256, 4) k_shadow2(DevScene sc, Wavefront wf, uint32_t seg, float4* accum,
                                                     int postpone_sp, int refill_min) {
     const uint32_t n_sun = wf.counters[kCntShadow + seg], n_sky = wf.counters[kCntSky + seg];
     const uint32_t sh_cap = wf.capacity * (sc.num_lights + 1u);
