@@ -77,6 +77,7 @@ def parse():
     p.add_argument("--train-frames", type=int, default=120, help="cache: online training frames before timing")
     p.add_argument("--ema", type=float, default=-1.0, help="cache: weight moving-average decay (-1: library default)")
     p.add_argument("--cache-lr", type=float, default=-1.0, help="cache: Adam learning rate (-1: library default)")
+    p.add_argument("--train-paths", type=int, default=0, help="cache: training paths per frame (0: library default)")
     p.add_argument("--tune-cache", default=None, help="autotuner cache file (batch workload)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -620,7 +621,7 @@ def run_instanced(a, dist):
 def run_cache(a, dist):
     """Radiance cache on the terrain scene: relMSE against a high-spp plain render and device time per frame,
     for the plain pass (8 segments) and the cached pass (paths end in the cache at their third vertex; the cache
-    keeps training online, 65,536 training paths and 4 Adam steps of 16,384 vertices per frame, counted in its
+    keeps training online, 32,768 training paths and 4 Adam steps of 16,384 vertices per frame, counted in its
     frame time), then frames/s of each at equal relMSE."""
     bsm = importlib.import_module("bisemutum-engine_gb300")
     scene = bsm.generate_scene(bsm.BSM_SCENE_TERRAIN, seed=a.seed, grid=a.grid, spheres=a.spheres, width=a.width,
@@ -660,6 +661,8 @@ def run_cache(a, dist):
         cs.ema_decay = a.ema
     if a.cache_lr > 0.0:
         cs.lr = a.cache_lr
+    if a.train_paths > 0:
+        cs.train_paths = a.train_paths
     t0 = time.perf_counter()
     losses = []
     for f in range(a.train_frames):
@@ -725,7 +728,8 @@ def run_cache(a, dist):
             "train": {"frames": a.train_frames, "seconds": round(train_s, 2),
                       "loss_first10": round(float(np.mean(losses[:10])), 4),
                       "loss_last10": round(float(np.mean(losses[-10:])), 4),
-                      "per_frame": f"65536 training paths, 4 Adam steps of 16384 vertices, lr {cs.lr:g}",
+                      "per_frame": f"{cs.train_paths} training paths, {cs.train_steps} Adam steps of {cs.train_batch} "
+                                   f"vertices, lr {cs.lr:g}",
                       "ema_decay": round(float(cs.ema_decay), 4)},
             "config": workload_config(a, scene.num_triangles)}
     line["config"]["workload"] = f"radiance cache on the terrain scene, {a.width}x{a.height}, cache after 2 bounces"

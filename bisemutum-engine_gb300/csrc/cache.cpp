@@ -46,7 +46,7 @@ void upload_weights(bsm_cache* c, const float* w) {
 extern "C" void bsm_cache_settings_default(bsm_cache_settings* cs) {
     if (!cs) return;
     cs->cache_segment = 2;
-    cs->train_paths = 65536;
+    cs->train_paths = 32768;
     cs->train_segments = 8;
     cs->train_batch = 16384;
     cs->train_steps = 4;
@@ -70,7 +70,7 @@ extern "C" bsm_status bsm_cache_create(bsm_context* ctx, uint64_t seed, bsm_cach
               cudaMalloc((void**)&c->adam_m, kMlpParams * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->adam_v, kMlpParams * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->dW, kMlpParams * 4) == cudaSuccess &&
-              cudaMalloc((void**)&c->loss, 4) == cudaSuccess &&
+              cudaMalloc((void**)&c->loss, kLossSlots * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->sample_count, 4) == cudaSuccess &&
               cudaMalloc((void**)&c->view_dev, sizeof(DevView)) == cudaSuccess;
     if (!ok) {
@@ -160,25 +160,38 @@ bsm_status train_device(bsm_cache* c, const float4* samples, uint32_t n, uint32_
         c->ema_decay = ema_decay;
     }
     if (batch == 0) batch = 16384;
+    // each step's loss goes to its own device slot; the host reads them once per kLossSlots steps, so
+    // the steps are queued back to back without a host round trip
     double loss_sum = 0.0;
     uint32_t steps = 0;
+    float host_loss[kLossSlots];
+    auto drain = [&](uint32_t k) -> bool {
+        if (k == 0) return true;
+        if (cudaMemcpyAsync(host_loss, c->loss, k * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return false;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return false;
+        for (uint32_t j = 0; j < k; ++j) loss_sum += host_loss[j];
+        return true;
+    };
+    uint32_t slot = 0;
     for (uint32_t off = 0; off < n; off += batch) {
         uint32_t nb = std::min(batch, n - off);
+        if (slot == 0) cudaMemsetAsync(c->loss, 0, kLossSlots * 4, st);
         cudaMemsetAsync(c->dW, 0, kMlpParams * 4, st);
-        cudaMemsetAsync(c->loss, 0, 4, st);
-        if (launch_mlp_train(c->device, st, c->w_bf16, samples + 4 * (size_t)off, nb, c->dW, c->loss) != cudaSuccess)
+        if (launch_mlp_train(c->device, st, c->w_bf16, samples + 4 * (size_t)off, nb, c->dW, c->loss + slot) !=
+            cudaSuccess)
             return BSM_ERR_CUDA;
         c->step++;
         if (ema_decay > 0.0f) c->ema_steps++;
         if (launch_mlp_adam(st, c->w_master, c->w_bf16, c->dW, c->adam_m, c->adam_v, lr, c->step, c->w_ema,
                             c->w_ema_bf16, ema_decay, c->ema_steps) != cudaSuccess)
             return BSM_ERR_CUDA;
-        float l = 0.0f;
-        cudaMemcpyAsync(&l, c->loss, 4, cudaMemcpyDeviceToHost, st);
-        cudaStreamSynchronize(st);
-        loss_sum += l;
         ++steps;
+        if (++slot == kLossSlots) {
+            if (!drain(slot)) return BSM_ERR_CUDA;
+            slot = 0;
+        }
     }
+    if (!drain(slot)) return BSM_ERR_CUDA;
     if (mean_loss) *mean_loss = steps ? (float)(loss_sum / steps) : 0.0f;
     return BSM_OK;
 }

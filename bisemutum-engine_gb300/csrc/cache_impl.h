@@ -7,6 +7,8 @@
 #include "bsm_pt.h"
 #include "pt_device.h"
 
+constexpr uint32_t kLossSlots = 64;  // per-step loss slots on the device (read back together)
+
 struct bsm_cache {
     bsm_context* ctx = nullptr;
     int device = 0;
@@ -19,7 +21,7 @@ struct bsm_cache {
     float* adam_m = nullptr;
     float* adam_v = nullptr;
     float* dW = nullptr;
-    float* loss = nullptr;       // device scalar
+    float* loss = nullptr;       // device: one loss per Adam step of a training call (kLossSlots)
     float4* samples = nullptr;   // training samples (4 float4 each)
     uint32_t* sample_count = nullptr;
     uint32_t sample_cap = 0;

@@ -23,7 +23,7 @@ namespace bsm {
 
 constexpr int kTrainMaxVerts = 16;
 
-__global__ void __launch_bounds__(128) k_train_paths(DevScene sc, const DevView* __restrict__ view, uint32_t n_paths,
+__global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevView* __restrict__ view, uint32_t n_paths,
                                                      uint32_t frame, uint32_t max_seg, float4* samples,
                                                      uint32_t* count, uint32_t max_samples) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;

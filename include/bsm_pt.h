@@ -469,7 +469,7 @@ typedef struct bsm_cache bsm_cache;
 
 typedef struct bsm_cache_settings {
     uint32_t cache_segment;   /* hits of this segment query the cache (2 = after two bounces) */
-    uint32_t train_paths;     /* full-length training paths per frame (65536) */
+    uint32_t train_paths;     /* full-length training paths per frame (32768) */
     uint32_t train_segments;  /* their maximum segments (8) */
     uint32_t train_batch;     /* samples per Adam step (16384) */
     uint32_t train_steps;     /* Adam steps per frame (4); 0 = render only */
