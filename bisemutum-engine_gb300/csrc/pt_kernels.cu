@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(256, 4) k_shadow2(DevScene sc, Wavefront wf, u
 }
 
 // ----------------------------------------------------------------- shade ----
-__global__ void __launch_bounds__(256, 3) k_shade(DevScene sc, const DevView* __restrict__ views, Wavefront wf,
+__global__ void __launch_bounds__(256, 4) k_shade(DevScene sc, const DevView* __restrict__ views, Wavefront wf,
                                                int q, uint32_t seg, float4* accum) {
     const uint32_t n = wf.counters[kCntQueue + seg];
     const uint32_t cap = wf.capacity;
