@@ -193,8 +193,6 @@ const char* camera_problem(const bsm_camera& c) {
 
 bool same_camera(const bsm_camera& a, const bsm_camera& b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
 
-// Sky sampling tables: weights (r + g + b) * sin(theta at the row centre),
-// prefix sums in double, stored as float.
 // Sky sampling tables: texel weights (r + g + b) * sin(theta at the row centre),
 // the pdf of each texel in (u, v) space, and an alias table over the texels
 // (Walker's method with Vose's construction): entry k keeps texel k with
