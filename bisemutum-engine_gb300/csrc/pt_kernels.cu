@@ -39,6 +39,27 @@ __device__ __forceinline__ uint32_t warp_alloc(bool pred, uint32_t* counter) {
     return base + (uint32_t)__popc(b & lanemask_lt());
 }
 
+// Queue slots for the threads of a block with `pred`, grouped by the octant of
+// `dir` (one atomic on `counter` per block).  Consecutive slots then hold rays
+// heading the same way from neighbouring paths, which keeps the warps of the
+// next traversal and shading launches coherent.  Every thread of the block
+// must call it (it synchronises the block); returns 0 for threads without pred.
+__device__ __forceinline__ uint32_t block_alloc_by_octant(bool pred, V3 dir, uint32_t* counter) {
+    __shared__ uint32_t s_cnt[9], s_off[8], s_base;
+    if (threadIdx.x < 9) s_cnt[threadIdx.x] = 0u;
+    __syncthreads();
+    uint32_t key = pred ? ((dir.x < 0.0f ? 1u : 0u) | (dir.y < 0.0f ? 2u : 0u) | (dir.z < 0.0f ? 4u : 0u)) : 8u;
+    uint32_t rank = atomicAdd(&s_cnt[key], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int k = 0; k < 8; ++k) { s_off[k] = acc; acc += s_cnt[k]; }
+        s_base = acc ? atomicAdd(counter, acc) : 0u;
+    }
+    __syncthreads();
+    return pred ? s_base + s_off[key] + rank : 0u;
+}
+
 __device__ __forceinline__ void accum_add(float4* accum, uint32_t idx, V3 c) {
     atomicAdd(accum + idx, make_float4(c.x, c.y, c.z, 0.0f));
 }
@@ -386,7 +407,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(DevScene sc, const DevView* __
                 cont = max_comp(nthr) > 0.0f;
             }
         }
-        uint32_t slot = warp_alloc(cont, wf.counters + kCntQueue + seg + 1);
+        // the next rays, grouped by octant per block (sorting the sky shadow rays the same way measured no gain)
+        uint32_t slot = block_alloc_by_octant(cont, L, wf.counters + kCntQueue + seg + 1);
         if (cont) {
             if (slot < cap) {
                 out_o[slot] = make_float4(org.x, org.y, org.z, tmin);
