@@ -597,6 +597,9 @@ bsm_status setup_shading(bsm_context* ctx, Scene* sc, const bsm_material* materi
         d.d = make_float4(ev.x, ev.y, ev.z, 0.0f);
     }
     ds.num_lights = nl;
+    ds.dir_lights_only = 1u;
+    for (uint32_t l = 0; l < nl; ++l)
+        if (f2u(ds.lights[l].a.w) != kLightDir) ds.dir_lights_only = 0u;
     ds.sky.kind = sky.kind;
     ds.sky.cr = sky.color[0]; ds.sky.cg = sky.color[1]; ds.sky.cb = sky.color[2];
     if (sky.kind == BSM_SKY_EQUIRECT) {
@@ -1143,7 +1146,7 @@ void record_render(bsm_context* ctx, const Scene* sc, uint32_t n_views, uint64_t
         for (uint32_t seg = 0; seg < max_seg; ++seg) {
             launch_extend(lc, st, sc->dev, ctx->wf, q, seg, count_traversal);
             mark(1);
-            launch_shade(lc, st, sc->dev, views, ctx->wf, q, seg, accum);
+            launch_shade(lc, st, sc->dev, views, ctx->wf, q, seg, accum, cache_wb != nullptr);
             mark(2);
             launch_shadow(lc, st, sc->dev, ctx->wf, seg, accum);
             mark(3);

@@ -57,6 +57,7 @@ struct DevScene {
     DevLight lights[kMaxLights];
     DevSky sky;
     uint32_t has_non_opaque;   // some triangle has a transparency (alpha test / translucent)
+    uint32_t dir_lights_only;  // every light is directional (the shading kernel's slim variant)
     float ray_offset;          // origin offset along the geometric normal
     float box_lo[3];           // scene bounds: radiance-cache inputs are normalised to them
     float box_inv[3];
@@ -128,8 +129,9 @@ void launch_camera(const LaunchCfg& lc, cudaStream_t st, const DevView* views, u
                    uint64_t path_begin, uint32_t path_count, const Wavefront& wf, uint32_t max_segments);
 void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, int q,
                    uint32_t seg, bool count_traversal);
+// `cache`: some view of the launch queries the radiance cache
 void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const DevView* views,
-                  const Wavefront& wf, int q, uint32_t seg, float4* accum);
+                  const Wavefront& wf, int q, uint32_t seg, float4* accum, bool cache = false);
 void launch_shadow(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, uint32_t seg,
                    float4* accum);
 void launch_resolve(cudaStream_t st, const float4* accum, uint32_t width, uint32_t height, float inv_spp,

@@ -214,6 +214,9 @@ __global__ void __launch_bounds__(256, 4) k_shadow2(DevScene sc, Wavefront wf, u
 }
 
 // ----------------------------------------------------------------- shade ----
+// kGeneral: point, spot or rect lights, or radiance-cache queries; the slim
+// variant (directional lights only, no cache) leaves that code out.
+template <bool kGeneral>
 __global__ void __launch_bounds__(256, 4) k_shade(DevScene sc, const DevView* __restrict__ views, Wavefront wf,
                                                int q, uint32_t seg, float4* accum) {
     const uint32_t n = wf.counters[kCntQueue + seg];
@@ -293,7 +296,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(DevScene sc, const DevView* __
         }
         // radiance cache: a hit of the cache segment becomes a query (NRC-style
         // termination) — the cache's prediction includes the direct light there
-        bool cache_q = is_hit && cache_seg != 0u && segi == cache_seg;
+        bool cache_q = kGeneral && is_hit && cache_seg != 0u && segi == cache_seg;
         {
             uint32_t slot = warp_alloc(cache_q, wf.counters + kCntCache);
             if (cache_q) {
@@ -330,11 +333,23 @@ __global__ void __launch_bounds__(256, 4) k_shade(DevScene sc, const DevView* __
             V3 c = v3s(0.0f), L = v3s(0.0f);
             float smax = ray_len;
             float ur0 = 0.0f, ur1 = 0.0f;
-            if (is_hit && __float_as_uint(lt.a.w) == kLightRect) { ur0 = pcg_uniform(g); ur1 = pcg_uniform(g); }
+            if (kGeneral && is_hit && __float_as_uint(lt.a.w) == kLightRect) {
+                ur0 = pcg_uniform(g);
+                ur1 = pcg_uniform(g);
+            }
             bool emit = false;
             if (is_hit && (vflags & BSM_PT_NO_SUN_NEE) == 0u) {
                 V3 e;
-                if (light_sample(lt, P, ur0, ur1, ray_len, L, smax, e)) {
+                bool lit;
+                if (kGeneral) {
+                    lit = light_sample(lt, P, ur0, ur1, ray_len, L, smax, e);
+                } else {  // directional: light_sample's first case
+                    L = v3(lt.a.x, lt.a.y, lt.a.z);
+                    e = v3(lt.b.x, lt.b.y, lt.b.z);
+                    smax = ray_len;
+                    lit = true;
+                }
+                if (lit) {
                     V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
                     c = thr * e * f;
                     emit = max_comp(c) > 0.0f;
@@ -592,8 +607,11 @@ void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, con
 #undef BSM_EXTEND
 }
 void launch_shade(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const DevView* views,
-                  const Wavefront& wf, int q, uint32_t seg, float4* accum) {
-    k_shade<<<lc.grid_shade, lc.block_shade, 0, st>>>(sc, views, wf, q, seg, accum);
+                  const Wavefront& wf, int q, uint32_t seg, float4* accum, bool cache) {
+    if (cache || !sc.dir_lights_only)
+        k_shade<true><<<lc.grid_shade, lc.block_shade, 0, st>>>(sc, views, wf, q, seg, accum);
+    else
+        k_shade<false><<<lc.grid_shade, lc.block_shade, 0, st>>>(sc, views, wf, q, seg, accum);
 }
 void launch_shadow(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, uint32_t seg,
                    float4* accum) {
@@ -649,7 +667,7 @@ void query_launch_cfg(int device, int block_trace, LaunchCfg* lc) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, 1, true>, block_trace, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<1, true>, block_trace, 0);
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_shade, k_shade, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_shade, k_shade<true>, 256, 0);
     int per_sm2_ext = 0, per_sm2_sh = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2_ext, k_extend2<true>, block_trace, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2_sh, k_shadow2<true>, block_trace, 0);
