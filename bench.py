@@ -190,14 +190,15 @@ def peaks():
 
 
 def profile_traffic():
-    """Per-ray DRAM traffic of the extend kernel from the committed ncu summary, if any."""
+    """Per-ray DRAM traffic of the extend kernel from the committed ncu summary, if any, and the summary's
+    issue-slot use (the bound of an issue-limited traversal)."""
     path = os.path.join(ROOT, "profiles", "k_extend_traffic.json")
     try:
         with open(path) as f:
             j = json.load(f)
-        return float(j["dram_bytes_per_ray"]), j.get("source", path)
+        return float(j["dram_bytes_per_ray"]), j.get("source", path), j.get("issue")
     except (OSError, KeyError, ValueError):
-        return None, None
+        return None, None, None
 
 
 # -------------------------------------------------------------- CPU legs ----
@@ -353,7 +354,7 @@ def run_ours(a, dist: Dist):
         per_launch_rays = rays / max(1, a.steps * ext_launches)
         per_launch_ms = ms_ext / max(1, a.steps * ext_launches)
         achieved = EXTEND_BYTES_PER_RAY * rays / (ms_ext / 1e3) / 1e9 if ms_ext > 0 else None
-        traffic_per_ray, traffic_src = profile_traffic()
+        traffic_per_ray, traffic_src, issue = profile_traffic()
         roofline = {"bound": "hbm", "kernel": "k_extend", "achieved": round(achieved, 2) if achieved else None,
                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
                     "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
@@ -364,7 +365,8 @@ def run_ours(a, dist: Dist):
                     "l2_traversal_gbs": round((NODE_BYTES * nodes_per_ray + TRI_BYTES * tris_per_ray) * rays /
                                               (ms_ext / 1e3) / 1e9, 1) if ms_ext > 0 else None,
                     "nodes_per_ray": round(nodes_per_ray, 2), "tris_per_ray": round(tris_per_ray, 2),
-                    "extend_mrays_per_s_kernel_only": round(rays / (ms_ext / 1e3) / 1e6, 1) if ms_ext > 0 else None}
+                    "extend_mrays_per_s_kernel_only": round(rays / (ms_ext / 1e3) / 1e6, 1) if ms_ext > 0 else None,
+                    "issue": issue}
         cpu = None
         if not a.no_cpu_baseline:
             r = cpu_sample(scene, cam.as_array(), a, a.cpu_seconds)
