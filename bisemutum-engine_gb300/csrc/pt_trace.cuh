@@ -541,8 +541,10 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
 
 namespace bsm {
 
-constexpr int kStackSize2 = 64;   // two-level: TLAS groups (<= 12 + 1) + exit marker + BLAS groups + postponed
-static_assert(kMaxTlasDepth + 3 + kMaxTraversalDepth + kPostponeMaxSp <= kStackSize2, "two-level stack budget");
+// two-level: TLAS node groups (<= 12) + postponed TLAS groups (< 16) + 2 groups and an exit marker at an
+// instance entry + BLAS node groups (<= 24) + postponed BLAS groups (<= 16)
+constexpr int kStackSize2 = 80;
+static_assert(kMaxTlasDepth + 3 + kMaxTraversalDepth + 2 * kPostponeMaxSp <= kStackSize2, "two-level stack budget");
 
 // Persistent, warp-synchronous traversal of a queue of rays through a two-level
 // scene (TLAS over per-geometry BLASes), with trace_queue's refill and
@@ -550,8 +552,9 @@ static_assert(kMaxTlasDepth + 3 + kMaxTraversalDepth + kPostponeMaxSp <= kStackS
 // reaches one pushes the rest of its TLAS work and an exit marker, moves its
 // ray into the instance's space and continues in the BLAS on the same stack;
 // popping the marker reloads the world ray (`load`) and returns to the TLAS.
-// Triangle groups are postponed only inside a BLAS, at most `postpone_sp`
-// entries above the BLAS's exit marker, so the stack stays within
+// Leaf groups (instances in the TLAS, triangles in a BLAS) are postponed while
+// the stack holds fewer than `postpone_sp` entries above the current BVH's
+// base (0 in the TLAS, the exit marker in a BLAS), so the stack stays within
 // kStackSize2 (TLAS depth <= kMaxTlasDepth, BLAS depth <= kMaxTraversalDepth).
 // Results and the opacity rule are those of trace_ray2: object-space
 // triangle tests with t unchanged, ties to the lower global primitive id,
@@ -622,7 +625,7 @@ __device__ __forceinline__ void trace_queue2(const CwNode* __restrict__ tlas, co
             uint32_t m = __ballot_sync(0xffffffffu, want);
             if (m == 0u) break;
             if (__popc(m) * 4 < __popc(act)) {
-                if (want && tris != nullptr && sp < sp_blas + postpone_sp) {
+                if (want && sp < sp_blas + postpone_sp) {
                     stack[sp++] = make_uint2(T.x | kTriGroupFlag, T.y);
                     T.y = 0u;
                 }
