@@ -551,7 +551,8 @@ static_assert(kMaxTlasDepth + 3 + kMaxTraversalDepth + 2 * kPostponeMaxSp <= kSt
 // triangle postponing.  A TLAS leaf "triangle" is an instance: a lane that
 // reaches one pushes the rest of its TLAS work and an exit marker, moves its
 // ray into the instance's space and continues in the BLAS on the same stack;
-// popping the marker reloads the world ray (`load`) and returns to the TLAS.
+// popping the marker reloads the world ray's origin and direction (`load`),
+// takes its divided constants from shared memory and returns to the TLAS.
 // Leaf groups (instances in the TLAS, triangles in a BLAS) are postponed while
 // the stack holds fewer than `postpone_sp` entries above the current BVH's
 // base (0 in the TLAS, the exit marker in a BLAS), so the stack stays within
@@ -577,6 +578,9 @@ __device__ __forceinline__ void trace_queue2(const CwNode* __restrict__ tlas, co
     uint2 G = make_uint2(0, 0), T = make_uint2(0, 0);
     uint2 stack[kStackSize2];
     int sp = 0, sp_blas = 0;       // sp_blas: stack depth just above the current BLAS's exit marker
+    // the world ray's divided constants (reciprocals, shear, axis order), kept per thread so that leaving an
+    // instance reloads only origin and direction (blocks have at most 256 threads: __launch_bounds__)
+    __shared__ float4 s_world[256][2];
     while (true) {
         uint32_t idle = __ballot_sync(0xffffffffu, !has);
         if (!exhausted && (__popc(idle) >= refill_min || idle == 0xffffffffu)) {
@@ -590,6 +594,10 @@ __device__ __forceinline__ void trace_queue2(const CwNode* __restrict__ tlas, co
                     float4 o, d;
                     load(i, o, d);
                     r = make_ray(o, d);
+                    s_world[threadIdx.x][0] = make_float4(
+                        r.idx, r.idy, r.idz,
+                        __uint_as_float(r.oct_key | ((uint32_t)r.kx << 4) | ((uint32_t)r.ky << 8) | ((uint32_t)r.kz << 12)));
+                    s_world[threadIdx.x][1] = make_float4(r.Sx, r.Sy, r.Sz, 0.0f);
                     tbest = d.w;
                     best_leaf = kMissPrim; best_prim = kMissPrim; best_inst = kMissPrim; bu = 0.0f; bv = 0.0f;
                     nodes = tlas; tris = nullptr; inst = kMissPrim; prim_base = 0u; mat_override = kMissPrim;
@@ -680,9 +688,15 @@ __device__ __forceinline__ void trace_queue2(const CwNode* __restrict__ tlas, co
             if (!done && sp > 0) {
                 e = stack[--sp];
                 if (e.y == 0u) {  // exit marker: back to the world ray and the TLAS
-                    float4 o4, d4;
+                    float4 o4, d4, c0 = s_world[threadIdx.x][0], c1 = s_world[threadIdx.x][1];
                     load(idx, o4, d4);
-                    r = make_ray(o4, d4);
+                    const uint32_t pk = __float_as_uint(c0.w);
+                    r.ox = o4.x; r.oy = o4.y; r.oz = o4.z; r.tmin = o4.w;
+                    r.dx = d4.x; r.dy = d4.y; r.dz = d4.z;
+                    r.idx = c0.x; r.idy = c0.y; r.idz = c0.z;
+                    r.oct_key = pk & 15u;
+                    r.kx = (int)((pk >> 4) & 15u); r.ky = (int)((pk >> 8) & 15u); r.kz = (int)((pk >> 12) & 15u);
+                    r.Sx = c1.x; r.Sy = c1.y; r.Sz = c1.z;
                     nodes = tlas; tris = nullptr; inst = kMissPrim; prim_base = 0u; mat_override = kMissPrim;
                     sp_blas = 0;
                     e = sp > 0 ? stack[--sp] : make_uint2(0u, 0u);
