@@ -627,7 +627,7 @@ __device__ __forceinline__ void trace_queue2(const CwNode* __restrict__ tlas, co
                 node_test(r, nodes, ni, tbest, G, T);
             }
         }
-        // leaf steps: instances in the TLAS, triangles (postponed while few lanes have them) in a BLAS
+        // leaf steps: instances in the TLAS, triangles in a BLAS (both postponed while few lanes have them)
         while (true) {
             bool want = has && has_tris(T);
             uint32_t m = __ballot_sync(0xffffffffu, want);
