@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(256, 4) k_shadow2(DevScene sc, Wavefront wf, u
 // kGeneral: point, spot or rect lights, or radiance-cache queries; the slim
 // variant (directional lights only, no cache) leaves that code out.
 template <bool kGeneral>
-__global__ void __launch_bounds__(256, 4) k_shade(DevScene sc, const DevView* __restrict__ views, Wavefront wf,
+__global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __restrict__ views, Wavefront wf,
                                                int q, uint32_t seg, float4* accum) {
     const uint32_t n = wf.counters[kCntQueue + seg];
     const uint32_t cap = wf.capacity;
@@ -667,7 +667,7 @@ void query_launch_cfg(int device, int block_trace, LaunchCfg* lc) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ext, k_extend<false, 1, true>, block_trace, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_sh, k_shadow<1, true>, block_trace, 0);
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_shade, k_shade<true>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_shade, k_shade<true>, 512, 0);
     int per_sm2_ext = 0, per_sm2_sh = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2_ext, k_extend2<true>, block_trace, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2_sh, k_shadow2<true>, block_trace, 0);
@@ -679,7 +679,7 @@ void query_launch_cfg(int device, int block_trace, LaunchCfg* lc) {
     if (per_sm_shade < 1) per_sm_shade = 1;
     lc->block_trace = block_trace;
     lc->grid_persistent = sms * per_sm;
-    lc->block_shade = 256;
+    lc->block_shade = 512;   // the octant grouping of the next rays spans a block
     lc->grid_shade = sms * per_sm_shade * 4;
 }
 
