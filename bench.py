@@ -78,6 +78,7 @@ def parse():
     p.add_argument("--ema", type=float, default=-1.0, help="cache: weight moving-average decay (-1: library default)")
     p.add_argument("--cache-lr", type=float, default=-1.0, help="cache: Adam learning rate (-1: library default)")
     p.add_argument("--train-paths", type=int, default=0, help="cache: training paths per frame (0: library default)")
+    p.add_argument("--train-segments", type=int, default=0, help="cache: segments of a training path (0: default)")
     p.add_argument("--tune-cache", default=None, help="autotuner cache file (batch workload)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -668,6 +669,8 @@ def run_cache(a, dist):
         cs.lr = a.cache_lr
     if a.train_paths > 0:
         cs.train_paths = a.train_paths
+    if a.train_segments > 0:
+        cs.train_segments = a.train_segments
     t0 = time.perf_counter()
     losses = []
     for f in range(a.train_frames):
