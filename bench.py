@@ -75,6 +75,7 @@ def parse():
     p.add_argument("--serve-lanes", type=int, default=4, help="serve: lanes (streams)")
     p.add_argument("--ref-spp", type=int, default=4096, help="cache: spp of the plain reference render")
     p.add_argument("--train-frames", type=int, default=120, help="cache: online training frames before timing")
+    p.add_argument("--cache-spps", default="1,2,4,8,16,32,64", help="cache: samples per pixel of the compared frames")
     p.add_argument("--ema", type=float, default=-1.0, help="cache: weight moving-average decay (-1: library default)")
     p.add_argument("--cache-lr", type=float, default=-1.0, help="cache: Adam learning rate (-1: library default)")
     p.add_argument("--train-paths", type=int, default=0, help="cache: training paths per frame (0: library default)")
@@ -192,14 +193,14 @@ def peaks():
 
 def profile_traffic():
     """Per-ray DRAM traffic of the extend kernel from the committed ncu summary, if any, and the summary's
-    issue-slot use (the bound of an issue-limited traversal)."""
+    issue-slot use (the bound of an issue-limited traversal) and its measured L2 traffic."""
     path = os.path.join(ROOT, "profiles", "k_extend_traffic.json")
     try:
         with open(path) as f:
             j = json.load(f)
-        return float(j["dram_bytes_per_ray"]), j.get("source", path), j.get("issue")
+        return float(j["dram_bytes_per_ray"]), j.get("source", path), j.get("issue"), j.get("l2")
     except (OSError, KeyError, ValueError):
-        return None, None, None
+        return None, None, None, None
 
 
 # -------------------------------------------------------------- CPU legs ----
@@ -355,7 +356,7 @@ def run_ours(a, dist: Dist):
         per_launch_rays = rays / max(1, a.steps * ext_launches)
         per_launch_ms = ms_ext / max(1, a.steps * ext_launches)
         achieved = EXTEND_BYTES_PER_RAY * rays / (ms_ext / 1e3) / 1e9 if ms_ext > 0 else None
-        traffic_per_ray, traffic_src, issue = profile_traffic()
+        traffic_per_ray, traffic_src, issue, l2_ncu = profile_traffic()
         roofline = {"bound": "hbm", "kernel": "k_extend", "achieved": round(achieved, 2) if achieved else None,
                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
                     "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
@@ -367,6 +368,7 @@ def run_ours(a, dist: Dist):
                                               (ms_ext / 1e3) / 1e9, 1) if ms_ext > 0 else None,
                     "nodes_per_ray": round(nodes_per_ray, 2), "tris_per_ray": round(tris_per_ray, 2),
                     "extend_mrays_per_s_kernel_only": round(rays / (ms_ext / 1e3) / 1e6, 1) if ms_ext > 0 else None,
+                    "l2_ncu": l2_ncu,
                     "issue": issue}
         cpu = None
         if not a.no_cpu_baseline:
@@ -644,7 +646,7 @@ def run_cache(a, dist):
                              outputs=last)
     ref = imgs[0] if a.ref_spp > per else ctx.render(sid, [cam], bsm.settings(spp=per, max_segments=a.segments,
                                                                               seed=90000))[0][0]
-    spps = [1, 2, 4, 8, 16, 32, 64]
+    spps = [int(x) for x in a.cache_spps.split(",")]
     seeds = 3
 
     def trimmed(img, r):
