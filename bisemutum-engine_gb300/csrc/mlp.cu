@@ -47,13 +47,39 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// Loads the BF16 weights (global, row-major [out][64]) into padded shared rows.
+// Loads the BF16 weights (global, row-major [out][64], 16-byte aligned) into
+// padded shared rows, 16 bytes per load.
 __device__ __forceinline__ void load_weights(const __nv_bfloat16* __restrict__ w, __nv_bfloat16* sw) {
     const int rows = kMlpHidden * 64 + kMlpOutPad;
-    for (int i = threadIdx.x; i < rows * 32; i += blockDim.x) {
-        int r = i >> 5, c = (i & 31) * 2;
-        *reinterpret_cast<uint32_t*>(sw + r * kLd + c) = *reinterpret_cast<const uint32_t*>(w + r * 64 + c);
+    const uint4* src = reinterpret_cast<const uint4*>(w);
+#pragma unroll 4
+    for (int i = threadIdx.x; i < rows * 8; i += blockDim.x) {
+        int r = i >> 3, c = (i & 7) * 8;
+        *reinterpret_cast<uint4*>(sw + r * kLd + c) = __ldg(src + i);
     }
+}
+
+// Four 8x8 BF16 matrices from shared memory (ldmatrix): lane L gives the
+// address of row L & 7 of matrix L >> 3; register i of lane (g, t) receives
+// elements (g, 2t) and (g, 2t + 1) of matrix i.
+__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
+    uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a)
+                 : "memory");
+}
+
+// Four transposed 8x8 BF16 matrices from shared memory (ldmatrix .trans):
+// lane L gives the address of row L & 7 of matrix L >> 3; register i of lane
+// (g, t) receives elements (2t, g) and (2t + 1, g) of matrix i, which is the
+// mma fragment layout of a matrix stored with its K dimension along the rows.
+__device__ __forceinline__ void ldsm_x4_t(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
+    uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a)
+                 : "memory");
 }
 
 // Encoded input tile as A fragments: act[kk] covers features 16kk..16kk+15.
@@ -69,17 +95,23 @@ __device__ __forceinline__ void encode_tile(const float* raw_g, const float* raw
 }
 
 // One hidden layer: out = relu(W act) as A fragments of the next layer.
+// B[k=in][n=out] = W[out][in] lies in shared memory with K along the rows'
+// length, so plain 8x8 matrix loads give the B fragments (matrices: k half
+// (lane >> 3) & 1, n block of the pair (lane >> 4)).
 __device__ __forceinline__ void hidden_layer(const __nv_bfloat16* sw, const uint32_t (&in)[4][4], uint32_t (&out)[4][4],
                                              int g, int t) {
+    const int lane = threadIdx.x & 31, mi = lane >> 3, r = lane & 7;
     float acc[8][4];
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const __nv_bfloat16* wr = sw + (8 * j + g) * kLd + 16 * kk + 2 * t;
-            mma16816(acc[j], in[kk], *reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8));
+        for (int jp = 0; jp < 4; ++jp) {
+            uint32_t b0, b1, b2, b3;
+            ldsm_x4(b0, b1, b2, b3, sw + (8 * (2 * jp + (mi >> 1)) + r) * kLd + 16 * kk + (mi & 1) * 8);
+            mma16816(acc[2 * jp], in[kk], b0, b1);
+            mma16816(acc[2 * jp + 1], in[kk], b2, b3);
         }
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
@@ -91,13 +123,17 @@ __device__ __forceinline__ void hidden_layer(const __nv_bfloat16* sw, const uint
 }
 
 // Output layer (8 rows, 3 used): y fragment (row g: y[0], y[1] = channels 2t, 2t+1; row g+8: y[2], y[3]).
+// One matrix load covers two k steps (matrices: k half (lane >> 3) & 1, k step of the pair (lane >> 4)).
 __device__ __forceinline__ void output_layer(const __nv_bfloat16* sw4, const uint32_t (&in)[4][4], float (&y)[4],
                                              int g, int t) {
+    const int lane = threadIdx.x & 31, mi = lane >> 3, r = lane & 7;
     y[0] = y[1] = y[2] = y[3] = 0.0f;
 #pragma unroll
-    for (int kk = 0; kk < 4; ++kk) {
-        const __nv_bfloat16* wr = sw4 + g * kLd + 16 * kk + 2 * t;
-        mma16816(y, in[kk], *reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8));
+    for (int kp = 0; kp < 2; ++kp) {
+        uint32_t b0, b1, b2, b3;
+        ldsm_x4(b0, b1, b2, b3, sw4 + r * kLd + 16 * (2 * kp + (mi >> 1)) + (mi & 1) * 8);
+        mma16816(y, in[2 * kp], b0, b1);
+        mma16816(y, in[2 * kp + 1], b2, b3);
     }
 }
 
@@ -225,75 +261,111 @@ __device__ __forceinline__ void relu_grad(const float (&ga)[8][4], const __nv_bf
     }
 }
 
-// g_a = g_z W for a [64 out][64 in] weight block (B[k=out][n=in] = W[out][in]).
+// g_a = g_z W for a [64 out][64 in] weight block: B[k=out][n=in] = W[out][in]
+// lies in shared memory with K along the rows, so transposed loads give the
+// B fragments (matrices: k half (lane >> 3) & 1, n block of the pair (lane >> 4)).
 __device__ __forceinline__ void backward_data(const __nv_bfloat16* sw, const uint32_t (&gz)[4][4], float (&ga)[8][4],
-                                              int g, int t) {
-    const uint16_t* w16 = reinterpret_cast<const uint16_t*>(sw);
+                                              int lane) {
+    const int mi = lane >> 3, r = lane & 7;
 #pragma unroll
     for (int j = 0; j < 8; ++j) ga[j][0] = ga[j][1] = ga[j][2] = ga[j][3] = 0.0f;
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            int k0 = 16 * kk + 2 * t, n = 8 * j + g;
-            uint32_t b0 = pack_u16(w16[k0 * kLd + n], w16[(k0 + 1) * kLd + n]);
-            uint32_t b1 = pack_u16(w16[(k0 + 8) * kLd + n], w16[(k0 + 9) * kLd + n]);
-            mma16816(ga[j], gz[kk], b0, b1);
+        for (int jp = 0; jp < 4; ++jp) {
+            uint32_t b0, b1, b2, b3;
+            ldsm_x4_t(b0, b1, b2, b3, sw + (16 * kk + (mi & 1) * 8 + r) * kLd + 8 * (2 * jp + (mi >> 1)));
+            mma16816(ga[2 * jp], gz[kk], b0, b1);
+            mma16816(ga[2 * jp + 1], gz[kk], b2, b3);
         }
 }
 
-// dW[out][in] += sum over the 16 samples of gz[s][out] * a[s][in]  (rows_out = 64 or 8)
-__device__ __forceinline__ void weight_grad(const __nv_bfloat16* gz_tile, const __nv_bfloat16* a_tile, float* dW,
-                                            int rows_out, int g, int t) {
-    const uint16_t* gz16 = reinterpret_cast<const uint16_t*>(gz_tile);
-    const uint16_t* a16 = reinterpret_cast<const uint16_t*>(a_tile);
-    for (int m = 0; m < rows_out; m += 16) {
-        uint32_t A[4];
-        int o0 = m + g, o1 = m + g + 8, s0 = 2 * t;
-        bool v1 = o1 < rows_out;
-        A[0] = pack_u16(gz16[s0 * kLd + o0], gz16[(s0 + 1) * kLd + o0]);
-        A[1] = v1 ? pack_u16(gz16[s0 * kLd + o1], gz16[(s0 + 1) * kLd + o1]) : 0u;
-        A[2] = pack_u16(gz16[(s0 + 8) * kLd + o0], gz16[(s0 + 9) * kLd + o0]);
-        A[3] = v1 ? pack_u16(gz16[(s0 + 8) * kLd + o1], gz16[(s0 + 9) * kLd + o1]) : 0u;
+// Rows [m0, m0 + 16) of dW[out][in] += sum over the block's 64 samples (the
+// four warps' 16-sample tiles) of gz[s][out] * a[s][in], for one 64x64 layer.
+// A[m=out][k=s] and B[k=s][n=in] are both stored [s][.]: transposed loads.
+// The calling warp owns these rows, so the update is a plain read-add-write.
+__device__ __forceinline__ void weight_grad_rows(const __nv_bfloat16* const (&gz_q)[4],
+                                                 const __nv_bfloat16* const (&a_q)[4], float* dW, int m0, int lane) {
+    const int mi = lane >> 3, r = lane & 7, g = lane >> 2, t = lane & 3;
+    float acc[8][4];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            int n = 8 * j + g;
-            uint32_t b0 = pack_u16(a16[s0 * kLd + n], a16[(s0 + 1) * kLd + n]);
-            uint32_t b1 = pack_u16(a16[(s0 + 8) * kLd + n], a16[(s0 + 9) * kLd + n]);
-            float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            mma16816(c, A, b0, b1);
-            int col = 8 * j + 2 * t;
-            atomicAdd(dW + o0 * 64 + col, c[0]);
-            atomicAdd(dW + o0 * 64 + col + 1, c[1]);
-            if (v1) {
-                atomicAdd(dW + o1 * 64 + col, c[2]);
-                atomicAdd(dW + o1 * 64 + col + 1, c[3]);
-            }
+    for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint32_t A[4];
+        ldsm_x4_t(A[0], A[1], A[2], A[3], gz_q[q] + ((mi >> 1) * 8 + r) * kLd + m0 + (mi & 1) * 8);
+#pragma unroll
+        for (int jp = 0; jp < 4; ++jp) {
+            uint32_t b0, b1, b2, b3;
+            ldsm_x4_t(b0, b1, b2, b3, a_q[q] + ((mi & 1) * 8 + r) * kLd + 8 * (2 * jp + (mi >> 1)));
+            mma16816(acc[2 * jp], A, b0, b1);
+            mma16816(acc[2 * jp + 1], A, b2, b3);
         }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        float2* p0 = reinterpret_cast<float2*>(dW + (m0 + g) * 64 + 8 * j + 2 * t);
+        float2* p1 = reinterpret_cast<float2*>(dW + (m0 + g + 8) * 64 + 8 * j + 2 * t);
+        float2 v0 = *p0, v1 = *p1;
+        *p0 = make_float2(v0.x + acc[j][0], v0.y + acc[j][1]);
+        *p1 = make_float2(v1.x + acc[j][2], v1.y + acc[j][3]);
+    }
+}
+
+// Output layer (8 rows): columns [16 jb, 16 jb + 16) of dW4[out][in] += sum over
+// the block's 64 samples of gy[s][out] * a3[s][in]; rows 8..15 of the A tile are zero.
+__device__ __forceinline__ void weight_grad_out(const __nv_bfloat16* const (&gy_q)[4],
+                                                const __nv_bfloat16* const (&a_q)[4], float* dW4, int jb, int lane) {
+    const int mi = lane >> 3, r = lane & 7, g = lane >> 2, t = lane & 3;
+    float acc[2][4] = {{0.0f, 0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f, 0.0f}};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint32_t A[4];
+        ldsm_x4_t(A[0], A[1], A[2], A[3], gy_q[q] + ((mi >> 1) * 8 + r) * kLd);  // matrices 1, 3 repeat 0, 2
+        A[1] = 0u;
+        A[3] = 0u;
+        uint32_t b0, b1, b2, b3;
+        ldsm_x4_t(b0, b1, b2, b3, a_q[q] + ((mi & 1) * 8 + r) * kLd + 8 * (2 * jb + (mi >> 1)));
+        mma16816(acc[0], A, b0, b1);
+        mma16816(acc[1], A, b2, b3);
+    }
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj) {
+        float2* p = reinterpret_cast<float2*>(dW4 + g * 64 + 8 * (2 * jb + jj) + 2 * t);
+        float2 v = *p;
+        *p = make_float2(v.x + acc[jj][0], v.y + acc[jj][1]);
     }
 }
 
 // samples: as k_mlp_predict (targets in the 4th float4).  Accumulates the
 // gradient of the mean relative L2 loss over `n` samples into dW_global and
-// the loss into loss_out[0].
+// the loss into loss_out[0].  A block takes 64 samples at a time (one 16-row
+// tile per warp); after forward and backward passes each warp reduces its own
+// rows of every layer's weight gradient over all 64 samples on the tensor
+// cores, into the block's FP32 copy, and the block adds that copy to
+// dW_global once at the end.
 __global__ void __launch_bounds__(128) k_mlp_train(const __nv_bfloat16* __restrict__ w, const float4* __restrict__ s,
                                                    uint32_t n, float* dW_global, float* loss_out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem_raw);
     float* sdw = reinterpret_cast<float*>(smem_raw + kWSmem * 2);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    __nv_bfloat16* wt = reinterpret_cast<__nv_bfloat16*>(smem_raw + kWSmem * 2 + kMlpParams * 4 + warp * kTrainWarpBytes);
+    auto tile_of = [&](int wq, int i) {
+        return reinterpret_cast<__nv_bfloat16*>(smem_raw + kWSmem * 2 + kMlpParams * 4 + wq * kTrainWarpBytes) +
+               i * kTileElems;
+    };
     __nv_bfloat16* act_t[5];  // e, a0, a1, a2, a3
     __nv_bfloat16* gz_t[5];   // gz0, gz1, gz2, gz3, gy
-    for (int i = 0; i < 5; ++i) { act_t[i] = wt + i * kTileElems; gz_t[i] = wt + (5 + i) * kTileElems; }
+    for (int i = 0; i < 5; ++i) { act_t[i] = tile_of(warp, i); gz_t[i] = tile_of(warp, 5 + i); }
     load_weights(w, sw);
-    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) sdw[i] = 0.0f;
+    for (int i = threadIdx.x; i < kMlpParams / 4; i += blockDim.x)
+        reinterpret_cast<float4*>(sdw)[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     __syncthreads();
     const float inv = 1.0f / (3.0f * (float)n);
     float loss = 0.0f;
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + warp; tile * 16 < n; tile += warps) {
-        uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
+    const uint32_t groups = (n + 63) / 64;
+    for (uint32_t grp = blockIdx.x; grp < groups; grp += gridDim.x) {   // uniform trip count within the block
+        uint32_t r0 = (grp * 4 + warp) * 16 + g, r1 = r0 + 8;          // rows >= n: zero loss gradient
         float raw0[kMlpRaw], raw1[kMlpRaw];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
@@ -339,42 +411,55 @@ __global__ void __launch_bounds__(128) k_mlp_train(const __nv_bfloat16* __restri
             *reinterpret_cast<uint32_t*>(gyt + g * kLd + c) = gyp0;
             *reinterpret_cast<uint32_t*>(gyt + (g + 8) * kLd + c) = gyp1;
         }
-        // g_a3 = gy W4 (K = 8 padded to 16)
+        // g_a3 = gy W4 (K = 8 padded to 16): B[k=out][n=in] rows 0..7 of W4, four n blocks per transposed load
         float ga[8][4];
         uint32_t gz[4][4];
         {
             uint32_t A[4] = {gyp0, gyp1, 0u, 0u};
-            const uint16_t* w16 = reinterpret_cast<const uint16_t*>(sw + 4 * 64 * kLd);
-            for (int j = 0; j < 8; ++j) {
-                ga[j][0] = ga[j][1] = ga[j][2] = ga[j][3] = 0.0f;
-                int k0 = 2 * t, nn = 8 * j + g;
-                uint32_t b0 = pack_u16(w16[k0 * kLd + nn], w16[(k0 + 1) * kLd + nn]);
-                mma16816(ga[j], A, b0, 0u);
+            const __nv_bfloat16* w4 = sw + 4 * 64 * kLd;
+#pragma unroll
+            for (int jq = 0; jq < 2; ++jq) {
+                uint32_t b[4];
+                ldsm_x4_t(b[0], b[1], b[2], b[3], w4 + (lane & 7) * kLd + 8 * (4 * jq + (lane >> 3)));
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    float* c = ga[4 * jq + i];
+                    c[0] = c[1] = c[2] = c[3] = 0.0f;
+                    mma16816(ga[4 * jq + i], A, b[i], 0u);
+                }
             }
         }
         __syncwarp();
         relu_grad(ga, act_t[4], gz_t[3], gz, g, t);   // gz3
-        backward_data(sw + 3 * 64 * kLd, gz, ga, g, t);
+        backward_data(sw + 3 * 64 * kLd, gz, ga, lane);
         relu_grad(ga, act_t[3], gz_t[2], gz, g, t);   // gz2
-        backward_data(sw + 2 * 64 * kLd, gz, ga, g, t);
+        backward_data(sw + 2 * 64 * kLd, gz, ga, lane);
         relu_grad(ga, act_t[2], gz_t[1], gz, g, t);   // gz1
-        backward_data(sw + 1 * 64 * kLd, gz, ga, g, t);
+        backward_data(sw + 1 * 64 * kLd, gz, ga, lane);
         relu_grad(ga, act_t[1], gz_t[0], gz, g, t);   // gz0
-        __syncwarp();
-        // weight gradients: dW_l = gz_l^T a_{l-1}; dW4 = gy^T a3
-        weight_grad(gz_t[0], act_t[0], sdw + 0 * kMlpLayerParams, 64, g, t);
-        weight_grad(gz_t[1], act_t[1], sdw + 1 * kMlpLayerParams, 64, g, t);
-        weight_grad(gz_t[2], act_t[2], sdw + 2 * kMlpLayerParams, 64, g, t);
-        weight_grad(gz_t[3], act_t[3], sdw + 3 * kMlpLayerParams, 64, g, t);
-        weight_grad(gz_t[4], act_t[4], sdw + 4 * kMlpLayerParams, kMlpOutPad, g, t);
-        __syncwarp();
+        __syncthreads();                               // all four tiles of the group are in shared memory
+        // weight gradients: dW_l = gz_l^T a_{l-1}; dW4 = gy^T a3.  Warp w: rows 16w..16w+15 of the
+        // hidden layers, columns 16w..16w+15 of the output layer.
+#pragma unroll 1
+        for (int l = 0; l < 4; ++l) {
+            const __nv_bfloat16* const gq[4] = {tile_of(0, 5 + l), tile_of(1, 5 + l), tile_of(2, 5 + l),
+                                                tile_of(3, 5 + l)};
+            const __nv_bfloat16* const aq[4] = {tile_of(0, l), tile_of(1, l), tile_of(2, l), tile_of(3, l)};
+            weight_grad_rows(gq, aq, sdw + l * kMlpLayerParams, 16 * warp, lane);
+        }
+        {
+            const __nv_bfloat16* const gq[4] = {tile_of(0, 9), tile_of(1, 9), tile_of(2, 9), tile_of(3, 9)};
+            const __nv_bfloat16* const aq[4] = {tile_of(0, 4), tile_of(1, 4), tile_of(2, 4), tile_of(3, 4)};
+            weight_grad_out(gq, aq, sdw + 4 * kMlpLayerParams, warp, lane);
+        }
+        __syncthreads();                               // tiles are rewritten by the next group
     }
     for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
     if (lane == 0) atomicAdd(loss_out, loss);
-    __syncthreads();
-    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) {
-        float v = sdw[i];
-        if (v != 0.0f) atomicAdd(dW_global + i, v);
+    for (int i = threadIdx.x; i < kMlpParams / 4; i += blockDim.x) {
+        float4 v = reinterpret_cast<const float4*>(sdw)[i];
+        if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f)
+            atomicAdd(reinterpret_cast<float4*>(dW_global) + i, v);
     }
 }
 
@@ -446,9 +531,10 @@ cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const 
     cudaError_t e = mlp_setup(device);
     if (e != cudaSuccess) return e;
     if (n == 0) return cudaSuccess;
-    uint32_t tiles = (n + 15) / 16;
-    uint32_t grid = (uint32_t)g_mlp_grid;
-    if (tiles < grid * 4) grid = (tiles + 3) / 4;
+    // 64 samples per block and step; as few blocks as keep the number of steps per block minimal
+    uint32_t groups = (n + 63) / 64;
+    uint32_t per_block = (groups + (uint32_t)g_mlp_grid - 1) / (uint32_t)g_mlp_grid;
+    uint32_t grid = (groups + per_block - 1) / per_block;
     k_mlp_train<<<grid, 128, kTrainSmem, st>>>((const __nv_bfloat16*)wb, samples, n, dW, loss);
     return cudaGetLastError();
 }
