@@ -123,6 +123,13 @@ bsm_status fail(bsm_context* ctx, bsm_status st, const std::string& msg) {
     if (ctx) ctx->err = msg;
     return st;
 }
+// Message for the device error word (counters[kCntError]).
+std::string device_flag_text(uint32_t flag) {
+    std::string m = "device error flag set:";
+    if (flag & 1u) m += " a kernel queue overflowed;";
+    if (flag & 2u) m += " a tensor-core wait of the radiance cache timed out;";
+    return m;
+}
 bsm_status cuda_fail(bsm_context* ctx, cudaError_t e, const char* what) {
     return fail(ctx, BSM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -386,7 +393,7 @@ extern "C" bsm_status bsm_sync(bsm_context* ctx, uint32_t timeout_ms) {
     if (ctx->wf.counters) {
         uint32_t flag = 0;
         CK(cudaMemcpy(&flag, ctx->wf.counters + kCntError, 4, cudaMemcpyDeviceToHost));
-        if (flag) return fail(ctx, BSM_ERR_DEVICE_CHECK, "a kernel queue overflowed (error flag set)");
+        if (flag) return fail(ctx, BSM_ERR_DEVICE_CHECK, device_flag_text(flag));
     }
     return BSM_OK;
 }
@@ -1153,7 +1160,8 @@ void record_render(bsm_context* ctx, const Scene* sc, uint32_t n_views, uint64_t
             q ^= 1;
         }
         if (cache_wb)
-            launch_mlp_infer(ctx->device, st, cache_wb, ctx->wf.cache_q, ctx->wf.counters + kCntCache, capacity, accum);
+            launch_mlp_infer(ctx->device, st, cache_wb, ctx->wf.cache_q, ctx->wf.counters + kCntCache, capacity, accum,
+                             ctx->wf.counters + kCntError);
     }
 }
 
@@ -1336,7 +1344,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         CK(cudaStreamSynchronize(ctx->stream));
         uint32_t flag = 0;
         CK(cudaMemcpy(&flag, ctx->wf.counters + kCntError, 4, cudaMemcpyDeviceToHost));
-        if (flag) return fail(ctx, BSM_ERR_DEVICE_CHECK, "a kernel queue overflowed (error flag set)");
+        if (flag) return fail(ctx, BSM_ERR_DEVICE_CHECK, device_flag_text(flag));
     }
     if (stats) {
         unsigned long long h[kStatWords];

@@ -126,14 +126,18 @@ extern "C" bsm_status bsm_cache_predict(bsm_cache* c, const float* samples, uint
     if (!c || (!samples && n) || (!out && n)) return BSM_ERR_INVALID_ARG;
     if (n == 0) return BSM_OK;
     cudaSetDevice(c->device);
-    size_t in_b = (size_t)n * 64, out_b = (size_t)n * 12;
-    if (cache_io(c, in_b + out_b)) return BSM_ERR_OUT_OF_MEMORY;
+    size_t in_b = (size_t)n * 64, out_b = (size_t)n * 12, err_off = in_b + ((out_b + 15) & ~(size_t)15);
+    if (cache_io(c, err_off + 16)) return BSM_ERR_OUT_OF_MEMORY;
     char* b = (char*)c->io;
+    uint32_t* err = (uint32_t*)(b + err_off);
     cudaMemcpy(b, samples, in_b, cudaMemcpyHostToDevice);
-    if (launch_mlp_predict(c->device, 0, c->w_bf16, (const float4*)b, n, (float*)(b + in_b)) != cudaSuccess)
+    cudaMemset(err, 0, 4);
+    if (launch_mlp_predict(c->device, 0, c->w_bf16, (const float4*)b, n, (float*)(b + in_b), err) != cudaSuccess)
         return BSM_ERR_CUDA;
     if (cudaMemcpy(out, b + in_b, out_b, cudaMemcpyDeviceToHost) != cudaSuccess) return BSM_ERR_CUDA;
-    return BSM_OK;
+    uint32_t flag = 0;
+    if (cudaMemcpy(&flag, err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BSM_ERR_CUDA;
+    return flag ? BSM_ERR_DEVICE_CHECK : BSM_OK;
 }
 
 extern "C" bsm_status bsm_cache_gradient(bsm_cache* c, const float* samples, uint32_t n, float* dW, float* loss) {

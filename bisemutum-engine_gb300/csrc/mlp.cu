@@ -6,15 +6,18 @@
 // of the next layer, so activations stay in registers from layer to layer
 // (the fully fused scheme of Müller et al., "Real-time Neural Radiance
 // Caching for Path Tracing", 2021).  Weights sit in shared memory with rows
-// padded to 72 elements (conflict-free B-fragment loads).
+// padded to 72 elements, so that ldmatrix's eight 16-byte rows fall in
+// distinct banks.
 //
-//   k_mlp_infer   encode -> 5 layers -> radiance; adds throughput x max(y, 0)
-//                 to the pixel accumulator of each cache query
-//   k_mlp_predict same forward, writes y (tests, evaluation)
+// (Inference runs on the tcgen05 path of mlp_tc.cu; the training step stays
+// on mma.sync, whose register fragments carry the activations through the
+// backward pass.)
+//
 //   k_mlp_train   forward, relative-L2 loss gradient, backward through the
 //                 layers, weight gradients dW_l = g_z^T a_{l-1} (also on the
-//                 tensor cores, reduced in shared FP32, then one global atomic
-//                 per weight per block)
+//                 tensor cores: per block 64 samples at a time, each warp
+//                 owning 16 rows of every layer's gradient in shared FP32,
+//                 then one global vector atomic per 4 weights per block)
 //   k_mlp_adam    Adam on the FP32 master weights, BF16 copies for the next pass
 //
 // Plain mma.sync is the right instruction for 64-wide layers: a tcgen05 tile
@@ -137,89 +140,6 @@ __device__ __forceinline__ void output_layer(const __nv_bfloat16* sw4, const uin
     }
 }
 
-__device__ __forceinline__ void forward(const __nv_bfloat16* sw, uint32_t (&act)[4][4], float (&y)[4], int g, int t) {
-    uint32_t tmp[4][4];
-    hidden_layer(sw + 0 * 64 * kLd, act, tmp, g, t);
-    hidden_layer(sw + 1 * 64 * kLd, tmp, act, g, t);
-    hidden_layer(sw + 2 * 64 * kLd, act, tmp, g, t);
-    hidden_layer(sw + 3 * 64 * kLd, tmp, act, g, t);
-    output_layer(sw + 4 * 64 * kLd, act, y, g, t);
-}
-
-// ------------------------------------------------------------- inference ----
-// queries: 4 float4 per query: raw[0..3], raw[4..7], raw[8..11], (throughput rgb, accumulator index bits)
-__global__ void __launch_bounds__(128) k_mlp_infer(const __nv_bfloat16* __restrict__ w, const float4* __restrict__ q,
-                                                   const uint32_t* __restrict__ count, uint32_t capacity,
-                                                   float4* accum) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    load_weights(w, sw);
-    __syncthreads();
-    const uint32_t n = min(*count, capacity);   // queries beyond the queue were dropped by the shade kernel
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16 < n; tile += warps) {
-        uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
-        float raw0[kMlpRaw], raw1[kMlpRaw];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            float4 a = r0 < n ? q[4 * (size_t)r0 + k] : make_float4(0, 0, 0, 0);
-            float4 b = r1 < n ? q[4 * (size_t)r1 + k] : make_float4(0, 0, 0, 0);
-            raw0[4 * k] = a.x; raw0[4 * k + 1] = a.y; raw0[4 * k + 2] = a.z; raw0[4 * k + 3] = a.w;
-            raw1[4 * k] = b.x; raw1[4 * k + 1] = b.y; raw1[4 * k + 2] = b.z; raw1[4 * k + 3] = b.w;
-        }
-        uint32_t act[4][4];
-        encode_tile(raw0, raw1, act, t);
-        float y[4];
-        forward(sw, act, y, g, t);
-        // lane t=0 holds channels 0,1 and gets channel 2 from lane t=1
-        float y2a = __shfl_down_sync(0xffffffffu, y[0], 1);
-        float y2b = __shfl_down_sync(0xffffffffu, y[2], 1);
-        if (t == 0) {
-            if (r0 < n) {
-                float4 m = q[4 * (size_t)r0 + 3];
-                float4 c = make_float4(m.x * fmaxf(y[0], 0.0f), m.y * fmaxf(y[1], 0.0f), m.z * fmaxf(y2a, 0.0f), 0.0f);
-                atomicAdd(accum + __float_as_uint(m.w), c);
-            }
-            if (r1 < n) {
-                float4 m = q[4 * (size_t)r1 + 3];
-                float4 c = make_float4(m.x * fmaxf(y[2], 0.0f), m.y * fmaxf(y[3], 0.0f), m.z * fmaxf(y2b, 0.0f), 0.0f);
-                atomicAdd(accum + __float_as_uint(m.w), c);
-            }
-        }
-    }
-}
-
-// samples: 4 float4 per sample: raw[0..3], raw[4..7], raw[8..11], (target rgb, unused)
-__global__ void __launch_bounds__(128) k_mlp_predict(const __nv_bfloat16* __restrict__ w,
-                                                     const float4* __restrict__ s, uint32_t n, float* out) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    load_weights(w, sw);
-    __syncthreads();
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16 < n; tile += warps) {
-        uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
-        float raw0[kMlpRaw], raw1[kMlpRaw];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            float4 a = r0 < n ? s[4 * (size_t)r0 + k] : make_float4(0, 0, 0, 0);
-            float4 b = r1 < n ? s[4 * (size_t)r1 + k] : make_float4(0, 0, 0, 0);
-            raw0[4 * k] = a.x; raw0[4 * k + 1] = a.y; raw0[4 * k + 2] = a.z; raw0[4 * k + 3] = a.w;
-            raw1[4 * k] = b.x; raw1[4 * k + 1] = b.y; raw1[4 * k + 2] = b.z; raw1[4 * k + 3] = b.w;
-        }
-        uint32_t act[4][4];
-        encode_tile(raw0, raw1, act, t);
-        float y[4];
-        forward(sw, act, y, g, t);
-        int c0 = 2 * t;
-        if (c0 < 3) {
-            if (r0 < n) { out[3 * (size_t)r0 + c0] = y[0]; if (c0 + 1 < 3) out[3 * (size_t)r0 + c0 + 1] = y[1]; }
-            if (r1 < n) { out[3 * (size_t)r1 + c0] = y[2]; if (c0 + 1 < 3) out[3 * (size_t)r1 + c0 + 1] = y[3]; }
-        }
-    }
-}
 
 // --------------------------------------------------------------- training ----
 // Shared memory: weights | dW (fp32) | per warp: activations e,a0..a3 and
@@ -507,23 +427,6 @@ static cudaError_t mlp_setup(int device) {
         g_mlp_grid = sms;
     }
     return cudaSuccess;
-}
-
-cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const float4* queries, const uint32_t* count,
-                             uint32_t capacity, float4* accum) {
-    cudaError_t e = mlp_setup(device);
-    if (e != cudaSuccess) return e;
-    k_mlp_infer<<<g_mlp_grid * 4, 128, kWSmem * 2, st>>>((const __nv_bfloat16*)wb, queries, count, capacity, accum);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
-                               float* out) {
-    cudaError_t e = mlp_setup(device);
-    if (e != cudaSuccess) return e;
-    if (n == 0) return cudaSuccess;
-    k_mlp_predict<<<g_mlp_grid * 4, 128, kWSmem * 2, st>>>((const __nv_bfloat16*)wb, samples, n, out);
-    return cudaGetLastError();
 }
 
 cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,

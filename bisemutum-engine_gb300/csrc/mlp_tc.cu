@@ -1,0 +1,327 @@
+// mlp_tc.cu — the radiance cache's forward pass on the 5th-generation tensor
+// cores (tcgen05, accumulators in tensor memory).
+//
+// A CTA of 128 threads takes 128 queries at a time; thread i owns query row i.
+// Each layer is one 128 x N x 64 product, D[query][out] = sum_in
+// act[query][in] W[out][in], issued as four K = 16 tcgen05.mma by one thread:
+//   A  activations, 128 rows x 64 BF16 in shared memory (16 KB)
+//   B  the layer's weights, N rows x 64 BF16 in shared memory (N = 64, or 16
+//      for the output layer: 8 weight rows and 8 zero rows)
+//   D  FP32 in tensor memory: lane = query row, column = output feature.
+// Both operands are K-major with the 128-byte swizzle: a row of 64 BF16 is
+// one 128-byte swizzle row, rows come in 8-row groups 1024 bytes apart, and
+// the 16-byte chunk c of row r sits at chunk c ^ (r mod 8).  The K = 16 step
+// k starts 32 k bytes into the rows.  tcgen05.commit signals an mbarrier when
+// the four products are done; each warp then reads its 32 rows of D
+// (tcgen05.ld 32x32b), applies ReLU, rounds to BF16 and writes them back as
+// the next layer's A.  Rounding points and FP32 accumulation are those of the
+// mma.sync training kernels (mlp.cu); only the order of the FP32 sums differs.
+//
+// Every mbarrier wait gives up after one second: the kernel then sets bit 1
+// of the error word, stops issuing products and frees its tensor memory.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "mlp.cuh"
+#include "pt_device.h"
+
+namespace bsm {
+namespace {
+
+constexpr int kTcRows = 128;                                    // queries per tile (MMA M)
+constexpr int kTcW4Rows = 16;                                   // output layer as an N = 16 product
+constexpr int kTcWRows = kMlpHidden * 64 + kTcW4Rows;           // 272 weight rows in shared memory
+constexpr int kTcActOff = kTcWRows * 128;                       // 34816 = 34 x 1024
+constexpr int kTcBarOff = kTcActOff + kTcRows * 128;            // 51200
+constexpr int kTcSmem = kTcBarOff + 16 + 1024;                  // + slack to align the base to 1024
+constexpr uint32_t kTcCols = 64;                                // tensor-memory columns per CTA
+constexpr uint32_t kTcErrTimeout = 2u;                          // error word bit: a tensor-core wait timed out
+static_assert(kTcActOff % 1024 == 0, "swizzled tiles start on 1024-byte boundaries");
+
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16
+// A and B (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at
+// bits 17-22, M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// Shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading
+// byte offset 16 >> 4 (bits 16-29; not used by swizzled K-major operands),
+// stride byte offset 1024 >> 4 between 8-row groups (bits 32-45), descriptor
+// version 1 (bits 46-47), base offset 0 (tiles are 1024-byte aligned),
+// layout 2 = 128-byte swizzle (bits 61-63).
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase of parity `parity` to complete; false after one second.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (global_ns() - t0 > 1000000000ull) return false;
+    return true;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// generic-proxy shared-memory writes become visible to the tensor core
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_alloc(uint32_t slot, uint32_t cols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(cols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t cols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols) : "memory");
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// 16 columns of the warp's 32 lanes; the wait names the registers so that no
+// use of them is scheduled before the load has landed.
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                   "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]),
+                   "+r"(v[15])
+                 :
+                 : "memory");
+}
+
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// 16-byte chunk c (features 8c..8c+7) of row r of a swizzled 128-row tile.
+__device__ __forceinline__ uint4* tile_chunk(unsigned char* tile, int r, int c) {
+    return reinterpret_cast<uint4*>(tile + r * 128 + ((c ^ (r & 7)) << 4));
+}
+
+// Encoded features of one query (the encoding of mlp_feature), written as
+// row r of the activation tile: chunk d < 7 holds sin/cos(2^k pi raw[d]),
+// k = 0..3; chunk 7 holds raw[7..11], 1, 0, 0.
+__device__ __forceinline__ void encode_row(const float (&raw)[kMlpRaw], unsigned char* act, int r) {
+#pragma unroll
+    for (int d = 0; d < 7; ++d) {
+        uint32_t p[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float s, c;
+            sincos_turns(raw[d] * (float)(1 << k) * 0.5f, &s, &c);
+            p[k] = pack2(s, c);
+        }
+        *tile_chunk(act, r, d) = make_uint4(p[0], p[1], p[2], p[3]);
+    }
+    *tile_chunk(act, r, 7) =
+        make_uint4(pack2(raw[7], raw[8]), pack2(raw[9], raw[10]), pack2(raw[11], 1.0f), pack2(0.0f, 0.0f));
+}
+
+// kInfer: queries (4 float4: raw[0..11], then throughput rgb and the pixel
+// accumulator index bits), n = min(*count, n_max); adds throughput x max(y, 0)
+// to the accumulator.  Otherwise: samples (raw in the first 3 float4), n =
+// n_max, writes y (3 floats per sample) to out.
+template <bool kInfer>
+__global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16* __restrict__ w,
+                                                            const float4* __restrict__ q, const uint32_t* count,
+                                                            uint32_t n_max, float4* accum, float* out, uint32_t* err) {
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t raw_s = smem_u32(smem_raw);
+    const uint32_t base_s = (raw_s + 1023u) & ~1023u;
+    unsigned char* base = smem_raw + (base_s - raw_s);
+    unsigned char* act = base + kTcActOff;
+    const uint32_t act_s = base_s + kTcActOff, bar = base_s + kTcBarOff;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kTcBarOff + 8);
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    // weights: rows 0..263 from global (W0..W3, W4), rows 264..271 zero
+    const uint4* wsrc = reinterpret_cast<const uint4*>(w);
+    static_assert(kTcWRows * 8 % kTcRows == 0, "whole rounds of 16-byte weight loads");
+#pragma unroll
+    for (int j = 0; j < kTcWRows * 8 / kTcRows; ++j) {   // all loads in flight before the stores
+        int i = tid + j * kTcRows, r = i >> 3, c = i & 7;
+        *tile_chunk(base, r, c) = r < kMlpHidden * 64 + kMlpOutPad ? __ldg(wsrc + i) : make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (tid == 0) mbar_init(bar, 1);
+    __syncwarp();
+    if (warp == 0) tc_alloc(smem_u32(tmem_slot), kTcCols);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t rows_tmem = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
+    const uint32_t n = kInfer ? min(*count, n_max) : n_max;
+    uint32_t phase = 0;
+    bool failed = false;
+
+    // this row's query of the next tile, loaded while the current tile is in the tensor cores
+    auto fetch = [&](uint32_t row, float4 (&f)[4]) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            f[k] = row < n && (kInfer || k < 3) ? q[4 * (size_t)row + k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    };
+    float4 next[4];
+    fetch(blockIdx.x * kTcRows + tid, next);
+    for (uint32_t tile = blockIdx.x; tile * kTcRows < n && !failed; tile += gridDim.x) {
+        const uint32_t row = tile * kTcRows + tid;
+        const float4 m = next[3];   // throughput and accumulator index (queries)
+        {
+            float raw[kMlpRaw];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                raw[4 * k] = next[k].x; raw[4 * k + 1] = next[k].y; raw[4 * k + 2] = next[k].z; raw[4 * k + 3] = next[k].w;
+            }
+            fetch(row + gridDim.x * kTcRows, next);
+            encode_row(raw, act, tid);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        for (int l = 0; l <= kMlpHidden; ++l) {
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t w_s = base_s + l * 64 * 128;
+                const uint32_t idesc = l < kMlpHidden ? tc_idesc(kTcRows, 64) : tc_idesc(kTcRows, kTcW4Rows);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) tc_mma(tmem, tc_sdesc(act_s + 32 * k), tc_sdesc(w_s + 32 * k), idesc, k);
+                tc_commit(bar);
+            }
+            __syncwarp();
+            const bool done = mbar_wait(bar, phase);
+            phase ^= 1u;
+            __syncwarp();   // the tensor-memory loads below are warp-collective
+            tc_fence_after();
+            if (l < kMlpHidden) {
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {   // 16 columns = two chunks of the next layer's input
+                    uint32_t v[16];
+                    tc_ld16(rows_tmem + 16 * h, v);
+                    uint32_t p[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        p[i] = pack2(fmaxf(__uint_as_float(v[2 * i]), 0.0f), fmaxf(__uint_as_float(v[2 * i + 1]), 0.0f));
+                    *tile_chunk(act, tid, 2 * h) = make_uint4(p[0], p[1], p[2], p[3]);
+                    *tile_chunk(act, tid, 2 * h + 1) = make_uint4(p[4], p[5], p[6], p[7]);
+                }
+            } else {
+                uint32_t v[16];
+                tc_ld16(rows_tmem, v);
+                float y0 = __uint_as_float(v[0]), y1 = __uint_as_float(v[1]), y2 = __uint_as_float(v[2]);
+                if (done && row < n) {
+                    if (kInfer) {
+                        atomicAdd(accum + __float_as_uint(m.w),
+                                  make_float4(m.x * fmaxf(y0, 0.0f), m.y * fmaxf(y1, 0.0f), m.z * fmaxf(y2, 0.0f), 0.0f));
+                    } else {
+                        out[3 * (size_t)row] = y0;
+                        out[3 * (size_t)row + 1] = y1;
+                        out[3 * (size_t)row + 2] = y2;
+                    }
+                }
+            }
+            fence_async_smem();
+            tc_fence_before();
+            if (__syncthreads_or(!done)) { failed = true; break; }
+        }
+    }
+    if (failed) {
+        if (tid == 0) {
+            atomicOr(err, kTcErrTimeout);
+            mbar_wait(bar, phase ^ 1u);   // the products of the abandoned layer, once more bounded
+        }
+        tc_fence_before();
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tc_dealloc(tmem, kTcCols);
+    }
+}
+
+int g_tc_grid = 0;
+bool g_tc_attr = false;
+
+cudaError_t tc_setup(int device) {
+    if (!g_tc_attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_mlp_forward_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+        if (e != cudaSuccess) return e;
+        g_tc_attr = true;
+    }
+    if (!g_tc_grid) {
+        int sms = 0;
+        cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (e != cudaSuccess) return e;
+        g_tc_grid = sms * 4;   // 4 CTAs per SM: 4 x 53 KB shared memory, 4 x 64 of the 512 tensor-memory columns
+    }
+    return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const float4* queries, const uint32_t* count,
+                             uint32_t capacity, float4* accum, uint32_t* err) {
+    cudaError_t e = tc_setup(device);
+    if (e != cudaSuccess) return e;
+    k_mlp_forward_tc<true><<<g_tc_grid, kTcRows, kTcSmem, st>>>((const __nv_bfloat16*)wb, queries, count, capacity,
+                                                                accum, nullptr, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
+                               float* out, uint32_t* err) {
+    cudaError_t e = tc_setup(device);
+    if (e != cudaSuccess) return e;
+    if (n == 0) return cudaSuccess;
+    uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+    uint32_t grid = tiles < (uint32_t)g_tc_grid ? tiles : (uint32_t)g_tc_grid;
+    k_mlp_forward_tc<false><<<grid, kTcRows, kTcSmem, st>>>((const __nv_bfloat16*)wb, samples, nullptr, n, nullptr, out,
+                                                            err);
+    return cudaGetLastError();
+}
+
+}  // namespace bsm

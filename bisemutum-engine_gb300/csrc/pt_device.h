@@ -85,7 +85,8 @@ enum : uint32_t {
     kCntWork = kCntShadow + 16,    // [2 * kMaxSeg] persistent-kernel work counters
     kCntSky = kCntWork + 32,       // [kMaxSeg] sky shadow rays of segment s (queue back)
     kCntCache = kCntSky + 16,      // radiance-cache queries of the chunk
-    kCntError = kCntCache + 1,     // error flags (bit 0: queue overflow); words below it are cleared per chunk
+    kCntError = kCntCache + 1,     // error flags (bit 0: queue overflow, bit 1: a tensor-core wait timed out);
+                                   // words below it are cleared per chunk
     kCntWords = kCntError + 1
 };
 // stats[] (uint64) offsets
@@ -146,10 +147,11 @@ void launch_tlas_refit(cudaStream_t st, CwNode* nodes, float* node_box, const fl
 void launch_primary(cudaStream_t st, const DevScene& sc, const DevView& v, float near_z, float far_z, float* depth,
                     float4* const gb[4], float4* hitpos);
 // radiance cache (mlp.cu)
+// (mlp_tc.cu; `err`: a device word that gets bit 1 if a tensor-core wait timed out)
 cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const float4* queries, const uint32_t* count,
-                             uint32_t capacity, float4* accum);
+                             uint32_t capacity, float4* accum, uint32_t* err);
 cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
-                               float* out);
+                               float* out, uint32_t* err);
 cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
                              float* dW, float* loss);
 // Adam step; with ema_decay > 0 also updates the weights' moving average `ema` and writes its
