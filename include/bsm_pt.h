@@ -61,7 +61,7 @@ enum {
     BSM_ERR_BAD_STATE = -6,
     BSM_ERR_NO_DEVICE = -7,
     BSM_ERR_UNSUPPORTED = -8,
-    BSM_ERR_DEVICE_CHECK = -9,   /* a kernel's own bounds/overflow check fired */
+    BSM_ERR_DEVICE_CHECK = -9,   /* a kernel's own bounds/overflow check or bounded wait fired */
     BSM_ERR_ADMISSION = -10      /* serving: request does not fit the memory budget */
 };
 
@@ -490,7 +490,9 @@ BSM_API bsm_status bsm_cache_weights(bsm_cache* cache, float* get, const float* 
  * master weights over the Adam steps taken with ema_decay > 0, or the master weights before any. */
 BSM_API bsm_status bsm_cache_render_weights(bsm_cache* cache, float* out);
 /* samples: n x 16 floats (12 raw inputs, 3 target radiance, 1 unused), host memory.
- * Prediction (n x 3) / gradient of the mean relative L2 loss (bsm_cache_param_count floats). */
+ * Prediction (n x 3) / gradient of the mean relative L2 loss (bsm_cache_param_count floats).
+ * Prediction runs the render's tcgen05 inference kernel; BSM_ERR_DEVICE_CHECK if one of its bounded
+ * tensor-core waits gave up (a render reports the same through its device error word). */
 BSM_API bsm_status bsm_cache_predict(bsm_cache* cache, const float* samples, uint32_t n, float* out);
 BSM_API bsm_status bsm_cache_gradient(bsm_cache* cache, const float* samples, uint32_t n, float* dW, float* loss);
 /* Adam steps over `samples` in batches; returns the mean loss. */
