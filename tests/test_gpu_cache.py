@@ -38,6 +38,31 @@ def test_forward_matches_oracle(cache, oracle):
     assert np.median(np.abs(g - o)) <= 1e-3 * scale
 
 
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 4097, 100_000])
+def test_forward_sizes_match_oracle(cache, oracle, n):
+    """Partial and multiple 128-query tiles of the tensor-core forward (several tiles per CTA at 100,000)."""
+    S = random_samples(n, 10 + n % 97)
+    W = cache.weights()
+    g = cache.predict(S)
+    o = oracle.mlp_forward(W, S, bf16=True)
+    scale = float(np.abs(o).max())
+    assert g.shape == o.shape
+    assert np.abs(g - o).max() <= 1e-2 * scale + 1e-5
+
+
+@pytest.mark.parametrize("n", [64, 20_000])
+def test_gradient_sizes_match_oracle(cache, oracle, n):
+    """One 64-sample group, and several groups per block of the training kernel."""
+    S = random_samples(n, 20 + n % 89)
+    W = cache.weights()
+    dg, lg = cache.gradient(S)
+    do, lo = oracle.mlp_gradient(W, S, bf16=True)
+    assert abs(lg - lo) <= 1e-3 * abs(lo)
+    x, y = dg.astype(np.float64), do.astype(np.float64)
+    assert float(x @ y / (np.linalg.norm(x) * np.linalg.norm(y))) > 0.999
+    assert np.abs(x - y).max() <= 2e-2 * np.abs(y).max()
+
+
 def test_gradient_matches_oracle(cache, oracle):
     S = random_samples(777, 2)     # not a multiple of the 16-row tile
     W = cache.weights()
