@@ -24,6 +24,7 @@
 // of 128 rows would leave most of the tensor memory and the pipeline idle at
 // this width, and the whole frame's inference is ~69 GFLOP.
 #include <cuda_bf16.h>
+#include <atomic>
 #include <cuda_runtime.h>
 
 #include "mlp.cuh"
@@ -412,19 +413,22 @@ __global__ void k_mlp_adam(float* __restrict__ wm, __nv_bfloat16* __restrict__ w
 }
 
 // ------------------------------------------------------------- launchers ----
-static int g_mlp_grid = 0;
-static bool g_mlp_attr = false;
+// Per device (ordinal < 64): the opt-in shared-memory size is a per-device function attribute.
+static std::atomic<uint64_t> g_mlp_attr{0};
+static int g_mlp_grid[64] = {};
 
 static cudaError_t mlp_setup(int device) {
-    if (!g_mlp_attr) {
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    if (!(g_mlp_attr.load() & (1ull << device))) {
         cudaError_t e = cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
         if (e != cudaSuccess) return e;
-        g_mlp_attr = true;
+        g_mlp_attr.fetch_or(1ull << device);
     }
-    if (!g_mlp_grid) {
+    if (!g_mlp_grid[device]) {
         int sms = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-        g_mlp_grid = sms;
+        cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (e != cudaSuccess) return e;
+        g_mlp_grid[device] = sms;
     }
     return cudaSuccess;
 }
@@ -436,7 +440,8 @@ cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const 
     if (n == 0) return cudaSuccess;
     // 64 samples per block and step; as few blocks as keep the number of steps per block minimal
     uint32_t groups = (n + 63) / 64;
-    uint32_t per_block = (groups + (uint32_t)g_mlp_grid - 1) / (uint32_t)g_mlp_grid;
+    const uint32_t sms = (uint32_t)g_mlp_grid[device];
+    uint32_t per_block = (groups + sms - 1) / sms;
     uint32_t grid = (groups + per_block - 1) / per_block;
     k_mlp_train<<<grid, 128, kTrainSmem, st>>>((const __nv_bfloat16*)wb, samples, n, dW, loss);
     return cudaGetLastError();

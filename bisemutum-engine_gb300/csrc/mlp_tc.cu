@@ -20,6 +20,7 @@
 // Every mbarrier wait gives up after one second: the kernel then sets bit 1
 // of the error word, stops issuing products and frees its tensor memory.
 #include <cuda_bf16.h>
+#include <atomic>
 #include <cuda_runtime.h>
 
 #include "mlp.cuh"
@@ -281,22 +282,24 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
     }
 }
 
-int g_tc_grid = 0;
-bool g_tc_attr = false;
+// Per device (ordinal < 64): the opt-in shared-memory size is a per-device function attribute.
+std::atomic<uint64_t> g_tc_attr{0};
+int g_tc_grid[64] = {};
 
 cudaError_t tc_setup(int device) {
-    if (!g_tc_attr) {
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    if (!(g_tc_attr.load() & (1ull << device))) {
         cudaError_t e = cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_mlp_forward_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
         if (e != cudaSuccess) return e;
-        g_tc_attr = true;
+        g_tc_attr.fetch_or(1ull << device);
     }
-    if (!g_tc_grid) {
+    if (!g_tc_grid[device]) {
         int sms = 0;
         cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
         if (e != cudaSuccess) return e;
-        g_tc_grid = sms * 4;   // 4 CTAs per SM: 4 x 53 KB shared memory, 4 x 64 of the 512 tensor-memory columns
+        g_tc_grid[device] = sms * 4;   // 4 CTAs per SM: 4 x 53 KB shared memory, 4 x 64 of 512 tensor-memory columns
     }
     return cudaSuccess;
 }
@@ -307,7 +310,7 @@ cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const 
                              uint32_t capacity, float4* accum, uint32_t* err) {
     cudaError_t e = tc_setup(device);
     if (e != cudaSuccess) return e;
-    k_mlp_forward_tc<true><<<g_tc_grid, kTcRows, kTcSmem, st>>>((const __nv_bfloat16*)wb, queries, count, capacity,
+    k_mlp_forward_tc<true><<<g_tc_grid[device], kTcRows, kTcSmem, st>>>((const __nv_bfloat16*)wb, queries, count, capacity,
                                                                 accum, nullptr, err);
     return cudaGetLastError();
 }
@@ -318,7 +321,7 @@ cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, cons
     if (e != cudaSuccess) return e;
     if (n == 0) return cudaSuccess;
     uint32_t tiles = (n + kTcRows - 1) / kTcRows;
-    uint32_t grid = tiles < (uint32_t)g_tc_grid ? tiles : (uint32_t)g_tc_grid;
+    uint32_t grid = tiles < (uint32_t)g_tc_grid[device] ? tiles : (uint32_t)g_tc_grid[device];
     k_mlp_forward_tc<false><<<grid, kTcRows, kTcSmem, st>>>((const __nv_bfloat16*)wb, samples, nullptr, n, nullptr, out,
                                                             err);
     return cudaGetLastError();
