@@ -20,9 +20,10 @@
 //                 then one global vector atomic per 4 weights per block)
 //   k_mlp_adam    Adam on the FP32 master weights, BF16 copies for the next pass
 //
-// Plain mma.sync is the right instruction for 64-wide layers: a tcgen05 tile
-// of 128 rows would leave most of the tensor memory and the pipeline idle at
-// this width, and the whole frame's inference is ~69 GFLOP.
+// The training step stays on mma.sync because its backward pass reuses the
+// forward's register fragments and needs the activations and gradients
+// transposed for the weight gradient: 16-sample tiles in registers and
+// shared memory serve both, at 26 us per Adam step of ~13,000 vertices.
 #include <cuda_bf16.h>
 #include <atomic>
 #include <cuda_runtime.h>
