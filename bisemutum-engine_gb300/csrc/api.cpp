@@ -1407,7 +1407,7 @@ extern "C" bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, con
         dv.t_min = settings->t_min;
         dv.seed = settings->seed;
         dv.max_segments = std::min(std::max(cs.train_segments, 1u), 16u);
-        bsm_status e = cache_train_frame(cache, sc->dev, dv, cs, ctx->stream, train_loss, nullptr);
+        bsm_status e = cache_train_frame(cache, sc->dev, dv, cs, ctx->lc, ctx->stream, train_loss, nullptr);
         if (e) return fail(ctx, e, "radiance-cache training failed");
     }
     std::vector<ViewReq> req(1);

@@ -98,7 +98,8 @@ extern "C" void bsm_cache_destroy(bsm_cache* c) {
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
     for (void* p : {(void*)c->w_master, c->w_bf16, (void*)c->w_ema, c->w_ema_bf16, (void*)c->adam_m, (void*)c->adam_v, (void*)c->dW, (void*)c->loss,
-                    (void*)c->samples, (void*)c->sample_count, (void*)c->view_dev, (void*)c->io})
+                    (void*)c->samples, (void*)c->sample_count, (void*)c->view_dev, (void*)c->io, (void*)c->tv_raw,
+                    (void*)c->tv_thr, (void*)c->tv_rad, (void*)c->tv_count, c->tv_queue})
         if (p) cudaFree(p);
     delete c;
 }
@@ -249,9 +250,31 @@ extern "C" bsm_status bsm_cache_load(bsm_cache* c, const char* path) {
 }
 
 namespace bsm {
+// Per-vertex records of the training paths and their shadow-ray queue, grown on demand.
+static bsm_status ensure_train_verts(bsm_cache* c, uint32_t paths, uint32_t verts, uint32_t lights1) {
+    if (c->tv_cap >= verts && c->tv_paths >= paths && c->tv_lights >= lights1) return BSM_OK;
+    if ((uint64_t)verts * lights1 >= (1ull << 32) || (uint64_t)verts >= (1ull << 31)) return BSM_ERR_INVALID_ARG;
+    for (void** p : {(void**)&c->tv_raw, (void**)&c->tv_thr, (void**)&c->tv_rad, (void**)&c->tv_count, &c->tv_queue})
+        if (*p) { cudaFree(*p); *p = nullptr; }
+    c->tv_cap = c->tv_paths = c->tv_lights = 0;
+    const size_t sh = (size_t)verts * lights1;
+    const size_t qbytes = 3 * sh * 16 + ((sh * 4 + 255) & ~(size_t)255) + kCntWords * 4 + 256 + kStatWords * 8;
+    bool ok = cudaMalloc((void**)&c->tv_raw, (size_t)verts * 48) == cudaSuccess &&
+              cudaMalloc((void**)&c->tv_thr, (size_t)verts * 16) == cudaSuccess &&
+              cudaMalloc((void**)&c->tv_rad, (size_t)verts * 16) == cudaSuccess &&
+              cudaMalloc((void**)&c->tv_count, (size_t)paths * 4) == cudaSuccess &&
+              cudaMalloc(&c->tv_queue, qbytes) == cudaSuccess;
+    if (!ok) return BSM_ERR_OUT_OF_MEMORY;
+    c->tv_cap = verts;
+    c->tv_paths = paths;
+    c->tv_lights = lights1;
+    return BSM_OK;
+}
+
 bsm_status cache_train_frame(bsm_cache* c, const DevScene& sc, const DevView& view, const bsm_cache_settings& cs,
-                             cudaStream_t st, float* loss_out, uint32_t* samples_out) {
-    uint32_t cap = cs.train_paths * std::max(1u, std::min(cs.train_segments, 16u));
+                             const LaunchCfg& lc, cudaStream_t st, float* loss_out, uint32_t* samples_out) {
+    const uint32_t segs = std::max(1u, std::min(cs.train_segments, 16u));
+    const uint32_t cap = cs.train_paths * segs;
     if (c->sample_cap < cap) {
         if (c->samples) cudaFree(c->samples);
         c->samples = nullptr;
@@ -259,10 +282,27 @@ bsm_status cache_train_frame(bsm_cache* c, const DevScene& sc, const DevView& vi
         if (cudaMalloc((void**)&c->samples, (size_t)cap * 64) != cudaSuccess) return BSM_ERR_OUT_OF_MEMORY;
         c->sample_cap = cap;
     }
+    const uint32_t lights1 = sc.num_lights + 1u;
+    if (bsm_status e = ensure_train_verts(c, cs.train_paths, cap, lights1)) return e;
+    // shadow queue view (the fields launch_shadow reads), sized for `cap` vertices x (lights + 1) rays
+    const size_t sh = (size_t)cap * lights1;
+    char* qb = (char*)c->tv_queue;
+    Wavefront q{};
+    q.capacity = cap;
+    q.sh_o = (float4*)qb;
+    q.sh_d = (float4*)(qb + sh * 16);
+    q.sh_c = (float4*)(qb + 2 * sh * 16);
+    q.sh_seed = (uint32_t*)(qb + 3 * sh * 16);
+    q.counters = (uint32_t*)(qb + 3 * sh * 16 + ((sh * 4 + 255) & ~(size_t)255));
+    q.stats = (unsigned long long*)((char*)q.counters + ((kCntWords * 4 + 255) & ~(size_t)255));
+    TrainVerts tv{c->tv_raw, c->tv_thr, c->tv_rad, c->tv_count, segs};
     cudaMemcpyAsync(c->view_dev, &view, sizeof(DevView), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(c->sample_count, 0, 4, st);
-    launch_train_paths(st, sc, c->view_dev, cs.train_paths, c->frame++, cs.train_segments, c->samples,
-                       c->sample_count, c->sample_cap);
+    cudaMemsetAsync(q.counters, 0, kCntWords * 4, st);
+    launch_train_paths(st, sc, c->view_dev, cs.train_paths, c->frame++, tv, q);
+    launch_shadow(lc, st, sc, q, 0, c->tv_rad);
+    launch_train_targets(st, cs.train_paths, tv, c->samples, c->sample_count, c->sample_cap);
+    if (cudaGetLastError() != cudaSuccess) return BSM_ERR_CUDA;
     uint32_t n = 0;
     cudaMemcpyAsync(&n, c->sample_count, 4, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return BSM_ERR_CUDA;

@@ -25,6 +25,15 @@ struct bsm_cache {
     float4* samples = nullptr;   // training samples (4 float4 each)
     uint32_t* sample_count = nullptr;
     uint32_t sample_cap = 0;
+    // training paths: per-vertex records (vertex v = path x segments + k) and their shadow-ray queue
+    float4* tv_raw = nullptr;      // 3 float4 per vertex: the cache's raw inputs
+    float4* tv_thr = nullptr;      // path throughput at the vertex
+    float4* tv_rad = nullptr;      // radiance gathered at the vertex (NEE through the shadow pass, sky on escape)
+    uint32_t* tv_count = nullptr;  // vertices per path
+    void* tv_queue = nullptr;      // shadow rays (origin, direction, contribution + vertex, seed), counters, stats
+    uint32_t tv_cap = 0;           // vertices the buffers hold
+    uint32_t tv_paths = 0;         // paths tv_count holds
+    uint32_t tv_lights = 0;        // lights the shadow queue was sized for
     bsm::DevView* view_dev = nullptr;
     float* io = nullptr;         // device staging for host-buffer entry points
     size_t io_bytes = 0;
@@ -37,5 +46,5 @@ namespace bsm {
 inline const void* cache_render_weights(const bsm_cache* c) { return c->ema_steps > 0 ? c->w_ema_bf16 : c->w_bf16; }
 // Runs train paths + Adam steps for one camera (cache.cpp).
 bsm_status cache_train_frame(bsm_cache* c, const DevScene& sc, const DevView& view, const bsm_cache_settings& cs,
-                             cudaStream_t st, float* loss_out, uint32_t* samples_out);
+                             const LaunchCfg& lc, cudaStream_t st, float* loss_out, uint32_t* samples_out);
 }

@@ -158,9 +158,22 @@ cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const 
 // bias-corrected bf16 copy `ema_b` (ema_step: steps averaged, this one included)
 cudaError_t launch_mlp_adam(cudaStream_t st, float* wm, void* wb, const float* dW, float* m, float* v, float lr,
                             int step, float* ema, void* ema_b, float ema_decay, int ema_step);
-// training paths (train_paths.cu): full-length paths that record per-vertex cache samples
+// training paths (train_paths.cu): full-length paths that record per-vertex cache samples.
+// Vertex v = path x segments + k.  The path kernel writes each vertex's raw inputs (3 float4), throughput
+// and directly gathered radiance, and queues its next-event shadow rays in `shadow` (sun/light rays from the
+// front, sky rays from the back, contribution.w = the vertex's bits); the shadow pass (launch_shadow with
+// accum = vrad) adds the unoccluded ones; the targets kernel turns each vertex into a training sample.
+struct TrainVerts {
+    float4* raw;
+    float4* thr;
+    float4* rad;
+    uint32_t* count;   // vertices per path
+    uint32_t segments;
+};
 void launch_train_paths(cudaStream_t st, const DevScene& sc, const DevView* view, uint32_t n_paths, uint32_t frame,
-                        uint32_t max_segments, float4* samples, uint32_t* count, uint32_t max_samples);
+                        const TrainVerts& tv, const Wavefront& shadow);
+void launch_train_targets(cudaStream_t st, uint32_t n_paths, const TrainVerts& tv, float4* samples, uint32_t* count,
+                          uint32_t max_samples);
 
 // Fills the persistent-kernel grids from the device's SM count and occupancy
 // (for the kernel variant lc->regcap selects).

@@ -1,12 +1,17 @@
 // train_paths.cu — training data for the radiance cache, generated by the tracer.
 //
-// One thread traces one full-length path (the plain pass's stages in one loop:
-// closest hit, sun and sky next-event estimation with any-hit visibility, lobe
-// sampling, sky on escape with MIS) and records every vertex k it reaches: the
-// cache's raw inputs there and the radiance the rest of the path carried back
-// to it, T_k = (sum of contributions at vertices j >= k) / throughput_k.  Those
-// (input, T_k) pairs are what the network learns, so that a path cut short at
-// a vertex can be finished with throughput x cache(vertex).
+// One thread follows one full-length path (the plain pass's stages: closest
+// hit, sun/light and sky next-event estimation, lobe sampling, sky on escape
+// with MIS) and records every vertex k it reaches: the cache's raw inputs, the
+// path throughput there, and the radiance gathered there directly (the sky on
+// escape).  Its next-event shadow rays are not traced in the thread: they go
+// to a shadow queue, which the persistent any-hit kernel traces afterwards in
+// one launch, adding each unoccluded contribution to its vertex.  A thread's
+// serial chain is thus its closest-hit rays only.  The targets kernel then
+// forms T_k = (sum of radiance at vertices j >= k) / throughput_k, the radiance
+// the rest of the path carried back to vertex k: the (input, T_k) pairs are
+// what the network learns, so that a path cut short at a vertex can be
+// finished with throughput x cache(vertex).
 // Pixels are drawn per frame by a hash of (frame, path index); random numbers
 // are PCG32 streams keyed to the pixel and a per-frame sample index.
 #include <cuda_runtime.h>
@@ -23,9 +28,26 @@ namespace bsm {
 
 constexpr int kTrainMaxVerts = 16;
 
+// A slot of `ctr` for each calling lane, one atomic per group of converged lanes.
+__device__ __forceinline__ uint32_t agg_alloc(uint32_t* ctr) {
+    const uint32_t m = __activemask(), lane = threadIdx.x & 31u;
+    const uint32_t leader = (uint32_t)__ffs(m) - 1u;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(ctr, (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void queue_shadow(const Wavefront& q, uint32_t slot, V3 o, float tmin, V3 d, float tmax,
+                                             V3 c, uint32_t vertex, uint32_t seed) {
+    q.sh_o[slot] = make_float4(o.x, o.y, o.z, tmin);
+    q.sh_d[slot] = make_float4(d.x, d.y, d.z, tmax);
+    q.sh_c[slot] = make_float4(c.x, c.y, c.z, __uint_as_float(vertex));
+    q.sh_seed[slot] = seed;
+}
+
 __global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevView* __restrict__ view, uint32_t n_paths,
-                                                     uint32_t frame, uint32_t max_seg, float4* samples,
-                                                     uint32_t* count, uint32_t max_samples) {
+                                                     uint32_t frame, TrainVerts tv, Wavefront q) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_paths) return;
     const DevView& v = *view;
@@ -41,12 +63,12 @@ __global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevVi
     V3 o = v3(v.pos[0], v.pos[1], v.pos[2]);
     V3 thr = v3s(1.0f);
     float last_pdf = 0.0f;
-    float raw[kTrainMaxVerts][kMlpRaw];
-    V3 thr_k[kTrainMaxVerts], contrib[kTrainMaxVerts];
     int nv = 0;
     const V3 box_lo = v3(sc.box_lo[0], sc.box_lo[1], sc.box_lo[2]);
     const V3 box_inv = v3(sc.box_inv[0], sc.box_inv[1], sc.box_inv[2]);
-    uint32_t segs = max_seg < (uint32_t)kTrainMaxVerts ? max_seg : (uint32_t)kTrainMaxVerts;
+    const uint32_t segs = tv.segments;
+    const uint32_t v0 = i * segs;                               // this path's first vertex
+    const uint32_t sh_back = q.capacity * (sc.num_lights + 1u) - 1u;
     for (uint32_t seg = 0; seg < segs; ++seg) {
         RayPre r = make_ray(make_float4(o.x, o.y, o.z, v.t_min), make_float4(d.x, d.y, d.z, v.ray_length));
         float t, hu, hv;
@@ -57,7 +79,9 @@ __global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevVi
                 V3 le = sky_eval(sc.sky, d);
                 float pl = sky_pdf(sc.sky, d), pb = last_pdf;
                 float w = (pb * pb + pl * pl) > 0.0f ? pb * pb / (pb * pb + pl * pl) : 1.0f;
-                contrib[nv - 1] = contrib[nv - 1] + thr * le * w;
+                float4& rad = tv.rad[v0 + nv - 1];
+                V3 e = thr * le * w;
+                rad = make_float4(rad.x + e.x, rad.y + e.y, rad.z + e.z, 0.0f);
             }
             break;
         }
@@ -74,10 +98,17 @@ __global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevVi
         surf.f90 = v3s(1.0f);
         surf.ior = 1.5f;
         V3 V = -d;
-        mlp_raw_inputs(P, box_lo, box_inv, V, N, surf.roughness, surf.base_color, (float)seg * 0.125f, raw[nv]);
-        thr_k[nv] = thr;
-        contrib[nv] = v3s(0.0f);
-        int k = nv++;
+        const uint32_t vk = v0 + (uint32_t)nv++;
+        {
+            float raw[kMlpRaw];
+            mlp_raw_inputs(P, box_lo, box_inv, V, N, surf.roughness, surf.base_color, (float)seg * 0.125f, raw);
+            float4* rw = tv.raw + 3 * (size_t)vk;
+            rw[0] = make_float4(raw[0], raw[1], raw[2], raw[3]);
+            rw[1] = make_float4(raw[4], raw[5], raw[6], raw[7]);
+            rw[2] = make_float4(raw[8], raw[9], raw[10], raw[11]);
+        }
+        tv.thr[vk] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+        tv.rad[vk] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         Frame fr = create_frame(N);
         V3 org = P + N * sc.ray_offset;
         float u_sky0 = pcg_uniform(g), u_sky1 = pcg_uniform(g), u_sky2 = pcg_uniform(g), u_lobe = pcg_uniform(g),
@@ -95,13 +126,8 @@ __global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevVi
             if (!light_sample(lt, P, ur0, ur1, v.ray_length, L, smax, e)) continue;
             V3 f = surface_eval_lit(N, fr.x, fr.y, V, L, surf);
             V3 c = thr * e * f;
-            if (max_comp(c) > 0.0f) {
-                RayPre sr = make_ray(make_float4(org.x, org.y, org.z, v.t_min), make_float4(L.x, L.y, L.z, smax));
-                float a, b2, c2;
-                uint32_t si;
-                if (trace_scene<true>(sc, sr, smax, a, b2, c2, si, (uint32_t)g.state) == kMissPrim)
-                    contrib[k] = contrib[k] + c;
-            }
+            if (max_comp(c) > 0.0f)
+                queue_shadow(q, agg_alloc(q.counters + kCntShadow), org, v.t_min, L, smax, c, vk, (uint32_t)g.state);
         }
         {
             float pl;
@@ -112,12 +138,9 @@ __global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevVi
                 if (max_comp(f) > 0.0f) {
                     float pb = mixture_pdf(lv, to_local(fr, L), rx, ry, p_spec);
                     V3 c = thr * le * f * ((pl * pl) / (pl * pl + pb * pb) / pl);
-                    RayPre sr = make_ray(make_float4(org.x, org.y, org.z, v.t_min), make_float4(L.x, L.y, L.z, v.ray_length));
-                    float a, b2, c2;
-                    uint32_t si;
-                    if (max_comp(c) > 0.0f &&
-                        trace_scene<true>(sc, sr, v.ray_length, a, b2, c2, si, (uint32_t)g.state) == kMissPrim)
-                        contrib[k] = contrib[k] + c;
+                    if (max_comp(c) > 0.0f)
+                        queue_shadow(q, sh_back - agg_alloc(q.counters + kCntSky), org, v.t_min, L, v.ray_length, c,
+                                     vk, (uint32_t)g.state);
                 }
             }
         }
@@ -135,29 +158,45 @@ __global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevVi
         d = L;
         last_pdf = pdf;
     }
-    // targets: radiance carried back to each vertex
+    tv.count[i] = (uint32_t)nv;
+}
+
+// Targets: radiance carried back to each vertex of a path, as training samples.
+__global__ void k_train_targets(uint32_t n_paths, TrainVerts tv, float4* samples, uint32_t* count,
+                                uint32_t max_samples) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_paths) return;
+    const uint32_t v0 = i * tv.segments;
+    const int nv = (int)tv.count[i];
     V3 acc = v3s(0.0f);
     for (int k = nv - 1; k >= 0; --k) {
-        acc = acc + contrib[k];
-        V3 tk = thr_k[k];
+        float4 rad = tv.rad[v0 + k], tk4 = tv.thr[v0 + k];
+        acc = acc + v3(rad.x, rad.y, rad.z);
+        V3 tk = v3(tk4.x, tk4.y, tk4.z);
         if (!(tk.x > 0.0f && tk.y > 0.0f && tk.z > 0.0f)) continue;
         V3 target = v3(acc.x / tk.x, acc.y / tk.y, acc.z / tk.z);
         if (!isfinite(target.x) || !isfinite(target.y) || !isfinite(target.z)) continue;
         uint32_t slot = atomicAdd(count, 1u);
         if (slot >= max_samples) continue;
+        const float4* rw = tv.raw + 3 * (size_t)(v0 + k);
         float4* sd = samples + 4 * (size_t)slot;
-        sd[0] = make_float4(raw[k][0], raw[k][1], raw[k][2], raw[k][3]);
-        sd[1] = make_float4(raw[k][4], raw[k][5], raw[k][6], raw[k][7]);
-        sd[2] = make_float4(raw[k][8], raw[k][9], raw[k][10], raw[k][11]);
+        sd[0] = rw[0];
+        sd[1] = rw[1];
+        sd[2] = rw[2];
         sd[3] = make_float4(target.x, target.y, target.z, 0.0f);
     }
 }
 
 void launch_train_paths(cudaStream_t st, const DevScene& sc, const DevView* view, uint32_t n_paths, uint32_t frame,
-                        uint32_t max_segments, float4* samples, uint32_t* count, uint32_t max_samples) {
+                        const TrainVerts& tv, const Wavefront& shadow) {
     if (n_paths == 0) return;
-    k_train_paths<<<(n_paths + 127) / 128, 128, 0, st>>>(sc, view, n_paths, frame, max_segments, samples, count,
-                                                        max_samples);
+    k_train_paths<<<(n_paths + 127) / 128, 128, 0, st>>>(sc, view, n_paths, frame, tv, shadow);
+}
+
+void launch_train_targets(cudaStream_t st, uint32_t n_paths, const TrainVerts& tv, float4* samples, uint32_t* count,
+                          uint32_t max_samples) {
+    if (n_paths == 0) return;
+    k_train_targets<<<(n_paths + 255) / 256, 256, 0, st>>>(n_paths, tv, samples, count, max_samples);
 }
 
 }  // namespace bsm
