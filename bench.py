@@ -37,7 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Mrays/s (extend rays entering closest-hit) at 1 GB300, plain wavefront PT"
-DEV_VIEW_BYTES = 120  # bytes of the per-view record the render call uploads (DevView)
+DEV_VIEW_BYTES = 128  # bytes of the per-view record the render call uploads (DevView)
 EXTEND_BYTES_PER_RAY = 48  # 32 B ray read + 16 B hit written (compulsory HBM)
 NODE_BYTES, TRI_BYTES = 80, 48
 
@@ -254,7 +254,7 @@ def run_reference(a, dist: Dist):
             "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "CPU implementation of the pass (multithreaded C++ oracle, -O2, no fast-math); the reference's "
+            "note": "CPU implementation of the pass (multithreaded C++ oracle, -O3, no -march=native, no fast-math); the reference's "
                     "own pass needs a graphics ray-tracing pipeline, unavailable on this box"}
     print(json.dumps(line), flush=True)
     return 0
@@ -349,6 +349,7 @@ def run_ours(a, dist: Dist):
     e2e_val = rays_all / a.steps * e2e_steps / e2e_s / 1e6
     L.bsm_host_free(ctx.h, host)
     L.bsm_device_free(ctx.h, flush)
+    bvh_cmp = bvh_comparison(bsm, ctx, scene, a, bvh, st_dev_frame=(rays, sum(ms_dev))) if dist.rank == 0 else None
 
     line = None
     if dist.rank == 0:
@@ -394,14 +395,48 @@ def run_ours(a, dist: Dist):
                                   "extend_per_segment": seg_rays},
                 "shadow_mrays_per_s": round(shadow_rays / (ms_shadow / 1e3) / 1e6, 1) if ms_shadow > 0 else None,
                 "bvh": {"collapse": "sah-optimal" if a.collapse == 0 else "greedy",
-                        "build_s_host": round(bvh.build_ms / 1e3, 3), "nodes": bvh.num_nodes,
+                        "builder": "device" if bvh.builder == bsm.BSM_BUILD_DEVICE else "host",
+                        "build_ms": round(bvh.build_ms, 2), "nodes": bvh.num_nodes,
                         "depth": bvh.max_depth, "bytes": bvh.node_bytes + bvh.tri_bytes,
-                        "upload_and_build_s": round(setup_s, 3)},
+                        "upload_and_build_s": round(setup_s, 3), **(bvh_cmp or {})},
                 "wall_s_timed": round(wall, 3)}
     ctx.close()
     if line is not None:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def bvh_comparison(bsm, ctx, scene, a, bvh, st_dev_frame):
+    """Device against host BVH build (untimed region): build times for this scene and for the 4,973,058-triangle
+    serving scene, and the plain frame's Mrays/s traversing the host-built tree against the device-built one the
+    timed steps used (same frame, same paths)."""
+    out = {}
+    t0 = time.perf_counter()
+    sid_h = ctx.upload(scene)
+    hst = ctx.build_bvh(sid_h, sah_bins=a.bins, max_leaf=a.max_leaf, collapse=a.collapse, tri_cost=a.tri_cost,
+                        builder=bsm.BSM_BUILD_HOST)
+    out["host_build_ms"] = round(hst.build_ms, 1)
+    out["host_tree"] = {"nodes": hst.num_nodes, "depth": hst.max_depth, "sah_cost": round(hst.sah_cost, 3)}
+    out["device_tree"] = {"nodes": bvh.num_nodes, "depth": bvh.max_depth, "sah_cost": round(bvh.sah_cost, 3)}
+    jitter = bsm.BSM_PT_JITTER if a.jitter else 0
+    s = bsm.settings(spp=a.spp, max_segments=a.segments, seed=a.seed, flags=jitter, block_size=a.block,
+                     wavefront_capacity=a.capacity)
+    ctx.render(sid_h, [scene.camera], s, outputs=False)
+    _, st = ctx.render(sid_h, [scene.camera], s, outputs=False)
+    rays, ms = st_dev_frame
+    out["mrays_per_s_device_tree"] = round(rays / (ms / 1e3) / 1e6, 1)
+    out["mrays_per_s_host_tree"] = round(st.extend_rays / (st.ms_total / 1e3) / 1e6, 1)
+    ctx.release(sid_h)
+    big = bsm.generate_scene(bsm.BSM_SCENE_TERRAIN, seed=a.seed, grid=1024, spheres=6000)
+    sid_b = ctx.upload(big)
+    dst = ctx.build_bvh(sid_b)
+    out["device_build_ms_4.97M"] = round(dst.build_ms, 1)
+    hb = ctx.build_bvh(sid_b, builder=bsm.BSM_BUILD_HOST)
+    out["host_build_ms_4.97M"] = round(hb.build_ms, 1)
+    out["triangles_4.97M"] = big.num_triangles
+    ctx.release(sid_b)
+    out["comparison_s"] = round(time.perf_counter() - t0, 1)
+    return out
 
 
 # ----------------------------------------------------------------- batch ----

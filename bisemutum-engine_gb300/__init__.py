@@ -26,7 +26,7 @@ BSM_OK = 0
 STATUS_NAMES = {
     0: "BSM_OK", -1: "BSM_ERR_INVALID_ARG", -2: "BSM_ERR_OUT_OF_MEMORY", -3: "BSM_ERR_CUDA", -4: "BSM_ERR_TIMEOUT",
     -5: "BSM_ERR_NOT_FOUND", -6: "BSM_ERR_BAD_STATE", -7: "BSM_ERR_NO_DEVICE", -8: "BSM_ERR_UNSUPPORTED",
-    -9: "BSM_ERR_DEVICE_CHECK", -10: "BSM_ERR_ADMISSION",
+    -9: "BSM_ERR_DEVICE_CHECK", -10: "BSM_ERR_ADMISSION", -11: "BSM_ERR_CANCELLED",
 }
 BSM_HOST, BSM_DEVICE = 0, 1
 BSM_SKY_CONSTANT, BSM_SKY_EQUIRECT, BSM_SKY_CUBEMAP = 0, 1, 2
@@ -82,16 +82,17 @@ class SceneDesc(C.Structure):
 
 
 BSM_COLLAPSE_SAH_OPTIMAL, BSM_COLLAPSE_GREEDY = 0, 1
+BSM_BUILD_DEVICE, BSM_BUILD_HOST = 0, 1
 
 
 class BvhOpts(C.Structure):
     _fields_ = [("sah_bins", C.c_uint32), ("max_leaf_tris", C.c_uint32), ("num_threads", C.c_uint32),
-                ("collapse", C.c_uint32), ("tri_cost", C.c_float)]
+                ("collapse", C.c_uint32), ("tri_cost", C.c_float), ("builder", C.c_uint32)]
 
 
 class BvhStats(C.Structure):
     _fields_ = [("num_nodes", C.c_uint32), ("num_tris", C.c_uint32), ("max_depth", C.c_uint32),
-                ("reserved", C.c_uint32), ("build_ms", C.c_double), ("sah_cost", C.c_double),
+                ("builder", C.c_uint32), ("build_ms", C.c_double), ("sah_cost", C.c_double),
                 ("node_bytes", C.c_uint64), ("tri_bytes", C.c_uint64)]
 
 
@@ -153,7 +154,7 @@ class Request(C.Structure):
 
 
 class RequestStatus(C.Structure):
-    _fields_ = [("state", C.c_uint32), ("reserved", C.c_uint32), ("submit_ms", C.c_double),
+    _fields_ = [("state", C.c_uint32), ("cancelled", C.c_uint32), ("submit_ms", C.c_double),
                 ("admit_ms", C.c_double), ("done_ms", C.c_double), ("paths", C.c_uint64)]
 
 
@@ -161,16 +162,16 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
                 ("rejected", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("pool_bytes", C.c_uint64), ("pool_used_bytes", C.c_uint64), ("active", C.c_uint32),
-                ("queued", C.c_uint32), ("elapsed_ms", C.c_double)]
+                ("queued", C.c_uint32), ("elapsed_ms", C.c_double), ("cancelled", C.c_uint64)]
 
 
-BSM_REQ_QUEUED, BSM_REQ_RUNNING, BSM_REQ_DONE, BSM_REQ_FAILED = 0, 1, 2, 3
+BSM_REQ_QUEUED, BSM_REQ_RUNNING, BSM_REQ_DONE, BSM_REQ_FAILED, BSM_REQ_CANCELLED = 0, 1, 2, 3, 4
 
 
 class CacheSettings(C.Structure):
     _fields_ = [("cache_segment", C.c_uint32), ("train_paths", C.c_uint32), ("train_segments", C.c_uint32),
                 ("train_batch", C.c_uint32), ("train_steps", C.c_uint32), ("lr", C.c_float),
-                ("ema_decay", C.c_float)]
+                ("ema_decay", C.c_float), ("min_roughness", C.c_float), ("extra_segments", C.c_uint32)]
 
 
 class SceneGenParams(C.Structure):
@@ -229,6 +230,9 @@ _SIGS = {
     "bsm_last_error": (C.c_char_p, [C.c_void_p]),
     "bsm_api_version": (C.c_int, []),
     "bsm_sync": (C.c_int32, [C.c_void_p, C.c_uint32]),
+    "bsm_set_stream": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "bsm_get_stream": (C.c_void_p, [C.c_void_p]),
+    "bsm_render_stats_read": (C.c_int32, [C.c_void_p, C.POINTER(RenderStats)]),
     "bsm_device_alloc": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
     "bsm_device_free": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "bsm_memcpy": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int]),
@@ -266,6 +270,7 @@ _SIGS = {
     "bsm_server_wait": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(RequestStatus)]),
     "bsm_server_get_stats": (C.c_int32, [C.c_void_p, C.POINTER(ServerStats)]),
     "bsm_server_stop": (C.c_int32, [C.c_void_p]),
+    "bsm_server_cancel": (C.c_int32, [C.c_void_p, C.c_uint64]),
     "bsm_cache_settings_default": (None, [C.POINTER(CacheSettings)]),
     "bsm_cache_param_count": (C.c_uint32, []),
     "bsm_cache_create": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
@@ -764,15 +769,17 @@ class Context:
         self.check(self._L.bsm_scene_upload(self.h, C.byref(scene.desc()), C.byref(sid)))
         return sid.value
 
-    def build_bvh(self, scene_id: int, sah_bins=0, max_leaf=0, threads=0, collapse=0, tri_cost=0.0) -> BvhStats:
-        o = BvhOpts(sah_bins, max_leaf, threads, collapse, tri_cost)
+    def build_bvh(self, scene_id: int, sah_bins=0, max_leaf=0, threads=0, collapse=0, tri_cost=0.0,
+                  builder=BSM_BUILD_DEVICE) -> BvhStats:
+        """Builds the scene's BVH, on the device by default (builder=BSM_BUILD_HOST: the host builder)."""
+        o = BvhOpts(sah_bins, max_leaf, threads, collapse, tri_cost, builder)
         s = BvhStats()
         self.check(self._L.bsm_scene_build_bvh(self.h, scene_id, C.byref(o), C.byref(s)))
         return s
 
-    def load_scene(self, scene: SceneData, collapse: int = 0) -> int:
+    def load_scene(self, scene: SceneData, collapse: int = 0, builder: int = BSM_BUILD_DEVICE) -> int:
         sid = self.upload(scene)
-        self.build_bvh(sid, collapse=collapse)
+        self.build_bvh(sid, collapse=collapse, builder=builder)
         return sid
 
     def release(self, scene_id: int):
@@ -780,13 +787,13 @@ class Context:
         for gid in self._scene_geoms.pop(scene_id, []):
             self._L.bsm_geometry_release(self.h, gid)
 
-    def create_geometry(self, g: GeometryData, sah_bins=0, max_leaf=0, threads=0) -> int:
+    def create_geometry(self, g: GeometryData, sah_bins=0, max_leaf=0, threads=0, builder=BSM_BUILD_DEVICE) -> int:
         pos = np.ascontiguousarray(g.positions, np.float32)
         idx = None if g.indices is None else np.ascontiguousarray(g.indices, np.uint32)
         mids = None if g.material_ids is None else np.ascontiguousarray(g.material_ids, np.uint32)
         d = GeometryDesc(pos.shape[0], _ptr(pos), g.num_triangles, _ptr(idx, C.c_uint32) if idx is not None else None,
                          _ptr(mids, C.c_uint32) if mids is not None else None)
-        o = BvhOpts(sah_bins, max_leaf, threads)
+        o = BvhOpts(sah_bins, max_leaf, threads, 0, 0.0, builder)
         gid = C.c_uint32()
         self.check(self._L.bsm_geometry_create(self.h, C.byref(d), C.byref(o), C.byref(gid)))
         return gid.value
@@ -957,6 +964,10 @@ class Context:
         self.check(self._L.bsm_server_poll(self.h, rid, C.byref(st)))
         return st
 
+    def cancel(self, rid: int):
+        """Cancels a request (bsm_server_cancel); its output array is not written afterwards."""
+        self.check(self._L.bsm_server_cancel(self.h, rid))
+
     def server_stats(self) -> ServerStats:
         st = ServerStats()
         self.check(self._L.bsm_server_get_stats(self.h, C.byref(st)))
@@ -968,6 +979,16 @@ class Context:
 
     def sync(self, timeout_ms: int = 0):
         self.check(self._L.bsm_sync(self.h, timeout_ms))
+
+    def set_stream(self, stream: int | None):
+        """Runs later work on a caller's cudaStream_t (an integer handle), or on the context's own stream (None)."""
+        self.check(self._L.bsm_set_stream(self.h, C.c_void_p(stream) if stream else None))
+
+    def last_stats(self) -> RenderStats:
+        """Waits for the last render issued and returns its statistics (bsm_render_stats_read)."""
+        rs = RenderStats()
+        self.check(self._L.bsm_render_stats_read(self.h, C.byref(rs)))
+        return rs
 
 
 # ------------------------------------------------------- radiance cache ----

@@ -25,6 +25,7 @@
 
 #include "bsm_pt.h"
 #include "bvh_build.h"
+#include "bvh_gpu.h"
 #include "cache_impl.h"
 #include "pt_device.h"
 #include "pt_math.cuh"
@@ -86,7 +87,14 @@ struct GraphEntry {
 
 struct bsm_context {
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;     // the context's own stream (and the one renders are captured on)
+    cudaStream_t user_stream = nullptr;  // bsm_set_stream: the caller's stream, or null
+    bool has_user_stream = false;
+    uint32_t pending_flags = 0;        // device error flags read back but not yet reported
+    uint32_t* noalloc_counters = nullptr;  // counters of the last bsm_render_noalloc call (its fixed array)
+    bsm_render_stats last_stats{};     // host-side part of the last render's statistics
+    bool last_stats_valid = false;
+    bool last_stats_timing = false;    // the last render recorded per-stage events
     uint64_t budget = 0;
     uint64_t used = 0;
     std::string err;
@@ -118,6 +126,9 @@ struct bsm_context {
 namespace {
 
 void clear_graphs(bsm_context* ctx);
+
+// The stream a context's work runs on: the caller's (bsm_set_stream) or its own.
+cudaStream_t WS(const bsm_context* ctx) { return ctx->has_user_stream ? ctx->user_stream : ctx->stream; }
 
 bsm_status fail(bsm_context* ctx, bsm_status st, const std::string& msg) {
     if (ctx) ctx->err = msg;
@@ -299,6 +310,12 @@ bsm_status ensure_wavefront(bsm_context* ctx, uint32_t capacity, uint32_t lights
     size_t o_shs = sz(sh * 4);
     size_t o_cnt = sz(kCntWords * 4), o_st = sz(kStatWords * 8);
     clear_graphs(ctx);  // graphs hold the old pointers
+    if (ctx->wf.counters) {  // keep the old buffer's error flags for the next sync point
+        uint32_t f = 0;
+        if (cudaStreamSynchronize(WS(ctx)) == cudaSuccess &&
+            cudaMemcpy(&f, ctx->wf.counters + kCntError, 4, cudaMemcpyDeviceToHost) == cudaSuccess)
+            ctx->pending_flags |= f;
+    }
     dev_free(ctx, ctx->wf_buf);
     bsm_status s = dev_alloc(ctx, ctx->wf_buf, bytes);
     if (s) { ctx->wf = Wavefront{}; return s; }
@@ -317,6 +334,41 @@ bsm_status ensure_wavefront(bsm_context* ctx, uint32_t capacity, uint32_t lights
     w.stats = (unsigned long long*)(b + o_st);
     ctx->wf_lights = lights;
     if (cudaMemset(w.counters, 0, kCntWords * 4) != cudaSuccess) return fail(ctx, BSM_ERR_CUDA, "counter clear failed");
+    return BSM_OK;
+}
+
+// Reads and clears the device error words of the context's work (its wavefront's
+// and the fixed array's of its last allocation-free render) after waiting for
+// the work stream.  A flag stays set on the device until a sync point reads it,
+// so renders queued back to back cannot hide one another's errors.
+bsm_status take_device_flags(bsm_context* ctx, uint32_t* flags) {
+    cudaStream_t st = WS(ctx);
+    CK(cudaStreamSynchronize(st));
+    uint32_t f = ctx->pending_flags;
+    ctx->pending_flags = 0;
+    uint32_t* words[2] = {ctx->wf.counters ? ctx->wf.counters + kCntError : nullptr,
+                          ctx->noalloc_counters ? ctx->noalloc_counters + kCntError : nullptr};
+    for (uint32_t* w : words) {
+        if (!w) continue;
+        uint32_t h = 0;
+        CK(cudaMemcpyAsync(&h, w, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (h) {
+            f |= h;
+            CK(cudaMemsetAsync(w, 0, 4, st));
+        }
+    }
+    CK(cudaStreamSynchronize(st));
+    *flags = f;
+    return BSM_OK;
+}
+
+// Waits for the work stream and turns set device flags into BSM_ERR_DEVICE_CHECK.
+bsm_status check_device_flags(bsm_context* ctx) {
+    uint32_t flag = 0;
+    bsm_status s = take_device_flags(ctx, &flag);
+    if (s) return s;
+    if (flag) return fail(ctx, BSM_ERR_DEVICE_CHECK, device_flag_text(flag));
     return BSM_OK;
 }
 
@@ -358,6 +410,7 @@ extern "C" void bsm_destroy(bsm_context* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->server) bsm_server_stop(ctx);
+    cudaStreamSynchronize(WS(ctx));
     cudaStreamSynchronize(ctx->stream);
     for (auto& g : ctx->graphs) if (g.exec) cudaGraphExecDestroy(g.exec);
     for (auto& kv : ctx->scenes) {
@@ -383,20 +436,36 @@ extern "C" bsm_status bsm_sync(bsm_context* ctx, uint32_t timeout_ms) {
     cudaSetDevice(ctx->device);
     auto t0 = std::chrono::steady_clock::now();
     while (true) {
-        cudaError_t e = cudaStreamQuery(ctx->stream);
+        cudaError_t e = cudaStreamQuery(WS(ctx));
         if (e == cudaSuccess) break;
         if (e != cudaErrorNotReady) return cuda_fail(ctx, e, "cudaStreamQuery");
         auto ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         if (timeout_ms && ms > timeout_ms) return fail(ctx, BSM_ERR_TIMEOUT, "bsm_sync timed out");
         std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
-    if (ctx->wf.counters) {
-        uint32_t flag = 0;
-        CK(cudaMemcpy(&flag, ctx->wf.counters + kCntError, 4, cudaMemcpyDeviceToHost));
-        if (flag) return fail(ctx, BSM_ERR_DEVICE_CHECK, device_flag_text(flag));
+    return check_device_flags(ctx);
+}
+
+extern "C" bsm_status bsm_set_stream(bsm_context* ctx, void* stream) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "the stream cannot change while the server runs");
+    cudaSetDevice(ctx->device);
+    cudaStream_t next = stream ? (cudaStream_t)stream : ctx->stream;
+    if (next != WS(ctx)) {
+        // work queued on the old stream keeps its order before work on the new one
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        cudaError_t r = cudaEventRecord(e, WS(ctx));
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(next, e, 0);
+        cudaEventDestroy(e);
+        if (r != cudaSuccess) return cuda_fail(ctx, r, "bsm_set_stream: ordering against the previous stream");
     }
+    ctx->user_stream = (cudaStream_t)stream;
+    ctx->has_user_stream = stream != nullptr;
     return BSM_OK;
 }
+
+extern "C" void* bsm_get_stream(bsm_context* ctx) { return ctx ? (void*)WS(ctx) : nullptr; }
 
 extern "C" bsm_status bsm_device_alloc(bsm_context* ctx, uint64_t bytes, void** ptr) {
     if (!ctx || !ptr) return BSM_ERR_INVALID_ARG;
@@ -416,8 +485,8 @@ extern "C" bsm_status bsm_memcpy(bsm_context* ctx, void* dst, const void* src, u
     if (!ctx) return BSM_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
     cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : kind == 1 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-    CK(cudaMemcpyAsync(dst, src, bytes, k, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpyAsync(dst, src, bytes, k, WS(ctx)));
+    CK(cudaStreamSynchronize(WS(ctx)));
     return BSM_OK;
 }
 
@@ -636,6 +705,69 @@ bsm_status setup_shading(bsm_context* ctx, Scene* sc, const bsm_material* materi
 
 }  // namespace
 
+namespace {
+
+// Builds a BVH with the device builder from host arrays: uploads them to one
+// temporary buffer, runs bvh_gpu.cu's build on the context's own stream and
+// adopts the node and triangle buffers it returns.  The scratch the build holds
+// counts against the memory budget while it runs.
+bsm_status device_bvh(bsm_context* ctx, const float* positions, uint32_t nv, const uint32_t* indices, uint32_t nt,
+                      const uint32_t* material_ids, const std::vector<float>& transparency, const bsm_bvh_opts* opts,
+                      DevBuf& nodes, DevBuf& tris, bsm_bvh_stats& s) {
+    auto a256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t b_pos = a256((size_t)nv * 12), b_idx = indices ? a256((size_t)nt * 12) : 0,
+                 b_mat = material_ids ? a256((size_t)nt * 4) : 0, b_tr = a256(transparency.size() * 4 + 4);
+    const uint64_t need = b_pos + b_idx + b_mat + b_tr + device_build_scratch_bytes(nt) + device_build_output_bytes(nt);
+    if (ctx->budget && ctx->used + need > ctx->budget)
+        return fail(ctx, BSM_ERR_OUT_OF_MEMORY, "device BVH build needs " + std::to_string(need) +
+                                                    " bytes beyond the memory budget");
+    auto t0 = std::chrono::steady_clock::now();
+    char* in = nullptr;
+    CK(cudaMalloc(&in, b_pos + b_idx + b_mat + b_tr));
+    cudaStream_t st = ctx->stream;
+    float* d_pos = (float*)in;
+    uint32_t* d_idx = indices ? (uint32_t*)(in + b_pos) : nullptr;
+    uint32_t* d_mat = material_ids ? (uint32_t*)(in + b_pos + b_idx) : nullptr;
+    float* d_tr = transparency.empty() ? nullptr : (float*)(in + b_pos + b_idx + b_mat);
+    cudaError_t e = cudaMemcpyAsync(d_pos, positions, (size_t)nv * 12, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && d_idx) e = cudaMemcpyAsync(d_idx, indices, (size_t)nt * 12, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && d_mat) e = cudaMemcpyAsync(d_mat, material_ids, (size_t)nt * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && d_tr)
+        e = cudaMemcpyAsync(d_tr, transparency.data(), transparency.size() * 4, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { cudaFree(in); return cuda_fail(ctx, e, "device BVH build: input upload"); }
+    DeviceBvhResult r;
+    std::string err;
+    bool ok = build_cwbvh_device(st, d_pos, nv, d_idx, nt, d_mat, d_tr, (uint32_t)transparency.size(), opts, r, err);
+    cudaFree(in);
+    if (!ok) return fail(ctx, BSM_ERR_INVALID_ARG, "BVH build failed: " + err);
+    if (r.max_depth > (uint32_t)kMaxTraversalDepth) {
+        cudaFree(r.nodes);
+        cudaFree(r.tris);
+        return fail(ctx, BSM_ERR_UNSUPPORTED, "BVH deeper than the traversal stack (" + std::to_string(r.max_depth) + ")");
+    }
+    dev_free(ctx, nodes);
+    dev_free(ctx, tris);
+    nodes.ptr = r.nodes;
+    nodes.bytes = (size_t)r.num_nodes * sizeof(CwNode);
+    tris.ptr = r.tris;
+    tris.bytes = (size_t)r.num_tris * sizeof(CwTri);
+    ctx->used += nodes.bytes + tris.bytes;
+    s = bsm_bvh_stats{};
+    s.num_nodes = r.num_nodes;
+    s.num_tris = r.num_tris;
+    s.max_depth = r.max_depth;
+    s.builder = BSM_BUILD_DEVICE;
+    s.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    s.sah_cost = r.sah_cost;
+    s.node_bytes = nodes.bytes;
+    s.tri_bytes = tris.bytes;
+    return BSM_OK;
+}
+
+bool use_host_builder(const bsm_bvh_opts* opts) { return opts && opts->builder == BSM_BUILD_HOST; }
+
+}  // namespace
+
 // ================================================================ scenes ====
 extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d, uint32_t* scene_id) {
     if (!ctx || !d || !scene_id) return BSM_ERR_INVALID_ARG;
@@ -692,10 +824,26 @@ extern "C" bsm_status bsm_scene_build_bvh(bsm_context* ctx, uint32_t scene_id, c
     if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
     if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
     if (sc->instanced) {  // a full rebuild of the TLAS from the current transforms
-        cudaStreamSynchronize(ctx->stream);
+        cudaStreamSynchronize(WS(ctx));
         bsm_status st = build_tlas(ctx, sc);
         if (!st && stats) *stats = sc->bvh_stats;
         return st;
+    }
+    if (opts && opts->builder > BSM_BUILD_HOST) return fail(ctx, BSM_ERR_INVALID_ARG, "unknown BVH builder");
+    if (!use_host_builder(opts)) {
+        bsm_bvh_stats s{};
+        bsm_status st = device_bvh(ctx, sc->positions.data(), (uint32_t)(sc->positions.size() / 3),
+                                   sc->indices.empty() ? nullptr : sc->indices.data(), sc->num_triangles,
+                                   sc->material_ids.empty() ? nullptr : sc->material_ids.data(), sc->transparency,
+                                   opts, sc->nodes, sc->tris, s);
+        if (st) return st;
+        sc->dev.nodes = (const CwNode*)sc->nodes.ptr;
+        sc->dev.tris = (const CwTri*)sc->tris.ptr;
+        sc->has_bvh = true;
+        sc->bvh_stats = s;
+        clear_graphs(ctx);
+        if (stats) *stats = s;
+        return BSM_OK;
     }
     BvhBuildResult r;
     std::string err;
@@ -722,6 +870,7 @@ extern "C" bsm_status bsm_scene_build_bvh(bsm_context* ctx, uint32_t scene_id, c
     s.num_nodes = (uint32_t)r.nodes.size();
     s.num_tris = (uint32_t)r.tris.size();
     s.max_depth = r.max_depth;
+    s.builder = BSM_BUILD_HOST;
     s.build_ms = r.build_ms;
     s.sah_cost = r.sah_cost;
     s.node_bytes = r.nodes.size() * sizeof(CwNode);
@@ -747,6 +896,7 @@ extern "C" bsm_status bsm_bvh_build_host(const bsm_scene_desc* d, const bsm_bvh_
     s.num_nodes = (uint32_t)r.nodes.size();
     s.num_tris = (uint32_t)r.tris.size();
     s.max_depth = r.max_depth;
+    s.builder = BSM_BUILD_HOST;
     s.build_ms = r.build_ms;
     s.sah_cost = r.sah_cost;
     s.node_bytes = r.nodes.size() * sizeof(CwNode);
@@ -769,7 +919,7 @@ extern "C" bsm_status bsm_scene_release(bsm_context* ctx, uint32_t scene_id) {
     Scene* sc = find_scene(ctx, scene_id);
     if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
     if (ctx->server) return fail(ctx, BSM_ERR_BAD_STATE, "scenes cannot change while the server runs");
-    cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(WS(ctx));
     free_scene_buffers(ctx, *sc);
     ctx->scenes.erase(scene_id);
     clear_graphs(ctx);
@@ -947,6 +1097,20 @@ extern "C" bsm_status bsm_geometry_create(bsm_context* ctx, const bsm_geometry_d
         }
     if (d->material_ids)
         for (uint32_t t = 0; t < d->num_triangles; ++t) g->max_material = std::max(g->max_material, d->material_ids[t]);
+    if (opts && opts->builder > BSM_BUILD_HOST) return fail(ctx, BSM_ERR_INVALID_ARG, "unknown BVH builder");
+    if (!use_host_builder(opts)) {
+        bsm_bvh_stats s{};
+        // the two-level stack bound below holds for any BLAS within the traversal stack
+        bsm_status st = device_bvh(ctx, d->positions, d->num_vertices, d->indices, d->num_triangles, d->material_ids,
+                                   std::vector<float>(), opts, g->nodes, g->tris, s);
+        if (st) return st;
+        g->num_triangles = d->num_triangles;
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        uint32_t id = ctx->next_geom++;
+        ctx->geoms[id] = std::move(g);
+        *geometry_id = id;
+        return BSM_OK;
+    }
     BvhBuildResult r;
     std::string err;
     if (!build_cwbvh(d->positions, d->indices, d->num_triangles, d->material_ids, opts, r, err))
@@ -1060,7 +1224,7 @@ extern "C" bsm_status bsm_scene_update_instances(bsm_context* ctx, uint32_t scen
     bool moved_bounds = extent != sc->extent;
     for (int k = 0; k < 3; ++k)
         moved_bounds = moved_bounds || ds.box_lo[k] != lo[k] || ds.box_inv[k] != 1.0f / std::max(hi[k] - lo[k], 1e-6f);
-    CK(cudaStreamSynchronize(ctx->stream));  // no render may read the records while they change
+    CK(cudaStreamSynchronize(WS(ctx)));  // no render may read the records while they change
     if (moved_bounds) {
         sc->extent = extent;
         ds.ray_offset = 2e-5f * extent;
@@ -1071,14 +1235,14 @@ extern "C" bsm_status bsm_scene_update_instances(bsm_context* ctx, uint32_t scen
         clear_graphs(ctx);  // captured launches hold the scene record by value
     }
     CK(cudaMemcpyAsync(sc->insts.ptr, sc->inst_host.data(), sc->inst_host.size() * sizeof(InstDev),
-                       cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(sc->inst_box.ptr, boxes.data(), boxes.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+                       cudaMemcpyHostToDevice, WS(ctx)));
+    CK(cudaMemcpyAsync(sc->inst_box.ptr, boxes.data(), boxes.size() * 4, cudaMemcpyHostToDevice, WS(ctx)));
     // refit bottom-up: one launch per breadth-first level, deepest first
     for (size_t lv = sc->level_begin.size() - 1; lv-- > 0;)
-        launch_tlas_refit(ctx->stream, (CwNode*)sc->nodes.ptr, (float*)sc->node_box.ptr, (const float*)sc->inst_box.ptr,
+        launch_tlas_refit(WS(ctx), (CwNode*)sc->nodes.ptr, (float*)sc->node_box.ptr, (const float*)sc->inst_box.ptr,
                           sc->level_begin[lv], sc->level_begin[lv + 1]);
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaStreamSynchronize(WS(ctx)));
     return BSM_OK;
 }
 
@@ -1121,15 +1285,15 @@ extern "C" void bsm_pt_settings_default(bsm_pt_settings* s) {
 
 namespace {
 
-// Records the launch sequence of one render (all chunks) on ctx->stream.
+// Records the launch sequence of one render (all chunks) on `st` (the capture
+// stream when a graph is being recorded, else the work stream).
 // With `ev` non-null an event is recorded after every launch (no host waits):
 // ev[0] before the first launch, then one per stage; `tags` gets the stage of
 // each interval (0 camera, 1 extend, 2 shade, 3 shadow).
-void record_render(bsm_context* ctx, const Scene* sc, uint32_t n_views, uint64_t total_paths, uint32_t capacity,
-                   uint32_t max_seg, bool count_traversal, std::vector<cudaEvent_t>* ev, std::vector<int>* tags,
-                   const void* cache_wb = nullptr) {
+void record_render(bsm_context* ctx, cudaStream_t st, const Scene* sc, uint32_t n_views, uint64_t total_paths,
+                   uint32_t capacity, uint32_t max_seg, bool count_traversal, std::vector<cudaEvent_t>* ev,
+                   std::vector<int>* tags, const void* cache_wb = nullptr) {
     const LaunchCfg& lc = ctx->lc;
-    cudaStream_t st = ctx->stream;
     const DevView* views = (const DevView*)ctx->views_dev.ptr;
     float4* accum = (float4*)ctx->accum.ptr;
     size_t k = 0;
@@ -1169,6 +1333,29 @@ void record_render(bsm_context* ctx, const Scene* sc, uint32_t n_views, uint64_t
 
 namespace {
 
+// Statistics of the last render issued on the context, once its work is done:
+// the host-side part kept at issue time plus the device's ray counters and the
+// device time between the render's two events.
+bsm_status read_last_stats(bsm_context* ctx, bsm_render_stats* out) {
+    CK(cudaEventSynchronize(ctx->ev[9]));
+    unsigned long long h[kStatWords];
+    CK(cudaMemcpyAsync(h, ctx->wf.stats, sizeof(h), cudaMemcpyDeviceToHost, WS(ctx)));
+    CK(cudaStreamSynchronize(WS(ctx)));
+    *out = ctx->last_stats;
+    out->extend_rays = out->shadow_rays = 0;
+    for (uint32_t k = 0; k < (uint32_t)kMaxSeg; ++k) {
+        out->rays_per_segment[k] = h[kStatExtend + k];
+        out->extend_rays += h[kStatExtend + k];
+        out->shadow_rays += h[kStatShadow + k];
+    }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev[8], ctx->ev[9]);
+    out->ms_total = ms;
+    out->traversal_nodes = h[kStatNodes];
+    out->traversal_tris = h[kStatTris];
+    return BSM_OK;
+}
+
 // One view of a render call: camera plus the per-view sample count, segment
 // limit and seed (uniform for bsm_render, per view for bsm_render_batch).
 struct ViewReq {
@@ -1180,7 +1367,7 @@ struct ViewReq {
 
 bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<ViewReq>& req,
                        const bsm_pt_settings& s, const bsm_view_output* outputs, bsm_render_stats* stats,
-                       const void* cache_wb = nullptr, uint32_t cache_seg = 0) {
+                       const void* cache_wb = nullptr, uint32_t cache_seg = 0, float cache_rough = 0.0f) {
     const uint32_t n_views = (uint32_t)req.size();
     cudaSetDevice(ctx->device);
     Scene* sc = find_scene(ctx, scene_id);
@@ -1219,10 +1406,10 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
     if (total_px >= (1ull << 32)) return fail(ctx, BSM_ERR_INVALID_ARG, "too many pixels in one call");
     if (n_views > 65535) return fail(ctx, BSM_ERR_INVALID_ARG, "at most 65535 views per call");
     if (relayout) {
-        cudaStreamSynchronize(ctx->stream);
+        cudaStreamSynchronize(WS(ctx));
         clear_graphs(ctx);
         if ((st = dev_alloc(ctx, ctx->accum, total_px * sizeof(float4)))) return st;
-        CK(cudaMemsetAsync(ctx->accum.ptr, 0, total_px * sizeof(float4), ctx->stream));
+        CK(cudaMemsetAsync(ctx->accum.ptr, 0, total_px * sizeof(float4), WS(ctx)));
         ctx->layout.assign(n_views, {0, 0});
         ctx->hist.assign(n_views, ViewHist{});
         uint32_t base = 0;
@@ -1239,7 +1426,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         bool reset = !s.accumulate || !h.valid || !same_camera(h.cam, views[v]);
         if (reset) {
             CK(cudaMemsetAsync((float4*)ctx->accum.ptr + h.accum_base, 0,
-                               (size_t)views[v].width * views[v].height * sizeof(float4), ctx->stream));
+                               (size_t)views[v].width * views[v].height * sizeof(float4), WS(ctx)));
             h.spp = 0;
             h.cam = views[v];
             h.valid = true;
@@ -1257,6 +1444,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         dv.max_segments = req[v].max_seg;
         dv.flags = s.flags;
         dv.cache_segment = cache_wb ? cache_seg : 0u;
+        dv.cache_min_rough = cache_wb ? cache_rough : 0.0f;
         total_paths += (uint64_t)views[v].width * views[v].height * req[v].spp;
     }
     uint32_t cap_req = s.wavefront_capacity ? s.wavefront_capacity : (sc->tuned ? sc->tune.wavefront_capacity : 0u);
@@ -1266,16 +1454,15 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
     capacity = std::min(capacity, ctx->wf.capacity);
     if ((st = dev_alloc(ctx, ctx->views_dev, n_views * sizeof(DevView)))) return st;
     CK(cudaMemcpyAsync(ctx->views_dev.ptr, ctx->views_host.data(), n_views * sizeof(DevView), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    CK(cudaMemsetAsync(ctx->wf.stats, 0, kStatWords * 8, ctx->stream));
-    CK(cudaMemsetAsync(ctx->wf.counters + kCntError, 0, 4, ctx->stream));
+                       WS(ctx)));
+    CK(cudaMemsetAsync(ctx->wf.stats, 0, kStatWords * 8, WS(ctx)));
 
     bool timing = (s.flags & BSM_PT_STAGE_TIMING) != 0;
     bool counting = (s.flags & BSM_PT_COUNT_TRAVERSAL) != 0;
     bool use_graph = !timing && !counting && !(s.flags & BSM_PT_NO_GRAPH);
     float stage_ms[4] = {0, 0, 0, 0};
     std::vector<int> tags;
-    CK(cudaEventRecord(ctx->ev[8], ctx->stream));
+    CK(cudaEventRecord(ctx->ev[8], WS(ctx)));
     if (use_graph) {
         // key: everything the recorded launches depend on
         std::vector<uint8_t> key(64);
@@ -1290,7 +1477,8 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         if (!exec) {
             cudaGraph_t graph;
             CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-            record_render(ctx, sc, n_views, total_paths, capacity, max_seg, false, nullptr, nullptr, cache_wb);
+            record_render(ctx, ctx->stream, sc, n_views, total_paths, capacity, max_seg, false, nullptr, nullptr,
+                          cache_wb);
             CK(cudaStreamEndCapture(ctx->stream, &graph));
             CK(cudaGraphInstantiate(&exec, graph, 0));
             cudaGraphDestroy(graph);
@@ -1300,13 +1488,13 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
             }
             ctx->graphs.push_back({exec, key});
         }
-        CK(cudaGraphLaunch(exec, ctx->stream));
+        CK(cudaGraphLaunch(exec, WS(ctx)));
     } else {
-        record_render(ctx, sc, n_views, total_paths, capacity, max_seg, counting, timing ? &ctx->stage_ev : nullptr,
-                      &tags, cache_wb);
+        record_render(ctx, WS(ctx), sc, n_views, total_paths, capacity, max_seg, counting,
+                      timing ? &ctx->stage_ev : nullptr, &tags, cache_wb);
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(ctx->ev[9], ctx->stream));
+    CK(cudaEventRecord(ctx->ev[9], WS(ctx)));
     for (uint32_t v = 0; v < n_views; ++v) ctx->hist[v].spp += req[v].spp;
 
     // outputs: running mean
@@ -1321,53 +1509,42 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
             float inv = 1.0f / (float)ctx->hist[v].spp;
             const float4* acc = (const float4*)ctx->accum.ptr + ctx->hist[v].accum_base;
             if (o.location == BSM_DEVICE) {
-                launch_resolve(ctx->stream, acc, W, H, inv, (float4*)o.rgba, pitch);
+                launch_resolve(WS(ctx), acc, W, H, inv, (float4*)o.rgba, pitch);
             } else {
                 if ((st = dev_alloc(ctx, ctx->out_stage, (size_t)W * H * sizeof(float4)))) return st;
-                launch_resolve(ctx->stream, acc, W, H, inv, (float4*)ctx->out_stage.ptr, W);
+                launch_resolve(WS(ctx), acc, W, H, inv, (float4*)ctx->out_stage.ptr, W);
                 CK(cudaMemcpy2DAsync(o.rgba, (size_t)pitch * 16, ctx->out_stage.ptr, (size_t)W * 16, (size_t)W * 16, H,
-                                     cudaMemcpyDeviceToHost, ctx->stream));
+                                     cudaMemcpyDeviceToHost, WS(ctx)));
                 host_out = true;
             }
         }
         CK(cudaGetLastError());
     }
+    // host-side statistics of this render; the device counts stay on the device until a read
+    bsm_render_stats& ls = ctx->last_stats;
+    std::memset(&ls, 0, sizeof(ls));
+    ls.paths = total_paths;
+    ls.chunks = (uint32_t)((total_paths + capacity - 1) / capacity);
+    ls.extend_launches = ls.chunks * max_seg;
+    ctx->last_stats_valid = true;
+    ctx->last_stats_timing = timing;
     if (timing) {
-        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaStreamSynchronize(WS(ctx)));
         for (size_t i = 0; i < tags.size(); ++i) {
             float ms = 0.0f;
             cudaEventElapsedTime(&ms, ctx->stage_ev[i], ctx->stage_ev[i + 1]);
             stage_ms[tags[i]] += ms;
         }
+        ls.ms_camera = stage_ms[0];
+        ls.ms_extend = stage_ms[1];
+        ls.ms_shade = stage_ms[2];
+        ls.ms_shadow = stage_ms[3];
     }
-    if (host_out || stats) {
-        CK(cudaStreamSynchronize(ctx->stream));
-        uint32_t flag = 0;
-        CK(cudaMemcpy(&flag, ctx->wf.counters + kCntError, 4, cudaMemcpyDeviceToHost));
-        if (flag) return fail(ctx, BSM_ERR_DEVICE_CHECK, device_flag_text(flag));
-    }
-    if (stats) {
-        unsigned long long h[kStatWords];
-        CK(cudaMemcpy(h, ctx->wf.stats, sizeof(h), cudaMemcpyDeviceToHost));
-        std::memset(stats, 0, sizeof(*stats));
-        stats->paths = total_paths;
-        for (uint32_t k = 0; k < (uint32_t)kMaxSeg; ++k) {
-            stats->rays_per_segment[k] = h[kStatExtend + k];
-            stats->extend_rays += h[kStatExtend + k];
-            stats->shadow_rays += h[kStatShadow + k];
-        }
-        stats->chunks = (uint32_t)((total_paths + capacity - 1) / capacity);
-        stats->extend_launches = stats->chunks * max_seg;
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, ctx->ev[8], ctx->ev[9]);
-        stats->ms_total = ms;
-        stats->ms_camera = stage_ms[0];
-        stats->ms_extend = stage_ms[1];
-        stats->ms_shade = stage_ms[2];
-        stats->ms_shadow = stage_ms[3];
-        stats->traversal_nodes = h[kStatNodes];
-        stats->traversal_tris = h[kStatTris];
-    }
+    // Device outputs and no statistics: the call returns with the work queued on the work stream
+    // (bsm_sync / bsm_render_stats_read wait for it and report the device error flags).
+    if (!host_out && !stats && !timing) return BSM_OK;
+    if ((st = check_device_flags(ctx))) return st;
+    if (stats) return read_last_stats(ctx, stats);
     return BSM_OK;
 }
 
@@ -1383,6 +1560,15 @@ extern "C" bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_
     std::vector<ViewReq> req(n_views);
     for (uint32_t v = 0; v < n_views; ++v) req[v] = ViewReq{views[v], s.spp, max_seg, s.seed};
     return render_impl(ctx, scene_id, req, s, outputs, stats);
+}
+
+extern "C" bsm_status bsm_render_stats_read(bsm_context* ctx, bsm_render_stats* stats) {
+    if (!ctx || !stats) return BSM_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (!ctx->last_stats_valid || !ctx->wf.stats) return fail(ctx, BSM_ERR_NOT_FOUND, "no render issued yet");
+    bsm_status st = check_device_flags(ctx);
+    if (st) return st;
+    return read_last_stats(ctx, stats);
 }
 
 extern "C" bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, const bsm_camera* cam,
@@ -1407,12 +1593,15 @@ extern "C" bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, con
         dv.t_min = settings->t_min;
         dv.seed = settings->seed;
         dv.max_segments = std::min(std::max(cs.train_segments, 1u), 16u);
-        bsm_status e = cache_train_frame(cache, sc->dev, dv, cs, ctx->lc, ctx->stream, train_loss, nullptr);
+        bsm_status e = cache_train_frame(cache, sc->dev, dv, cs, ctx->lc, WS(ctx), train_loss, nullptr);
         if (e) return fail(ctx, e, "radiance-cache training failed");
     }
     std::vector<ViewReq> req(1);
-    req[0] = ViewReq{*cam, settings->spp, cs.cache_segment + 1, settings->seed};
-    return render_impl(ctx, scene_id, req, *settings, output, stats, cache_render_weights(cache), cs.cache_segment);
+    if (!(cs.min_roughness >= 0.0f) || cs.cache_segment + 1 + cs.extra_segments > (uint32_t)kMaxSeg)
+        return fail(ctx, BSM_ERR_INVALID_ARG, "min_roughness must be >= 0 and cache_segment + extra_segments <= 15");
+    req[0] = ViewReq{*cam, settings->spp, cs.cache_segment + 1 + cs.extra_segments, settings->seed};
+    return render_impl(ctx, scene_id, req, *settings, output, stats, cache_render_weights(cache), cs.cache_segment,
+                       cs.extra_segments ? cs.min_roughness : 0.0f);
 }
 
 extern "C" bsm_status bsm_render_batch(bsm_context* ctx, uint32_t scene_id, const bsm_view_desc* views,
@@ -1586,16 +1775,16 @@ extern "C" bsm_status bsm_read_view(bsm_context* ctx, uint32_t view_index, const
     const float4* acc = (const float4*)ctx->accum.ptr + h.accum_base;
     float inv = 1.0f / (float)h.spp;
     if (o->location == BSM_DEVICE) {
-        launch_resolve(ctx->stream, acc, W, H, inv, (float4*)o->rgba, pitch);
+        launch_resolve(WS(ctx), acc, W, H, inv, (float4*)o->rgba, pitch);
         CK(cudaGetLastError());
         return BSM_OK;
     }
     bsm_status st;
     if ((st = dev_alloc(ctx, ctx->out_stage, (size_t)W * H * sizeof(float4)))) return st;
-    launch_resolve(ctx->stream, acc, W, H, inv, (float4*)ctx->out_stage.ptr, W);
+    launch_resolve(WS(ctx), acc, W, H, inv, (float4*)ctx->out_stage.ptr, W);
     CK(cudaMemcpy2DAsync(o->rgba, (size_t)pitch * 16, ctx->out_stage.ptr, (size_t)W * 16, (size_t)W * 16, H,
-                         cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+                         cudaMemcpyDeviceToHost, WS(ctx)));
+    CK(cudaStreamSynchronize(WS(ctx)));
     return BSM_OK;
 }
 
@@ -1608,8 +1797,8 @@ extern "C" bsm_status bsm_export_history(bsm_context* ctx, uint32_t view_index, 
     const ViewHist& h = ctx->hist[view_index];
     size_t bytes = (size_t)ctx->layout[view_index].first * ctx->layout[view_index].second * sizeof(float4);
     CK(cudaMemcpyAsync(sums, (float4*)ctx->accum.ptr + h.accum_base, bytes,
-                       location == BSM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+                       location == BSM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, WS(ctx)));
+    CK(cudaStreamSynchronize(WS(ctx)));
     *spp = h.spp;
     return BSM_OK;
 }
@@ -1624,8 +1813,8 @@ extern "C" bsm_status bsm_import_history(bsm_context* ctx, uint32_t view_index, 
     ViewHist& h = ctx->hist[view_index];
     size_t bytes = (size_t)cam->width * cam->height * sizeof(float4);
     CK(cudaMemcpyAsync((float4*)ctx->accum.ptr + h.accum_base, sums, bytes,
-                       location == BSM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+                       location == BSM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, WS(ctx)));
+    CK(cudaStreamSynchronize(WS(ctx)));
     h.cam = *cam;
     h.spp = spp;
     h.valid = true;
@@ -1653,19 +1842,18 @@ extern "C" bsm_status bsm_trace_closest(bsm_context* ctx, uint32_t scene_id, con
     if (n == 0) return BSM_OK;
     if (!rays || !hits) return BSM_ERR_INVALID_ARG;
     if (location == BSM_DEVICE) {
-        launch_trace_closest(ctx->stream, sc->dev, (const float4*)rays, n, (uint4*)hits, 128);
+        launch_trace_closest(WS(ctx), sc->dev, (const float4*)rays, n, (uint4*)hits, 128);
         CK(cudaGetLastError());
-        CK(cudaStreamSynchronize(ctx->stream));
-        return BSM_OK;
+        return BSM_OK;   // queued on the work stream
     }
     size_t rb = (size_t)n * 32, hb = (size_t)n * 16;
     if ((st = dev_alloc(ctx, ctx->tmp, rb + hb))) return st;
     char* b = (char*)ctx->tmp.ptr;
-    CK(cudaMemcpyAsync(b, rays, rb, cudaMemcpyHostToDevice, ctx->stream));
-    launch_trace_closest(ctx->stream, sc->dev, (const float4*)b, n, (uint4*)(b + rb), 128);
+    CK(cudaMemcpyAsync(b, rays, rb, cudaMemcpyHostToDevice, WS(ctx)));
+    launch_trace_closest(WS(ctx), sc->dev, (const float4*)b, n, (uint4*)(b + rb), 128);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(hits, b + rb, hb, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpyAsync(hits, b + rb, hb, cudaMemcpyDeviceToHost, WS(ctx)));
+    CK(cudaStreamSynchronize(WS(ctx)));
     return BSM_OK;
 }
 
@@ -1677,19 +1865,18 @@ extern "C" bsm_status bsm_trace_any(bsm_context* ctx, uint32_t scene_id, const f
     if (n == 0) return BSM_OK;
     if (!rays || !occluded) return BSM_ERR_INVALID_ARG;
     if (location == BSM_DEVICE) {
-        launch_trace_any(ctx->stream, sc->dev, (const float4*)rays, n, occluded, 128);
+        launch_trace_any(WS(ctx), sc->dev, (const float4*)rays, n, occluded, 128);
         CK(cudaGetLastError());
-        CK(cudaStreamSynchronize(ctx->stream));
-        return BSM_OK;
+        return BSM_OK;   // queued on the work stream
     }
     size_t rb = (size_t)n * 32;
     if ((st = dev_alloc(ctx, ctx->tmp, rb + n + 16))) return st;
     char* b = (char*)ctx->tmp.ptr;
-    CK(cudaMemcpyAsync(b, rays, rb, cudaMemcpyHostToDevice, ctx->stream));
-    launch_trace_any(ctx->stream, sc->dev, (const float4*)b, n, (uint8_t*)(b + rb), 128);
+    CK(cudaMemcpyAsync(b, rays, rb, cudaMemcpyHostToDevice, WS(ctx)));
+    launch_trace_any(WS(ctx), sc->dev, (const float4*)b, n, (uint8_t*)(b + rb), 128);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(occluded, b + rb, n, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpyAsync(occluded, b + rb, n, cudaMemcpyDeviceToHost, WS(ctx)));
+    CK(cudaStreamSynchronize(WS(ctx)));
     return BSM_OK;
 }
 
@@ -1705,11 +1892,11 @@ extern "C" bsm_status bsm_trace_counts(bsm_context* ctx, uint32_t scene_id, cons
     size_t rb = (size_t)n * 32, cb = (size_t)n * 8;
     if ((st = dev_alloc(ctx, ctx->tmp, rb + cb))) return st;
     char* b = (char*)ctx->tmp.ptr;
-    CK(cudaMemcpyAsync(b, rays, rb, cudaMemcpyHostToDevice, ctx->stream));
-    launch_trace_count(ctx->stream, sc->dev, (const float4*)b, n, (uint2*)(b + rb));
+    CK(cudaMemcpyAsync(b, rays, rb, cudaMemcpyHostToDevice, WS(ctx)));
+    launch_trace_count(WS(ctx), sc->dev, (const float4*)b, n, (uint2*)(b + rb));
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(counts, b + rb, cb, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpyAsync(counts, b + rb, cb, cudaMemcpyDeviceToHost, WS(ctx)));
+    CK(cudaStreamSynchronize(WS(ctx)));
     return BSM_OK;
 }
 
@@ -1759,12 +1946,12 @@ extern "C" bsm_status bsm_render_primary(bsm_context* ctx, uint32_t scene_id, co
             if (dst[k]) { dev[k] = (float*)b; b += bytes[k]; }
     }
     float4* gb[4] = {(float4*)dev[1], (float4*)dev[2], (float4*)dev[3], (float4*)dev[4]};
-    launch_primary(ctx->stream, sc->dev, v, near_z, far_z, dev[0], gb, (float4*)dev[5]);
+    launch_primary(WS(ctx), sc->dev, v, near_z, far_z, dev[0], gb, (float4*)dev[5]);
     CK(cudaGetLastError());
-    if (out->location == BSM_HOST)
-        for (int k = 0; k < 6; ++k)
-            if (dst[k]) CK(cudaMemcpyAsync(dst[k], dev[k], bytes[k], cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    if (out->location == BSM_DEVICE) return BSM_OK;   // queued on the work stream
+    for (int k = 0; k < 6; ++k)
+        if (dst[k]) CK(cudaMemcpyAsync(dst[k], dev[k], bytes[k], cudaMemcpyDeviceToHost, WS(ctx)));
+    CK(cudaStreamSynchronize(WS(ctx)));
     return BSM_OK;
 }
 
@@ -1777,7 +1964,8 @@ bool ctx_scene(bsm_context* ctx, uint32_t scene_id, DevScene* out) {
     *out = sc->dev;
     return true;
 }
-cudaStream_t ctx_stream(bsm_context* ctx) { return ctx->stream; }
+cudaStream_t ctx_stream(bsm_context* ctx) { return WS(ctx); }
+void ctx_note_noalloc(bsm_context* ctx, uint32_t* counters) { ctx->noalloc_counters = counters; }
 int ctx_device(bsm_context* ctx) { return ctx->device; }
 void ctx_set_error(bsm_context* ctx, const char* msg) { ctx->err = msg; }
 void ctx_make_view(const bsm_camera* c, DevView* v) { make_view(*c, *v); }

@@ -52,6 +52,8 @@ extern "C" void bsm_cache_settings_default(bsm_cache_settings* cs) {
     cs->train_steps = 4;
     cs->lr = 1e-2f;
     cs->ema_decay = 0.99f;
+    cs->min_roughness = 0.0f;
+    cs->extra_segments = 0;
 }
 
 extern "C" uint32_t bsm_cache_param_count(void) { return (uint32_t)kMlpParams; }

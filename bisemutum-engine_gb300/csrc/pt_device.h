@@ -76,6 +76,8 @@ struct DevView {
     uint32_t flags;            // BSM_PT_* bits that reach the device
     uint32_t cache_segment;    // >0: hits of this segment query the radiance cache instead of shading
     uint64_t first_path;       // index (within the view) of the path at path_base; >0 when a view is split
+    float cache_min_rough;     // hits smoother than this do not query the cache (but the last segment's do)
+    uint32_t pad;
 };
 
 // counters[] word offsets
@@ -187,7 +189,10 @@ struct bsm_camera;
 namespace bsm {
 // Context internals for entry points defined outside api.cpp.
 bool ctx_scene(bsm_context* ctx, uint32_t scene_id, DevScene* out);
-cudaStream_t ctx_stream(bsm_context* ctx);
+cudaStream_t ctx_stream(bsm_context* ctx);   // the work stream (the caller's after bsm_set_stream)
+// Records where an allocation-free render keeps its counters, so that the context's sync points read
+// and clear that call's device error word too.
+void ctx_note_noalloc(bsm_context* ctx, uint32_t* counters);
 int ctx_device(bsm_context* ctx);
 void ctx_set_error(bsm_context* ctx, const char* msg);
 void ctx_make_view(const bsm_camera* c, DevView* v);

@@ -247,11 +247,13 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
         uint32_t vflags = 0;
         uint32_t stream = 0;
         uint32_t cache_seg = 0;
+        float cache_rough = 0.0f;
         if (active) {
             const DevView& v = views[view_id];
             vflags = v.flags;
             stream = m4.x - v.accum_base;
             cache_seg = v.cache_segment;
+            cache_rough = v.cache_min_rough;
         }
         sky_nee = (vflags & BSM_PT_NO_SKY_NEE) == 0u;
         if (active && !is_hit) {
@@ -294,9 +296,10 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
             u_sky0 = pcg_uniform(g); u_sky1 = pcg_uniform(g); u_sky2 = pcg_uniform(g); u_lobe = pcg_uniform(g);
             u_b0 = pcg_uniform(g); u_b1 = pcg_uniform(g);
         }
-        // radiance cache: a hit of the cache segment becomes a query (NRC-style
-        // termination) — the cache's prediction includes the direct light there
-        bool cache_q = kGeneral && is_hit && cache_seg != 0u && segi == cache_seg;
+        // radiance cache: a hit of the cache segment (or a later one, when the earlier hits were too smooth)
+        // becomes a query (NRC-style termination) — the cache's prediction includes the direct light there
+        bool cache_q = kGeneral && is_hit && cache_seg != 0u && segi >= cache_seg &&
+                       (surf.roughness >= cache_rough || segi + 1u >= maxseg);
         {
             uint32_t slot = warp_alloc(cache_q, wf.counters + kCntCache);
             if (cache_q) {

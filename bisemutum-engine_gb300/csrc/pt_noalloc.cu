@@ -68,6 +68,9 @@ __global__ void k_noalloc_mean(float4* acc, uint32_t n, float inv_spp) {
 
 // Scratch layout: counters | stats | view record | wavefront arrays.
 constexpr size_t kHeaderBytes = 3 * 256 + 2048;
+constexpr size_t align256c(size_t x) { return (x + 255) & ~(size_t)255; }
+static_assert(align256c(kCntWords * 4) + align256c(kStatWords * 8) + align256c(sizeof(DevView)) <= kHeaderBytes,
+              "the counters, statistics and view record must fit the scratch header");
 
 // 9 float4 path arrays, 3 float4 per shadow slot, and a 4-byte opacity seed per
 // shadow slot for scenes with non-opaque triangles
@@ -89,6 +92,14 @@ using namespace bsm;
 extern "C" bsm_status bsm_render_noalloc(bsm_context* ctx, uint32_t scene_id, const bsm_camera* cam,
                                          const bsm_pt_settings* s, float* out_rgba) {
     if (!ctx || !cam || !s || !out_rgba) return BSM_ERR_INVALID_ARG;
+    if (((uintptr_t)out_rgba & 15u) != 0u) {  // read and written as float4
+        ctx_set_error(ctx, "bsm_render_noalloc: out_rgba must be 16-byte aligned");
+        return BSM_ERR_INVALID_ARG;
+    }
+    if (s->block_size != 0 && s->block_size != 64 && s->block_size != 128 && s->block_size != 256) {
+        ctx_set_error(ctx, "bsm_render_noalloc: block_size must be 0, 64, 128 or 256");
+        return BSM_ERR_INVALID_ARG;
+    }
     int dev = ctx_device(ctx);
     if (dev < 0 || dev >= kMaxDevices) return BSM_ERR_INVALID_ARG;
     if (cudaSetDevice(dev) != cudaSuccess) return BSM_ERR_CUDA;
@@ -184,7 +195,10 @@ extern "C" bsm_status bsm_render_noalloc(bsm_context* ctx, uint32_t scene_id, co
     NA_CK(cudaMemcpyAsync(view_dev, &dv, sizeof(dv), cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemsetAsync(out_rgba, 0, npix * 16, st));
     NA_CK(cudaMemsetAsync(wf.stats, 0, kStatWords * 8, st));
-    NA_CK(cudaMemsetAsync(wf.counters, 0, kCntWords * 4, st));
+    // the error word (kCntError) is not cleared here: it keeps a flag until a sync point of the context
+    // (bsm_sync, bsm_render_stats_read) reads and clears it
+    NA_CK(cudaMemsetAsync(wf.counters, 0, kCntError * 4, st));
+    ctx_note_noalloc(ctx, wf.counters);
     for (uint64_t begin = 0; begin < total; begin += capacity) {
         uint32_t count = (uint32_t)std::min<uint64_t>(capacity, total - begin);
         NA_CK(cudaMemsetAsync(wf.counters, 0, kCntError * 4, st));

@@ -54,6 +54,7 @@ struct Request {
     uint64_t accum_len = 0;
     double submit_ms = 0, admit_ms = 0, done_ms = 0;
     bool finishing = false;
+    bool cancelled = false;      // bsm_server_cancel: no more paths are issued, no output is written
     cudaEvent_t fin_ev = nullptr;
     cudaEvent_t zero_ev = nullptr;   // accumulator cleared (recorded on the admission stream)
     int fin_lane = -1;
@@ -163,7 +164,7 @@ uint32_t build_chunk_locked(Server& S, Lane& lane, uint32_t* rr_scene) {
     uint32_t scene = 0;
     uint32_t best_after = 0xffffffffu, best_any = 0xffffffffu;
     for (Request* r : S.active) {
-        if (r->issued >= r->total_paths) continue;
+        if (r->issued >= r->total_paths || r->cancelled) continue;
         uint32_t sid = r->r.scene_id;
         if (sid > *rr_scene && sid < best_after) best_after = sid;
         if (sid < best_any) best_any = sid;
@@ -173,7 +174,7 @@ uint32_t build_chunk_locked(Server& S, Lane& lane, uint32_t* rr_scene) {
     *rr_scene = scene;
     uint32_t left = S.opts.chunk_paths;
     for (Request* r : S.active) {
-        if (r->r.scene_id != scene || r->issued >= r->total_paths) continue;
+        if (r->r.scene_id != scene || r->issued >= r->total_paths || r->cancelled) continue;
         if (lane.ranges.size() >= S.opts.max_views_per_chunk || left == 0) break;
         uint64_t n = std::min<uint64_t>(left, r->total_paths - r->issued);
         lane.ranges.push_back(Range{r, r->issued, (uint32_t)n});
@@ -263,7 +264,7 @@ void worker_main(Server* Sp) {
             // a finished request resolves on this (now idle) lane
             for (const Range& rg : lane.ranges) {
                 Request* r = rg.req;
-                if (r->done == r->total_paths && !r->finishing) finish_request(S, lane, r);
+                if (r->done == r->total_paths && !r->finishing && !r->cancelled) finish_request(S, lane, r);
             }
             lane.ranges.clear();
         }
@@ -272,6 +273,18 @@ void worker_main(Server* Sp) {
             // finished outputs
             for (size_t i = 0; i < S.active.size();) {
                 Request* r = S.active[i];
+                if (r->cancelled && !r->finishing && r->done == r->issued) {
+                    // no chunk of it is in flight any more: its accumulator goes back to the pool
+                    if (r->zero_ev) { cudaEventSynchronize(r->zero_ev); cudaEventDestroy(r->zero_ev); }
+                    r->zero_ev = nullptr;
+                    r->done_ms = S.now_ms();
+                    r->state = BSM_REQ_CANCELLED;
+                    S.pool.release(r->accum_off, r->accum_len);
+                    S.stats.cancelled++;
+                    S.active.erase(S.active.begin() + i);
+                    did = true;
+                    continue;
+                }
                 if (r->finishing && cudaEventQuery(r->fin_ev) == cudaSuccess) {
                     cudaEventDestroy(r->fin_ev);
                     r->fin_ev = nullptr;
@@ -431,8 +444,8 @@ extern "C" bsm_status bsm_server_submit(bsm_context* ctx, const bsm_request* r, 
 }
 
 static void fill_status(const Request* r, bsm_request_status* st) {
+    st->cancelled = r->cancelled ? 1u : 0u;
     st->state = r->state;
-    st->reserved = 0;
     st->submit_ms = r->submit_ms;
     st->admit_ms = r->admit_ms;
     st->done_ms = r->done_ms;
@@ -458,7 +471,9 @@ extern "C" bsm_status bsm_server_wait(bsm_context* ctx, uint64_t id, uint32_t ti
     auto it = S->all.find(id);
     if (it == S->all.end()) return BSM_ERR_NOT_FOUND;
     Request* r = it->second.get();
-    auto pred = [&] { return r->state == BSM_REQ_DONE || r->state == BSM_REQ_FAILED; };
+    auto pred = [&] {
+        return r->state == BSM_REQ_DONE || r->state == BSM_REQ_FAILED || r->state == BSM_REQ_CANCELLED;
+    };
     if (timeout_ms) {
         if (!S->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) {
             fill_status(r, st);
@@ -468,7 +483,38 @@ extern "C" bsm_status bsm_server_wait(bsm_context* ctx, uint64_t id, uint32_t ti
         S->cv.wait(lk, pred);
     }
     fill_status(r, st);
+    if (r->state == BSM_REQ_CANCELLED) return BSM_ERR_CANCELLED;
     return r->state == BSM_REQ_DONE ? BSM_OK : BSM_ERR_CUDA;
+}
+
+extern "C" bsm_status bsm_server_cancel(bsm_context* ctx, uint64_t id) {
+    if (!ctx) return BSM_ERR_INVALID_ARG;
+    Server* S = get(ctx);
+    if (!S) return BSM_ERR_BAD_STATE;
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->all.find(id);
+    if (it == S->all.end()) return BSM_ERR_NOT_FOUND;
+    Request* r = it->second.get();
+    if (r->state == BSM_REQ_QUEUED) {   // never admitted: nothing of it is on the device
+        S->queued.erase(std::find(S->queued.begin(), S->queued.end(), r));
+        r->cancelled = true;
+        r->state = BSM_REQ_CANCELLED;
+        r->done_ms = S->now_ms();
+        S->stats.cancelled++;
+    } else if (r->state == BSM_REQ_RUNNING) {
+        if (r->finishing) {
+            // its output copy is already queued: let it land before returning, so that the library
+            // writes nothing into out_rgba after this call; the request completes normally
+            cudaEvent_t e = r->fin_ev;
+            lk.unlock();
+            cudaSetDevice(S->device);
+            cudaEventSynchronize(e);
+            return BSM_OK;
+        }
+        r->cancelled = true;   // the worker releases it when its chunks in flight are done
+    }
+    S->cv.notify_all();
+    return BSM_OK;
 }
 
 extern "C" bsm_status bsm_server_get_stats(bsm_context* ctx, bsm_server_stats* out) {

@@ -29,6 +29,16 @@
  *     buffer lives in host memory (BSM_HOST) or device memory (BSM_DEVICE).
  *   - One context per host thread.  Calls on one context are serialised by the
  *     caller; the serving entry points (bsm_server_*) take an internal lock.
+ *   - Work runs on the context's stream, or on the caller's stream after
+ *     bsm_set_stream.  Calls whose results stay on the device (renders to device
+ *     outputs or to the view history, device-located traces, primary outputs on
+ *     the device) return with their kernels queued, as the reference's pass only
+ *     records work that runs later in RenderGraph::execute
+ *     (bisemutum/src/graphics/graphics_manager.cpp:418-419).  Calls that hand a
+ *     result to host memory wait for it.  Kernels report overflows and timed-out
+ *     waits in a device error word that stays set until a sync point
+ *     (bsm_sync, bsm_render_stats_read, or a call that waits) reads it and
+ *     returns BSM_ERR_DEVICE_CHECK.
  *   - Scene data passed to bsm_scene_upload is copied; the caller may free its
  *     buffers when the call returns.
  */
@@ -62,7 +72,8 @@ enum {
     BSM_ERR_NO_DEVICE = -7,
     BSM_ERR_UNSUPPORTED = -8,
     BSM_ERR_DEVICE_CHECK = -9,   /* a kernel's own bounds/overflow check or bounded wait fired */
-    BSM_ERR_ADMISSION = -10      /* serving: request does not fit the memory budget */
+    BSM_ERR_ADMISSION = -10,     /* serving: request does not fit the memory budget */
+    BSM_ERR_CANCELLED = -11      /* serving: the request was cancelled (bsm_server_cancel) */
 };
 
 enum { BSM_HOST = 0, BSM_DEVICE = 1 };
@@ -79,8 +90,21 @@ BSM_API bsm_status bsm_create(bsm_context** ctx, int device_ordinal, uint64_t me
 BSM_API void bsm_destroy(bsm_context* ctx);
 BSM_API const char* bsm_last_error(const bsm_context* ctx);
 BSM_API int bsm_api_version(void);
-/* Waits for all work on the context's streams; BSM_ERR_TIMEOUT after timeout_ms. */
+/* Waits for all work on the context's work stream (timeout_ms = 0: no limit;
+ * BSM_ERR_TIMEOUT when the limit runs out, the work keeps running), then reads
+ * and clears the device error word: BSM_ERR_DEVICE_CHECK if a kernel's check
+ * fired since the last sync point. */
 BSM_API bsm_status bsm_sync(bsm_context* ctx, uint32_t timeout_ms);
+/* Runs the context's later work on `stream` (a cudaStream_t of the context's
+ * device, owned by the caller, that must outlive that work), or on the
+ * context's own stream again when `stream` is NULL.  Work queued before the
+ * switch stays ordered before work queued after it.  Replaces the engine's
+ * command encoder that the reference's render graph records the pass into
+ * (GraphicsManager::execute_in_this_frame, graphics_manager.cpp:407-427).
+ * Refused while the serving loop runs (it uses streams of its own). */
+BSM_API bsm_status bsm_set_stream(bsm_context* ctx, void* stream);
+/* The stream the context's work runs on (cudaStream_t). */
+BSM_API void* bsm_get_stream(bsm_context* ctx);
 
 /* Device memory helpers for callers without their own allocator. */
 BSM_API bsm_status bsm_device_alloc(bsm_context* ctx, uint64_t bytes, void** ptr);
@@ -163,22 +187,24 @@ typedef struct bsm_scene_desc {
 } bsm_scene_desc;
 
 enum { BSM_COLLAPSE_SAH_OPTIMAL = 0, BSM_COLLAPSE_GREEDY = 1 };
+enum { BSM_BUILD_DEVICE = 0, BSM_BUILD_HOST = 1 };
 typedef struct bsm_bvh_opts {
-    uint32_t sah_bins;        /* 0 = 32 */
+    uint32_t sah_bins;        /* 0 = 32 (the device builder takes 4..32, the host builder 4..256) */
     uint32_t max_leaf_tris;   /* 1..2, 0 = 2 */
-    uint32_t num_threads;     /* 0 = hardware concurrency */
+    uint32_t num_threads;     /* host builder threads; 0 = hardware concurrency */
     uint32_t collapse;        /* binary -> 8-wide: BSM_COLLAPSE_SAH_OPTIMAL (dynamic programming over a
                                  binary tree of single-triangle leaves) or BSM_COLLAPSE_GREEDY (open the
                                  largest child) */
     float tri_cost;           /* SAH-optimal collapse: cost of a triangle test relative to a node test; 0 = 1.0 */
+    uint32_t builder;         /* BSM_BUILD_DEVICE (default: sm_103a kernels) or BSM_BUILD_HOST (C++ threads) */
 } bsm_bvh_opts;
 
 typedef struct bsm_bvh_stats {
     uint32_t num_nodes;       /* 8-wide compressed nodes (80 B each) */
     uint32_t num_tris;
     uint32_t max_depth;
-    uint32_t reserved;
-    double build_ms;          /* host build time */
+    uint32_t builder;         /* BSM_BUILD_* that built it */
+    double build_ms;          /* build time (wall clock, uploads and waits included) */
     double sah_cost;          /* SAH cost of the binary BVH before collapsing */
     uint64_t node_bytes;
     uint64_t tri_bytes;
@@ -187,8 +213,11 @@ typedef struct bsm_bvh_stats {
 /* Copies a scene to the device.  Replaces the GPU-scene upload the reference
  * does in GpuSceneSystem (bisemutum/src/graphics/gpu_scene_system.cpp). */
 BSM_API bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* desc, uint32_t* scene_id);
-/* SAH-binned build of the compressed 8-wide BVH; replaces the driver BLAS/TLAS
- * build of AccelerationStructure (bisemutum/src/graphics/accel.cpp:11-159). */
+/* SAH-binned build of the compressed 8-wide BVH, on the device by default
+ * (opts->builder); replaces the driver BLAS/TLAS build of
+ * AccelerationStructure (bisemutum/src/graphics/accel.cpp:11-159), which the
+ * reference also runs on the GPU (graphics_manager.cpp:475-478).  Synchronous.
+ * A two-level scene rebuilds its TLAS from the current transforms. */
 BSM_API bsm_status bsm_scene_build_bvh(bsm_context* ctx, uint32_t scene_id, const bsm_bvh_opts* opts,
                                        bsm_bvh_stats* stats);
 BSM_API bsm_status bsm_scene_release(bsm_context* ctx, uint32_t scene_id);
@@ -268,10 +297,22 @@ typedef struct bsm_render_stats {
  * history (kept per view index, reset when the camera or size changes, as
  * path_tracing.cpp:224-245 does); outputs receive the running mean.
  * `outputs` may be NULL to keep the result on the device (bsm_read_view).
- * `stats` may be NULL. */
+ * `stats` may be NULL.
+ * Asynchronous when every output is in device memory (or `outputs` is NULL),
+ * `stats` is NULL and BSM_PT_STAGE_TIMING is not set: the call queues the
+ * render on the work stream and returns; bsm_sync or bsm_render_stats_read
+ * wait for it.  A host output, a non-NULL `stats` or stage timing make the
+ * call wait for the render (and report device errors).  The first render of a
+ * new view layout or a larger wavefront allocates and waits. */
 BSM_API bsm_status bsm_render(bsm_context* ctx, uint32_t scene_id, const bsm_camera* views, uint32_t n_views,
                               const bsm_pt_settings* settings, const bsm_view_output* outputs,
                               bsm_render_stats* stats);
+/* Waits for the last render issued on the context (bsm_render, bsm_render_batch,
+ * bsm_render_cached) and returns its statistics; BSM_ERR_DEVICE_CHECK if a device
+ * error flag is set (the flag is then cleared).  BSM_ERR_NOT_FOUND before any
+ * render.  No reference counterpart (the engine's profiler scopes, not its
+ * pass, time the frame). */
+BSM_API bsm_status bsm_render_stats_read(bsm_context* ctx, bsm_render_stats* stats);
 /* One view of a batched render: its camera, samples per pixel, segment limit
  * and seed (0 = the value in the settings). */
 typedef struct bsm_view_desc {
@@ -335,7 +376,9 @@ BSM_API bsm_status bsm_import_history(bsm_context* ctx, uint32_t view_index, con
 /* rays: n * 8 floats (ox, oy, oz, tmin, dx, dy, dz, tmax).
  * hits: n * 4 words (t as f32, primitive id as u32, u, v as f32); a miss has
  * primitive id 0xffffffff and t = tmax.  Replaces TraceRay in rt_gbuffer_rgen
- * with the closest-hit shader (rt_gbuffer.hlsl:7-36, rt_gbuffer_hit.hlsl:6-18). */
+ * with the closest-hit shader (rt_gbuffer.hlsl:7-36, rt_gbuffer_hit.hlsl:6-18).
+ * With location BSM_DEVICE both buffers are device memory and the call is
+ * asynchronous on the work stream; with BSM_HOST it waits. */
 BSM_API bsm_status bsm_trace_closest(bsm_context* ctx, uint32_t scene_id, const float* rays, uint32_t n,
                                      void* hits, uint32_t location);
 /* occluded: n bytes, 1 if any triangle lies in (tmin, tmax].  Replaces the
@@ -372,7 +415,7 @@ typedef struct bsm_primary_output {
  * sample (same ray, same t_min / ray_length from `settings`; NULL = defaults).
  * `near_z` / `far_z` are the camera's clip planes for the reverse-Z
  * projection (camera.hpp:54-55; 0 = the reference defaults 0.01 / 10000).
- * Synchronous. */
+ * Asynchronous on the work stream for device outputs; waits for host outputs. */
 BSM_API bsm_status bsm_render_primary(bsm_context* ctx, uint32_t scene_id, const bsm_camera* camera,
                                       const bsm_pt_settings* settings, float near_z, float far_z,
                                       const bsm_primary_output* out);
@@ -394,11 +437,18 @@ BSM_API bsm_status bsm_host_free(bsm_context* ctx, void* ptr);
  * some material is not opaque); a larger wavefront_capacity is
  * rejected with BSM_ERR_INVALID_ARG.  Any image size works: paths run in chunks.
  * `out_rgba` is a caller-owned device buffer of width*height RGBA floats,
- * tightly packed; it receives the per-pixel sums and then the mean.  The first
- * call on a device looks up the array's device address (set-up); make that
- * first call before any stream capture.  All calls share the array and it
- * keeps the last call's contents, so calls that overlap on the GPU race.  The
- * call is asynchronous on the context's stream (bsm_sync waits for it). */
+ * tightly packed and 16-byte aligned (else BSM_ERR_INVALID_ARG); it receives
+ * the per-pixel sums and then the mean of this call's samples.  Settings the
+ * call does not use: `accumulate` (every call writes a fresh mean), `denoise`,
+ * and flags other than BSM_PT_JITTER, BSM_PT_NO_SUN_NEE and BSM_PT_NO_SKY_NEE;
+ * `block_size` must be 0, 64, 128 or 256 and the kernels run with 128.  The
+ * first call on a device looks up the array's device address (set-up); make
+ * that first call before any stream capture.  All calls share the array and it
+ * keeps the last call's contents, so calls that overlap on the GPU race (that
+ * includes the array's device error word, which a sync point of any context
+ * that called this entry point reads and clears).  The call is asynchronous on
+ * the work stream; bsm_sync waits for it and reports a queue overflow of the
+ * call as BSM_ERR_DEVICE_CHECK. */
 BSM_API bsm_status bsm_render_noalloc(bsm_context* ctx, uint32_t scene_id, const bsm_camera* camera,
                                       const bsm_pt_settings* settings, float* out_rgba);
 
@@ -422,11 +472,11 @@ typedef struct bsm_request {
                                      must stay valid until the request is done */
 } bsm_request;
 
-enum { BSM_REQ_QUEUED = 0, BSM_REQ_RUNNING = 1, BSM_REQ_DONE = 2, BSM_REQ_FAILED = 3 };
+enum { BSM_REQ_QUEUED = 0, BSM_REQ_RUNNING = 1, BSM_REQ_DONE = 2, BSM_REQ_FAILED = 3, BSM_REQ_CANCELLED = 4 };
 
 typedef struct bsm_request_status {
     uint32_t state;               /* BSM_REQ_* */
-    uint32_t reserved;
+    uint32_t cancelled;           /* bsm_server_cancel was called (the state may still be DONE) */
     double submit_ms, admit_ms, done_ms;  /* since bsm_server_start */
     uint64_t paths;
 } bsm_request_status;
@@ -437,6 +487,7 @@ typedef struct bsm_server_stats {
     uint64_t pool_bytes, pool_used_bytes;
     uint32_t active, queued;
     double elapsed_ms;
+    uint64_t cancelled;
 } bsm_server_stats;
 
 /* Starts the serving loop on a context: a worker thread that admits requests
@@ -450,10 +501,19 @@ BSM_API bsm_status bsm_server_start(bsm_context* ctx, const bsm_server_opts* opt
 /* Queues a request; BSM_ERR_ADMISSION if it can never fit the pool. */
 BSM_API bsm_status bsm_server_submit(bsm_context* ctx, const bsm_request* request, uint64_t* request_id);
 BSM_API bsm_status bsm_server_poll(bsm_context* ctx, uint64_t request_id, bsm_request_status* status);
-/* Waits for a request (timeout_ms = 0: no limit); BSM_ERR_TIMEOUT when it runs out. */
+/* Waits for a request (timeout_ms = 0: no limit); BSM_ERR_TIMEOUT when it runs out,
+ * BSM_ERR_CANCELLED for a cancelled request. */
 BSM_API bsm_status bsm_server_wait(bsm_context* ctx, uint64_t request_id, uint32_t timeout_ms,
                                    bsm_request_status* status);
 BSM_API bsm_status bsm_server_get_stats(bsm_context* ctx, bsm_server_stats* stats);
+/* Cancels a request.  A queued one is dropped at once; a running one issues no
+ * more paths and gives its accumulator back to the pool when its chunks in
+ * flight finish (state BSM_REQ_CANCELLED).  If its output copy is already
+ * queued the call waits for it and the request completes normally.  Either way
+ * the library writes nothing into the request's out_rgba after the call
+ * returns, so the caller may free it.  No-op on finished requests.  No
+ * reference counterpart (the engine has no request queue). */
+BSM_API bsm_status bsm_server_cancel(bsm_context* ctx, uint64_t request_id);
 /* Stops the worker after the chunks in flight; queued requests are dropped. */
 BSM_API bsm_status bsm_server_stop(bsm_context* ctx);
 
@@ -476,6 +536,11 @@ typedef struct bsm_cache_settings {
     float lr;                 /* Adam learning rate (1e-2) */
     float ema_decay;          /* renders read an exponential moving average of the weights with this
                                  decay per Adam step (bias-corrected); 0 = the current weights */
+    float min_roughness;      /* a hit of the cache segment or later whose roughness is below this does not
+                                 query the cache: the path shades it and goes on (a near-mirror vertex's
+                                 outgoing radiance holds a sun glint the network cannot resolve) */
+    uint32_t extra_segments;  /* segments a path may go past cache_segment looking for a rough enough hit;
+                                 the last one queries the cache whatever its roughness */
 } bsm_cache_settings;
 
 BSM_API void bsm_cache_settings_default(bsm_cache_settings* cs);

@@ -24,7 +24,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = "/root/reference"
+# where the reference tree is read from (BSM_REFERENCE_ROOT overrides the default location)
+REFERENCE_ROOT = os.environ.get("BSM_REFERENCE_ROOT", "/root/reference")
 REF_SHADERS = [
     "bisemutum/shaders/core/utils/math.hlsl",
     "bisemutum/shaders/core/material/utils.hlsl",
@@ -39,7 +40,9 @@ REF_EXTRACTS = [
       "oct_wrap", "oct_encode", "oct_decode", "pack_normal_and_tangent", "unpack_normal_and_tangent"]),
     ("bisemutum/shaders/renderer/gbuffer.hlsl", ["GBuffer", "pack_surface_to_gbuffer", "unpack_gbuffer_to_surface"]),
 ]
-CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
+# -O3 without -march=native (the same build on x86 and Arm hosts) and without fast-math or FMA contraction:
+# IEEE float semantics at every optimisation level, so results equal the kernels'
+CXXFLAGS = ["-std=c++17", "-O3", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
 
 def _stale(out: str, deps: list[str]) -> bool:

@@ -20,7 +20,7 @@ import zlib
 import numpy as np
 import pytest
 
-REF_EXAMPLE = "/root/reference/examples/scene_basic"
+REF_EXAMPLE = os.path.join(os.environ.get("BSM_REFERENCE_ROOT", "/root/reference"), "examples/scene_basic")
 MAGIC = 0x0B1A55E7
 
 
