@@ -76,6 +76,10 @@ def parse():
     p.add_argument("--ref-spp", type=int, default=4096, help="cache: spp of the plain reference render")
     p.add_argument("--train-frames", type=int, default=120, help="cache: online training frames before timing")
     p.add_argument("--cache-spps", default="1,2,4,8,16,32,64", help="cache: samples per pixel of the compared frames")
+    p.add_argument("--cache-seeds", type=int, default=8, help="cache: frames (seeds) averaged per spp point")
+    p.add_argument("--no-extras", action="store_true",
+                   help="plain workload: leave out the BVH builder comparison and the batch / serve / cache "
+                        "summaries of the bench line")
     p.add_argument("--ema", type=float, default=-1.0, help="cache: weight moving-average decay (-1: library default)")
     p.add_argument("--cache-lr", type=float, default=-1.0, help="cache: Adam learning rate (-1: library default)")
     p.add_argument("--train-paths", type=int, default=0, help="cache: training paths per frame (0: library default)")
@@ -349,7 +353,9 @@ def run_ours(a, dist: Dist):
     e2e_val = rays_all / a.steps * e2e_steps / e2e_s / 1e6
     L.bsm_host_free(ctx.h, host)
     L.bsm_device_free(ctx.h, flush)
-    bvh_cmp = bvh_comparison(bsm, ctx, scene, a, bvh, st_dev_frame=(rays, sum(ms_dev))) if dist.rank == 0 else None
+    bvh_cmp = None
+    if dist.rank == 0 and not a.no_extras:
+        bvh_cmp = bvh_comparison(bsm, ctx, scene, a, bvh, st_dev_frame=(rays, sum(ms_dev)))
 
     line = None
     if dist.rank == 0:
@@ -401,6 +407,15 @@ def run_ours(a, dist: Dist):
                         "upload_and_build_s": round(setup_s, 3), **(bvh_cmp or {})},
                 "wall_s_timed": round(wall, 3)}
     ctx.close()
+    if line is not None and not a.no_extras:
+        # the benchmark spec's other forms, each on its own context after the timed region: 64 uneven views batched
+        # against one render per view, a Poisson request stream at 50 req/s for 10 s, and the radiance cache
+        # against the plain pass at equal relMSE
+        t_ex = time.perf_counter()
+        line["batch"] = batch_summary(a, bsm, dist.local, 64, 2, compare=8)
+        line["serve"] = serve_summary(a, bsm, dist.local, [50.0], 10.0, 600, 120)
+        line["cache"] = cache_summary(a, bsm, dist.local, [2, 4, 8, 16, 32], 4, 1024, 120)
+        line["extras_s"] = round(time.perf_counter() - t_ex, 1)
     if line is not None:
         print(json.dumps(line), flush=True)
     return 0
@@ -440,11 +455,11 @@ def bvh_comparison(bsm, ctx, scene, a, bvh, st_dev_frame):
 
 
 # ----------------------------------------------------------------- batch ----
-def batch_views(bsm, a):
+def batch_views(bsm, a, n=None):
     """Uneven views of the terrain: side log-uniform in [64, 1024], spp in {4, 8, 16, 32, 64}."""
     rng = np.random.default_rng(a.seed + 77)
     views = []
-    for i in range(a.views):
+    for i in range(a.views if n is None else n):
         side = int(round(float(np.exp(rng.uniform(np.log(64), np.log(1024))))))
         spp = int(rng.choice([4, 8, 16, 32, 64]))
         pos = (rng.uniform(0.15, 0.85), rng.uniform(0.35, 0.6), rng.uniform(-0.15, 0.35))
@@ -454,56 +469,59 @@ def batch_views(bsm, a):
     return views
 
 
-def run_batch(a, dist):
-    bsm = importlib.import_module("bisemutum-engine_gb300")
+def batch_summary(a, bsm, device, n_views, steps, compare=16):
+    """Uneven views rendered by one bsm_render_batch call (one wavefront, one graph; launch parameters from the
+    autotuner) against one bsm_render call per view (same paths, so equal relMSE: checked pixel by pixel on
+    `compare` views).  Device time (events) for both forms."""
     scene = bsm.generate_scene(bsm.BSM_SCENE_TERRAIN, seed=a.seed, grid=a.grid, spheres=a.spheres)
-    ctx = bsm.Context(dist.local)
-    sid = ctx.load_scene(scene)
-    views = batch_views(bsm, a)
-    s = bsm.settings(max_segments=a.segments, spp=1)
-    t0 = time.perf_counter()
-    tune = ctx.autotune(sid, views, s, a.tune_cache)
-    tune_s = time.perf_counter() - t0
-    # batched: one wavefront over all views
-    ctx.render_batch(sid, views, s, outputs=False)
-    b_ms, b_rays = [], 0
-    for _ in range(a.steps):
-        _, st = ctx.render_batch(sid, views, s, outputs=False)
-        b_ms.append(st.ms_total)
-        b_rays += st.extend_rays
-    # plain: one render call per view (each replays its own captured graph)
-    for cam, spp, segs, seed in views[:4]:
-        ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=segs, seed=seed), outputs=False)
-    p_ms, p_wall, p_rays = 0.0, 0.0, 0
-    for _ in range(max(1, a.steps // 2)):
-        ctx.sync()
-        w0 = time.perf_counter()
-        for cam, spp, segs, seed in views:
-            _, st = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=segs, seed=seed), outputs=False)
-            p_ms += st.ms_total
-            p_rays += st.extend_rays
-        ctx.sync()
-        p_wall += time.perf_counter() - w0
-    p_steps = max(1, a.steps // 2)
-    # equal relMSE: both forms trace the same paths; compare the images of a sample of views
-    sample = views[:16]
-    imgs, _ = ctx.render_batch(sid, sample, s)
-    worst = 0.0
-    for (cam, spp, segs, seed), img in zip(sample, imgs):
-        alone, _ = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=segs, seed=seed))
-        g, c = img[..., :3].astype(np.float64), alone[0][..., :3].astype(np.float64)
-        worst = max(worst, float((np.abs(g - c) / np.maximum(np.abs(c), 1e-3)).max()))
-    ctx.close()
+    ctx = bsm.Context(device)
+    try:
+        sid = ctx.load_scene(scene)
+        views = batch_views(bsm, a, n_views)
+        s = bsm.settings(max_segments=a.segments, spp=1)
+        t0 = time.perf_counter()
+        tune = ctx.autotune(sid, views, s, a.tune_cache)
+        tune_s = time.perf_counter() - t0
+        ctx.render_batch(sid, views, s, outputs=False)
+        b_ms, b_rays = [], 0
+        for _ in range(steps):
+            _, st = ctx.render_batch(sid, views, s, outputs=False)
+            b_ms.append(st.ms_total)
+            b_rays += st.extend_rays
+        for cam, spp, segs, seed in views[:4]:
+            ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=segs, seed=seed), outputs=False)
+        p_steps = max(1, steps // 2)
+        p_ms, p_wall, p_rays = 0.0, 0.0, 0
+        for _ in range(p_steps):
+            ctx.sync()
+            w0 = time.perf_counter()
+            for cam, spp, segs, seed in views:
+                _, st = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=segs, seed=seed), outputs=False)
+                p_ms += st.ms_total
+                p_rays += st.extend_rays
+            ctx.sync()
+            p_wall += time.perf_counter() - w0
+        sample = views[:compare]
+        imgs, _ = ctx.render_batch(sid, sample, s)
+        worst = 0.0
+        for (cam, spp, segs, seed), img in zip(sample, imgs):
+            alone, _ = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=segs, seed=seed))
+            g, c = img[..., :3].astype(np.float64), alone[0][..., :3].astype(np.float64)
+            worst = max(worst, float((np.abs(g - c) / np.maximum(np.abs(c), 1e-3)).max()))
+    finally:
+        ctx.close()
     b_s = min(b_ms) / 1e3
     p_s = p_ms / p_steps / 1e3
     px = sum(v[0].width * v[0].height for v in views)
     paths = sum(v[0].width * v[0].height * v[1] for v in views)
-    line = {"workload": "batch", "metric": "views/s at equal relMSE, batched vs one render per view",
+    return {"metric": "views/s at equal relMSE, batched vs one render per view",
+            "workload": f"{len(views)} views of the terrain, side log-uniform 64..1024, spp in {{4,8,16,32,64}}, "
+                        f"{a.segments} segments",
             "views": len(views), "pixels": px, "paths": paths,
             "batched_views_per_s": round(len(views) / b_s, 2), "plain_views_per_s": round(len(views) / p_s, 2),
             "plain_views_per_s_wall": round(len(views) * p_steps / p_wall, 2),
             "speedup": round(p_s / b_s, 3),
-            "batched_mrays_per_s": round(b_rays / a.steps / b_s / 1e6, 1),
+            "batched_mrays_per_s": round(b_rays / steps / b_s / 1e6, 1),
             "plain_mrays_per_s": round(p_rays / p_steps / p_s / 1e6, 1),
             "batch_ms": round(b_s * 1e3, 2), "plain_ms_device": round(p_s * 1e3, 2),
             "equal_relmse_check": {"views_compared": len(sample), "max_rel_diff": worst},
@@ -511,74 +529,88 @@ def run_batch(a, dist):
                      "postpone_depth": tune.best.postpone_depth, "refill_lanes": tune.best.refill_lanes,
                      "register_cap": tune.best.register_cap,
                      "best_ms": round(tune.best_ms, 3), "default_ms": round(tune.default_ms, 3),
-                     "tried": tune.tried, "from_cache": tune.from_cache, "seconds": round(tune_s, 2)},
-            "config": workload_config(a, scene.num_triangles)}
-    line["config"]["workload"] = (f"{len(views)} views of the terrain, side log-uniform 64..1024, "
-                                  f"spp in {{4,8,16,32,64}}, {a.segments} segments")
+                     "worst_ms": round(tune.worst_ms, 3),
+                     "tried": tune.tried, "from_cache": tune.from_cache, "seconds": round(tune_s, 2)}}
+
+
+def run_batch(a, dist):
     if dist.rank == 0:
+        bsm = importlib.import_module("bisemutum-engine_gb300")
+        line = {"workload": "batch", **batch_summary(a, bsm, dist.local, a.views, a.steps),
+                "config": workload_config(a)}
         print(json.dumps(line), flush=True)
     return 0
 
 
 # ----------------------------------------------------------------- serve ----
-def run_serve(a, dist):
+SERVE_MIX = "scene uniform, resolution log-uniform 128x128..1920x1080, spp {1,4,16,32}, bounces {2,4,8}"
+
+
+def serve_summary(a, bsm, device, rates, seconds, max_requests, saturation_n):
     """Poisson request stream over four resident scenes (20,504 / 250,050 / 1,482,242 / 4,973,058 triangles);
     per request: scene uniform, resolution log-uniform 128x128..1920x1080, spp in {1,4,16,32}, bounces in
-    {2,4,8}.  Reports p50/p99 latency (submit -> result in host memory) and rays/s per arrival rate."""
-    bsm = importlib.import_module("bisemutum-engine_gb300")
-    ctx = bsm.Context(dist.local)
-    specs = [(bsm.BSM_SCENE_ROOM, 0, 64), (bsm.BSM_SCENE_TERRAIN, 256, 250), (bsm.BSM_SCENE_TERRAIN, 512, 2000),
-             (bsm.BSM_SCENE_TERRAIN, 1024, 6000)]
-    scenes, ids, tris = [], [], []
-    t0 = time.perf_counter()
-    for kind, grid, sph in specs:
-        sc = bsm.generate_scene(kind, seed=a.seed, grid=grid, spheres=sph)
-        scenes.append(sc)
-        ids.append(ctx.load_scene(sc))
-        tris.append(sc.num_triangles)
-    setup_s = time.perf_counter() - t0
-    rng = np.random.default_rng(a.seed + 5)
-    results = []
-    for lam in [float(x) for x in a.rates.split(",")]:
-        n = int(min(a.max_requests, max(20, lam * a.serve_seconds)))
-        ctx.server_start(pool_bytes=16 << 30, chunk_paths=a.serve_chunk, lanes=a.serve_lanes)
-        arrivals = np.cumsum(rng.exponential(1.0 / lam, n))
-        reqs = []
-        for i in range(n):
-            k = int(rng.integers(0, 4))
-            u = float(rng.uniform())
-            w = int(round(128 * (1920 / 128) ** u))
-            h = int(round(128 * (1080 / 128) ** u))
-            base = scenes[k].camera
-            cam = bsm.make_camera(tuple(base.position), tuple(base.front), width=w, height=h)
-            reqs.append((ids[k], cam, int(rng.choice([1, 4, 16, 32])), int(rng.choice([2, 4, 8])), int(i + 1)))
-        start = time.perf_counter()
-        rids = []
-        for (sid, cam, spp, segs, seed), t_arr in zip(reqs, arrivals):
-            delay = start + t_arr - time.perf_counter()
-            if delay > 0:
-                time.sleep(delay)
-            rids.append(ctx.submit(sid, cam, spp, segs, seed)[0])
-        lat = []
-        for rid in rids:
-            st = ctx.wait(rid, timeout_ms=600000)
-            lat.append(st.done_ms - st.submit_ms)
-        wall = time.perf_counter() - start
-        ss = ctx.server_stats()
-        ctx.server_stop()
-        lat = np.array(lat)
-        results.append({"rate_req_s": lam, "requests": n, "p50_ms": round(float(np.percentile(lat, 50)), 2),
-                        "p99_ms": round(float(np.percentile(lat, 99)), 2),
-                        "mean_ms": round(float(lat.mean()), 2), "completed_req_s": round(n / wall, 2),
-                        "mrays_per_s": round(ss.extend_rays / wall / 1e6, 1), "wall_s": round(wall, 2)})
-    saturated = serve_saturated(a, bsm, ctx, ids, scenes, rng)
-    ctx.close()
-    line = {"workload": "serve", "metric": "p50/p99 request latency and rays/s per Poisson arrival rate",
+    {2,4,8}.  p50/p99 latency (submit -> result in host memory) and rays/s per arrival rate, then the
+    efficiency at saturation against batched renders of the same views."""
+    ctx = bsm.Context(device)
+    try:
+        specs = [(bsm.BSM_SCENE_ROOM, 0, 64), (bsm.BSM_SCENE_TERRAIN, 256, 250), (bsm.BSM_SCENE_TERRAIN, 512, 2000),
+                 (bsm.BSM_SCENE_TERRAIN, 1024, 6000)]
+        scenes, ids, tris = [], [], []
+        t0 = time.perf_counter()
+        for kind, grid, sph in specs:
+            sc = bsm.generate_scene(kind, seed=a.seed, grid=grid, spheres=sph)
+            scenes.append(sc)
+            ids.append(ctx.load_scene(sc))
+            tris.append(sc.num_triangles)
+        setup_s = time.perf_counter() - t0
+        rng = np.random.default_rng(a.seed + 5)
+        results = []
+        for lam in rates:
+            n = int(min(max_requests, max(20, lam * seconds)))
+            ctx.server_start(pool_bytes=16 << 30, chunk_paths=a.serve_chunk, lanes=a.serve_lanes)
+            arrivals = np.cumsum(rng.exponential(1.0 / lam, n))
+            reqs = []
+            for i in range(n):
+                k = int(rng.integers(0, 4))
+                u = float(rng.uniform())
+                w = int(round(128 * (1920 / 128) ** u))
+                h = int(round(128 * (1080 / 128) ** u))
+                base = scenes[k].camera
+                cam = bsm.make_camera(tuple(base.position), tuple(base.front), width=w, height=h)
+                reqs.append((ids[k], cam, int(rng.choice([1, 4, 16, 32])), int(rng.choice([2, 4, 8])), int(i + 1)))
+            start = time.perf_counter()
+            rids = []
+            for (sid, cam, spp, segs, seed), t_arr in zip(reqs, arrivals):
+                delay = start + t_arr - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                rids.append(ctx.submit(sid, cam, spp, segs, seed)[0])
+            lat = []
+            for rid in rids:
+                st = ctx.wait(rid, timeout_ms=600000)
+                lat.append(st.done_ms - st.submit_ms)
+            wall = time.perf_counter() - start
+            ss = ctx.server_stats()
+            ctx.server_stop()
+            lat = np.array(lat)
+            results.append({"rate_req_s": lam, "requests": n, "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                            "p99_ms": round(float(np.percentile(lat, 99)), 2),
+                            "mean_ms": round(float(lat.mean()), 2), "completed_req_s": round(n / wall, 2),
+                            "mrays_per_s": round(ss.extend_rays / wall / 1e6, 1), "wall_s": round(wall, 2)})
+        saturated = serve_saturated(a, bsm, ctx, ids, scenes, rng, n=saturation_n) if saturation_n else None
+    finally:
+        ctx.close()
+    return {"metric": "p50/p99 request latency and rays/s per Poisson arrival rate",
             "scenes_triangles": tris, "setup_s": round(setup_s, 1), "results": results, "saturated": saturated,
-            "request_mix": "scene uniform, resolution log-uniform 128x128..1920x1080, spp {1,4,16,32}, "
-                           "bounces {2,4,8}", "server": {"pool_bytes": 16 << 30, "chunk_paths": a.serve_chunk,
-                                                          "lanes": a.serve_lanes}}
+            "request_mix": SERVE_MIX,
+            "server": {"pool_bytes": 16 << 30, "chunk_paths": a.serve_chunk, "lanes": a.serve_lanes}}
+
+
+def run_serve(a, dist):
     if dist.rank == 0:
+        bsm = importlib.import_module("bisemutum-engine_gb300")
+        rates = [float(x) for x in a.rates.split(",")]
+        line = {"workload": "serve", **serve_summary(a, bsm, dist.local, rates, a.serve_seconds, a.max_requests, 240)}
         print(json.dumps(line), flush=True)
     return 0
 
@@ -661,91 +693,75 @@ def run_instanced(a, dist):
 
 
 # ----------------------------------------------------------------- cache ----
-def run_cache(a, dist):
-    """Radiance cache on the terrain scene: relMSE against a high-spp plain render and device time per frame,
-    for the plain pass (8 segments) and the cached pass (paths end in the cache at their third vertex; the cache
-    keeps training online, 32,768 training paths and 4 Adam steps of 16,384 vertices per frame, counted in its
-    frame time), then frames/s of each at equal relMSE."""
-    bsm = importlib.import_module("bisemutum-engine_gb300")
+def cache_summary(a, bsm, device, spps, seeds, ref_spp, train_frames):
+    """Radiance cache on the terrain scene: relMSE against a high-spp plain render and DEVICE time per frame
+    (CUDA events; the cached frame's training step included), for the plain pass (8 segments) and the cached
+    pass (paths end in the cache at their third vertex; 32,768 training paths and 4 Adam steps of 16,384
+    vertices per frame), then frames/s of each at equal relMSE, untrimmed and with the largest 0.1 % of per-value
+    errors dropped.  Both passes use the same seeds (common random numbers): their paths agree up to the cache
+    vertex, so rare fireflies of the shared prefix (sun glints on near-mirror spheres) fall on both sides."""
     scene = bsm.generate_scene(bsm.BSM_SCENE_TERRAIN, seed=a.seed, grid=a.grid, spheres=a.spheres, width=a.width,
                                height=a.height)
-    ctx = bsm.Context(dist.local)
-    sid = ctx.load_scene(scene)
-    cam = scene.camera
-    # reference: ref_spp in progressive calls of 256
-    per = min(256, a.ref_spp)
-    ctx.render(sid, [cam], bsm.settings(spp=per, max_segments=a.segments, seed=90000, accumulate=0), outputs=False)
-    for k in range(1, a.ref_spp // per):
-        last = k == a.ref_spp // per - 1
-        imgs, _ = ctx.render(sid, [cam], bsm.settings(spp=per, max_segments=a.segments, seed=90000, accumulate=1),
-                             outputs=last)
-    ref = imgs[0] if a.ref_spp > per else ctx.render(sid, [cam], bsm.settings(spp=per, max_segments=a.segments,
-                                                                              seed=90000))[0][0]
-    spps = [int(x) for x in a.cache_spps.split(",")]
-    seeds = 3
+    ctx = bsm.Context(device)
+    try:
+        sid = ctx.load_scene(scene)
+        cam = scene.camera
+        per = min(256, ref_spp)
+        ctx.render(sid, [cam], bsm.settings(spp=per, max_segments=a.segments, seed=90000, accumulate=0),
+                   outputs=ref_spp <= per)
+        imgs = None
+        for k in range(1, ref_spp // per):
+            last = k == ref_spp // per - 1
+            imgs, _ = ctx.render(sid, [cam], bsm.settings(spp=per, max_segments=a.segments, seed=90000,
+                                                          accumulate=1), outputs=last)
+        ref = imgs[0] if imgs is not None else ctx.render(sid, [cam], bsm.settings(
+            spp=per, max_segments=a.segments, seed=90000))[0][0]
+        seed_of = [7 + 1000 * k for k in range(seeds)]
 
-    def trimmed(img, r):
-        return bsm.rel_mse(img, r, trim=0.001)
+        def measure(render):
+            rows = []
+            for spp in spps:
+                render(spp, seed_of[0])   # warm-up: graph capture for this size
+                errs, terrs, ms = [], [], []
+                for sd in seed_of:
+                    img, st = render(spp, sd + spp)
+                    errs.append(bsm.rel_mse(img, ref))
+                    terrs.append(bsm.rel_mse(img, ref, trim=0.001))
+                    ms.append(st.ms_total)
+                rows.append({"spp": spp, "relmse": float(np.mean(errs)), "relmse_trimmed": float(np.mean(terrs)),
+                             "relmse_median": float(np.median(errs)), "ms": float(np.mean(ms))})
+            return rows
 
-    plain = []
-    for spp in spps:
-        ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=a.segments, seed=5 + spp), outputs=False)
-        errs, terrs, ms = [], [], []
-        for k in range(seeds):
-            img, st = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=a.segments, seed=7 + 100 * k + spp))
-            errs.append(bsm.rel_mse(img[0], ref))
-            terrs.append(trimmed(img[0], ref))
-            ms.append(st.ms_total)
-        plain.append({"spp": spp, "relmse": float(np.mean(errs)), "relmse_trimmed": float(np.mean(terrs)),
-                      "ms": float(np.mean(ms))})
-    cache = bsm.RadianceCache(ctx, seed=a.seed)
-    cs = bsm.cache_settings()
-    if a.ema >= 0.0:
-        cs.ema_decay = a.ema
-    if a.cache_lr > 0.0:
-        cs.lr = a.cache_lr
-    if a.train_paths > 0:
-        cs.train_paths = a.train_paths
-    if a.train_segments > 0:
-        cs.train_segments = a.train_segments
-    t0 = time.perf_counter()
-    losses = []
-    for f in range(a.train_frames):
-        _, _, loss = cache.render(sid, cam, bsm.settings(spp=1, seed=1000 + f), cs, outputs=False)
-        losses.append(loss)
-    train_s = time.perf_counter() - t0
-    cached = []
-    for spp in spps:
-        errs, terrs, ms, msr = [], [], [], []
-        for k in range(seeds):
-            ctx.sync()
-            w0 = time.perf_counter()
-            img, st, _ = cache.render(sid, cam, bsm.settings(spp=spp, seed=3000 + 100 * k + spp), cs)  # train + render
-            ms.append((time.perf_counter() - w0) * 1e3)
-            msr.append(st.ms_total)
-            errs.append(bsm.rel_mse(img, ref))
-            terrs.append(trimmed(img, ref))
-        cached.append({"spp": spp, "relmse": float(np.mean(errs)), "relmse_trimmed": float(np.mean(terrs)),
-                       "ms": float(np.mean(ms)), "ms_render": float(np.mean(msr))})
-    cache.close()
-    ctx.close()
+        def plain_render(spp, sd):
+            img, st = ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=a.segments, seed=sd))
+            return img[0], st
 
-    def fit_err(curve, key, biased):
-        """relMSE(spp) ~ V / spp (+ B for the biased cached estimator), least squares on the measured points."""
-        x = np.array([1.0 / c["spp"] for c in curve])
-        y = np.array([c[key] for c in curve])
-        if biased:
-            A = np.stack([x, np.ones_like(x)], 1)
-            (V, B), *_ = np.linalg.lstsq(A, y, rcond=None)
-            return float(V), float(max(B, 0.0))
-        return float((x @ y) / (x @ x)), 0.0
+        plain = measure(plain_render)
+        cache = bsm.RadianceCache(ctx, seed=a.seed)
+        cs = bsm.cache_settings()
+        if a.ema >= 0.0:
+            cs.ema_decay = a.ema
+        if a.cache_lr > 0.0:
+            cs.lr = a.cache_lr
+        if a.train_paths > 0:
+            cs.train_paths = a.train_paths
+        if a.train_segments > 0:
+            cs.train_segments = a.train_segments
+        t0 = time.perf_counter()
+        losses = []
+        for f in range(train_frames):
+            _, _, loss = cache.render(sid, cam, bsm.settings(spp=1, seed=100000 + f), cs, outputs=False)
+            losses.append(loss)
+        train_s = time.perf_counter() - t0
 
-    def fit_time(curve):
-        x = np.array([c["spp"] for c in curve], np.float64)
-        y = np.array([c["ms"] for c in curve])
-        A = np.stack([x, np.ones_like(x)], 1)
-        (t1, t0_), *_ = np.linalg.lstsq(A, y, rcond=None)
-        return float(t1), float(t0_)
+        def cached_render(spp, sd):
+            img, st, _ = cache.render(sid, cam, bsm.settings(spp=spp, seed=sd), cs)   # trains, then renders
+            return img, st
+
+        cached = measure(cached_render)
+        cache.close()
+    finally:
+        ctx.close()
 
     def time_at(curve, key, target):
         """Frame time the method needs for `target` error: log-log interpolation between measured points."""
@@ -757,28 +773,37 @@ def run_cache(a, dist):
         return None
 
     equal = {}
-    for key in ("relmse_trimmed", "relmse"):
+    for key in ("relmse", "relmse_trimmed"):
         rows = []
-        for c in plain:
+        for c, k in zip(plain, cached):
             tc = time_at(cached, key, c[key])
+            # where the cached frame at the same spp is both at least as accurate and faster, it reaches the plain
+            # frame's error in at most its own time: plain ms / cached ms bounds the equal-error speedup from below
+            # (robust where single fireflies make the untrimmed error curve non-monotone in spp)
+            lower = round(c["ms"] / k["ms"], 3) if k[key] <= c[key] else None
             rows.append({"plain_spp": c["spp"], "target": round(c[key], 6), "plain_fps": round(1e3 / c["ms"], 2),
                          "cached_fps": round(1e3 / tc, 2) if tc else None,
-                         "speedup": round(c["ms"] / tc, 3) if tc else None})
-        Vp, _ = fit_err(plain, key, False)
-        Vc, Bc = fit_err(cached, key, True)
-        equal[key] = {"at_plain_points": rows, "plain_fit_V": Vp, "cached_fit": {"V": Vc, "B": Bc}}
-    line = {"workload": "cache", "metric": "frames/s at equal relMSE, cached vs plain pass",
-            "reference_spp": a.ref_spp, "seeds_per_point": seeds, "plain": plain, "cached": cached,
-            "equal_relmse": equal,
-            "train": {"frames": a.train_frames, "seconds": round(train_s, 2),
+                         "speedup": round(c["ms"] / tc, 3) if tc else None,
+                         "speedup_lower_bound_same_spp": lower})
+        equal[key] = rows
+    return {"metric": "frames/s at equal relMSE, cached vs plain pass (device time, training included)",
+            "workload": f"radiance cache on the terrain scene, {a.width}x{a.height}, paths end in the cache after "
+                        f"2 bounces",
+            "reference_spp": ref_spp, "seeds_per_point": seeds, "seeds": "common random numbers (same per point)",
+            "plain": plain, "cached": cached, "equal_relmse": equal,
+            "train": {"frames": train_frames, "seconds": round(train_s, 2),
                       "loss_first10": round(float(np.mean(losses[:10])), 4),
                       "loss_last10": round(float(np.mean(losses[-10:])), 4),
                       "per_frame": f"{cs.train_paths} training paths, {cs.train_steps} Adam steps of {cs.train_batch} "
-                                   f"vertices, lr {cs.lr:g}",
-                      "ema_decay": round(float(cs.ema_decay), 4)},
-            "config": workload_config(a, scene.num_triangles)}
-    line["config"]["workload"] = f"radiance cache on the terrain scene, {a.width}x{a.height}, cache after 2 bounces"
+                                   f"vertices, lr {cs.lr:g}", "ema_decay": round(float(cs.ema_decay), 4)}}
+
+
+def run_cache(a, dist):
     if dist.rank == 0:
+        bsm = importlib.import_module("bisemutum-engine_gb300")
+        spps = [int(x) for x in a.cache_spps.split(",")]
+        line = {"workload": "cache", **cache_summary(a, bsm, dist.local, spps, a.cache_seeds, a.ref_spp,
+                                                     a.train_frames), "config": workload_config(a)}
         print(json.dumps(line), flush=True)
     return 0
 

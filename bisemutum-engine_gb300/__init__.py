@@ -78,7 +78,7 @@ class SceneDesc(C.Structure):
                 ("materials", C.POINTER(Material)), ("num_dir_lights", C.c_uint32),
                 ("dir_lights", C.POINTER(DirLight)), ("sky", Sky), ("num_point_lights", C.c_uint32),
                 ("point_lights", C.POINTER(PointLight)), ("num_rect_lights", C.c_uint32),
-                ("rect_lights", C.POINTER(RectLight))]
+                ("rect_lights", C.POINTER(RectLight)), ("normals", C.POINTER(C.c_float))]
 
 
 BSM_COLLAPSE_SAH_OPTIMAL, BSM_COLLAPSE_GREEDY = 0, 1
@@ -140,7 +140,7 @@ class TuneParams(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("best", TuneParams), ("best_ms", C.c_float), ("default_ms", C.c_float), ("tried", C.c_uint32),
-                ("from_cache", C.c_uint32)]
+                ("from_cache", C.c_uint32), ("worst_ms", C.c_float), ("reserved", C.c_uint32)]
 
 
 class ServerOpts(C.Structure):
@@ -347,6 +347,7 @@ class SceneData:
     point_lights: np.ndarray | None = None  # (P, 12): position, emission, range, direction to light, cos_inner, cos_outer
     rect_lights: np.ndarray | None = None   # (R, 15): centre, axis x, axis y, width, height, emission, two_sided
     sky_transform: np.ndarray | None = None  # (9,) cubemap lookup rotation, row-major
+    normals: np.ndarray | None = None  # (V, 3) float32 vertex normals (shading normals), or None
 
     @property
     def num_triangles(self) -> int:
@@ -378,6 +379,12 @@ class SceneData:
         d.num_dir_lights = len(self.lights)
         d.dir_lights = lights
         keep = [pos, idx, mids, mats, lights]
+        if self.normals is not None:
+            nrm = np.ascontiguousarray(self.normals, np.float32).reshape(-1, 3)
+            if nrm.shape[0] != pos.shape[0]:
+                raise ValueError("normals need one row per vertex")
+            d.normals = _ptr(nrm)
+            keep.append(nrm)
         keep += _fill_sky_and_lights(d, self)
         self._keep = keep
         return d
@@ -605,8 +612,9 @@ def _scene_from_desc(d: SceneDesc, cam: Camera | None) -> SceneData:
                     for p in (d.point_lights[i] for i in range(d.num_point_lights))], np.float32).reshape(-1, 12)
     rects = np.array([[*r.center, *r.axis_x, *r.axis_y, r.width, r.height, *r.emission, r.two_sided]
                       for r in (d.rect_lights[i] for i in range(d.num_rect_lights))], np.float32).reshape(-1, 15)
+    nrm = np.ctypeslib.as_array(d.normals, (nv, 3)).copy() if (d.normals and nv) else None
     return SceneData(pos, idx, mids, mats, lights, d.sky.kind, tuple(d.sky.color), tex, cam, point_lights=pts,
-                     rect_lights=rects)
+                     rect_lights=rects, normals=nrm)
 
 
 _MESH_ARRAYS = [("positions", "num_vertices", 3, np.float32), ("normals", "num_normals", 3, np.float32),

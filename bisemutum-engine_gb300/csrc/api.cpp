@@ -44,6 +44,7 @@ struct Scene {
     std::vector<float> positions;
     std::vector<uint32_t> indices;
     std::vector<uint32_t> material_ids;
+    std::vector<float> normals;             // per vertex (3 floats), empty when the scene has none
     std::vector<float> transparency;  // per material: 0 opaque, else what the any-hit rule compares against
     uint32_t num_triangles = 0;
     float extent = 1.0f;
@@ -51,7 +52,7 @@ struct Scene {
     bsm_bvh_stats bvh_stats{};
     bool tuned = false;
     bsm_tune_params tune{};
-    DevBuf nodes, tris, materials, texels, sky_alias, pdf_tab;
+    DevBuf nodes, tris, materials, texels, sky_alias, pdf_tab, tri_normals;
     // two-level scenes: instances (caller order), their TLAS leaves, refit data
     bool instanced = false;
     std::vector<bsm_instance> instances;
@@ -415,7 +416,8 @@ extern "C" void bsm_destroy(bsm_context* ctx) {
     for (auto& g : ctx->graphs) if (g.exec) cudaGraphExecDestroy(g.exec);
     for (auto& kv : ctx->scenes) {
         Scene* s = kv.second.get();
-        for (DevBuf* b : {&s->nodes, &s->tris, &s->materials, &s->texels, &s->sky_alias, &s->pdf_tab})
+        for (DevBuf* b : {&s->nodes, &s->tris, &s->materials, &s->texels, &s->sky_alias, &s->pdf_tab,
+                          &s->tri_normals})
             dev_free(ctx, *b);
     }
     dev_free(ctx, ctx->wf_buf);
@@ -507,7 +509,7 @@ bsm_status build_tlas(bsm_context* ctx, Scene* sc);
 
 // Device buffers of a scene; an instanced scene also lets go of its geometries.
 void free_scene_buffers(bsm_context* ctx, Scene& sc) {
-    for (DevBuf* b : {&sc.nodes, &sc.tris, &sc.materials, &sc.texels, &sc.sky_alias, &sc.pdf_tab,
+    for (DevBuf* b : {&sc.nodes, &sc.tris, &sc.materials, &sc.texels, &sc.sky_alias, &sc.pdf_tab, &sc.tri_normals,
                       &sc.insts, &sc.inst_box, &sc.node_box, &sc.mat_tr})
         dev_free(ctx, *b);
     if (sc.instanced)
@@ -766,6 +768,30 @@ bsm_status device_bvh(bsm_context* ctx, const float* positions, uint32_t nv, con
 
 bool use_host_builder(const bsm_bvh_opts* opts) { return opts && opts->builder == BSM_BUILD_HOST; }
 
+// The leaf-ordered vertex normals of a scene that has them (after every BVH build: the leaf order changes).
+bsm_status make_tri_normals(bsm_context* ctx, Scene* sc) {
+    sc->dev.tri_normals = nullptr;
+    if (sc->normals.empty()) return BSM_OK;
+    bsm_status st;
+    if ((st = dev_alloc(ctx, sc->tri_normals, (size_t)sc->num_triangles * 48))) return st;
+    const size_t b_n = (sc->normals.size() * 4 + 255) & ~(size_t)255, b_i = sc->indices.size() * 4;
+    char* tmp = nullptr;
+    CK(cudaMalloc(&tmp, b_n + b_i + 16));
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaMemcpyAsync(tmp, sc->normals.data(), sc->normals.size() * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && b_i) e = cudaMemcpyAsync(tmp + b_n, sc->indices.data(), b_i, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        launch_gather_normals(s, (const CwTri*)sc->tris.ptr, sc->num_triangles, (const float*)tmp,
+                              b_i ? (const uint32_t*)(tmp + b_n) : nullptr, (float4*)sc->tri_normals.ptr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "vertex normals");
+    sc->dev.tri_normals = (const float4*)sc->tri_normals.ptr;
+    return BSM_OK;
+}
+
 }  // namespace
 
 // ================================================================ scenes ====
@@ -790,6 +816,11 @@ extern "C" bsm_status bsm_scene_upload(bsm_context* ctx, const bsm_scene_desc* d
             if (m >= d->num_materials) return fail(ctx, BSM_ERR_INVALID_ARG, "material id out of range");
     }
     sc->num_triangles = d->num_triangles;
+    if (d->normals) {
+        sc->normals.assign(d->normals, d->normals + 3 * (size_t)d->num_vertices);
+        for (float x : sc->normals)
+            if (!std::isfinite(x)) return fail(ctx, BSM_ERR_INVALID_ARG, "non-finite vertex normal");
+    }
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (size_t i = 0; i < (size_t)d->num_vertices; ++i)
         for (int k = 0; k < 3; ++k) {
@@ -839,6 +870,7 @@ extern "C" bsm_status bsm_scene_build_bvh(bsm_context* ctx, uint32_t scene_id, c
         if (st) return st;
         sc->dev.nodes = (const CwNode*)sc->nodes.ptr;
         sc->dev.tris = (const CwTri*)sc->tris.ptr;
+        if ((st = make_tri_normals(ctx, sc))) return st;
         sc->has_bvh = true;
         sc->bvh_stats = s;
         clear_graphs(ctx);
@@ -865,6 +897,7 @@ extern "C" bsm_status bsm_scene_build_bvh(bsm_context* ctx, uint32_t scene_id, c
     CK(cudaMemcpy(sc->tris.ptr, r.tris.data(), r.tris.size() * sizeof(CwTri), cudaMemcpyHostToDevice));
     sc->dev.nodes = (const CwNode*)sc->nodes.ptr;
     sc->dev.tris = (const CwTri*)sc->tris.ptr;
+    if ((st = make_tri_normals(ctx, sc))) return st;
     sc->has_bvh = true;
     bsm_bvh_stats s{};
     s.num_nodes = (uint32_t)r.nodes.size();
@@ -1252,7 +1285,7 @@ extern "C" bsm_status bsm_scene_device_bytes(bsm_context* ctx, uint32_t scene_id
     if (!sc) return fail(ctx, BSM_ERR_NOT_FOUND, "unknown scene id");
     uint64_t b = 0;
     for (DevBuf* x : {&sc->nodes, &sc->tris, &sc->materials, &sc->texels, &sc->sky_alias, &sc->pdf_tab,
-                      &sc->insts, &sc->inst_box, &sc->node_box, &sc->mat_tr})
+                      &sc->tri_normals, &sc->insts, &sc->inst_box, &sc->node_box, &sc->mat_tr})
         b += x->bytes;
     *bytes = b;
     return BSM_OK;
@@ -1367,7 +1400,8 @@ struct ViewReq {
 
 bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<ViewReq>& req,
                        const bsm_pt_settings& s, const bsm_view_output* outputs, bsm_render_stats* stats,
-                       const void* cache_wb = nullptr, uint32_t cache_seg = 0, float cache_rough = 0.0f) {
+                       const void* cache_wb = nullptr, uint32_t cache_seg = 0, float cache_rough = 0.0f,
+                       bool start_recorded = false) {
     const uint32_t n_views = (uint32_t)req.size();
     cudaSetDevice(ctx->device);
     Scene* sc = find_scene(ctx, scene_id);
@@ -1462,7 +1496,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
     bool use_graph = !timing && !counting && !(s.flags & BSM_PT_NO_GRAPH);
     float stage_ms[4] = {0, 0, 0, 0};
     std::vector<int> tags;
-    CK(cudaEventRecord(ctx->ev[8], WS(ctx)));
+    if (!start_recorded) CK(cudaEventRecord(ctx->ev[8], WS(ctx)));   // start of the device time of this render
     if (use_graph) {
         // key: everything the recorded launches depend on
         std::vector<uint8_t> key(64);
@@ -1586,6 +1620,8 @@ extern "C" bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, con
     if (cs.cache_segment == 0 || cs.cache_segment >= (uint32_t)kMaxSeg)
         return fail(ctx, BSM_ERR_INVALID_ARG, "cache_segment must be 1..15");
     if (train_loss) *train_loss = 0.0f;
+    // the frame's device time (stats->ms_total) starts before its training step
+    CK(cudaEventRecord(ctx->ev[8], WS(ctx)));
     if (cs.train_steps > 0 && cs.train_paths > 0) {
         DevView dv{};
         make_view(*cam, dv);
@@ -1601,7 +1637,7 @@ extern "C" bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, con
         return fail(ctx, BSM_ERR_INVALID_ARG, "min_roughness must be >= 0 and cache_segment + extra_segments <= 15");
     req[0] = ViewReq{*cam, settings->spp, cs.cache_segment + 1 + cs.extra_segments, settings->seed};
     return render_impl(ctx, scene_id, req, *settings, output, stats, cache_render_weights(cache), cs.cache_segment,
-                       cs.extra_segments ? cs.min_roughness : 0.0f);
+                       cs.extra_segments ? cs.min_roughness : 0.0f, /*start_recorded=*/true);
 }
 
 extern "C" bsm_status bsm_render_batch(bsm_context* ctx, uint32_t scene_id, const bsm_view_desc* views,
@@ -1715,6 +1751,7 @@ extern "C" bsm_status bsm_autotune(bsm_context* ctx, uint32_t scene_id, const bs
         }
         *ms_out = best;
         result->tried++;
+        result->worst_ms = std::max(result->worst_ms, best);
         return BSM_OK;
     };
     bsm_tune_params cur{128, 0, 16, 8, 1};

@@ -711,6 +711,21 @@ struct Affine {
     void linear(const double* d, double* o) const {
         for (int i = 0; i < 3; ++i) o[i] = L[i][0] * d[0] + L[i][1] * d[1] + L[i][2] * d[2];
     }
+    // normals: the inverse transpose of L (cofactors over the determinant), as the reference's hit shader
+    // takes an object normal to the world with WorldToObject4x3 (raytracing/hit.hlsl:158); false when L is
+    // singular
+    bool normal(const double* n, double* o) const {
+        double C[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+                C[i][j] = L[i1][j1] * L[i2][j2] - L[i1][j2] * L[i2][j1];
+            }
+        double det = L[0][0] * C[0][0] + L[0][1] * C[0][1] + L[0][2] * C[0][2];
+        if (!(std::fabs(det) > 0.0)) return false;
+        for (int i = 0; i < 3; ++i) o[i] = (C[i][0] * n[0] + C[i][1] * n[1] + C[i][2] * n[2]) / det;
+        return true;
+    }
     // rotation part (columns of L normalised): Transform::from_matrix, transform.cpp:36-47
     void rotate(const double* d, double* o) const {
         double cl[3];
@@ -752,6 +767,8 @@ Affine transform_from(const TVal* v) {
 
 struct ProjectOwned {
     std::vector<float> pos;
+    std::vector<float> nrm;      // world-space vertex normals (zero for meshes without normals)
+    bool any_normals = false;
     std::vector<uint32_t> idx, mat;
     std::vector<bsm_material> mats;
     std::vector<bsm_dir_light> lights;
@@ -1243,12 +1260,20 @@ bsm_status project_load(const char* project_dir, bsm_scene_desc* desc, bsm_proje
             } else {
                 mid = mit->second;
             }
-            if (!placed) {  // the object's vertices in world space, once
+            if (!placed) {  // the object's vertices (and normals, where the mesh has them) in world space, once
+                const bool has_n = mo->nrm.size() == 3 * (size_t)nv;
                 for (uint32_t v = 0; v < nv; ++v) {
                     double p[3] = {mo->pos[3 * v], mo->pos[3 * v + 1], mo->pos[3 * v + 2]}, w[3];
                     world[i].apply(p, w);
                     for (int k = 0; k < 3; ++k) own->pos.push_back((float)w[k]);
+                    double n[3] = {0, 0, 0}, wn[3] = {0, 0, 0};
+                    if (has_n) {
+                        n[0] = mo->nrm[3 * v]; n[1] = mo->nrm[3 * v + 1]; n[2] = mo->nrm[3 * v + 2];
+                        if (!world[i].normal(n, wn)) wn[0] = wn[1] = wn[2] = 0.0;
+                    }
+                    for (int k = 0; k < 3; ++k) own->nrm.push_back((float)wn[k]);
                 }
+                own->any_normals = own->any_normals || has_n;
                 placed = true;
             }
             // ~0 = to the end of the index data (mesh.cpp:84-87, graphics_manager.cpp:726-729)
@@ -1292,6 +1317,7 @@ bsm_status project_load(const char* project_dir, bsm_scene_desc* desc, bsm_proje
     desc->point_lights = own->points.empty() ? nullptr : own->points.data();
     desc->num_rect_lights = (uint32_t)own->rects.size();
     desc->rect_lights = own->rects.empty() ? nullptr : own->rects.data();
+    desc->normals = own->any_normals ? own->nrm.data() : nullptr;
     // no SkyboxComponent texture support: the reference's black 1x1 cube when none is set
     // (skybox.cpp:47-50)
     desc->sky.kind = BSM_SKY_CONSTANT;

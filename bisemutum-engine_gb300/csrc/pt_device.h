@@ -48,6 +48,7 @@ struct DevSky {
 struct DevScene {
     const CwNode* nodes;       // the BVH; in a two-level scene the TLAS
     const CwTri* tris;         // leaf-ordered triangles (null in a two-level scene)
+    const float4* tri_normals; // single-level scenes with vertex normals: 3 per leaf triangle (xyz), else null
     const InstDev* insts;      // two-level scene: instances in TLAS leaf order, else null
     uint32_t num_instances;
     const float* mat_tr;       // two-level scene with non-opaque materials: per-material transparency, else null
@@ -144,6 +145,10 @@ void launch_trace_closest(cudaStream_t st, const DevScene& sc, const float4* ray
 void launch_trace_any(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint8_t* occluded,
                       int block);
 void launch_trace_count(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint2* counts);
+// Vertex normals of every leaf triangle in leaf order (3 float4 each) from per-vertex normals (3 floats each,
+// indexed by `idx`, or a soup when idx is null); all pointers are device memory.
+void launch_gather_normals(cudaStream_t st, const CwTri* tris, uint32_t n, const float* vn, const uint32_t* idx,
+                           float4* out);
 void launch_tlas_refit(cudaStream_t st, CwNode* nodes, float* node_box, const float* inst_box, uint32_t begin,
                        uint32_t end);
 void launch_primary(cudaStream_t st, const DevScene& sc, const DevView& v, float near_z, float far_z, float* depth,

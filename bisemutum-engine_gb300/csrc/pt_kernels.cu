@@ -270,8 +270,8 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
             V3 c = thr * le * w;
             if (max_comp(c) > 0.0f) accum_add(accum, m4.x, c);
         }
-        // surface at the hit
-        V3 N = v3(0.0f, 0.0f, 1.0f), P = v3(0.0f, 0.0f, 0.0f);
+        // surface at the hit: N shades (the interpolated vertex normal where the scene has them), Ng offsets
+        V3 N = v3(0.0f, 0.0f, 1.0f), Ng = N, P = v3(0.0f, 0.0f, 0.0f);
         Surface surf;
         surf.base_color = v3s(0.5f); surf.f0 = v3s(0.04f); surf.f90 = v3s(1.0f); surf.roughness = 0.5f; surf.ior = 1.5f;
         if (is_hit) {
@@ -279,7 +279,12 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
             uint32_t mi;
             hit_geometry(sc, leaf, sc.insts ? __float_as_uint(h4.z) : kMissPrim, ng, edge, mi);
             if (dot(ng, d) > 0.0f) ng = -ng;
+            Ng = ng;
             N = ng;
+            if (sc.tri_normals) {
+                N = shading_normal(sc, leaf, h4.z, h4.w, ng);
+                if (dot(N, d) > 0.0f) N = -N;
+            }
             P = v3(o4.x, o4.y, o4.z) + d * h4.x;
             float4 m0 = sc.materials[2 * mi], m1 = sc.materials[2 * mi + 1];
             surf.base_color = v3(m0.x, m0.y, m0.z);
@@ -319,7 +324,7 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
             }
         }
         if (cache_q) is_hit = false;  // no NEE, no continuation at a cache vertex
-        V3 org = P + N * sc.ray_offset;
+        V3 org = P + Ng * sc.ray_offset;
         const DevView* vp = views + view_id;
         float ray_len = is_hit ? vp->ray_length : 0.0f;
         float tmin = is_hit ? vp->t_min : 0.0f;
@@ -451,6 +456,20 @@ __global__ void k_resolve(const float4* __restrict__ accum, uint32_t width, uint
     out[(size_t)y * pitch + x] = make_float4(a.x * inv_spp, a.y * inv_spp, a.z * inv_spp, 1.0f);
 }
 
+// ------------------------------------------------------- vertex normals ----
+// The three vertex normals of every leaf triangle, in leaf order, from the
+// scene's per-vertex normals (indexed like the positions).
+__global__ void k_gather_normals(const CwTri* __restrict__ tris, uint32_t n, const float* __restrict__ vn,
+                                 const uint32_t* __restrict__ idx, float4* __restrict__ out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t prim = tris[i].prim;
+    for (int k = 0; k < 3; ++k) {
+        const size_t v = idx ? idx[3 * (size_t)prim + k] : 3 * (size_t)prim + k;
+        out[3 * (size_t)i + k] = make_float4(vn[3 * v], vn[3 * v + 1], vn[3 * v + 2], 0.0f);
+    }
+}
+
 // ------------------------------------------------------ stage entry points ----
 __global__ void __launch_bounds__(256) k_trace_closest(DevScene sc, const float4* __restrict__ rays, uint32_t n,
                                                        uint4* __restrict__ hits) {
@@ -503,6 +522,10 @@ __global__ void __launch_bounds__(256) k_primary(DevScene sc, DevView v, float n
         uint32_t mi;
         hit_geometry(sc, leaf, inst, ng, edge, mi);
         if (dot(ng, dw) > 0.0f) ng = -ng;
+        if (sc.tri_normals) {
+            ng = shading_normal(sc, leaf, hu, hv, ng);
+            if (dot(ng, dw) > 0.0f) ng = -ng;
+        }
         V3 T = normalize(edge);
         float4 m0 = sc.materials[2 * mi], m1 = sc.materials[2 * mi + 1];
         pack_gbuffer(ng, T, v3(m0.x, m0.y, m0.z), v3(m1.x, m1.y, m1.z), m0.w, g);
@@ -587,6 +610,11 @@ void launch_camera(const LaunchCfg& lc, cudaStream_t st, const DevView* views, u
     if (blocks == 0) blocks = 1;
     k_camera<<<blocks, lc.block_shade, 0, st>>>(views, n_views, path_begin, path_count, wf, max_segments);
 }
+void launch_gather_normals(cudaStream_t st, const CwTri* tris, uint32_t n, const float* vn, const uint32_t* idx,
+                           float4* out) {
+    if (n) k_gather_normals<<<(n + 255) / 256, 256, 0, st>>>(tris, n, vn, idx, out);
+}
+
 void launch_extend(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, const Wavefront& wf, int q,
                    uint32_t seg, bool count_traversal) {
 #define BSM_EXTEND(C, B, O)                                                                                    \

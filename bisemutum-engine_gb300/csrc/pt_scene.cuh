@@ -48,4 +48,19 @@ __device__ __forceinline__ void hit_geometry(const DevScene& sc, uint32_t leaf, 
     if (material >= sc.num_materials) material = 0;
 }
 
+// The shading normal of a hit on a scene that carries vertex normals.  The
+// reference's fetch_vertex_attributes (bisemutum/shaders/core/raytracing/
+// hit.hlsl:55-71, 158) interpolates n0 + (n1 - n0) b1 + (n2 - n0) b2, b1 and b2
+// the barycentric weights of the second and third vertex, and normalises the
+// result.  A hit's (u, v) are the weights of the first and second vertex, so
+// b1 = v and b2 = 1 - u - v.  A zero interpolated normal falls back to `ng`.
+__device__ __forceinline__ V3 shading_normal(const DevScene& sc, uint32_t leaf, float u, float v, V3 ng) {
+    const float4* np = sc.tri_normals + 3 * (size_t)leaf;
+    const float4 a = np[0], b = np[1], c = np[2];
+    const V3 n0 = v3(a.x, a.y, a.z), n1 = v3(b.x, b.y, b.z), n2 = v3(c.x, c.y, c.z);
+    const float b1 = v, b2 = 1.0f - u - v;
+    V3 n = n0 + (n1 - n0) * b1 + (n2 - n0) * b2;
+    return dot(n, n) > 0.0f ? normalize(n) : ng;
+}
+
 }  // namespace bsm

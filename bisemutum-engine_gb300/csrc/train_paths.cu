@@ -89,6 +89,11 @@ __global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevVi
         uint32_t mi;
         hit_geometry(sc, leaf, inst, N, edge, mi);
         if (dot(N, d) > 0.0f) N = -N;
+        const V3 Ng = N;
+        if (sc.tri_normals) {
+            N = shading_normal(sc, leaf, hu, hv, N);
+            if (dot(N, d) > 0.0f) N = -N;
+        }
         V3 P = o + d * t;
         float4 m0 = sc.materials[2 * mi], m1 = sc.materials[2 * mi + 1];
         Surface surf;
@@ -110,7 +115,7 @@ __global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevVi
         tv.thr[vk] = make_float4(thr.x, thr.y, thr.z, 0.0f);
         tv.rad[vk] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         Frame fr = create_frame(N);
-        V3 org = P + N * sc.ray_offset;
+        V3 org = P + Ng * sc.ray_offset;
         float u_sky0 = pcg_uniform(g), u_sky1 = pcg_uniform(g), u_sky2 = pcg_uniform(g), u_lobe = pcg_uniform(g),
               u_b0 = pcg_uniform(g), u_b1 = pcg_uniform(g);
         float rx, ry;

@@ -184,6 +184,10 @@ typedef struct bsm_scene_desc {
     const bsm_point_light* point_lights;
     uint32_t num_rect_lights;
     const bsm_rect_light* rect_lights;
+    const float* normals;             /* 3 * num_vertices vertex normals (world space, any length), or NULL:
+                                         hits shade with the interpolated, normalised vertex normal
+                                         (hit.hlsl:55-71, 158), else with the geometric normal; either is
+                                         faced towards the ray */
 } bsm_scene_desc;
 
 enum { BSM_COLLAPSE_SAH_OPTIMAL = 0, BSM_COLLAPSE_GREEDY = 1 };
@@ -347,6 +351,8 @@ typedef struct bsm_tune_result {
     float default_ms;             /* ... with the built-in defaults */
     uint32_t tried;               /* configurations timed (0 when read from the cache file) */
     uint32_t from_cache;
+    float worst_ms;               /* ... with the slowest configuration timed (what a bad choice costs) */
+    uint32_t reserved;
 } bsm_tune_result;
 
 /* Picks block size, queue capacity and traversal stack budget for a scene and
@@ -568,7 +574,8 @@ BSM_API bsm_status bsm_cache_load(bsm_cache* cache, const char* path);
 
 /* One frame with the cache: optionally trains on `train_paths` fresh full-length
  * paths of this camera, then renders with paths terminated into the cache at
- * `cache_segment` (settings->max_segments is ignored).  `train_loss` may be NULL. */
+ * `cache_segment` (settings->max_segments is ignored).  `train_loss` may be NULL.
+ * stats->ms_total is the device time of the whole frame, training included. */
 BSM_API bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, const bsm_camera* camera,
                                      const bsm_pt_settings* settings, bsm_cache* cache,
                                      const bsm_cache_settings* cache_settings, const bsm_view_output* output,

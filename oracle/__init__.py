@@ -33,7 +33,7 @@ def lib() -> C.CDLL:
         path = _b.build_oracle()
         L = C.CDLL(path)
         vp, u32, u64, f32, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_int
-        L.orc_scene_create.argtypes = [vp, u32, vp, u32, vp, vp, u32, vp, u32, u32, vp, u32, u32, vp, vp,
+        L.orc_scene_create.argtypes = [vp, u32, vp, u32, vp, vp, u32, vp, u32, u32, vp, u32, u32, vp, vp, vp,
                                        C.POINTER(vp)]
         L.orc_scene_create.restype = i32
         L.orc_scene_destroy.argtypes = [vp]
@@ -62,6 +62,8 @@ def lib() -> C.CDLL:
         L.orc_scene_create_instanced.restype = i32
         L.orc_sky_sample.argtypes = [vp, vp, u32, vp]
         L.orc_scene_bvh_nodes.argtypes = [vp]
+        L.orc_light_eval.argtypes = [vp, vp, vp, u32, f32, vp]
+        L.orc_light_eval.restype = i32
         L.orc_cwbvh_trace.argtypes = [vp, u64, vp, u64, vp, u32, i32, vp, vp, i32]
         L.orc_cwbvh_trace.restype = i32
         L.orc_scene_bvh_nodes.restype = u32
@@ -79,7 +81,7 @@ def ref_lib() -> C.CDLL | None:
             return None
         R = C.CDLL(path)
         for fn in ("ref_eval_lit", "ref_vndf", "ref_frame", "ref_aniso", "ref_samplers", "ref_gbuffer",
-                   "ref_gbuffer_unpack"):
+                   "ref_gbuffer_unpack", "ref_point_light", "ref_dir_light"):
             getattr(R, fn).argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
         R.ref_inv_pi.restype = C.c_float
         _ref = R
@@ -140,11 +142,14 @@ class OracleScene:
         lights = light_rows(scene)
         color = _f32(scene.sky_color)
         tex, sw, sh, sxf = sky_args(scene)
+        nrm = getattr(scene, "normals", None)
+        nrm = None if nrm is None else _f32(nrm).reshape(-1, 3)
         h = C.c_void_p()
         st = L.orc_scene_create(pos.ctypes.data, pos.shape[0], None if idx is None else idx.ctypes.data,
                                 mids.shape[0], mids.ctypes.data, mats.ctypes.data, mats.shape[0],
                                 lights.ctypes.data, lights.shape[0], scene.sky_kind, color.ctypes.data,
-                                sw, sh, None if tex is None else tex.ctypes.data, sxf.ctypes.data, C.byref(h))
+                                sw, sh, None if tex is None else tex.ctypes.data, sxf.ctypes.data,
+                                None if nrm is None else nrm.ctypes.data, C.byref(h))
         if st != 0:
             raise RuntimeError("orc_scene_create failed")
         self.h = h
@@ -251,6 +256,19 @@ def cwbvh_trace(nodes: np.ndarray, tris: np.ndarray, rays: np.ndarray, any_hit: 
     if st != 0:
         raise RuntimeError("orc_cwbvh_trace failed")
     return hits, cnt
+
+
+def light_eval(row, P, u=None, ray_len: float = 100.0) -> np.ndarray:
+    """Next-event sample of one light (a 16-float row: kind, then its fields as light_rows() lays them out) from
+    points P (n, 3): (n, 8) = arriving radiance, direction to the light, shadow-ray length, reached (0/1)."""
+    row = _f32(row).reshape(16)
+    P = _f32(P).reshape(-1, 3)
+    uu = None if u is None else _f32(u).reshape(-1, 2)
+    out = np.zeros((P.shape[0], 8), np.float32)
+    if lib().orc_light_eval(row.ctypes.data, P.ctypes.data, None if uu is None else uu.ctypes.data, P.shape[0],
+                            ray_len, out.ctypes.data) != 0:
+        raise RuntimeError("orc_light_eval failed")
+    return out
 
 
 def pcg32(initstate: int, initseq: int, n: int) -> np.ndarray:

@@ -5,12 +5,14 @@
   rounds exactly like the CUDA kernels.
 * ``oracle/_ref/libref_bsdf.so`` — only where the reference tree is present:
   the reference's own shader math (math.hlsl, material/utils.hlsl,
-  material/lit.hlsl, utils/frame.hlsl, utils/sampling.hlsl, and the G-buffer
-  packing functions of utils/pack.hlsl and renderer/gbuffer.hlsl) compiled
+  material/lit.hlsl, utils/frame.hlsl, utils/sampling.hlsl, the G-buffer
+  packing functions of utils/pack.hlsl and renderer/gbuffer.hlsl, and the
+  light evaluation of renderer/lights.hlsl with its light structs) compiled
   with g++ through ``ref_shim/hlsl_shim.h``.  The sources are read in place;
   the only rewrite is ``out T x`` / ``inout T x`` -> ``T& x`` (HLSL output
-  parameters); of pack.hlsl and gbuffer.hlsl only the named functions and
-  structs are taken (the rest of those files uses HLSL the shim lacks).
+  parameters); of pack.hlsl, gbuffer.hlsl, lights_struct.hlsl and lights.hlsl
+  only the named functions and structs are taken (the rest of those files uses
+  HLSL the shim lacks: textures, samplers, the LTC integrals).
   The generated translation unit and the library stay under ``oracle/_ref/``,
   which is not committed.
 """
@@ -39,6 +41,8 @@ REF_EXTRACTS = [
      ["pack_u32_to_unorm16x2", "unpack_u32_from_unorm16x2", "pack_color_rg11b10", "unpack_color_rg11b10",
       "oct_wrap", "oct_encode", "oct_decode", "pack_normal_and_tangent", "unpack_normal_and_tangent"]),
     ("bisemutum/shaders/renderer/gbuffer.hlsl", ["GBuffer", "pack_surface_to_gbuffer", "unpack_gbuffer_to_surface"]),
+    ("bisemutum/shaders/renderer/lights_struct.hlsl", ["DirLightData", "PointLightData"]),
+    ("bisemutum/shaders/renderer/lights.hlsl", ["dir_light_eval", "point_light_eval"]),
 ]
 # -O3 without -march=native (the same build on x86 and Arm hosts) and without fast-math or FMA contraction:
 # IEEE float semantics at every optimisation level, so results equal the kernels'

@@ -240,7 +240,8 @@ static float mix_pdf(F3 lv, F3 ll, float rx, float ry, float ps) {
 }
 
 // ------------------------------------------------------------- scene ----
-struct Tri { F3 a, b, c; uint32_t prim, mat; float tr; };  // tr: transparency of the any-hit rule (0 = opaque)
+// tr: transparency of the any-hit rule (0 = opaque); na..nc: vertex normals where the scene has them (has_n)
+struct Tri { F3 a, b, c; uint32_t prim, mat; float tr; F3 na, nb, nc; uint32_t has_n; };
 struct BNode { float lo[3], hi[3]; uint32_t left_or_first, count; uint32_t axis; };  // count > 0: leaf
 
 struct Scene {
@@ -550,6 +551,18 @@ static void hit_geom(const Scene& S, uint32_t leaf, uint32_t inst, F3& ng, F3& e
     if (mat >= S.nmat) mat = 0;
 }
 
+// Shading normal of a hit on a triangle with vertex normals (hit.hlsl:55-71, 158): n0 + (n1 - n0) b1 +
+// (n2 - n0) b2 normalised, b1 = v and b2 = 1 - u - v the weights of the second and third vertex; a zero
+// interpolated normal keeps ng.  Single-level scenes only (a two-level hit keeps its geometric normal).
+static F3 shade_normal(const Scene& S, uint32_t leaf, uint32_t inst, float u, float v, F3 ng) {
+    if (inst != UINT32_MAX) return ng;
+    const Tri& T = S.tris[leaf];
+    if (!T.has_n) return ng;
+    float b1 = v, b2 = 1.0f - u - v;
+    F3 n = add(add(T.na, muls(sub(T.nb, T.na), b1)), muls(sub(T.nc, T.na), b2));
+    return dot3(n, n) > 0.0f ? norm3(n) : ng;
+}
+
 // ------------------------------------------------------------------ sky ----
 static F3 texel(const Scene& S, uint32_t i, uint32_t j) {
     const uint16_t* t = &S.texels[((size_t)i * S.sw + j) * 4];
@@ -772,7 +785,8 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                 uint32_t mat;
                 hit_geom(S, hit, hinst, ng, edge, mat);
                 if (dot3(ng, d) > 0.0f) ng = neg(ng);
-                F3 N = ng;
+                F3 N = shade_normal(S, hit, hinst, u, v, ng);
+                if (dot3(N, d) > 0.0f) N = neg(N);
                 F3 P = add(q.o[i], muls(d, t));
                 const float* m = &S.mats[8 * (size_t)mat];
                 Surf surf{f3(m[0], m[1], m[2]), f3(m[4], m[5], m[6]), f3(1, 1, 1), m[3], 1.5f};
@@ -781,7 +795,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                 Pcg g = q.rng[i];
                 float us0 = pcg_uniform(g), us1 = pcg_uniform(g), us2 = pcg_uniform(g), ul = pcg_uniform(g),
                       ub0 = pcg_uniform(g), ub1 = pcg_uniform(g);
-                F3 org = add(P, muls(N, S.offset));
+                F3 org = add(P, muls(ng, S.offset));
                 float rx, ry;
                 aniso_rough(surf.rough, &rx, &ry);
                 F3 lv = local_of(fr, V);
@@ -864,7 +878,7 @@ using namespace orc;
 
 // Triangles and the binary BVH of a mesh (a scene's or a two-level geometry's).
 static void build_geometry(Scene* S, const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
-                           const uint32_t* mat_ids) {
+                           const uint32_t* mat_ids, const float* normals = nullptr) {
     std::vector<BuildRef> refs(nt);
     std::vector<Tri> soup(nt);
     for (uint32_t t = 0; t < nt; ++t) {
@@ -877,6 +891,12 @@ static void build_geometry(Scene* S, const float* pos, uint32_t nv, const uint32
         T.prim = t;
         T.mat = mat_ids ? mat_ids[t] : 0;
         T.tr = 0.0f;
+        T.has_n = normals ? 1u : 0u;
+        if (normals) {
+            T.na = f3(normals[3 * v[0]], normals[3 * v[0] + 1], normals[3 * v[0] + 2]);
+            T.nb = f3(normals[3 * v[1]], normals[3 * v[1] + 1], normals[3 * v[1] + 2]);
+            T.nc = f3(normals[3 * v[2]], normals[3 * v[2] + 1], normals[3 * v[2] + 2]);
+        }
         BuildRef& R = refs[t];
         const F3 vs[3] = {T.a, T.b, T.c};
         for (int k = 0; k < 3; ++k) {
@@ -1024,13 +1044,13 @@ static bool setup_shading(Scene* S, const float* materials, uint32_t nm, const f
 ORC_API int orc_scene_create(const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt, const uint32_t* mat_ids,
                              const float* materials, uint32_t nm, const float* lights, uint32_t nl, uint32_t sky_kind,
                              const float* sky_color, uint32_t sky_w, uint32_t sky_h, const uint16_t* sky_texels,
-                             const float* sky_xf, void** out) {
+                             const float* sky_xf, const float* normals, void** out) {
     if (!pos || !nt || !materials || !nm || !out || nl > 8) return -1;
     Scene* S = new Scene();
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint32_t i = 0; i < nv; ++i)
         for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], pos[3 * i + k]); hi[k] = std::max(hi[k], pos[3 * i + k]); }
-    build_geometry(S, pos, nv, idx, nt, mat_ids);
+    build_geometry(S, pos, nv, idx, nt, mat_ids, normals);
     if (!setup_shading(S, materials, nm, lights, nl, sky_kind, sky_color, sky_w, sky_h, sky_texels, sky_xf, lo, hi)) {
         delete S;
         return -1;
@@ -1309,6 +1329,8 @@ ORC_API int orc_primary(void* sp, const float* camera, float ray_length, float t
                     uint32_t mi;
                     hit_geom(S, h, hi, ng, edge, mi);
                     if (dot3(ng, dw) > 0.0f) ng = neg(ng);
+                    ng = shade_normal(S, h, hi, u, v, ng);
+                    if (dot3(ng, dw) > 0.0f) ng = neg(ng);
                     F3 tan = norm3(edge);
                     const float* m = S.mats.data() + 8 * (size_t)mi;
                     gbuffer_pack(ng, tan, f3(m[0], m[1], m[2]), f3(m[4], m[5], m[6]), m[3], g);
@@ -1393,6 +1415,26 @@ ORC_API void orc_sky_sample(void* sp, const float* u, uint32_t n, float* out) {
 }
 
 ORC_API uint32_t orc_scene_bvh_nodes(void* sp) { return (uint32_t)((Scene*)sp)->nodes.size(); }
+
+// The next-event sample of one light (a 16-float row as the scene takes it) from n points P (3 floats each),
+// with the uniforms (u0, u1) of rect lights: out 8 floats per point = arriving radiance (3), direction to the
+// light (3), shadow-ray length, 1 when the light reaches P.  The render's own light_sample.
+ORC_API int orc_light_eval(const float* row, const float* P, const float* u, uint32_t n, float ray_len, float* out) {
+    Scene S;
+    const float mat[7] = {0.5f, 0.5f, 0.5f, 0.5f, 0.0f, 1.0f, 0.0f};
+    const float col[3] = {0.0f, 0.0f, 0.0f}, lo[3] = {0.0f, 0.0f, 0.0f}, hi[3] = {1.0f, 1.0f, 1.0f};
+    if (!setup_shading(&S, mat, 1, row, 1, 0, col, 0, 0, nullptr, nullptr, lo, hi)) return 1;
+    for (uint32_t i = 0; i < n; ++i) {
+        F3 dir{0, 0, 0}, e{0, 0, 0};
+        float tmax = 0.0f;
+        bool lit = light_sample(S.lights[0], f3(P[3 * i], P[3 * i + 1], P[3 * i + 2]), u ? u[2 * i] : 0.0f,
+                                u ? u[2 * i + 1] : 0.0f, ray_len, dir, tmax, e);
+        float* o = out + 8 * (size_t)i;
+        o[0] = e.x; o[1] = e.y; o[2] = e.z; o[3] = dir.x; o[4] = dir.y; o[5] = dir.z; o[6] = tmax;
+        o[7] = lit ? 1.0f : 0.0f;
+    }
+    return 0;
+}
 
 // ============================================ compressed-BVH traversal ====
 // Restatement of the product's single-ray traversal of its compressed 8-wide

@@ -1,7 +1,8 @@
 // ref_bsdf.cpp — TEST INFRASTRUCTURE: compiles the reference's shader math
 // (bisemutum/shaders/core/utils/math.hlsl, core/material/utils.hlsl,
 // core/material/lit.hlsl, core/utils/frame.hlsl, core/utils/sampling.hlsl,
-// and the G-buffer packing of core/utils/pack.hlsl and renderer/gbuffer.hlsl)
+// the G-buffer packing of core/utils/pack.hlsl and renderer/gbuffer.hlsl, and
+// the light evaluation of renderer/lights.hlsl)
 // through hlsl_shim.h and exposes it to the golden-vector generator.  The
 // sources are read where they lie in the reference tree by oracle/build.py,
 // which only rewrites `out T x` / `inout T x` parameters to `T& x`; the result
@@ -99,5 +100,38 @@ REF_API void ref_gbuffer_unpack(const float* in, uint32_t n, float* out) {
                              s.f0_color.x, s.f0_color.y, s.f0_color.z, s.f90_color.x, s.f90_color.y, s.f90_color.z,
                              s.roughness, s.anisotropy, s.ior, (float)model, 0.0f};
         for (int k = 0; k < 20; ++k) out[20 * (size_t)i + k] = v[k];
+    }
+}
+
+// in: light position3, emission3, range, direction to the light3, cos_inner, cos_outer, P3 (16 floats);
+// out: point_light_eval's radiance (3) and light_dir (3) (renderer/lights.hlsl:15-25).
+REF_API void ref_point_light(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + 16 * (size_t)i;
+        PointLightData L{};
+        L.position = float3(a[0], a[1], a[2]);
+        L.emission = float3(a[3], a[4], a[5]);
+        L.range_sqr_inv = 1.0f / (a[6] * a[6]);
+        L.direction = float3(a[7], a[8], a[9]);
+        L.cos_inner = a[10];
+        L.cos_outer = a[11];
+        float3 dir;
+        float3 e = point_light_eval(L, float3(a[12], a[13], a[14]), dir);
+        float* o = out + 6 * (size_t)i;
+        o[0] = e.x; o[1] = e.y; o[2] = e.z; o[3] = dir.x; o[4] = dir.y; o[5] = dir.z;
+    }
+}
+// in: direction to the light3, emission3, P3; out: dir_light_eval's radiance (3) and light_dir (3)
+// (renderer/lights.hlsl:10-13).
+REF_API void ref_dir_light(const float* in, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = in + 9 * (size_t)i;
+        DirLightData L{};
+        L.direction = float3(a[0], a[1], a[2]);
+        L.emission = float3(a[3], a[4], a[5]);
+        float3 dir;
+        float3 e = dir_light_eval(L, float3(a[6], a[7], a[8]), dir);
+        float* o = out + 6 * (size_t)i;
+        o[0] = e.x; o[1] = e.y; o[2] = e.z; o[3] = dir.x; o[4] = dir.y; o[5] = dir.z;
     }
 }

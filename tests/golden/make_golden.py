@@ -1,15 +1,16 @@
-"""Generates tests/golden/bsdf_golden.npz and gbuffer_golden.npz from the
-reference's own shader math.
+"""Generates tests/golden/bsdf_golden.npz, gbuffer_golden.npz and
+lights_golden.npz from the reference's own shader math.
 
 The reference's material / frame / sampling HLSL files (bisemutum/shaders/core/
 material/utils.hlsl, lit.hlsl, core/utils/frame.hlsl, sampling.hlsl, math.hlsl)
-and its G-buffer packing (renderer/gbuffer.hlsl pack_surface_to_gbuffer with
-the helpers of core/utils/pack.hlsl) are compiled from their sources by
+its G-buffer packing (renderer/gbuffer.hlsl pack_surface_to_gbuffer with the
+helpers of core/utils/pack.hlsl) and its light evaluation (renderer/lights.hlsl
+dir_light_eval and point_light_eval) are compiled from their sources by
 oracle/build.py (through a C++ HLSL shim) and evaluated here on seeded inputs.
 Needs the reference tree; the committed .npz files are what the tests read.
 
-    python tests/golden/make_golden.py            # both files
-    python tests/golden/make_golden.py gbuffer    # one of them
+    python tests/golden/make_golden.py            # all three files
+    python tests/golden/make_golden.py lights     # one of them
 """
 import ctypes as C
 import os
@@ -71,12 +72,50 @@ def gbuffer(R):
     print("wrote", out, os.path.getsize(out), "bytes")
 
 
-def main(which=("bsdf", "gbuffer")):
+def lights(R):
+    """point_light_eval on random point and spot lights (range falloff, spot ramp inside, on the edges of and
+    outside the cone, points beyond the range and nearer than sqrt(0.001)) and dir_light_eval."""
+    rng = np.random.default_rng(20240603)
+    n = 4096
+    pos = rng.uniform(-2.0, 2.0, (n, 3))
+    emis = rng.uniform(0.1, 5.0, (n, 3))
+    rng_ = rng.uniform(0.2, 4.0, (n, 1))
+    axis = unit(rng.normal(size=(n, 3)))
+    outer = rng.uniform(0.1, 1.4, (n, 1))
+    inner = outer * rng.uniform(0.0, 1.0, (n, 1))
+    spot = rng.uniform(size=(n, 1)) < 0.6
+    ci = np.where(spot, np.cos(inner), 0.0)
+    co = np.where(spot, np.cos(outer), 0.0)
+    P = pos + unit(rng.normal(size=(n, 3))) * rng.uniform(0.0, 1.0, (n, 1)) * rng_ * 1.3
+    P[:64] = pos[:64] + unit(rng.normal(size=(64, 3))) * 0.01          # closer than sqrt(0.001)
+    # points on the cone's edges: the direction from the light to P at the inner / outer angle
+    k = slice(64, 192)
+    t = unit(np.cross(axis[k], rng.normal(size=(128, 3))))
+    ang = np.where(np.arange(128)[:, None] % 2 == 0, inner[k], outer[k])
+    d_from_light = -(axis[k] * np.cos(ang) + t * np.sin(ang))          # axis points to the light
+    P[k] = pos[k] + d_from_light * rng.uniform(0.1, 1.0, (128, 1)) * rng_[k]
+    spot[k] = True
+    ci[k], co[k] = np.cos(inner[k]), np.cos(outer[k])
+    pin = np.concatenate([pos, emis, rng_, axis, ci, co, P, np.zeros((n, 1))], 1).astype(np.float32)
+    pout = np.zeros((n, 6), np.float32)
+    R.ref_point_light(pin.ctypes.data, n, pout.ctypes.data)
+    din = np.concatenate([unit(rng.normal(size=(256, 3))), rng.uniform(0.0, 4.0, (256, 3)),
+                          rng.uniform(-1, 1, (256, 3))], 1).astype(np.float32)
+    dout = np.zeros((256, 6), np.float32)
+    R.ref_dir_light(din.ctypes.data, 256, dout.ctypes.data)
+    out = os.path.join(HERE, "lights_golden.npz")
+    np.savez_compressed(out, point_in=pin, point_out=pout, dir_in=din, dir_out=dout)
+    print("wrote", out, os.path.getsize(out), "bytes")
+
+
+def main(which=("bsdf", "gbuffer", "lights")):
     R = oracle.ref_lib()
     if R is None:
         raise SystemExit("reference tree not present: cannot regenerate the golden vectors")
     if "gbuffer" in which:
         gbuffer(R)
+    if "lights" in which:
+        lights(R)
     if "bsdf" not in which:
         return
     rng = np.random.default_rng(20240601)
@@ -125,4 +164,4 @@ def main(which=("bsdf", "gbuffer")):
 
 if __name__ == "__main__":
     R_ = C  # keep ctypes imported for the loaded library's argtypes
-    main(tuple(sys.argv[1:]) or ("bsdf", "gbuffer"))
+    main(tuple(sys.argv[1:]) or ("bsdf", "gbuffer", "lights"))

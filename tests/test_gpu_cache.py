@@ -121,40 +121,68 @@ def test_save_load_roundtrip(bsm, ctx, cache, tmp_path):
         other.close()
 
 
-def test_trained_cache_gains_over_the_method_without_it(bsm, ctx):
-    """Paths end at their third vertex in both renders; with the trained network
-    that vertex contributes the learned outgoing radiance, without it (a network
-    whose output layer is zero) it contributes nothing.  The trained cache must be
-    much closer to a 512-spp plain render (relMSE with the largest 0.1 % of the
-    errors dropped)."""
+def test_trained_cache_beats_the_plain_tracer_at_equal_device_time(bsm, ctx):
+    """The gain the learned part brings over the method without it: the plain full-length tracer.  In the
+    room scene (light reaches most points over several bounces) the cache, trained online for 60 frames,
+    renders frames whose device time (training step included) is at most the plain pass's, with a lower relMSE
+    against a 1024-spp plain render: untrimmed, averaged over three seeds."""
     scene = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=41, spheres=24)
     sid = ctx.load_scene(scene)
-    cam = bsm.make_camera(tuple(scene.camera.position), tuple(scene.camera.front), width=96, height=96)
-    refs, rst = ctx.render(sid, [cam], bsm.settings(spp=512, max_segments=8, seed=1000))
+    cam = bsm.make_camera(tuple(scene.camera.position), tuple(scene.camera.front), width=256, height=256)
+    ctx.render(sid, [cam], bsm.settings(spp=256, max_segments=8, seed=1000, accumulate=0), outputs=False)
+    for k in range(3):
+        refs, _ = ctx.render(sid, [cam], bsm.settings(spp=256, max_segments=8, seed=1000, accumulate=1),
+                             outputs=k == 2)
     ref = refs[0]
-    assert rst.rays_per_segment[1] > 0
     c = bsm.RadianceCache(ctx, seed=5)
-    off = bsm.RadianceCache(ctx, seed=5)
     try:
-        w = off.weights()
-        w[4 * 4096:] = 0.0
-        off.weights(w)
-        cs = bsm.cache_settings(train_paths=16384, train_batch=8192, train_steps=2, cache_segment=2)
-        losses = [c.render(sid, cam, bsm.settings(spp=1, seed=f + 1), cs, outputs=False)[2] for f in range(60)]
-        cs_eval = bsm.cache_settings(train_steps=0, cache_segment=2)
-        cached, st, _ = c.render(sid, cam, bsm.settings(spp=64, seed=77), cs_eval)
-        without, _, _ = off.render(sid, cam, bsm.settings(spp=64, seed=77), cs_eval)
-        # trimmed relMSE: a single firefly shared by both renders (same paths up to the cache vertex)
-        # otherwise decides the comparison
-        e_cached = bsm.rel_mse(cached, ref, trim=0.001)
-        e_without = bsm.rel_mse(without, ref, trim=0.001)
-        assert np.isfinite(cached).all()
-        assert st.rays_per_segment[3] == 0           # no path goes past the cache vertex
-        assert np.mean(losses[-10:]) < np.mean(losses[:10])
-        assert e_cached < 0.5 * e_without, (e_cached, e_without)
+        cs = bsm.cache_settings(cache_segment=2)
+        for f in range(60):
+            c.render(sid, cam, bsm.settings(spp=1, seed=f + 1), cs, outputs=False)
+        seeds = (77, 177, 277)
+
+        def plain(spp):
+            out = [ctx.render(sid, [cam], bsm.settings(spp=spp, max_segments=8, seed=sd)) for sd in seeds]
+            return np.mean([bsm.rel_mse(im[0], ref) for im, _ in out]), np.mean([st.ms_total for _, st in out])
+
+        def cached(spp):
+            out = [c.render(sid, cam, bsm.settings(spp=spp, seed=sd), cs) for sd in seeds]   # trains, then renders
+            return np.mean([bsm.rel_mse(im, ref) for im, _, _ in out]), np.mean([st.ms_total for _, st, _ in out])
+
+        plain(16)
+        e_plain, t_plain = plain(16)
+        spp_c, e_c, t_c = None, None, None
+        for spp in (4, 8, 16, 32):
+            cached(spp)
+            e, t = cached(spp)
+            if t <= t_plain:
+                spp_c, e_c, t_c = spp, e, t
+        assert spp_c is not None, ("no cached frame as fast as the plain one", t_plain)
+        assert e_c < e_plain, (spp_c, e_c, t_c, e_plain, t_plain)
     finally:
         c.close()
-        off.close()
+    ctx.release(sid)
+
+
+def test_smooth_hits_continue_past_the_cache_segment(bsm, ctx):
+    """min_roughness / extra_segments: hits of the cache segment smoother than the threshold shade and
+    continue; the last allowed segment queries the cache whatever its roughness, so no path goes further."""
+    scene = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=41, spheres=24)
+    sid = ctx.load_scene(scene)
+    cam = bsm.make_camera(tuple(scene.camera.position), tuple(scene.camera.front), width=64, height=64)
+    c = bsm.RadianceCache(ctx, seed=6)
+    try:
+        base = bsm.cache_settings(cache_segment=2, train_steps=0)
+        _, st0, _ = c.render(sid, cam, bsm.settings(spp=4, seed=3), base)
+        assert st0.rays_per_segment[3] == 0
+        gated = bsm.cache_settings(cache_segment=2, train_steps=0, min_roughness=0.5, extra_segments=2)
+        img, st1, _ = c.render(sid, cam, bsm.settings(spp=4, seed=3), gated)
+        assert list(st1.rays_per_segment[:3]) == list(st0.rays_per_segment[:3])   # same prefix
+        assert st1.rays_per_segment[3] > 0 and st1.rays_per_segment[5] == 0
+        assert np.isfinite(img).all()
+    finally:
+        c.close()
+    ctx.release(sid)
 
 
 def test_renders_read_the_corrected_moving_average(bsm, ctx):
