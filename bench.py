@@ -196,15 +196,14 @@ def peaks():
 
 
 def profile_traffic():
-    """Per-ray DRAM traffic of the extend kernel from the committed ncu summary, if any, and the summary's
-    issue-slot use (the bound of an issue-limited traversal) and its measured L2 traffic."""
+    """The extend kernel's DRAM bytes per ray (primary and bounce launches), issue-slot use and L2 traffic from
+    the last ncu capture committed under profiles/ (a file, not a measurement of this run), or None."""
     path = os.path.join(ROOT, "profiles", "k_extend_traffic.json")
     try:
         with open(path) as f:
-            j = json.load(f)
-        return float(j["dram_bytes_per_ray"]), j.get("source", path), j.get("issue"), j.get("l2")
-    except (OSError, KeyError, ValueError):
-        return None, None, None, None
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
 
 
 # -------------------------------------------------------------- CPU legs ----
@@ -363,20 +362,28 @@ def run_ours(a, dist: Dist):
         per_launch_rays = rays / max(1, a.steps * ext_launches)
         per_launch_ms = ms_ext / max(1, a.steps * ext_launches)
         achieved = EXTEND_BYTES_PER_RAY * rays / (ms_ext / 1e3) / 1e9 if ms_ext > 0 else None
-        traffic_per_ray, traffic_src, issue, l2_ncu = profile_traffic()
+        prof = profile_traffic()
+        traffic = None
+        if prof:
+            # per launch: segment 0's rays at the primary launch's bytes per ray, the others at the bounce figure
+            b0, b1 = prof["dram_bytes_per_ray_primary"], prof["dram_bytes_per_ray_bounce"]
+            traffic = round((b0 * seg_rays[0] + b1 * sum(seg_rays[1:])) / max(1, ext_launches))
         roofline = {"bound": "hbm", "kernel": "k_extend", "achieved": round(achieved, 2) if achieved else None,
                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5) if achieved else None,
                     "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                    "traffic": round(traffic_per_ray * per_launch_rays) if traffic_per_ray else None,
-                    "traffic_source": traffic_src,
+                    "traffic": traffic,
+                    "traffic_source": (f"last ncu capture (commit {prof['captured_at_commit']}, {prof['capture']}): "
+                                       f"{prof['dram_bytes_per_ray_primary']} B/ray on primary and "
+                                       f"{prof['dram_bytes_per_ray_bounce']} B/ray on bounce launches, weighted by "
+                                       f"this frame's rays per segment") if prof else None,
                     "algorithmic_bytes_per_launch": round(EXTEND_BYTES_PER_RAY * per_launch_rays),
                     "avg_launch_ms": round(per_launch_ms, 4),
                     "l2_traversal_gbs": round((NODE_BYTES * nodes_per_ray + TRI_BYTES * tris_per_ray) * rays /
                                               (ms_ext / 1e3) / 1e9, 1) if ms_ext > 0 else None,
                     "nodes_per_ray": round(nodes_per_ray, 2), "tris_per_ray": round(tris_per_ray, 2),
                     "extend_mrays_per_s_kernel_only": round(rays / (ms_ext / 1e3) / 1e6, 1) if ms_ext > 0 else None,
-                    "l2_ncu": l2_ncu,
-                    "issue": issue}
+                    "from_last_ncu_capture": ({"commit": prof["captured_at_commit"], "l2": prof["l2"],
+                                               "issue": prof["issue"]} if prof else None)}
         cpu = None
         if not a.no_cpu_baseline:
             r = cpu_sample(scene, cam.as_array(), a, a.cpu_seconds)

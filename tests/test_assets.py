@@ -184,19 +184,23 @@ def affine(t, r, s):
     return M
 
 
-def quad_mesh():
-    # two submeshes: a unit quad in y = 0 and a triangle above it
+def quad_mesh(normals=False):
+    # two submeshes: a unit quad in y = 0 and a triangle above it; optionally with bent vertex normals
     pos = np.array([[-1, 0, -1], [1, 0, -1], [1, 0, 1], [-1, 0, 1], [0, 1, 0], [1, 1, 0], [0, 1, 1]], np.float32)
     idx = np.array([0, 2, 1, 0, 3, 2, 0, 1, 2], np.uint32)
-    return {"positions": pos, "indices": idx,
-            "submeshes": np.array([[0, 0, 6, 3], [4, 6, 3, 3]], np.uint32)}
+    m = {"positions": pos, "indices": idx, "submeshes": np.array([[0, 0, 6, 3], [4, 6, 3, 3]], np.uint32)}
+    if normals:
+        n = pos * np.array([0.4, 0.0, 0.4], np.float32) + np.array([0.0, 1.0, 0.0], np.float32)
+        n[4:] = [[0.2, 0.3, 1.0], [-0.3, 0.1, 1.0], [0.1, -0.2, 1.0]]
+        m["normals"] = (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32)
+    return m
 
 
-def write_project(root, bsm):
+def write_project(root, bsm, normals=False):
     os.makedirs(os.path.join(root, "meshes"))
     os.makedirs(os.path.join(root, "materials"))
     with open(os.path.join(root, "meshes", "q.static_mesh.biasset"), "wb") as f:
-        f.write(bsm.write_static_mesh(quad_mesh(), 2))
+        f.write(bsm.write_static_mesh(quad_mesh(normals), 2))
     with open(os.path.join(root, "project.toml"), "w") as f:
         f.write('name = "T"\nasset_metadata_file = "/project/meta.toml"\nscene_file = "/project/scene.toml"\n'
                 'renderer = "BasicRenderer"\n')
@@ -390,6 +394,29 @@ def test_project_loads_into_world_space(bsm, tmp_path):
     assert np.isclose(info.near_z, 0.05) and info.far_z == 500.0
     s = info.settings
     assert (s.max_bounces, s.accumulate, s.ray_length) == (5, 0, 40.0)
+
+
+def test_project_normals_go_to_world_space(bsm, tmp_path):
+    """Vertex normals leave the loader as the inverse transpose of each object's linear transform times the
+    mesh normal (hit.hlsl:158 applies WorldToObject to normals); scale does not matter, direction does."""
+    root = str(tmp_path / "proj")
+    write_project(root, bsm, normals=True)
+    sc, info = bsm.load_project(root)
+    assert sc.normals is not None and sc.normals.shape == sc.positions.shape
+    n = quad_mesh(True)["normals"].astype(np.float64)
+    P = affine([1, 0, 0], [0, 90, 0], [2, 1, 2])
+    Cw = P @ affine([0, 3, 0], [0, 0, 45], [1, 1, 1])
+    unit = lambda v: v / np.linalg.norm(v, axis=-1, keepdims=True)
+    expect_parent = unit(n @ np.linalg.inv(P[:3, :3]))          # (L^-T n)^T = n^T L^-1
+    expect_child = unit(n @ np.linalg.inv(Cw[:3, :3]))
+    got = unit(sc.normals.astype(np.float64))
+    assert np.allclose(got[:7], expect_parent, atol=1e-6)
+    assert np.allclose(got[7:14], expect_child, atol=1e-6)
+    # a project whose meshes have no normals gives none
+    root2 = str(tmp_path / "proj2")
+    write_project(root2, bsm)
+    sc2, _ = bsm.load_project(root2)
+    assert sc2.normals is None
 
 
 def test_project_errors(bsm, tmp_path):

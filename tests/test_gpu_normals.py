@@ -4,19 +4,14 @@ bisemutum/shaders/core/raytracing/hit.hlsl:55-71, 158), on the GPU against the o
 * A scene of UV spheres carrying their analytic vertex normals: closest hits are
   unchanged by the normals; renders take the oracle's paths (equal ray counts
   per segment, radiance within 1e-4); the primary G-buffer's packed normal
-  equals the oracle's bit for bit, follows the sphere's analytic normal closely
-  and differs from the faceted render's.
-* The reference's example project loaded from its files (its meshes carry
-  normals): the GPU render matches the oracle and differs from the same scene
+  equals the oracle's bit for bit and differs from the faceted render's.
+* A project in the reference's format whose mesh carries normals, loaded from
+  its files: the GPU render matches the oracle and differs from the same scene
   shaded with geometric normals."""
-import os
-
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
-
-REF_EXAMPLE = os.path.join(os.environ.get("BSM_REFERENCE_ROOT", "/root/reference"), "examples", "scene_basic")
 
 
 def rel_err(g, c):
@@ -83,7 +78,7 @@ def test_smooth_spheres_match_oracle(bsm, ctx, oracle):
         assert rel_err(imgs[0], ref).max() <= 1e-4
         flat_img, _ = ctx.render(fid, [sc.camera], s)
         assert rel_err(imgs[0], flat_img[0]).max() > 0.05, "vertex normals did not change the shading"
-        # primary G-buffer: packed shading normal bit-exact with the oracle, close to the analytic normal
+        # primary G-buffer: packed shading normal bit-exact with the oracle
         depth, gb, hp = ctx.render_primary(sid, sc.camera)
         od, ogb, ohp = osc.primary(sc.camera.as_array())
         assert np.array_equal(gb, ogb) and np.array_equal(depth, od)
@@ -100,23 +95,29 @@ def test_smooth_spheres_match_oracle(bsm, ctx, oracle):
         ctx.release(fid)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLE), reason="reference example project not present")
-def test_loaded_project_with_normals_matches_oracle(bsm, ctx, oracle):
-    scene, info = bsm.load_project(REF_EXAMPLE)
+def test_loaded_project_with_normals_matches_oracle(bsm, ctx, oracle, tmp_path):
+    """A project in the reference's format whose mesh carries vertex normals (written to a temporary directory):
+    the loader turns them to world space, the GPU render matches the oracle and differs from the same scene
+    shaded with geometric normals."""
+    from test_assets import write_project
+    root = str(tmp_path / "proj")
+    write_project(root, bsm, normals=True)
+    scene, info = bsm.load_project(root)
     assert scene.normals is not None and np.abs(scene.normals).sum() > 0
-    cam = bsm.make_camera(tuple(scene.camera.position), tuple(scene.camera.front), tuple(scene.camera.up),
-                          scene.camera.yfov_deg, width=80, height=60)
+    cam = scene.camera
     sid = ctx.load_scene(scene)
     flat = bsm.SceneData(scene.positions, scene.indices, scene.material_ids, scene.materials, scene.lights,
                          scene.sky_kind, scene.sky_color, scene.sky_texels, cam, point_lights=scene.point_lights,
                          rect_lights=scene.rect_lights)
     fid = ctx.load_scene(flat)
     try:
-        s = bsm.settings(spp=8, max_segments=4, seed=2)
+        s = bsm.settings(spp=8, max_segments=4, seed=2, ray_length=info.settings.ray_length)
         imgs, st = ctx.render(sid, [cam], s)
-        ref, ost, _ = oracle.OracleScene(scene).render(cam.as_array(), spp=8, max_segments=4, seed=2)
+        ref, ost, _ = oracle.OracleScene(scene).render(cam.as_array(), spp=8, max_segments=4, seed=2,
+                                                       ray_length=info.settings.ray_length)
         assert [int(x) for x in st.rays_per_segment[:4]] == [int(x) for x in ost[:4]]
         assert rel_err(imgs[0], ref).max() <= 1e-4
+        assert ref[..., :3].max() > 0.0
         flat_img, _ = ctx.render(fid, [cam], s)
         assert not np.allclose(imgs[0], flat_img[0]), "the project's normals did not reach the shading"
     finally:
