@@ -73,6 +73,7 @@ extern "C" bsm_status bsm_cache_create(bsm_context* ctx, uint64_t seed, bsm_cach
               cudaMalloc((void**)&c->adam_v, kMlpParams * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->dW, kMlpParams * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->loss, kLossSlots * 4) == cudaSuccess &&
+              cudaMalloc((void**)&c->err, 16) == cudaSuccess && cudaMemset(c->err, 0, 16) == cudaSuccess &&
               cudaMalloc((void**)&c->sample_count, 4) == cudaSuccess &&
               cudaMalloc((void**)&c->view_dev, sizeof(DevView)) == cudaSuccess;
     if (!ok) {
@@ -99,7 +100,7 @@ extern "C" void bsm_cache_destroy(bsm_cache* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
-    for (void* p : {(void*)c->w_master, c->w_bf16, (void*)c->w_ema, c->w_ema_bf16, (void*)c->adam_m, (void*)c->adam_v, (void*)c->dW, (void*)c->loss,
+    for (void* p : {(void*)c->w_master, c->w_bf16, (void*)c->w_ema, c->w_ema_bf16, (void*)c->adam_m, (void*)c->adam_v, (void*)c->dW, (void*)c->loss, (void*)c->err,
                     (void*)c->samples, (void*)c->sample_count, (void*)c->view_dev, (void*)c->io, (void*)c->tv_raw,
                     (void*)c->tv_thr, (void*)c->tv_rad, (void*)c->tv_count, c->tv_queue})
         if (p) cudaFree(p);
@@ -143,6 +144,20 @@ extern "C" bsm_status bsm_cache_predict(bsm_cache* c, const float* samples, uint
     return flag ? BSM_ERR_DEVICE_CHECK : BSM_OK;
 }
 
+namespace {
+// Reads and clears the training kernels' error word (after the work on `st`).
+bsm_status take_train_error(bsm_cache* c, cudaStream_t st) {
+    uint32_t flag = 0;
+    if (cudaMemcpyAsync(&flag, c->err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return BSM_ERR_CUDA;
+    if (!flag) return BSM_OK;
+    cudaMemsetAsync(c->err, 0, 4, st);
+    return BSM_ERR_DEVICE_CHECK;
+}
+
+}  // namespace
+
 extern "C" bsm_status bsm_cache_gradient(bsm_cache* c, const float* samples, uint32_t n, float* dW, float* loss) {
     if (!c || !samples || !dW || n == 0) return BSM_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
@@ -151,11 +166,11 @@ extern "C" bsm_status bsm_cache_gradient(bsm_cache* c, const float* samples, uin
     cudaMemcpy(c->io, samples, in_b, cudaMemcpyHostToDevice);
     cudaMemset(c->dW, 0, kMlpParams * 4);
     cudaMemset(c->loss, 0, 4);
-    if (launch_mlp_train(c->device, 0, c->w_bf16, (const float4*)c->io, n, c->dW, c->loss) != cudaSuccess)
+    if (launch_mlp_train(c->device, 0, c->w_bf16, (const float4*)c->io, n, c->dW, c->loss, c->err) != cudaSuccess)
         return BSM_ERR_CUDA;
     if (cudaMemcpy(dW, c->dW, kMlpParams * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BSM_ERR_CUDA;
     if (loss) cudaMemcpy(loss, c->loss, 4, cudaMemcpyDeviceToHost);
-    return BSM_OK;
+    return take_train_error(c, 0);
 }
 
 namespace {
@@ -184,8 +199,8 @@ bsm_status train_device(bsm_cache* c, const float4* samples, uint32_t n, uint32_
         uint32_t nb = std::min(batch, n - off);
         if (slot == 0) cudaMemsetAsync(c->loss, 0, kLossSlots * 4, st);
         cudaMemsetAsync(c->dW, 0, kMlpParams * 4, st);
-        if (launch_mlp_train(c->device, st, c->w_bf16, samples + 4 * (size_t)off, nb, c->dW, c->loss + slot) !=
-            cudaSuccess)
+        if (launch_mlp_train(c->device, st, c->w_bf16, samples + 4 * (size_t)off, nb, c->dW, c->loss + slot,
+                             c->err) != cudaSuccess)
             return BSM_ERR_CUDA;
         c->step++;
         if (ema_decay > 0.0f) c->ema_steps++;
@@ -200,7 +215,7 @@ bsm_status train_device(bsm_cache* c, const float4* samples, uint32_t n, uint32_
     }
     if (!drain(slot)) return BSM_ERR_CUDA;
     if (mean_loss) *mean_loss = steps ? (float)(loss_sum / steps) : 0.0f;
-    return BSM_OK;
+    return take_train_error(c, st);
 }
 }  // namespace
 

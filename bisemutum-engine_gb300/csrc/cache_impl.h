@@ -22,6 +22,7 @@ struct bsm_cache {
     float* adam_v = nullptr;
     float* dW = nullptr;
     float* loss = nullptr;       // device: one loss per Adam step of a training call (kLossSlots)
+    uint32_t* err = nullptr;     // device error word of the training kernels (bit 1: a tensor-core wait timed out)
     float4* samples = nullptr;   // training samples (4 float4 each)
     uint32_t* sample_count = nullptr;
     uint32_t sample_cap = 0;

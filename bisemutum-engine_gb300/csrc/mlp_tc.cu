@@ -17,6 +17,17 @@
 // the next layer's A.  Rounding points and FP32 accumulation are those of the
 // mma.sync training kernels (mlp.cu); only the order of the FP32 sums differs.
 //
+// The training step (k_mlp_train_tc) runs forward and backward passes of
+// 128-sample tiles on the same units.  Its backward products read operands
+// that are stored for the forward ones, in the MN-major form of the same
+// swizzled tiles (no transposed copies):
+//   g_a = g_z W      A: the gradient tile [sample][out], K-major (K = out)
+//                    B: W [out][in] read MN-major (N = in, K = out)
+//   dW += g_z^T a    A: the gradient tile read MN-major (M = out, K = sample)
+//                    B: the activation tile [sample][in] read MN-major
+// with every layer's weight gradient accumulated in tensor memory over all
+// the tiles a CTA takes, and added to the global FP32 gradient at the end.
+//
 // Every mbarrier wait gives up after one second: the kernel then sets bit 1
 // of the error word, stops issuing products and frees its tensor memory.
 #include <cuda_bf16.h>
@@ -45,6 +56,10 @@ static_assert(kTcActOff % 1024 == 0, "swizzled tiles start on 1024-byte boundari
 __host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
+// The same with A (bit 15) and / or B (bit 16) read MN-major.
+__host__ __device__ constexpr uint32_t tc_idesc_mn(int m, int n, bool a_mn, bool b_mn) {
+    return tc_idesc(m, n) | (a_mn ? 1u << 15 : 0u) | (b_mn ? 1u << 16 : 0u);
+}
 
 // Shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading
 // byte offset 16 >> 4 (bits 16-29; not used by swizzled K-major operands),
@@ -54,6 +69,16 @@ __host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
 __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr) {
     return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
            ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// An MN-major operand in the same swizzled tiles: a tile row is one K index
+// holding 64 consecutive M (or N) elements, 8-row K groups lie 1024 bytes
+// apart (stride byte offset), and the leading byte offset steps to the next
+// 64 M elements.  It is 0 here: an M = 128 operand reads its 64 rows twice,
+// and the product's rows 64..127 repeat rows 0..63.
+__device__ __forceinline__ uint64_t tc_sdesc_mn(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) |
+           ((uint64_t)2 << 61);
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -289,6 +314,246 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
     }
 }
 
+// ------------------------------------------------------------- training ----
+// Shared memory of k_mlp_train_tc: the weights (as the forward kernel), the
+// five activation tiles of a 128-sample tile (encoded input e, a0..a3), two
+// gradient tiles that alternate between the backward steps (gy, gz3, gz2, gz1,
+// gz0), one mbarrier and the tensor-memory address (167 KB: one CTA per SM).
+constexpr int kTrTile = kTcRows * 128;                          // 16 KB per 128 x 64 BF16 tile
+constexpr int kTrActOff = kTcWRows * 128;                       // 34816
+constexpr int kTrGradOff = kTrActOff + 5 * kTrTile;             // 116736
+constexpr int kTrBarOff = kTrGradOff + 2 * kTrTile;             // 149504
+// 16 KB beyond the barrier are never written: every operand window of the products
+// (start + 16 rows x 128 bytes per K step, or a whole 16 KB tile read K-major)
+// lies inside the allocation.
+constexpr int kTrSmem = kTrBarOff + 16384 + 1024;
+// Tensor memory: columns 0..63 hold the product being read back (forward z,
+// backward g_a); 64 + 64 l .. 127 + 64 l hold dW_l (l = 0..4; rows = outputs).
+constexpr uint32_t kTrCols = 512;
+constexpr uint32_t kTrDw = 64;
+static_assert(kTrGradOff % 1024 == 0 && kTrBarOff % 1024 == 0, "swizzled tiles start on 1024-byte boundaries");
+static_assert(kTrDw + 5 * 64 <= kTrCols, "tensor-memory columns");
+
+// The 8 chunks of row r of a tile as 64 BF16 values (4 per uint2 pair): used for the ReLU masks.
+__device__ __forceinline__ void load_row(const unsigned char* tile, int r, uint4 (&row)[8]) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) row[c] = *reinterpret_cast<const uint4*>(tile + r * 128 + ((c ^ (r & 7)) << 4));
+}
+
+// g_z = g_a * (a > 0) for 16 columns [16 h, 16 h + 16) of row `tid`, as two BF16 chunks.
+__device__ __forceinline__ void relu_grad_chunks(const uint32_t (&v)[16], const uint4& a0, const uint4& a1,
+                                                 uint4& o0, uint4& o1) {
+    const uint32_t av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+    uint32_t p[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float lo = __uint_as_float(av[i] << 16) > 0.0f ? __uint_as_float(v[2 * i]) : 0.0f;
+        const float hi = __uint_as_float(av[i] & 0xffff0000u) > 0.0f ? __uint_as_float(v[2 * i + 1]) : 0.0f;
+        p[i] = pack2(lo, hi);
+    }
+    o0 = make_uint4(p[0], p[1], p[2], p[3]);
+    o1 = make_uint4(p[4], p[5], p[6], p[7]);
+}
+
+// samples: 4 float4 each (raw inputs in the first three, the target rgb in
+// the fourth).  Adds the gradient of the mean relative L2 loss over the n
+// samples, sum over channels of (y - t)^2 / (y^2 + 0.01) / (3 n) with the
+// denominator held constant, to dW_global, and the loss to loss_out[0].
+// Rounding points: encoded inputs, activations and gradients g_y, g_z in
+// BF16, products in FP32 (those of the oracle's BF16 network).
+__global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16* __restrict__ w,
+                                                             const float4* __restrict__ s, uint32_t n,
+                                                             float* dW_global, float* loss_out, uint32_t* err) {
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t raw_s = smem_u32(smem_raw);
+    const uint32_t base_s = (raw_s + 1023u) & ~1023u;
+    unsigned char* base = smem_raw + (base_s - raw_s);
+    const uint32_t act_s = base_s + kTrActOff, grad_s = base_s + kTrGradOff, bar = base_s + kTrBarOff;
+    unsigned char* act = base + kTrActOff;
+    unsigned char* grad = base + kTrGradOff;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kTrBarOff + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    const uint4* wsrc = reinterpret_cast<const uint4*>(w);
+#pragma unroll
+    for (int j = 0; j < kTcWRows * 8 / kTcRows; ++j) {
+        int i = tid + j * kTcRows, r = i >> 3, c = i & 7;
+        *tile_chunk(base, r, c) = r < kMlpHidden * 64 + kMlpOutPad ? __ldg(wsrc + i) : make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (tid == 0) mbar_init(bar, 1);
+    __syncwarp();
+    if (warp == 0) tc_alloc(smem_u32(tmem_slot), kTrCols);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t rows_tmem = tmem + ((uint32_t)(warp * 32) << 16);
+    const float inv = 1.0f / (3.0f * (float)n);
+    float loss = 0.0f;
+    uint32_t phase = 0;
+    bool failed = false;
+    const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+
+    // one round of products issued by thread 0, then the wait of all threads; false when it timed out
+    auto run = [&](auto issue) -> bool {
+        if (tid == 0) {
+            tc_fence_after();
+            issue();
+            tc_commit(bar);
+        }
+        __syncwarp();
+        const bool done = mbar_wait(bar, phase);
+        phase ^= 1u;
+        __syncwarp();
+        tc_fence_after();
+        return done;
+    };
+    // all threads' shared-memory writes reach the tensor core; true when some thread's wait timed out
+    auto publish = [&](bool done) -> bool {
+        fence_async_smem();
+        tc_fence_before();
+        return __syncthreads_or(!done) != 0;
+    };
+
+    for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const bool first = tile == blockIdx.x;
+        const uint32_t row = tile * kTcRows + tid;
+        float4 tg = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        {
+            float raw[kMlpRaw];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float4 f = row < n ? s[4 * (size_t)row + k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                raw[4 * k] = f.x; raw[4 * k + 1] = f.y; raw[4 * k + 2] = f.z; raw[4 * k + 3] = f.w;
+            }
+            if (row < n) tg = s[4 * (size_t)row + 3];
+            encode_row(raw, act, tid);
+        }
+        if (publish(true)) { failed = true; break; }
+        // forward: act[l + 1] = relu(act[l] W_l^T), y = a3 W4^T
+        float y0 = 0.0f, y1 = 0.0f, y2 = 0.0f;
+        for (int l = 0; l <= kMlpHidden && !failed; ++l) {
+            const bool done = run([&] {
+                const uint32_t w_s = base_s + l * 64 * 128, a_s = act_s + l * kTrTile;
+                const uint32_t idesc = l < kMlpHidden ? tc_idesc(kTcRows, 64) : tc_idesc(kTcRows, kTcW4Rows);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) tc_mma(tmem, tc_sdesc(a_s + 32 * k), tc_sdesc(w_s + 32 * k), idesc, k);
+            });
+            if (l < kMlpHidden) {
+                unsigned char* out = act + (l + 1) * kTrTile;
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    uint32_t v[16];
+                    tc_ld16(rows_tmem + 16 * h, v);
+                    uint32_t p[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        p[i] = pack2(fmaxf(__uint_as_float(v[2 * i]), 0.0f), fmaxf(__uint_as_float(v[2 * i + 1]), 0.0f));
+                    *tile_chunk(out, tid, 2 * h) = make_uint4(p[0], p[1], p[2], p[3]);
+                    *tile_chunk(out, tid, 2 * h + 1) = make_uint4(p[4], p[5], p[6], p[7]);
+                }
+            } else {
+                uint32_t v[16];
+                tc_ld16(rows_tmem, v);
+                y0 = __uint_as_float(v[0]); y1 = __uint_as_float(v[1]); y2 = __uint_as_float(v[2]);
+            }
+            if (publish(done)) failed = true;
+        }
+        if (failed) break;
+        // loss gradient g_y (rows >= n: zero), into gradient tile 0 (chunk 0: channels 0..7; the rest zero)
+        {
+            const float yv[3] = {y0, y1, y2}, tv[3] = {tg.x, tg.y, tg.z};
+            float gy[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float d = yv[c] - tv[c], den = yv[c] * yv[c] + 0.01f;
+                loss += row < n ? d * d / den * inv : 0.0f;
+                gy[c] = row < n ? 2.0f * d / den * inv : 0.0f;
+            }
+            *tile_chunk(grad, tid, 0) = make_uint4(pack2(gy[0], gy[1]), pack2(gy[2], 0.0f), 0u, 0u);
+#pragma unroll
+            for (int c = 1; c < 8; ++c) *tile_chunk(grad, tid, c) = make_uint4(0u, 0u, 0u, 0u);
+        }
+        if (publish(true)) { failed = true; break; }
+        // backward: step L reads gradient tile L & 1 (g_y, then g_z3 .. g_z0), adds dW_L and, for L > 0,
+        // writes g_z(L-1) = (g_in W_L) * (a(L-1) > 0) into the other gradient tile
+        for (int L = kMlpHidden; L >= 0 && !failed; --L) {
+            const uint32_t g_s = grad_s + (uint32_t)((kMlpHidden - L) & 1) * kTrTile;
+            const uint32_t a_s = act_s + L * kTrTile;   // a(L-1): e for L = 0, a3 for L = 4
+            const bool done = run([&] {
+                if (L > 0) {   // g_a = g_in W_L: K = outputs of layer L (16 for the output layer)
+                    const uint32_t w_s = base_s + L * 64 * 128;
+                    const uint32_t idesc = tc_idesc_mn(kTcRows, 64, false, true);
+                    const int ks = L == kMlpHidden ? 1 : 4;
+                    for (int k = 0; k < ks; ++k)
+                        tc_mma(tmem, tc_sdesc(g_s + 32 * k), tc_sdesc_mn(w_s + 2048 * k), idesc, k);
+                }
+                // dW_L += g_in^T a(L-1): M = outputs (rows 64..127 repeat them), K = the 128 samples
+                const uint32_t idesc = tc_idesc_mn(kTcRows, 64, true, true);
+                const uint32_t d = tmem + kTrDw + 64 * (uint32_t)L;
+#pragma unroll
+                for (int k = 0; k < kTcRows / 16; ++k)
+                    tc_mma(d, tc_sdesc_mn(g_s + 2048 * k), tc_sdesc_mn(a_s + 2048 * k), idesc, first && k == 0 ? 0u : 1u);
+            });
+            if (L > 0) {
+                const unsigned char* a_row = act + L * kTrTile;   // the mask of g_z(L-1) is a(L-1) > 0
+                unsigned char* out = grad + (uint32_t)((kMlpHidden - L + 1) & 1) * kTrTile;
+                uint4 ar[8];
+                load_row(a_row, tid, ar);
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    uint32_t v[16];
+                    tc_ld16(rows_tmem + 16 * h, v);
+                    uint4 o0, o1;
+                    relu_grad_chunks(v, ar[2 * h], ar[2 * h + 1], o0, o1);
+                    *tile_chunk(out, tid, 2 * h) = o0;
+                    *tile_chunk(out, tid, 2 * h + 1) = o1;
+                }
+            }
+            if (publish(done)) failed = true;
+        }
+    }
+    // loss: one atomic per warp
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
+    if (lane == 0 && loss != 0.0f) atomicAdd(loss_out, loss);
+    if (failed) {
+        if (tid == 0) {
+            atomicOr(err, kTcErrTimeout);
+            mbar_wait(bar, phase ^ 1u);   // the products of the abandoned round, once more bounded
+        }
+        tc_fence_before();
+    } else if (blockIdx.x < tiles) {
+        tc_fence_after();
+        // weight gradients: TMEM lane o = output o (lanes 64..127 repeat 0..63).  Warps 0, 1 add columns 0..31
+        // of rows 0..63, warps 2, 3 columns 32..63 of the same rows; the output layer has rows 0..2.
+        const uint32_t o = (uint32_t)((warp & 1) * 32 + lane);
+        const uint32_t c0 = warp < 2 ? 0u : 32u;
+        for (int l = 0; l <= kMlpHidden; ++l) {
+            const bool rows_ok = l < kMlpHidden || o < (uint32_t)kMlpOut;
+            float4* dst = reinterpret_cast<float4*>(dW_global + l * kMlpLayerParams + o * 64 + c0);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                uint32_t v[16];
+                tc_ld16(rows_tmem + kTrDw + 64 * (uint32_t)l + c0 + 16 * h, v);
+                if (rows_ok) {
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        atomicAdd(dst + 4 * h + i, make_float4(__uint_as_float(v[4 * i]), __uint_as_float(v[4 * i + 1]),
+                                                               __uint_as_float(v[4 * i + 2]), __uint_as_float(v[4 * i + 3])));
+                }
+            }
+        }
+        tc_fence_before();
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tc_dealloc(tmem, kTrCols);
+    }
+}
+
 // Per device (ordinal < 64): the opt-in shared-memory size is a per-device function attribute.
 std::atomic<uint64_t> g_tc_attr{0};
 int g_tc_grid[64] = {};
@@ -299,6 +564,8 @@ cudaError_t tc_setup(int device) {
         cudaError_t e = cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_mlp_forward_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrSmem);
         if (e != cudaSuccess) return e;
         g_tc_attr.fetch_or(1ull << device);
     }
@@ -319,6 +586,18 @@ cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const 
     if (e != cudaSuccess) return e;
     k_mlp_forward_tc<true><<<g_tc_grid[device], kTcRows, kTcSmem, st>>>((const __nv_bfloat16*)wb, queries, count, capacity,
                                                                 accum, nullptr, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
+                             float* dW, float* loss, uint32_t* err) {
+    cudaError_t e = tc_setup(device);
+    if (e != cudaSuccess) return e;
+    if (n == 0) return cudaSuccess;
+    // one CTA per SM (512 tensor-memory columns, 167 KB of shared memory), 128 samples at a time
+    const uint32_t tiles = (n + kTcRows - 1) / kTcRows, sms = (uint32_t)g_tc_grid[device] / 4;
+    k_mlp_train_tc<<<tiles < sms ? tiles : sms, kTcRows, kTrSmem, st>>>((const __nv_bfloat16*)wb, samples, n, dW, loss,
+                                                                        err);
     return cudaGetLastError();
 }
 

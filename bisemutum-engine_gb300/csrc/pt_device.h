@@ -159,8 +159,10 @@ cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const 
                              uint32_t capacity, float4* accum, uint32_t* err);
 cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
                                float* out, uint32_t* err);
+// gradient of the mean relative L2 loss over n samples added to dW, the loss to loss[0]; a tensor-core wait
+// that timed out sets bit 1 of *err
 cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
-                             float* dW, float* loss);
+                             float* dW, float* loss, uint32_t* err);
 // Adam step; with ema_decay > 0 also updates the weights' moving average `ema` and writes its
 // bias-corrected bf16 copy `ema_b` (ema_step: steps averaged, this one included)
 cudaError_t launch_mlp_adam(cudaStream_t st, float* wm, void* wb, const float* dW, float* m, float* v, float lr,

@@ -42,22 +42,31 @@ __device__ __forceinline__ uint32_t warp_alloc(bool pred, uint32_t* counter) {
 // Queue slots for the threads of a block with `pred`, grouped by the octant of
 // `dir` (one atomic on `counter` per block).  Consecutive slots then hold rays
 // heading the same way from neighbouring paths, which keeps the warps of the
-// next traversal and shading launches coherent.  Every thread of the block
-// must call it (it synchronises the block); returns 0 for threads without pred.
-__device__ __forceinline__ uint32_t block_alloc_by_octant(bool pred, V3 dir, uint32_t* counter) {
-    __shared__ uint32_t s_cnt[9], s_off[8], s_base;
-    if (threadIdx.x < 9) s_cnt[threadIdx.x] = 0u;
-    __syncthreads();
+// next traversal and shading launches coherent.  The lanes of a warp that
+// share an octant take their ranks from one shared-memory atomic.  Every
+// thread of the block must call it with the same `parity`, alternating 0 / 1
+// from call to call, after s_oct_cnt[0] was cleared: each call clears the
+// other parity's counters for the next one, so it needs two block barriers
+// instead of three.  Returns 0 for threads without pred.
+__shared__ uint32_t s_oct_cnt[2][9];
+__device__ __forceinline__ uint32_t block_alloc_by_octant(bool pred, V3 dir, uint32_t* counter, int parity) {
+    __shared__ uint32_t s_off[2][8], s_base[2];
     uint32_t key = pred ? ((dir.x < 0.0f ? 1u : 0u) | (dir.y < 0.0f ? 2u : 0u) | (dir.z < 0.0f ? 4u : 0u)) : 8u;
-    uint32_t rank = atomicAdd(&s_cnt[key], 1u);
+    // one shared atomic per octant present in the warp (the lanes of an octant share it)
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    const uint32_t leader = (uint32_t)__ffs(peers) - 1u;
+    uint32_t rank = 0;
+    if ((threadIdx.x & 31u) == leader && pred) rank = atomicAdd(&s_oct_cnt[parity][key], (uint32_t)__popc(peers));
+    rank = __shfl_sync(0xffffffffu, rank, (int)leader) + (uint32_t)__popc(peers & lanemask_lt());
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t acc = 0;
-        for (int k = 0; k < 8; ++k) { s_off[k] = acc; acc += s_cnt[k]; }
-        s_base = acc ? atomicAdd(counter, acc) : 0u;
+        for (int k = 0; k < 8; ++k) { s_off[parity][k] = acc; acc += s_oct_cnt[parity][k]; }
+        s_base[parity] = acc ? atomicAdd(counter, acc) : 0u;
     }
+    if (threadIdx.x < 9) s_oct_cnt[parity ^ 1][threadIdx.x] = 0u;
     __syncthreads();
-    return pred ? s_base + s_off[key] + rank : 0u;
+    return pred ? s_base[parity] + s_off[parity][key] + rank : 0u;
 }
 
 __device__ __forceinline__ void accum_add(float4* accum, uint32_t idx, V3 c) {
@@ -231,7 +240,10 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
     uint4* out_p = wf.path[q ^ 1];
     float4* out_t = wf.thr[q ^ 1];
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    if (threadIdx.x < 9) s_oct_cnt[0][threadIdx.x] = 0u;
+    __syncthreads();
+    int parity = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride, parity ^= 1) {
         uint32_t i = base + threadIdx.x;
         bool active = i < n;
         float4 o4 = make_float4(0, 0, 0, 0), d4 = make_float4(0, 0, 1, 0), h4 = make_float4(0, 0, 0, 0);
@@ -431,7 +443,7 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
             }
         }
         // the next rays, grouped by octant per block (sorting the sky shadow rays the same way measured no gain)
-        uint32_t slot = block_alloc_by_octant(cont, L, wf.counters + kCntQueue + seg + 1);
+        uint32_t slot = block_alloc_by_octant(cont, L, wf.counters + kCntQueue + seg + 1, parity);
         if (cont) {
             if (slot < cap) {
                 out_o[slot] = make_float4(org.x, org.y, org.z, tmin);
