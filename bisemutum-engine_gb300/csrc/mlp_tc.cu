@@ -157,6 +157,37 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
                  : "memory");
 }
 
+// 64 columns in one load and one wait.
+__device__ __forceinline__ void tc_ld64(uint32_t taddr, uint32_t (&v)[64]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 {"
+                 "%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+                 "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+                 "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63"
+                 "}, [%64];"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                   "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+                   "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+                   "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31]),
+                   "=r"(v[32]), "=r"(v[33]), "=r"(v[34]), "=r"(v[35]), "=r"(v[36]), "=r"(v[37]), "=r"(v[38]), "=r"(v[39]),
+                   "=r"(v[40]), "=r"(v[41]), "=r"(v[42]), "=r"(v[43]), "=r"(v[44]), "=r"(v[45]), "=r"(v[46]), "=r"(v[47]),
+                   "=r"(v[48]), "=r"(v[49]), "=r"(v[50]), "=r"(v[51]), "=r"(v[52]), "=r"(v[53]), "=r"(v[54]), "=r"(v[55]),
+                   "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]), "=r"(v[62]), "=r"(v[63])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                   "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15]),
+                   "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]), "+r"(v[22]), "+r"(v[23]),
+                   "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]), "+r"(v[29]), "+r"(v[30]), "+r"(v[31]),
+                   "+r"(v[32]), "+r"(v[33]), "+r"(v[34]), "+r"(v[35]), "+r"(v[36]), "+r"(v[37]), "+r"(v[38]), "+r"(v[39]),
+                   "+r"(v[40]), "+r"(v[41]), "+r"(v[42]), "+r"(v[43]), "+r"(v[44]), "+r"(v[45]), "+r"(v[46]), "+r"(v[47]),
+                   "+r"(v[48]), "+r"(v[49]), "+r"(v[50]), "+r"(v[51]), "+r"(v[52]), "+r"(v[53]), "+r"(v[54]), "+r"(v[55]),
+                   "+r"(v[56]), "+r"(v[57]), "+r"(v[58]), "+r"(v[59]), "+r"(v[60]), "+r"(v[61]), "+r"(v[62]), "+r"(v[63])
+                 :
+                 : "memory");
+}
+
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
@@ -269,16 +300,16 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
             __syncwarp();   // the tensor-memory loads below are warp-collective
             tc_fence_after();
             if (l < kMlpHidden) {
+                uint32_t v[64];
+                tc_ld64(rows_tmem, v);
 #pragma unroll
-                for (int h = 0; h < 4; ++h) {   // 16 columns = two chunks of the next layer's input
-                    uint32_t v[16];
-                    tc_ld16(rows_tmem + 16 * h, v);
-                    uint32_t p[8];
+                for (int c = 0; c < 8; ++c) {   // 8 columns = one chunk of the next layer's input
+                    uint32_t p[4];
 #pragma unroll
-                    for (int i = 0; i < 8; ++i)
-                        p[i] = pack2(fmaxf(__uint_as_float(v[2 * i]), 0.0f), fmaxf(__uint_as_float(v[2 * i + 1]), 0.0f));
-                    *tile_chunk(act, tid, 2 * h) = make_uint4(p[0], p[1], p[2], p[3]);
-                    *tile_chunk(act, tid, 2 * h + 1) = make_uint4(p[4], p[5], p[6], p[7]);
+                    for (int i = 0; i < 4; ++i)
+                        p[i] = pack2(fmaxf(__uint_as_float(v[8 * c + 2 * i]), 0.0f),
+                                     fmaxf(__uint_as_float(v[8 * c + 2 * i + 1]), 0.0f));
+                    *tile_chunk(act, tid, c) = make_uint4(p[0], p[1], p[2], p[3]);
                 }
             } else {
                 uint32_t v[16];
@@ -334,21 +365,48 @@ constexpr uint32_t kTrDw = 64;
 static_assert(kTrGradOff % 1024 == 0 && kTrBarOff % 1024 == 0, "swizzled tiles start on 1024-byte boundaries");
 static_assert(kTrDw + 5 * 64 <= kTrCols, "tensor-memory columns");
 
+// Bulk reduction of `bytes` (a multiple of 16) FP32 values from shared memory into global memory (element-wise
+// add, performed by the tensor-memory-access unit), tracked by this thread's bulk-async group.
+__device__ __forceinline__ void bulk_reduce_add_f32(float* gdst, uint32_t ssrc, uint32_t bytes) {
+    asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f32 [%0], [%1], %2;" ::"l"(gdst), "r"(ssrc),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit_and_wait() {
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+// r[j] = v[(j + k) mod 8] for k = 0..7 in three conditional rotations (no indexed register access).
+__device__ __forceinline__ void rotate8(uint4 (&r)[8], uint32_t k) {
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        const int sh = 1 << b;
+        const bool on = (k >> b) & 1u;
+        uint4 t[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) t[j] = on ? r[(j + sh) & 7] : r[j];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) r[j] = t[j];
+    }
+}
+
 // The 8 chunks of row r of a tile as 64 BF16 values (4 per uint2 pair): used for the ReLU masks.
 __device__ __forceinline__ void load_row(const unsigned char* tile, int r, uint4 (&row)[8]) {
 #pragma unroll
     for (int c = 0; c < 8; ++c) row[c] = *reinterpret_cast<const uint4*>(tile + r * 128 + ((c ^ (r & 7)) << 4));
 }
 
-// g_z = g_a * (a > 0) for 16 columns [16 h, 16 h + 16) of row `tid`, as two BF16 chunks.
-__device__ __forceinline__ void relu_grad_chunks(const uint32_t (&v)[16], const uint4& a0, const uint4& a1,
+// g_z = g_a * (a > 0) for the 16 columns [c, c + 16) of row `tid` (v: the row's 64 columns of g_a), as two
+// BF16 chunks.
+__device__ __forceinline__ void relu_grad_chunks(const uint32_t (&v)[64], int c, const uint4& a0, const uint4& a1,
                                                  uint4& o0, uint4& o1) {
     const uint32_t av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
     uint32_t p[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const float lo = __uint_as_float(av[i] << 16) > 0.0f ? __uint_as_float(v[2 * i]) : 0.0f;
-        const float hi = __uint_as_float(av[i] & 0xffff0000u) > 0.0f ? __uint_as_float(v[2 * i + 1]) : 0.0f;
+        const float lo = __uint_as_float(av[i] << 16) > 0.0f ? __uint_as_float(v[c + 2 * i]) : 0.0f;
+        const float hi = __uint_as_float(av[i] & 0xffff0000u) > 0.0f ? __uint_as_float(v[c + 2 * i + 1]) : 0.0f;
         p[i] = pack2(lo, hi);
     }
     o0 = make_uint4(p[0], p[1], p[2], p[3]);
@@ -374,6 +432,13 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kTrBarOff + 8);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
+    // this row's sample of the next tile (raw inputs, target), loaded ahead: the first before the weights
+    float4 nx[4];
+    auto fetch = [&](uint32_t row) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) nx[k] = row < n ? s[4 * (size_t)row + k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    };
+    fetch(blockIdx.x * kTcRows + tid);
     const uint4* wsrc = reinterpret_cast<const uint4*>(w);
 #pragma unroll
     for (int j = 0; j < kTcWRows * 8 / kTcRows; ++j) {
@@ -419,15 +484,14 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
     for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
         const bool first = tile == blockIdx.x;
         const uint32_t row = tile * kTcRows + tid;
-        float4 tg = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float4 tg = nx[3];
         {
             float raw[kMlpRaw];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const float4 f = row < n ? s[4 * (size_t)row + k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                raw[4 * k] = f.x; raw[4 * k + 1] = f.y; raw[4 * k + 2] = f.z; raw[4 * k + 3] = f.w;
+                raw[4 * k] = nx[k].x; raw[4 * k + 1] = nx[k].y; raw[4 * k + 2] = nx[k].z; raw[4 * k + 3] = nx[k].w;
             }
-            if (row < n) tg = s[4 * (size_t)row + 3];
+            fetch(row + gridDim.x * kTcRows);
             encode_row(raw, act, tid);
         }
         if (publish(true)) { failed = true; break; }
@@ -442,16 +506,16 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
             });
             if (l < kMlpHidden) {
                 unsigned char* out = act + (l + 1) * kTrTile;
+                uint32_t v[64];
+                tc_ld64(rows_tmem, v);
 #pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    uint32_t v[16];
-                    tc_ld16(rows_tmem + 16 * h, v);
-                    uint32_t p[8];
+                for (int c = 0; c < 8; ++c) {
+                    uint32_t p[4];
 #pragma unroll
-                    for (int i = 0; i < 8; ++i)
-                        p[i] = pack2(fmaxf(__uint_as_float(v[2 * i]), 0.0f), fmaxf(__uint_as_float(v[2 * i + 1]), 0.0f));
-                    *tile_chunk(out, tid, 2 * h) = make_uint4(p[0], p[1], p[2], p[3]);
-                    *tile_chunk(out, tid, 2 * h + 1) = make_uint4(p[4], p[5], p[6], p[7]);
+                    for (int i = 0; i < 4; ++i)
+                        p[i] = pack2(fmaxf(__uint_as_float(v[8 * c + 2 * i]), 0.0f),
+                                     fmaxf(__uint_as_float(v[8 * c + 2 * i + 1]), 0.0f));
+                    *tile_chunk(out, tid, c) = make_uint4(p[0], p[1], p[2], p[3]);
                 }
             } else {
                 uint32_t v[16];
@@ -481,6 +545,8 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
         for (int L = kMlpHidden; L >= 0 && !failed; --L) {
             const uint32_t g_s = grad_s + (uint32_t)((kMlpHidden - L) & 1) * kTrTile;
             const uint32_t a_s = act_s + L * kTrTile;   // a(L-1): e for L = 0, a3 for L = 4
+            uint4 ar[8];                                  // the mask of g_z(L-1) is a(L-1) > 0
+            if (L > 0) load_row(act + L * kTrTile, tid, ar);
             const bool done = run([&] {
                 if (L > 0) {   // g_a = g_in W_L: K = outputs of layer L (16 for the output layer)
                     const uint32_t w_s = base_s + L * 64 * 128;
@@ -497,16 +563,13 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
                     tc_mma(d, tc_sdesc_mn(g_s + 2048 * k), tc_sdesc_mn(a_s + 2048 * k), idesc, first && k == 0 ? 0u : 1u);
             });
             if (L > 0) {
-                const unsigned char* a_row = act + L * kTrTile;   // the mask of g_z(L-1) is a(L-1) > 0
                 unsigned char* out = grad + (uint32_t)((kMlpHidden - L + 1) & 1) * kTrTile;
-                uint4 ar[8];
-                load_row(a_row, tid, ar);
+                uint32_t v[64];
+                tc_ld64(rows_tmem, v);
 #pragma unroll
                 for (int h = 0; h < 4; ++h) {
-                    uint32_t v[16];
-                    tc_ld16(rows_tmem + 16 * h, v);
                     uint4 o0, o1;
-                    relu_grad_chunks(v, ar[2 * h], ar[2 * h + 1], o0, o1);
+                    relu_grad_chunks(v, 16 * h, ar[2 * h], ar[2 * h + 1], o0, o1);
                     *tile_chunk(out, tid, 2 * h) = o0;
                     *tile_chunk(out, tid, 2 * h + 1) = o1;
                 }
@@ -526,26 +589,42 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
         tc_fence_before();
     } else if (blockIdx.x < tiles) {
         tc_fence_after();
-        // weight gradients: TMEM lane o = output o (lanes 64..127 repeat 0..63).  Warps 0, 1 add columns 0..31
-        // of rows 0..63, warps 2, 3 columns 32..63 of the same rows; the output layer has rows 0..2.
+        // weight gradients: TMEM lane o = output o (lanes 64..127 repeat 0..63).  Warps 0, 1 take columns 0..31
+        // of rows 0..63, warps 2, 3 columns 32..63 of the same rows; the output layer has rows 0..2.  They are
+        // written in dW's own layout, FP32 [layer][out][in], over the activation tiles (free now), and added to
+        // dW_global by one bulk reduction per layer.  A lane stores its row's eight 16-byte chunks rotated by
+        // its lane index, so the eight lanes of each store phase hit distinct banks.
         const uint32_t o = (uint32_t)((warp & 1) * 32 + lane);
         const uint32_t c0 = warp < 2 ? 0u : 32u;
+        float* stage = reinterpret_cast<float*>(act);
         for (int l = 0; l <= kMlpHidden; ++l) {
-            const bool rows_ok = l < kMlpHidden || o < (uint32_t)kMlpOut;
-            float4* dst = reinterpret_cast<float4*>(dW_global + l * kMlpLayerParams + o * 64 + c0);
+            uint4 r[8];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 uint32_t v[16];
                 tc_ld16(rows_tmem + kTrDw + 64 * (uint32_t)l + c0 + 16 * h, v);
-                if (rows_ok) {
 #pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        atomicAdd(dst + 4 * h + i, make_float4(__uint_as_float(v[4 * i]), __uint_as_float(v[4 * i + 1]),
-                                                               __uint_as_float(v[4 * i + 2]), __uint_as_float(v[4 * i + 3])));
-                }
+                for (int i = 0; i < 4; ++i) r[4 * h + i] = make_uint4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+            }
+            if (l < kMlpHidden || o < (uint32_t)kMlpOut) {
+                const uint32_t k = (uint32_t)lane & 7u;
+                rotate8(r, k);
+                float* row = stage + l * kMlpLayerParams + o * 64 + c0;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) *reinterpret_cast<uint4*>(row + 4 * ((j + k) & 7u)) = r[j];
             }
         }
         tc_fence_before();
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            for (int l = 0; l < kMlpHidden; ++l)
+                bulk_reduce_add_f32(dW_global + l * kMlpLayerParams, smem_u32(stage + l * kMlpLayerParams),
+                                    kMlpLayerParams * 4);
+            bulk_reduce_add_f32(dW_global + kMlpHidden * kMlpLayerParams, smem_u32(stage + kMlpHidden * kMlpLayerParams),
+                                kMlpOut * 64 * 4);
+            bulk_commit_and_wait();
+        }
     }
     __syncthreads();
     if (warp == 0) {
