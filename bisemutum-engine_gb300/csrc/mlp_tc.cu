@@ -193,6 +193,13 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
+// max(lo, 0) and max(hi, 0) rounded to BF16 in one conversion (cvt.rn.relu); lo in the low half.
+__device__ __forceinline__ uint32_t pack2_relu(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
 // 16-byte chunk c (features 8c..8c+7) of row r of a swizzled 128-row tile.
 __device__ __forceinline__ uint4* tile_chunk(unsigned char* tile, int r, int c) {
     return reinterpret_cast<uint4*>(tile + r * 128 + ((c ^ (r & 7)) << 4));
@@ -307,8 +314,7 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
                     uint32_t p[4];
 #pragma unroll
                     for (int i = 0; i < 4; ++i)
-                        p[i] = pack2(fmaxf(__uint_as_float(v[8 * c + 2 * i]), 0.0f),
-                                     fmaxf(__uint_as_float(v[8 * c + 2 * i + 1]), 0.0f));
+                        p[i] = pack2_relu(__uint_as_float(v[8 * c + 2 * i]), __uint_as_float(v[8 * c + 2 * i + 1]));
                     *tile_chunk(act, tid, c) = make_uint4(p[0], p[1], p[2], p[3]);
                 }
             } else {
@@ -513,8 +519,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
                     uint32_t p[4];
 #pragma unroll
                     for (int i = 0; i < 4; ++i)
-                        p[i] = pack2(fmaxf(__uint_as_float(v[8 * c + 2 * i]), 0.0f),
-                                     fmaxf(__uint_as_float(v[8 * c + 2 * i + 1]), 0.0f));
+                        p[i] = pack2_relu(__uint_as_float(v[8 * c + 2 * i]), __uint_as_float(v[8 * c + 2 * i + 1]));
                     *tile_chunk(out, tid, c) = make_uint4(p[0], p[1], p[2], p[3]);
                 }
             } else {
