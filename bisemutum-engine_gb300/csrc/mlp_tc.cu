@@ -207,16 +207,19 @@ __device__ __forceinline__ uint4* tile_chunk(unsigned char* tile, int r, int c) 
 
 // Encoded features of one query (the encoding of mlp_feature), written as
 // row r of the activation tile: chunk d < 7 holds sin/cos(2^k pi raw[d]),
-// k = 0..3; chunk 7 holds raw[7..11], 1, 0, 0.  Frequencies k > 0 come from
-// k - 1 by the double-angle identities (sin 2a = 2 sin a cos a, cos 2a =
-// (cos a - sin a)(cos a + sin a)); three doublings add a few float ulps,
-// far below the BF16 rounding that follows.
+// k = 0..3; chunk 7 holds raw[7..11], 1, 0, 0.  The base frequency comes from
+// the special-function unit (__sincosf: absolute error below 2^-21 for
+// arguments in [-pi, pi], which pi raw[d] is for the normalised inputs);
+// frequencies k > 0 come from k - 1 by the double-angle identities
+// (sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)(cos a + sin a)).  Both
+// errors lie far below the BF16 rounding that follows; the training and the
+// inference kernels share this encoding.
 __device__ __forceinline__ void encode_row(const float (&raw)[kMlpRaw], unsigned char* act, int r) {
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
         uint32_t p[4];
         float s, c;
-        sincos_turns(raw[d] * 0.5f, &s, &c);
+        __sincosf(raw[d] * 3.14159265f, &s, &c);
         p[0] = pack2(s, c);
 #pragma unroll
         for (int k = 1; k < 4; ++k) {
