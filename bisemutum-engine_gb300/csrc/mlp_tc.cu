@@ -157,6 +157,27 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
                  : "memory");
 }
 
+// 32 columns in one load and one wait.
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {"
+                 "%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31"
+                 "}, [%32];"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                   "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+                   "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+                   "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                   "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15]),
+                   "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]), "+r"(v[22]), "+r"(v[23]),
+                   "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]), "+r"(v[29]), "+r"(v[30]), "+r"(v[31])
+                 :
+                 : "memory");
+}
+
 // 64 columns in one load and one wait.
 __device__ __forceinline__ void tc_ld64(uint32_t taddr, uint32_t (&v)[64]) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 {"
@@ -381,7 +402,7 @@ __device__ __forceinline__ void bulk_reduce_add_f32(float* gdst, uint32_t ssrc, 
                  "r"(bytes)
                  : "memory");
 }
-__device__ __forceinline__ void bulk_commit_and_wait() {
+__device__ __forceinline__ void bulk_wait_all() {
     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
     asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
@@ -420,6 +441,27 @@ __device__ __forceinline__ void relu_grad_chunks(const uint32_t (&v)[64], int c,
     }
     o0 = make_uint4(p[0], p[1], p[2], p[3]);
     o1 = make_uint4(p[4], p[5], p[6], p[7]);
+}
+
+// One layer's weight gradient from tensor memory (dw: this warp's lanes, column 0 of the layer; lane o = output o,
+// lanes 64..127 repeat 0..63) into shared memory as FP32 [out][64] (rows < `rows`).  Warps 0, 1 take columns
+// 0..31 of rows 0..63, warps 2, 3 columns 32..63 of the same rows.  A lane stores its row's eight 16-byte chunks
+// rotated by its lane index, so the eight lanes of each store phase hit distinct banks.
+__device__ __forceinline__ void stage_weight_grad(uint32_t dw, uint32_t rows, float* stage, int warp, int lane) {
+    const uint32_t o = (uint32_t)((warp & 1) * 32 + lane);
+    const uint32_t c0 = warp < 2 ? 0u : 32u;
+    uint32_t v[32];
+    tc_ld32(dw + c0, v);
+    if (o < rows) {
+        uint4 r[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) r[i] = make_uint4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+        const uint32_t k = (uint32_t)lane & 7u;
+        rotate8(r, k);
+        float* row = stage + o * 64 + c0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) *reinterpret_cast<uint4*>(row + 4 * ((j + k) & 7u)) = r[j];
+    }
 }
 
 // samples: 4 float4 each (raw inputs in the first three, the target rgb in
@@ -470,18 +512,33 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
     const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
 
     // one round of products issued by thread 0, then the wait of all threads; false when it timed out
-    auto run = [&](auto issue) -> bool {
+    // `between` runs on all threads while the products execute
+    auto run = [&](auto issue, auto between) -> bool {
         if (tid == 0) {
             tc_fence_after();
             issue();
             tc_commit(bar);
         }
+        between();
         __syncwarp();
         const bool done = mbar_wait(bar, phase);
         phase ^= 1u;
         __syncwarp();
         tc_fence_after();
         return done;
+    };
+    auto nothing = [] {};
+    // dW_L is complete after stage L of the CTA's last tile, and act tile L is no longer read: all threads stage
+    // it there, and thread 0 adds it to dW_global with a bulk reduction that overlaps the remaining work
+    auto reduce_weight_grad = [&](int L) {
+        tc_fence_after();
+        const uint32_t rows = L < kMlpHidden ? 64u : (uint32_t)kMlpOut;
+        stage_weight_grad(rows_tmem + kTrDw + 64 * (uint32_t)L, rows, reinterpret_cast<float*>(act + L * kTrTile),
+                          warp, lane);
+        tc_fence_before();
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) bulk_reduce_add_f32(dW_global + L * kMlpLayerParams, act_s + L * kTrTile, rows * 64u * 4u);
     };
     // all threads' shared-memory writes reach the tensor core; true when some thread's wait timed out
     auto publish = [&](bool done) -> bool {
@@ -491,7 +548,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
     };
 
     for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
-        const bool first = tile == blockIdx.x;
+        const bool first = tile == blockIdx.x, last = tile + gridDim.x >= tiles;
         const uint32_t row = tile * kTcRows + tid;
         const float4 tg = nx[3];
         {
@@ -512,7 +569,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
                 const uint32_t idesc = l < kMlpHidden ? tc_idesc(kTcRows, 64) : tc_idesc(kTcRows, kTcW4Rows);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) tc_mma(tmem, tc_sdesc(a_s + 32 * k), tc_sdesc(w_s + 32 * k), idesc, k);
-            });
+            }, nothing);
             if (l < kMlpHidden) {
                 unsigned char* out = act + (l + 1) * kTrTile;
                 uint32_t v[64];
@@ -539,9 +596,9 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
             float gy[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const float d = yv[c] - tv[c], den = yv[c] * yv[c] + 0.01f;
-                loss += row < n ? d * d / den * inv : 0.0f;
-                gy[c] = row < n ? 2.0f * d / den * inv : 0.0f;
+                const float d = yv[c] - tv[c], rden = __frcp_rn(yv[c] * yv[c] + 0.01f) * inv;
+                loss += row < n ? d * d * rden : 0.0f;
+                gy[c] = row < n ? 2.0f * d * rden : 0.0f;
             }
             *tile_chunk(grad, tid, 0) = make_uint4(pack2(gy[0], gy[1]), pack2(gy[2], 0.0f), 0u, 0u);
 #pragma unroll
@@ -569,6 +626,8 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
 #pragma unroll
                 for (int k = 0; k < kTcRows / 16; ++k)
                     tc_mma(d, tc_sdesc_mn(g_s + 2048 * k), tc_sdesc_mn(a_s + 2048 * k), idesc, first && k == 0 ? 0u : 1u);
+            }, [&] {   // the previous stage's layer, complete on the last tile, while this stage's products run
+                if (last && L < kMlpHidden) reduce_weight_grad(L + 1);
             });
             if (L > 0) {
                 unsigned char* out = grad + (uint32_t)((kMlpHidden - L + 1) & 1) * kTrTile;
@@ -584,6 +643,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
             }
             if (publish(done)) failed = true;
         }
+        if (last && !failed) reduce_weight_grad(0);
     }
     // loss: one atomic per warp
 #pragma unroll
@@ -595,45 +655,8 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
             mbar_wait(bar, phase ^ 1u);   // the products of the abandoned round, once more bounded
         }
         tc_fence_before();
-    } else if (blockIdx.x < tiles) {
-        tc_fence_after();
-        // weight gradients: TMEM lane o = output o (lanes 64..127 repeat 0..63).  Warps 0, 1 take columns 0..31
-        // of rows 0..63, warps 2, 3 columns 32..63 of the same rows; the output layer has rows 0..2.  They are
-        // written in dW's own layout, FP32 [layer][out][in], over the activation tiles (free now), and added to
-        // dW_global by one bulk reduction per layer.  A lane stores its row's eight 16-byte chunks rotated by
-        // its lane index, so the eight lanes of each store phase hit distinct banks.
-        const uint32_t o = (uint32_t)((warp & 1) * 32 + lane);
-        const uint32_t c0 = warp < 2 ? 0u : 32u;
-        float* stage = reinterpret_cast<float*>(act);
-        for (int l = 0; l <= kMlpHidden; ++l) {
-            uint4 r[8];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                uint32_t v[16];
-                tc_ld16(rows_tmem + kTrDw + 64 * (uint32_t)l + c0 + 16 * h, v);
-#pragma unroll
-                for (int i = 0; i < 4; ++i) r[4 * h + i] = make_uint4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-            }
-            if (l < kMlpHidden || o < (uint32_t)kMlpOut) {
-                const uint32_t k = (uint32_t)lane & 7u;
-                rotate8(r, k);
-                float* row = stage + l * kMlpLayerParams + o * 64 + c0;
-#pragma unroll
-                for (int j = 0; j < 8; ++j) *reinterpret_cast<uint4*>(row + 4 * ((j + k) & 7u)) = r[j];
-            }
-        }
-        tc_fence_before();
-        fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            for (int l = 0; l < kMlpHidden; ++l)
-                bulk_reduce_add_f32(dW_global + l * kMlpLayerParams, smem_u32(stage + l * kMlpLayerParams),
-                                    kMlpLayerParams * 4);
-            bulk_reduce_add_f32(dW_global + kMlpHidden * kMlpLayerParams, smem_u32(stage + kMlpHidden * kMlpLayerParams),
-                                kMlpOut * 64 * 4);
-            bulk_commit_and_wait();
-        }
     }
+    if (tid == 0) bulk_wait_all();   // the weight-gradient reductions (shared memory is read until they end)
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
