@@ -29,8 +29,8 @@ bsm_status cache_io(bsm_cache* c, size_t bytes) {
 }
 
 void upload_weights(bsm_cache* c, const float* w) {
-    std::vector<__nv_bfloat16> b(kMlpParams);
-    for (int i = 0; i < kMlpParams; ++i) b[i] = __float2bfloat16_rn(w[i]);
+    std::vector<__nv_bfloat16> b(kMlpParams);   // in the tensor-core kernels' tile layout
+    for (int i = 0; i < kMlpParams; ++i) b[bsm::mlp_tile_index(i)] = __float2bfloat16_rn(w[i]);
     cudaMemcpy(c->w_master, w, kMlpParams * 4, cudaMemcpyHostToDevice);
     cudaMemcpy(c->w_bf16, b.data(), kMlpParams * 2, cudaMemcpyHostToDevice);
     cudaMemset(c->adam_m, 0, kMlpParams * 4);

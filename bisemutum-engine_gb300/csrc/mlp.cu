@@ -14,7 +14,8 @@
 
 namespace bsm {
 
-// Adam (Kingma and Ba 2015) on the fp32 master weights; writes the bf16 copy.
+// Adam (Kingma and Ba 2015) on the fp32 master weights; writes the bf16 copy
+// in the kernels' tile layout (mlp_tile_index).
 // With ema_decay > 0 it also keeps an exponential moving average of the
 // weights (zero-started, so ema_corr = 1 / (1 - decay^steps) corrects its bias)
 // and writes the corrected average's bf16 copy, which renders read.
@@ -34,11 +35,12 @@ __global__ void k_mlp_adam(float* __restrict__ wm, __nv_bfloat16* __restrict__ w
     // padded output rows stay zero
     if (i >= kMlpHidden * kMlpLayerParams + kMlpOut * kMlpHid) wi = 0.0f;
     wm[i] = wi;
-    wb[i] = __float2bfloat16_rn(wi);
+    const int t = mlp_tile_index(i);
+    wb[t] = __float2bfloat16_rn(wi);
     if (ema_decay > 0.0f) {
         float e = ema_decay * ema[i] + (1.0f - ema_decay) * wi;
         ema[i] = e;
-        emab[i] = __float2bfloat16_rn(e * ema_corr);
+        emab[t] = __float2bfloat16_rn(e * ema_corr);
     }
 }
 

@@ -29,6 +29,16 @@ constexpr int kMlpHidden = 4;      // hidden layers
 constexpr int kMlpLayerParams = kMlpHid * kMlpIn;
 constexpr int kMlpParams = kMlpHidden * kMlpLayerParams + kMlpOutPad * kMlpHid;  // 16896
 
+// Position of parameter i (row i / 64, column i % 64 of the row-major [264][64]
+// weight matrix) in the BF16 copies the tensor-core kernels read: each row is
+// one 128-byte line whose 16-byte chunk c (columns 8c..8c+7) sits at chunk
+// c ^ (row mod 8), the layout of the kernels' shared-memory tiles (128-byte
+// swizzle), so that one bulk copy moves the weights into shared memory.
+BSM_HD int mlp_tile_index(int i) {
+    const int r = i >> 6, c = i & 63;
+    return (r << 6) | ((((c >> 3) ^ (r & 7)) << 3) | (c & 7));
+}
+
 // Encoded feature f of a sample with raw inputs `raw`.
 BSM_HD float mlp_feature(const float* raw, int f) {
     if (f < 56) {

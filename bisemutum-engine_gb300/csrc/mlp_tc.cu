@@ -45,7 +45,8 @@ constexpr int kTcW4Rows = 16;                                   // output layer 
 constexpr int kTcWRows = kMlpHidden * 64 + kTcW4Rows;           // 272 weight rows in shared memory
 constexpr int kTcActOff = kTcWRows * 128;                       // 34816 = 34 x 1024
 constexpr int kTcBarOff = kTcActOff + kTcRows * 128;            // 51200
-constexpr int kTcSmem = kTcBarOff + 16 + 1024;                  // + slack to align the base to 1024
+constexpr int kTcSmem = kTcBarOff + 32 + 1024;                  // + slack to align the base to 1024
+constexpr uint32_t kTcWBytes = (kMlpHidden * 64 + kMlpOutPad) * 128;   // 33,792: the weights' tile image
 constexpr uint32_t kTcCols = 64;                                // tensor-memory columns per CTA
 constexpr uint32_t kTcErrTimeout = 2u;                          // error word bit: a tensor-core wait timed out
 static_assert(kTcActOff % 1024 == 0, "swizzled tiles start on 1024-byte boundaries");
@@ -113,6 +114,17 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     while (!mbar_try_wait(bar, parity))
         if (global_ns() - t0 > 1000000000ull) return false;
     return true;
+}
+
+// Bulk copy of `bytes` (a multiple of 16) from global to shared memory, completing on mbarrier `bar` (the
+// expected byte count is announced first by the same thread).
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -226,6 +238,19 @@ __device__ __forceinline__ uint4* tile_chunk(unsigned char* tile, int r, int c) 
     return reinterpret_cast<uint4*>(tile + r * 128 + ((c ^ (r & 7)) << 4));
 }
 
+// The weights into rows 0..271 of the tile at `base`: rows 0..263 by one bulk copy of their tile image (the
+// BF16 copies are kept in that layout, mlp_tile_index), completing on `wbar`; rows 264..271 zeroed.  Thread 0
+// starts the copy; every thread waits on `wbar` (phase 0) before the first product reads the tile.
+__device__ __forceinline__ void load_weights_async(const __nv_bfloat16* w, unsigned char* base, uint32_t base_s,
+                                                   uint32_t wbar, int tid) {
+    if (tid == 0) {
+        mbar_init(wbar, 1);
+        mbar_expect_tx(wbar, kTcWBytes);
+        bulk_load(base_s, w, kTcWBytes, wbar);
+    }
+    if (tid < 64) *tile_chunk(base, kMlpHidden * 64 + kMlpOutPad + (tid >> 3), tid & 7) = make_uint4(0u, 0u, 0u, 0u);
+}
+
 // Encoded features of one query (the encoding of mlp_feature), written as
 // row r of the activation tile: chunk d < 7 holds sin/cos(2^k pi raw[d]),
 // k = 0..3; chunk 7 holds raw[7..11], 1, 0, 0.  The base frequency comes from
@@ -269,17 +294,13 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
     unsigned char* base = smem_raw + (base_s - raw_s);
     unsigned char* act = base + kTcActOff;
     const uint32_t act_s = base_s + kTcActOff, bar = base_s + kTcBarOff;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kTcBarOff + 8);
+    const uint32_t wbar = bar + 8;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kTcBarOff + 16);
     const int tid = threadIdx.x, warp = tid >> 5;
 
-    // weights: rows 0..263 from global (W0..W3, W4), rows 264..271 zero
-    const uint4* wsrc = reinterpret_cast<const uint4*>(w);
-    static_assert(kTcWRows * 8 % kTcRows == 0, "whole rounds of 16-byte weight loads");
-#pragma unroll
-    for (int j = 0; j < kTcWRows * 8 / kTcRows; ++j) {   // all loads in flight before the stores
-        int i = tid + j * kTcRows, r = i >> 3, c = i & 7;
-        *tile_chunk(base, r, c) = r < kMlpHidden * 64 + kMlpOutPad ? __ldg(wsrc + i) : make_uint4(0u, 0u, 0u, 0u);
-    }
+    const uint32_t n = kInfer ? min(*count, n_max) : n_max;
+    const bool has_work = blockIdx.x * kTcRows < n;   // CTAs past the queries copy no weights
+    if (has_work) load_weights_async(w, base, base_s, wbar, tid);
     if (tid == 0) mbar_init(bar, 1);
     __syncwarp();
     if (warp == 0) tc_alloc(smem_u32(tmem_slot), kTcCols);
@@ -289,7 +310,6 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     const uint32_t rows_tmem = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
-    const uint32_t n = kInfer ? min(*count, n_max) : n_max;
     uint32_t phase = 0;
     bool failed = false;
 
@@ -301,6 +321,7 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
     };
     float4 next[4];
     fetch(blockIdx.x * kTcRows + tid, next);
+    bool weights = false;   // the weight copy has landed
     for (uint32_t tile = blockIdx.x; tile * kTcRows < n && !failed; tile += gridDim.x) {
         const uint32_t row = tile * kTcRows + tid;
         const float4 m = next[3];   // throughput and accumulator index (queries)
@@ -313,9 +334,11 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
             fetch(row + gridDim.x * kTcRows, next);
             encode_row(raw, act, tid);
         }
+        const bool w_ok = weights || mbar_wait(wbar, 0);
+        weights = true;
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
+        if (__syncthreads_or(!w_ok)) { failed = true; break; }
         for (int l = 0; l <= kMlpHidden; ++l) {
             if (tid == 0) {
                 tc_fence_after();
@@ -368,6 +391,7 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
         }
         tc_fence_before();
     }
+    if (has_work && !weights && tid == 0) mbar_wait(wbar, 0);   // no copy into shared memory outlives the CTA
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
@@ -481,6 +505,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
     unsigned char* act = base + kTrActOff;
     unsigned char* grad = base + kTrGradOff;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kTrBarOff + 8);
+    const uint32_t wbar = bar + 16;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // this row's sample of the next tile (raw inputs, target), loaded ahead: the first before the weights
@@ -490,12 +515,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
         for (int k = 0; k < 4; ++k) nx[k] = row < n ? s[4 * (size_t)row + k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     };
     fetch(blockIdx.x * kTcRows + tid);
-    const uint4* wsrc = reinterpret_cast<const uint4*>(w);
-#pragma unroll
-    for (int j = 0; j < kTcWRows * 8 / kTcRows; ++j) {
-        int i = tid + j * kTcRows, r = i >> 3, c = i & 7;
-        *tile_chunk(base, r, c) = r < kMlpHidden * 64 + kMlpOutPad ? __ldg(wsrc + i) : make_uint4(0u, 0u, 0u, 0u);
-    }
+    load_weights_async(w, base, base_s, wbar, tid);
     if (tid == 0) mbar_init(bar, 1);
     __syncwarp();
     if (warp == 0) tc_alloc(smem_u32(tmem_slot), kTrCols);
@@ -560,7 +580,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
             fetch(row + gridDim.x * kTcRows);
             encode_row(raw, act, tid);
         }
-        if (publish(true)) { failed = true; break; }
+        if (publish(!first || mbar_wait(wbar, 0))) { failed = true; break; }
         // forward: act[l + 1] = relu(act[l] W_l^T), y = a3 W4^T
         float y0 = 0.0f, y1 = 0.0f, y2 = 0.0f;
         for (int l = 0; l <= kMlpHidden && !failed; ++l) {
