@@ -278,6 +278,16 @@ bsm_status ensure_launch_cfg(bsm_context* ctx, uint32_t block, int regcap = 0) {
     return BSM_OK;
 }
 
+// The launch configuration of a render of scene `sc`: tuned parameters of the scene fill in what the
+// settings leave at 0.
+bsm_status prepare_launch(bsm_context* ctx, const Scene* sc, const bsm_pt_settings& s) {
+    uint32_t block = s.block_size ? s.block_size : (sc->tuned ? sc->tune.block_size : 0u);
+    if (bsm_status st = ensure_launch_cfg(ctx, block, sc->tuned ? (int)(sc->tune.register_cap != 0) : 1)) return st;
+    ctx->lc.postpone_sp = sc->tuned ? (int)sc->tune.postpone_depth : 16;
+    ctx->lc.refill_min = sc->tuned ? (int)sc->tune.refill_lanes : 8;
+    return BSM_OK;
+}
+
 // Device bytes of the wavefront per path slot (the layout of ensure_wavefront):
 // 9 arrays of 16 B (rays, paths and throughputs ping-pong, hits), 64 B of cache
 // query, and (lights + 1) shadow records of 3 x 16 B + a 4 B opacity seed.
@@ -1417,11 +1427,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
     if (!(s.ray_length > 0.0f)) return fail(ctx, BSM_ERR_INVALID_ARG, "ray_length must be > 0");
     if (s.t_min < 0.0f) return fail(ctx, BSM_ERR_INVALID_ARG, "t_min must be >= 0");
     bsm_status st;
-    // tuned parameters of this scene fill in what the settings leave at 0
-    uint32_t block = s.block_size ? s.block_size : (sc->tuned ? sc->tune.block_size : 0u);
-    if ((st = ensure_launch_cfg(ctx, block, sc->tuned ? (int)(sc->tune.register_cap != 0) : 1))) return st;
-    ctx->lc.postpone_sp = sc->tuned ? (int)sc->tune.postpone_depth : 16;
-    ctx->lc.refill_min = sc->tuned ? (int)sc->tune.refill_lanes : 8;
+    if ((st = prepare_launch(ctx, sc, s))) return st;
     const bsm_camera* views = nullptr;
     std::vector<bsm_camera> cams(n_views);
     for (uint32_t v = 0; v < n_views; ++v) cams[v] = req[v].cam;
@@ -1620,6 +1626,9 @@ extern "C" bsm_status bsm_render_cached(bsm_context* ctx, uint32_t scene_id, con
     if (cs.cache_segment == 0 || cs.cache_segment >= (uint32_t)kMaxSeg)
         return fail(ctx, BSM_ERR_INVALID_ARG, "cache_segment must be 1..15");
     if (train_loss) *train_loss = 0.0f;
+    // the training paths' shadow pass launches with the render's configuration, which a first call on a
+    // context has not set yet
+    if (bsm_status e = prepare_launch(ctx, sc, *settings)) return e;
     // the frame's device time (stats->ms_total) starts before its training step
     CK(cudaEventRecord(ctx->ev[8], WS(ctx)));
     if (cs.train_steps > 0 && cs.train_paths > 0) {

@@ -208,3 +208,32 @@ def test_renders_read_the_corrected_moving_average(bsm, ctx):
     finally:
         c.close()
     ctx.release(sid)
+
+
+def test_cached_render_as_the_first_call_of_a_context(bsm):
+    """bsm_render_cached on a context that has rendered nothing before: its training paths' shadow pass launches
+    with the configuration the render sets up, and the frame agrees with the same frame on a context that
+    rendered a plain frame first (same seeds, fresh caches with the same start weights; the training step's
+    gradient sums run in another order, so the two trained networks differ in the last bits)."""
+    scene = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=41, spheres=24)
+    cam = bsm.make_camera(tuple(scene.camera.position), tuple(scene.camera.front), width=64, height=48)
+    cs = bsm.cache_settings(cache_segment=2, train_paths=2048, train_batch=4096, train_steps=1)
+    images = []
+    for warm in (False, True):
+        c2 = bsm.Context(0)
+        try:
+            sid = c2.load_scene(scene)
+            if warm:
+                c2.render(sid, [cam], bsm.settings(spp=1, max_segments=4, seed=3), outputs=False)
+            cache = bsm.RadianceCache(c2, seed=5)
+            try:
+                img, st, loss = cache.render(sid, cam, bsm.settings(spp=2, seed=9), cs)
+                assert st.extend_rays > 0 and np.isfinite(loss)
+                images.append(img)
+            finally:
+                cache.close()
+        finally:
+            c2.close()
+    a, b = images[0][..., :3].astype(np.float64), images[1][..., :3].astype(np.float64)
+    assert np.isfinite(a).all() and np.isfinite(b).all()
+    assert np.abs(a - b).mean() <= 1e-2 * np.abs(b).mean()
