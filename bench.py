@@ -771,10 +771,16 @@ def cache_summary(a, bsm, device, spps, seeds, ref_spp, train_frames):
         ctx.close()
 
     def time_at(curve, key, target):
-        """Frame time the method needs for `target` error: log-log interpolation between measured points."""
-        pts = sorted(((c[key], c["ms"]) for c in curve), reverse=True)   # decreasing error
-        for (e0, t0_), (e1, t1) in zip(pts[:-1], pts[1:]):
-            if e1 <= target <= e0 and e0 > e1:
+        """Frame time the method needs for `target` error: log-log interpolation along the error envelope (points
+        in order of frame time, each kept only if its error is below every cheaper point's), so that a noisy
+        point whose error is above a cheaper one's cannot make an error look reachable sooner than measured.
+        None when the target lies outside the envelope's range."""
+        env = []
+        for c in sorted(curve, key=lambda c: c["ms"]):
+            if not env or c[key] < env[-1][0]:
+                env.append((c[key], c["ms"]))
+        for (e0, t0_), (e1, t1) in zip(env[:-1], env[1:]):
+            if e1 <= target <= e0:
                 u = (np.log(target) - np.log(e0)) / (np.log(e1) - np.log(e0))
                 return float(np.exp(np.log(t0_) + u * (np.log(t1) - np.log(t0_))))
         return None
