@@ -26,7 +26,9 @@
 //   dW += g_z^T a    A: the gradient tile read MN-major (M = out, K = sample)
 //                    B: the activation tile [sample][in] read MN-major
 // with every layer's weight gradient accumulated in tensor memory over all
-// the tiles a CTA takes, and added to the global FP32 gradient at the end.
+// the tiles a CTA takes, and added to the global FP32 gradient on its last
+// tile by bulk reductions.  A training CTA has 256 threads, two per sample
+// row, each reading back and storing half of the row's 64 columns.
 //
 // Every mbarrier wait gives up after one second: the kernel then sets bit 1
 // of the error word, stops issuing products and frees its tensor memory.
@@ -415,6 +417,7 @@ constexpr int kTrSmem = kTrBarOff + 16384 + 1024;
 // Tensor memory: columns 0..63 hold the product being read back (forward z,
 // backward g_a); 64 + 64 l .. 127 + 64 l hold dW_l (l = 0..4; rows = outputs).
 constexpr uint32_t kTrCols = 512;
+constexpr int kTrThreads = 256;                                 // two threads per sample row
 constexpr uint32_t kTrDw = 64;
 static_assert(kTrGradOff % 1024 == 0 && kTrBarOff % 1024 == 0, "swizzled tiles start on 1024-byte boundaries");
 static_assert(kTrDw + 5 * 64 <= kTrCols, "tensor-memory columns");
@@ -431,29 +434,10 @@ __device__ __forceinline__ void bulk_wait_all() {
     asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
-// r[j] = v[(j + k) mod 8] for k = 0..7 in three conditional rotations (no indexed register access).
-__device__ __forceinline__ void rotate8(uint4 (&r)[8], uint32_t k) {
-#pragma unroll
-    for (int b = 0; b < 3; ++b) {
-        const int sh = 1 << b;
-        const bool on = (k >> b) & 1u;
-        uint4 t[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) t[j] = on ? r[(j + sh) & 7] : r[j];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) r[j] = t[j];
-    }
-}
-
-// The 8 chunks of row r of a tile as 64 BF16 values (4 per uint2 pair): used for the ReLU masks.
-__device__ __forceinline__ void load_row(const unsigned char* tile, int r, uint4 (&row)[8]) {
-#pragma unroll
-    for (int c = 0; c < 8; ++c) row[c] = *reinterpret_cast<const uint4*>(tile + r * 128 + ((c ^ (r & 7)) << 4));
-}
-
-// g_z = g_a * (a > 0) for the 16 columns [c, c + 16) of row `tid` (v: the row's 64 columns of g_a), as two
+// g_z = g_a * (a > 0) for the 16 columns [c, c + 16) of v (this thread's columns of its row of g_a), as two
 // BF16 chunks.
-__device__ __forceinline__ void relu_grad_chunks(const uint32_t (&v)[64], int c, const uint4& a0, const uint4& a1,
+template <int kN>
+__device__ __forceinline__ void relu_grad_chunks(const uint32_t (&v)[kN], int c, const uint4& a0, const uint4& a1,
                                                  uint4& o0, uint4& o1) {
     const uint32_t av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
     uint32_t p[8];
@@ -467,24 +451,63 @@ __device__ __forceinline__ void relu_grad_chunks(const uint32_t (&v)[64], int c,
     o1 = make_uint4(p[4], p[5], p[6], p[7]);
 }
 
-// One layer's weight gradient from tensor memory (dw: this warp's lanes, column 0 of the layer; lane o = output o,
-// lanes 64..127 repeat 0..63) into shared memory as FP32 [out][64] (rows < `rows`).  Warps 0, 1 take columns
-// 0..31 of rows 0..63, warps 2, 3 columns 32..63 of the same rows.  A lane stores its row's eight 16-byte chunks
-// rotated by its lane index, so the eight lanes of each store phase hit distinct banks.
+// Half h of the encoded features of one sample, written into row r of the activation tile: h = 0 encodes
+// raw[0..3] (f0) as chunks 0..3; h = 1 encodes raw[4..6] (f0.xyz) as chunks 4..6 and writes chunk 7 from
+// raw[7] = f0.w and raw[8..11] = f1.  The values are those of encode_row.
+__device__ __forceinline__ void encode_half(int h, const float4& f0, const float4& f1, unsigned char* act, int r) {
+    const float x[4] = {f0.x, f0.y, f0.z, f0.w};
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        if (h && d == 3) break;
+        uint32_t p[4];
+        float s, c;
+        __sincosf(x[d] * 3.14159265f, &s, &c);
+        p[0] = pack2(s, c);
+#pragma unroll
+        for (int k = 1; k < 4; ++k) {
+            float s2 = 2.0f * s * c, c2 = (c - s) * (c + s);
+            s = s2;
+            c = c2;
+            p[k] = pack2(s, c);
+        }
+        *tile_chunk(act, r, 4 * h + d) = make_uint4(p[0], p[1], p[2], p[3]);
+    }
+    if (h)
+        *tile_chunk(act, r, 7) =
+            make_uint4(pack2(f0.w, f1.x), pack2(f1.y, f1.z), pack2(f1.w, 1.0f), pack2(0.0f, 0.0f));
+}
+
+// r[j] = v[(j + k) mod 4] for k = 0..3 in two conditional rotations (no indexed register access).
+__device__ __forceinline__ void rotate4(uint4 (&r)[4], uint32_t k) {
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+        const int sh = 1 << b;
+        const bool on = (k >> b) & 1u;
+        uint4 t[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) t[j] = on ? r[(j + sh) & 3] : r[j];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) r[j] = t[j];
+    }
+}
+
+// One layer's weight gradient from tensor memory into shared memory as FP32 [out][64] (rows < `rows`), by all
+// eight warps: warp w reads its lanes (lane o = output o; lanes 64..127 repeat 0..63), rows 32 (w & 1) + lane,
+// columns 16 (w >> 1) .. 16 (w >> 1) + 15.  Lanes store their four 16-byte chunks rotated by the lane index.
 __device__ __forceinline__ void stage_weight_grad(uint32_t dw, uint32_t rows, float* stage, int warp, int lane) {
     const uint32_t o = (uint32_t)((warp & 1) * 32 + lane);
-    const uint32_t c0 = warp < 2 ? 0u : 32u;
-    uint32_t v[32];
-    tc_ld32(dw + c0, v);
+    const uint32_t c0 = 16u * (uint32_t)(warp >> 1);
+    uint32_t v[16];
+    tc_ld16(dw + c0, v);
     if (o < rows) {
-        uint4 r[8];
+        uint4 r[4];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) r[i] = make_uint4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-        const uint32_t k = (uint32_t)lane & 7u;
-        rotate8(r, k);
+        for (int i = 0; i < 4; ++i) r[i] = make_uint4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+        const uint32_t k = (uint32_t)lane & 3u;
+        rotate4(r, k);
         float* row = stage + o * 64 + c0;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) *reinterpret_cast<uint4*>(row + 4 * ((j + k) & 7u)) = r[j];
+        for (int j = 0; j < 4; ++j) *reinterpret_cast<uint4*>(row + 4 * ((j + k) & 3u)) = r[j];
     }
 }
 
@@ -494,9 +517,15 @@ __device__ __forceinline__ void stage_weight_grad(uint32_t dw, uint32_t rows, fl
 // denominator held constant, to dW_global, and the loss to loss_out[0].
 // Rounding points: encoded inputs, activations and gradients g_y, g_z in
 // BF16, products in FP32 (those of the oracle's BF16 network).
-__global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16* __restrict__ w,
-                                                             const float4* __restrict__ s, uint32_t n,
-                                                             float* dW_global, float* loss_out, uint32_t* err) {
+//
+// 256 threads: threads t and t + 128 share sample row t of the tile.  The
+// first (warps 0..3) loads the sample's raw inputs 0..3 and its target,
+// encodes features 0..31, and reads back columns 0..31 of every product;
+// the second (warps 4..7, which reach the same tensor-memory lanes) loads
+// raw inputs 4..11 and takes features and columns 32..63.
+__global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloat16* __restrict__ w,
+                                                                const float4* __restrict__ s, uint32_t n,
+                                                                float* dW_global, float* loss_out, uint32_t* err) {
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw_s = smem_u32(smem_raw);
     const uint32_t base_s = (raw_s + 1023u) & ~1023u;
@@ -506,15 +535,15 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
     unsigned char* grad = base + kTrGradOff;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kTrBarOff + 8);
     const uint32_t wbar = bar + 16;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, r = tid & (kTcRows - 1), h = tid >> 7;
 
-    // this row's sample of the next tile (raw inputs, target), loaded ahead: the first before the weights
-    float4 nx[4];
+    // this thread's half of its row's sample in the next tile, loaded ahead: the first before the weights
+    float4 nx[2];
     auto fetch = [&](uint32_t row) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) nx[k] = row < n ? s[4 * (size_t)row + k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        nx[0] = row < n ? s[4 * (size_t)row + (h ? 1 : 0)] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        nx[1] = row < n ? s[4 * (size_t)row + (h ? 2 : 3)] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     };
-    fetch(blockIdx.x * kTcRows + tid);
+    fetch(blockIdx.x * kTcRows + r);
     load_weights_async(w, base, base_s, wbar, tid);
     if (tid == 0) mbar_init(bar, 1);
     __syncwarp();
@@ -524,7 +553,8 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t rows_tmem = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t rows_tmem = tmem + ((uint32_t)((warp & 3) * 32) << 16);   // this warp's 32 lanes
+    const uint32_t cols = 32u * (uint32_t)h;                                  // this thread's 32 columns
     const float inv = 1.0f / (3.0f * (float)n);
     float loss = 0.0f;
     uint32_t phase = 0;
@@ -569,17 +599,10 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
 
     for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
         const bool first = tile == blockIdx.x, last = tile + gridDim.x >= tiles;
-        const uint32_t row = tile * kTcRows + tid;
-        const float4 tg = nx[3];
-        {
-            float raw[kMlpRaw];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                raw[4 * k] = nx[k].x; raw[4 * k + 1] = nx[k].y; raw[4 * k + 2] = nx[k].z; raw[4 * k + 3] = nx[k].w;
-            }
-            fetch(row + gridDim.x * kTcRows);
-            encode_row(raw, act, tid);
-        }
+        const uint32_t row = tile * kTcRows + r;
+        const float4 f0 = nx[0], f1 = nx[1];   // h = 0: f1 is the target
+        fetch(row + gridDim.x * kTcRows);
+        encode_half(h, f0, f1, act, r);
         if (publish(!first || mbar_wait(wbar, 0))) { failed = true; break; }
         // forward: act[l + 1] = relu(act[l] W_l^T), y = a3 W4^T
         float y0 = 0.0f, y1 = 0.0f, y2 = 0.0f;
@@ -592,17 +615,17 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
             }, nothing);
             if (l < kMlpHidden) {
                 unsigned char* out = act + (l + 1) * kTrTile;
-                uint32_t v[64];
-                tc_ld64(rows_tmem, v);
+                uint32_t v[32];
+                tc_ld32(rows_tmem + cols, v);
 #pragma unroll
-                for (int c = 0; c < 8; ++c) {
+                for (int c = 0; c < 4; ++c) {
                     uint32_t p[4];
 #pragma unroll
                     for (int i = 0; i < 4; ++i)
                         p[i] = pack2_relu(__uint_as_float(v[8 * c + 2 * i]), __uint_as_float(v[8 * c + 2 * i + 1]));
-                    *tile_chunk(out, tid, c) = make_uint4(p[0], p[1], p[2], p[3]);
+                    *tile_chunk(out, r, 4 * h + c) = make_uint4(p[0], p[1], p[2], p[3]);
                 }
-            } else {
+            } else if (h == 0) {
                 uint32_t v[16];
                 tc_ld16(rows_tmem, v);
                 y0 = __uint_as_float(v[0]); y1 = __uint_as_float(v[1]); y2 = __uint_as_float(v[2]);
@@ -611,8 +634,8 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
         }
         if (failed) break;
         // loss gradient g_y (rows >= n: zero), into gradient tile 0 (chunk 0: channels 0..7; the rest zero)
-        {
-            const float yv[3] = {y0, y1, y2}, tv[3] = {tg.x, tg.y, tg.z};
+        if (h == 0) {
+            const float yv[3] = {y0, y1, y2}, tv[3] = {f1.x, f1.y, f1.z};
             float gy[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -620,18 +643,21 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
                 loss += row < n ? d * d * rden : 0.0f;
                 gy[c] = row < n ? 2.0f * d * rden : 0.0f;
             }
-            *tile_chunk(grad, tid, 0) = make_uint4(pack2(gy[0], gy[1]), pack2(gy[2], 0.0f), 0u, 0u);
-#pragma unroll
-            for (int c = 1; c < 8; ++c) *tile_chunk(grad, tid, c) = make_uint4(0u, 0u, 0u, 0u);
+            *tile_chunk(grad, r, 0) = make_uint4(pack2(gy[0], gy[1]), pack2(gy[2], 0.0f), 0u, 0u);
         }
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (h || c > 0) *tile_chunk(grad, r, 4 * h + c) = make_uint4(0u, 0u, 0u, 0u);
         if (publish(true)) { failed = true; break; }
         // backward: step L reads gradient tile L & 1 (g_y, then g_z3 .. g_z0), adds dW_L and, for L > 0,
         // writes g_z(L-1) = (g_in W_L) * (a(L-1) > 0) into the other gradient tile
         for (int L = kMlpHidden; L >= 0 && !failed; --L) {
             const uint32_t g_s = grad_s + (uint32_t)((kMlpHidden - L) & 1) * kTrTile;
             const uint32_t a_s = act_s + L * kTrTile;   // a(L-1): e for L = 0, a3 for L = 4
-            uint4 ar[8];                                  // the mask of g_z(L-1) is a(L-1) > 0
-            if (L > 0) load_row(act + L * kTrTile, tid, ar);
+            uint4 ar[4];                                  // this thread's half of the mask row: a(L-1) > 0
+            if (L > 0)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) ar[c] = *tile_chunk(act + L * kTrTile, r, 4 * h + c);
             const bool done = run([&] {
                 if (L > 0) {   // g_a = g_in W_L: K = outputs of layer L (16 for the output layer)
                     const uint32_t w_s = base_s + L * 64 * 128;
@@ -651,14 +677,14 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_train_tc(const __nv_bfloat16
             });
             if (L > 0) {
                 unsigned char* out = grad + (uint32_t)((kMlpHidden - L + 1) & 1) * kTrTile;
-                uint32_t v[64];
-                tc_ld64(rows_tmem, v);
+                uint32_t v[32];
+                tc_ld32(rows_tmem + cols, v);
 #pragma unroll
-                for (int h = 0; h < 4; ++h) {
+                for (int q = 0; q < 2; ++q) {
                     uint4 o0, o1;
-                    relu_grad_chunks(v, 16 * h, ar[2 * h], ar[2 * h + 1], o0, o1);
-                    *tile_chunk(out, tid, 2 * h) = o0;
-                    *tile_chunk(out, tid, 2 * h + 1) = o1;
+                    relu_grad_chunks(v, 16 * q, ar[2 * q], ar[2 * q + 1], o0, o1);
+                    *tile_chunk(out, r, 4 * h + 2 * q) = o0;
+                    *tile_chunk(out, r, 4 * h + 2 * q + 1) = o1;
                 }
             }
             if (publish(done)) failed = true;
@@ -726,7 +752,7 @@ cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const 
     if (n == 0) return cudaSuccess;
     // one CTA per SM (512 tensor-memory columns, 167 KB of shared memory), 128 samples at a time
     const uint32_t tiles = (n + kTcRows - 1) / kTcRows, sms = (uint32_t)g_tc_grid[device] / 4;
-    k_mlp_train_tc<<<tiles < sms ? tiles : sms, kTcRows, kTrSmem, st>>>((const __nv_bfloat16*)wb, samples, n, dW, loss,
+    k_mlp_train_tc<<<tiles < sms ? tiles : sms, kTrThreads, kTrSmem, st>>>((const __nv_bfloat16*)wb, samples, n, dW, loss,
                                                                         err);
     return cudaGetLastError();
 }
