@@ -601,6 +601,7 @@ def serve_summary(a, bsm, device, rates, seconds, max_requests, saturation_n):
             ctx.server_stop()
             lat = np.array(lat)
             results.append({"rate_req_s": lam, "requests": n, "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                            "p90_ms": round(float(np.percentile(lat, 90)), 2),
                             "p99_ms": round(float(np.percentile(lat, 99)), 2),
                             "mean_ms": round(float(lat.mean()), 2), "completed_req_s": round(n / wall, 2),
                             "mrays_per_s": round(ss.extend_rays / wall / 1e6, 1), "wall_s": round(wall, 2)})

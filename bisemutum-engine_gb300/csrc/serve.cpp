@@ -10,7 +10,8 @@
 //   * every lane (a CUDA stream with its own wavefront queues) that is idle
 //     takes the next chunk: path ranges of one scene's active requests, up to
 //     the chunk capacity, described by one view record per range — requests
-//     that arrived while others were on the GPU join the next chunk;
+//     that arrived while others were on the GPU join the next chunk, the ones
+//     with the least work left first (those admitted over 200 ms ago first);
 //   * lanes run concurrently, so chunks of different scenes (and of the same
 //     scene) overlap on the device;
 //   * when all of a request's paths are traced, its mean is resolved into a
@@ -156,6 +157,9 @@ bool admit_locked(Server& S) {
     return any;
 }
 
+// Requests admitted longer ago than this are served in arrival order, ahead of the least-work-first rule.
+constexpr double kServeAgeMs = 200.0;
+
 // Builds the next chunk for `lane` from the active requests of one scene
 // (round-robin over scenes).  Returns the scene id, or 0 when there is no work.
 uint32_t build_chunk_locked(Server& S, Lane& lane, uint32_t* rr_scene) {
@@ -173,8 +177,20 @@ uint32_t build_chunk_locked(Server& S, Lane& lane, uint32_t* rr_scene) {
     if (scene == 0xffffffffu || scene == 0) return 0;
     *rr_scene = scene;
     uint32_t left = S.opts.chunk_paths;
-    for (Request* r : S.active) {
-        if (r->r.scene_id != scene || r->issued >= r->total_paths || r->cancelled) continue;
+    std::vector<Request*> cand;
+    for (Request* r : S.active)
+        if (r->r.scene_id == scene && r->issued < r->total_paths && !r->cancelled) cand.push_back(r);
+    // Order within the scene: requests admitted more than kServeAgeMs ago first, oldest first; then the
+    // others by the work they have left (paths still to issue x segments), least first, so that a small
+    // request arriving while a large one of the same scene runs joins the next chunk instead of waiting for
+    // the large one's paths.
+    const double now = S.now_ms();
+    auto key = [&](const Request* r) {
+        const bool aged = now - r->admit_ms > kServeAgeMs;
+        return std::make_pair(aged ? 0.0 : 1.0, aged ? r->admit_ms : (double)(r->total_paths - r->issued) * r->max_seg);
+    };
+    std::stable_sort(cand.begin(), cand.end(), [&](const Request* a, const Request* b) { return key(a) < key(b); });
+    for (Request* r : cand) {
         if (lane.ranges.size() >= S.opts.max_views_per_chunk || left == 0) break;
         uint64_t n = std::min<uint64_t>(left, r->total_paths - r->issued);
         lane.ranges.push_back(Range{r, r->issued, (uint32_t)n});
