@@ -701,6 +701,22 @@ def run_instanced(a, dist):
 
 
 # ----------------------------------------------------------------- cache ----
+def equal_error_time(curve, key, target):
+    """Frame time a method needs for `target` error, from its measured points (dicts with "ms" and `key`):
+    log-log interpolation along the error envelope (points in order of frame time, each kept only if its error
+    is below every cheaper point's), so that a noisy point whose error is above a cheaper one's cannot make an
+    error look reachable sooner than measured.  None when the target lies outside the envelope's range."""
+    env = []
+    for c in sorted(curve, key=lambda c: c["ms"]):
+        if not env or c[key] < env[-1][0]:
+            env.append((c[key], c["ms"]))
+    for (e0, t0_), (e1, t1) in zip(env[:-1], env[1:]):
+        if e1 <= target <= e0:
+            u = (np.log(target) - np.log(e0)) / (np.log(e1) - np.log(e0))
+            return float(np.exp(np.log(t0_) + u * (np.log(t1) - np.log(t0_))))
+    return None
+
+
 def cache_summary(a, bsm, device, spps, seeds, ref_spp, train_frames):
     """Radiance cache on the terrain scene: relMSE against a high-spp plain render and DEVICE time per frame
     (CUDA events; the cached frame's training step included), for the plain pass (8 segments) and the cached
@@ -771,26 +787,11 @@ def cache_summary(a, bsm, device, spps, seeds, ref_spp, train_frames):
     finally:
         ctx.close()
 
-    def time_at(curve, key, target):
-        """Frame time the method needs for `target` error: log-log interpolation along the error envelope (points
-        in order of frame time, each kept only if its error is below every cheaper point's), so that a noisy
-        point whose error is above a cheaper one's cannot make an error look reachable sooner than measured.
-        None when the target lies outside the envelope's range."""
-        env = []
-        for c in sorted(curve, key=lambda c: c["ms"]):
-            if not env or c[key] < env[-1][0]:
-                env.append((c[key], c["ms"]))
-        for (e0, t0_), (e1, t1) in zip(env[:-1], env[1:]):
-            if e1 <= target <= e0:
-                u = (np.log(target) - np.log(e0)) / (np.log(e1) - np.log(e0))
-                return float(np.exp(np.log(t0_) + u * (np.log(t1) - np.log(t0_))))
-        return None
-
     equal = {}
     for key in ("relmse", "relmse_trimmed"):
         rows = []
         for c, k in zip(plain, cached):
-            tc = time_at(cached, key, c[key])
+            tc = equal_error_time(cached, key, c[key])
             # where the cached frame at the same spp is both at least as accurate and faster, it reaches the plain
             # frame's error in at most its own time: plain ms / cached ms bounds the equal-error speedup from below
             # (robust where single fireflies make the untrimmed error curve non-monotone in spp)
