@@ -1,5 +1,5 @@
 // mlp.cuh — the radiance-cache network: input encoding and parameter layout,
-// shared by the CUDA kernels (mlp.cu) and the host code.
+// shared by the CUDA kernels (mlp_tc.cu, mlp.cu, train_paths.cu) and the host code.
 //
 // Network: 12 raw inputs -> 64 encoded features -> 4 hidden layers of 64 with
 // ReLU -> 3 outputs (RGB radiance), no biases (a constant-1 feature feeds the

@@ -14,8 +14,8 @@
 // k starts 32 k bytes into the rows.  tcgen05.commit signals an mbarrier when
 // the four products are done; each warp then reads its 32 rows of D
 // (tcgen05.ld 32x32b), applies ReLU, rounds to BF16 and writes them back as
-// the next layer's A.  Rounding points and FP32 accumulation are those of the
-// mma.sync training kernels (mlp.cu); only the order of the FP32 sums differs.
+// the next layer's A.  Rounding points (BF16 operands, FP32 accumulation) are
+// those of the oracle's BF16 network; only the order of the FP32 sums differs.
 //
 // The training step (k_mlp_train_tc) runs forward and backward passes of
 // 128-sample tiles on the same units.  Its backward products read operands

@@ -153,8 +153,8 @@ void launch_tlas_refit(cudaStream_t st, CwNode* nodes, float* node_box, const fl
                        uint32_t end);
 void launch_primary(cudaStream_t st, const DevScene& sc, const DevView& v, float near_z, float far_z, float* depth,
                     float4* const gb[4], float4* hitpos);
-// radiance cache (mlp.cu)
-// (mlp_tc.cu; `err`: a device word that gets bit 1 if a tensor-core wait timed out)
+// radiance cache: the network's tensor-core kernels (mlp_tc.cu; `err`: a device word that gets bit 1 if a
+// tensor-core wait timed out) and Adam (mlp.cu)
 cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const float4* queries, const uint32_t* count,
                              uint32_t capacity, float4* accum, uint32_t* err);
 cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
