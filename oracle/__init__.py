@@ -42,6 +42,8 @@ def lib() -> C.CDLL:
         L.orc_render.argtypes = [vp, vp, u32, u32, u32, u32, u64, f32, f32, u32, u32, vp, vp, i32,
                                  C.POINTER(C.c_double)]
         L.orc_render.restype = i32
+        L.orc_render_cached.argtypes = [vp, vp, u32, u32, u32, u64, f32, f32, vp, u32, f32, u32, u32, vp, vp, i32]
+        L.orc_render_cached.restype = i32
         L.orc_pcg32.argtypes = [u64, u64, u32, vp]
         L.orc_sincos_turns.argtypes = [vp, u32, vp, vp]
         L.orc_atan2.argtypes = [vp, vp, u32, vp]
@@ -215,6 +217,27 @@ class OracleScene:
             raise RuntimeError("orc_render failed")
         return out, stats, sec.value
 
+
+    def render_cached(self, camera: np.ndarray, spp: int, weights: np.ndarray, cache_segment: int,
+                      extra_segments: int = 0, min_roughness: float = 0.0, seed: int = 1, flags: int = 0,
+                      ray_length: float = 100.0, t_min: float = 0.0, rows=None, threads: int = 0):
+        """The cached pass without its training step (bsm_render_cached with train_steps = 0): paths run
+        cache_segment + 1 + extra_segments segments and end in a query of the network with `weights` at the
+        first hit of segment cache_segment or later whose roughness is at least min_roughness (at the last
+        segment whatever its roughness).  Returns (mean RGBA image of the rows, stats[32])."""
+        cam = _f32(camera)
+        w, h = int(cam[10]), int(cam[11])
+        r0, r1 = rows if rows is not None else (0, h)
+        W = _f32(weights)
+        out = np.zeros((r1 - r0, w, 4), np.float32)
+        stats = np.zeros(32, np.uint64)
+        st = self._L.orc_render_cached(self.h, cam.ctypes.data, spp, cache_segment + 1 + extra_segments, flags, seed,
+                                       ray_length, t_min, W.ctypes.data, cache_segment,
+                                       min_roughness if extra_segments else 0.0, r0, r1, out.ctypes.data,
+                                       stats.ctypes.data, threads)
+        if st != 0:
+            raise RuntimeError("orc_render_cached failed")
+        return out, stats
 
     def primary(self, camera: np.ndarray, ray_length: float = 100.0, t_min: float = 0.0, near_z: float = 0.01,
                 far_z: float = 10000.0, seed: int = 1, sample_offset: int = 0, threads: int = 0):

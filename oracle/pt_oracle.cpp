@@ -262,6 +262,7 @@ struct Scene {
     std::vector<float> ptab, aprob;   // sky: pdf per texel, alias keep probability
     std::vector<uint32_t> alias;
     float extent = 1.0f, offset = 0.0f;
+    float box_lo[3] = {0, 0, 0}, box_inv[3] = {1, 1, 1};   // the radiance cache's position normalisation
     // two-level scenes: instances of geometries (each a Scene holding tris + BVH only)
     struct Inst {
         const struct Scene* geo;
@@ -684,7 +685,30 @@ struct Settings {
     uint32_t spp, max_seg, sample_offset, flags;
     uint64_t seed;
     float ray_length, t_min;
+    // radiance cache: hits of segment cache_seg or later whose roughness is at least cache_rough (or that
+    // reach the last segment) end in a query of the network with weights cache_w (0 / null: no cache)
+    uint32_t cache_seg = 0;
+    float cache_rough = 0.0f;
+    const float* cache_w = nullptr;
 };
+
+// The cache network's output for raw inputs `raw` (defined with the network below).
+static void cache_predict(const float* W, const float* raw, float y[3]);
+
+// Raw inputs of a cache query at a path vertex: position normalised to the scene box, outgoing direction and
+// normal as (theta / pi, phi / 2pi + 1/2), roughness, albedo, depth = bounce / 8 (the kernels' mlp_raw_inputs).
+static void cache_raw_inputs(const Scene& S, F3 p, F3 wo, F3 n, float rough, F3 albedo, float depth, float* raw) {
+    raw[0] = (p.x - S.box_lo[0]) * S.box_inv[0];
+    raw[1] = (p.y - S.box_lo[1]) * S.box_inv[1];
+    raw[2] = (p.z - S.box_lo[2]) * S.box_inv[2];
+    raw[3] = atan2_det(std::sqrt(wo.x * wo.x + wo.z * wo.z), wo.y) * kInvPi;
+    raw[4] = atan2_det(wo.z, wo.x) * (0.5f * kInvPi) + 0.5f;
+    raw[5] = atan2_det(std::sqrt(n.x * n.x + n.z * n.z), n.y) * kInvPi;
+    raw[6] = atan2_det(n.z, n.x) * (0.5f * kInvPi) + 0.5f;
+    raw[7] = rough;
+    raw[8] = albedo.x; raw[9] = albedo.y; raw[10] = albedo.z;
+    raw[11] = depth;
+}
 enum { F_JITTER = 1, F_NO_SUN = 2, F_NO_SKY = 4 };
 
 struct PathQ {  // one wavefront queue in the oracle (structure of arrays)
@@ -790,6 +814,15 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                 F3 P = add(q.o[i], muls(d, t));
                 const float* m = &S.mats[8 * (size_t)mat];
                 Surf surf{f3(m[0], m[1], m[2]), f3(m[4], m[5], m[6]), f3(1, 1, 1), m[3], 1.5f};
+                if (st.cache_w && seg >= st.cache_seg && (surf.rough >= st.cache_rough || seg + 1 >= st.max_seg)) {
+                    // a cache query ends the path: throughput x max(prediction, 0), no NEE, no continuation
+                    float raw[12], y[3];
+                    cache_raw_inputs(S, P, neg(d), N, surf.rough, surf.base, (float)seg * 0.125f, raw);
+                    cache_predict(st.cache_w, raw, y);
+                    F3 c = mul(thr, f3(std::fmax(y[0], 0.0f), std::fmax(y[1], 0.0f), std::fmax(y[2], 0.0f)));
+                    a[0] += c.x; a[1] += c.y; a[2] += c.z;
+                    continue;
+                }
                 Frm fr = make_frame(N);
                 F3 V = neg(d);
                 Pcg g = q.rng[i];
@@ -985,6 +1018,10 @@ static bool setup_shading(Scene* S, const float* materials, uint32_t nm, const f
                           const uint16_t* sky_texels, const float* sky_xf, const float lo[3], const float hi[3]) {
     S->extent = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), std::max(hi[2] - lo[2], 1e-6f));
     S->offset = 2e-5f * S->extent;
+    for (int k = 0; k < 3; ++k) {
+        S->box_lo[k] = lo[k];
+        S->box_inv[k] = 1.0f / std::max(hi[k] - lo[k], 1e-6f);
+    }
     S->nmat = nm;
     S->mats.resize(8 * (size_t)nm);
     S->trm.assign(nm, 0.0f);
@@ -1202,13 +1239,36 @@ ORC_API int orc_trace(void* sp, const float* rays, uint32_t n, uint32_t* hits, i
 // camera: pos3 front3 up3 fov w h (12 floats); settings: spp, max_seg, sample_offset, flags (u32),
 // seed (u64), ray_length, t_min.  Renders rows [row_begin, row_end); out = w x (rows) x 4 mean RGBA.
 // stats: [16] extend rays per segment, [16] shadow rays per segment.
+static int render_rows(void* sp, const float* camera, const Settings& st, uint32_t row_begin, uint32_t row_end,
+                       float* out, uint64_t* stats, int threads, double* seconds);
+
 ORC_API int orc_render(void* sp, const float* camera, uint32_t spp, uint32_t max_seg, uint32_t sample_offset,
                        uint32_t flags, uint64_t seed, float ray_length, float t_min, uint32_t row_begin,
                        uint32_t row_end, float* out, uint64_t* stats, int threads, double* seconds) {
+    Settings st{spp, max_seg, sample_offset, flags, seed, ray_length, t_min};
+    return render_rows(sp, camera, st, row_begin, row_end, out, stats, threads, seconds);
+}
+
+// The cached pass (bsm_render_cached without its training step): paths end in a query of the network with
+// weights W (kMlpParams floats, rounded to bfloat16 as the kernels' copies are) at segment cache_seg.
+ORC_API int orc_render_cached(void* sp, const float* camera, uint32_t spp, uint32_t max_seg, uint32_t flags,
+                              uint64_t seed, float ray_length, float t_min, const float* W, uint32_t cache_seg,
+                              float cache_rough, uint32_t row_begin, uint32_t row_end, float* out, uint64_t* stats,
+                              int threads) {
+    if (!W || cache_seg == 0 || cache_seg >= max_seg) return -1;
+    Settings st{spp, max_seg, 0, flags, seed, ray_length, t_min};
+    st.cache_seg = cache_seg;
+    st.cache_rough = cache_rough;
+    st.cache_w = W;
+    return render_rows(sp, camera, st, row_begin, row_end, out, stats, threads, nullptr);
+}
+
+static int render_rows(void* sp, const float* camera, const Settings& st, uint32_t row_begin, uint32_t row_end,
+                       float* out, uint64_t* stats, int threads, double* seconds) {
     const Scene& S = *(Scene*)sp;
     Cam K = make_cam(camera);
+    const uint32_t spp = st.spp, max_seg = st.max_seg;
     if (row_end > K.h || row_begin >= row_end || max_seg == 0 || max_seg > 16 || spp == 0) return -1;
-    Settings st{spp, max_seg, sample_offset, flags, seed, ray_length, t_min};
     uint32_t p0 = row_begin * K.w, p1 = row_end * K.w;
     std::vector<float> acc(3 * (size_t)(p1 - p0), 0.0f);
     const uint32_t tile = 256;  // 16 x 16 pixels worth of paths per task
@@ -1645,6 +1705,11 @@ static void mlp_fwd(const float* W, const float* raw, bool bf, MlpAct& A) {
         for (int i = 0; i < 64; ++i) z += bf16r(W4[o * 64 + i], bf) * in[i];
         A.y[o] = o < 3 ? z : 0.0f;
     }
+}
+static void cache_predict(const float* W, const float* raw, float y[3]) {
+    MlpAct A;
+    mlp_fwd(W, raw, true, A);
+    for (int c = 0; c < 3; ++c) y[c] = A.y[c];
 }
 }  // namespace orc
 

@@ -50,9 +50,10 @@ def test_forward_sizes_match_oracle(cache, oracle, n):
     assert np.abs(g - o).max() <= 1e-2 * scale + 1e-5
 
 
-@pytest.mark.parametrize("n", [64, 20_000])
+@pytest.mark.parametrize("n", [1, 64, 129, 20_000])
 def test_gradient_sizes_match_oracle(cache, oracle, n):
-    """One 64-sample group, and several groups per block of the training kernel."""
+    """One sample, part of one 128-sample tile, a full tile and one row of a second, and more tiles than SMs
+    (so that CTAs of the training kernel take several tiles and reduce their gradients on the last)."""
     S = random_samples(n, 20 + n % 89)
     W = cache.weights()
     dg, lg = cache.gradient(S)
@@ -237,3 +238,33 @@ def test_cached_render_as_the_first_call_of_a_context(bsm):
     a, b = images[0][..., :3].astype(np.float64), images[1][..., :3].astype(np.float64)
     assert np.isfinite(a).all() and np.isfinite(b).all()
     assert np.abs(a - b).mean() <= 1e-2 * np.abs(b).mean()
+
+
+@pytest.mark.parametrize("extra, min_rough", [(0, 0.0), (2, 0.5)])
+def test_cached_render_matches_oracle(bsm, ctx, oracle, extra, min_rough):
+    """The cached pass without its training step (bsm_render_cached, train_steps = 0) against the oracle's
+    cached pass with the same network weights: the paths agree up to their cache vertex (equal rays per
+    segment), and the radiance agrees within the network's tolerance.  The cache-vertex terms differ only by
+    the two networks' arithmetic (BF16 products with sums in another order; the encoding's base sine and
+    cosine from the special-function unit on the GPU, which can move a BF16 feature by one step).  With
+    extra segments, hits smoother than min_roughness shade and continue, and the last segment queries."""
+    scene = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=41, spheres=24)
+    sid = ctx.load_scene(scene)
+    cam = bsm.make_camera(tuple(scene.camera.position), tuple(scene.camera.front), width=64, height=48)
+    c = bsm.RadianceCache(ctx, seed=5)
+    try:
+        W = c.weights()
+        cs = bsm.cache_settings(cache_segment=2, train_steps=0, extra_segments=extra, min_roughness=min_rough)
+        img, st, _ = c.render(sid, cam, bsm.settings(spp=4, seed=9), cs)
+        ref, ost = oracle.OracleScene(scene).render_cached(cam.as_array(), spp=4, weights=W, cache_segment=2,
+                                                            extra_segments=extra, min_roughness=min_rough, seed=9)
+        segs = 3 + extra
+        assert [int(x) for x in st.rays_per_segment[:segs]] == [int(x) for x in ost[:segs]]
+        g, o = img[..., :3].astype(np.float64), ref[..., :3].astype(np.float64)
+        assert o.mean() > 0.0
+        err = np.abs(g - o)
+        assert err.max() <= 2e-2 * max(float(np.abs(o).max()), 1e-3)
+        assert np.median(err / np.maximum(np.abs(o), 1e-3 * o.mean())) <= 1e-3
+    finally:
+        c.close()
+        ctx.release(sid)
