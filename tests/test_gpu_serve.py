@@ -92,3 +92,26 @@ def test_scenes_locked_while_serving(bsm, served):
             ctx.upload(scenes[0])
     finally:
         ctx.server_stop()
+
+
+def test_small_request_passes_a_large_one_of_the_same_scene(bsm, served):
+    """Least work first within a scene: a small request submitted just after a large one of the same scene joins
+    the next chunk and finishes long before the large one, whose image is still the same as rendered alone."""
+    ctx, scenes, ids = served
+    base = scenes[2].camera
+    large = bsm.make_camera(tuple(base.position), tuple(base.front), width=640, height=480)
+    small = bsm.make_camera(tuple(base.position), tuple(base.front), width=32, height=24)
+    ctx.server_start(pool_bytes=64 << 20, chunk_paths=1 << 16, lanes=2)
+    try:
+        rid_l, img_l = ctx.submit(ids[2], large, 8, 8, 5)
+        rid_s, img_s = ctx.submit(ids[2], small, 1, 4, 6)
+        st_s = ctx.wait(rid_s, timeout_ms=60000)
+        st_l = ctx.wait(rid_l, timeout_ms=60000)
+        assert st_s.state == bsm.BSM_REQ_DONE and st_l.state == bsm.BSM_REQ_DONE
+        assert st_s.done_ms < st_l.done_ms
+    finally:
+        ctx.server_stop()
+    ref_l, _ = ctx.render(ids[2], [large], bsm.settings(spp=8, max_segments=8, seed=5))
+    ref_s, _ = ctx.render(ids[2], [small], bsm.settings(spp=1, max_segments=4, seed=6))
+    assert rel_err(img_l, ref_l[0]).max() <= RTOL
+    assert rel_err(img_s, ref_s[0]).max() <= RTOL
