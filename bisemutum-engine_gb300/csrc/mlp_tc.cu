@@ -1,5 +1,5 @@
-// mlp_tc.cu — the radiance cache's forward pass on the 5th-generation tensor
-// cores (tcgen05, accumulators in tensor memory).
+// mlp_tc.cu — the radiance cache's network on the 5th-generation tensor cores
+// (tcgen05, accumulators in tensor memory): inference and the training step.
 //
 // A CTA of 128 threads takes 128 queries at a time; thread i owns query row i.
 // Each layer is one 128 x N x 64 product, D[query][out] = sum_in
@@ -13,8 +13,10 @@
 // the 16-byte chunk c of row r sits at chunk c ^ (r mod 8).  The K = 16 step
 // k starts 32 k bytes into the rows.  tcgen05.commit signals an mbarrier when
 // the four products are done; each warp then reads its 32 rows of D
-// (tcgen05.ld 32x32b), applies ReLU, rounds to BF16 and writes them back as
-// the next layer's A.  Rounding points (BF16 operands, FP32 accumulation) are
+// (tcgen05.ld 32x32b, 64 columns at once), applies ReLU and rounds to BF16 in
+// one conversion per pair, and writes them back as the next layer's A.  The
+// weights reach shared memory by one bulk copy: their BF16 copies are kept in
+// global memory in the tile layout (mlp_tile_index).  Rounding points (BF16 operands, FP32 accumulation) are
 // those of the oracle's BF16 network; only the order of the FP32 sums differs.
 //
 // The training step (k_mlp_train_tc) runs forward and backward passes of
