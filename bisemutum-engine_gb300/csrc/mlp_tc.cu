@@ -4,19 +4,23 @@
 // A CTA of 128 threads takes 128 queries at a time; thread i owns query row i.
 // Each layer is one 128 x N x 64 product, D[query][out] = sum_in
 // act[query][in] W[out][in], issued as four K = 16 tcgen05.mma by one thread:
-//   A  activations, 128 rows x 64 BF16 in shared memory (16 KB)
+//   A  activations, 128 rows x 64 BF16 in tensor memory: lane = query row,
+//      32 columns of BF16 pairs (feature 2j in the low half of column j)
 //   B  the layer's weights, N rows x 64 BF16 in shared memory (N = 64, or 16
 //      for the output layer: 8 weight rows and 8 zero rows)
 //   D  FP32 in tensor memory: lane = query row, column = output feature.
-// Both operands are K-major with the 128-byte swizzle: a row of 64 BF16 is
-// one 128-byte swizzle row, rows come in 8-row groups 1024 bytes apart, and
-// the 16-byte chunk c of row r sits at chunk c ^ (r mod 8).  The K = 16 step
-// k starts 32 k bytes into the rows.  tcgen05.commit signals an mbarrier when
-// the four products are done; each warp then reads its 32 rows of D
-// (tcgen05.ld 32x32b, 64 columns at once), applies ReLU and rounds to BF16 in
-// one conversion per pair, and writes them back as the next layer's A.  The
-// weights reach shared memory by one bulk copy: their BF16 copies are kept in
-// global memory in the tile layout (mlp_tile_index).  Rounding points (BF16 operands, FP32 accumulation) are
+// B is K-major with the 128-byte swizzle: a row of 64 BF16 is one 128-byte
+// swizzle row, rows come in 8-row groups 1024 bytes apart, and the 16-byte
+// chunk c of row r sits at chunk c ^ (r mod 8).  The K = 16 step k starts
+// 32 k bytes into B's rows and 8 k columns into A.  tcgen05.commit signals an
+// mbarrier when the four products are done; each warp then reads its 32 rows
+// of D (tcgen05.ld 32x32b, 64 columns at once), applies ReLU and rounds to
+// BF16 in one conversion per pair, and stores them (tcgen05.st, 32 columns)
+// as the next layer's A.  Keeping A in tensor memory leaves shared memory
+// with the weights alone: a layer moves 8 KB through it instead of 16 KB of
+// stores and 24 KB of operand reads.  The weights reach shared memory by one
+// bulk copy: their BF16 copies are kept in global memory in the tile layout
+// (mlp_tile_index).  Rounding points (BF16 operands, FP32 accumulation) are
 // those of the oracle's BF16 network; only the order of the FP32 sums differs.
 //
 // The training step (k_mlp_train_tc) runs forward and backward passes of
@@ -47,13 +51,16 @@ namespace {
 constexpr int kTcRows = 128;                                    // queries per tile (MMA M)
 constexpr int kTcW4Rows = 16;                                   // output layer as an N = 16 product
 constexpr int kTcWRows = kMlpHidden * 64 + kTcW4Rows;           // 272 weight rows in shared memory
-constexpr int kTcActOff = kTcWRows * 128;                       // 34816 = 34 x 1024
-constexpr int kTcBarOff = kTcActOff + kTcRows * 128;            // 51200
-constexpr int kTcSmem = kTcBarOff + 32 + 1024;                  // + slack to align the base to 1024
+constexpr int kTcBarOff = kTcWRows * 128;                       // 34816 = 34 x 1024
+// The inference kernel's request: its 36 KB (weights, barriers, alignment slack) padded to 48 KB so that at
+// most 4 CTAs share an SM, the number whose tensor memory fits (4 x 128 of 512 columns); a fifth CTA would
+// wait in tcgen05.alloc until one of the four has finished all its tiles.
+constexpr int kTcSmem = 48 * 1024;
+static_assert(kTcBarOff + 32 + 1024 <= kTcSmem, "inference shared memory");
 constexpr uint32_t kTcWBytes = (kMlpHidden * 64 + kMlpOutPad) * 128;   // 33,792: the weights' tile image
-constexpr uint32_t kTcCols = 64;                                // tensor-memory columns per CTA
+constexpr uint32_t kTcCols = 128;                               // tensor-memory columns per CTA
+constexpr uint32_t kTcACol = 64;                                // first column of the A operand (32 columns)
 constexpr uint32_t kTcErrTimeout = 2u;                          // error word bit: a tensor-core wait timed out
-static_assert(kTcActOff % 1024 == 0, "swizzled tiles start on 1024-byte boundaries");
 
 // Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16
 // A and B (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at
@@ -152,6 +159,15 @@ __device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint3
         "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
         : "memory");
 }
+// The same with A read from tensor memory (`a`: its first column, lane 0).
+__device__ __forceinline__ void tc_mma_ts(uint32_t d, uint32_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d),
+        "r"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
 __device__ __forceinline__ void tc_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
@@ -225,6 +241,20 @@ __device__ __forceinline__ void tc_ld64(uint32_t taddr, uint32_t (&v)[64]) {
                  : "memory");
 }
 
+// 32 columns of the warp's 32 lanes stored, then waited for (the stores complete before the thread goes on).
+__device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&v)[32]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {"
+                 "%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+                 "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32"
+                 "};" ::"r"(taddr),
+                 "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+                 "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]),
+                 "r"(v[16]), "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]),
+                 "r"(v[24]), "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31])
+                 : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
@@ -255,33 +285,34 @@ __device__ __forceinline__ void load_weights_async(const __nv_bfloat16* w, unsig
     if (tid < 64) *tile_chunk(base, kMlpHidden * 64 + kMlpOutPad + (tid >> 3), tid & 7) = make_uint4(0u, 0u, 0u, 0u);
 }
 
-// Encoded features of one query (the encoding of mlp_feature), written as
-// row r of the activation tile: chunk d < 7 holds sin/cos(2^k pi raw[d]),
-// k = 0..3; chunk 7 holds raw[7..11], 1, 0, 0.  The base frequency comes from
+// Encoded features of one query (the encoding of mlp_feature) as 32 BF16
+// pairs, feature 2j in the low half of word j: words 4d..4d+3 (d < 7) hold
+// sin/cos(2^k pi raw[d]), k = 0..3; words 28..31 hold raw[7..11], 1, 0, 0.
+// The base frequency comes from
 // the special-function unit (__sincosf: absolute error below 2^-21 for
 // arguments in [-pi, pi], which pi raw[d] is for the normalised inputs);
 // frequencies k > 0 come from k - 1 by the double-angle identities
 // (sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)(cos a + sin a)).  Both
 // errors lie far below the BF16 rounding that follows; the training and the
 // inference kernels share this encoding.
-__device__ __forceinline__ void encode_row(const float (&raw)[kMlpRaw], unsigned char* act, int r) {
+__device__ __forceinline__ void encode_words(const float (&raw)[kMlpRaw], uint32_t (&p)[32]) {
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
-        uint32_t p[4];
         float s, c;
         __sincosf(raw[d] * 3.14159265f, &s, &c);
-        p[0] = pack2(s, c);
+        p[4 * d] = pack2(s, c);
 #pragma unroll
         for (int k = 1; k < 4; ++k) {
             float s2 = 2.0f * s * c, c2 = (c - s) * (c + s);
             s = s2;
             c = c2;
-            p[k] = pack2(s, c);
+            p[4 * d + k] = pack2(s, c);
         }
-        *tile_chunk(act, r, d) = make_uint4(p[0], p[1], p[2], p[3]);
     }
-    *tile_chunk(act, r, 7) =
-        make_uint4(pack2(raw[7], raw[8]), pack2(raw[9], raw[10]), pack2(raw[11], 1.0f), pack2(0.0f, 0.0f));
+    p[28] = pack2(raw[7], raw[8]);
+    p[29] = pack2(raw[9], raw[10]);
+    p[30] = pack2(raw[11], 1.0f);
+    p[31] = pack2(0.0f, 0.0f);
 }
 
 // kInfer: queries (4 float4: raw[0..11], then throughput rgb and the pixel
@@ -296,8 +327,7 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
     const uint32_t raw_s = smem_u32(smem_raw);
     const uint32_t base_s = (raw_s + 1023u) & ~1023u;
     unsigned char* base = smem_raw + (base_s - raw_s);
-    unsigned char* act = base + kTcActOff;
-    const uint32_t act_s = base_s + kTcActOff, bar = base_s + kTcBarOff;
+    const uint32_t bar = base_s + kTcBarOff;
     const uint32_t wbar = bar + 8;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kTcBarOff + 16);
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -336,11 +366,13 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
                 raw[4 * k] = next[k].x; raw[4 * k + 1] = next[k].y; raw[4 * k + 2] = next[k].z; raw[4 * k + 3] = next[k].w;
             }
             fetch(row + gridDim.x * kTcRows, next);
-            encode_row(raw, act, tid);
+            uint32_t p[32];
+            encode_words(raw, p);
+            tc_st32(rows_tmem + kTcACol, p);
         }
         const bool w_ok = weights || mbar_wait(wbar, 0);
         weights = true;
-        fence_async_smem();
+        fence_async_smem();   // the zeroed weight rows
         tc_fence_before();
         if (__syncthreads_or(!w_ok)) { failed = true; break; }
         for (int l = 0; l <= kMlpHidden; ++l) {
@@ -349,7 +381,7 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
                 const uint32_t w_s = base_s + l * 64 * 128;
                 const uint32_t idesc = l < kMlpHidden ? tc_idesc(kTcRows, 64) : tc_idesc(kTcRows, kTcW4Rows);
 #pragma unroll
-                for (int k = 0; k < 4; ++k) tc_mma(tmem, tc_sdesc(act_s + 32 * k), tc_sdesc(w_s + 32 * k), idesc, k);
+                for (int k = 0; k < 4; ++k) tc_mma_ts(tmem, tmem + kTcACol + 8 * k, tc_sdesc(w_s + 32 * k), idesc, k);
                 tc_commit(bar);
             }
             __syncwarp();
@@ -358,16 +390,11 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
             __syncwarp();   // the tensor-memory loads below are warp-collective
             tc_fence_after();
             if (l < kMlpHidden) {
-                uint32_t v[64];
+                uint32_t v[64], p[32];
                 tc_ld64(rows_tmem, v);
 #pragma unroll
-                for (int c = 0; c < 8; ++c) {   // 8 columns = one chunk of the next layer's input
-                    uint32_t p[4];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        p[i] = pack2_relu(__uint_as_float(v[8 * c + 2 * i]), __uint_as_float(v[8 * c + 2 * i + 1]));
-                    *tile_chunk(act, tid, c) = make_uint4(p[0], p[1], p[2], p[3]);
-                }
+                for (int i = 0; i < 32; ++i) p[i] = pack2_relu(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+                tc_st32(rows_tmem + kTcACol, p);   // the next layer's A
             } else {
                 uint32_t v[16];
                 tc_ld16(rows_tmem, v);
@@ -383,7 +410,6 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
                     }
                 }
             }
-            fence_async_smem();
             tc_fence_before();
             if (__syncthreads_or(!done)) { failed = true; break; }
         }
@@ -455,7 +481,7 @@ __device__ __forceinline__ void relu_grad_chunks(const uint32_t (&v)[kN], int c,
 
 // Half h of the encoded features of one sample, written into row r of the activation tile: h = 0 encodes
 // raw[0..3] (f0) as chunks 0..3; h = 1 encodes raw[4..6] (f0.xyz) as chunks 4..6 and writes chunk 7 from
-// raw[7] = f0.w and raw[8..11] = f1.  The values are those of encode_row.
+// raw[7] = f0.w and raw[8..11] = f1.  The values are those of encode_words.
 __device__ __forceinline__ void encode_half(int h, const float4& f0, const float4& f1, unsigned char* act, int r) {
     const float x[4] = {f0.x, f0.y, f0.z, f0.w};
 #pragma unroll
@@ -731,7 +757,7 @@ cudaError_t tc_setup(int device) {
         int sms = 0;
         cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
         if (e != cudaSuccess) return e;
-        g_tc_grid[device] = sms * 4;   // 4 CTAs per SM: 4 x 53 KB shared memory, 4 x 64 of 512 tensor-memory columns
+        g_tc_grid[device] = sms * 4;   // 4 CTAs per SM: 4 x 128 of 512 tensor-memory columns
     }
     return cudaSuccess;
 }
