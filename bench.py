@@ -88,6 +88,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--jitter", action="store_true", help="jitter the camera ray inside the pixel per sample")
+    p.add_argument("--deterministic", action="store_true",
+                   help="plain pass: bit-reproducible fixed-point accumulation (BSM_PT_DETERMINISTIC)")
     return p.parse_args()
 
 
@@ -97,6 +99,7 @@ def workload_config(a, tris=None):
             "scene_triangles": tris, "width": a.width, "height": a.height, "spp": a.spp,
             "max_segments": a.segments, "sky": "1024x512 RGBA16F equirect + alias table", "seed": a.seed,
             "camera": "jittered inside the pixel per sample" if a.jitter else "pixel-centre rays (as the reference)",
+            **({"accumulation": "32.32 fixed point (BSM_PT_DETERMINISTIC)"} if a.deterministic else {}),
             "parallelism": "replicas" if a.gpus > 1 else "single GPU",
             "l2": "inputs larger than L2 (the wavefront queues hold up to 2^27 paths, 312 B each: 41 GB for "
                   "the 1920x1080x64 frame) and a 512 MB device copy between timed steps flushes L2"}
@@ -279,6 +282,8 @@ def run_ours(a, dist: Dist):
     cam = scene.camera
     seed = a.seed + 1000 * dist.rank
     jitter = bsm.BSM_PT_JITTER if a.jitter else 0
+    if a.deterministic:
+        jitter |= bsm.BSM_PT_DETERMINISTIC
     flags_timed = bsm.BSM_PT_STAGE_TIMING | jitter
     s_timed = bsm.settings(spp=a.spp, max_segments=a.segments, seed=seed, flags=flags_timed, block_size=a.block,
                            wavefront_capacity=a.capacity)

@@ -33,6 +33,7 @@ BSM_SKY_CONSTANT, BSM_SKY_EQUIRECT, BSM_SKY_CUBEMAP = 0, 1, 2
 BSM_SCENE_ROOM, BSM_SCENE_TERRAIN = 0, 1
 BSM_PT_JITTER, BSM_PT_NO_SUN_NEE, BSM_PT_NO_SKY_NEE, BSM_PT_STAGE_TIMING, BSM_PT_NO_GRAPH = 1, 2, 4, 8, 16
 BSM_PT_COUNT_TRAVERSAL = 32
+BSM_PT_DETERMINISTIC = 64
 MISS = 0xFFFFFFFF
 
 

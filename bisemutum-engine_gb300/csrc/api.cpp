@@ -113,6 +113,7 @@ struct bsm_context {
     DevBuf views_dev;
     std::vector<DevView> views_host;
     DevBuf accum;                 // float4 per pixel, all views
+    DevBuf accum_fx;              // BSM_PT_DETERMINISTIC: one call's 32.32 fixed-point sums, 3 words per pixel
     std::vector<ViewHist> hist;   // per view index
     std::vector<std::pair<uint32_t, uint32_t>> layout;  // (width, height) per view
     DevBuf out_stage;             // device staging for host outputs
@@ -433,6 +434,7 @@ extern "C" void bsm_destroy(bsm_context* ctx) {
     dev_free(ctx, ctx->wf_buf);
     dev_free(ctx, ctx->views_dev);
     dev_free(ctx, ctx->accum);
+    dev_free(ctx, ctx->accum_fx);
     dev_free(ctx, ctx->out_stage);
     dev_free(ctx, ctx->tmp);
     for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
@@ -1332,13 +1334,18 @@ namespace {
 // stream when a graph is being recorded, else the work stream).
 // With `ev` non-null an event is recorded after every launch (no host waits):
 // ev[0] before the first launch, then one per stage; `tags` gets the stage of
-// each interval (0 camera, 1 extend, 2 shade, 3 shadow).
+// each interval (0 camera, 1 extend, 2 shade, 3 shadow).  With `fx_px` > 0
+// (BSM_PT_DETERMINISTIC) the contributions go to fixed-point sums over the
+// call's fx_px accumulator pixels, added to the FP32 accumulator at the end.
 void record_render(bsm_context* ctx, cudaStream_t st, const Scene* sc, uint32_t n_views, uint64_t total_paths,
                    uint32_t capacity, uint32_t max_seg, bool count_traversal, std::vector<cudaEvent_t>* ev,
-                   std::vector<int>* tags, const void* cache_wb = nullptr) {
+                   std::vector<int>* tags, const void* cache_wb = nullptr, uint32_t fx_px = 0) {
     const LaunchCfg& lc = ctx->lc;
     const DevView* views = (const DevView*)ctx->views_dev.ptr;
     float4* accum = (float4*)ctx->accum.ptr;
+    Wavefront wf = ctx->wf;
+    wf.accum_fx = fx_px ? (unsigned long long*)ctx->accum_fx.ptr : nullptr;
+    if (fx_px) cudaMemsetAsync(wf.accum_fx, 0, (size_t)fx_px * 24, st);
     size_t k = 0;
     auto mark = [&](int tag) {
         if (!ev) return;
@@ -1353,23 +1360,24 @@ void record_render(bsm_context* ctx, cudaStream_t st, const Scene* sc, uint32_t 
     mark(-1);
     for (uint64_t begin = 0; begin < total_paths; begin += capacity) {
         uint32_t count = (uint32_t)std::min<uint64_t>(capacity, total_paths - begin);
-        cudaMemsetAsync(ctx->wf.counters, 0, kCntError * 4, st);
-        launch_camera(lc, st, views, n_views, begin, count, ctx->wf, max_seg);
+        cudaMemsetAsync(wf.counters, 0, kCntError * 4, st);
+        launch_camera(lc, st, views, n_views, begin, count, wf, max_seg);
         mark(0);
         int q = 0;
         for (uint32_t seg = 0; seg < max_seg; ++seg) {
-            launch_extend(lc, st, sc->dev, ctx->wf, q, seg, count_traversal);
+            launch_extend(lc, st, sc->dev, wf, q, seg, count_traversal);
             mark(1);
-            launch_shade(lc, st, sc->dev, views, ctx->wf, q, seg, accum, cache_wb != nullptr);
+            launch_shade(lc, st, sc->dev, views, wf, q, seg, accum, cache_wb != nullptr);
             mark(2);
-            launch_shadow(lc, st, sc->dev, ctx->wf, seg, accum);
+            launch_shadow(lc, st, sc->dev, wf, seg, accum);
             mark(3);
             q ^= 1;
         }
         if (cache_wb)
-            launch_mlp_infer(ctx->device, st, cache_wb, ctx->wf.cache_q, ctx->wf.counters + kCntCache, capacity, accum,
-                             ctx->wf.counters + kCntError);
+            launch_mlp_infer(ctx->device, st, cache_wb, wf.cache_q, wf.counters + kCntCache, capacity, accum,
+                             wf.accum_fx, wf.counters + kCntError);
     }
+    if (fx_px) launch_fold_fixed(st, wf.accum_fx, accum, fx_px);
 }
 
 }  // namespace
@@ -1500,25 +1508,32 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
     bool timing = (s.flags & BSM_PT_STAGE_TIMING) != 0;
     bool counting = (s.flags & BSM_PT_COUNT_TRAVERSAL) != 0;
     bool use_graph = !timing && !counting && !(s.flags & BSM_PT_NO_GRAPH);
+    const uint32_t fx_px = (s.flags & BSM_PT_DETERMINISTIC) ? (uint32_t)total_px : 0u;
+    if (fx_px && ctx->accum_fx.bytes < (size_t)fx_px * 24) {
+        cudaStreamSynchronize(WS(ctx));   // earlier renders may still add to the old sums
+        clear_graphs(ctx);
+        if ((st = dev_alloc(ctx, ctx->accum_fx, (size_t)fx_px * 24))) return st;
+    }
     float stage_ms[4] = {0, 0, 0, 0};
     std::vector<int> tags;
     if (!start_recorded) CK(cudaEventRecord(ctx->ev[8], WS(ctx)));   // start of the device time of this render
     if (use_graph) {
         // key: everything the recorded launches depend on
-        std::vector<uint8_t> key(64);
-        uint64_t kv[8] = {(uint64_t)scene_id, (uint64_t)n_views, total_paths,
+        std::vector<uint8_t> key(72);
+        uint64_t kv[9] = {(uint64_t)scene_id, (uint64_t)n_views, total_paths,
                           capacity | ((uint64_t)ctx->lc.postpone_sp << 32) | ((uint64_t)ctx->lc.refill_min << 40),
                           max_seg | ((uint64_t)(uintptr_t)cache_wb << 8), (uint64_t)(uintptr_t)ctx->wf_buf.ptr,
                           (uint64_t)(uintptr_t)ctx->accum.ptr,
-                          (uint64_t)(uintptr_t)ctx->views_dev.ptr ^ ((uint64_t)ctx->lc_block << 56)};
-        std::memcpy(key.data(), kv, 64);
+                          (uint64_t)(uintptr_t)ctx->views_dev.ptr ^ ((uint64_t)ctx->lc_block << 56),
+                          fx_px ? (uint64_t)(uintptr_t)ctx->accum_fx.ptr : 0u};
+        std::memcpy(key.data(), kv, 72);
         cudaGraphExec_t exec = nullptr;
         for (auto& g : ctx->graphs) if (g.key == key) exec = g.exec;
         if (!exec) {
             cudaGraph_t graph;
             CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
             record_render(ctx, ctx->stream, sc, n_views, total_paths, capacity, max_seg, false, nullptr, nullptr,
-                          cache_wb);
+                          cache_wb, fx_px);
             CK(cudaStreamEndCapture(ctx->stream, &graph));
             CK(cudaGraphInstantiate(&exec, graph, 0));
             cudaGraphDestroy(graph);
@@ -1531,7 +1546,7 @@ bsm_status render_impl(bsm_context* ctx, uint32_t scene_id, const std::vector<Vi
         CK(cudaGraphLaunch(exec, WS(ctx)));
     } else {
         record_render(ctx, WS(ctx), sc, n_views, total_paths, capacity, max_seg, counting,
-                      timing ? &ctx->stage_ev : nullptr, &tags, cache_wb);
+                      timing ? &ctx->stage_ev : nullptr, &tags, cache_wb, fx_px);
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[9], WS(ctx)));

@@ -317,12 +317,13 @@ __device__ __forceinline__ void encode_words(const float (&raw)[kMlpRaw], uint32
 
 // kInfer: queries (4 float4: raw[0..11], then throughput rgb and the pixel
 // accumulator index bits), n = min(*count, n_max); adds throughput x max(y, 0)
-// to the accumulator.  Otherwise: samples (raw in the first 3 float4), n =
+// to the accumulator (to the fixed-point sums `accum_fx` when set).  Otherwise: samples (raw in the first 3 float4), n =
 // n_max, writes y (3 floats per sample) to out.
 template <bool kInfer>
 __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16* __restrict__ w,
                                                             const float4* __restrict__ q, const uint32_t* count,
-                                                            uint32_t n_max, float4* accum, float* out, uint32_t* err) {
+                                                            uint32_t n_max, float4* accum,
+                                                            unsigned long long* accum_fx, float* out, uint32_t* err) {
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw_s = smem_u32(smem_raw);
     const uint32_t base_s = (raw_s + 1023u) & ~1023u;
@@ -401,8 +402,9 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
                 float y0 = __uint_as_float(v[0]), y1 = __uint_as_float(v[1]), y2 = __uint_as_float(v[2]);
                 if (done && row < n) {
                     if (kInfer) {
-                        atomicAdd(accum + __float_as_uint(m.w),
-                                  make_float4(m.x * fmaxf(y0, 0.0f), m.y * fmaxf(y1, 0.0f), m.z * fmaxf(y2, 0.0f), 0.0f));
+                        const float c0 = m.x * fmaxf(y0, 0.0f), c1 = m.y * fmaxf(y1, 0.0f), c2 = m.z * fmaxf(y2, 0.0f);
+                        if (accum_fx) accum_fixed_add(accum_fx, __float_as_uint(m.w), c0, c1, c2);
+                        else atomicAdd(accum + __float_as_uint(m.w), make_float4(c0, c1, c2, 0.0f));
                     } else {
                         out[3 * (size_t)row] = y0;
                         out[3 * (size_t)row + 1] = y1;
@@ -765,11 +767,11 @@ cudaError_t tc_setup(int device) {
 }  // namespace
 
 cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const float4* queries, const uint32_t* count,
-                             uint32_t capacity, float4* accum, uint32_t* err) {
+                             uint32_t capacity, float4* accum, unsigned long long* accum_fx, uint32_t* err) {
     cudaError_t e = tc_setup(device);
     if (e != cudaSuccess) return e;
     k_mlp_forward_tc<true><<<g_tc_grid[device], kTcRows, kTcSmem, st>>>((const __nv_bfloat16*)wb, queries, count, capacity,
-                                                                accum, nullptr, err);
+                                                                accum, accum_fx, nullptr, err);
     return cudaGetLastError();
 }
 
@@ -792,8 +794,8 @@ cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, cons
     if (n == 0) return cudaSuccess;
     uint32_t tiles = (n + kTcRows - 1) / kTcRows;
     uint32_t grid = tiles < (uint32_t)g_tc_grid[device] ? tiles : (uint32_t)g_tc_grid[device];
-    k_mlp_forward_tc<false><<<grid, kTcRows, kTcSmem, st>>>((const __nv_bfloat16*)wb, samples, nullptr, n, nullptr, out,
-                                                            err);
+    k_mlp_forward_tc<false><<<grid, kTcRows, kTcSmem, st>>>((const __nv_bfloat16*)wb, samples, nullptr, n, nullptr,
+                                                            nullptr, out, err);
     return cudaGetLastError();
 }
 

@@ -113,6 +113,9 @@ struct Wavefront {
     float4* sh_c;
     uint32_t* sh_seed;         // [(L+1) C] opacity seeds of the shadow rays (written for non-opaque scenes)
     float4* cache_q;           // radiance-cache queries (4 float4 each), capacity C; may be null
+    // BSM_PT_DETERMINISTIC: the call's per-pixel sums as 32.32 fixed point (3 words per accumulator pixel);
+    // null: contributions go to the FP32 accumulator by atomics
+    unsigned long long* accum_fx;
     uint32_t* counters;
     unsigned long long* stats;
 };
@@ -128,6 +131,18 @@ struct LaunchCfg {
     int regcap = 1;         // 1: traversal kernels compiled for 4 blocks of 256 (64 registers); the default
 };
 
+#if defined(__CUDACC__)
+// Adds the contribution (x, y, z) to accumulator pixel `idx` of 32.32 fixed-point sums: each positive value
+// is rounded once to a multiple of 2^-32 and added as an integer, which makes the sums independent of the
+// order of the additions.  Zero, negative and NaN values add nothing.
+__device__ __forceinline__ void accum_fixed_add(unsigned long long* fx, uint32_t idx, float x, float y, float z) {
+    unsigned long long* p = fx + 3 * (size_t)idx;
+    if (x > 0.0f) atomicAdd(p, __float2ull_rn(x * 4294967296.0f));
+    if (y > 0.0f) atomicAdd(p + 1, __float2ull_rn(y * 4294967296.0f));
+    if (z > 0.0f) atomicAdd(p + 2, __float2ull_rn(z * 4294967296.0f));
+}
+#endif
+
 // ---- launch wrappers (pt_kernels.cu) ----
 void launch_camera(const LaunchCfg& lc, cudaStream_t st, const DevView* views, uint32_t n_views,
                    uint64_t path_begin, uint32_t path_count, const Wavefront& wf, uint32_t max_segments);
@@ -140,6 +155,8 @@ void launch_shadow(const LaunchCfg& lc, cudaStream_t st, const DevScene& sc, con
                    float4* accum);
 void launch_resolve(cudaStream_t st, const float4* accum, uint32_t width, uint32_t height, float inv_spp,
                     float4* out, uint32_t pitch_px);
+// accum[p] += fx[3p .. 3p + 2] * 2^-32 for the n accumulator pixels (one add per pixel: deterministic)
+void launch_fold_fixed(cudaStream_t st, const unsigned long long* fx, float4* accum, uint32_t n);
 void launch_trace_closest(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint4* hits,
                           int block);
 void launch_trace_any(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint8_t* occluded,
@@ -156,7 +173,7 @@ void launch_primary(cudaStream_t st, const DevScene& sc, const DevView& v, float
 // radiance cache: the network's tensor-core kernels (mlp_tc.cu; `err`: a device word that gets bit 1 if a
 // tensor-core wait timed out) and Adam (mlp.cu)
 cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const float4* queries, const uint32_t* count,
-                             uint32_t capacity, float4* accum, uint32_t* err);
+                             uint32_t capacity, float4* accum, unsigned long long* accum_fx, uint32_t* err);
 cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
                                float* out, uint32_t* err);
 // gradient of the mean relative L2 loss over n samples added to dW, the loss to loss[0]; a tensor-core wait

@@ -69,8 +69,11 @@ __device__ __forceinline__ uint32_t block_alloc_by_octant(bool pred, V3 dir, uin
     return pred ? s_base[parity] + s_off[parity][key] + rank : 0u;
 }
 
-__device__ __forceinline__ void accum_add(float4* accum, uint32_t idx, V3 c) {
-    atomicAdd(accum + idx, make_float4(c.x, c.y, c.z, 0.0f));
+// A path's contribution to its pixel: FP32 atomics, or the call's fixed-point sums when `fx` is set
+// (BSM_PT_DETERMINISTIC).
+__device__ __forceinline__ void accum_add(float4* accum, unsigned long long* fx, uint32_t idx, V3 c) {
+    if (fx) accum_fixed_add(fx, idx, c.x, c.y, c.z);
+    else atomicAdd(accum + idx, make_float4(c.x, c.y, c.z, 0.0f));
 }
 
 // ---------------------------------------------------------------- camera ----
@@ -170,7 +173,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_shadow(DevScene sc, Wavefro
         [&](uint32_t i, uint32_t leaf, float, float, float) {
             if (leaf == kMissPrim) {
                 float4 c = scn[slot(i)];
-                accum_add(accum, __float_as_uint(c.w), v3(c.x, c.y, c.z));
+                accum_add(accum, wf.accum_fx, __float_as_uint(c.w), v3(c.x, c.y, c.z));
             }
         },
         [&](uint32_t i) { return wf.sh_seed ? wf.sh_seed[slot(i)] : 0u; },
@@ -215,7 +218,7 @@ __global__ void __launch_bounds__(256, 4) k_shadow2(DevScene sc, Wavefront wf, u
         [&](uint32_t i, uint32_t leaf, float, float, float, uint32_t) {
             if (leaf == kMissPrim) {
                 float4 c = scn[slot(i)];
-                accum_add(accum, __float_as_uint(c.w), v3(c.x, c.y, c.z));
+                accum_add(accum, wf.accum_fx, __float_as_uint(c.w), v3(c.x, c.y, c.z));
             }
         },
         [&](uint32_t i) { return wf.sh_seed ? wf.sh_seed[slot(i)] : 0u; },
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
                 w = pb2 + pl2 > 0.0f ? pb2 / (pb2 + pl2) : 1.0f;
             }
             V3 c = thr * le * w;
-            if (max_comp(c) > 0.0f) accum_add(accum, m4.x, c);
+            if (max_comp(c) > 0.0f) accum_add(accum, wf.accum_fx, m4.x, c);
         }
         // surface at the hit: N shades (the interpolated vertex normal where the scene has them), Ng offsets
         V3 N = v3(0.0f, 0.0f, 1.0f), Ng = N, P = v3(0.0f, 0.0f, 0.0f);
@@ -459,6 +462,18 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
 }
 
 // --------------------------------------------------------------- resolve ----
+// The call's fixed-point sums added to the FP32 accumulator, one add per pixel and channel.
+__global__ void k_fold_fixed(const unsigned long long* __restrict__ fx, float4* __restrict__ accum, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long* p = fx + 3 * (size_t)i;
+    float4 a = accum[i];
+    a.x += (float)((double)p[0] * 0x1p-32);
+    a.y += (float)((double)p[1] * 0x1p-32);
+    a.z += (float)((double)p[2] * 0x1p-32);
+    accum[i] = a;
+}
+
 __global__ void k_resolve(const float4* __restrict__ accum, uint32_t width, uint32_t height, float inv_spp,
                           float4* __restrict__ out, uint32_t pitch) {
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -676,6 +691,10 @@ void launch_resolve(cudaStream_t st, const float4* accum, uint32_t width, uint32
                     float4* out, uint32_t pitch_px) {
     dim3 grid((width + 255) / 256, height);
     k_resolve<<<grid, 256, 0, st>>>(accum, width, height, inv_spp, out, pitch_px);
+}
+void launch_fold_fixed(cudaStream_t st, const unsigned long long* fx, float4* accum, uint32_t n) {
+    if (n == 0) return;
+    k_fold_fixed<<<(n + 255) / 256, 256, 0, st>>>(fx, accum, n);
 }
 void launch_trace_closest(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint4* hits,
                           int block) {

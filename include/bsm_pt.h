@@ -253,7 +253,13 @@ enum {
     BSM_PT_NO_SKY_NEE = 1u << 2,    /* sky only through BSDF-sampled escapes */
     BSM_PT_STAGE_TIMING = 1u << 3,  /* record per-stage CUDA events into bsm_render_stats */
     BSM_PT_NO_GRAPH = 1u << 4,      /* launch stages directly instead of replaying a CUDA graph */
-    BSM_PT_COUNT_TRAVERSAL = 1u << 5 /* count BVH nodes visited / triangles tested by the extend stage */
+    BSM_PT_COUNT_TRAVERSAL = 1u << 5, /* count BVH nodes visited / triangles tested by the extend stage */
+    BSM_PT_DETERMINISTIC = 1u << 6  /* bit-reproducible images: the call's contributions are summed per pixel
+                                       as 32.32 fixed-point integers (exact, so the order of the additions does
+                                       not matter) and added to the view's history once; contributions are
+                                       non-negative and below 2^31 each.  Default: FP32 atomics, whose last bits
+                                       depend on the order in which the GPU adds them. bsm_render,
+                                       bsm_render_batch and bsm_render_cached; the serving loop ignores it */
 };
 
 typedef struct bsm_pt_settings {
