@@ -709,7 +709,17 @@ static void cache_raw_inputs(const Scene& S, F3 p, F3 wo, F3 n, float rough, F3 
     raw[8] = albedo.x; raw[9] = albedo.y; raw[10] = albedo.z;
     raw[11] = depth;
 }
-enum { F_JITTER = 1, F_NO_SUN = 2, F_NO_SKY = 4 };
+enum { F_JITTER = 1, F_NO_SUN = 2, F_NO_SKY = 4, F_FIXED = 64 };
+
+// F_FIXED (the library's BSM_PT_DETERMINISTIC, pt_device.h accum_fixed_add and pt_kernels.cu k_fold_fixed):
+// a contribution value x > 0 as a 32.32 fixed-point integer, x * 2^32 rounded to nearest even (saturating);
+// the pixel's sum of these is exact, so it does not depend on the order of the additions.
+static uint64_t fixed32(float x) {
+    if (!(x > 0.0f)) return 0;
+    const float y = x * 4294967296.0f;
+    if (y >= 18446744073709551616.0f) return UINT64_MAX;
+    return (uint64_t)std::nearbyint((double)y);
+}
 
 struct PathQ {  // one wavefront queue in the oracle (structure of arrays)
     std::vector<F3> o, d, thr;
@@ -760,11 +770,17 @@ static bool light_sample(const Scene::Light& L, F3 P, float u0, float u1, float 
 }
 
 // Renders pixels [pix_begin, pix_end) of one camera; `acc` receives RGB sums
-// (3 floats per pixel, indexed from pix_begin).
+// (3 floats per pixel, indexed from pix_begin), or `fx` their 32.32 fixed-point
+// sums (F_FIXED).
 static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32_t pix_begin, uint32_t pix_end,
-                        float* acc, uint64_t* ext_cnt, uint64_t* sh_cnt) {
+                        float* acc, uint64_t* fx, uint64_t* ext_cnt, uint64_t* sh_cnt) {
     PathQ q, nq;
     ShadowQ sq;
+    auto add_px = [&](uint32_t pix, F3 c) {
+        const size_t k = 3 * (size_t)(pix - pix_begin);
+        if (fx) { fx[k] += fixed32(c.x); fx[k + 1] += fixed32(c.y); fx[k + 2] += fixed32(c.z); }
+        else { acc[k] += c.x; acc[k + 1] += c.y; acc[k + 2] += c.z; }
+    };
     for (uint32_t s = 0; s < st.spp; ++s) {
         q.clear();
         // camera (generate_camera_ray.hlsl:9-15)
@@ -791,7 +807,6 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                 uint32_t hinst;
                 uint32_t hit = trace(S, r, false, t, u, v, nullptr, &hinst);
                 F3 d = q.d[i], thr = q.thr[i];
-                float* a = acc + 3 * (size_t)(q.pix[i] - pix_begin);
                 if (hit == UINT32_MAX) {  // deferred_lighting_secondary.hlsl:23-29
                     F3 le = sky_eval(S, d);
                     float w = 1.0f;
@@ -801,7 +816,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                         w = pb2 + pl2 > 0.0f ? pb2 / (pb2 + pl2) : 1.0f;
                     }
                     F3 c = muls(mul(thr, le), w);
-                    if (maxc(c) > 0.0f) { a[0] += c.x; a[1] += c.y; a[2] += c.z; }
+                    if (maxc(c) > 0.0f) add_px(q.pix[i], c);
                     continue;
                 }
                 // shade
@@ -820,7 +835,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
                     cache_raw_inputs(S, P, neg(d), N, surf.rough, surf.base, (float)seg * 0.125f, raw);
                     cache_predict(st.cache_w, raw, y);
                     F3 c = mul(thr, f3(std::fmax(y[0], 0.0f), std::fmax(y[1], 0.0f), std::fmax(y[2], 0.0f)));
-                    a[0] += c.x; a[1] += c.y; a[2] += c.z;
+                    add_px(q.pix[i], c);
                     continue;
                 }
                 Frm fr = make_frame(N);
@@ -890,10 +905,7 @@ static void render_tile(const Scene& S, const Cam& K, const Settings& st, uint32
             for (size_t k = 0; k < sq.o.size(); ++k) {
                 Ray r = make_ray(sq.o[k], sq.tmin[k], sq.d[k], sq.tmax[k], sq.seed[k]);
                 float t, u, v;
-                if (trace(S, r, true, t, u, v, nullptr) == UINT32_MAX) {
-                    float* a = acc + 3 * (size_t)(sq.pix[k] - pix_begin);
-                    a[0] += sq.c[k].x; a[1] += sq.c[k].y; a[2] += sq.c[k].z;
-                }
+                if (trace(S, r, true, t, u, v, nullptr) == UINT32_MAX) add_px(sq.pix[k], sq.c[k]);
             }
             std::swap(q, nq);
         }
@@ -1270,7 +1282,9 @@ static int render_rows(void* sp, const float* camera, const Settings& st, uint32
     const uint32_t spp = st.spp, max_seg = st.max_seg;
     if (row_end > K.h || row_begin >= row_end || max_seg == 0 || max_seg > 16 || spp == 0) return -1;
     uint32_t p0 = row_begin * K.w, p1 = row_end * K.w;
-    std::vector<float> acc(3 * (size_t)(p1 - p0), 0.0f);
+    const bool fixed = (st.flags & F_FIXED) != 0;
+    std::vector<float> acc(fixed ? 0 : 3 * (size_t)(p1 - p0), 0.0f);
+    std::vector<uint64_t> fxs(fixed ? 3 * (size_t)(p1 - p0) : 0, 0);
     const uint32_t tile = 256;  // 16 x 16 pixels worth of paths per task
     uint32_t ntiles = (p1 - p0 + tile - 1) / tile;
     std::atomic<uint32_t> next{0};
@@ -1282,7 +1296,8 @@ static int render_rows(void* sp, const float* camera, const Settings& st, uint32
             uint32_t k = next.fetch_add(1);
             if (k >= ntiles) break;
             uint32_t b = p0 + k * tile, e = std::min(p1, b + tile);
-            render_tile(S, K, st, b, e, acc.data() + 3 * (size_t)(b - p0), ext[id].data(), sh[id].data());
+            render_tile(S, K, st, b, e, fixed ? nullptr : acc.data() + 3 * (size_t)(b - p0),
+                        fixed ? fxs.data() + 3 * (size_t)(b - p0) : nullptr, ext[id].data(), sh[id].data());
         }
     };
     std::vector<std::thread> ts;
@@ -1293,9 +1308,11 @@ static int render_rows(void* sp, const float* camera, const Settings& st, uint32
     if (seconds) *seconds = sec;
     float inv = 1.0f / (float)spp;
     for (size_t p = 0; p < (size_t)(p1 - p0); ++p) {
-        out[4 * p] = acc[3 * p] * inv;
-        out[4 * p + 1] = acc[3 * p + 1] * inv;
-        out[4 * p + 2] = acc[3 * p + 2] * inv;
+        for (int c = 0; c < 3; ++c) {
+            // F_FIXED: the sum to FP32 as the library folds it (double, then float), then the mean
+            const float sum = fixed ? (float)((double)fxs[3 * p + c] * 0x1p-32) : acc[3 * p + c];
+            out[4 * p + c] = sum * inv;
+        }
         out[4 * p + 3] = 1.0f;
     }
     if (stats) {

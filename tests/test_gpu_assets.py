@@ -3,6 +3,7 @@ the oracle renders it (same paths), and its primary outputs match bit for bit.""
 import numpy as np
 import pytest
 
+from conftest import assert_bits_equal
 from test_assets import write_project
 
 pytestmark = pytest.mark.gpu
@@ -26,6 +27,12 @@ def test_loaded_project_renders_like_the_oracle(bsm, ctx, oracle, tmp_path):
     o = ref[..., :3].astype(np.float64)
     assert (np.abs(g - o) / np.maximum(np.abs(o), 1e-3)).max() <= 1e-4
     assert o.max() > 0.0                     # the sun lights the quads
+    s.flags |= bsm.BSM_PT_DETERMINISTIC      # fixed-point sums on both sides: equal bit for bit
+    dimg, _ = ctx.render(sid, [cam], s)
+    dref, _, _ = osc.render(cam.as_array(), spp=4, max_segments=4, seed=int(s.seed), ray_length=s.ray_length,
+                            flags=bsm.BSM_PT_DETERMINISTIC)
+    assert_bits_equal(dimg[0], dref)
+    s.flags &= ~bsm.BSM_PT_DETERMINISTIC
     d, gb, h = ctx.render_primary(sid, cam, s, info.near_z, info.far_z)
     do, go, ho = osc.primary(cam.as_array(), ray_length=s.ray_length, near_z=info.near_z, far_z=info.far_z)
     assert np.array_equal(d.view(np.uint32), do.view(np.uint32))

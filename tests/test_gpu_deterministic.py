@@ -5,8 +5,10 @@ bits of an image depend on the order in which the GPU adds them.  With the
 flag, a call sums its contributions per pixel as 32.32 fixed-point integers
 (exact, so independent of the order) and adds them to the view's history
 once.  The images must then be identical bit for bit across repeats, launch
-paths (graph or direct), wavefront chunking and batching, and still match the
-oracle within the parity tolerance."""
+paths (graph or direct), wavefront chunking and batching, and equal the
+oracle's images bit for bit when the oracle sums the same way (its F_FIXED
+mode): every path's contributions agree exactly, only the float summation
+order ever differed."""
 import numpy as np
 import pytest
 
@@ -23,6 +25,12 @@ def rel_err(g, c):
 
 def bits(img):
     return np.ascontiguousarray(img).view(np.uint32)
+
+
+@pytest.fixture(scope="module")
+def room(bsm, ctx, oracle):
+    sc = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=1, width=64, height=64)
+    return sc, ctx.load_scene(sc), oracle.OracleScene(sc)
 
 
 @pytest.fixture(scope="module")
@@ -51,6 +59,24 @@ def test_deterministic_render_matches_oracle(bsm, terrain, ctx):
     assert rel_err(imgs[0], ref).max() <= RTOL
     plain, _ = ctx.render(sid, [sc.camera], bsm.settings(spp=4, max_segments=8, seed=4))
     assert rel_err(imgs[0], plain[0]).max() <= 1e-5
+
+
+@pytest.mark.parametrize("which, flags, spp, segs", [("room", 0, 4, 4), ("room", 1, 4, 4), ("room", 2, 4, 4),
+                                                     ("room", 4, 4, 4), ("terrain", 0, 4, 8), ("terrain", 1, 8, 6)])
+def test_images_equal_the_oracle_bit_for_bit(bsm, room, terrain, ctx, which, flags, spp, segs):
+    """The oracle's F_FIXED mode sums the same contributions as the same fixed-point integers and converts them
+    as the library does, so where every contribution agrees bit for bit the images do too."""
+    sc, sid, osc = room if which == "room" else terrain
+    imgs, st = ctx.render(sid, [sc.camera], bsm.settings(spp=spp, max_segments=segs, seed=3,
+                                                         flags=flags | bsm.BSM_PT_DETERMINISTIC))
+    ref, ost, _ = osc.render(sc.camera.as_array(), spp=spp, max_segments=segs, seed=3,
+                             flags=flags | bsm.BSM_PT_DETERMINISTIC)
+    assert list(st.rays_per_segment[:segs]) == [int(x) for x in ost[:segs]]
+    g, o = bits(imgs[0]), bits(ref)
+    bad = np.argwhere(g != o)
+    assert bad.size == 0, (f"{len(bad)} values differ, first {bad[:4].tolist()}: gpu "
+                           f"{imgs[0][tuple(bad[0])]!r} oracle {ref[tuple(bad[0])]!r}, largest ulp distance "
+                           f"{int(np.abs(g.astype(np.int64) - o.astype(np.int64)).max())}")
 
 
 def test_same_bits_with_chunks_and_without_graphs(bsm, terrain, ctx):

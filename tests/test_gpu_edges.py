@@ -11,6 +11,7 @@
 import numpy as np
 import pytest
 
+from conftest import assert_bits_equal
 from edge_scenes import MISS, coincident_scene, edge_rays, grid_scene, invalid_rays, rays_along_z
 
 pytestmark = pytest.mark.gpu
@@ -54,6 +55,10 @@ def test_tiny_and_odd_images(bsm, ctx, oracle, w, h):
     assert list(st.rays_per_segment[:4]) == [int(x) for x in ost[:4]]
     gi, ci = imgs[0][..., :3].astype(np.float64), ref[..., :3].astype(np.float64)
     assert (np.abs(gi - ci) / np.maximum(np.abs(ci), 1e-3)).max() <= 1e-4
+    det = bsm.BSM_PT_DETERMINISTIC   # fixed-point sums on both sides: equal bit for bit
+    dimg, _ = ctx.render(sid, [sc.camera], bsm.settings(spp=3, max_segments=4, seed=2, flags=det))
+    dref, _, _ = oracle.OracleScene(sc).render(sc.camera.as_array(), spp=3, max_segments=4, seed=2, flags=det)
+    assert_bits_equal(dimg[0], dref)
     ctx.release(sid)
 
 

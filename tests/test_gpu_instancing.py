@@ -13,6 +13,8 @@ import ctypes as C
 import numpy as np
 import pytest
 
+from conftest import assert_bits_equal
+
 from test_instancing_oracle import random_world_rays
 
 pytestmark = pytest.mark.gpu
@@ -53,6 +55,10 @@ def test_render_and_primary_equal_oracle(bsm, ctx, inst_scene):
         assert [int(x) for x in st.rays_per_segment[:4]] == [int(x) for x in ost[:4]]
         assert int(st.shadow_rays) == int(ost[16:32].sum())
         assert rel_err(imgs[0], ref).max() <= 1e-4
+        det = flags | bsm.BSM_PT_DETERMINISTIC   # fixed-point sums on both sides: equal bit for bit
+        imgs, _ = ctx.render(sid, [sc.camera], bsm.settings(spp=2, max_segments=4, seed=9, flags=det))
+        ref, _, _ = osc.render(sc.camera.as_array(), spp=2, max_segments=4, seed=9, flags=det)
+        assert_bits_equal(imgs[0], ref)
     d, g, h = ctx.render_primary(sid, sc.camera)
     do, go, ho = osc.primary(sc.camera.as_array())
     assert np.array_equal(h.view(np.uint32), ho.view(np.uint32))
@@ -101,6 +107,10 @@ def test_non_opaque_materials_in_two_level_scene(bsm, ctx, oracle):
         ref, ost, _ = osc.render(sc.camera.as_array(), spp=2, max_segments=4, seed=1)
         assert [int(x) for x in st.rays_per_segment[:4]] == [int(x) for x in ost[:4]]
         assert rel_err(imgs[0], ref).max() <= 1e-4
+        det = bsm.BSM_PT_DETERMINISTIC
+        imgs, _ = ctx.render(sid, [sc.camera], bsm.settings(spp=2, max_segments=4, seed=1, flags=det))
+        ref, _, _ = osc.render(sc.camera.as_array(), spp=2, max_segments=4, seed=1, flags=det)
+        assert_bits_equal(imgs[0], ref)
     finally:
         ctx.release(sid)
 

@@ -4,6 +4,8 @@ with up to eight lights of all kinds, in one- and two-level scenes."""
 import numpy as np
 import pytest
 
+from conftest import assert_bits_equal
+
 pytestmark = pytest.mark.gpu
 
 
@@ -55,6 +57,11 @@ def test_lights_equal_oracle(bsm, ctx, oracle, n_dir, n_point, n_rect, cube):
             assert [int(x) for x in st.rays_per_segment[:4]] == [int(x) for x in ost[:4]]
             assert int(st.shadow_rays) == int(ost[16:32].sum())
             assert rel_err(imgs[0], ref).max() <= 1e-4
+        # fixed-point sums on both sides: equal bit for bit
+        det = flags | bsm.BSM_PT_DETERMINISTIC
+        imgs, _ = ctx.render(sid, [sc.camera], bsm.settings(spp=2, max_segments=4, seed=5, flags=det))
+        ref, _, _ = osc.render(sc.camera.as_array(), spp=2, max_segments=4, seed=5, flags=det)
+        assert_bits_equal(imgs[0], ref)
     finally:
         ctx.release(sid)
 
@@ -73,6 +80,10 @@ def test_lights_in_two_level_scene(bsm, ctx, oracle):
         ref, ost, _ = oracle.OracleScene(sc).render(sc.camera.as_array(), spp=2, max_segments=3, seed=3)
         assert [int(x) for x in st.rays_per_segment[:3]] == [int(x) for x in ost[:3]]
         assert rel_err(imgs[0], ref).max() <= 1e-4
+        det = bsm.BSM_PT_DETERMINISTIC
+        imgs, _ = ctx.render(sid, [sc.camera], bsm.settings(spp=2, max_segments=3, seed=3, flags=det))
+        ref, _, _ = oracle.OracleScene(sc).render(sc.camera.as_array(), spp=2, max_segments=3, seed=3, flags=det)
+        assert_bits_equal(imgs[0], ref)
     finally:
         ctx.release(sid)
 

@@ -11,6 +11,8 @@ bisemutum/shaders/core/raytracing/hit.hlsl:55-71, 158), on the GPU against the o
 import numpy as np
 import pytest
 
+from conftest import assert_bits_equal
+
 pytestmark = pytest.mark.gpu
 
 
@@ -76,6 +78,10 @@ def test_smooth_spheres_match_oracle(bsm, ctx, oracle):
         ref, ost, _ = osc.render(sc.camera.as_array(), spp=4, max_segments=6, seed=5)
         assert [int(x) for x in st.rays_per_segment[:6]] == [int(x) for x in ost[:6]]
         assert rel_err(imgs[0], ref).max() <= 1e-4
+        det = bsm.BSM_PT_DETERMINISTIC
+        dimg, _ = ctx.render(sid, [sc.camera], bsm.settings(spp=4, max_segments=6, seed=5, flags=det))
+        dref, _, _ = osc.render(sc.camera.as_array(), spp=4, max_segments=6, seed=5, flags=det)
+        assert_bits_equal(dimg[0], dref)
         flat_img, _ = ctx.render(fid, [sc.camera], s)
         assert rel_err(imgs[0], flat_img[0]).max() > 0.05, "vertex normals did not change the shading"
         # primary G-buffer: packed shading normal bit-exact with the oracle
@@ -118,6 +124,12 @@ def test_loaded_project_with_normals_matches_oracle(bsm, ctx, oracle, tmp_path):
         assert [int(x) for x in st.rays_per_segment[:4]] == [int(x) for x in ost[:4]]
         assert rel_err(imgs[0], ref).max() <= 1e-4
         assert ref[..., :3].max() > 0.0
+        det = bsm.BSM_PT_DETERMINISTIC
+        dimg, _ = ctx.render(sid, [cam], bsm.settings(spp=8, max_segments=4, seed=2, ray_length=info.settings.ray_length,
+                                                      flags=det))
+        dref, _, _ = oracle.OracleScene(scene).render(cam.as_array(), spp=8, max_segments=4, seed=2,
+                                                      ray_length=info.settings.ray_length, flags=det)
+        assert_bits_equal(dimg[0], dref)
         flat_img, _ = ctx.render(fid, [cam], s)
         assert not np.allclose(imgs[0], flat_img[0]), "the project's normals did not reach the shading"
     finally:

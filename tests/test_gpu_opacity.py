@@ -10,6 +10,8 @@
 import numpy as np
 import pytest
 
+from conftest import assert_bits_equal
+
 pytestmark = pytest.mark.gpu
 
 
@@ -83,6 +85,10 @@ def test_render_with_non_opaque_materials_equals_oracle(bsm, ctx, oracle):
         g = imgs[0][..., :3].astype(np.float64)
         o = ref[..., :3].astype(np.float64)
         assert (np.abs(g - o) / np.maximum(np.abs(o), 1e-3)).max() <= 1e-4
+        det = flags | bsm.BSM_PT_DETERMINISTIC   # fixed-point sums on both sides: equal bit for bit
+        imgs, _ = ctx.render(sid, [sc.camera], bsm.settings(spp=3, max_segments=5, seed=4, flags=det))
+        ref, _, _ = osc.render(sc.camera.as_array(), spp=3, max_segments=5, seed=4, flags=det)
+        assert_bits_equal(imgs[0], ref)
     d, gb, hp = ctx.render_primary(sid, sc.camera, bsm.settings(seed=4))
     do, go, ho = osc.primary(sc.camera.as_array(), seed=4)
     assert np.array_equal(hp.view(np.uint32), ho.view(np.uint32))

@@ -16,6 +16,9 @@
     compared with the oracle's render of the same rows at 64 spp;
   - the whole frame at 2 spp against the oracle's whole frame: every pixel
     within 1e-4, per-segment extend counts and the shadow count equal.
+* The image tests run twice: with FP32 atomic sums (1e-4), and with
+  BSM_PT_DETERMINISTIC against the oracle's fixed-point sums, where every
+  pixel must be equal bit for bit.
 
 Each oracle leg stays within seconds on the host cores.  The module uses its own
 context and closes it, so the 41 GB frame-sized wavefront is freed afterwards."""
@@ -33,6 +36,21 @@ def rel_err(g, c):
     g = g[..., :3].astype(np.float64)
     c = c[..., :3].astype(np.float64)
     return np.abs(g - c) / np.maximum(np.abs(c), 1e-3)
+
+
+def assert_same_image(g, c, det, what=""):
+    """det: equal bit for bit (fixed-point sums on both sides); else within RTOL."""
+    if det:
+        gb, cb = np.ascontiguousarray(g).view(np.uint32), np.ascontiguousarray(c).view(np.uint32)
+        bad = np.argwhere(gb != cb)
+        assert bad.size == 0, f"{what}{len(bad)} values differ, first {bad[:4].tolist()}"
+    else:
+        err = rel_err(g, c)
+        assert err.max() <= RTOL, f"{what}max rel err {err.max():.3g} at {np.unravel_index(err.argmax(), err.shape)}"
+
+
+def flags_of(bsm, det):
+    return bsm.BSM_PT_DETERMINISTIC if det else 0
 
 
 def assert_same_hits(g, c):
@@ -72,19 +90,20 @@ def big(bsm):
     ctx.close()
 
 
-def test_config0_exact(bsm, big, oracle):
+@pytest.mark.parametrize("det", [False, True])
+def test_config0_exact(bsm, big, oracle, det):
     """Config 0 as benchmarked: room of 20,504 triangles, 256x256, 16 spp, 4 segments, seed 1."""
     sc = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=1, width=256, height=256)
     assert sc.num_triangles == 20504
     sid = big.load_scene(sc)
     osc = oracle.OracleScene(sc)
-    imgs, st = big.render(sid, [sc.camera], bsm.settings(spp=16, max_segments=4, seed=1))
-    ref, ost, _ = osc.render(sc.camera.as_array(), spp=16, max_segments=4, seed=1)
+    f = flags_of(bsm, det)
+    imgs, st = big.render(sid, [sc.camera], bsm.settings(spp=16, max_segments=4, seed=1, flags=f))
+    ref, ost, _ = osc.render(sc.camera.as_array(), spp=16, max_segments=4, seed=1, flags=f)
     assert st.paths == 256 * 256 * 16
     assert [int(x) for x in st.rays_per_segment[:4]] == [int(x) for x in ost[:4]]
     assert st.shadow_rays == int(ost[16:].sum())
-    err = rel_err(imgs[0], ref)
-    assert err.max() <= RTOL, f"max rel err {err.max():.3g} at {np.unravel_index(err.argmax(), err.shape)}"
+    assert_same_image(imgs[0], ref, det)
     big.release(sid)
 
 
@@ -127,27 +146,29 @@ def test_config1_camera_rays_bit_exact(terrain, big):
     assert (c[:, 1] != 0xFFFFFFFF).mean() > 0.3
 
 
-def test_config1_frame_64spp_one_chunk_bands(bsm, terrain, big):
+@pytest.mark.parametrize("det", [False, True])
+def test_config1_frame_64spp_one_chunk_bands(bsm, terrain, big, det):
     """The benchmarked frame: 1920x1080, 64 spp, 8 segments, one chunk of 132.7 M paths."""
     sc, sid, osc, _ = terrain
-    s = bsm.settings(spp=64, max_segments=8, seed=1, wavefront_capacity=0)
+    f = flags_of(bsm, det)
+    s = bsm.settings(spp=64, max_segments=8, seed=1, wavefront_capacity=0, flags=f)
     imgs, st = big.render(sid, [sc.camera], s)
     assert st.paths == 1920 * 1080 * 64
     assert st.chunks == 1, "the frame must run as one frame-sized chunk"
     img = imgs[0]
     assert np.isfinite(img).all()
     for r0, r1 in [(0, 6), (537, 549), (1074, 1080)]:
-        ref, ost, _ = osc.render(sc.camera.as_array(), spp=64, max_segments=8, seed=1, rows=(r0, r1))
-        err = rel_err(img[r0:r1], ref)
-        assert err.max() <= RTOL, f"rows {r0}-{r1}: max rel err {err.max():.3g}"
+        ref, ost, _ = osc.render(sc.camera.as_array(), spp=64, max_segments=8, seed=1, rows=(r0, r1), flags=f)
+        assert_same_image(img[r0:r1], ref, det, f"rows {r0}-{r1}: ")
 
 
-def test_config1_frame_2spp_whole(bsm, terrain, big):
+@pytest.mark.parametrize("det", [False, True])
+def test_config1_frame_2spp_whole(bsm, terrain, big, det):
     sc, sid, osc, _ = terrain
-    imgs, st = big.render(sid, [sc.camera], bsm.settings(spp=2, max_segments=8, seed=3))
-    ref, ost, _ = osc.render(sc.camera.as_array(), spp=2, max_segments=8, seed=3)
+    f = flags_of(bsm, det)
+    imgs, st = big.render(sid, [sc.camera], bsm.settings(spp=2, max_segments=8, seed=3, flags=f))
+    ref, ost, _ = osc.render(sc.camera.as_array(), spp=2, max_segments=8, seed=3, flags=f)
     assert [int(x) for x in st.rays_per_segment[:8]] == [int(x) for x in ost[:8]]
     assert st.shadow_rays == int(ost[16:].sum())
-    err = rel_err(imgs[0], ref)
-    assert err.max() <= RTOL, f"max rel err {err.max():.3g} at {np.unravel_index(err.argmax(), err.shape)}"
+    assert_same_image(imgs[0], ref, det)
     assert imgs[0][..., :3].mean() > 0.01

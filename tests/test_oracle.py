@@ -167,6 +167,24 @@ def test_oracle_render_is_deterministic_and_finite(bsm, oracle):
     assert sa[0] == 32 * 32 * 2
 
 
+def test_oracle_fixed_point_sums(bsm, oracle):
+    """F_FIXED (64, the library's BSM_PT_DETERMINISTIC): exact 32.32 fixed-point pixel sums; the image equals
+    the FP32-sum image within the quantisation and does not depend on threads or on a split into row bands."""
+    sc = small_scene(bsm, spheres=10)
+    osc = oracle.OracleScene(sc)
+    cam = sc.camera.as_array()
+    f, sf, _ = osc.render(cam, spp=3, max_segments=4, seed=9, flags=64, threads=3)
+    g, _, _ = osc.render(cam, spp=3, max_segments=4, seed=9, flags=64, threads=1)
+    top, _, _ = osc.render(cam, spp=3, max_segments=4, seed=9, flags=64, rows=(0, 13))
+    bottom, _, _ = osc.render(cam, spp=3, max_segments=4, seed=9, flags=64, rows=(13, 32))
+    a, sa, _ = osc.render(cam, spp=3, max_segments=4, seed=9)
+    assert np.array_equal(f.view(np.uint32), g.view(np.uint32))
+    assert np.array_equal(f.view(np.uint32), np.concatenate([top, bottom]).view(np.uint32))
+    assert np.array_equal(sf, sa)
+    err = np.abs(f[..., :3].astype(np.float64) - a[..., :3]) / np.maximum(np.abs(a[..., :3]), 1e-3)
+    assert err.max() <= 1e-6 and f[..., :3].mean() > 0.0
+
+
 @pytest.mark.parametrize("flags", [0, 1, 2, 4, 6])
 def test_oracle_render_flags(bsm, oracle, flags):
     sc = small_scene(bsm, spheres=4, seed=2)
