@@ -34,6 +34,7 @@ BSM_SCENE_ROOM, BSM_SCENE_TERRAIN = 0, 1
 BSM_PT_JITTER, BSM_PT_NO_SUN_NEE, BSM_PT_NO_SKY_NEE, BSM_PT_STAGE_TIMING, BSM_PT_NO_GRAPH = 1, 2, 4, 8, 16
 BSM_PT_COUNT_TRAVERSAL = 32
 BSM_PT_DETERMINISTIC = 64
+BSM_SERVER_DETERMINISTIC = 1
 MISS = 0xFFFFFFFF
 
 
@@ -146,7 +147,7 @@ class TuneResult(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("pool_bytes", C.c_uint64), ("chunk_paths", C.c_uint32), ("lanes", C.c_uint32),
-                ("max_views_per_chunk", C.c_uint32), ("reserved", C.c_uint32)]
+                ("max_views_per_chunk", C.c_uint32), ("flags", C.c_uint32)]
 
 
 class Request(C.Structure):
@@ -949,10 +950,11 @@ class Context:
         self.check(self._L.bsm_set_tuning(self.h, scene_id, C.byref(params) if params is not None else None))
 
     # serving loop
-    def server_start(self, pool_bytes=0, chunk_paths=0, lanes=0, max_views_per_chunk=0):
+    def server_start(self, pool_bytes=0, chunk_paths=0, lanes=0, max_views_per_chunk=0, deterministic=False):
         self._reqs = {}
+        flags = BSM_SERVER_DETERMINISTIC if deterministic else 0
         self.check(self._L.bsm_server_start(self.h, C.byref(ServerOpts(pool_bytes, chunk_paths, lanes,
-                                                                       max_views_per_chunk, 0))))
+                                                                       max_views_per_chunk, flags))))
 
     def submit(self, scene_id: int, cam: Camera, spp: int, max_segments: int = 8, seed: int = 1):
         """Queues a request; returns (id, output array filled when the request is done)."""

@@ -157,6 +157,10 @@ void launch_resolve(cudaStream_t st, const float4* accum, uint32_t width, uint32
                     float4* out, uint32_t pitch_px);
 // accum[p] += fx[3p .. 3p + 2] * 2^-32 for the n accumulator pixels (one add per pixel: deterministic)
 void launch_fold_fixed(cudaStream_t st, const unsigned long long* fx, float4* accum, uint32_t n);
+// launch_resolve from fixed-point sums: out = (fx * 2^-32 as float) * inv_spp, alpha 1 (the same values as a
+// fold into a cleared accumulator followed by launch_resolve)
+void launch_resolve_fixed(cudaStream_t st, const unsigned long long* fx, uint32_t width, uint32_t height,
+                          float inv_spp, float4* out, uint32_t pitch_px);
 void launch_trace_closest(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint4* hits,
                           int block);
 void launch_trace_any(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint8_t* occluded,

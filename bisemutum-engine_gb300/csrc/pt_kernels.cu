@@ -474,6 +474,16 @@ __global__ void k_fold_fixed(const unsigned long long* __restrict__ fx, float4* 
     accum[i] = a;
 }
 
+__global__ void k_resolve_fixed(const unsigned long long* __restrict__ fx, uint32_t width, uint32_t height,
+                                float inv_spp, float4* __restrict__ out, uint32_t pitch) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= width || y >= height) return;
+    const unsigned long long* p = fx + 3 * ((size_t)y * width + x);
+    out[(size_t)y * pitch + x] = make_float4((float)((double)p[0] * 0x1p-32) * inv_spp,
+                                             (float)((double)p[1] * 0x1p-32) * inv_spp,
+                                             (float)((double)p[2] * 0x1p-32) * inv_spp, 1.0f);
+}
+
 __global__ void k_resolve(const float4* __restrict__ accum, uint32_t width, uint32_t height, float inv_spp,
                           float4* __restrict__ out, uint32_t pitch) {
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -691,6 +701,11 @@ void launch_resolve(cudaStream_t st, const float4* accum, uint32_t width, uint32
                     float4* out, uint32_t pitch_px) {
     dim3 grid((width + 255) / 256, height);
     k_resolve<<<grid, 256, 0, st>>>(accum, width, height, inv_spp, out, pitch_px);
+}
+void launch_resolve_fixed(cudaStream_t st, const unsigned long long* fx, uint32_t width, uint32_t height,
+                          float inv_spp, float4* out, uint32_t pitch_px) {
+    dim3 grid((width + 255) / 256, height);
+    k_resolve_fixed<<<grid, 256, 0, st>>>(fx, width, height, inv_spp, out, pitch_px);
 }
 void launch_fold_fixed(cudaStream_t st, const unsigned long long* fx, float4* accum, uint32_t n) {
     if (n == 0) return;

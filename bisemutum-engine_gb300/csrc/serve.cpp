@@ -5,8 +5,9 @@
 // window tick (graphics_manager.cpp:407-427).  Here a worker thread owns the
 // device work of a context:
 //   * requests (scene, camera, spp, segments, seed, host output) queue FIFO;
-//   * a request is admitted when its accumulator (width x height float4) fits
-//     in the accumulator pool (first-fit), so admission follows free memory;
+//   * a request is admitted when its accumulator (width x height float4, or
+//     three 64-bit fixed-point sums per pixel with BSM_SERVER_DETERMINISTIC)
+//     fits in the accumulator pool (first-fit), so admission follows free memory;
 //   * every lane (a CUDA stream with its own wavefront queues) that is idle
 //     takes the next chunk: path ranges of one scene's active requests, up to
 //     the chunk capacity, described by one view record per range — requests
@@ -19,7 +20,8 @@
 //     returns to the pool.
 // A request's random numbers depend only on its seed, pixel and sample, never
 // on the chunk or slot it ran in, so its image is the same alone and in a mix
-// (up to the order of the per-pixel float sums).
+// (up to the order of the per-pixel float sums; bit for bit with exact
+// fixed-point sums, BSM_SERVER_DETERMINISTIC).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -119,7 +121,9 @@ struct Server {
     uint32_t lights = 1;
     cudaStream_t admin = nullptr;      // clears admitted requests' accumulators
     std::vector<Lane> lanes;
-    float4* pool_mem = nullptr;
+    float4* pool_mem = nullptr;              // FP32 sums (one float4 per pixel)
+    unsigned long long* pool_fx = nullptr;   // BSM_SERVER_DETERMINISTIC: fixed-point sums (3 words per pixel)
+    bool det = false;
     Pool pool;
     std::mutex mu;
     std::condition_variable cv;
@@ -145,7 +149,8 @@ bool admit_locked(Server& S) {
         if (!S.pool.alloc(r->accum_len, &off)) break;  // FIFO: wait for memory to free up
         S.queued.pop_front();
         r->accum_off = off;
-        cudaMemsetAsync(S.pool_mem + off, 0, r->accum_len * 16, S.admin);
+        if (S.det) cudaMemsetAsync(S.pool_fx + 3 * off, 0, r->accum_len * 24, S.admin);
+        else cudaMemsetAsync(S.pool_mem + off, 0, r->accum_len * 16, S.admin);
         cudaEventCreateWithFlags(&r->zero_ev, cudaEventDisableTiming);
         cudaEventRecord(r->zero_ev, S.admin);
         r->state = BSM_REQ_RUNNING;
@@ -249,8 +254,12 @@ bool launch_chunk(Server& S, Lane& lane, uint32_t scene) {
 void finish_request(Server& S, Lane& lane, Request* r) {
     const bsm_camera& c = r->r.camera;
     size_t px = (size_t)c.width * c.height;
-    launch_resolve(lane.stream, S.pool_mem + r->accum_off, c.width, c.height, 1.0f / (float)r->r.spp, lane.stage,
-                   c.width);
+    if (S.det)
+        launch_resolve_fixed(lane.stream, S.pool_fx + 3 * r->accum_off, c.width, c.height, 1.0f / (float)r->r.spp,
+                             lane.stage, c.width);
+    else
+        launch_resolve(lane.stream, S.pool_mem + r->accum_off, c.width, c.height, 1.0f / (float)r->r.spp,
+                       lane.stage, c.width);
     cudaMemcpyAsync(r->r.out_rgba, lane.stage, px * 16, cudaMemcpyDeviceToHost, lane.stream);
     cudaEventCreateWithFlags(&r->fin_ev, cudaEventDisableTiming);
     cudaEventRecord(r->fin_ev, lane.stream);
@@ -331,7 +340,7 @@ void worker_main(Server* Sp) {
             }
             S.stats.active = (uint32_t)S.active.size();
             S.stats.queued = (uint32_t)S.queued.size();
-            S.stats.pool_used_bytes = S.pool.used * 16;
+            S.stats.pool_used_bytes = S.pool.used * (S.det ? 24 : 16);
         }
         S.cv.notify_all();
         if (!did) std::this_thread::sleep_for(std::chrono::microseconds(50));
@@ -357,10 +366,12 @@ extern "C" bsm_status bsm_server_start(bsm_context* ctx, const bsm_server_opts* 
     if (!S->opts.chunk_paths) S->opts.chunk_paths = 1u << 21;
     if (!S->opts.lanes) S->opts.lanes = 4;
     if (!S->opts.max_views_per_chunk) S->opts.max_views_per_chunk = 256;
-    if (S->opts.lanes > 16 || S->opts.chunk_paths < 1024 || S->opts.max_views_per_chunk > 4096) {
-        ctx_set_error(ctx, "server options out of range (lanes <= 16, chunk_paths >= 1024, views <= 4096)");
+    if (S->opts.lanes > 16 || S->opts.chunk_paths < 1024 || S->opts.max_views_per_chunk > 4096 ||
+        (S->opts.flags & ~(uint32_t)BSM_SERVER_DETERMINISTIC)) {
+        ctx_set_error(ctx, "server options out of range (lanes <= 16, chunk_paths >= 1024, views <= 4096, flags)");
         return BSM_ERR_INVALID_ARG;
     }
+    S->det = (S->opts.flags & BSM_SERVER_DETERMINISTIC) != 0;
     S->lc.regcap = 1;
     query_launch_cfg(S->device, 128, &S->lc);
     S->lights = std::max(ctx_max_lights(ctx), (uint32_t)kMaxLights);
@@ -374,6 +385,7 @@ extern "C" bsm_status bsm_server_start(bsm_context* ctx, const bsm_server_opts* 
             if (l.ev) cudaEventDestroy(l.ev);
         }
         if (S->pool_mem) cudaFree(S->pool_mem);
+        if (S->pool_fx) cudaFree(S->pool_fx);
         if (S->stats_host) cudaFreeHost(S->stats_host);
         ctx_set_error(ctx, m);
         return BSM_ERR_OUT_OF_MEMORY;
@@ -410,10 +422,16 @@ extern "C" bsm_status bsm_server_start(bsm_context* ctx, const bsm_server_opts* 
     }
     if (cudaHostAlloc((void**)&S->stats_host, S->lanes.size() * kStatWords * 8, 0) != cudaSuccess)
         return fail_cleanup("server: pinned stats");
-    uint64_t pool_n = S->opts.pool_bytes / 16;
-    if (cudaMalloc((void**)&S->pool_mem, pool_n * 16) != cudaSuccess) return fail_cleanup("server: accumulator pool");
+    const uint64_t px_bytes = S->det ? 24 : 16;
+    uint64_t pool_n = S->opts.pool_bytes / px_bytes;
+    if (S->det) {
+        if (cudaMalloc((void**)&S->pool_fx, pool_n * 24) != cudaSuccess) return fail_cleanup("server: accumulator pool");
+        for (Lane& l : S->lanes) l.wf.accum_fx = S->pool_fx;   // contributions go to the fixed-point sums
+    } else if (cudaMalloc((void**)&S->pool_mem, pool_n * 16) != cudaSuccess) {
+        return fail_cleanup("server: accumulator pool");
+    }
     S->pool.init(pool_n);
-    S->stats.pool_bytes = pool_n * 16;
+    S->stats.pool_bytes = pool_n * px_bytes;
     cudaStreamCreateWithFlags(&S->admin, cudaStreamNonBlocking);
     S->t0 = Clock::now();
     Server* raw = S.release();
@@ -564,7 +582,8 @@ extern "C" bsm_status bsm_server_stop(bsm_context* ctx) {
         if (kv.second->fin_ev) cudaEventDestroy(kv.second->fin_ev);
         if (kv.second->zero_ev) cudaEventDestroy(kv.second->zero_ev);
     }
-    cudaFree(S->pool_mem);
+    if (S->pool_mem) cudaFree(S->pool_mem);
+    if (S->pool_fx) cudaFree(S->pool_fx);
     cudaFreeHost(S->stats_host);
     ctx_server_slot(ctx) = nullptr;
     delete S;

@@ -467,12 +467,20 @@ BSM_API bsm_status bsm_render_noalloc(bsm_context* ctx, uint32_t scene_id, const
 /* ---- serving: resident scenes, requests admitted by memory, continuous batching ---- */
 
 typedef struct bsm_server_opts {
-    uint64_t pool_bytes;          /* accumulator pool: admission budget (16 B per pixel); 0 = 1 GiB */
+    uint64_t pool_bytes;          /* accumulator pool: admission budget (16 B per pixel, 24 with
+                                     BSM_SERVER_DETERMINISTIC); 0 = 1 GiB */
     uint32_t chunk_paths;         /* paths per in-flight chunk (queue capacity of a lane); 0 = 2^21 */
     uint32_t lanes;               /* chunks in flight at once, one CUDA stream each; 0 = 4 */
     uint32_t max_views_per_chunk; /* request ranges one chunk can hold; 0 = 256 */
-    uint32_t reserved;
+    uint32_t flags;               /* BSM_SERVER_* (0: FP32 atomic sums) */
 } bsm_server_opts;
+
+enum {
+    /* every request sums its contributions as exact 32.32 fixed-point integers (24 B per pixel of the pool
+       instead of 16), as BSM_PT_DETERMINISTIC does for bsm_render: a result is then the same bit for bit
+       alone, in any mix of requests, and as bsm_render with that flag renders it */
+    BSM_SERVER_DETERMINISTIC = 1u << 0
+};
 
 typedef struct bsm_request {
     uint32_t scene_id;

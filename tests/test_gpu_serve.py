@@ -1,7 +1,8 @@
 """Serving loop (GPU): resident scenes, admission by memory, continuous
 batching.  A request's image is the same rendered alone and in a mix of
 requests on several scenes, and equals bsm_render of the same view (within
-the 1e-4 relative radiance tolerance)."""
+the 1e-4 relative radiance tolerance; bit for bit when the server and the
+render both sum in fixed point)."""
 import numpy as np
 import pytest
 
@@ -63,6 +64,29 @@ def test_same_alone_and_in_the_mix(bsm, served):
     for (sid_i, cam_i, spp_i, segs_i, seed_i), (_, img) in list(zip(mix, outs))[:8]:
         r, _ = ctx.render(sid_i, [cam_i], bsm.settings(spp=spp_i, max_segments=segs_i, seed=seed_i))
         assert rel_err(img, r[0]).max() <= RTOL
+
+
+def test_same_bits_alone_in_the_mix_and_as_rendered(bsm, served):
+    """BSM_SERVER_DETERMINISTIC: exact fixed-point sums make a request's image independent of the chunks and the
+    company it ran in, bit for bit, and equal to bsm_render's with BSM_PT_DETERMINISTIC."""
+    ctx, scenes, ids = served
+    mix = request_mix(bsm, scenes, ids, 24, seed=3)
+    sid, cam, spp, segs, seed = mix[7]
+    ctx.server_start(pool_bytes=96 << 20, chunk_paths=1 << 16, lanes=3, deterministic=True)
+    try:
+        rid, alone = ctx.submit(sid, cam, spp, segs, seed)
+        assert ctx.wait(rid, timeout_ms=60000).state == bsm.BSM_REQ_DONE
+        outs = [ctx.submit(*r) for r in mix]
+        for rid_i, _ in outs:
+            assert ctx.wait(rid_i, timeout_ms=60000).state == bsm.BSM_REQ_DONE
+    finally:
+        ctx.server_stop()
+    assert alone[..., :3].max() > 0.0
+    assert np.array_equal(outs[7][1].view(np.uint32), alone.view(np.uint32))
+    det = bsm.BSM_PT_DETERMINISTIC
+    for (sid_i, cam_i, spp_i, segs_i, seed_i), (_, img) in list(zip(mix, outs))[:8]:
+        r, _ = ctx.render(sid_i, [cam_i], bsm.settings(spp=spp_i, max_segments=segs_i, seed=seed_i, flags=det))
+        assert np.array_equal(img.view(np.uint32), r[0].view(np.uint32))
 
 
 def test_admission_waits_for_memory(bsm, served):
