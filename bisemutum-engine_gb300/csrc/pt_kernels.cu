@@ -709,7 +709,7 @@ void launch_resolve_fixed(cudaStream_t st, const unsigned long long* fx, uint32_
 }
 void launch_fold_fixed(cudaStream_t st, const unsigned long long* fx, float4* accum, uint32_t n) {
     if (n == 0) return;
-    k_fold_fixed<<<(n + 255) / 256, 256, 0, st>>>(fx, accum, n);
+    k_fold_fixed<<<(unsigned)(((uint64_t)n + 255) / 256), 256, 0, st>>>(fx, accum, n);
 }
 void launch_trace_closest(cudaStream_t st, const DevScene& sc, const float4* rays, uint32_t n, uint4* hits,
                           int block) {

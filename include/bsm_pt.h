@@ -256,8 +256,9 @@ enum {
     BSM_PT_COUNT_TRAVERSAL = 1u << 5, /* count BVH nodes visited / triangles tested by the extend stage */
     BSM_PT_DETERMINISTIC = 1u << 6  /* bit-reproducible images: the call's contributions are summed per pixel
                                        as 32.32 fixed-point integers (exact, so the order of the additions does
-                                       not matter) and added to the view's history once; contributions are
-                                       non-negative and below 2^31 each.  Default: FP32 atomics, whose last bits
+                                       not matter) and added to the view's history once; negative
+                                       contributions count as 0, and a pixel's sum over one call must stay
+                                       below 2^32 per channel.  Default: FP32 atomics, whose last bits
                                        depend on the order in which the GPU adds them. bsm_render,
                                        bsm_render_batch and bsm_render_cached; the serving loop ignores it */
 };
