@@ -72,6 +72,10 @@ extern "C" bsm_status bsm_cache_create(bsm_context* ctx, uint64_t seed, bsm_cach
               cudaMalloc((void**)&c->adam_m, kMlpParams * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->adam_v, kMlpParams * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->dW, kMlpParams * 4) == cudaSuccess &&
+              mlp_train_parts(c->device) > 0 &&
+              cudaMalloc((void**)&c->dW_parts, (size_t)mlp_train_parts(c->device) * kMlpParams * 4) == cudaSuccess &&
+              // the output layer's padded rows of every slot are never written: they stay zero
+              cudaMemset(c->dW_parts, 0, (size_t)mlp_train_parts(c->device) * kMlpParams * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->loss, kLossSlots * 4) == cudaSuccess &&
               cudaMalloc((void**)&c->err, 16) == cudaSuccess && cudaMemset(c->err, 0, 16) == cudaSuccess &&
               cudaMalloc((void**)&c->sample_count, 4) == cudaSuccess &&
@@ -100,9 +104,11 @@ extern "C" void bsm_cache_destroy(bsm_cache* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
-    for (void* p : {(void*)c->w_master, c->w_bf16, (void*)c->w_ema, c->w_ema_bf16, (void*)c->adam_m, (void*)c->adam_v, (void*)c->dW, (void*)c->loss, (void*)c->err,
+    for (void* p : {(void*)c->w_master, c->w_bf16, (void*)c->w_ema, c->w_ema_bf16, (void*)c->adam_m,
+                    (void*)c->adam_v, (void*)c->dW, (void*)c->dW_parts, (void*)c->loss, (void*)c->err,
                     (void*)c->samples, (void*)c->sample_count, (void*)c->view_dev, (void*)c->io, (void*)c->tv_raw,
-                    (void*)c->tv_thr, (void*)c->tv_rad, (void*)c->tv_count, c->tv_queue})
+                    (void*)c->tv_thr, (void*)c->tv_rad, (void*)c->tv_count, (void*)c->tv_fx, (void*)c->tv_nsamp,
+                    (void*)c->tv_offs, c->tv_queue})
         if (p) cudaFree(p);
     delete c;
 }
@@ -164,9 +170,11 @@ extern "C" bsm_status bsm_cache_gradient(bsm_cache* c, const float* samples, uin
     size_t in_b = (size_t)n * 64;
     if (cache_io(c, in_b)) return BSM_ERR_OUT_OF_MEMORY;
     cudaMemcpy(c->io, samples, in_b, cudaMemcpyHostToDevice);
-    cudaMemset(c->dW, 0, kMlpParams * 4);
     cudaMemset(c->loss, 0, 4);
-    if (launch_mlp_train(c->device, 0, c->w_bf16, (const float4*)c->io, n, c->dW, c->loss, c->err) != cudaSuccess)
+    uint32_t parts = 0;
+    if (launch_mlp_train(c->device, 0, c->w_bf16, (const float4*)c->io, n, c->dW_parts, &parts, c->loss, c->err) !=
+            cudaSuccess ||
+        launch_mlp_sum_parts(0, c->dW_parts, parts, c->dW) != cudaSuccess)
         return BSM_ERR_CUDA;
     if (cudaMemcpy(dW, c->dW, kMlpParams * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BSM_ERR_CUDA;
     if (loss) cudaMemcpy(loss, c->loss, 4, cudaMemcpyDeviceToHost);
@@ -198,14 +206,14 @@ bsm_status train_device(bsm_cache* c, const float4* samples, uint32_t n, uint32_
     for (uint32_t off = 0; off < n; off += batch) {
         uint32_t nb = std::min(batch, n - off);
         if (slot == 0) cudaMemsetAsync(c->loss, 0, kLossSlots * 4, st);
-        cudaMemsetAsync(c->dW, 0, kMlpParams * 4, st);
-        if (launch_mlp_train(c->device, st, c->w_bf16, samples + 4 * (size_t)off, nb, c->dW, c->loss + slot,
-                             c->err) != cudaSuccess)
+        uint32_t parts = 0;
+        if (launch_mlp_train(c->device, st, c->w_bf16, samples + 4 * (size_t)off, nb, c->dW_parts, &parts,
+                             c->loss + slot, c->err) != cudaSuccess)
             return BSM_ERR_CUDA;
         c->step++;
         if (ema_decay > 0.0f) c->ema_steps++;
-        if (launch_mlp_adam(st, c->w_master, c->w_bf16, c->dW, c->adam_m, c->adam_v, lr, c->step, c->w_ema,
-                            c->w_ema_bf16, ema_decay, c->ema_steps) != cudaSuccess)
+        if (launch_mlp_adam(st, c->w_master, c->w_bf16, c->dW_parts, parts, c->adam_m, c->adam_v, lr, c->step,
+                            c->w_ema, c->w_ema_bf16, ema_decay, c->ema_steps) != cudaSuccess)
             return BSM_ERR_CUDA;
         ++steps;
         if (++slot == kLossSlots) {
@@ -271,7 +279,8 @@ namespace bsm {
 static bsm_status ensure_train_verts(bsm_cache* c, uint32_t paths, uint32_t verts, uint32_t lights1) {
     if (c->tv_cap >= verts && c->tv_paths >= paths && c->tv_lights >= lights1) return BSM_OK;
     if ((uint64_t)verts * lights1 >= (1ull << 32) || (uint64_t)verts >= (1ull << 31)) return BSM_ERR_INVALID_ARG;
-    for (void** p : {(void**)&c->tv_raw, (void**)&c->tv_thr, (void**)&c->tv_rad, (void**)&c->tv_count, &c->tv_queue})
+    for (void** p : {(void**)&c->tv_raw, (void**)&c->tv_thr, (void**)&c->tv_rad, (void**)&c->tv_count,
+                     (void**)&c->tv_fx, (void**)&c->tv_nsamp, (void**)&c->tv_offs, &c->tv_queue})
         if (*p) { cudaFree(*p); *p = nullptr; }
     c->tv_cap = c->tv_paths = c->tv_lights = 0;
     const size_t sh = (size_t)verts * lights1;
@@ -280,6 +289,9 @@ static bsm_status ensure_train_verts(bsm_cache* c, uint32_t paths, uint32_t vert
               cudaMalloc((void**)&c->tv_thr, (size_t)verts * 16) == cudaSuccess &&
               cudaMalloc((void**)&c->tv_rad, (size_t)verts * 16) == cudaSuccess &&
               cudaMalloc((void**)&c->tv_count, (size_t)paths * 4) == cudaSuccess &&
+              cudaMalloc((void**)&c->tv_fx, (size_t)verts * 24) == cudaSuccess &&
+              cudaMalloc((void**)&c->tv_nsamp, (size_t)paths * 4) == cudaSuccess &&
+              cudaMalloc((void**)&c->tv_offs, (size_t)paths * 4) == cudaSuccess &&
               cudaMalloc(&c->tv_queue, qbytes) == cudaSuccess;
     if (!ok) return BSM_ERR_OUT_OF_MEMORY;
     c->tv_cap = verts;
@@ -312,8 +324,10 @@ bsm_status cache_train_frame(bsm_cache* c, const DevScene& sc, const DevView& vi
     q.sh_seed = (uint32_t*)(qb + 3 * sh * 16);
     q.counters = (uint32_t*)(qb + 3 * sh * 16 + ((sh * 4 + 255) & ~(size_t)255));
     q.stats = (unsigned long long*)((char*)q.counters + ((kCntWords * 4 + 255) & ~(size_t)255));
-    TrainVerts tv{c->tv_raw, c->tv_thr, c->tv_rad, c->tv_count, segs};
+    q.accum_fx = c->tv_fx;   // the shadow pass adds exact fixed-point sums per vertex
+    TrainVerts tv{c->tv_raw, c->tv_thr, c->tv_rad, c->tv_count, segs, c->tv_fx, c->tv_nsamp, c->tv_offs};
     cudaMemcpyAsync(c->view_dev, &view, sizeof(DevView), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(c->tv_fx, 0, (size_t)cap * 24, st);
     cudaMemsetAsync(c->sample_count, 0, 4, st);
     cudaMemsetAsync(q.counters, 0, kCntWords * 4, st);
     launch_train_paths(st, sc, c->view_dev, cs.train_paths, c->frame++, tv, q);

@@ -20,7 +20,8 @@ struct bsm_cache {
     float ema_decay = 0.0f;      // decay of the running average
     float* adam_m = nullptr;
     float* adam_v = nullptr;
-    float* dW = nullptr;
+    float* dW = nullptr;         // the summed gradient (bsm_cache_gradient)
+    float* dW_parts = nullptr;   // the training kernel's per-CTA gradient slots (mlp_train_parts of them)
     float* loss = nullptr;       // device: one loss per Adam step of a training call (kLossSlots)
     uint32_t* err = nullptr;     // device error word of the training kernels (bit 1: a tensor-core wait timed out)
     float4* samples = nullptr;   // training samples (4 float4 each)
@@ -31,6 +32,9 @@ struct bsm_cache {
     float4* tv_thr = nullptr;      // path throughput at the vertex
     float4* tv_rad = nullptr;      // radiance gathered at the vertex (NEE through the shadow pass, sky on escape)
     uint32_t* tv_count = nullptr;  // vertices per path
+    unsigned long long* tv_fx = nullptr;  // 3 words per vertex: the shadow pass's fixed-point radiance sums
+    uint32_t* tv_nsamp = nullptr;  // per block of 256 paths: samples, then the block's first sample
+    uint32_t* tv_offs = nullptr;   // each path's first sample within its block
     void* tv_queue = nullptr;      // shadow rays (origin, direction, contribution + vertex, seed), counters, stats
     uint32_t tv_cap = 0;           // vertices the buffers hold
     uint32_t tv_paths = 0;         // paths tv_count holds

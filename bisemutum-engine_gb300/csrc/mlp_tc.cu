@@ -32,8 +32,8 @@
 //   dW += g_z^T a    A: the gradient tile read MN-major (M = out, K = sample)
 //                    B: the activation tile [sample][in] read MN-major
 // with every layer's weight gradient accumulated in tensor memory over all
-// the tiles a CTA takes, and added to the global FP32 gradient on its last
-// tile by bulk reductions.  A training CTA has 256 threads, two per sample
+// the tiles a CTA takes, and copied on its last tile (bulk copies) to the
+// CTA's own FP32 gradient slot; Adam sums the slots in a fixed order.  A training CTA has 256 threads, two per sample
 // row, each reading back and storing half of the row's 64 columns.
 //
 // Every mbarrier wait gives up after one second: the kernel then sets bit 1
@@ -452,11 +452,10 @@ constexpr uint32_t kTrDw = 64;
 static_assert(kTrGradOff % 1024 == 0 && kTrBarOff % 1024 == 0, "swizzled tiles start on 1024-byte boundaries");
 static_assert(kTrDw + 5 * 64 <= kTrCols, "tensor-memory columns");
 
-// Bulk reduction of `bytes` (a multiple of 16) FP32 values from shared memory into global memory (element-wise
-// add, performed by the tensor-memory-access unit), tracked by this thread's bulk-async group.
-__device__ __forceinline__ void bulk_reduce_add_f32(float* gdst, uint32_t ssrc, uint32_t bytes) {
-    asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f32 [%0], [%1], %2;" ::"l"(gdst), "r"(ssrc),
-                 "r"(bytes)
+// Bulk copy of `bytes` (a multiple of 16) from shared to global memory, tracked by this thread's bulk-async
+// group.
+__device__ __forceinline__ void bulk_store(void* gdst, uint32_t ssrc, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(ssrc), "r"(bytes)
                  : "memory");
 }
 __device__ __forceinline__ void bulk_wait_all() {
@@ -542,9 +541,12 @@ __device__ __forceinline__ void stage_weight_grad(uint32_t dw, uint32_t rows, fl
 }
 
 // samples: 4 float4 each (raw inputs in the first three, the target rgb in
-// the fourth).  Adds the gradient of the mean relative L2 loss over the n
-// samples, sum over channels of (y - t)^2 / (y^2 + 0.01) / (3 n) with the
-// denominator held constant, to dW_global, and the loss to loss_out[0].
+// the fourth).  Writes the CTA's share of the gradient of the mean relative
+// L2 loss over the n samples, sum over channels of (y - t)^2 / (y^2 + 0.01) /
+// (3 n) with the denominator held constant, to its slot dW_parts + CTA x
+// kMlpParams (summed over the slots in a fixed order afterwards, so the
+// gradient does not depend on which CTA finishes first), and adds the loss to
+// loss_out[0].
 // Rounding points: encoded inputs, activations and gradients g_y, g_z in
 // BF16, products in FP32 (those of the oracle's BF16 network).
 //
@@ -555,7 +557,7 @@ __device__ __forceinline__ void stage_weight_grad(uint32_t dw, uint32_t rows, fl
 // raw inputs 4..11 and takes features and columns 32..63.
 __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloat16* __restrict__ w,
                                                                 const float4* __restrict__ s, uint32_t n,
-                                                                float* dW_global, float* loss_out, uint32_t* err) {
+                                                                float* dW_parts, float* loss_out, uint32_t* err) {
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw_s = smem_u32(smem_raw);
     const uint32_t base_s = (raw_s + 1023u) & ~1023u;
@@ -609,7 +611,8 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloa
     };
     auto nothing = [] {};
     // dW_L is complete after stage L of the CTA's last tile, and act tile L is no longer read: all threads stage
-    // it there, and thread 0 adds it to dW_global with a bulk reduction that overlaps the remaining work
+    // it there, and thread 0 copies it to the CTA's gradient slot with a bulk copy that overlaps the remaining work
+    float* const dW_slot = dW_parts + (size_t)blockIdx.x * kMlpParams;
     auto reduce_weight_grad = [&](int L) {
         tc_fence_after();
         const uint32_t rows = L < kMlpHidden ? 64u : (uint32_t)kMlpOut;
@@ -618,7 +621,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloa
         tc_fence_before();
         fence_async_smem();
         __syncthreads();
-        if (tid == 0) bulk_reduce_add_f32(dW_global + L * kMlpLayerParams, act_s + L * kTrTile, rows * 64u * 4u);
+        if (tid == 0) bulk_store(dW_slot + L * kMlpLayerParams, act_s + L * kTrTile, rows * 64u * 4u);
     };
     // all threads' shared-memory writes reach the tensor core; true when some thread's wait timed out
     auto publish = [&](bool done) -> bool {
@@ -732,7 +735,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloa
         }
         tc_fence_before();
     }
-    if (tid == 0) bulk_wait_all();   // the weight-gradient reductions (shared memory is read until they end)
+    if (tid == 0) bulk_wait_all();   // the weight-gradient copies (shared memory is read until they end)
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
@@ -776,16 +779,19 @@ cudaError_t launch_mlp_infer(int device, cudaStream_t st, const void* wb, const 
 }
 
 cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
-                             float* dW, float* loss, uint32_t* err) {
+                             float* dW_parts, uint32_t* parts, float* loss, uint32_t* err) {
+    *parts = 0;
     cudaError_t e = tc_setup(device);
     if (e != cudaSuccess) return e;
     if (n == 0) return cudaSuccess;
     // one CTA per SM (512 tensor-memory columns, 167 KB of shared memory), 128 samples at a time
     const uint32_t tiles = (n + kTcRows - 1) / kTcRows, sms = (uint32_t)g_tc_grid[device] / 4;
-    k_mlp_train_tc<<<tiles < sms ? tiles : sms, kTrThreads, kTrSmem, st>>>((const __nv_bfloat16*)wb, samples, n, dW, loss,
-                                                                        err);
+    *parts = tiles < sms ? tiles : sms;
+    k_mlp_train_tc<<<*parts, kTrThreads, kTrSmem, st>>>((const __nv_bfloat16*)wb, samples, n, dW_parts, loss, err);
     return cudaGetLastError();
 }
+
+uint32_t mlp_train_parts(int device) { return tc_setup(device) == cudaSuccess ? (uint32_t)g_tc_grid[device] / 4 : 0u; }
 
 cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
                                float* out, uint32_t* err) {

@@ -182,26 +182,39 @@ cudaError_t launch_mlp_predict(int device, cudaStream_t st, const void* wb, cons
                                float* out, uint32_t* err);
 // gradient of the mean relative L2 loss over n samples added to dW, the loss to loss[0]; a tensor-core wait
 // that timed out sets bit 1 of *err
+// Each CTA writes its share of the gradient to its own slot, dW_parts + cta x kMlpParams (rows 3..7 of the
+// output layer are not written: they keep the zeros the slots start with); *parts = the CTAs launched.
 cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const float4* samples, uint32_t n,
-                             float* dW, float* loss, uint32_t* err);
+                             float* dW_parts, uint32_t* parts, float* loss, uint32_t* err);
+// Gradient slots written by launch_mlp_train (at most mlp_train_parts(device) of them).
+uint32_t mlp_train_parts(int device);
+// dW = sum over the n_parts gradient slots, in slot order (mlp.cu)
+cudaError_t launch_mlp_sum_parts(cudaStream_t st, const float* dW_parts, uint32_t n_parts, float* dW);
 // Adam step; with ema_decay > 0 also updates the weights' moving average `ema` and writes its
 // bias-corrected bf16 copy `ema_b` (ema_step: steps averaged, this one included)
-cudaError_t launch_mlp_adam(cudaStream_t st, float* wm, void* wb, const float* dW, float* m, float* v, float lr,
-                            int step, float* ema, void* ema_b, float ema_decay, int ema_step);
+// The gradient is the sum of the n_parts slots of dW_parts, taken in slot order.
+cudaError_t launch_mlp_adam(cudaStream_t st, float* wm, void* wb, const float* dW_parts, uint32_t n_parts, float* m,
+                            float* v, float lr, int step, float* ema, void* ema_b, float ema_decay, int ema_step);
 // training paths (train_paths.cu): full-length paths that record per-vertex cache samples.
 // Vertex v = path x segments + k.  The path kernel writes each vertex's raw inputs (3 float4), throughput
 // and directly gathered radiance, and queues its next-event shadow rays in `shadow` (sun/light rays from the
-// front, sky rays from the back, contribution.w = the vertex's bits); the shadow pass (launch_shadow with
-// accum = vrad) adds the unoccluded ones; the targets kernel turns each vertex into a training sample.
+// front, sky rays from the back, contribution.w = the vertex's bits); the shadow pass (launch_shadow with the
+// queue's accum_fx = fx) adds the unoccluded ones as exact fixed-point sums; the targets kernels turn each
+// vertex into a training sample, written at an offset from a scan of the per-path counts, so the samples'
+// order (and everything trained on them) does not depend on the order of the GPU's atomics.
 struct TrainVerts {
     float4* raw;
     float4* thr;
     float4* rad;
     uint32_t* count;   // vertices per path
     uint32_t segments;
+    unsigned long long* fx;   // 3 words per vertex: the shadow pass's 32.32 fixed-point sums
+    uint32_t* nsamp;          // per block of 256 paths: its sample count, then (scanned) its first sample
+    uint32_t* offs;           // each path's first sample within its block
 };
 void launch_train_paths(cudaStream_t st, const DevScene& sc, const DevView* view, uint32_t n_paths, uint32_t frame,
                         const TrainVerts& tv, const Wavefront& shadow);
+// Samples of the n_paths paths at scanned offsets; *count = their total (those past max_samples are dropped).
 void launch_train_targets(cudaStream_t st, uint32_t n_paths, const TrainVerts& tv, float4* samples, uint32_t* count,
                           uint32_t max_samples);
 

@@ -7,11 +7,14 @@
 // escape).  Its next-event shadow rays are not traced in the thread: they go
 // to a shadow queue, which the persistent any-hit kernel traces afterwards in
 // one launch, adding each unoccluded contribution to its vertex.  A thread's
-// serial chain is thus its closest-hit rays only.  The targets kernel then
-// forms T_k = (sum of radiance at vertices j >= k) / throughput_k, the radiance
+// serial chain is thus its closest-hit rays only (the shadow pass adds exact
+// fixed-point sums, so a vertex's radiance does not depend on the order of the
+// additions).  The targets kernels then
+// form T_k = (sum of radiance at vertices j >= k) / throughput_k, the radiance
 // the rest of the path carried back to vertex k: the (input, T_k) pairs are
 // what the network learns, so that a path cut short at a vertex can be
-// finished with throughput x cache(vertex).
+// finished with throughput x cache(vertex).  Each path's samples go to an
+// offset from a scan of the per-path counts, so their order is fixed.
 // Pixels are drawn per frame by a hash of (frame, path index); random numbers
 // are PCG32 streams keyed to the pixel and a per-frame sample index.
 #include <cuda_runtime.h>
@@ -166,30 +169,100 @@ __global__ void __launch_bounds__(128, 4) k_train_paths(DevScene sc, const DevVi
     tv.count[i] = (uint32_t)nv;
 }
 
-// Targets: radiance carried back to each vertex of a path, as training samples.
-__global__ void k_train_targets(uint32_t n_paths, TrainVerts tv, float4* samples, uint32_t* count,
-                                uint32_t max_samples) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_paths) return;
+// A vertex's gathered radiance: what its path thread wrote (the sky on escape) plus the shadow pass's exact
+// fixed-point sums of its unoccluded next-event rays.
+__device__ __forceinline__ V3 vertex_radiance(const TrainVerts& tv, uint32_t v) {
+    const float4 r = tv.rad[v];
+    const unsigned long long* p = tv.fx + 3 * (size_t)v;
+    return v3(r.x + (float)((double)p[0] * 0x1p-32), r.y + (float)((double)p[1] * 0x1p-32),
+              r.z + (float)((double)p[2] * 0x1p-32));
+}
+
+// Targets of path i: the radiance carried back to each vertex k (from the last vertex down), divided by the
+// throughput there; emit(vertex, target) for each finite one, in that order.
+template <class Emit>
+__device__ __forceinline__ void path_targets(const TrainVerts& tv, uint32_t i, Emit emit) {
     const uint32_t v0 = i * tv.segments;
     const int nv = (int)tv.count[i];
     V3 acc = v3s(0.0f);
     for (int k = nv - 1; k >= 0; --k) {
-        float4 rad = tv.rad[v0 + k], tk4 = tv.thr[v0 + k];
-        acc = acc + v3(rad.x, rad.y, rad.z);
-        V3 tk = v3(tk4.x, tk4.y, tk4.z);
+        acc = acc + vertex_radiance(tv, v0 + (uint32_t)k);
+        const float4 tk4 = tv.thr[v0 + k];
+        const V3 tk = v3(tk4.x, tk4.y, tk4.z);
         if (!(tk.x > 0.0f && tk.y > 0.0f && tk.z > 0.0f)) continue;
-        V3 target = v3(acc.x / tk.x, acc.y / tk.y, acc.z / tk.z);
+        const V3 target = v3(acc.x / tk.x, acc.y / tk.y, acc.z / tk.z);
         if (!isfinite(target.x) || !isfinite(target.y) || !isfinite(target.z)) continue;
-        uint32_t slot = atomicAdd(count, 1u);
-        if (slot >= max_samples) continue;
-        const float4* rw = tv.raw + 3 * (size_t)(v0 + k);
-        float4* sd = samples + 4 * (size_t)slot;
-        sd[0] = rw[0];
-        sd[1] = rw[1];
-        sd[2] = rw[2];
-        sd[3] = make_float4(target.x, target.y, target.z, 0.0f);
+        emit(v0 + (uint32_t)k, target);
     }
+}
+
+// Inclusive sum of x over the threads of a block of kScanBlock threads up to this one; *total = the block's sum.
+constexpr uint32_t kScanBlock = 256;
+__device__ __forceinline__ uint32_t block_inclusive_scan(uint32_t x, uint32_t* total) {
+    __shared__ uint32_t s_warp[kScanBlock / 32];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[w] = x;
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kScanBlock / 32; ++k) {
+        const uint32_t t = s_warp[k];
+        before += k < w ? t : 0u;
+        all += t;
+    }
+    __syncthreads();   // s_warp is reused by the next call
+    *total = all;
+    return x + before;
+}
+
+// Per-path sample counts: each path's offset within its block (tv.offs) and each block's total (tv.nsamp[block]).
+__global__ void __launch_bounds__(kScanBlock) k_train_count(uint32_t n_paths, TrainVerts tv) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t c = 0;
+    if (i < n_paths) path_targets(tv, i, [&](uint32_t, V3) { ++c; });
+    uint32_t total;
+    const uint32_t incl = block_inclusive_scan(c, &total);
+    if (i < n_paths) tv.offs[i] = incl - c;
+    if (threadIdx.x == 0) tv.nsamp[blockIdx.x] = total;
+}
+
+// Exclusive scan, in place, of the n block totals by one block (in tiles of kScanBlock); *total = their sum.
+__global__ void __launch_bounds__(kScanBlock) k_scan_blocks(uint32_t* cnt, uint32_t n, uint32_t* total) {
+    uint32_t carry = 0;
+    for (uint32_t b = 0; b < n; b += kScanBlock) {
+        const uint32_t i = b + threadIdx.x;
+        const uint32_t x = i < n ? cnt[i] : 0u;
+        uint32_t sum;
+        const uint32_t incl = block_inclusive_scan(x, &sum);
+        if (i < n) cnt[i] = carry + incl - x;
+        carry += sum;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// Writes path i's samples from its scanned offset on (those past max_samples are dropped); blocks of
+// kScanBlock paths, as k_train_count's.
+__global__ void __launch_bounds__(kScanBlock) k_train_targets(uint32_t n_paths, TrainVerts tv, float4* samples,
+                                                              uint32_t max_samples) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_paths) return;
+    uint32_t slot = tv.nsamp[blockIdx.x] + tv.offs[i];   // the block's first sample + the path's offset in it
+    path_targets(tv, i, [&](uint32_t v, V3 target) {
+        if (slot < max_samples) {
+            const float4* rw = tv.raw + 3 * (size_t)v;
+            float4* sd = samples + 4 * (size_t)slot;
+            sd[0] = rw[0];
+            sd[1] = rw[1];
+            sd[2] = rw[2];
+            sd[3] = make_float4(target.x, target.y, target.z, 0.0f);
+        }
+        ++slot;
+    });
 }
 
 void launch_train_paths(cudaStream_t st, const DevScene& sc, const DevView* view, uint32_t n_paths, uint32_t frame,
@@ -201,7 +274,10 @@ void launch_train_paths(cudaStream_t st, const DevScene& sc, const DevView* view
 void launch_train_targets(cudaStream_t st, uint32_t n_paths, const TrainVerts& tv, float4* samples, uint32_t* count,
                           uint32_t max_samples) {
     if (n_paths == 0) return;
-    k_train_targets<<<(n_paths + 255) / 256, 256, 0, st>>>(n_paths, tv, samples, count, max_samples);
+    const uint32_t blocks = (n_paths + kScanBlock - 1) / kScanBlock;
+    k_train_count<<<blocks, kScanBlock, 0, st>>>(n_paths, tv);
+    k_scan_blocks<<<1, kScanBlock, 0, st>>>(tv.nsamp, blocks, count);
+    k_train_targets<<<blocks, kScanBlock, 0, st>>>(n_paths, tv, samples, max_samples);
 }
 
 }  // namespace bsm

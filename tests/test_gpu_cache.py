@@ -240,6 +240,36 @@ def test_cached_render_as_the_first_call_of_a_context(bsm):
     assert np.abs(a - b).mean() <= 1e-2 * np.abs(b).mean()
 
 
+def test_online_training_is_bit_reproducible(bsm, ctx):
+    """Two caches from the same seed, trained online by the same cached frames, end with the same weights and
+    render the same images bit for bit: the training paths' shadow pass sums each vertex's radiance exactly,
+    the samples sit at offsets from a scan of the per-path counts, and Adam sums the training kernel's per-CTA
+    gradient slots in a fixed order (the frames sum in fixed point too: BSM_PT_DETERMINISTIC)."""
+    scene = bsm.generate_scene(bsm.BSM_SCENE_ROOM, seed=41, spheres=24)
+    sid = ctx.load_scene(scene)
+    cam = bsm.make_camera(tuple(scene.camera.position), tuple(scene.camera.front), width=64, height=48)
+    cs = bsm.cache_settings(cache_segment=2, train_paths=20000, train_steps=2, train_batch=8192)
+    s = bsm.settings(spp=2, seed=9, flags=bsm.BSM_PT_DETERMINISTIC)
+    runs = []
+    try:
+        for _ in range(2):
+            c = bsm.RadianceCache(ctx, seed=5)
+            try:
+                w0 = c.weights().copy()
+                frames = [c.render(sid, cam, s, cs)[0] for _ in range(3)]
+                runs.append((w0, c.weights().copy(), frames))
+            finally:
+                c.close()
+    finally:
+        ctx.release(sid)
+    (w0, wa, fa), (_, wb, fb) = runs
+    assert not np.array_equal(w0, wa), "no training happened"
+    assert np.array_equal(wa.view(np.uint32), wb.view(np.uint32))
+    for x, y in zip(fa, fb):
+        assert x[..., :3].mean() > 0.0
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
 @pytest.mark.parametrize("extra, min_rough", [(0, 0.0), (2, 0.5)])
 def test_cached_render_matches_oracle(bsm, ctx, oracle, extra, min_rough):
     """The cached pass without its training step (bsm_render_cached, train_steps = 0) against the oracle's
