@@ -356,6 +356,23 @@ def run_ours(a, dist: Dist):
     e2e_s = dist.max(time.perf_counter() - e0)
     e2e_val = rays_all / a.steps * e2e_steps / e2e_s / 1e6
     L.bsm_host_free(ctx.h, host)
+    # the same frame with bit-reproducible fixed-point accumulation (BSM_PT_DETERMINISTIC), device time
+    det = None
+    if not a.no_extras and not a.deterministic:
+        s_det = bsm.settings(spp=a.spp, max_segments=a.segments, seed=seed,
+                             flags=flags_timed | bsm.BSM_PT_DETERMINISTIC, block_size=a.block,
+                             wavefront_capacity=a.capacity)
+        ctx.render(sid, [cam], s_det, outputs=False)
+        det_ms, det_rays, det_steps = 0.0, 0, 3
+        for _ in range(det_steps):
+            flush_l2()
+            _, dst = ctx.render(sid, [cam], s_det, outputs=False)
+            det_ms += dst.ms_total
+            det_rays += dst.extend_rays
+        det = {"mrays_per_s": round(det_rays / (det_ms / 1e3) / 1e6, 2), "ms_per_step": round(det_ms / det_steps, 3),
+               "steps": det_steps,
+               "what": "BSM_PT_DETERMINISTIC: exact 32.32 fixed-point per-pixel sums; images bit-identical from run "
+                       "to run and to the CPU oracle's fixed-point mode"}
     L.bsm_device_free(ctx.h, flush)
     bvh_cmp = None
     if dist.rank == 0 and not a.no_extras:
@@ -417,7 +434,8 @@ def run_ours(a, dist: Dist):
                         "build_ms": round(bvh.build_ms, 2), "nodes": bvh.num_nodes,
                         "depth": bvh.max_depth, "bytes": bvh.node_bytes + bvh.tri_bytes,
                         "upload_and_build_s": round(setup_s, 3), **(bvh_cmp or {})},
-                "wall_s_timed": round(wall, 3)}
+                "wall_s_timed": round(wall, 3),
+                **({"deterministic": det} if det else {})}
     ctx.close()
     if line is not None and not a.no_extras:
         # the benchmark spec's other forms, each on its own context after the timed region: 64 uneven views batched
