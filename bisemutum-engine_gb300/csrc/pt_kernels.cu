@@ -39,19 +39,25 @@ __device__ __forceinline__ uint32_t warp_alloc(bool pred, uint32_t* counter) {
     return base + (uint32_t)__popc(b & lanemask_lt());
 }
 
-// Queue slots for the threads of a block with `pred`, grouped by the octant of
-// `dir` (one atomic on `counter` per block).  Consecutive slots then hold rays
-// heading the same way from neighbouring paths, which keeps the warps of the
-// next traversal and shading launches coherent.  The lanes of a warp that
-// share an octant take their ranks from one shared-memory atomic.  Every
+// Queue slots for the threads of a block with `pred`, grouped by the direction
+// of `dir`: its octant and its dominant axis, 24 bins (one atomic on `counter`
+// per block).  Consecutive slots then hold rays heading the same way from
+// neighbouring paths, which keeps the warps of the next traversal and shading
+// launches coherent.  The lanes of a warp that share a bin take their ranks
+// from one shared-memory atomic; warp 0 scans the bins.  Every
 // thread of the block must call it with the same `parity`, alternating 0 / 1
 // from call to call, after s_oct_cnt[0] was cleared: each call clears the
 // other parity's counters for the next one, so it needs two block barriers
 // instead of three.  Returns 0 for threads without pred.
-__shared__ uint32_t s_oct_cnt[2][9];
+constexpr uint32_t kDirBins = 24;   // octant x dominant axis
+static_assert(kDirBins <= 32, "one warp scans the bins");
+__shared__ uint32_t s_oct_cnt[2][kDirBins + 1];
 __device__ __forceinline__ uint32_t block_alloc_by_octant(bool pred, V3 dir, uint32_t* counter, int parity) {
-    __shared__ uint32_t s_off[2][8], s_base[2];
-    uint32_t key = pred ? ((dir.x < 0.0f ? 1u : 0u) | (dir.y < 0.0f ? 2u : 0u) | (dir.z < 0.0f ? 4u : 0u)) : 8u;
+    __shared__ uint32_t s_off[2][kDirBins], s_base[2];
+    const float ax = fabsf(dir.x), ay = fabsf(dir.y), az = fabsf(dir.z);
+    const uint32_t dom = (ax >= ay && ax >= az) ? 0u : (ay >= az ? 1u : 2u);
+    uint32_t key = pred ? ((dir.x < 0.0f ? 1u : 0u) | (dir.y < 0.0f ? 2u : 0u) | (dir.z < 0.0f ? 4u : 0u)) * 3u + dom
+                        : kDirBins;
     // one shared atomic per octant present in the warp (the lanes of an octant share it)
     const uint32_t peers = __match_any_sync(0xffffffffu, key);
     const uint32_t leader = (uint32_t)__ffs(peers) - 1u;
@@ -59,12 +65,20 @@ __device__ __forceinline__ uint32_t block_alloc_by_octant(bool pred, V3 dir, uin
     if ((threadIdx.x & 31u) == leader && pred) rank = atomicAdd(&s_oct_cnt[parity][key], (uint32_t)__popc(peers));
     rank = __shfl_sync(0xffffffffu, rank, (int)leader) + (uint32_t)__popc(peers & lanemask_lt());
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (int k = 0; k < 8; ++k) { s_off[parity][k] = acc; acc += s_oct_cnt[parity][k]; }
-        s_base[parity] = acc ? atomicAdd(counter, acc) : 0u;
+    if (threadIdx.x < 32) {   // exclusive prefix over the bins by warp 0, one bin per lane
+        const uint32_t lane = threadIdx.x;
+        const uint32_t c = lane < kDirBins ? s_oct_cnt[parity][lane] : 0u;
+        uint32_t x = c;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane < kDirBins) s_off[parity][lane] = x - c;
+        const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
+        if (lane == 0) s_base[parity] = total ? atomicAdd(counter, total) : 0u;
     }
-    if (threadIdx.x < 9) s_oct_cnt[parity ^ 1][threadIdx.x] = 0u;
+    if (threadIdx.x <= kDirBins) s_oct_cnt[parity ^ 1][threadIdx.x] = 0u;
     __syncthreads();
     return pred ? s_base[parity] + s_off[parity][key] + rank : 0u;
 }
@@ -243,7 +257,7 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
     uint4* out_p = wf.path[q ^ 1];
     float4* out_t = wf.thr[q ^ 1];
     const uint32_t stride = gridDim.x * blockDim.x;
-    if (threadIdx.x < 9) s_oct_cnt[0][threadIdx.x] = 0u;
+    if (threadIdx.x <= kDirBins) s_oct_cnt[0][threadIdx.x] = 0u;
     __syncthreads();
     int parity = 0;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride, parity ^= 1) {
