@@ -24,13 +24,17 @@
 // those of the oracle's BF16 network; only the order of the FP32 sums differs.
 //
 // The training step (k_mlp_train_tc) runs forward and backward passes of
-// 128-sample tiles on the same units.  Its backward products read operands
-// that are stored for the forward ones, in the MN-major form of the same
-// swizzled tiles (no transposed copies):
-//   g_a = g_z W      A: the gradient tile [sample][out], K-major (K = out)
+// 128-sample tiles on the same units.  The forward layers read A from tensor
+// memory as inference does, and also keep each activation tile in shared
+// memory, where the backward products read them in the MN-major form of the
+// same swizzled tiles (no transposed copies):
+//   g_a = g_z W      A: the gradient [sample][out] in tensor memory (K = out)
 //                    B: W [out][in] read MN-major (N = in, K = out)
 //   dW += g_z^T a    A: the gradient tile read MN-major (M = out, K = sample)
 //                    B: the activation tile [sample][in] read MN-major
+// The dW products are issued by a second thread and waited for two steps
+// later (three gradient tiles rotate), so they run beside the chain of g_a
+// products and epilogues.
 // with every layer's weight gradient accumulated in tensor memory over all
 // the tiles a CTA takes, and copied on its last tile (bulk copies) to the
 // CTA's own FP32 gradient slot; Adam sums the slots in a fixed order.  A training CTA has 256 threads, two per sample
@@ -255,6 +259,22 @@ __device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&v)[32])
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
+// 16 and 8 columns of the warp's 32 lanes stored, then waited for.
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const uint32_t (&v)[16]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {"
+                 "%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+                 "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+                 "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+                 : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_st8(uint32_t taddr, const uint32_t (&v)[8]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+                 "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
@@ -433,24 +453,27 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward_tc(const __nv_bfloat16*
 
 // ------------------------------------------------------------- training ----
 // Shared memory of k_mlp_train_tc: the weights (as the forward kernel), the
-// five activation tiles of a 128-sample tile (encoded input e, a0..a3), two
-// gradient tiles that alternate between the backward steps (gy, gz3, gz2, gz1,
-// gz0), one mbarrier and the tensor-memory address (167 KB: one CTA per SM).
+// five activation tiles of a 128-sample tile (encoded input e, a0..a3), three
+// gradient tiles that rotate over the backward steps (gy, gz3, gz2, gz1, gz0:
+// a step's weight-gradient product may still read its tile while the next two
+// steps run), the mbarriers and the tensor-memory address (183 KB: one CTA per SM).
 constexpr int kTrTile = kTcRows * 128;                          // 16 KB per 128 x 64 BF16 tile
 constexpr int kTrActOff = kTcWRows * 128;                       // 34816
 constexpr int kTrGradOff = kTrActOff + 5 * kTrTile;             // 116736
-constexpr int kTrBarOff = kTrGradOff + 2 * kTrTile;             // 149504
+constexpr int kTrBarOff = kTrGradOff + 3 * kTrTile;             // 165888
 // 16 KB beyond the barrier are never written: every operand window of the products
 // (start + 16 rows x 128 bytes per K step, or a whole 16 KB tile read K-major)
 // lies inside the allocation.
 constexpr int kTrSmem = kTrBarOff + 16384 + 1024;
 // Tensor memory: columns 0..63 hold the product being read back (forward z,
-// backward g_a); 64 + 64 l .. 127 + 64 l hold dW_l (l = 0..4; rows = outputs).
+// backward g_a); 64 + 64 l .. 127 + 64 l hold dW_l (l = 0..4; rows = outputs);
+// 384..415 hold the A operand (activations, then gradients) as BF16 pairs.
 constexpr uint32_t kTrCols = 512;
 constexpr int kTrThreads = 256;                                 // two threads per sample row
 constexpr uint32_t kTrDw = 64;
+constexpr uint32_t kTrA = kTrDw + 5 * 64;                       // 384: the A operand (32 columns)
 static_assert(kTrGradOff % 1024 == 0 && kTrBarOff % 1024 == 0, "swizzled tiles start on 1024-byte boundaries");
-static_assert(kTrDw + 5 * 64 <= kTrCols, "tensor-memory columns");
+static_assert(kTrA + 32 <= kTrCols, "tensor-memory columns");
 
 // Bulk copy of `bytes` (a multiple of 16) from shared to global memory, tracked by this thread's bulk-async
 // group.
@@ -463,47 +486,53 @@ __device__ __forceinline__ void bulk_wait_all() {
     asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
-// g_z = g_a * (a > 0) for the 16 columns [c, c + 16) of v (this thread's columns of its row of g_a), as two
-// BF16 chunks.
-template <int kN>
-__device__ __forceinline__ void relu_grad_chunks(const uint32_t (&v)[kN], int c, const uint4& a0, const uint4& a1,
-                                                 uint4& o0, uint4& o1) {
-    const uint32_t av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-    uint32_t p[8];
+// g_z = g_a * (a > 0) for this thread's 32 columns v of its row of g_a, as 16 BF16 pairs (a: the same
+// columns of the activation row, 4 chunks).
+__device__ __forceinline__ void relu_grad_words(const uint32_t (&v)[32], const uint4 (&a)[4], uint32_t (&p)[16]) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const float lo = __uint_as_float(av[i] << 16) > 0.0f ? __uint_as_float(v[c + 2 * i]) : 0.0f;
-        const float hi = __uint_as_float(av[i] & 0xffff0000u) > 0.0f ? __uint_as_float(v[c + 2 * i + 1]) : 0.0f;
-        p[i] = pack2(lo, hi);
+    for (int c = 0; c < 4; ++c) {
+        const uint32_t av[4] = {a[c].x, a[c].y, a[c].z, a[c].w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int j = 4 * c + i;
+            const float lo = __uint_as_float(av[i] << 16) > 0.0f ? __uint_as_float(v[2 * j]) : 0.0f;
+            const float hi = __uint_as_float(av[i] & 0xffff0000u) > 0.0f ? __uint_as_float(v[2 * j + 1]) : 0.0f;
+            p[j] = pack2(lo, hi);
+        }
     }
-    o0 = make_uint4(p[0], p[1], p[2], p[3]);
-    o1 = make_uint4(p[4], p[5], p[6], p[7]);
 }
 
-// Half h of the encoded features of one sample, written into row r of the activation tile: h = 0 encodes
-// raw[0..3] (f0) as chunks 0..3; h = 1 encodes raw[4..6] (f0.xyz) as chunks 4..6 and writes chunk 7 from
-// raw[7] = f0.w and raw[8..11] = f1.  The values are those of encode_words.
-__device__ __forceinline__ void encode_half(int h, const float4& f0, const float4& f1, unsigned char* act, int r) {
+// Half h of the encoded features of one sample (features 32 h .. 32 h + 31) as 16 BF16 pairs, word 4 d + k
+// of chunk 4 h + d: h = 0 encodes raw[0..3] (f0) as chunks 0..3; h = 1 encodes raw[4..6] (f0.xyz) as chunks
+// 4..6 and fills chunk 7 from raw[7] = f0.w and raw[8..11] = f1.  The values are those of encode_words.
+__device__ __forceinline__ void encode_half(int h, const float4& f0, const float4& f1, uint32_t (&p)[16]) {
     const float x[4] = {f0.x, f0.y, f0.z, f0.w};
 #pragma unroll
     for (int d = 0; d < 4; ++d) {
         if (h && d == 3) break;
-        uint32_t p[4];
         float s, c;
         __sincosf(x[d] * 3.14159265f, &s, &c);
-        p[0] = pack2(s, c);
+        p[4 * d] = pack2(s, c);
 #pragma unroll
         for (int k = 1; k < 4; ++k) {
             float s2 = 2.0f * s * c, c2 = (c - s) * (c + s);
             s = s2;
             c = c2;
-            p[k] = pack2(s, c);
+            p[4 * d + k] = pack2(s, c);
         }
-        *tile_chunk(act, r, 4 * h + d) = make_uint4(p[0], p[1], p[2], p[3]);
     }
-    if (h)
-        *tile_chunk(act, r, 7) =
-            make_uint4(pack2(f0.w, f1.x), pack2(f1.y, f1.z), pack2(f1.w, 1.0f), pack2(0.0f, 0.0f));
+    if (h) {
+        p[12] = pack2(f0.w, f1.x);
+        p[13] = pack2(f1.y, f1.z);
+        p[14] = pack2(f1.w, 1.0f);
+        p[15] = pack2(0.0f, 0.0f);
+    }
+}
+
+// Row r's words p (16 per half h, as encode_half lays them out) into the chunks 4 h .. 4 h + 3 of a tile.
+__device__ __forceinline__ void store_half(unsigned char* tile, int r, int h, const uint32_t (&p)[16]) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) *tile_chunk(tile, r, 4 * h + c) = make_uint4(p[4 * c], p[4 * c + 1], p[4 * c + 2], p[4 * c + 3]);
 }
 
 // r[j] = v[(j + k) mod 4] for k = 0..3 in two conditional rotations (no indexed register access).
@@ -567,6 +596,9 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloa
     unsigned char* grad = base + kTrGradOff;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kTrBarOff + 8);
     const uint32_t wbar = bar + 16;
+    // the weight-gradient products (issued by thread 128): dW_L commits to dwbar(L & 1), so that each barrier
+    // has at most one commit outstanding when it is waited on (the waits lag the commits by two steps)
+    auto dwbar = [&](int L) -> uint32_t { return bar + 24 + 8 * (uint32_t)(L & 1); };
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, r = tid & (kTcRows - 1), h = tid >> 7;
 
     // this thread's half of its row's sample in the next tile, loaded ahead: the first before the weights
@@ -577,7 +609,11 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloa
     };
     fetch(blockIdx.x * kTcRows + r);
     load_weights_async(w, base, base_s, wbar, tid);
-    if (tid == 0) mbar_init(bar, 1);
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_init(dwbar(0), 1);
+        mbar_init(dwbar(1), 1);
+    }
     __syncwarp();
     if (warp == 0) tc_alloc(smem_u32(tmem_slot), kTrCols);
     fence_async_smem();
@@ -587,29 +623,22 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloa
     const uint32_t tmem = *tmem_slot;
     const uint32_t rows_tmem = tmem + ((uint32_t)((warp & 3) * 32) << 16);   // this warp's 32 lanes
     const uint32_t cols = 32u * (uint32_t)h;                                  // this thread's 32 columns
+    const uint32_t a_half = rows_tmem + kTrA + 16u * (uint32_t)h;             // its 16 columns of A
     const float inv = 1.0f / (3.0f * (float)n);
     float loss = 0.0f;
-    uint32_t phase = 0;
+    uint32_t phase = 0, dw_phase[2] = {0u, 0u};
     bool failed = false;
     const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
 
-    // one round of products issued by thread 0, then the wait of all threads; false when it timed out
-    // `between` runs on all threads while the products execute
-    auto run = [&](auto issue, auto between) -> bool {
-        if (tid == 0) {
-            tc_fence_after();
-            issue();
-            tc_commit(bar);
-        }
-        between();
+    // all threads wait for the products committed to `b`; false when the wait timed out
+    auto wait_products = [&](uint32_t b, uint32_t& ph) -> bool {
         __syncwarp();
-        const bool done = mbar_wait(bar, phase);
-        phase ^= 1u;
+        const bool ok = mbar_wait(b, ph);
+        ph ^= 1u;
         __syncwarp();
         tc_fence_after();
-        return done;
+        return ok;
     };
-    auto nothing = [] {};
     // dW_L is complete after stage L of the CTA's last tile, and act tile L is no longer read: all threads stage
     // it there, and thread 0 copies it to the CTA's gradient slot with a bulk copy that overlaps the remaining work
     float* const dW_slot = dW_parts + (size_t)blockIdx.x * kMlpParams;
@@ -623,41 +652,51 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloa
         __syncthreads();
         if (tid == 0) bulk_store(dW_slot + L * kMlpLayerParams, act_s + L * kTrTile, rows * 64u * 4u);
     };
-    // all threads' shared-memory writes reach the tensor core; true when some thread's wait timed out
+    // all threads' shared- and tensor-memory writes reach the tensor core; true when some thread's wait timed out
     auto publish = [&](bool done) -> bool {
         fence_async_smem();
         tc_fence_before();
         return __syncthreads_or(!done) != 0;
     };
 
+    // Products: the forward layers and the backward g_a read A (activations, then gradients) from tensor
+    // memory (columns kTrA..), where each thread stores its 16 columns, and B (the weights) from shared
+    // memory; the weight gradients dW_L += g_in^T a(L-1) read both operands from the shared-memory tiles
+    // (MN-major), issued by thread 128 and waited for two steps later, so that they run while the chain of
+    // g_a products and their epilogues goes on.  The gradient of step L lives in tile gtile(L).
+    auto gtile = [](int L) -> uint32_t { return (uint32_t)((kMlpHidden - L) % 3) * kTrTile; };
+    auto wait_dw = [&](int L) -> bool { return wait_products(dwbar(L), dw_phase[L & 1]); };
     for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
         const bool first = tile == blockIdx.x, last = tile + gridDim.x >= tiles;
         const uint32_t row = tile * kTcRows + r;
         const float4 f0 = nx[0], f1 = nx[1];   // h = 0: f1 is the target
         fetch(row + gridDim.x * kTcRows);
-        encode_half(h, f0, f1, act, r);
+        {
+            uint32_t p[16];
+            encode_half(h, f0, f1, p);
+            store_half(act, r, h, p);   // e, read by dW_0
+            tc_st16(a_half, p);         // A of layer 0
+        }
         if (publish(!first || mbar_wait(wbar, 0))) { failed = true; break; }
         // forward: act[l + 1] = relu(act[l] W_l^T), y = a3 W4^T
         float y0 = 0.0f, y1 = 0.0f, y2 = 0.0f;
         for (int l = 0; l <= kMlpHidden && !failed; ++l) {
-            const bool done = run([&] {
-                const uint32_t w_s = base_s + l * 64 * 128, a_s = act_s + l * kTrTile;
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t w_s = base_s + l * 64 * 128;
                 const uint32_t idesc = l < kMlpHidden ? tc_idesc(kTcRows, 64) : tc_idesc(kTcRows, kTcW4Rows);
 #pragma unroll
-                for (int k = 0; k < 4; ++k) tc_mma(tmem, tc_sdesc(a_s + 32 * k), tc_sdesc(w_s + 32 * k), idesc, k);
-            }, nothing);
+                for (int k = 0; k < 4; ++k) tc_mma_ts(tmem, tmem + kTrA + 8 * k, tc_sdesc(w_s + 32 * k), idesc, k);
+                tc_commit(bar);
+            }
+            const bool done = wait_products(bar, phase);
             if (l < kMlpHidden) {
-                unsigned char* out = act + (l + 1) * kTrTile;
-                uint32_t v[32];
+                uint32_t v[32], p[16];
                 tc_ld32(rows_tmem + cols, v);
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    uint32_t p[4];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        p[i] = pack2_relu(__uint_as_float(v[8 * c + 2 * i]), __uint_as_float(v[8 * c + 2 * i + 1]));
-                    *tile_chunk(out, r, 4 * h + c) = make_uint4(p[0], p[1], p[2], p[3]);
-                }
+                for (int i = 0; i < 16; ++i) p[i] = pack2_relu(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+                store_half(act + (l + 1) * kTrTile, r, h, p);   // a_l, read by the backward pass
+                tc_st16(a_half, p);                              // A of layer l + 1
             } else if (h == 0) {
                 uint32_t v[16];
                 tc_ld16(rows_tmem, v);
@@ -666,7 +705,8 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloa
             if (publish(done)) failed = true;
         }
         if (failed) break;
-        // loss gradient g_y (rows >= n: zero), into gradient tile 0 (chunk 0: channels 0..7; the rest zero)
+        // loss gradient g_y (rows >= n: zero): gradient tile 0 (chunk 0: channels 0..7; the rest zero) and, as
+        // the A of g_a(4) (K = 16), tensor-memory columns kTrA .. kTrA + 7
         if (h == 0) {
             const float yv[3] = {y0, y1, y2}, tv[3] = {f1.x, f1.y, f1.z};
             float gy[3];
@@ -676,52 +716,58 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloa
                 loss += row < n ? d * d * rden : 0.0f;
                 gy[c] = row < n ? 2.0f * d * rden : 0.0f;
             }
-            *tile_chunk(grad, r, 0) = make_uint4(pack2(gy[0], gy[1]), pack2(gy[2], 0.0f), 0u, 0u);
+            const uint32_t g[8] = {pack2(gy[0], gy[1]), pack2(gy[2], 0.0f), 0u, 0u, 0u, 0u, 0u, 0u};
+            *tile_chunk(grad, r, 0) = make_uint4(g[0], g[1], 0u, 0u);
+            tc_st8(rows_tmem + kTrA, g);
         }
 #pragma unroll
         for (int c = 0; c < 4; ++c)
             if (h || c > 0) *tile_chunk(grad, r, 4 * h + c) = make_uint4(0u, 0u, 0u, 0u);
         if (publish(true)) { failed = true; break; }
-        // backward: step L reads gradient tile L & 1 (g_y, then g_z3 .. g_z0), adds dW_L and, for L > 0,
-        // writes g_z(L-1) = (g_in W_L) * (a(L-1) > 0) into the other gradient tile
+        // backward: step L reads gradient tile gtile(L) (g_y, then g_z3 .. g_z0; the same values as A in tensor
+        // memory), adds dW_L and, for L > 0, writes g_z(L-1) = (g_in W_L) * (a(L-1) > 0) into tile gtile(L-1)
+        // and into A
         for (int L = kMlpHidden; L >= 0 && !failed; --L) {
-            const uint32_t g_s = grad_s + (uint32_t)((kMlpHidden - L) & 1) * kTrTile;
+            const uint32_t g_s = grad_s + gtile(L);
             const uint32_t a_s = act_s + L * kTrTile;   // a(L-1): e for L = 0, a3 for L = 4
             uint4 ar[4];                                  // this thread's half of the mask row: a(L-1) > 0
             if (L > 0)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) ar[c] = *tile_chunk(act + L * kTrTile, r, 4 * h + c);
-            const bool done = run([&] {
-                if (L > 0) {   // g_a = g_in W_L: K = outputs of layer L (16 for the output layer)
-                    const uint32_t w_s = base_s + L * 64 * 128;
-                    const uint32_t idesc = tc_idesc_mn(kTcRows, 64, false, true);
-                    const int ks = L == kMlpHidden ? 1 : 4;
-                    for (int k = 0; k < ks; ++k)
-                        tc_mma(tmem, tc_sdesc(g_s + 32 * k), tc_sdesc_mn(w_s + 2048 * k), idesc, k);
-                }
-                // dW_L += g_in^T a(L-1): M = outputs (rows 64..127 repeat them), K = the 128 samples
+            // dW_{L+2} has read tile gtile(L-1) = gtile(L+2), which this step overwrites, and is in tensor memory
+            bool done = L + 2 > kMlpHidden || wait_dw(L + 2);
+            if (tid == 0 && L > 0) {   // g_a = g_in W_L: K = outputs of layer L (16 for the output layer)
+                tc_fence_after();
+                const uint32_t w_s = base_s + L * 64 * 128;
+                const uint32_t idesc = tc_idesc_mn(kTcRows, 64, false, true);
+                const int ks = L == kMlpHidden ? 1 : 4;
+                for (int k = 0; k < ks; ++k) tc_mma_ts(tmem, tmem + kTrA + 8 * k, tc_sdesc_mn(w_s + 2048 * k), idesc, k);
+                tc_commit(bar);
+            }
+            if (tid == 128) {   // dW_L += g_in^T a(L-1): M = outputs (rows 64..127 repeat them), K = the 128 samples
+                tc_fence_after();
                 const uint32_t idesc = tc_idesc_mn(kTcRows, 64, true, true);
                 const uint32_t d = tmem + kTrDw + 64 * (uint32_t)L;
 #pragma unroll
                 for (int k = 0; k < kTcRows / 16; ++k)
                     tc_mma(d, tc_sdesc_mn(g_s + 2048 * k), tc_sdesc_mn(a_s + 2048 * k), idesc, first && k == 0 ? 0u : 1u);
-            }, [&] {   // the previous stage's layer, complete on the last tile, while this stage's products run
-                if (last && L < kMlpHidden) reduce_weight_grad(L + 1);
-            });
+                tc_commit(dwbar(L));
+            }
+            // the layer two steps back, complete on the last tile, while this step's products run
+            if (last && L + 2 <= kMlpHidden) reduce_weight_grad(L + 2);
             if (L > 0) {
-                unsigned char* out = grad + (uint32_t)((kMlpHidden - L + 1) & 1) * kTrTile;
-                uint32_t v[32];
+                done = wait_products(bar, phase) && done;
+                uint32_t v[32], p[16];
                 tc_ld32(rows_tmem + cols, v);
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    uint4 o0, o1;
-                    relu_grad_chunks(v, 16 * q, ar[2 * q], ar[2 * q + 1], o0, o1);
-                    *tile_chunk(out, r, 4 * h + 2 * q) = o0;
-                    *tile_chunk(out, r, 4 * h + 2 * q + 1) = o1;
-                }
+                relu_grad_words(v, ar, p);
+                store_half(grad + gtile(L - 1), r, h, p);   // read by dW_(L-1)
+                tc_st16(a_half, p);                         // A of g_a(L-1)
             }
             if (publish(done)) failed = true;
         }
+        // dW_1 and dW_0: the next tile's forward pass overwrites the tiles they read
+        if (!failed && publish(wait_dw(1) && wait_dw(0))) failed = true;
+        if (last && !failed) reduce_weight_grad(1);
         if (last && !failed) reduce_weight_grad(0);
     }
     // loss: one atomic per warp
@@ -731,7 +777,9 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(const __nv_bfloa
     if (failed) {
         if (tid == 0) {
             atomicOr(err, kTcErrTimeout);
-            mbar_wait(bar, phase ^ 1u);   // the products of the abandoned round, once more bounded
+            mbar_wait(bar, phase ^ 1u);     // the products of the abandoned round, once more bounded
+            mbar_wait(dwbar(0), dw_phase[0] ^ 1u);
+            mbar_wait(dwbar(1), dw_phase[1] ^ 1u);
         }
         tc_fence_before();
     }
