@@ -832,7 +832,7 @@ cudaError_t launch_mlp_train(int device, cudaStream_t st, const void* wb, const 
     cudaError_t e = tc_setup(device);
     if (e != cudaSuccess) return e;
     if (n == 0) return cudaSuccess;
-    // one CTA per SM (512 tensor-memory columns, 167 KB of shared memory), 128 samples at a time
+    // one CTA per SM (512 tensor-memory columns, 183 KB of shared memory), 128 samples at a time
     const uint32_t tiles = (n + kTcRows - 1) / kTcRows, sms = (uint32_t)g_tc_grid[device] / 4;
     *parts = tiles < sms ? tiles : sms;
     k_mlp_train_tc<<<*parts, kTrThreads, kTrSmem, st>>>((const __nv_bfloat16*)wb, samples, n, dW_parts, loss, err);
