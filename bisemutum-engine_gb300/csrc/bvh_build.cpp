@@ -55,8 +55,8 @@ struct Builder {
     std::vector<BNode>& nodes;
     std::atomic<uint32_t> node_count{0};
     std::atomic<int> threads_free{0};
-    uint32_t bins;
-    uint32_t max_leaf;
+    uint32_t bins = 0;       // set by the caller before build()
+    uint32_t max_leaf = 0;
 
     uint32_t alloc() { return node_count.fetch_add(1); }
 

@@ -29,8 +29,6 @@
 
 namespace bsm {
 
-constexpr int kTrainMaxVerts = 16;
-
 // A slot of `ctr` for each calling lane, one atomic per group of converged lanes.
 __device__ __forceinline__ uint32_t agg_alloc(uint32_t* ctr) {
     const uint32_t m = __activemask(), lane = threadIdx.x & 31u;
