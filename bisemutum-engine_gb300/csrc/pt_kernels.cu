@@ -46,13 +46,13 @@ __device__ __forceinline__ uint32_t warp_alloc(bool pred, uint32_t* counter) {
 // launches coherent.  The lanes of a warp that share a bin take their ranks
 // from one shared-memory atomic; warp 0 scans the bins.  Every
 // thread of the block must call it with the same `parity`, alternating 0 / 1
-// from call to call, after s_oct_cnt[0] was cleared: each call clears the
+// from call to call, after s_dir_cnt[0] was cleared: each call clears the
 // other parity's counters for the next one, so it needs two block barriers
 // instead of three.  Returns 0 for threads without pred.
 constexpr uint32_t kDirBins = 24;   // octant x dominant axis
 static_assert(kDirBins <= 32, "one warp scans the bins");
-__shared__ uint32_t s_oct_cnt[2][kDirBins + 1];
-__device__ __forceinline__ uint32_t block_alloc_by_octant(bool pred, V3 dir, uint32_t* counter, int parity) {
+__shared__ uint32_t s_dir_cnt[2][kDirBins + 1];
+__device__ __forceinline__ uint32_t block_alloc_by_direction(bool pred, V3 dir, uint32_t* counter, int parity) {
     __shared__ uint32_t s_off[2][kDirBins], s_base[2];
     const float ax = fabsf(dir.x), ay = fabsf(dir.y), az = fabsf(dir.z);
     const uint32_t dom = (ax >= ay && ax >= az) ? 0u : (ay >= az ? 1u : 2u);
@@ -62,12 +62,12 @@ __device__ __forceinline__ uint32_t block_alloc_by_octant(bool pred, V3 dir, uin
     const uint32_t peers = __match_any_sync(0xffffffffu, key);
     const uint32_t leader = (uint32_t)__ffs(peers) - 1u;
     uint32_t rank = 0;
-    if ((threadIdx.x & 31u) == leader && pred) rank = atomicAdd(&s_oct_cnt[parity][key], (uint32_t)__popc(peers));
+    if ((threadIdx.x & 31u) == leader && pred) rank = atomicAdd(&s_dir_cnt[parity][key], (uint32_t)__popc(peers));
     rank = __shfl_sync(0xffffffffu, rank, (int)leader) + (uint32_t)__popc(peers & lanemask_lt());
     __syncthreads();
     if (threadIdx.x < 32) {   // exclusive prefix over the bins by warp 0, one bin per lane
         const uint32_t lane = threadIdx.x;
-        const uint32_t c = lane < kDirBins ? s_oct_cnt[parity][lane] : 0u;
+        const uint32_t c = lane < kDirBins ? s_dir_cnt[parity][lane] : 0u;
         uint32_t x = c;
 #pragma unroll
         for (uint32_t o = 1; o < 32; o <<= 1) {
@@ -78,7 +78,7 @@ __device__ __forceinline__ uint32_t block_alloc_by_octant(bool pred, V3 dir, uin
         const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
         if (lane == 0) s_base[parity] = total ? atomicAdd(counter, total) : 0u;
     }
-    if (threadIdx.x <= kDirBins) s_oct_cnt[parity ^ 1][threadIdx.x] = 0u;
+    if (threadIdx.x <= kDirBins) s_dir_cnt[parity ^ 1][threadIdx.x] = 0u;
     __syncthreads();
     return pred ? s_base[parity] + s_off[parity][key] + rank : 0u;
 }
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
     uint4* out_p = wf.path[q ^ 1];
     float4* out_t = wf.thr[q ^ 1];
     const uint32_t stride = gridDim.x * blockDim.x;
-    if (threadIdx.x <= kDirBins) s_oct_cnt[0][threadIdx.x] = 0u;
+    if (threadIdx.x <= kDirBins) s_dir_cnt[0][threadIdx.x] = 0u;
     __syncthreads();
     int parity = 0;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride, parity ^= 1) {
@@ -459,8 +459,8 @@ __global__ void __launch_bounds__(512, 2) k_shade(DevScene sc, const DevView* __
                 cont = max_comp(nthr) > 0.0f;
             }
         }
-        // the next rays, grouped by octant per block (sorting the sky shadow rays the same way measured no gain)
-        uint32_t slot = block_alloc_by_octant(cont, L, wf.counters + kCntQueue + seg + 1, parity);
+        // the next rays, grouped by direction per block (sorting the sky shadow rays by octant measured no gain)
+        uint32_t slot = block_alloc_by_direction(cont, L, wf.counters + kCntQueue + seg + 1, parity);
         if (cont) {
             if (slot < cap) {
                 out_o[slot] = make_float4(org.x, org.y, org.z, tmin);
