@@ -58,7 +58,7 @@ __device__ __forceinline__ uint32_t block_alloc_by_direction(bool pred, V3 dir, 
     const uint32_t dom = (ax >= ay && ax >= az) ? 0u : (ay >= az ? 1u : 2u);
     uint32_t key = pred ? ((dir.x < 0.0f ? 1u : 0u) | (dir.y < 0.0f ? 2u : 0u) | (dir.z < 0.0f ? 4u : 0u)) * 3u + dom
                         : kDirBins;
-    // one shared atomic per octant present in the warp (the lanes of an octant share it)
+    // one shared atomic per bin present in the warp (the lanes of a bin share it)
     const uint32_t peers = __match_any_sync(0xffffffffu, key);
     const uint32_t leader = (uint32_t)__ffs(peers) - 1u;
     uint32_t rank = 0;
@@ -770,7 +770,7 @@ void query_launch_cfg(int device, int block_trace, LaunchCfg* lc) {
     if (per_sm_shade < 1) per_sm_shade = 1;
     lc->block_trace = block_trace;
     lc->grid_persistent = sms * per_sm;
-    lc->block_shade = 512;   // the octant grouping of the next rays spans a block
+    lc->block_shade = 512;   // the direction grouping of the next rays spans a block
     lc->grid_shade = sms * per_sm_shade * 4;
 }
 
