@@ -484,7 +484,9 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
             }
             if (base + cntn >= n) exhausted = true;
         }
-        if (__ballot_sync(0xffffffffu, has) == 0u) break;
+        const uint32_t act = __ballot_sync(0xffffffffu, has);   // lanes holding a ray in this iteration
+        if (act == 0u) break;
+        const int n_act = __popc(act);
         // node step
         if (has) {
             if (G.x & kTriGroupFlag) {
@@ -505,8 +507,7 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
             bool want = has && has_tris(T);
             uint32_t m = __ballot_sync(0xffffffffu, want);
             if (m == 0u) break;
-            uint32_t act = __ballot_sync(0xffffffffu, has);
-            if (__popc(m) * 4 < __popc(act)) {
+            if (__popc(m) * 4 < n_act) {
                 if (want && sp < postpone_sp) { stack[sp++] = make_uint2(T.x | kTriGroupFlag, T.y); T.y = 0u; }
                 if (__ballot_sync(0xffffffffu, has && has_tris(T)) == 0u) break;
                 want = has && has_tris(T);
