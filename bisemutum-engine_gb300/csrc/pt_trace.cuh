@@ -77,9 +77,10 @@ __device__ __forceinline__ RayPre make_ray(float4 o, float4 d) {
     // slab, far inside the half quantisation step of padding left for a hit at
     // t below 1e17 times the node's extent.  The triangle test uses the true
     // direction.
-    r.idx = __fdiv_rn(1.0f, box_dir(d.x));
-    r.idy = __fdiv_rn(1.0f, box_dir(d.y));
-    r.idz = __fdiv_rn(1.0f, box_dir(d.z));
+    // __frcp_rn: the correctly rounded 1 / x, the same bits as the IEEE division 1.0f / x
+    r.idx = __frcp_rn(box_dir(d.x));
+    r.idy = __frcp_rn(box_dir(d.y));
+    r.idz = __frcp_rn(box_dir(d.z));
     uint32_t oct = (r.idx < 0.0f ? 1u : 0u) | (r.idy < 0.0f ? 2u : 0u) | (r.idz < 0.0f ? 4u : 0u);
     r.oct_key = 7u ^ oct;
     float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
@@ -94,7 +95,7 @@ __device__ __forceinline__ RayPre make_ray(float4 o, float4 d) {
     r.kx = kx; r.ky = ky; r.kz = kz;
     r.Sx = __fdiv_rn(sel3(kx, d.x, d.y, d.z), dkz);
     r.Sy = __fdiv_rn(sel3(ky, d.x, d.y, d.z), dkz);
-    r.Sz = __fdiv_rn(1.0f, dkz);
+    r.Sz = __frcp_rn(dkz);
     return r;
 }
 
@@ -147,7 +148,7 @@ __device__ __forceinline__ bool tri_test(const RayPre& r, float4 a, float4 b, fl
     float adet = fabsf(det);
     if (Ts <= 0.0f && r.tmin >= 0.0f) return false;
     if (Ts > adet * tbest * BSM_BOX_PAD) return false;
-    float rcp = __fdiv_rn(1.0f, det);
+    float rcp = __frcp_rn(det);
     float t = __fmul_rn(T, rcp);
     if (!(t > r.tmin)) return false;
     if (!(t < tbest || (t == tbest && prim < best_prim))) return false;
