@@ -462,7 +462,8 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
     int sp = 0;
     while (true) {
         // refill lanes whose ray finished (one atomic per warp)
-        uint32_t idle = __ballot_sync(0xffffffffu, !has);
+        const uint32_t idle = __ballot_sync(0xffffffffu, !has);
+        uint32_t act = ~idle;   // lanes holding a ray in this iteration (taken again after a refill)
         if (!exhausted && (__popc(idle) >= refill_min || idle == 0xffffffffu)) {
             uint32_t cntn = (uint32_t)__popc(idle);
             uint32_t base = 0;
@@ -484,8 +485,8 @@ __device__ __forceinline__ void trace_queue(const CwNode* __restrict__ nodes, co
                 }
             }
             if (base + cntn >= n) exhausted = true;
+            act = __ballot_sync(0xffffffffu, has);
         }
-        const uint32_t act = __ballot_sync(0xffffffffu, has);   // lanes holding a ray in this iteration
         if (act == 0u) break;
         const int n_act = __popc(act);
         // node step
@@ -584,7 +585,8 @@ __device__ __forceinline__ void trace_queue2(const CwNode* __restrict__ tlas, co
     // instance reloads only origin and direction (blocks have at most 256 threads: __launch_bounds__)
     __shared__ float4 s_world[256][2];
     while (true) {
-        uint32_t idle = __ballot_sync(0xffffffffu, !has);
+        const uint32_t idle = __ballot_sync(0xffffffffu, !has);
+        uint32_t act = ~idle;   // lanes holding a ray in this iteration (taken again after a refill)
         if (!exhausted && (__popc(idle) >= refill_min || idle == 0xffffffffu)) {
             uint32_t cntn = (uint32_t)__popc(idle);
             uint32_t base = 0;
@@ -612,8 +614,8 @@ __device__ __forceinline__ void trace_queue2(const CwNode* __restrict__ tlas, co
                 }
             }
             if (base + cntn >= n) exhausted = true;
+            act = __ballot_sync(0xffffffffu, has);
         }
-        const uint32_t act = __ballot_sync(0xffffffffu, has);
         if (act == 0u) break;
         // node step
         if (has) {
