@@ -585,8 +585,7 @@ __device__ __forceinline__ void trace_queue2(const CwNode* __restrict__ tlas, co
     // instance reloads only origin and direction (blocks have at most 256 threads: __launch_bounds__)
     __shared__ float4 s_world[256][2];
     while (true) {
-        const uint32_t idle = __ballot_sync(0xffffffffu, !has);
-        uint32_t act = ~idle;   // lanes holding a ray in this iteration (taken again after a refill)
+        uint32_t idle = __ballot_sync(0xffffffffu, !has);
         if (!exhausted && (__popc(idle) >= refill_min || idle == 0xffffffffu)) {
             uint32_t cntn = (uint32_t)__popc(idle);
             uint32_t base = 0;
@@ -614,8 +613,8 @@ __device__ __forceinline__ void trace_queue2(const CwNode* __restrict__ tlas, co
                 }
             }
             if (base + cntn >= n) exhausted = true;
-            act = __ballot_sync(0xffffffffu, has);
         }
+        const uint32_t act = __ballot_sync(0xffffffffu, has);
         if (act == 0u) break;
         // node step
         if (has) {
