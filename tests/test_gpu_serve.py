@@ -108,6 +108,15 @@ def test_admission_waits_for_memory(bsm, served):
         ctx.server_stop()
 
 
+def test_server_rejects_unknown_flags(bsm, served):
+    ctx, _, _ = served
+    import ctypes as C
+    opts = bsm.ServerOpts(1 << 20, 0, 0, 0, 2)   # bit 1 is not a server flag
+    assert ctx._L.bsm_server_start(ctx.h, C.byref(opts)) == -1   # BSM_ERR_INVALID_ARG
+    ctx.server_start(pool_bytes=1 << 20, deterministic=True)   # the one defined flag starts
+    ctx.server_stop()
+
+
 def test_scenes_locked_while_serving(bsm, served):
     ctx, scenes, ids = served
     ctx.server_start(pool_bytes=1 << 20)
